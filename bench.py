@@ -1,0 +1,345 @@
+#!/usr/bin/env python3
+"""Benchmark of the ePIC2D time-step loop on GB300.
+
+One "step" is one iteration of the loop body of the reference (deposit of all
+species, charge density, Poisson solve, E-field, push of all species, MCC) on
+the GPU-resident workload.  Prints one JSON line.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+* value      — particle-steps/s with all state resident in HBM (CUDA events on
+               the simulation's stream around K steps).
+* e2e        — the same metric through the public API with host-owned
+               particles: every step uploads all particles from pinned host
+               memory (epic_set_particles), runs epic_step, and downloads them
+               (epic_get_particles).
+* roofline   — the dominant phase's algorithmic bytes per launch over its
+               measured average launch time, against the measured HBM copy
+               bandwidth.
+* cpu_baseline — the oracle's C restatement of the reference loop timed on
+               this host for a bounded sample of the same workload.
+* --impl reference — the reference's CPU implementation of the loop (the
+               restatement, or the reference's own objects where they were
+               compiled on this machine) on the same workload, one full loop
+               iteration per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = "beam_mcc_256"
+METRIC = "particle-steps/s on 1 GB300 (plain FP64 time-step loop)"
+UNIT = "particle-steps/s"
+
+# Algorithmic bytes per unit of each phase (FP64 plain form).
+BYTES = {
+    "push": 64,       # per particle: x, y, vx, vy read + written
+    "deposit": 16,    # per particle: x, y read (accumulation stays in L2)
+    "mcc": 24,        # per electron: vx, vy, vz read (collided ones also written)
+    "solve": 88,      # per node per PCG iteration (11 FP64 words)
+    "finalize": 24,   # per node per species: accumulator read + density write + rho share
+    "efield": 40,     # per node: phi read, efx, efy, (efx, efy) written
+}
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+            os.close(fd)
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.f.close()
+        rows = []
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.remove(self.path)
+        if not rows:
+            return None
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for _, _, r in rows for k in range(4) if r[k].lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in rows), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(rows)}
+
+
+def write_deck(name):
+    from epic2d_mcc_gb300 import workloads
+
+    d = tempfile.mkdtemp(prefix="epic_bench_")
+    path = os.path.join(d, name + ".ini")
+    with open(path, "w") as f:
+        f.write(workloads.deck(name))
+    return path
+
+
+def collisions_on(ini):
+    from oracle import oracle as O
+
+    s = O.setup(ini)
+    return s.elastic or s.excitation or s.ionization
+
+
+# ------------------------------------------------------------ CPU arm ---
+def cpu_port_run(ini, steps, warmup, budget_s=None):
+    """The oracle restatement of the reference loop (single thread, as the
+    reference).  Returns (particle-steps/s, steps timed, particles, kind)."""
+    from epic2d_mcc_gb300 import workloads
+    from oracle import oracle as O
+
+    coll = collisions_on(ini)
+    sim = O.OracleSim(ini)
+    if coll:
+        e, ela, exc, ion = workloads.synthetic_table()
+        sim.R.set_log_table(ela, exc, ion, e[0], e[-1])
+    for _ in range(warmup):
+        sim.step(collisions=coll)
+    done, n_acc = 0, 0
+    t0 = time.perf_counter()
+    while True:
+        n_acc += sum(len(p) for p in sim.parts)
+        sim.step(collisions=coll)
+        done += 1
+        el = time.perf_counter() - t0
+        if steps is not None and done >= steps:
+            break
+        if budget_s is not None and el >= budget_s:
+            break
+    el = time.perf_counter() - t0
+    return n_acc / el, done, n_acc // done, "port"
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    ini = write_deck(args.workload)
+    value, done, n, kind = cpu_port_run(ini, args.steps, args.warmup)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / value * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (particles loaded from mt19937 seed 0, as the reference's Init)",
+            "config": {"workload": args.workload, "particles": n},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
+                             "sample": "%d full loop iterations of %s (%d particles), single thread; the "
+                                       "reference loop is serial" % (done, args.workload, n)},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------ GPU arm ---
+def run_ours(args, rank, world):
+    import numpy as np
+    import torch
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    import epic2d_mcc_gb300 as E
+    from epic2d_mcc_gb300 import build as B
+    from epic2d_mcc_gb300 import workloads
+
+    B.build()
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if dist:
+            dist.barrier()
+
+    def max_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum_over_ranks(x):
+        if not dist:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        return float(t.item())
+
+    ini = write_deck(args.workload)
+    coll = collisions_on(ini)
+    sim = E.Simulation.from_ini(ini)
+    if coll:
+        e, ela, exc, ion = workloads.synthetic_table()
+        sim.set_log_cross_sections(ela, exc, ion, e[0], e[-1])
+    sim.load_particles(0)
+    sim.initial_field()
+    nsp = len(sim.species)
+    for _ in range(args.warmup):
+        sim.run(1, collisions=coll, graph=False)
+    stream = torch.cuda.ExternalStream(sim.stream)
+    n_before = sum(sim.num_particles(s) for s in range(nsp))
+    sim.set_profiling(True)
+    sim.profile()
+    launches0 = sim.launches
+    clocks = Clocks(local)
+    barrier()
+    torch.cuda.synchronize()
+    sim.sync()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    sim.run(args.steps, collisions=coll, graph=False)
+    ev1.record(stream)
+    ev1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    launches = sim.launches - launches0
+    prof, iters = sim.profile()
+    sim.set_profiling(False)
+    n_after = sum(sim.num_particles(s) for s in range(nsp))
+    ms_max = max_over_ranks(ms)
+    pst_rank = 0.5 * (n_before + n_after) * args.steps
+    value = sum_over_ranks(pst_rank) / (ms_max / 1e3)
+
+    # roofline of the dominant phase
+    g = sim.cfg
+    nodes = g.nx * g.ny
+    n_e = sim.num_particles(0)
+    dom = max(prof, key=lambda k: prof[k][0])
+    d_ms, d_launch = prof[dom]
+    if dom == "solve":
+        per_step_bytes = BYTES["solve"] * nodes * (iters / max(d_launch, 1))
+    elif dom in ("push", "deposit"):
+        per_step_bytes = BYTES[dom] * 0.5 * (n_before + n_after) / nsp
+    elif dom == "mcc":
+        per_step_bytes = BYTES["mcc"] * n_e
+    else:
+        per_step_bytes = BYTES[dom] * nodes * (nsp if dom == "finalize" else 1)
+    achieved = per_step_bytes / (d_ms / max(d_launch, 1) / 1e3) / 1e9
+    peak, peak_kind = load_peaks()
+    traffic = TRAFFIC.get(dom)
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": traffic,
+                "algorithmic_bytes_per_launch": per_step_bytes, "avg_launch_ms": d_ms / max(d_launch, 1),
+                "phases_ms_per_step": {k: v[0] / args.steps for k, v in prof.items()},
+                "solver_iterations_per_step": iters / args.steps}
+
+    # e2e through the public API with host-owned particles
+    caps = [sim.species[s].capacity or (sim.species[s].numparticle * 3 // 2 + 4096) for s in range(nsp)]
+    bufs = [torch.empty((int(c), 5), dtype=torch.float64, pin_memory=True).numpy() for c in caps]
+    counts = [sim.particles_into(s, bufs[s]) for s in range(nsp)]
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier()
+    t0 = time.perf_counter()
+    h2d = d2h = 0
+    for _ in range(e2e_steps):
+        for s in range(nsp):
+            sim.set_particles(s, bufs[s][:counts[s]])
+            h2d += counts[s] * 40
+        sim.step(collisions=coll)
+        for s in range(nsp):
+            counts[s] = sim.particles_into(s, bufs[s])
+            d2h += counts[s] * 40
+    el = time.perf_counter() - t0
+    el = max_over_ranks(el)
+    e2e_value = sum_over_ranks(sum(counts) * e2e_steps) / el
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        v, done, n, kind = cpu_port_run(ini, None, 0, budget_s=args.cpu_seconds)
+        cpu = {"value": v, "unit": UNIT, "cores": 1, "kind": kind,
+               "sample": "%d full loop iterations of %s (%d particles) on one host core after load + initial "
+                         "field (the reference loop is serial)" % (done, args.workload, n)}
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (particles loaded from mt19937 seed 0, as the reference's Init)",
+                "config": {"workload": args.workload, "particles": int(0.5 * (n_before + n_after)),
+                           "grid": [g.nx, g.ny], "solver": "PCG tol 1e-10 (cold start, as the reference)",
+                           "mcc": "direct MCC, Philox uniforms, 1000-point log table" if coll else "off",
+                           "l2": "inputs larger than L2 (particles %.0f MB)" % (n_before * 40 / 1e6),
+                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
+                        "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
+                "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk}
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+# Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of each
+# phase's kernel from the ncu captures summarised under profiles/; None where
+# no capture exists yet.
+TRAFFIC = {}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default=WORKLOAD)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_ours(args, rank, world)
+
+
+if __name__ == "__main__":
+    main()

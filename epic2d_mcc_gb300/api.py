@@ -1,0 +1,312 @@
+"""ctypes binding of the C ABI (include/epic2d.h).
+
+:class:`Simulation` mirrors the reference's per-step interface — the methods of
+Species, Domain, FieldSolve and CollisionHandler that src/main.cpp calls — over
+one GPU-resident simulation.  There is no CPU implementation behind it: if the
+CUDA library is missing the import fails.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libepic2d_gb300.so")
+
+EPIC_OK = 0
+EPIC_WARN_NOT_CONVERGED = 5
+STATUS = {0: "OK", 1: "INVALID", 2: "CUDA", 3: "NOMEM", 4: "CAPACITY", 5: "NOT_CONVERGED", 6: "DOMAIN",
+          7: "TIMEOUT", 8: "BUDGET", 9: "IO"}
+CIC, NGP = 0, 1
+PBC, OPEN, REFLECTIVE = 0, 1, 2
+SOLVER_GS, SOLVER_PCG = 0, 1
+SOR_LEXICOGRAPHIC, SOR_REDBLACK = 0, 1
+DEPOSIT_FIXED, DEPOSIT_FP64 = 0, 1
+MCC_PHILOX, MCC_INJECTED, MCC_NULL = 0, 1, 2
+GRID = {"phi": 0, "rho": 1, "efx": 2, "efy": 3}
+
+
+class EpicError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("%s: %s" % (STATUS.get(status, status), msg))
+        self.status = status
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("nx", ctypes.c_int), ("ny", ctypes.c_int),
+                ("x0", ctypes.c_double), ("y0", ctypes.c_double), ("dx", ctypes.c_double), ("dy", ctypes.c_double),
+                ("DT", ctypes.c_double), ("L", ctypes.c_double), ("W", ctypes.c_double),
+                ("vel_norm", ctypes.c_double), ("LDe", ctypes.c_double), ("wpe", ctypes.c_double),
+                ("LDi", ctypes.c_double), ("wpi", ctypes.c_double), ("density", ctypes.c_double),
+                ("shape", ctypes.c_int), ("bc", ctypes.c_int), ("solver", ctypes.c_int),
+                ("tolerance", ctypes.c_double), ("max_iteration", ctypes.c_int), ("ionfixed", ctypes.c_int),
+                ("normscheme", ctypes.c_int), ("gas_density", ctypes.c_double),
+                ("elastic", ctypes.c_int), ("excitation", ctypes.c_int), ("ionization", ctypes.c_int),
+                ("sor_omega", ctypes.c_double), ("sor_mode", ctypes.c_int), ("deposit_mode", ctypes.c_int),
+                ("mcc_mode", ctypes.c_int), ("seed", ctypes.c_uint64), ("warm_start", ctypes.c_int),
+                ("reserved", ctypes.c_int * 16)]
+
+
+class SpeciesDesc(ctypes.Structure):
+    _fields_ = [("name", ctypes.c_char * 32), ("mass", ctypes.c_double), ("charge", ctypes.c_double),
+                ("spwt", ctypes.c_double), ("temp", ctypes.c_double), ("numparticle", ctypes.c_int),
+                ("vsx", ctypes.c_double), ("vsy", ctypes.c_double), ("fract_den", ctypes.c_double),
+                ("load", ctypes.c_char * 32), ("capacity", ctypes.c_int64)]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Load the CUDA library (built by epic2d_mcc_gb300.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError("libepic2d_gb300.so is not built; run `python -c 'import __graft_entry__ as g; g.build()'`")
+    L = ctypes.CDLL(LIB_PATH)
+    vp, i, i64, d, st = ctypes.c_void_p, ctypes.c_int, ctypes.c_int64, ctypes.c_double, ctypes.c_int
+    pd = ctypes.POINTER(ctypes.c_double)
+    sigs = {
+        "epic_last_error": ([], ctypes.c_char_p),
+        "epic_config_defaults": ([vp], None),
+        "epic_config_from_ini": ([ctypes.c_char_p, vp, vp, i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)], st),
+        "epic_create": ([vp, ctypes.POINTER(vp)], st),
+        "epic_destroy": ([vp], None),
+        "epic_add_species": ([vp, vp, ctypes.POINTER(ctypes.c_int)], st),
+        "epic_load_particles": ([vp, ctypes.c_uint32], st),
+        "epic_set_particles": ([vp, i, vp, i64], st),
+        "epic_get_particles": ([vp, i, vp, i64, ctypes.POINTER(ctypes.c_int64)], st),
+        "epic_num_particles": ([vp, i, ctypes.POINTER(ctypes.c_int64)], st),
+        "epic_scatter_species": ([vp, i], st),
+        "epic_compute_rho": ([vp], st),
+        "epic_potential_solver": ([vp, ctypes.POINTER(ctypes.c_int), pd], st),
+        "epic_calculate_efield": ([vp], st),
+        "epic_push_species": ([vp, i, i], st),
+        "epic_rewind_species": ([vp, i], st),
+        "epic_set_cross_sections": ([vp, vp, vp, vp, vp, i64, d], st),
+        "epic_set_reference_cross_sections": ([vp], st),
+        "epic_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
+        "epic_handle_collisions": ([vp, i, i, vp, i, ctypes.POINTER(ctypes.c_int64)], st),
+        "epic_step": ([vp, i], st),
+        "epic_initial_field": ([vp], st),
+        "epic_run": ([vp, i, i, i], st),
+        "epic_compute_ke": ([vp, i, i, vp], st),
+        "epic_compute_momentum": ([vp, i, i, vp], st),
+        "epic_compute_pe": ([vp, i, pd], st),
+        "epic_delta_phi": ([vp, pd], st),
+        "epic_get_grid": ([vp, i, vp], st),
+        "epic_set_grid": ([vp, i, vp], st),
+        "epic_sync": ([vp], st),
+        "epic_kernel_launches": ([vp], i64),
+        "epic_stream": ([vp], vp),
+        "epic_set_profiling": ([vp, i], st),
+        "epic_get_profile": ([vp, vp, vp, ctypes.POINTER(ctypes.c_int64)], st),
+    }
+    for name, (args, res) in sigs.items():
+        fn = getattr(L, name)
+        fn.argtypes = args
+        fn.restype = res
+    _lib = L
+    return L
+
+
+def _check(status: int, allow=(EPIC_OK,)):
+    if status not in allow:
+        raise EpicError(status, lib().epic_last_error().decode())
+    return status
+
+
+def _ptr(a: np.ndarray):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def default_config() -> Config:
+    c = Config()
+    lib().epic_config_defaults(ctypes.byref(c))
+    return c
+
+
+def config_from_ini(path: str):
+    """INIParser::parse + src/main.cpp set-up: returns (Config, [SpeciesDesc], NUM_TS)."""
+    cfg = Config()
+    descs = (SpeciesDesc * 8)()
+    n = ctypes.c_int()
+    ts = ctypes.c_int()
+    _check(lib().epic_config_from_ini(path.encode(), ctypes.byref(cfg), descs, 8, ctypes.byref(n), ctypes.byref(ts)))
+    return cfg, [descs[k] for k in range(min(n.value, 8))], ts.value
+
+
+class Simulation:
+    """One simulation resident on the GPU (Domain + species + FieldSolve + CollisionHandler)."""
+
+    def __init__(self, cfg: Config, species):
+        self._h = ctypes.c_void_p()
+        _check(lib().epic_create(ctypes.byref(cfg), ctypes.byref(self._h)))
+        self.cfg = cfg
+        self.species = []
+        for d in species:
+            idx = ctypes.c_int()
+            _check(lib().epic_add_species(self._h, ctypes.byref(d), ctypes.byref(idx)))
+            self.species.append(d)
+        self.nx, self.ny = cfg.nx, cfg.ny
+
+    @classmethod
+    def from_ini(cls, path: str, **overrides):
+        cfg, descs, _ = config_from_ini(path)
+        for k, v in overrides.items():
+            if k == "capacity":
+                for d in descs:
+                    d.capacity = int(v)
+            else:
+                setattr(cfg, k, v)
+        return cls(cfg, descs)
+
+    def close(self):
+        if self._h:
+            lib().epic_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- particles ---
+    def load_particles(self, seed: int = 0):
+        _check(lib().epic_load_particles(self._h, seed))
+
+    def set_particles(self, sp: int, parts: np.ndarray):
+        parts = np.ascontiguousarray(parts, dtype=np.float64).reshape(-1, 5)
+        _check(lib().epic_set_particles(self._h, sp, _ptr(parts), len(parts)))
+
+    def num_particles(self, sp: int) -> int:
+        n = ctypes.c_int64()
+        _check(lib().epic_num_particles(self._h, sp, ctypes.byref(n)))
+        return n.value
+
+    def particles_into(self, sp: int, out: np.ndarray) -> int:
+        """Download species `sp` into a caller-owned (capacity, 5) float64 array; returns the count."""
+        got = ctypes.c_int64()
+        _check(lib().epic_get_particles(self._h, sp, _ptr(out), len(out), ctypes.byref(got)))
+        return got.value
+
+    def particles(self, sp: int) -> np.ndarray:
+        n = self.num_particles(sp)
+        out = np.zeros((max(n, 1), 5))
+        got = ctypes.c_int64()
+        _check(lib().epic_get_particles(self._h, sp, _ptr(out), len(out), ctypes.byref(got)))
+        return out[:got.value]
+
+    # --- the loop, phase by phase ---
+    def scatter_species(self, sp: int):
+        _check(lib().epic_scatter_species(self._h, sp))
+
+    def compute_rho(self):
+        _check(lib().epic_compute_rho(self._h))
+
+    def potential_solver(self):
+        it = ctypes.c_int()
+        err = ctypes.c_double()
+        st = _check(lib().epic_potential_solver(self._h, ctypes.byref(it), ctypes.byref(err)),
+                    allow=(EPIC_OK, EPIC_WARN_NOT_CONVERGED))
+        return it.value, err.value, st == EPIC_OK
+
+    def calculate_efield(self):
+        _check(lib().epic_calculate_efield(self._h))
+
+    def push_species(self, sp: int, sub_cycle: int = 1):
+        _check(lib().epic_push_species(self._h, sp, sub_cycle))
+
+    def rewind_species(self, sp: int):
+        _check(lib().epic_rewind_species(self._h, sp))
+
+    def set_reference_cross_sections(self):
+        _check(lib().epic_set_reference_cross_sections(self._h))
+
+    def set_cross_sections(self, tot, ela, exc, ion, de):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (tot, ela, exc, ion)]
+        _check(lib().epic_set_cross_sections(self._h, *[_ptr(a) for a in arrs], len(arrs[0]), de))
+
+    def set_log_cross_sections(self, ela, exc, ion, e_min, e_max):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (ela, exc, ion)]
+        _check(lib().epic_set_log_cross_sections(self._h, *[_ptr(a) for a in arrs], len(arrs[0]), e_min, e_max))
+
+    def handle_collisions(self, electrons: int = 0, ions: int = 1, uniforms: np.ndarray | None = None,
+                          ustride: int = 16) -> int:
+        nc = ctypes.c_int64()
+        u = None if uniforms is None else np.ascontiguousarray(uniforms, dtype=np.float64)
+        _check(lib().epic_handle_collisions(self._h, electrons, ions, None if u is None else _ptr(u), ustride,
+                                            ctypes.byref(nc)))
+        return nc.value
+
+    def step(self, collisions: bool = False):
+        _check(lib().epic_step(self._h, int(collisions)))
+
+    def initial_field(self):
+        _check(lib().epic_initial_field(self._h))
+
+    def run(self, steps: int, collisions: bool = False, graph: bool = True):
+        _check(lib().epic_run(self._h, steps, int(collisions), int(graph)))
+
+    # --- diagnostics ---
+    def compute_ke(self, sp: int, norm: int = 0) -> np.ndarray:
+        out = np.zeros(3)
+        _check(lib().epic_compute_ke(self._h, sp, norm, _ptr(out)))
+        return out
+
+    def compute_momentum(self, sp: int, norm: int = 0) -> np.ndarray:
+        out = np.zeros(3)
+        _check(lib().epic_compute_momentum(self._h, sp, norm, _ptr(out)))
+        return out
+
+    def compute_pe(self, norm: int = 0) -> float:
+        v = ctypes.c_double()
+        _check(lib().epic_compute_pe(self._h, norm, ctypes.byref(v)))
+        return v.value
+
+    def delta_phi(self) -> float:
+        v = ctypes.c_double()
+        _check(lib().epic_delta_phi(self._h, ctypes.byref(v)))
+        return v.value
+
+    def grid(self, which) -> np.ndarray:
+        code = GRID.get(which, which)
+        out = np.zeros(self.nx * self.ny)
+        _check(lib().epic_get_grid(self._h, code, _ptr(out)))
+        return out
+
+    def den(self, sp: int) -> np.ndarray:
+        return self.grid(10 + sp)
+
+    def set_grid(self, which, arr):
+        code = GRID.get(which, which)
+        a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        _check(lib().epic_set_grid(self._h, code, _ptr(a)))
+
+    def sync(self):
+        _check(lib().epic_sync(self._h))
+
+    @property
+    def launches(self) -> int:
+        return lib().epic_kernel_launches(self._h)
+
+    @property
+    def stream(self) -> int:
+        return lib().epic_stream(self._h) or 0
+
+    PHASES = ("deposit", "finalize", "solve", "efield", "push", "mcc")
+
+    def set_profiling(self, on: bool = True):
+        _check(lib().epic_set_profiling(self._h, int(on)))
+
+    def profile(self):
+        """{phase: (ms, launches)} accumulated since the last call, plus solver iterations."""
+        ms = np.zeros(6)
+        cnt = np.zeros(6, dtype=np.int64)
+        it = ctypes.c_int64()
+        _check(lib().epic_get_profile(self._h, _ptr(ms), _ptr(cnt), ctypes.byref(it)))
+        return {p: (float(ms[k]), int(cnt[k])) for k, p in enumerate(self.PHASES)}, it.value

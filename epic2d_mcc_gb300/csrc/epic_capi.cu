@@ -1,0 +1,860 @@
+// C ABI of include/epic2d.h: handle lifetime, device memory, and the
+// orchestration of the time-step loop on the handle's CUDA stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "epic_host.h"
+#include "epic_internal.cuh"
+
+using namespace epic;
+
+namespace {
+
+thread_local std::string g_err;
+
+epic_status fail(epic_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_err = buf;
+  return st;
+}
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) return fail(e_ == cudaErrorMemoryAllocation ? EPIC_ERR_NOMEM : EPIC_ERR_CUDA, \
+                                       "%s: %s", #call, cudaGetErrorString(e_));                 \
+  } while (0)
+
+#define CKL()                                                                                     \
+  do {                                                                                            \
+    cudaError_t e_ = cudaGetLastError();                                                          \
+    if (e_ != cudaSuccess) return fail(EPIC_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+epic_status dalloc(T** p, size_t count) {
+  *p = nullptr;
+  if (count == 0) count = 1;
+  CK(cudaMalloc((void**)p, count * sizeof(T)));
+  CK(cudaMemset(*p, 0, count * sizeof(T)));
+  return EPIC_OK;
+}
+
+long long nnodes(const epic_sim* s) { return (long long)s->cfg.nx * s->cfg.ny; }
+
+// Reads and clears the device error flags (the stream must be idle).
+epic_status take_flags(epic_sim* s) {
+  int f = 0;
+  CK(cudaMemcpy(&f, s->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+  if (!f) return EPIC_OK;
+  CK(cudaMemset(s->d_flags, 0, sizeof(int)));
+  if (f & FLAG_TIMEOUT) return fail(EPIC_ERR_TIMEOUT, "a device-side wait gave up (flags 0x%x)", f);
+  if (f & FLAG_CAPACITY) return fail(EPIC_ERR_CAPACITY, "a species outgrew its particle capacity (flags 0x%x)", f);
+  if (f & FLAG_OUT_OF_GRID)
+    return fail(EPIC_ERR_DOMAIN, "a particle left the grid (the reference raises std::out_of_range here)");
+  return fail(EPIC_ERR_CUDA, "device flags 0x%x", f);
+}
+
+epic_status sync(epic_sim* s) {
+  CK(cudaStreamSynchronize(s->stream));
+  return take_flags(s);
+}
+
+bool valid_species(epic_sim* s, int i) { return s && i >= 0 && i < (int)s->sp.size(); }
+
+epic_status ensure_tile_status(epic_sim* s, long long cap) {
+  long long need = cap / SCAN_TILE + 2;
+  if (need <= s->tile_status_len) return EPIC_OK;
+  if (s->tile_status) cudaFree(s->tile_status);
+  s->tile_status = nullptr;
+  epic_status st = dalloc(&s->tile_status, (size_t)need);
+  if (st) return st;
+  s->tile_status_len = need;
+  return EPIC_OK;
+}
+
+epic_status ensure_staging(epic_sim* s, size_t bytes) {
+  if (bytes <= s->staging_bytes) return EPIC_OK;
+  if (s->staging) cudaFree(s->staging);
+  s->staging = nullptr;
+  s->staging_bytes = 0;
+  CK(cudaMalloc(&s->staging, bytes));
+  s->staging_bytes = bytes;
+  return EPIC_OK;
+}
+
+__global__ void k_aos_to_soa(const double* __restrict__ aos, SoA p, long long n) {
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const double* r = aos + 5 * q;
+    p.x[q] = r[0]; p.y[q] = r[1]; p.vx[q] = r[2]; p.vy[q] = r[3]; p.vz[q] = r[4];
+  }
+}
+
+__global__ void k_soa_to_aos(double* __restrict__ aos, SoA p, const long long* d_n) {
+  const long long n = *d_n;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    double* r = aos + 5 * q;
+    r[0] = p.x[q]; r[1] = p.y[q]; r[2] = p.vx[q]; r[3] = p.vy[q]; r[4] = p.vz[q];
+  }
+}
+
+// Per-phase CUDA events on the handle's stream (epic_set_profiling).
+struct PhaseTimer {
+  epic_sim* s;
+  int phase;
+  cudaEvent_t a = nullptr, b = nullptr;
+  static cudaEvent_t take(epic_sim* s) {
+    if (!s->event_pool.empty()) {
+      cudaEvent_t e = s->event_pool.back();
+      s->event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
+  PhaseTimer(epic_sim* s_, int p) : s(s_), phase(p) {
+    if (!s->profiling) return;
+    cudaStreamCaptureStatus cs;
+    if (cudaStreamIsCapturing(s->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    a = take(s);
+    b = take(s);
+    cudaEventRecord(a, s->stream);
+  }
+  ~PhaseTimer() {
+    if (!a) return;
+    cudaEventRecord(b, s->stream);
+    s->prof_pending.push_back({phase, {a, b}});
+  }
+};
+
+// ---- phase launchers (no synchronisation; usable inside stream capture) ----
+epic_status do_deposit(epic_sim* s, int i) {
+  PhaseTimer t(s, 0);
+  epic_species_state& sp = s->sp[i];
+  CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
+  launch_deposit(s->stream, s->g, s->cfg.shape, s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED, sp.soa, sp.d_n,
+                 sp.desc.spwt, sp.den, sp.acc, sp.fx_scale, s->d_flags, s->part_grid);
+  s->launches += 1;
+  CKL();
+  return EPIC_OK;
+}
+
+FinalizeArgs finalize_args(epic_sim* s, int stage, int only) {
+  FinalizeArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = s->g;
+  a.bc = s->cfg.bc;
+  a.fixed = s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED;
+  a.stage = stage;
+  double cell_area = s->cfg.dx * s->cfg.dy;
+  double L2 = s->cfg.L * s->cfg.L;
+  a.div = cell_area * L2 * s->cfg.density;
+  a.nsp = (int)s->sp.size();
+  for (int k = 0; k < a.nsp; k++) {
+    epic_species_state& sp = s->sp[k];
+    a.acc[k] = sp.acc;
+    a.den[k] = sp.den;
+    a.spwt[k] = sp.desc.spwt;
+    a.inv_scale[k] = sp.fx_inv_scale;
+    a.charge_over_qe[k] = sp.desc.charge * (1 / QE);
+    a.active[k] = only < 0 || only == k;
+  }
+  a.rho = s->rho;
+  return a;
+}
+
+epic_status do_finalize(epic_sim* s, int stage, int only) {
+  PhaseTimer t(s, 1);
+  launch_finalize(s->stream, finalize_args(s, stage, only));
+  s->launches += 1;
+  CKL();
+  return EPIC_OK;
+}
+
+SolverArgs solver_args(epic_sim* s) {
+  SolverArgs a;
+  std::memset(&a, 0, sizeof(a));
+  a.g = s->g;
+  a.tol = s->cfg.tolerance;
+  a.max_iter = s->cfg.max_iteration;
+  a.omega = s->cfg.sor_omega;
+  a.K = (s->cfg.L * s->cfg.L) / (s->cfg.LDe * s->cfg.LDe);
+  a.rho = s->rho;
+  a.phi = s->phi;
+  a.info = s->d_info;
+  a.iter_total = s->d_iter_total;
+  a.flags = s->d_flags;
+  a.b = s->b;
+  a.r = s->r;
+  a.va = s->va;
+  a.vb = s->vb;
+  a.u = s->u;
+  a.partials = s->partials;
+  a.bar = s->bar;
+  a.warm = s->cfg.warm_start;
+  return a;
+}
+
+int solver_blocks(epic_sim* s, long long nodes_per_block) {
+  long long want = (nnodes(s) + nodes_per_block - 1) / nodes_per_block;
+  int mx = solver_max_blocks();
+  return (int)std::max(1LL, std::min<long long>(want, mx));
+}
+
+epic_status do_solve(epic_sim* s) {
+  PhaseTimer t(s, 2);
+  SolverArgs a = solver_args(s);
+  if (s->cfg.solver == EPIC_SOLVER_GS) {
+    if (s->cfg.sor_mode == EPIC_SOR_LEXICOGRAPHIC) launch_sor_lex(s->stream, a);
+    else launch_sor_redblack(s->stream, a, solver_blocks(s, 1024));
+  } else {
+    launch_pcg(s->stream, a, solver_blocks(s, 512));
+  }
+  s->launches += 1;
+  CKL();
+  return EPIC_OK;
+}
+
+epic_status do_efield(epic_sim* s) {
+  PhaseTimer t(s, 3);
+  launch_efield(s->stream, s->g, s->cfg.bc, s->phi, s->efx, s->efy, s->ef);
+  s->launches += 1;
+  CKL();
+  return EPIC_OK;
+}
+
+epic_status do_push(epic_sim* s, int i, int sub_cycle) {
+  PhaseTimer t(s, 4);
+  epic_species_state& sp = s->sp[i];
+  const epic_config& c = s->cfg;
+  double qm = sp.desc.charge / sp.desc.mass;
+  double K = (c.density * QE * c.L) / (EPS_0 * c.W * c.vel_norm);
+  double qmK = qm * K;
+  double cc = (c.vel_norm) / (c.L * c.W);
+  double dtsub = c.DT * sub_cycle;
+  if (c.bc == EPIC_OPEN) {
+    CK(cudaMemsetAsync(s->tile_ctr, 0, sizeof(unsigned int), s->stream));
+    CK(cudaMemsetAsync(s->tile_status, 0, s->tile_status_len * sizeof(unsigned long long), s->stream));
+  }
+  launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, qmK, cc, dtsub, s->d_flags, s->tile_status,
+              s->tile_ctr, s->part_grid);
+  s->launches += 1;
+  CKL();
+  return EPIC_OK;
+}
+
+epic_status do_mcc(epic_sim* s, int e, int ion, const double* d_uniforms, int ustride) {
+  PhaseTimer t(s, 5);
+  if (!s->cs.tot) return fail(EPIC_ERR_INVALID, "cross sections not set (epic_set_reference_cross_sections)");
+  epic_species_state& E = s->sp[e];
+  epic_species_state& I = s->sp[ion];
+  const epic_config& c = s->cfg;
+  CK(cudaMemsetAsync(s->tile_ctr, 0, sizeof(unsigned int), s->stream));
+  CK(cudaMemsetAsync(s->tile_status, 0, s->tile_status_len * sizeof(unsigned long long), s->stream));
+  int mode = c.mcc_mode;
+  if (mode == EPIC_MCC_INJECTED && !d_uniforms) mode = EPIC_MCC_PHILOX;
+  launch_mcc(s->stream, mode, s->cs, E.soa, E.d_n, E.cap, I.soa, I.d_n, I.cap, c.vel_norm, c.DT / c.W, I.desc.mass,
+             I.desc.temp, d_uniforms, ustride, c.seed, s->d_step, s->tile_status, s->tile_ctr, s->d_ncoll,
+             s->d_flags, s->part_grid);
+  s->launches += 2;
+  CKL();
+  return EPIC_OK;
+}
+
+// The loop body of src/main.cpp:405-423 as a launch sequence.
+epic_status do_step(epic_sim* s, int with_collisions) {
+  epic_status st;
+  const int nsp = (int)s->sp.size();
+  for (int i = 0; i < nsp; i++)
+    if ((st = do_deposit(s, i))) return st;
+  if ((st = do_finalize(s, FINALIZE_AND_RHO, -1))) return st;
+  if ((st = do_solve(s))) return st;
+  if ((st = do_efield(s))) return st;
+  for (int i = 0; i < nsp; i++) {
+    if (s->cfg.ionfixed == 1 && s->sp[i].name == "ion") continue;
+    if ((st = do_push(s, i, 1))) return st;
+  }
+  if (with_collisions && nsp >= 2)
+    if ((st = do_mcc(s, 0, 1, nullptr, 0))) return st;
+  return EPIC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* epic_last_error(void) { return g_err.c_str(); }
+
+void epic_config_defaults(epic_config* c) {
+  std::memset(c, 0, sizeof(*c));
+  c->dx = c->dy = 1.0;
+  c->shape = EPIC_CIC;
+  c->bc = EPIC_PBC;
+  c->solver = EPIC_SOLVER_GS;
+  c->tolerance = 1e-3;
+  c->max_iteration = 4000;
+  c->sor_omega = 1.4;
+  c->sor_mode = EPIC_SOR_LEXICOGRAPHIC;
+  c->deposit_mode = EPIC_DEPOSIT_FIXED;
+  c->mcc_mode = EPIC_MCC_PHILOX;
+  c->seed = 0;
+  c->warm_start = 0;
+}
+
+epic_status epic_config_from_ini(const char* path, epic_config* cfg, epic_species_desc* species, int max_species,
+                                 int* num_species, int* num_ts) {
+  if (!path || !cfg || !num_species) return fail(EPIC_ERR_INVALID, "null argument");
+  std::string err;
+  int st = config_from_ini(path, cfg, species, max_species, num_species, num_ts, err);
+  if (st) return fail((epic_status)st, "%s", err.c_str());
+  return EPIC_OK;
+}
+
+epic_status epic_create(const epic_config* cfg, epic_sim** out) {
+  if (!cfg || !out) return fail(EPIC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  if (cfg->nx < 3 || cfg->ny < 3) return fail(EPIC_ERR_INVALID, "grid needs at least 3x3 nodes");
+  if (!(cfg->dx > 0) || !(cfg->dy > 0) || !(cfg->L > 0) || !(cfg->W > 0) || !(cfg->vel_norm > 0) ||
+      !(cfg->density > 0) || !(cfg->LDe > 0))
+    return fail(EPIC_ERR_INVALID, "dx, dy, L, W, vel_norm, LDe and density must be positive");
+  if (cfg->shape != EPIC_CIC && cfg->shape != EPIC_NGP) return fail(EPIC_ERR_INVALID, "bad shape");
+  if (cfg->bc < EPIC_PBC || cfg->bc > EPIC_REFLECTIVE) return fail(EPIC_ERR_INVALID, "bad bc");
+  if (cfg->solver != EPIC_SOLVER_GS && cfg->solver != EPIC_SOLVER_PCG) return fail(EPIC_ERR_INVALID, "bad solver");
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  init_field_kernels();
+  epic_sim* s = new epic_sim();
+  s->cfg = *cfg;
+  s->g.nx = cfg->nx;
+  s->g.ny = cfg->ny;
+  s->g.x0 = cfg->x0;
+  s->g.y0 = cfg->y0;
+  s->g.dx = cfg->dx;
+  s->g.dy = cfg->dy;
+  s->g.Lx = (cfg->nx - 1) * cfg->dx;
+  s->g.Ly = (cfg->ny - 1) * cfg->dy;
+  cudaDeviceGetAttribute(&s->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  s->part_grid = s->num_sms * 8;
+  epic_status st = EPIC_OK;
+  const size_t nn = (size_t)nnodes(s);
+  auto guard = [&](epic_status x) {
+    if (x && !st) st = x;
+  };
+  guard(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess ? EPIC_OK : EPIC_ERR_CUDA);
+  guard(dalloc(&s->phi, nn));
+  guard(dalloc(&s->rho, nn));
+  guard(dalloc(&s->efx, nn));
+  guard(dalloc(&s->efy, nn));
+  guard(dalloc(&s->ef, nn));
+  guard(dalloc(&s->b, nn));
+  guard(dalloc(&s->r, nn));
+  guard(dalloc(&s->va, nn));
+  guard(dalloc(&s->vb, nn));
+  guard(dalloc(&s->u, nn));
+  guard(dalloc(&s->partials, 4 * (size_t)std::max(solver_max_blocks(), 256)));
+  guard(dalloc(&s->bar, 2));
+  guard(dalloc(&s->d_info, 1));
+  guard(dalloc(&s->d_iter_total, 1));
+  guard(dalloc(&s->tile_ctr, 1));
+  guard(dalloc(&s->d_ncoll, 4));
+  guard(dalloc(&s->d_step, 1));
+  guard(dalloc(&s->sum_partials, 3 * (size_t)s->part_grid));
+  guard(dalloc(&s->d_sums, 4));
+  guard(dalloc(&s->d_flags, 1));
+  if (st) {
+    std::string e = g_err;
+    epic_destroy(s);
+    return fail(st, "epic_create: %s", e.c_str());
+  }
+  *out = s;
+  return EPIC_OK;
+}
+
+void epic_destroy(epic_sim* s) {
+  if (!s) return;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  for (auto& sp : s->sp) {
+    cudaFree(sp.soa.x); cudaFree(sp.soa.y); cudaFree(sp.soa.vx); cudaFree(sp.soa.vy); cudaFree(sp.soa.vz);
+    cudaFree(sp.d_n); cudaFree(sp.den); cudaFree(sp.acc);
+  }
+  for (auto& pe : s->prof_pending) {
+    cudaEventDestroy(pe.second.first);
+    cudaEventDestroy(pe.second.second);
+  }
+  for (auto e : s->event_pool) cudaEventDestroy(e);
+  void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->b, s->r, s->va, s->vb, s->u, s->partials, s->bar,
+                  s->d_info, s->d_iter_total, s->tile_ctr, s->d_ncoll, s->d_step, s->sum_partials, s->d_sums, s->d_flags,
+                  s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  if (s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+}
+
+epic_status epic_add_species(epic_sim* s, const epic_species_desc* d, int* index) {
+  if (!s || !d) return fail(EPIC_ERR_INVALID, "null argument");
+  if (s->sp.size() >= 8) return fail(EPIC_ERR_INVALID, "at most 8 species");
+  if (d->numparticle < 0 || !(d->mass > 0)) return fail(EPIC_ERR_INVALID, "bad species %s", d->name);
+  epic_species_state sp;
+  std::memset(&sp.soa, 0, sizeof(sp.soa));
+  sp.desc = *d;
+  sp.desc.name[sizeof(sp.desc.name) - 1] = 0;
+  sp.name = sp.desc.name;
+  sp.cap = d->capacity > 0 ? d->capacity : (long long)d->numparticle + d->numparticle / 2 + 4096;
+  // Fixed-point scale 2^k with k chosen so that cap * 2^k * (1 + 2^-20) < 2^63:
+  // no node sum can overflow even if every particle lands on it.
+  int bits = 0;
+  while ((1LL << bits) < sp.cap + 1) bits++;
+  int k = 62 - bits;
+  if (k < 16) return fail(EPIC_ERR_INVALID, "capacity too large for the fixed-point deposit");
+  sp.fx_scale = std::ldexp(1.0, k);
+  sp.fx_inv_scale = std::ldexp(1.0, -k);
+  epic_status st = EPIC_OK;
+  auto guard = [&](epic_status x) {
+    if (x && !st) st = x;
+  };
+  const size_t cap = (size_t)sp.cap, nn = (size_t)nnodes(s);
+  guard(dalloc(&sp.soa.x, cap));
+  guard(dalloc(&sp.soa.y, cap));
+  guard(dalloc(&sp.soa.vx, cap));
+  guard(dalloc(&sp.soa.vy, cap));
+  guard(dalloc(&sp.soa.vz, cap));
+  guard(dalloc(&sp.d_n, 1));
+  guard(dalloc(&sp.den, nn));
+  guard(dalloc(&sp.acc, nn));
+  guard(ensure_tile_status(s, sp.cap));
+  if (st) {
+    cudaFree(sp.soa.x); cudaFree(sp.soa.y); cudaFree(sp.soa.vx); cudaFree(sp.soa.vy); cudaFree(sp.soa.vz);
+    cudaFree(sp.d_n); cudaFree(sp.den); cudaFree(sp.acc);
+    return st;
+  }
+  s->sp.push_back(sp);
+  if (index) *index = (int)s->sp.size() - 1;
+  return EPIC_OK;
+}
+
+epic_status epic_set_particles(epic_sim* s, int i, const double* parts, int64_t n) {
+  if (!valid_species(s, i) || n < 0 || (n > 0 && !parts)) return fail(EPIC_ERR_INVALID, "bad argument");
+  epic_species_state& sp = s->sp[i];
+  if (n > sp.cap) return fail(EPIC_ERR_CAPACITY, "%lld particles exceed the capacity %lld of %s", (long long)n,
+                              sp.cap, sp.name.c_str());
+  epic_status st = ensure_staging(s, std::max<size_t>(1, (size_t)n * 5 * sizeof(double)));
+  if (st) return st;
+  if (n) {
+    CK(cudaMemcpyAsync(s->staging, parts, (size_t)n * 5 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    k_aos_to_soa<<<s->part_grid, 256, 0, s->stream>>>((const double*)s->staging, sp.soa, n);
+    s->launches += 1;
+    CKL();
+  }
+  long long nn = n;
+  CK(cudaMemcpyAsync(sp.d_n, &nn, sizeof(long long), cudaMemcpyHostToDevice, s->stream));
+  return sync(s);
+}
+
+epic_status epic_num_particles(epic_sim* s, int i, int64_t* n) {
+  if (!valid_species(s, i) || !n) return fail(EPIC_ERR_INVALID, "bad argument");
+  long long v = 0;
+  CK(cudaMemcpyAsync(&v, s->sp[i].d_n, sizeof(long long), cudaMemcpyDeviceToHost, s->stream));
+  epic_status st = sync(s);
+  *n = v;
+  return st;
+}
+
+epic_status epic_get_particles(epic_sim* s, int i, double* parts, int64_t capacity, int64_t* n) {
+  if (!valid_species(s, i) || !n) return fail(EPIC_ERR_INVALID, "bad argument");
+  int64_t cnt = 0;
+  epic_status st = epic_num_particles(s, i, &cnt);
+  if (st) return st;
+  *n = cnt;
+  if (cnt > capacity) return fail(EPIC_ERR_CAPACITY, "output buffer holds %lld of %lld particles",
+                                  (long long)capacity, (long long)cnt);
+  if (!cnt) return EPIC_OK;
+  if ((st = ensure_staging(s, (size_t)cnt * 5 * sizeof(double)))) return st;
+  k_soa_to_aos<<<s->part_grid, 256, 0, s->stream>>>((double*)s->staging, s->sp[i].soa, s->sp[i].d_n);
+  s->launches += 1;
+  CKL();
+  CK(cudaMemcpyAsync(parts, s->staging, (size_t)cnt * 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  return sync(s);
+}
+
+epic_status epic_load_particles(epic_sim* s, uint32_t seed) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  std::vector<const epic_species_desc*> d;
+  for (auto& sp : s->sp) d.push_back(&sp.desc);
+  std::vector<std::vector<double>> parts;
+  std::string err;
+  int st = load_particles(s->cfg, d, parts, seed, err);
+  if (st) return fail((epic_status)st, "%s", err.c_str());
+  for (size_t i = 0; i < parts.size(); i++) {
+    epic_status e = epic_set_particles(s, (int)i, parts[i].data(), (int64_t)(parts[i].size() / 5));
+    if (e) return e;
+  }
+  return EPIC_OK;
+}
+
+epic_status epic_scatter_species(epic_sim* s, int i) {
+  if (!valid_species(s, i)) return fail(EPIC_ERR_INVALID, "bad species index");
+  epic_status st = do_deposit(s, i);
+  if (st) return st;
+  if ((st = do_finalize(s, FINALIZE_ONLY, i))) return st;
+  return sync(s);
+}
+
+epic_status epic_compute_rho(epic_sim* s) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  epic_status st = do_finalize(s, RHO_FROM_DEN, -1);
+  if (st) return st;
+  return sync(s);
+}
+
+epic_status epic_potential_solver(epic_sim* s, int* iterations, double* error) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  epic_status st = do_solve(s);
+  if (st) return st;
+  if ((st = sync(s))) return st;
+  SolveInfo info;
+  CK(cudaMemcpy(&info, s->d_info, sizeof(info), cudaMemcpyDeviceToHost));
+  if (iterations) *iterations = info.iterations;
+  if (error) *error = info.error;
+  if (!info.converged)
+    return fail(EPIC_WARN_NOT_CONVERGED, "solver did not reach the tolerance in %d iterations (error %g)",
+                info.iterations, info.error);
+  return EPIC_OK;
+}
+
+epic_status epic_calculate_efield(epic_sim* s) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  epic_status st = do_efield(s);
+  if (st) return st;
+  return sync(s);
+}
+
+epic_status epic_push_species(epic_sim* s, int i, int sub_cycle) {
+  if (!valid_species(s, i)) return fail(EPIC_ERR_INVALID, "bad species index");
+  epic_status st = do_push(s, i, sub_cycle);
+  if (st) return st;
+  return sync(s);
+}
+
+epic_status epic_rewind_species(epic_sim* s, int i) {
+  if (!valid_species(s, i)) return fail(EPIC_ERR_INVALID, "bad species index");
+  epic_species_state& sp = s->sp[i];
+  const epic_config& c = s->cfg;
+  double qm = sp.desc.charge / sp.desc.mass;
+  double K = (c.density * QE * c.L) / (EPS_0 * c.W * c.vel_norm);
+  double hqmK = 0.5 * qm * K;
+  launch_rewind(s->stream, s->g, c.shape, sp.soa, sp.d_n, s->ef, hqmK, c.DT, s->d_flags, s->part_grid);
+  s->launches += 1;
+  CKL();
+  return sync(s);
+}
+
+static epic_status upload_tables(epic_sim* s, const double* tot, const double* ela, const double* exc,
+                                 const double* ion, int64_t n) {
+  double** dst[4] = {&s->cs.tot, &s->cs.ela, &s->cs.exc, &s->cs.ion};
+  const double* src[4] = {tot, ela, exc, ion};
+  for (int k = 0; k < 4; k++) {
+    if (*dst[k]) cudaFree(*dst[k]);
+    *dst[k] = nullptr;
+    CK(cudaMalloc((void**)dst[k], (size_t)n * sizeof(double)));
+    CK(cudaMemcpy(*dst[k], src[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+  }
+  s->cs.n = n;
+  return EPIC_OK;
+}
+
+epic_status epic_set_cross_sections(epic_sim* s, const double* tot, const double* ela, const double* exc,
+                                    const double* ion, int64_t n, double de) {
+  if (!s || !tot || !ela || !exc || !ion || n < 2 || !(de > 0)) return fail(EPIC_ERR_INVALID, "bad argument");
+  epic_status st = upload_tables(s, tot, ela, exc, ion, n);
+  if (st) return st;
+  s->cs.kind = 0;
+  s->cs.de = de;
+  // Null-collision bound: nu = tot[idx] * |v| with |v| below v(E_idx + de/2).
+  double mx = 0;
+  for (int64_t i = 0; i < n; i++) {
+    double e = (i + 0.5) * de;
+    if (i == n - 1) e = 4 * n * de;  // energies past the table reuse the last entry
+    double v = sqrt(2.0 * e * EV / ME);
+    mx = std::max(mx, tot[i] * v);
+  }
+  s->cs.nu_max = mx;
+  return EPIC_OK;
+}
+
+epic_status epic_set_reference_cross_sections(epic_sim* s) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  std::vector<double> tot, ela, exc, ion;
+  reference_tables(s->cfg, tot, ela, exc, ion);
+  return epic_set_cross_sections(s, tot.data(), ela.data(), exc.data(), ion.data(), (int64_t)tot.size(), DE_CS);
+}
+
+epic_status epic_set_log_cross_sections(epic_sim* s, const double* ela, const double* exc, const double* ion,
+                                        int64_t n, double e_min, double e_max) {
+  if (!s || !ela || !exc || !ion || n < 2 || !(e_min > 0) || !(e_max > e_min))
+    return fail(EPIC_ERR_INVALID, "bad argument");
+  std::vector<double> tot(n);
+  for (int64_t i = 0; i < n; i++) tot[i] = (ela[i] + exc[i] + ion[i]) * s->cfg.gas_density;
+  epic_status st = upload_tables(s, tot.data(), ela, exc, ion, n);
+  if (st) return st;
+  s->cs.kind = 1;
+  s->cs.e_min = e_min;
+  s->cs.e_max = e_max;
+  s->cs.log_emin = log(e_min);
+  s->cs.inv_dlog = (n - 1) / (log(e_max) - log(e_min));
+  double mx = 0;
+  for (int64_t i = 0; i + 1 < n; i++) {
+    double e1 = exp(log(e_min) + (i + 1) / s->cs.inv_dlog);
+    mx = std::max(mx, std::max(tot[i], tot[i + 1]) * sqrt(2.0 * e1 * EV / ME));
+  }
+  mx = std::max(mx, tot[n - 1] * sqrt(2.0 * 4 * e_max * EV / ME));
+  s->cs.nu_max = mx;
+  return EPIC_OK;
+}
+
+epic_status epic_handle_collisions(epic_sim* s, int e, int ion, const double* uniforms, int ustride,
+                                   int64_t* collisions) {
+  if (!valid_species(s, e) || !valid_species(s, ion) || e == ion) return fail(EPIC_ERR_INVALID, "bad species");
+  const double* d_u = nullptr;
+  if (s->cfg.mcc_mode == EPIC_MCC_INJECTED) {
+    if (!uniforms || ustride < 14) return fail(EPIC_ERR_INVALID, "injected mode needs uniforms with stride >= 14");
+    int64_t ne = 0;
+    epic_status st = epic_num_particles(s, e, &ne);
+    if (st) return st;
+    size_t len = (size_t)std::max<int64_t>(ne, 1) * ustride;
+    if ((long long)len > s->uniforms_len) {
+      if (s->d_uniforms) cudaFree(s->d_uniforms);
+      s->d_uniforms = nullptr;
+      CK(cudaMalloc(&s->d_uniforms, len * sizeof(double)));
+      s->uniforms_len = (long long)len;
+    }
+    CK(cudaMemcpyAsync(s->d_uniforms, uniforms, (size_t)ne * ustride * sizeof(double), cudaMemcpyHostToDevice,
+                       s->stream));
+    d_u = s->d_uniforms;
+  }
+  epic_status st = do_mcc(s, e, ion, d_u, ustride);
+  if (st) return st;
+  if ((st = sync(s))) return st;
+  unsigned long long nc = 0;
+  CK(cudaMemcpy(&nc, s->d_ncoll, sizeof(nc), cudaMemcpyDeviceToHost));
+  if (collisions) *collisions = (int64_t)nc;
+  return EPIC_OK;
+}
+
+epic_status epic_step(epic_sim* s, int with_collisions) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  epic_status st = do_step(s, with_collisions);
+  if (st) return st;
+  return sync(s);
+}
+
+epic_status epic_initial_field(epic_sim* s) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  epic_status st;
+  for (int i = 0; i < (int)s->sp.size(); i++)
+    if ((st = do_deposit(s, i))) return st;
+  if ((st = do_finalize(s, FINALIZE_AND_RHO, -1))) return st;
+  if ((st = do_solve(s))) return st;
+  if ((st = do_efield(s))) return st;
+  if ((st = sync(s))) return st;
+  for (int i = 0; i < (int)s->sp.size(); i++)
+    if ((st = epic_rewind_species(s, i))) return st;
+  return EPIC_OK;
+}
+
+epic_status epic_run(epic_sim* s, int steps, int with_collisions, int use_graph) {
+  if (!s || steps < 0) return fail(EPIC_ERR_INVALID, "bad argument");
+  epic_status st;
+  if (!use_graph) {
+    for (int k = 0; k < steps; k++)
+      if ((st = do_step(s, with_collisions))) return st;
+    return sync(s);
+  }
+  if (!s->graph_exec || s->graph_collisions != with_collisions) {
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    s->graph_exec = nullptr;
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
+    int64_t before = s->launches;
+    st = do_step(s, with_collisions);
+    cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
+    if (st) return st;
+    if (ce != cudaSuccess) return fail(EPIC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    s->graph_launches = s->launches - before;
+    s->launches = before;
+    ce = cudaGraphInstantiate(&s->graph_exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return fail(EPIC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    s->graph_collisions = with_collisions;
+  }
+  for (int k = 0; k < steps; k++) {
+    CK(cudaGraphLaunch(s->graph_exec, s->stream));
+    s->launches += s->graph_launches;
+  }
+  return sync(s);
+}
+
+epic_status epic_compute_ke(epic_sim* s, int i, int norm, double out[3]) {
+  if (!valid_species(s, i) || !valid_species(s, norm) || !out) return fail(EPIC_ERR_INVALID, "bad argument");
+  epic_species_state& sp = s->sp[i];
+  launch_particle_sums(s->stream, 0, sp.soa, sp.d_n, s->cfg.vel_norm, s->sum_partials, s->d_sums, s->part_grid);
+  s->launches += 2;
+  CKL();
+  double k[3];
+  CK(cudaMemcpyAsync(k, s->d_sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  epic_status st = sync(s);
+  if (st) return st;
+  const epic_species_desc& n = s->sp[norm].desc;
+  double Th = (n.temp * EV) * (n.spwt) * n.numparticle;
+  for (int c = 0; c < 3; c++) {
+    k[c] *= 0.5 * (sp.desc.spwt * sp.desc.mass);
+    out[c] = k[c] / Th;
+  }
+  return EPIC_OK;
+}
+
+epic_status epic_compute_momentum(epic_sim* s, int i, int norm, double out[3]) {
+  if (!valid_species(s, i) || !valid_species(s, norm) || !out) return fail(EPIC_ERR_INVALID, "bad argument");
+  epic_species_state& sp = s->sp[i];
+  launch_particle_sums(s->stream, 1, sp.soa, sp.d_n, s->cfg.vel_norm, s->sum_partials, s->d_sums, s->part_grid);
+  s->launches += 2;
+  CKL();
+  double p[3];
+  CK(cudaMemcpyAsync(p, s->d_sums, 3 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  epic_status st = sync(s);
+  if (st) return st;
+  const epic_species_desc& n = s->sp[norm].desc;
+  double Thp = sqrt(n.temp * EV / ME) * n.spwt * n.numparticle * ME;
+  for (int c = 0; c < 3; c++) {
+    p[c] *= (sp.desc.spwt * sp.desc.mass);
+    out[c] = p[c] / Thp;
+  }
+  return EPIC_OK;
+}
+
+epic_status epic_compute_pe(epic_sim* s, int norm, double* pe) {
+  if (!valid_species(s, norm) || !pe) return fail(EPIC_ERR_INVALID, "bad argument");
+  launch_grid_sums(s->stream, 0, s->g, s->efx, s->efy, s->cfg.L, s->sum_partials, s->d_sums);
+  s->launches += 2;
+  CKL();
+  double v = 0;
+  CK(cudaMemcpyAsync(&v, s->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  epic_status st = sync(s);
+  if (st) return st;
+  const epic_config& c = s->cfg;
+  const epic_species_desc& n = s->sp[norm].desc;
+  double unnorm = (c.density * QE * c.L) / EPS_0;
+  double pe_norm = 0.5 * EPS_0 * v * unnorm * unnorm;
+  double Th = (n.temp * EV) * n.spwt * n.numparticle;
+  *pe = pe_norm / Th;
+  return EPIC_OK;
+}
+
+epic_status epic_delta_phi(epic_sim* s, double* dphi) {
+  if (!s || !dphi) return fail(EPIC_ERR_INVALID, "bad argument");
+  launch_grid_sums(s->stream, 1, s->g, s->phi, s->phi, 0.0, s->sum_partials, s->d_sums);
+  s->launches += 2;
+  CKL();
+  double v[2];
+  CK(cudaMemcpyAsync(v, s->d_sums, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaMemcpyAsync(v + 1, s->phi, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  epic_status st = sync(s);
+  if (st) return st;
+  *dphi = v[0] - v[1];
+  return EPIC_OK;
+}
+
+static double* grid_ptr(epic_sim* s, int which) {
+  switch (which) {
+    case EPIC_GRID_PHI: return s->phi;
+    case EPIC_GRID_RHO: return s->rho;
+    case EPIC_GRID_EFX: return s->efx;
+    case EPIC_GRID_EFY: return s->efy;
+    default:
+      if (which >= EPIC_GRID_DEN0 && which - EPIC_GRID_DEN0 < (int)s->sp.size()) return s->sp[which - EPIC_GRID_DEN0].den;
+      return nullptr;
+  }
+}
+
+epic_status epic_get_grid(epic_sim* s, int which, double* out) {
+  if (!s || !out) return fail(EPIC_ERR_INVALID, "bad argument");
+  double* p = grid_ptr(s, which);
+  if (!p) return fail(EPIC_ERR_INVALID, "unknown grid %d", which);
+  CK(cudaMemcpyAsync(out, p, nnodes(s) * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  return sync(s);
+}
+
+epic_status epic_set_grid(epic_sim* s, int which, const double* in) {
+  if (!s || !in) return fail(EPIC_ERR_INVALID, "bad argument");
+  double* p = grid_ptr(s, which);
+  if (!p) return fail(EPIC_ERR_INVALID, "unknown grid %d", which);
+  CK(cudaMemcpyAsync(p, in, nnodes(s) * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+  epic_status st = sync(s);
+  if (st) return st;
+  if (which == EPIC_GRID_EFX || which == EPIC_GRID_EFY) {
+    // keep the interleaved gather copy in step with the component grids
+    std::vector<double> ex(nnodes(s)), ey(nnodes(s));
+    CK(cudaMemcpy(ex.data(), s->efx, nnodes(s) * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ey.data(), s->efy, nnodes(s) * sizeof(double), cudaMemcpyDeviceToHost));
+    std::vector<double2> e2(nnodes(s));
+    for (long long k = 0; k < nnodes(s); k++) e2[k] = make_double2(ex[k], ey[k]);
+    CK(cudaMemcpy(s->ef, e2.data(), nnodes(s) * sizeof(double2), cudaMemcpyHostToDevice));
+  }
+  return EPIC_OK;
+}
+
+epic_status epic_sync(epic_sim* s) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  return sync(s);
+}
+
+int64_t epic_kernel_launches(epic_sim* s) { return s ? s->launches : 0; }
+
+void* epic_stream(epic_sim* s) { return s ? (void*)s->stream : nullptr; }
+
+epic_status epic_set_profiling(epic_sim* s, int enable) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  s->profiling = enable ? 1 : 0;
+  return EPIC_OK;
+}
+
+epic_status epic_get_profile(epic_sim* s, double ms[EPIC_NUM_PHASES], int64_t counts[EPIC_NUM_PHASES],
+                             int64_t* solver_iterations) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  CK(cudaStreamSynchronize(s->stream));
+  for (auto& pe : s->prof_pending) {
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, pe.second.first, pe.second.second));
+    s->prof_ms[pe.first] += t;
+    s->prof_count[pe.first] += 1;
+    s->event_pool.push_back(pe.second.first);
+    s->event_pool.push_back(pe.second.second);
+  }
+  s->prof_pending.clear();
+  unsigned long long it = 0;
+  CK(cudaMemcpy(&it, s->d_iter_total, sizeof(it), cudaMemcpyDeviceToHost));
+  CK(cudaMemset(s->d_iter_total, 0, sizeof(it)));
+  for (int k = 0; k < EPIC_NUM_PHASES; k++) {
+    if (ms) ms[k] = s->prof_ms[k];
+    if (counts) counts[k] = s->prof_count[k];
+    s->prof_ms[k] = 0;
+    s->prof_count[k] = 0;
+  }
+  if (solver_iterations) *solver_iterations = (int64_t)it;
+  return EPIC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,201 @@
+// Internal declarations shared by the kernel files and the C ABI.
+//
+// Device data layout (HBM, one simulation):
+//   particles : per species, structure of arrays x, y, vx, vy, vz (FP64),
+//               capacity `cap`, live count in device memory (`d_n`) so every
+//               particle kernel is a fixed-size launch that reads its bound on
+//               the device (graph-capturable, no host round trip per step).
+//   grids     : nx*ny FP64 arrays, node (i, j) at i*ny + j (the reference's
+//               Matrix<double>(nx, ny) order): phi, rho, efx, efy, one density
+//               per species, plus `ef` = interleaved (efx, efy) double2 so a
+//               gather costs one 16-byte load per node.
+//   deposit   : int64 fixed-point accumulators per species (deterministic) or
+//               FP64 atomics straight into the density grid.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/epic2d.h"
+
+namespace epic {
+
+// Constants of include/domain.h:204-215 and include/collision.h:14-15,
+// include/cross_sections.h:14-15 (PI is the reference's truncated value).
+constexpr double EPS_0 = 8.85418782e-12;
+constexpr double QE = 1.602176565e-19;
+constexpr double ME = 9.10938215e-31;
+constexpr double K_B = 1.380648e-23;
+constexpr double PI_REF = 3.141592653;
+constexpr double EV = 1.602176565e-19;
+constexpr int CS_RANGES = 5000000;
+constexpr double DE_CS = 0.005;
+constexpr double E_EXC_TH = 11.5;
+constexpr double E_ION_TH = 15.8;
+
+// Device error flag bits (sim->d_flags[0]).
+enum : int {
+  FLAG_OUT_OF_GRID = 1,
+  FLAG_CAPACITY = 2,
+  FLAG_TIMEOUT = 4,
+  FLAG_BAD_TABLE = 8,
+};
+
+// Bounded spin: polls of a device-side wait before it reports FLAG_TIMEOUT.
+constexpr long long SPIN_LIMIT = 1ll << 24;
+
+constexpr int PART_THREADS = 256;
+constexpr int SCAN_TILE = 1024;  // particles per ordered tile (push+compact, MCC append)
+
+struct Geom {
+  int nx, ny;
+  double x0, y0, dx, dy, Lx, Ly;
+};
+
+struct SoA {
+  double *x, *y, *vx, *vy, *vz;
+};
+
+// Per-launch solver outcome, written by the device.
+struct SolveInfo {
+  int iterations;
+  int converged;
+  double error;
+};
+
+struct CrossSections {
+  // kind 0: linear grid E_i = de*i (E_0 = de), nearest index (the reference);
+  // kind 1: logarithmic grid, linear interpolation in log E (extension).
+  int kind;
+  int64_t n;
+  double de, log_emin, inv_dlog, e_min, e_max;
+  double *tot, *ela, *exc, *ion;  // tot includes the gas density
+  double nu_max;                  // bound of tot(E)*v(E) for null collisions
+};
+
+// ---- kernel launchers (epic_particles.cu) ----
+void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const SoA& p, const long long* d_n,
+                    double spwt, double* den, unsigned long long* acc, double fx_scale, int* flags, int grid);
+void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
+                 const double2* ef, double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
+                 unsigned int* tile_ctr, int grid);
+void launch_rewind(cudaStream_t st, const Geom& g, int shape, const SoA& p, const long long* d_n, const double2* ef,
+                   double hqmK, double dt, int* flags, int grid);
+// d_step: device step counter (Philox counter word), advanced by every MCC
+// launch so replayed graphs draw fresh numbers.
+void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const SoA& e, long long* d_ne, long long e_cap,
+                const SoA& ion, long long* d_ni, long long i_cap, double vel_norm, double dt_phys, double ion_mass,
+                double ion_temp, const double* uniforms, int ustride, uint64_t seed, unsigned long long* d_step,
+                unsigned long long* tile_status, unsigned int* tile_ctr, unsigned long long* d_ncoll, int* flags,
+                int grid);
+void launch_particle_sums(cudaStream_t st, int what, const SoA& p, const long long* d_n, double vel_norm,
+                          double* partials, double* out3, int grid);
+
+// ---- kernel launchers (epic_field.cu) ----
+// FINALIZE_ONLY: density of the active species from its accumulator;
+// FINALIZE_AND_RHO: every species, then rho; RHO_FROM_DEN: rho from the
+// already finalised density grids.
+enum { FINALIZE_ONLY = 0, FINALIZE_AND_RHO = 1, RHO_FROM_DEN = 2 };
+struct FinalizeArgs {
+  Geom g;
+  int nsp;
+  int bc;
+  int fixed;
+  int stage;
+  int active[8];
+  double div;
+  const unsigned long long* acc[8];
+  double* den[8];
+  double spwt[8];
+  double inv_scale[8];
+  double charge_over_qe[8];
+  double* rho;
+};
+void launch_finalize(cudaStream_t st, const FinalizeArgs& a);
+void launch_efield(cudaStream_t st, const Geom& g, int bc, const double* phi, double* efx, double* efy, double2* ef);
+
+struct SolverArgs {
+  Geom g;
+  double tol;
+  int max_iter;
+  double omega;
+  double K;          // (L*L)/(LDe*LDe)
+  const double* rho;
+  double* phi;
+  SolveInfo* info;
+  unsigned long long* iter_total;  // running sum of iterations (profiling)
+  int* flags;
+  // PCG / red-black workspace
+  double *b, *r, *va, *vb, *u;
+  double* partials;  // 4 * max_blocks
+  unsigned int* bar; // grid barrier {count, generation}
+  int warm;
+};
+void init_field_kernels();  // one-time kernel attributes (called by epic_create)
+void launch_sor_lex(cudaStream_t st, const SolverArgs& a);
+void launch_sor_redblack(cudaStream_t st, const SolverArgs& a, int blocks);
+void launch_pcg(cudaStream_t st, const SolverArgs& a, int blocks);
+int solver_max_blocks();
+void launch_grid_sums(cudaStream_t st, int what, const Geom& g, const double* a, const double* b, double L,
+                      double* partials, double* out);
+
+}  // namespace epic
+
+// The opaque handle of the C ABI.
+struct epic_species_state {
+  epic_species_desc desc;
+  std::string name;
+  long long cap;
+  epic::SoA soa;
+  long long* d_n;
+  double* den;
+  unsigned long long* acc;
+  double fx_scale;      // 2^k
+  double fx_inv_scale;  // 2^-k
+};
+
+struct epic_sim {
+  epic_config cfg;
+  epic::Geom g;
+  cudaStream_t stream;
+  int num_sms;
+  int part_grid;
+  std::vector<epic_species_state> sp;
+  double *phi, *rho, *efx, *efy;
+  double2* ef;
+  // solver workspace
+  double *b, *r, *va, *vb, *u, *partials;
+  unsigned int* bar;
+  epic::SolveInfo* d_info;
+  unsigned long long* d_iter_total;
+  // particle scratch
+  unsigned long long* tile_status;
+  long long tile_status_len;
+  unsigned int* tile_ctr;
+  unsigned long long* d_ncoll;  // [0] collisions of the last MCC, [1..2] pending appends/collisions
+  unsigned long long* d_step;   // MCC launches so far (Philox counter)
+  void* staging;                // AoS staging for uploads/downloads
+  size_t staging_bytes;
+  double* d_uniforms;
+  long long uniforms_len;
+  double* sum_partials;
+  double* d_sums;
+  double* h_sums;  // pinned
+  int* d_flags;
+  epic::CrossSections cs;
+  int64_t launches;
+  cudaGraphExec_t graph_exec;
+  int64_t graph_launches;
+  int graph_collisions;
+  // per-phase profiling (events on `stream`)
+  int profiling;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
+  std::vector<cudaEvent_t> event_pool;
+  double prof_ms[EPIC_NUM_PHASES];
+  int64_t prof_count[EPIC_NUM_PHASES];
+  int64_t prof_iters;
+  int prof_solves;
+};

@@ -1,0 +1,131 @@
+"""Benchmark workloads as input.ini decks, and the synthetic cross-section table.
+
+Each workload is a deck in the reference's input.ini format.  Sizes follow the
+configurations the project is measured on:
+
+* ``periodic_64`` — 64x64 cells, 50 particles per cell per species
+  (204,800 electrons + 204,800 ions), Te 1 eV, Ti 0.026 eV, ion mass 1836 m_e,
+  n0 1e13 m^-3, dt 0.01/wpe, CIC, SOR (omega 1.8, tolerance 1e-8), no collisions.
+* ``beam_mcc_256`` — 256x256 cells, 100 particles per cell: 6,553,600 ions
+  (40 amu) and 6,553,600 electrons of which 10 % are a beam drifting at 5 v_th,e,
+  PCG to 1e-10, MCC against 1e20 m^-3 neutrals with the synthetic 1000-point
+  log-spaced table below.
+* ``periodic_1024`` — 1024x1024 cells, 100 particles per cell per species.
+
+Inputs are seeded synthetic plasmas (the reference loads positions and
+velocities from mt19937 seed 0; so do these decks).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+AMU = 1.660538921e-27
+ME = 9.10938215e-31
+
+_TEMPLATE = """[file]
+output = data/
+
+[time]
+NUM_TS = {num_ts}
+DT_coeff = {dt}
+
+[diagnostics]
+write_interval = 10
+write_interval_phase = 100
+write_diagnostics = 50
+write_flag = 0
+save_fig   = 0
+sub_cycle_interval = 20
+precision = 4
+
+[PlotFlags]
+phase_space     = 0
+config_space    = 0
+electric_field  = 0
+potential_field = 0
+density_contour = 0
+ke_components   = 1
+total_energy    = 1
+species_index   = 0
+
+[domain]
+Nx       = {n}
+Ny       = {n}
+x0       = 0
+y0       = 0
+
+[Grids]
+grid_count = 0
+
+[Emitters]
+count = 0
+
+[normalization]
+norm_scheme = 1
+vel_norm_scheme = 1
+lenght_scale = 0.005
+time_scale = omegape
+energy_scale = 1
+
+[solver]
+solvertype = {solver}
+tolerance = {tol}
+max_iteration = {maxit}
+{solver_extra}
+[simulation]
+shapefunction = CIC
+push_parallal  = false
+deposit_parallal = false
+density = 1E13
+bc = {bc}
+ionfixed = 0
+
+[collision]
+elastic    = {coll}
+excitation = {coll}
+ionization = {coll}
+GAS_DENSITY = {gas}
+
+[species]
+{species}
+"""
+
+
+def deck(name: str) -> str:
+    if name == "periodic_64":
+        n, ppc = 64, 50
+        sp = ["electron,%.8E,%d,1,-1,1,0,0,random" % (ME, n * n * ppc),
+              "ion,%.8E,%d,0.026,1,0,0,0,random" % (1836 * ME, n * n * ppc)]
+        return _TEMPLATE.format(num_ts=1000, dt=0.01, n=n, solver="gs", tol="1e-8", maxit=200000,
+                                solver_extra="sor_omega = 1.8\n", bc="pbc", coll="false", gas="1e20",
+                                species="\n".join(sp))
+    if name == "beam_mcc_256":
+        n, ppc = 256, 100
+        total_e = n * n * ppc
+        beam = total_e // 10
+        # fract_den is relative to the first species: 0.1/0.9 of the bulk.
+        sp = ["electron,%.8E,%d,1,-1,1,0,0,random" % (ME, total_e - beam),
+              "ion,%.8E,%d,0.026,1,0,0,0,random" % (40 * AMU, total_e),
+              "beam,%.8E,%d,1,-1,%.17g,5,0,random" % (ME, beam, 1.0 / 9.0)]
+        return _TEMPLATE.format(num_ts=2000, dt=0.01, n=n, solver="cg", tol="1e-10", maxit=100000,
+                                solver_extra="", bc="pbc", coll="true", gas="1e20", species="\n".join(sp))
+    if name == "periodic_1024":
+        n, ppc = 1024, 100
+        sp = ["electron,%.8E,%d,2,-1,1,0,0,random" % (ME, n * n * ppc),
+              "ion,%.8E,%d,0.05,1,0,0,0,random" % (1836 * ME, n * n * ppc)]
+        return _TEMPLATE.format(num_ts=500, dt=0.05, n=n, solver="cg", tol="1e-10", maxit=100000,
+                                solver_extra="", bc="pbc", coll="false", gas="1e20", species="\n".join(sp))
+    raise KeyError(name)
+
+
+def synthetic_table(n: int = 1000, e_min: float = 0.01, e_max: float = 1000.0):
+    """Synthetic e-/neutral cross sections [m^2] on n log-spaced energies [eV]:
+    elastic 1e-19 flat; excitation zero below 11.5 eV, rising linearly to
+    2e-20 at 50 eV and falling as 1/E above; ionisation zero below 15.8 eV,
+    x*exp(1-x) with x = (E-15.8)/(100-15.8), i.e. a 3e-20 peak at 100 eV."""
+    e = e_min * (e_max / e_min) ** (np.arange(n) / (n - 1))
+    ela = np.full(n, 1e-19)
+    exc = np.where(e < 11.5, 0.0, np.where(e < 50.0, 2e-20 * (e - 11.5) / (50.0 - 11.5), 2e-20 * 50.0 / e))
+    x = (e - 15.8) / (100.0 - 15.8)
+    ion = np.where(e < 15.8, 0.0, 3e-20 * x * np.exp(1.0 - x))
+    return e, ela, exc, ion

@@ -1,0 +1,207 @@
+/* epic2d.h — C ABI of the GB300 implementation of the ePIC2D time-step loop.
+ *
+ * One handle (epic_sim) owns one simulation resident on one GPU: particles as a
+ * structure of arrays per species, and the node grids phi, rho, efx, efy and
+ * one density grid per species.  Every entry point takes plain pointers and
+ * sizes, never throws, and returns an epic_status; epic_last_error() gives the
+ * message of the last failure on the calling thread.
+ *
+ * Each call replaces one method of the reference's C++ interface (the
+ * reference has no FFI of its own; its seam is the method sequence of
+ * src/main.cpp:359-423).  The citation beside each declaration names the
+ * method it replaces.  Host arrays use the reference's layouts: grids are
+ * row-major doubles with node (i, j) at i*ny + j (Matrix<double>(nx, ny),
+ * linearalgebra/linalg.h:208-220) and particles are records of five doubles
+ * {x, y, vx, vy, vz} (class Particle, include/species.h:22-37).
+ *
+ * A handle is used from one host thread at a time; all its GPU work runs in
+ * order on the handle's own CUDA stream.
+ */
+#ifndef EPIC2D_H
+#define EPIC2D_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  EPIC_OK = 0,
+  EPIC_ERR_INVALID = 1,       /* bad argument or configuration */
+  EPIC_ERR_CUDA = 2,          /* CUDA runtime error */
+  EPIC_ERR_NOMEM = 3,         /* device allocation failed */
+  EPIC_ERR_CAPACITY = 4,      /* a species outgrew its particle capacity */
+  EPIC_WARN_NOT_CONVERGED = 5,/* Poisson solve hit max_iteration (the reference prints to cerr) */
+  EPIC_ERR_DOMAIN = 6,        /* a particle left the grid (the reference throws std::out_of_range) */
+  EPIC_ERR_TIMEOUT = 7,       /* a device-side wait gave up */
+  EPIC_ERR_BUDGET = 8,        /* admission refused: the memory budget is exhausted */
+  EPIC_ERR_IO = 9             /* input file could not be read */
+} epic_status;
+
+enum { EPIC_CIC = 0, EPIC_NGP = 1 };                    /* [simulation] shapefunction */
+enum { EPIC_PBC = 0, EPIC_OPEN = 1, EPIC_REFLECTIVE = 2 }; /* [simulation] bc */
+enum { EPIC_SOLVER_GS = 0, EPIC_SOLVER_PCG = 1 };       /* [solver] solvertype gs | cg/iter/iterative */
+enum { EPIC_SOR_LEXICOGRAPHIC = 0, EPIC_SOR_REDBLACK = 1 };
+enum { EPIC_DEPOSIT_FIXED = 0, EPIC_DEPOSIT_FP64 = 1 };
+enum { EPIC_MCC_PHILOX = 0, EPIC_MCC_INJECTED = 1, EPIC_MCC_NULL = 2 };
+enum { EPIC_GRID_PHI = 0, EPIC_GRID_RHO = 1, EPIC_GRID_EFX = 2, EPIC_GRID_EFY = 3, EPIC_GRID_DEN0 = 10 };
+
+/* Everything Domain holds for the loop (include/domain.h:26-201), already
+ * normalised as src/main.cpp:151-245 and Domain::set_normscheme
+ * (src/domain.cpp:123-183) leave it, plus the GPU-side options.  Fields after
+ * `gas_density`..`ionization` are options with no reference counterpart;
+ * epic_config_defaults() sets each to the reference's behaviour. */
+typedef struct {
+  int nx, ny;                 /* node counts, Nx+1 and Ny+1 */
+  double x0, y0, dx, dy;      /* origin and cell size (normalised) */
+  double DT;                  /* normalised time step */
+  double L, W, vel_norm;      /* length, frequency and velocity scales */
+  double LDe, wpe, LDi, wpi;  /* Debye lengths and plasma frequencies */
+  double density;             /* n0 [m^-3] */
+  int shape;                  /* EPIC_CIC | EPIC_NGP */
+  int bc;                     /* EPIC_PBC | EPIC_OPEN | EPIC_REFLECTIVE */
+  int solver;                 /* EPIC_SOLVER_GS | EPIC_SOLVER_PCG */
+  double tolerance;
+  int max_iteration;
+  int ionfixed;               /* skip the push of the species named "ion" */
+  int normscheme;
+  double gas_density;         /* [collision] GAS_DENSITY */
+  int elastic, excitation, ionization;
+  /* --- options (no reference counterpart) --- */
+  double sor_omega;           /* 1.4, hard-coded at src/field.cpp:114 */
+  int sor_mode;               /* EPIC_SOR_LEXICOGRAPHIC reproduces gssolver's iterates */
+  int deposit_mode;           /* EPIC_DEPOSIT_FIXED: int64 fixed point, bit-reproducible */
+  int mcc_mode;               /* EPIC_MCC_PHILOX: the reference's direct MCC on a Philox stream */
+  uint64_t seed;              /* Philox key */
+  int warm_start;             /* 0: cold-start solves as the reference */
+  int reserved[16];
+} epic_config;
+
+/* One [species] line of input.ini (src/main.cpp:132-149) after set-up. */
+typedef struct {
+  char name[32];
+  double mass, charge, spwt, temp;
+  int numparticle;
+  double vsx, vsy, fract_den;
+  char load[32];              /* random | uniform | sin(n) | cos(n) */
+  int64_t capacity;           /* particle slots to allocate; 0 = default */
+} epic_species_desc;
+
+typedef struct epic_sim epic_sim;
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* epic_last_error(void);
+
+/* Reference behaviour for every option field. */
+void epic_config_defaults(epic_config* cfg);
+
+/* INIParser::parse + the set-up of src/main.cpp:34-261 (normalisation, species
+ * densities and weights; src/iniparser.cpp:4-113).  Also reads the optional
+ * keys sor_omega, sor_mode, deposit_mode, mcc_mode, seed, warm_start from
+ * [solver]/[simulation]/[collision].  *num_species is set to the number of
+ * species lines; at most max_species descriptors are written. */
+epic_status epic_config_from_ini(const char* path, epic_config* cfg, epic_species_desc* species, int max_species,
+                                 int* num_species, int* num_ts);
+
+/* Domain::Domain + FieldSolve::FieldSolve (src/domain.cpp:7-16, include/field.h:19). */
+epic_status epic_create(const epic_config* cfg, epic_sim** out);
+void epic_destroy(epic_sim* sim);
+
+/* Species::Species (src/species.cpp:6-22).  *index receives the species index. */
+epic_status epic_add_species(epic_sim* sim, const epic_species_desc* desc, int* index);
+
+/* Init::Init for every species in index order from one mt19937 stream seeded
+ * with `seed` (src/init.cpp:3-101; the reference seeds its global Rnd with 0,
+ * include/domain.h:223).  Host-side start-up, as in the reference. */
+epic_status epic_load_particles(epic_sim* sim, uint32_t seed);
+
+/* Particle upload/download in the Particle layout (5 doubles per particle). */
+epic_status epic_set_particles(epic_sim* sim, int species, const double* particles, int64_t n);
+epic_status epic_get_particles(epic_sim* sim, int species, double* particles, int64_t capacity, int64_t* n);
+epic_status epic_num_particles(epic_sim* sim, int species, int64_t* n);
+
+/* Species::ScatterSpecies_serial (src/species.cpp:172-226). */
+epic_status epic_scatter_species(epic_sim* sim, int species);
+/* Domain::ComputeRho (src/domain.cpp:194-202). */
+epic_status epic_compute_rho(epic_sim* sim);
+/* FieldSolve::PotentialSolver (src/field.cpp:266-272): gssolver or pcgsolver.
+ * iterations / error may be NULL; returns EPIC_WARN_NOT_CONVERGED at the cap. */
+epic_status epic_potential_solver(epic_sim* sim, int* iterations, double* error);
+/* FieldSolve::CalculateEfield (src/field.cpp:276-330). */
+epic_status epic_calculate_efield(epic_sim* sim);
+/* Species::Push_species_serial (src/species.cpp:29-170), no conductors. */
+epic_status epic_push_species(epic_sim* sim, int species, int sub_cycle);
+/* Species::Rewind_species (src/species.cpp:229-246). */
+epic_status epic_rewind_species(epic_sim* sim, int species);
+
+/* CollisionHandler::set_electron_cross_sections + calc_total_cross_sections
+ * (src/collision.cpp:12-42): per-energy tables on the linear grid
+ * E_i = de*i (E_0 = de), tot already multiplied by the gas density. */
+epic_status epic_set_cross_sections(epic_sim* sim, const double* tot, const double* ela, const double* exc,
+                                    const double* ion, int64_t n, double de);
+/* Fills the tables with the e-/Ar fits of src/cross_section.cpp:4-39 on the
+ * reference's 5,000,000-point, 0.005 eV grid (host-side start-up). */
+epic_status epic_set_reference_cross_sections(epic_sim* sim);
+/* Logarithmic table extension: n points from e_min to e_max [eV], sigma in
+ * m^2 (not yet multiplied by the gas density), interpolated linearly in
+ * log E.  Replaces the linear table. */
+epic_status epic_set_log_cross_sections(epic_sim* sim, const double* ela, const double* exc, const double* ion,
+                                        int64_t n, double e_min, double e_max);
+/* CollisionHandler::handle_collisions (src/collision.cpp:190-207) of electron
+ * species `electrons` against the neutral gas, with `ions` receiving the
+ * ionisation products.  In EPIC_MCC_INJECTED mode, `uniforms` is a host array
+ * of stride `ustride` per electron (the electron with index p draws
+ * uniforms[p*ustride + k] in the reference's draw order); otherwise it is
+ * ignored.  *collisions (may be NULL) receives the number of collisions. */
+epic_status epic_handle_collisions(epic_sim* sim, int electrons, int ions, const double* uniforms, int ustride,
+                                   int64_t* collisions);
+
+/* One iteration of the loop body of src/main.cpp:405-423 (no emitters):
+ * scatter all species, ComputeRho, PotentialSolver, CalculateEfield, push
+ * every species (the one named "ion" is skipped if ionfixed), then
+ * handle_collisions(species 0, species 1) if with_collisions. */
+epic_status epic_step(epic_sim* sim, int with_collisions);
+/* The prologue of src/main.cpp:366-382: scatter, rho, solve, E, rewind. */
+epic_status epic_initial_field(epic_sim* sim);
+/* Runs `steps` loop iterations; with use_graph=1 one step is captured as a
+ * CUDA graph and replayed (fixed-size launches, device-side counts). */
+epic_status epic_run(epic_sim* sim, int steps, int with_collisions, int use_graph);
+
+/* Species::Compute_KE / Compute_Momentum (src/species.cpp:248-297) and
+ * Domain::Compute_PE (src/domain.cpp:266-286); norm_species is the species
+ * whose temperature normalises (Output::storeKE_to_matrix, src/output.cpp:291-315). */
+epic_status epic_compute_ke(epic_sim* sim, int species, int norm_species, double out[3]);
+epic_status epic_compute_momentum(epic_sim* sim, int species, int norm_species, double out[3]);
+epic_status epic_compute_pe(epic_sim* sim, int norm_species, double* pe);
+/* max(phi) - phi(0,0) as printed by Output::diagnostics (src/output.cpp:320-336). */
+epic_status epic_delta_phi(epic_sim* sim, double* delta_phi);
+
+/* Grid download/upload (which = EPIC_GRID_*, EPIC_GRID_DEN0 + s). */
+epic_status epic_get_grid(epic_sim* sim, int which, double* out);
+epic_status epic_set_grid(epic_sim* sim, int which, const double* in);
+
+/* Waits for the handle's stream and reports any device-side error flag. */
+epic_status epic_sync(epic_sim* sim);
+/* Number of kernels this handle has launched (for launch accounting). */
+int64_t epic_kernel_launches(epic_sim* sim);
+/* The handle's CUDA stream (a cudaStream_t), for callers that order their own
+ * work or events after the simulation's. */
+void* epic_stream(epic_sim* sim);
+
+/* Per-phase timing with CUDA events recorded on the handle's stream around
+ * each phase of epic_step (no reference counterpart; the reference times the
+ * whole run only, src/main.cpp:282,465-469).  Phases: 0 deposit, 1 density
+ * finalisation + rho, 2 Poisson solve, 3 E-field, 4 push, 5 MCC.
+ * epic_get_profile waits for the stream, then returns accumulated
+ * milliseconds and step counts per phase and the solver iterations summed
+ * over the profiled steps; it resets the accumulators. */
+enum { EPIC_NUM_PHASES = 6 };
+epic_status epic_set_profiling(epic_sim* sim, int enable);
+epic_status epic_get_profile(epic_sim* sim, double ms[EPIC_NUM_PHASES], int64_t counts[EPIC_NUM_PHASES],
+                             int64_t* solver_iterations);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,113 @@
+"""The C ABI without a GPU: the library builds and loads, exports every entry
+point include/*.h declares, and its host-side set-up (INI parsing and
+normalisation, src/main.cpp:34-261) agrees with the oracle bit for bit."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import decks
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def E():
+    from epic2d_mcc_gb300 import build as B
+
+    B.build()
+    import epic2d_mcc_gb300 as E
+
+    return E
+
+
+def declared_symbols():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(epic_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_library_exports_every_declared_symbol(E):
+    L = E.lib()
+    syms = declared_symbols()
+    assert len(syms) >= 30
+    missing = [s for s in syms if not hasattr(L, s)]
+    assert not missing, missing
+
+
+DECKS = [dict(), dict(nx=20, ny=14, bc="open", shape="NGP", solver="cg", tol="1e-10"),
+         dict(norm=2, dt=0.001), dict(norm=4, te=3, ti=0.1),
+         dict(beam=dict(n=300, t=2, frac=0.5, vx=1, vy=2), collisions=True, gas="5e19")]
+
+
+@pytest.mark.parametrize("kw", DECKS)
+def test_config_from_ini_matches_oracle_setup(E, kw, tmp_path):
+    ini = decks.write(decks.deck(**kw), str(tmp_path))
+    cfg, descs, ts = E.config_from_ini(ini)
+    s = O.setup(ini)
+    assert (cfg.nx, cfg.ny) == (s.nx, s.ny)
+    for f in ("x0", "y0", "dx", "dy", "DT", "L", "W", "vel_norm", "LDe", "wpe", "LDi", "wpi", "density", "tolerance",
+              "gas_density"):
+        assert getattr(cfg, f) == getattr(s, f), f
+    assert cfg.max_iteration == s.max_iteration
+    assert cfg.bc == O.BC_CODES[s.bc] and cfg.shape == O.SHAPE_CODES[s.shape]
+    assert (cfg.elastic, cfg.excitation, cfg.ionization) == (s.elastic, s.excitation, s.ionization)
+    assert ts == s.num_ts
+    assert len(descs) == len(s.species)
+    for d, sp in zip(descs, s.species):
+        assert d.name.decode() == sp.name
+        assert (d.mass, d.charge, d.spwt, d.temp, d.numparticle, d.vsx, d.vsy) == (
+            sp.mass, sp.charge, sp.spwt, sp.temp, sp.numparticle, sp.vsx, sp.vsy)
+
+
+def test_config_defaults_are_reference_behaviour(E):
+    c = E.default_config()
+    assert c.sor_omega == 1.4  # src/field.cpp:114
+    assert c.sor_mode == 0 and c.warm_start == 0
+
+
+def test_optional_keys(E, tmp_path):
+    ini = decks.write(decks.deck(solver_extra="sor_omega = 1.8\nsor_mode = redblack\nwarm_start = true\n",
+                                 sim_extra="deposit_mode = fp64\n", coll_extra="mcc_mode = null\nseed = 7\n"),
+                      str(tmp_path))
+    cfg, _, _ = E.config_from_ini(ini)
+    assert cfg.sor_omega == 1.8 and cfg.sor_mode == 1 and cfg.warm_start == 1
+    assert cfg.deposit_mode == 1 and cfg.mcc_mode == 2 and cfg.seed == 7
+
+
+def test_errors_do_not_throw(E, tmp_path):
+    with pytest.raises(E.EpicError) as ei:
+        E.config_from_ini(str(tmp_path / "missing.ini"))
+    assert ei.value.status == 9  # EPIC_ERR_IO
+    text = decks.deck().replace("Ny       = 16\n", "")
+    with pytest.raises(E.EpicError) as ei:
+        E.config_from_ini(decks.write(text, str(tmp_path)))
+    assert ei.value.status == 1 and "Ny" in str(ei.value)
+    bad = decks.deck().replace("solvertype = gs", "solvertype = hybrid")
+    with pytest.raises(E.EpicError) as ei:
+        E.config_from_ini(decks.write(bad, str(tmp_path)))
+    assert "hybrid" in str(ei.value)
+
+
+def test_reference_input_deck_parses(E):
+    # The repository's example deck format (three species, conductor section
+    # present but grid_count = 0).
+    text = decks.deck(beam=dict(n=1000, t=1, frac=1, vx=10, vy=10))
+    cfg, descs, _ = E.config_from_ini(decks.write(text))
+    assert [d.name.decode() for d in descs] == ["electron", "ion", "beam"]
+    k = 2.0  # sum of -sign*frac = 1 + 0 + 1
+    assert descs[0].spwt == pytest.approx(1e13 / k * cfg.L ** 2 * 16 * 16 / 2000)
+
+
+def test_null_handle_is_rejected(E):
+    L = E.lib()
+    assert L.epic_step(None, 0) == 1
+    assert b"null" in L.epic_last_error()
