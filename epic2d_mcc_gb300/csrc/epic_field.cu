@@ -306,39 +306,85 @@ __device__ double sum_partials(const double* partials, int n, int stride, int of
 // = k/nx, col = k%nx) summed in column order is, term for term,
 //   u_k = ((v[k-nx] + v[k-1]) + (-4 v[k])) + v[k+1]) + v[k+nx]
 // with missing neighbours skipped.  Solution x lives in phi (unflatten keeps
-// the index i*ny + j).  Two grid barriers per iteration: the direction update
-// v <- w + s v is fused into the next SpMV, which recomputes the updated
-// neighbour values from r and the previous v (double-buffered).
+// the index i*ny + j).
+//
+// One cooperative launch runs the whole solve with two grid barriers per
+// iteration: the direction update v <- w + s v is fused into the next SpMV,
+// which recomputes the updated neighbour values from r and the previous v
+// (double-buffered).  Each barrier is preceded by one block reduction of two
+// values and followed by one parallel load of the per-block partials summed
+// in a fixed tree, so every block derives identical scalars and the solve is
+// deterministic.  The dot products are summed in another order than the
+// reference's serial loops and the updates use fused multiply-adds; on the
+// CPU such perturbations leave the iterates within ~1e-14 of the reference's
+// up to 257x257 and ~1000 iterations.  Data written by other blocks within
+// the launch is read with ld.global.cg (L2), never from a possibly stale L1.
+
+// (a, b) summed over the block; the result is returned to every thread.
+__device__ double2 block_sum2(double a, double b, double* sm /* >= 18 */) {
+  a = warp_sum_d(a);
+  b = warp_sum_d(b);
+  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  if ((threadIdx.x & 31) == 0) {
+    sm[w] = a;
+    sm[8 + w] = b;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0, tb = 0;
+    for (int k = 0; k < nw; k++) {
+      ta += sm[k];
+      tb += sm[8 + k];
+    }
+    sm[16] = ta;
+    sm[17] = tb;
+  }
+  __syncthreads();
+  double2 r = make_double2(sm[16], sm[17]);
+  __syncthreads();
+  return r;
+}
+
+// Grid total of per-block (a, b) partials, identical in every block.
+__device__ double2 grid_total2(const double2* P, int nb, double* sm) {
+  double a = 0, b = 0;
+  for (int k = threadIdx.x; k < nb; k += blockDim.x) {
+    double2 v = __ldcg(&P[k]);
+    a += v.x;
+    b += v.y;
+  }
+  return block_sum2(a, b, sm);
+}
+
 __device__ __forceinline__ double stencil_row(long k, int nx, int ny, const double* v) {
   long row = k / nx, col = k % nx;
   double sum = 0;
-  if (row > 0) sum += v[k - nx];
-  if (col > 0) sum += v[k - 1];
-  sum += -4 * v[k];
-  if (col < nx - 1) sum += v[k + 1];
-  if (row < ny - 1) sum += v[k + nx];
+  if (row > 0) sum += __ldcg(&v[k - nx]);
+  if (col > 0) sum += __ldcg(&v[k - 1]);
+  sum = fma(-4.0, __ldcg(&v[k]), sum);
+  if (col < nx - 1) sum += __ldcg(&v[k + 1]);
+  if (row < ny - 1) sum += __ldcg(&v[k + nx]);
   return sum;
 }
 
 __device__ __forceinline__ double vnext(long k, const double* r, const double* vp, double minv, double s) {
-  double w = minv * r[k];
-  return w + vp[k] * s;
+  return fma(__ldcg(&vp[k]), s, minv * __ldcg(&r[k]));
 }
 
 __device__ __forceinline__ double stencil_next(long k, int nx, int ny, const double* r, const double* vp, double minv,
-                                               double s) {
+                                               double s, double vk) {
   long row = k / nx, col = k % nx;
   double sum = 0;
   if (row > 0) sum += vnext(k - nx, r, vp, minv, s);
   if (col > 0) sum += vnext(k - 1, r, vp, minv, s);
-  sum += -4 * vnext(k, r, vp, minv, s);
+  sum = fma(-4.0, vk, sum);
   if (col < nx - 1) sum += vnext(k + 1, r, vp, minv, s);
   if (row < ny - 1) sum += vnext(k + nx, r, vp, minv, s);
   return sum;
 }
 
 __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
-  __shared__ double sm[40];
+  __shared__ double sm[20];
   const int nx = a.g.nx, ny = a.g.ny;
   const long n = (long)nx * ny;
   const long tid = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -348,7 +394,8 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
   double* b = a.b;
   double* r = a.r;
   double* u = a.u;
-  double* P = a.partials;  // [4][nb]
+  double2* PA = reinterpret_cast<double2*>(a.partials);  // [nb] (v.u, -)
+  double2* PB = PA + nb;                                  // [nb] (w.r, r.r)
   const double minv = 1.0 / -4.0;
   const double dx2 = a.g.dx * a.g.dx;
   // set-up: b (src/field.cpp:234-252), x = 0, r = b - A*0, w = M^-1 r, v = w.
@@ -363,18 +410,14 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
     r[k] = rk;
     double wk = minv * rk;
     a.va[k] = wk;
-    pa += wk * rk;
-    pr += rk * rk;
+    pa = fma(wk, rk, pa);
+    pr = fma(rk, rk, pr);
   }
-  pa = block_sum_256(pa, sm);
-  pr = block_sum_256(pr, sm);
-  if (threadIdx.x == 0) {
-    P[0 * nb + blockIdx.x] = pa;
-    P[1 * nb + blockIdx.x] = pr;
-  }
+  double2 bs = block_sum2(pa, pr, sm);
+  if (threadIdx.x == 0) PB[blockIdx.x] = bs;
   if (!grid_sync(a.bar, a.flags)) return;
-  double alpha = sum_partials(P, nb, 1, 0, sm);
-  double rr = sum_partials(P + nb, nb, 1, 0, sm);
+  double2 tot = grid_total2(PB, nb, sm);
+  double alpha = tot.x, rr = tot.y;
   unsigned int cap32 = (unsigned int)n * (unsigned int)n;
   int maxit = (int)cap32 < a.max_iter ? (int)cap32 : a.max_iter;
   double* vp = a.va;  // direction of the previous iteration
@@ -388,39 +431,36 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
     for (long k = tid; k < n; k += stride) {
       double vk, uk;
       if (it == 0) {
-        vk = vp[k];
+        vk = __ldcg(&vp[k]);
         uk = stencil_row(k, nx, ny, vp);
       } else {
         vk = vnext(k, r, vp, minv, s);
-        uk = stencil_next(k, nx, ny, r, vp, minv, s);
+        uk = stencil_next(k, nx, ny, r, vp, minv, s, vk);
       }
       vc[k] = vk;
       u[k] = uk;
-      pvu += vk * uk;
+      pvu = fma(vk, uk, pvu);
     }
-    pvu = block_sum_256(pvu, sm);
-    if (threadIdx.x == 0) P[2 * nb + blockIdx.x] = pvu;
+    bs = block_sum2(pvu, 0.0, sm);
+    if (threadIdx.x == 0) PA[blockIdx.x] = bs;
     if (!grid_sync(a.bar, a.flags)) return;
-    double t = alpha / sum_partials(P + 2 * nb, nb, 1, 0, sm);
+    double t = alpha / grid_total2(PA, nb, sm).x;
     double pb = 0, prr = 0;
     for (long k = tid; k < n; k += stride) {
-      double xk = x[k] + vc[k] * t;
-      double rk = r[k] - u[k] * t;
+      double xk = fma(vc[k], t, x[k]);
+      double rk = fma(-u[k], t, r[k]);
       x[k] = xk;
       r[k] = rk;
       double wk = minv * rk;
-      pb += wk * rk;
-      prr += rk * rk;
+      pb = fma(wk, rk, pb);
+      prr = fma(rk, rk, prr);
     }
-    pb = block_sum_256(pb, sm);
-    prr = block_sum_256(prr, sm);
-    if (threadIdx.x == 0) {
-      P[0 * nb + blockIdx.x] = pb;
-      P[1 * nb + blockIdx.x] = prr;
-    }
+    bs = block_sum2(pb, prr, sm);
+    if (threadIdx.x == 0) PB[blockIdx.x] = bs;
     if (!grid_sync(a.bar, a.flags)) return;
-    double beta = sum_partials(P, nb, 1, 0, sm);
-    rr = sum_partials(P + nb, nb, 1, 0, sm);
+    tot = grid_total2(PB, nb, sm);
+    double beta = tot.x;
+    rr = tot.y;
     s = beta / alpha;
     alpha = beta;
     double* tmp = vp;
@@ -431,12 +471,12 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
   double pe = 0;
   for (long k = tid; k < n; k += stride) {
     double e = stencil_row(k, nx, ny, x) - b[k];
-    pe += e * e;
+    pe = fma(e, e, pe);
   }
-  pe = block_sum_256(pe, sm);
-  if (threadIdx.x == 0) P[3 * nb + blockIdx.x] = pe;
+  bs = block_sum2(pe, 0.0, sm);
+  if (threadIdx.x == 0) PA[blockIdx.x] = bs;
   if (!grid_sync(a.bar, a.flags)) return;
-  double e2 = sum_partials(P + 3 * nb, nb, 1, 0, sm);
+  double e2 = grid_total2(PA, nb, sm).x;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.info->iterations = it;
     a.info->converged = it < maxit;
@@ -499,9 +539,10 @@ __global__ void __launch_bounds__(256) k_sor_rb(SolverArgs a) {
         int i = 1 + (int)(q / (ny - 2)), j = 1 + (int)(q % (ny - 2));
         if (((i + j) & 1) != color) continue;
         long k = (long)i * ny + j;
-        double phi_new =
-            inv_coeff * (a.rho[k] * a.K + ((phi[k + ny] + phi[k - ny]) / dx2) + ((phi[k + 1] + phi[k - 1]) / dy2));
-        phi[k] = phi[k] + a.omega * (phi_new - phi[k]);
+        double pE = __ldcg(&phi[k + ny]), pW = __ldcg(&phi[k - ny]);
+        double pN = __ldcg(&phi[k + 1]), pS = __ldcg(&phi[k - 1]), pk = __ldcg(&phi[k]);
+        double phi_new = inv_coeff * (a.rho[k] * a.K + ((pE + pW) / dx2) + ((pN + pS) / dy2));
+        phi[k] = pk + a.omega * (phi_new - pk);
       }
       if (!grid_sync(a.bar, a.flags)) return;
     }
@@ -512,8 +553,9 @@ __global__ void __launch_bounds__(256) k_sor_rb(SolverArgs a) {
       for (long q = tid; q < ni; q += stride) {
         int i = 1 + (int)(q / (ny - 2)), j = 1 + (int)(q % (ny - 2));
         long k = (long)i * ny + j;
-        double R = ((phi[k + ny] - 2 * phi[k] + phi[k - ny]) / dx2) + ((phi[k + 1] - 2 * phi[k] + phi[k - 1]) / dy2) +
-                   (a.rho[k]) * a.K;
+        double pE = __ldcg(&phi[k + ny]), pW = __ldcg(&phi[k - ny]);
+        double pN = __ldcg(&phi[k + 1]), pS = __ldcg(&phi[k - 1]), pk = __ldcg(&phi[k]);
+        double R = ((pE - 2 * pk + pW) / dx2) + ((pN - 2 * pk + pS) / dy2) + (a.rho[k]) * a.K;
         sum += R * R;
       }
       sum = block_sum_256(sum, sm);

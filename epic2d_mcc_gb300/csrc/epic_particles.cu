@@ -84,6 +84,15 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int* total, int* sm /
   return warp_prefix + x - v;
 }
 
+// Domain::XtoL / YtoL (src/domain.cpp:257-264).  With a unit cell (dx == 1,
+// the normalisation of norm_scheme 1-4) the division is the identity in IEEE
+// arithmetic, so the UNIT variant drops it without changing a bit; FP64
+// division is costly on GB300.
+template <bool UNIT>
+__device__ __forceinline__ double to_logical(double x, double x0, double dx) {
+  return UNIT ? (x - x0) : (x - x0) / dx;
+}
+
 // Domain::Interpolate (src/domain.cpp:231-255) of both field components from
 // the interleaved (efx, efy) grid; returns false when the stencil leaves the grid.
 template <int SHAPE>
@@ -115,7 +124,7 @@ __device__ __forceinline__ bool gather(const Geom& g, const double2* __restrict_
 // node can overflow): integer addition is associative, so the grid is
 // identical run to run; the weight is applied at finalisation.  Otherwise
 // FP64 atomics add spwt*w into the same accumulator buffer read as doubles.
-template <int SHAPE, bool FIXED>
+template <int SHAPE, bool FIXED, bool UNIT>
 __global__ void __launch_bounds__(PART_THREADS) k_deposit(Geom g, SoA p, const long long* __restrict__ d_n,
                                                           double spwt, double* __restrict__ den,
                                                           unsigned long long* __restrict__ acc, double fx_scale,
@@ -125,8 +134,8 @@ __global__ void __launch_bounds__(PART_THREADS) k_deposit(Geom g, SoA p, const l
   double* facc = reinterpret_cast<double*>(acc);
   bool bad = false;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
-    double lx = (p.x[q] - g.x0) / g.dx;
-    double ly = (p.y[q] - g.y0) / g.dy;
+    double lx = to_logical<UNIT>(p.x[q], g.x0, g.dx);
+    double ly = to_logical<UNIT>(p.y[q], g.y0, g.dy);
     if (SHAPE == EPIC_NGP) {
       int gx = (int)round(lx), gy = (int)round(ly);
       if (gx < 0 || gx >= g.nx || gy < 0 || gy >= g.ny) {
@@ -160,15 +169,20 @@ __global__ void __launch_bounds__(PART_THREADS) k_deposit(Geom g, SoA p, const l
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
 }
 
+static bool unit_cell(const Geom& g) { return g.dx == 1.0 && g.dy == 1.0; }
+
 void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const SoA& p, const long long* d_n,
                     double spwt, double* den, unsigned long long* acc, double fx_scale, int* flags, int grid) {
+#define DEP(SH, FX, U) k_deposit<SH, FX, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, spwt, den, acc, fx_scale, flags)
+  const bool u = unit_cell(g);
   if (shape == EPIC_NGP) {
-    if (fixed) k_deposit<EPIC_NGP, true><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, spwt, den, acc, fx_scale, flags);
-    else k_deposit<EPIC_NGP, false><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, spwt, den, acc, fx_scale, flags);
+    if (fixed) { if (u) DEP(EPIC_NGP, true, true); else DEP(EPIC_NGP, true, false); }
+    else { if (u) DEP(EPIC_NGP, false, true); else DEP(EPIC_NGP, false, false); }
   } else {
-    if (fixed) k_deposit<EPIC_CIC, true><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, spwt, den, acc, fx_scale, flags);
-    else k_deposit<EPIC_CIC, false><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, spwt, den, acc, fx_scale, flags);
+    if (fixed) { if (u) DEP(EPIC_CIC, true, true); else DEP(EPIC_CIC, true, false); }
+    else { if (u) DEP(EPIC_CIC, false, true); else DEP(EPIC_CIC, false, false); }
   }
+#undef DEP
 }
 
 // --------------------------------------------------------------- push ---
@@ -177,11 +191,11 @@ void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const 
 // then the boundary rule.  qmK = (q/m) * (n0*e*L)/(eps0*W*vel_norm) and
 // c = vel_norm/(L*W) come from the host, computed exactly as the reference
 // evaluates the leading factors of its expressions.
-template <int SHAPE, int BC>
+template <int SHAPE, int BC, bool UNIT>
 __device__ __forceinline__ bool push_one(const Geom& g, const double2* __restrict__ ef, double qmK, double c,
                                          double dtsub, double& x, double& y, double& vx, double& vy, bool& bad) {
-  double lx = (x - g.x0) / g.dx;
-  double ly = (y - g.y0) / g.dy;
+  double lx = to_logical<UNIT>(x, g.x0, g.dx);
+  double ly = to_logical<UNIT>(y, g.y0, g.dy);
   double ex, ey;
   if (!gather<SHAPE>(g, ef, lx, ly, ex, ey)) {
     bad = true;
@@ -209,7 +223,7 @@ __device__ __forceinline__ bool push_one(const Geom& g, const double2* __restric
   }
 }
 
-template <int SHAPE, int BC>
+template <int SHAPE, int BC, bool UNIT>
 __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long long* __restrict__ d_n,
                                                        const double2* __restrict__ ef, double qmK, double c,
                                                        double dtsub, int* flags) {
@@ -218,7 +232,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long
   bool bad = false;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
     double x = p.x[q], y = p.y[q], vx = p.vx[q], vy = p.vy[q];
-    push_one<SHAPE, BC>(g, ef, qmK, c, dtsub, x, y, vx, vy, bad);
+    push_one<SHAPE, BC, UNIT>(g, ef, qmK, c, dtsub, x, y, vx, vy, bad);
     p.x[q] = x;
     p.y[q] = y;
     p.vx[q] = vx;
@@ -233,7 +247,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long
 // survivors written in place at (prefix of earlier tiles) + rank.  A tile's
 // writes land only at or below its own range, in slots earlier tiles have
 // already loaded before publishing their counts, so no second buffer is needed.
-template <int SHAPE>
+template <int SHAPE, bool UNIT>
 __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, long long* d_n,
                                                                const double2* __restrict__ ef, double qmK, double c,
                                                                double dtsub, unsigned long long* status,
@@ -259,7 +273,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, lo
       keep[k] = 0;
       if (q < n) {
         x[k] = p.x[q]; y[k] = p.y[q]; vx[k] = p.vx[q]; vy[k] = p.vy[q]; vz[k] = p.vz[q];
-        keep[k] = push_one<SHAPE, EPIC_OPEN>(g, ef, qmK, c, dtsub, x[k], y[k], vx[k], vy[k], bad) ? 1 : 0;
+        keep[k] = push_one<SHAPE, EPIC_OPEN, UNIT>(g, ef, qmK, c, dtsub, x[k], y[k], vx[k], vy[k], bad) ? 1 : 0;
       }
     }
     int rank[ITEMS];
@@ -291,26 +305,29 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, lo
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n, const double2* ef,
                  double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
                  unsigned int* tile_ctr, int grid) {
-#define PUSH(SH, B) k_push<SH, B><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags)
+#define PUSH(SH, B, U) k_push<SH, B, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags)
+#define COMPACT(SH, U) \
+  k_push_compact<SH, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, tile_ctr, flags)
+#define BOTH(M, ...) \
+  do { if (u) M(__VA_ARGS__, true); else M(__VA_ARGS__, false); } while (0)
+  const bool u = unit_cell(g);
   if (bc == EPIC_OPEN) {
-    if (shape == EPIC_NGP)
-      k_push_compact<EPIC_NGP><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, tile_ctr,
-                                                               flags);
-    else
-      k_push_compact<EPIC_CIC><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, tile_ctr,
-                                                               flags);
+    if (shape == EPIC_NGP) BOTH(COMPACT, EPIC_NGP);
+    else BOTH(COMPACT, EPIC_CIC);
   } else if (bc == EPIC_PBC) {
-    if (shape == EPIC_NGP) PUSH(EPIC_NGP, EPIC_PBC);
-    else PUSH(EPIC_CIC, EPIC_PBC);
+    if (shape == EPIC_NGP) BOTH(PUSH, EPIC_NGP, EPIC_PBC);
+    else BOTH(PUSH, EPIC_CIC, EPIC_PBC);
   } else {
-    if (shape == EPIC_NGP) PUSH(EPIC_NGP, EPIC_REFLECTIVE);
-    else PUSH(EPIC_CIC, EPIC_REFLECTIVE);
+    if (shape == EPIC_NGP) BOTH(PUSH, EPIC_NGP, EPIC_REFLECTIVE);
+    else BOTH(PUSH, EPIC_CIC, EPIC_REFLECTIVE);
   }
+#undef BOTH
+#undef COMPACT
 #undef PUSH
 }
 
 // Species::Rewind_species (src/species.cpp:229-246): v -= (0.5*qm*K) * E * DT.
-template <int SHAPE>
+template <int SHAPE, bool UNIT>
 __global__ void __launch_bounds__(PART_THREADS) k_rewind(Geom g, SoA p, const long long* __restrict__ d_n,
                                                          const double2* __restrict__ ef, double hqmK, double dt,
                                                          int* flags) {
@@ -318,8 +335,8 @@ __global__ void __launch_bounds__(PART_THREADS) k_rewind(Geom g, SoA p, const lo
   const long long stride = (long long)gridDim.x * blockDim.x;
   bool bad = false;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
-    double lx = (p.x[q] - g.x0) / g.dx;
-    double ly = (p.y[q] - g.y0) / g.dy;
+    double lx = to_logical<UNIT>(p.x[q], g.x0, g.dx);
+    double ly = to_logical<UNIT>(p.y[q], g.y0, g.dy);
     double ex, ey;
     if (!gather<SHAPE>(g, ef, lx, ly, ex, ey)) {
       bad = true;
@@ -333,8 +350,11 @@ __global__ void __launch_bounds__(PART_THREADS) k_rewind(Geom g, SoA p, const lo
 
 void launch_rewind(cudaStream_t st, const Geom& g, int shape, const SoA& p, const long long* d_n, const double2* ef,
                    double hqmK, double dt, int* flags, int grid) {
-  if (shape == EPIC_NGP) k_rewind<EPIC_NGP><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, hqmK, dt, flags);
-  else k_rewind<EPIC_CIC><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, hqmK, dt, flags);
+#define RW(SH, U) k_rewind<SH, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, hqmK, dt, flags)
+  const bool u = unit_cell(g);
+  if (shape == EPIC_NGP) { if (u) RW(EPIC_NGP, true); else RW(EPIC_NGP, false); }
+  else { if (u) RW(EPIC_CIC, true); else RW(EPIC_CIC, false); }
+#undef RW
 }
 
 // ---------------------------------------------------------------- MCC ---
@@ -410,7 +430,7 @@ __device__ __forceinline__ double sample_vel(D& src, double mass, double temp) {
 }
 
 struct MccParams {
-  double vn, dt_phys, ion_mass, ion_temp, F1, F2, p_null;
+  double vn, dt_phys, ion_mass, ion_temp, F1, F2, p_cut;
   int null_collision;
 };
 
@@ -418,11 +438,20 @@ struct MccParams {
 // (src/collision.cpp:60-207), drawing uniforms from `src` in the reference's
 // order.  Returns 0 (none), 1 elastic, 2 excitation, 3 ionisation; for 3 the
 // secondary electron and the new ion are returned in pe / pi.
+//
+// Every electron first draws u0.  p_cut bounds the collision probability of
+// any electron from above (1 - exp(-nu_max dt), with nu_max >= tot(E)*|v| over
+// the table, plus a relative margin of 1e-9 for rounding), so u0 >= p_cut
+// means "no collision" in the reference's test p_coll > u0 too: such electrons
+// return before their velocity is even read.  In null-collision mode p_cut is
+// the null-collision probability itself and the second draw accepts with
+// nu/nu_max.
 template <class D>
-__device__ int mcc_one(const CrossSections& cs, const MccParams& m, double& vx, double& vy, double& vz, D& src,
-                       double pe[3], double pi[3]) {
+__device__ int mcc_one(const CrossSections& cs, const MccParams& m, const SoA& e, long long q, D& src, double pe[3],
+                       double pi[3]) {
   double u0 = src.next();
-  if (m.null_collision && !(u0 < m.p_null)) return 0;
+  if (!(u0 < m.p_cut)) return 0;
+  double vx = e.vx[q], vy = e.vy[q], vz = e.vz[q];
   double v_sqr = (vx * vx + vy * vy + vz * vz) * m.vn * m.vn;
   double velocity = sqrt(v_sqr);
   double energy = (0.5 * ME * v_sqr) / EV;
@@ -491,9 +520,9 @@ __device__ int mcc_one(const CrossSections& cs, const MccParams& m, double& vx, 
   gx = g * (ct * cc - st * sc * ce);
   gy = g * (st * cp * cc + ct * cp * sc * ce - sp * sc * se);
   gz = g * (st * sp * cc + ct * sp * sc * ce + cp * sc * se);
-  vx = wx + m.F2 * gx;
-  vy = wy + m.F2 * gy;
-  vz = wz + m.F2 * gz;
+  e.vx[q] = wx + m.F2 * gx;
+  e.vy[q] = wy + m.F2 * gy;
+  e.vz[q] = wz + m.F2 * gz;
   return kind;
 }
 
@@ -534,22 +563,16 @@ __global__ void __launch_bounds__(PART_THREADS) k_mcc(CrossSections cs, MccParam
       long long q = base + (long long)k * PART_THREADS + threadIdx.x;
       ionz[k] = 0;
       if (q < ne) {
-        double vx = e.vx[q], vy = e.vy[q], vz = e.vz[q];
         int kind;
         if (MODE == EPIC_MCC_INJECTED) {
           Injected src{uniforms + q * ustride};
-          kind = mcc_one(cs, m, vx, vy, vz, src, pe[k], pi[k]);
+          kind = mcc_one(cs, m, e, q, src, pe[k], pi[k]);
         } else {
           Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)seed, (uint32_t)(seed >> 32), 0,
                      make_uint4(0, 0, 0, 0)};
-          kind = mcc_one(cs, m, vx, vy, vz, src, pe[k], pi[k]);
+          kind = mcc_one(cs, m, e, q, src, pe[k], pi[k]);
         }
-        if (kind) {
-          ncoll++;
-          e.vx[q] = vx;
-          e.vy[q] = vy;
-          e.vz[q] = vz;
-        }
+        if (kind) ncoll++;
         if (kind == 3) {
           ionz[k] = 1;
           px[k] = e.x[q];
@@ -622,7 +645,8 @@ void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const SoA& e
   m.F1 = ME / (ME + ion_mass);
   m.F2 = ion_mass / (ME + ion_mass);
   m.null_collision = mode == EPIC_MCC_NULL;
-  m.p_null = 1 - exp(-cs.nu_max * dt_phys);
+  const double p_null = 1 - exp(-cs.nu_max * dt_phys);
+  m.p_cut = m.null_collision ? p_null : fmin(1.0, p_null * (1 + 1e-9) + 1e-300);
   unsigned long long* pending = d_ncoll + 1;
   if (mode == EPIC_MCC_INJECTED)
     k_mcc<EPIC_MCC_INJECTED><<<grid, PART_THREADS, 0, st>>>(cs, m, e, d_ne, e_cap, ion, d_ni, i_cap, uniforms,
