@@ -196,11 +196,7 @@ SolverArgs solver_args(epic_sim* s) {
   a.info = s->d_info;
   a.iter_total = s->d_iter_total;
   a.flags = s->d_flags;
-  a.b = s->b;
-  a.r = s->r;
-  a.va = s->va;
-  a.vb = s->vb;
-  a.u = s->u;
+  for (int k = 0; k < 8; k++) a.work[k] = s->work[k];
   a.partials = s->partials;
   a.bar = s->bar;
   a.warm = s->cfg.warm_start;
@@ -208,9 +204,13 @@ SolverArgs solver_args(epic_sim* s) {
 }
 
 int solver_blocks(epic_sim* s, long long nodes_per_block) {
-  long long want = (nnodes(s) + nodes_per_block - 1) / nodes_per_block;
   int mx = solver_max_blocks();
-  return (int)std::max(1LL, std::min<long long>(want, mx));
+  if (s->cfg.solver_blocks > 0) return std::min(s->cfg.solver_blocks, mx);
+  // One CTA per SM at most: a sweep over 16..304 CTAs on 65^2..257^2 grids
+  // found the per-iteration time lowest between 130 and 152 CTAs and worse
+  // at two per SM (more barrier arrivals, no more FP64 throughput per SM).
+  long long want = (nnodes(s) + nodes_per_block - 1) / nodes_per_block;
+  return (int)std::max(1LL, std::min<long long>(want, std::min(mx, s->num_sms)));
 }
 
 epic_status do_solve(epic_sim* s) {
@@ -255,20 +255,52 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle) {
   return EPIC_OK;
 }
 
+// Event scratch of the MCC for an electron capacity: marks (-1 = none) for
+// every slot, per-tile counts, and products for up to cap/8 ionisations per
+// call (more raise EPIC_ERR_CAPACITY).  Allocates, so it must run outside
+// stream capture; epic_run calls it before capturing.
+epic_status ensure_mcc_events(epic_sim* s, long long e_cap) {
+  if (s->mcc_ev_for_cap >= e_cap) return EPIC_OK;
+  cudaStreamCaptureStatus cs;
+  if (cudaStreamIsCapturing(s->stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
+    return fail(EPIC_ERR_INVALID, "MCC scratch must be allocated before stream capture");
+  McEvents& ev = s->mcc_ev;
+  cudaFree(ev.buf); cudaFree(ev.count); cudaFree(ev.slot); cudaFree(ev.tile_cnt); cudaFree(ev.tile_off);
+  cudaFree(ev.cand); cudaFree(ev.cand_count);
+  std::memset(&ev, 0, sizeof(ev));
+  s->mcc_ev_for_cap = 0;
+  const size_t tiles = (size_t)(e_cap / MCC_TILE + 2);
+  ev.cap = (unsigned int)std::min<long long>(std::max<long long>(e_cap / 8, 65536), 1LL << 30);
+  CK(cudaMalloc((void**)&ev.buf, (size_t)ev.cap * ion_event_bytes()));
+  CK(cudaMalloc((void**)&ev.cand, (size_t)e_cap * sizeof(unsigned int)));
+  CK(cudaMalloc((void**)&ev.cand_count, sizeof(unsigned int)));
+  CK(cudaMemset(ev.cand_count, 0, sizeof(unsigned int)));
+  CK(cudaMalloc((void**)&ev.count, sizeof(unsigned int)));
+  CK(cudaMalloc((void**)&ev.slot, (size_t)e_cap * sizeof(int)));
+  CK(cudaMalloc((void**)&ev.tile_cnt, tiles * sizeof(unsigned int)));
+  CK(cudaMalloc((void**)&ev.tile_off, tiles * sizeof(unsigned int)));
+  CK(cudaMemset(ev.count, 0, sizeof(unsigned int)));
+  CK(cudaMemset(ev.slot, 0xff, (size_t)e_cap * sizeof(int)));
+  CK(cudaMemset(ev.tile_cnt, 0, tiles * sizeof(unsigned int)));
+  s->mcc_ev_for_cap = e_cap;
+  return EPIC_OK;
+}
+
 epic_status do_mcc(epic_sim* s, int e, int ion, const double* d_uniforms, int ustride) {
   PhaseTimer t(s, 5);
   if (!s->cs.tot) return fail(EPIC_ERR_INVALID, "cross sections not set (epic_set_reference_cross_sections)");
   epic_species_state& E = s->sp[e];
   epic_species_state& I = s->sp[ion];
   const epic_config& c = s->cfg;
-  CK(cudaMemsetAsync(s->tile_ctr, 0, sizeof(unsigned int), s->stream));
-  CK(cudaMemsetAsync(s->tile_status, 0, s->tile_status_len * sizeof(unsigned long long), s->stream));
+  if (s->mcc_ev_for_cap < E.cap) {
+    epic_status st = ensure_mcc_events(s, E.cap);
+    if (st) return st;
+  }
   int mode = c.mcc_mode;
   if (mode == EPIC_MCC_INJECTED && !d_uniforms) mode = EPIC_MCC_PHILOX;
   launch_mcc(s->stream, mode, s->cs, E.soa, E.d_n, E.cap, I.soa, I.d_n, I.cap, c.vel_norm, c.DT / c.W, I.desc.mass,
-             I.desc.temp, d_uniforms, ustride, c.seed, s->d_step, s->tile_status, s->tile_ctr, s->d_ncoll,
-             s->d_flags, s->part_grid);
-  s->launches += 2;
+             I.desc.temp, d_uniforms, ustride, c.seed, s->d_step, s->mcc_ev, s->d_ncoll, s->d_flags, s->part_grid);
+  s->launches += 5;
   CKL();
   return EPIC_OK;
 }
@@ -358,11 +390,7 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   guard(dalloc(&s->efx, nn));
   guard(dalloc(&s->efy, nn));
   guard(dalloc(&s->ef, nn));
-  guard(dalloc(&s->b, nn));
-  guard(dalloc(&s->r, nn));
-  guard(dalloc(&s->va, nn));
-  guard(dalloc(&s->vb, nn));
-  guard(dalloc(&s->u, nn));
+  for (int k = 0; k < 8; k++) guard(dalloc(&s->work[k], nn));
   guard(dalloc(&s->partials, 4 * (size_t)std::max(solver_max_blocks(), 256)));
   guard(dalloc(&s->bar, 2));
   guard(dalloc(&s->d_info, 1));
@@ -395,7 +423,15 @@ void epic_destroy(epic_sim* s) {
     cudaEventDestroy(pe.second.second);
   }
   for (auto e : s->event_pool) cudaEventDestroy(e);
-  void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->b, s->r, s->va, s->vb, s->u, s->partials, s->bar,
+  cudaFree(s->mcc_ev.buf);
+  cudaFree(s->mcc_ev.count);
+  cudaFree(s->mcc_ev.slot);
+  cudaFree(s->mcc_ev.tile_cnt);
+  cudaFree(s->mcc_ev.tile_off);
+  cudaFree(s->mcc_ev.cand);
+  cudaFree(s->mcc_ev.cand_count);
+  for (int k = 0; k < 8; k++) cudaFree(s->work[k]);
+  void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->partials, s->bar,
                   s->d_info, s->d_iter_total, s->tile_ctr, s->d_ncoll, s->d_step, s->sum_partials, s->d_sums, s->d_flags,
                   s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion};
   for (void* p : ptrs)
@@ -686,13 +722,20 @@ epic_status epic_run(epic_sim* s, int steps, int with_collisions, int use_graph)
   if (!s->graph_exec || s->graph_collisions != with_collisions) {
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     s->graph_exec = nullptr;
+    if (with_collisions && s->sp.size() >= 2)
+      if ((st = ensure_mcc_events(s, s->sp[0].cap))) return st;
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     int64_t before = s->launches;
     st = do_step(s, with_collisions);
     cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
-    if (st) return st;
-    if (ce != cudaSuccess) return fail(EPIC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    if (st || ce != cudaSuccess) {
+      cudaGetLastError();  // a failed capture leaves its error pending; do not leak it to later calls
+      if (ce == cudaSuccess) cudaGraphDestroy(graph);
+      s->launches = before;
+      if (st) return st;
+      return fail(EPIC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    }
     s->graph_launches = s->launches - before;
     s->launches = before;
     ce = cudaGraphInstantiate(&s->graph_exec, graph, 0);

@@ -84,13 +84,30 @@ void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p
                  unsigned int* tile_ctr, int grid);
 void launch_rewind(cudaStream_t st, const Geom& g, int shape, const SoA& p, const long long* d_n, const double2* ef,
                    double hqmK, double dt, int* flags, int grid);
+// Ionisation events of one MCC launch: products in `buf` (count, cap), the
+// event index of each marked electron in `slot` (-1 otherwise; capacity of the
+// electron species) and the number of events per tile of MCC_TILE electrons
+// in tile_cnt, scanned into tile_off.  All of it is returned to the cleared
+// state (slot -1, counts 0) by the launch itself.
+constexpr int MCC_TILE = 512;
+struct IonEvent;
+struct McEvents {
+  IonEvent* buf;
+  unsigned int* count;
+  unsigned int cap;
+  int* slot;
+  unsigned int* tile_cnt;
+  unsigned int* tile_off;
+  unsigned int* cand;        // electrons whose first draw passed the cut (any order)
+  unsigned int* cand_count;
+};
 // d_step: device step counter (Philox counter word), advanced by every MCC
 // launch so replayed graphs draw fresh numbers.
 void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const SoA& e, long long* d_ne, long long e_cap,
                 const SoA& ion, long long* d_ni, long long i_cap, double vel_norm, double dt_phys, double ion_mass,
                 double ion_temp, const double* uniforms, int ustride, uint64_t seed, unsigned long long* d_step,
-                unsigned long long* tile_status, unsigned int* tile_ctr, unsigned long long* d_ncoll, int* flags,
-                int grid);
+                const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid);
+size_t ion_event_bytes();
 void launch_particle_sums(cudaStream_t st, int what, const SoA& p, const long long* d_n, double vel_norm,
                           double* partials, double* out3, int grid);
 
@@ -128,8 +145,8 @@ struct SolverArgs {
   SolveInfo* info;
   unsigned long long* iter_total;  // running sum of iterations (profiling)
   int* flags;
-  // PCG / red-black workspace
-  double *b, *r, *va, *vb, *u;
+  // PCG workspace: 8 node vectors (b, r x2, s x2, w x2, p)
+  double* work[8];
   double* partials;  // 4 * max_blocks
   unsigned int* bar; // grid barrier {count, generation}
   int warm;
@@ -167,7 +184,8 @@ struct epic_sim {
   double *phi, *rho, *efx, *efy;
   double2* ef;
   // solver workspace
-  double *b, *r, *va, *vb, *u, *partials;
+  double* work[8];
+  double* partials;
   unsigned int* bar;
   epic::SolveInfo* d_info;
   unsigned long long* d_iter_total;
@@ -177,6 +195,8 @@ struct epic_sim {
   unsigned int* tile_ctr;
   unsigned long long* d_ncoll;  // [0] collisions of the last MCC, [1..2] pending appends/collisions
   unsigned long long* d_step;   // MCC launches so far (Philox counter)
+  epic::McEvents mcc_ev;        // ionisation event scratch (allocated on first MCC)
+  long long mcc_ev_for_cap;     // electron capacity the scratch was sized for
   void* staging;                // AoS staging for uploads/downloads
   size_t staging_bytes;
   double* d_uniforms;

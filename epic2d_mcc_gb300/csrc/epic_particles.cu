@@ -375,13 +375,14 @@ struct Philox {
     }
     return c;
   }
-  __device__ double next() {
+  // The k-th draw as a 53-bit integer M; the uniform is M * 2^-53 in [0, 1).
+  __device__ unsigned long long next53() {
     if ((k & 1) == 0) cur = round10(make_uint4(c0, c1, c2, (uint32_t)(k >> 1)), key0, key1);
     uint32_t a = (k & 1) ? cur.z : cur.x, b = (k & 1) ? cur.w : cur.y;
     k++;
-    // 53-bit uniform in [0, 1) from two 32-bit words.
-    return ((double)(a >> 5) * 67108864.0 + (double)(b >> 6)) * (1.0 / 9007199254740992.0);
+    return ((unsigned long long)(a >> 5) << 26) | (b >> 6);
   }
+  __device__ double next() { return (double)next53() * (1.0 / 9007199254740992.0); }
 };
 
 struct Injected {
@@ -431,26 +432,33 @@ __device__ __forceinline__ double sample_vel(D& src, double mass, double temp) {
 
 struct MccParams {
   double vn, dt_phys, ion_mass, ion_temp, F1, F2, p_cut;
+  unsigned long long cut53;  // ceil(p_cut * 2^53): u < p_cut  <=>  M < cut53 for u = M * 2^-53
   int null_collision;
 };
 
+// Products of one ionisation: the secondary electron and the new ion at the
+// primary's position.
+struct IonEvent {
+  double x, y, ev[3], iv[3];
+};
+
 // CollisionHandler::handle_collisions for one electron plus collision_electron
-// (src/collision.cpp:60-207), drawing uniforms from `src` in the reference's
-// order.  Returns 0 (none), 1 elastic, 2 excitation, 3 ionisation; for 3 the
-// secondary electron and the new ion are returned in pe / pi.
+// (src/collision.cpp:60-207), after its first draw u0 passed the early-out
+// below; later draws come from `src` in the reference's order.  Returns 0
+// (none), 1 elastic, 2 excitation, 3 ionisation (products in evt).
 //
-// Every electron first draws u0.  p_cut bounds the collision probability of
-// any electron from above (1 - exp(-nu_max dt), with nu_max >= tot(E)*|v| over
-// the table, plus a relative margin of 1e-9 for rounding), so u0 >= p_cut
-// means "no collision" in the reference's test p_coll > u0 too: such electrons
-// return before their velocity is even read.  In null-collision mode p_cut is
-// the null-collision probability itself and the second draw accepts with
-// nu/nu_max.
+// Early-out: p_cut bounds the collision probability of every electron from
+// above (1 - exp(-nu_max dt), nu_max >= tot(E)*|v| over the table, plus a
+// relative margin of 1e-9 for rounding), so u0 >= p_cut means "no collision"
+// in the reference's test p_coll > u0 too, and such electrons are rejected
+// before their velocity is read.  With Philox the test is an integer compare
+// of the draw's 53-bit mantissa.  In null-collision mode p_cut is the
+// null-collision probability itself and a second draw accepts with nu/nu_max.
 template <class D>
-__device__ int mcc_one(const CrossSections& cs, const MccParams& m, const SoA& e, long long q, D& src, double pe[3],
-                       double pi[3]) {
-  double u0 = src.next();
-  if (!(u0 < m.p_cut)) return 0;
+__device__ int mcc_collide(const CrossSections& cs, const MccParams& m, const SoA& e, long long q, D& src, double u0,
+                           IonEvent& evt) {
+  double* pe = evt.ev;
+  double* pi = evt.iv;
   double vx = e.vx[q], vy = e.vy[q], vz = e.vz[q];
   double v_sqr = (vx * vx + vy * vy + vz * vz) * m.vn * m.vn;
   double velocity = sqrt(v_sqr);
@@ -515,6 +523,8 @@ __device__ int mcc_one(const CrossSections& cs, const MccParams& m, const SoA& e
     pi[2] = sample_vel(src, m.ion_mass, m.ion_temp);
     pi[1] = sample_vel(src, m.ion_mass, m.ion_temp);
     pi[0] = sample_vel(src, m.ion_mass, m.ion_temp);
+    evt.x = e.x[q];
+    evt.y = e.y[q];
   }
   double sc = sin(chi), cc = cos(chi), se = sin(eta), ce = cos(eta);
   gx = g * (ct * cc - st * sc * ce);
@@ -526,97 +536,175 @@ __device__ int mcc_one(const CrossSections& cs, const MccParams& m, const SoA& e
   return kind;
 }
 
-// One ordered pass over the electrons: collide, then append ionisation
-// products in electron order at [n_e + prefix + rank] / [n_i + prefix + rank]
-// (the reference appends in loop order, src/collision.cpp:163-164).  The new
-// counts go to pending[] and are committed by k_mcc_commit, so no block of
-// this launch ever sees the grown count.
+// Pass 1a: every electron draws u0 (no ordering, fixed grid); the few below
+// the cut are appended, in any order, to a candidate list.  Compacting them
+// first keeps whole warps on the FP64 collision path instead of one lane in
+// 32 (divergent FP64 work costs full warp throughput).
 template <int MODE>
-__global__ void __launch_bounds__(PART_THREADS) k_mcc(CrossSections cs, MccParams m, SoA e, const long long* d_ne,
-                                                      long long e_cap, SoA ion, const long long* d_ni,
-                                                      long long i_cap, const double* __restrict__ uniforms,
-                                                      int ustride, uint64_t seed,
-                                                      const unsigned long long* __restrict__ d_step,
-                                                      unsigned long long* status, unsigned int* tile_ctr,
-                                                      unsigned long long* pending, int* flags) {
-  constexpr int ITEMS = SCAN_TILE / PART_THREADS;
-  __shared__ int sm[40];
-  __shared__ unsigned long long s_prefix;
-  __shared__ int s_tile;
-  __shared__ unsigned long long s_coll;
-  const long long ne = *d_ne, ni = *d_ni;
+__global__ void __launch_bounds__(PART_THREADS) k_mcc_select(MccParams m, const long long* __restrict__ d_ne,
+                                                             const double* __restrict__ uniforms, int ustride,
+                                                             uint64_t seed, const unsigned long long* __restrict__ d_step,
+                                                             McEvents ev) {
+  const long long ne = *d_ne;
   const unsigned long long step = *d_step;
-  const int num_tiles = (int)((ne + SCAN_TILE - 1) / SCAN_TILE);
-  if (threadIdx.x == 0) s_coll = 0;
-  for (;;) {
-    if (threadIdx.x == 0) s_tile = (int)atomicAdd(tile_ctr, 1u);
-    __syncthreads();
-    const int tile = s_tile;
-    if (tile >= num_tiles) break;
-    const long long base = (long long)tile * SCAN_TILE;
-    int ionz[ITEMS];
-    double pe[ITEMS][3], pi[ITEMS][3];
-    double px[ITEMS], py[ITEMS];
-    int ncoll = 0;
-#pragma unroll
-    for (int k = 0; k < ITEMS; k++) {
-      long long q = base + (long long)k * PART_THREADS + threadIdx.x;
-      ionz[k] = 0;
-      if (q < ne) {
-        int kind;
-        if (MODE == EPIC_MCC_INJECTED) {
-          Injected src{uniforms + q * ustride};
-          kind = mcc_one(cs, m, e, q, src, pe[k], pi[k]);
-        } else {
-          Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)seed, (uint32_t)(seed >> 32), 0,
-                     make_uint4(0, 0, 0, 0)};
-          kind = mcc_one(cs, m, e, q, src, pe[k], pi[k]);
-        }
-        if (kind) ncoll++;
-        if (kind == 3) {
-          ionz[k] = 1;
-          px[k] = e.x[q];
-          py[k] = e.y[q];
-        }
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const long long nround = (ne + stride - 1) / stride;
+  for (long long rd = 0; rd < nround; rd++) {
+    const long long q = rd * stride + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool cand = false;
+    if (q < ne) {
+      if (MODE == EPIC_MCC_INJECTED) {
+        cand = __ldg(&uniforms[q * ustride]) < m.p_cut;
+      } else {
+        Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)seed, (uint32_t)(seed >> 32), 0,
+                   make_uint4(0, 0, 0, 0)};
+        cand = src.next53() < m.cut53;
       }
     }
-    if (ncoll) atomicAdd(&s_coll, (unsigned long long)ncoll);
-    int rank[ITEMS];
-    int tile_total = 0;
-#pragma unroll
-    for (int k = 0; k < ITEMS; k++) {
-      int row_total;
-      rank[k] = tile_total + block_exclusive_scan(ionz[k], &row_total, sm);
-      tile_total += row_total;
+    const unsigned int mask = __ballot_sync(0xffffffffu, cand);
+    if (mask) {
+      unsigned int base = 0;
+      if (lane == __ffs(mask) - 1) base = atomicAdd(ev.cand_count, (unsigned int)__popc(mask));
+      base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+      if (cand) ev.cand[base + __popc(mask & ((1u << lane) - 1))] = (unsigned int)q;
     }
-    if (threadIdx.x == 0) s_prefix = tile_lookback(status, tile, (unsigned long long)tile_total, flags);
-    __syncthreads();
-    const unsigned long long prefix = s_prefix;
-    if (prefix != ~0ull) {
-#pragma unroll
-      for (int k = 0; k < ITEMS; k++) {
-        if (ionz[k]) {
-          long long oe = ne + (long long)prefix + rank[k];
-          long long oi = ni + (long long)prefix + rank[k];
-          if (oe >= e_cap || oi >= i_cap) {
-            set_flag(flags, FLAG_CAPACITY);
-            continue;
-          }
-          e.x[oe] = px[k]; e.y[oe] = py[k]; e.vx[oe] = pe[k][0]; e.vy[oe] = pe[k][1]; e.vz[oe] = pe[k][2];
-          ion.x[oi] = px[k]; ion.y[oi] = py[k]; ion.vx[oi] = pi[k][0]; ion.vy[oi] = pi[k][1]; ion.vz[oi] = pi[k][2];
-        }
-      }
-      if (tile == num_tiles - 1 && threadIdx.x == 0) pending[0] = prefix + tile_total;
-    }
-    __syncthreads();
   }
+}
+
+// Pass 1b: the candidates, whole warps at a time.  Each redraws u0 from the
+// same stream position and runs the collision; an ionisation stores its
+// products in the event buffer and marks the electron (slot) and its tile of
+// MCC_TILE electrons (tile_cnt).
+template <int MODE>
+__global__ void __launch_bounds__(PART_THREADS) k_mcc_collide(CrossSections cs, MccParams m, SoA e,
+                                                              const double* __restrict__ uniforms, int ustride,
+                                                              uint64_t seed,
+                                                              const unsigned long long* __restrict__ d_step,
+                                                              McEvents ev, unsigned long long* pending, int* flags) {
+  __shared__ unsigned long long s_coll;
+  if (threadIdx.x == 0) s_coll = 0;
+  __syncthreads();
+  const unsigned int nc = *ev.cand_count;
+  const unsigned long long step = *d_step;
+  unsigned int ncoll = 0;
+  for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const long long q = ev.cand[c];
+    IonEvent evt;
+    int kind;
+    if (MODE == EPIC_MCC_INJECTED) {
+      Injected src{uniforms + q * ustride};
+      double u0 = src.next();
+      kind = mcc_collide(cs, m, e, q, src, u0, evt);
+    } else {
+      Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)seed, (uint32_t)(seed >> 32), 0,
+                 make_uint4(0, 0, 0, 0)};
+      unsigned long long M = src.next53();
+      kind = mcc_collide(cs, m, e, q, src, (double)M * (1.0 / 9007199254740992.0), evt);
+    }
+    ncoll += kind != 0;
+    if (kind == 3) {
+      unsigned int slot = atomicAdd(ev.count, 1u);
+      if (slot < ev.cap) {
+        ev.buf[slot] = evt;
+        ev.slot[q] = (int)slot;
+        atomicAdd(&ev.tile_cnt[q / MCC_TILE], 1u);
+      } else {
+        set_flag(flags, FLAG_CAPACITY);
+      }
+    }
+  }
+  if (ncoll) atomicAdd(&s_coll, (unsigned long long)ncoll);
   __syncthreads();
   if (threadIdx.x == 0 && s_coll) atomicAdd(&pending[1], s_coll);
 }
 
+// Pass 2 (one block): exclusive scan of the per-tile event counts.
+__global__ void __launch_bounds__(1024) k_mcc_scan(const long long* __restrict__ d_ne, McEvents ev,
+                                                   unsigned long long* pending) {
+  __shared__ unsigned int warp_tot[32];
+  __shared__ unsigned int carry;
+  const long long ne = *d_ne;
+  const int tiles = (int)((ne + MCC_TILE - 1) / MCC_TILE);
+  if (threadIdx.x == 0) carry = 0;
+  __syncthreads();
+  for (int base = 0; base < tiles; base += blockDim.x) {
+    const int t = base + threadIdx.x;
+    unsigned int v = t < tiles ? ev.tile_cnt[t] : 0u, x = v;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) warp_tot[w] = x;
+    __syncthreads();
+    if (w == 0) {
+      unsigned int y = warp_tot[lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        unsigned int z = __shfl_up_sync(0xffffffffu, y, o);
+        if (lane >= o) y += z;
+      }
+      warp_tot[lane] = y;
+    }
+    __syncthreads();
+    const unsigned int excl = carry + (w ? warp_tot[w - 1] : 0u) + x - v;
+    if (t < tiles) ev.tile_off[t] = excl;
+    __syncthreads();
+    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) pending[0] = carry;
+}
+
+// Pass 3: tiles that had events append their products in electron order at
+// [n_e + tile offset + rank] / [n_i + ...] (the reference appends in loop
+// order, src/collision.cpp:163-164), then clear their marks.
+__global__ void __launch_bounds__(PART_THREADS) k_mcc_append(SoA e, const long long* __restrict__ d_ne,
+                                                             long long e_cap, SoA ion,
+                                                             const long long* __restrict__ d_ni, long long i_cap,
+                                                             McEvents ev, int* flags) {
+  constexpr int ITEMS = MCC_TILE / PART_THREADS;
+  __shared__ int sm[40];
+  const long long ne = *d_ne, ni = *d_ni;
+  const int tiles = (int)((ne + MCC_TILE - 1) / MCC_TILE);
+  for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
+    if (ev.tile_cnt[t] == 0) continue;  // block-uniform
+    const long long base = (long long)t * MCC_TILE;
+    int slot[ITEMS], flag[ITEMS];
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+      const long long q = base + k * PART_THREADS + threadIdx.x;
+      slot[k] = q < ne ? ev.slot[q] : -1;
+      flag[k] = slot[k] >= 0;
+    }
+    int run = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+      int row_total;
+      const int rank = run + block_exclusive_scan(flag[k], &row_total, sm);
+      run += row_total;
+      if (flag[k]) {
+        const IonEvent v = ev.buf[slot[k]];
+        const long long oe = ne + ev.tile_off[t] + rank, oi = ni + ev.tile_off[t] + rank;
+        if (oe < e_cap && oi < i_cap) {
+          e.x[oe] = v.x; e.y[oe] = v.y; e.vx[oe] = v.ev[0]; e.vy[oe] = v.ev[1]; e.vz[oe] = v.ev[2];
+          ion.x[oi] = v.x; ion.y[oi] = v.y; ion.vx[oi] = v.iv[0]; ion.vy[oi] = v.iv[1]; ion.vz[oi] = v.iv[2];
+        } else {
+          set_flag(flags, FLAG_CAPACITY);
+        }
+        ev.slot[base + k * PART_THREADS + threadIdx.x] = -1;
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) ev.tile_cnt[t] = 0;
+  }
+}
+
 __global__ void k_mcc_commit(long long* d_ne, long long e_cap, long long* d_ni, long long i_cap,
                              unsigned long long* pending, unsigned long long* ncoll_out,
-                             unsigned long long* d_step, int* flags) {
+                             unsigned long long* d_step, McEvents ev, int* flags) {
   long long add = (long long)pending[0];
   long long ne = *d_ne + add, ni = *d_ni + add;
   if (ne > e_cap || ni > i_cap) {
@@ -629,14 +717,17 @@ __global__ void k_mcc_commit(long long* d_ne, long long e_cap, long long* d_ni, 
   *ncoll_out = pending[1];
   pending[0] = 0;
   pending[1] = 0;
+  *ev.count = 0;
+  *ev.cand_count = 0;
   *d_step += 1;
 }
+
+size_t ion_event_bytes() { return sizeof(IonEvent); }
 
 void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const SoA& e, long long* d_ne, long long e_cap,
                 const SoA& ion, long long* d_ni, long long i_cap, double vel_norm, double dt_phys, double ion_mass,
                 double ion_temp, const double* uniforms, int ustride, uint64_t seed, unsigned long long* d_step,
-                unsigned long long* tile_status, unsigned int* tile_ctr, unsigned long long* d_ncoll, int* flags,
-                int grid) {
+                const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid) {
   MccParams m;
   m.vn = vel_norm;
   m.dt_phys = dt_phys;
@@ -647,15 +738,20 @@ void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const SoA& e
   m.null_collision = mode == EPIC_MCC_NULL;
   const double p_null = 1 - exp(-cs.nu_max * dt_phys);
   m.p_cut = m.null_collision ? p_null : fmin(1.0, p_null * (1 + 1e-9) + 1e-300);
+  m.cut53 = (unsigned long long)ceil(m.p_cut * 9007199254740992.0);
   unsigned long long* pending = d_ncoll + 1;
-  if (mode == EPIC_MCC_INJECTED)
-    k_mcc<EPIC_MCC_INJECTED><<<grid, PART_THREADS, 0, st>>>(cs, m, e, d_ne, e_cap, ion, d_ni, i_cap, uniforms,
-                                                             ustride, seed, d_step, tile_status, tile_ctr, pending,
-                                                             flags);
-  else
-    k_mcc<EPIC_MCC_PHILOX><<<grid, PART_THREADS, 0, st>>>(cs, m, e, d_ne, e_cap, ion, d_ni, i_cap, uniforms, ustride,
-                                                           seed, d_step, tile_status, tile_ctr, pending, flags);
-  k_mcc_commit<<<1, 1, 0, st>>>(d_ne, e_cap, d_ni, i_cap, pending, d_ncoll, d_step, flags);
+  if (mode == EPIC_MCC_INJECTED) {
+    k_mcc_select<EPIC_MCC_INJECTED><<<grid, PART_THREADS, 0, st>>>(m, d_ne, uniforms, ustride, seed, d_step, ev);
+    k_mcc_collide<EPIC_MCC_INJECTED><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
+                                                                     pending, flags);
+  } else {
+    k_mcc_select<EPIC_MCC_PHILOX><<<grid, PART_THREADS, 0, st>>>(m, d_ne, uniforms, ustride, seed, d_step, ev);
+    k_mcc_collide<EPIC_MCC_PHILOX><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
+                                                                   pending, flags);
+  }
+  k_mcc_scan<<<1, 1024, 0, st>>>(d_ne, ev, pending);
+  k_mcc_append<<<grid, PART_THREADS, 0, st>>>(e, d_ne, e_cap, ion, d_ni, i_cap, ev, flags);
+  k_mcc_commit<<<1, 1, 0, st>>>(d_ne, e_cap, d_ni, i_cap, pending, d_ncoll, d_step, ev, flags);
 }
 
 // -------------------------------------------------------- reductions ---

@@ -99,8 +99,10 @@ def deck(name: str) -> str:
         return _TEMPLATE.format(num_ts=1000, dt=0.01, n=n, solver="gs", tol="1e-8", maxit=200000,
                                 solver_extra="sor_omega = 1.8\n", bc="pbc", coll="false", gas="1e20",
                                 species="\n".join(sp))
-    if name == "beam_mcc_256":
-        n, ppc = 256, 100
+    if name in ("beam_mcc_256", "beam_mcc_160"):
+        # beam_mcc_160 is the same plasma on 160x160 cells (5.1 M particles,
+        # 205 MB: still larger than L2) for profiler captures.
+        n, ppc = (256, 100) if name == "beam_mcc_256" else (160, 100)
         total_e = n * n * ppc
         beam = total_e // 10
         # fract_den is relative to the first species: 0.1/0.9 of the bulk.

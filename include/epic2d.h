@@ -75,7 +75,8 @@ typedef struct {
   int mcc_mode;               /* EPIC_MCC_PHILOX: the reference's direct MCC on a Philox stream */
   uint64_t seed;              /* Philox key */
   int warm_start;             /* 0: cold-start solves as the reference */
-  int reserved[16];
+  int solver_blocks;          /* CTAs of the grid-wide solvers; 0 = automatic */
+  int reserved[15];
 } epic_config;
 
 /* One [species] line of input.ini (src/main.cpp:132-149) after set-up. */
