@@ -293,6 +293,53 @@ def run_ours(args, rank, world):
     el = max_over_ranks(el)
     e2e_value = sum_over_ranks(sum(counts) * e2e_steps) / el
 
+    # The mixed-precision form on the same workload from the same start (the
+    # FP64 run above advanced warmup + steps + e2e steps; compare at equal steps).
+    mixed = None
+    if not args.no_mixed:
+        total_steps = args.warmup + args.steps + e2e_steps
+        ref = E.Simulation.from_ini(ini)
+        mx = E.Simulation.from_ini(ini, precision=1)
+        for s_ in (ref, mx):
+            if coll:
+                s_.set_log_cross_sections(ela, exc, ion, e[0], e[-1])
+            s_.load_particles(0)
+            s_.initial_field()
+        del sim
+        for _ in range(args.warmup):
+            mx.run(1, collisions=coll, graph=False)
+        mstream = torch.cuda.ExternalStream(mx.stream)
+        mx.set_profiling(True)
+        mx.profile()
+        m0 = torch.cuda.Event(enable_timing=True)
+        m1 = torch.cuda.Event(enable_timing=True)
+        nb = sum(mx.num_particles(s_) for s_ in range(nsp))
+        m0.record(mstream)
+        mx.run(args.steps, collisions=coll, graph=False)
+        m1.record(mstream)
+        m1.synchronize()
+        mms = max_over_ranks(m0.elapsed_time(m1))
+        mprof, miters = mx.profile()
+        mx.set_profiling(False)
+        na = sum(mx.num_particles(s_) for s_ in range(nsp))
+        mvalue = sum_over_ranks(0.5 * (nb + na) * args.steps) / (mms / 1e3)
+        ref.run(args.warmup + args.steps, collisions=coll, graph=False)
+
+        def energy(sm):
+            return sum(sm.compute_ke(k, 0).sum() for k in range(nsp)) + sm.compute_pe(0)
+
+        e_ref, e_mx = energy(ref), energy(mx)
+        phi_ref = ref.grid("phi")
+        mixed = {"value": mvalue, "unit": UNIT, "ms_per_step": mms / args.steps,
+                 "speedup_vs_fp64": mvalue / value, "dtype": "f32 particles/inner solve + f64 refinement",
+                 "phases_ms_per_step": {k: v[0] / args.steps for k, v in mprof.items()},
+                 "solver_refinements_per_step": miters / args.steps,
+                 "after_steps": args.warmup + args.steps,
+                 "total_energy_rel_err_vs_fp64": abs(e_mx - e_ref) / abs(e_ref),
+                 "phi_rel_err_vs_fp64": float(np.max(np.abs(mx.grid("phi") - phi_ref)) / np.max(np.abs(phi_ref)))}
+        ref.close()
+        mx.close()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, done, n, kind = cpu_port_run(ini, None, 0, budget_s=args.cpu_seconds)
@@ -311,7 +358,8 @@ def run_ours(args, rank, world):
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                         "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
-                "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk}
+                "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
+                "mixed_precision": mixed}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -332,6 +380,7 @@ def main():
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision measurement")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

@@ -46,7 +46,7 @@ class Config(ctypes.Structure):
                 ("elastic", ctypes.c_int), ("excitation", ctypes.c_int), ("ionization", ctypes.c_int),
                 ("sor_omega", ctypes.c_double), ("sor_mode", ctypes.c_int), ("deposit_mode", ctypes.c_int),
                 ("mcc_mode", ctypes.c_int), ("seed", ctypes.c_uint64), ("warm_start", ctypes.c_int),
-                ("solver_blocks", ctypes.c_int), ("reserved", ctypes.c_int * 15)]
+                ("solver_blocks", ctypes.c_int), ("precision", ctypes.c_int), ("reserved", ctypes.c_int * 14)]
 
 
 class SpeciesDesc(ctypes.Structure):

@@ -19,8 +19,8 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libepic2d_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_FP64 = ["epic_particles.cu", "epic_field.cu", "epic_capi.cu"]
-CU_FAST = ["epic_mixed.cu"]
+CU_FP64 = ["epic_particles.cu", "epic_field.cu", "epic_mcc.cu", "epic_capi.cu"]
+CU_FAST = ["epic_mixed.cu", "epic_spectral.cu"]
 CPP = ["epic_host.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -96,7 +96,24 @@ def build(force: bool = False, verbose: bool = False) -> str:
         f.write("\n".join(logs))
     if verbose:
         print("\n".join(logs))
+    build_driver()
     return LIB
+
+
+DRIVER = os.path.join(HERE, "epic2d")
+
+
+def build_driver() -> str:
+    """The `epic2d` command-line driver (host/main.cpp) over the C++ mirror of
+    the reference classes (host/epic2d.hpp), linked to the library."""
+    src = os.path.join(HERE, "host", "main.cpp")
+    hdr = os.path.join(HERE, "host", "epic2d.hpp")
+    if os.path.exists(DRIVER) and all(os.path.getmtime(DRIVER) >= os.path.getmtime(p) for p in (src, hdr, LIB)):
+        return DRIVER
+    tmp = DRIVER + ".tmp%d" % os.getpid()
+    _run(["g++", "-O2", "-std=c++17", "-I", INCLUDE, "-o", tmp, src, LIB, "-Wl,-rpath,$ORIGIN"])
+    os.replace(tmp, DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":

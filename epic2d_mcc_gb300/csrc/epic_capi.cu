@@ -94,6 +94,49 @@ epic_status ensure_staging(epic_sim* s, size_t bytes) {
   return EPIC_OK;
 }
 
+void free_species(epic_species_state& sp) {
+  void* ptrs[] = {sp.soa.x, sp.soa.y, sp.soa.vx, sp.soa.vy, sp.soa.vz, sp.mx.cell, sp.mx.ox, sp.mx.oy,
+                  sp.mx.vx, sp.mx.vy, sp.mx.vz, sp.d_n, sp.den, sp.acc};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+// Refinement stages of the mixed-precision Poisson solve (each gains ~6
+// digits; the loop stops on the reference's tolerance, usually after 2-3).
+constexpr int SPECTRAL_STAGES = 6;
+
+// Sine transform and inverse eigenvalues of the reference operator for the
+// mixed-precision solve: computed in FP64 on the host, stored in FP32.
+epic_status setup_spectral(epic_sim* s) {
+  SpectralSolver& sp = s->spec;
+  const bool gs = s->cfg.solver == EPIC_SOLVER_GS;
+  sp.n = gs ? s->cfg.nx - 2 : s->cfg.nx;
+  sp.off = gs ? 1 : 0;
+  sp.gs_norm = gs;
+  const int n = sp.n;
+  std::vector<float> Q((size_t)n * n), D((size_t)n * n);
+  std::vector<double> lam(n);
+  const double pi = 3.14159265358979323846;
+  const double c = std::sqrt(2.0 / (n + 1));
+  for (int j = 0; j < n; j++) {
+    for (int k = 0; k < n; k++) Q[(size_t)j * n + k] = (float)(c * std::sin(pi * (j + 1) * (double)(k + 1) / (n + 1)));
+    const double sn = std::sin(pi * (j + 1) / (2.0 * (n + 1)));
+    lam[j] = -4.0 * sn * sn;
+  }
+  for (int p = 0; p < n; p++)
+    for (int q = 0; q < n; q++) D[(size_t)p * n + q] = (float)(1.0 / (lam[p] + lam[q]));
+  CK(cudaMalloc((void**)&sp.Q, Q.size() * sizeof(float)));
+  CK(cudaMalloc((void**)&sp.D, D.size() * sizeof(float)));
+  CK(cudaMalloc((void**)&sp.t0, Q.size() * sizeof(float)));
+  CK(cudaMalloc((void**)&sp.t1, Q.size() * sizeof(float)));
+  CK(cudaMalloc((void**)&sp.partials, 256 * sizeof(double)));
+  CK(cudaMalloc((void**)&sp.state, 4 * sizeof(int)));
+  CK(cudaMemcpy(sp.Q, Q.data(), Q.size() * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(sp.D, D.data(), D.size() * sizeof(float), cudaMemcpyHostToDevice));
+  CK(cudaMemset(sp.state, 0, 4 * sizeof(int)));
+  return EPIC_OK;
+}
+
 __global__ void k_aos_to_soa(const double* __restrict__ aos, SoA p, long long n) {
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
     const double* r = aos + 5 * q;
@@ -144,8 +187,11 @@ epic_status do_deposit(epic_sim* s, int i) {
   PhaseTimer t(s, 0);
   epic_species_state& sp = s->sp[i];
   CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
-  launch_deposit(s->stream, s->g, s->cfg.shape, s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED, sp.soa, sp.d_n,
-                 sp.desc.spwt, sp.den, sp.acc, sp.fx_scale, s->d_flags, s->part_grid);
+  if (s->mixed)
+    launch_deposit_mixed(s->stream, s->g, s->cfg.shape, sp.mx, sp.d_n, sp.acc, s->d_flags, s->part_grid);
+  else
+    launch_deposit(s->stream, s->g, s->cfg.shape, s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED, sp.soa, sp.d_n,
+                   sp.desc.spwt, sp.den, sp.acc, sp.fx_scale, s->d_flags, s->part_grid);
   s->launches += 1;
   CKL();
   return EPIC_OK;
@@ -156,7 +202,7 @@ FinalizeArgs finalize_args(epic_sim* s, int stage, int only) {
   std::memset(&a, 0, sizeof(a));
   a.g = s->g;
   a.bc = s->cfg.bc;
-  a.fixed = s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED;
+  a.fixed = s->mixed || s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED;
   a.stage = stage;
   double cell_area = s->cfg.dx * s->cfg.dy;
   double L2 = s->cfg.L * s->cfg.L;
@@ -167,7 +213,7 @@ FinalizeArgs finalize_args(epic_sim* s, int stage, int only) {
     a.acc[k] = sp.acc;
     a.den[k] = sp.den;
     a.spwt[k] = sp.desc.spwt;
-    a.inv_scale[k] = sp.fx_inv_scale;
+    a.inv_scale[k] = s->mixed ? std::ldexp(1.0, -2 * MIXED_OFFSET_BITS) : sp.fx_inv_scale;
     a.charge_over_qe[k] = sp.desc.charge * (1 / QE);
     a.active[k] = only < 0 || only == k;
   }
@@ -216,6 +262,12 @@ int solver_blocks(epic_sim* s, long long nodes_per_block) {
 epic_status do_solve(epic_sim* s) {
   PhaseTimer t(s, 2);
   SolverArgs a = solver_args(s);
+  if (s->mixed && s->spec.Q) {
+    launch_spectral(s->stream, s->spec, a, SPECTRAL_STAGES);
+    s->launches += 3 + 6 * SPECTRAL_STAGES;
+    CKL();
+    return EPIC_OK;
+  }
   if (s->cfg.solver == EPIC_SOLVER_GS) {
     if (s->cfg.sor_mode == EPIC_SOR_LEXICOGRAPHIC) launch_sor_lex(s->stream, a);
     else launch_sor_redblack(s->stream, a, solver_blocks(s, 1024));
@@ -229,7 +281,7 @@ epic_status do_solve(epic_sim* s) {
 
 epic_status do_efield(epic_sim* s) {
   PhaseTimer t(s, 3);
-  launch_efield(s->stream, s->g, s->cfg.bc, s->phi, s->efx, s->efy, s->ef);
+  launch_efield(s->stream, s->g, s->cfg.bc, s->phi, s->efx, s->efy, s->ef, s->mixed ? s->ef32 : nullptr);
   s->launches += 1;
   CKL();
   return EPIC_OK;
@@ -248,8 +300,13 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle) {
     CK(cudaMemsetAsync(s->tile_ctr, 0, sizeof(unsigned int), s->stream));
     CK(cudaMemsetAsync(s->tile_status, 0, s->tile_status_len * sizeof(unsigned long long), s->stream));
   }
-  launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, qmK, cc, dtsub, s->d_flags, s->tile_status,
-              s->tile_ctr, s->part_grid);
+  if (s->mixed)
+    launch_push_mixed(s->stream, s->g, c.shape, c.bc, sp.mx, sp.d_n, s->ef32, (float)(qmK * dtsub),
+                      (float)(cc * dtsub / c.dx), (float)(cc * dtsub / c.dy), s->d_flags, s->tile_status,
+                      s->tile_ctr, s->part_grid);
+  else
+    launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, qmK, cc, dtsub, s->d_flags, s->tile_status,
+                s->tile_ctr, s->part_grid);
   s->launches += 1;
   CKL();
   return EPIC_OK;
@@ -298,7 +355,8 @@ epic_status do_mcc(epic_sim* s, int e, int ion, const double* d_uniforms, int us
   }
   int mode = c.mcc_mode;
   if (mode == EPIC_MCC_INJECTED && !d_uniforms) mode = EPIC_MCC_PHILOX;
-  launch_mcc(s->stream, mode, s->cs, E.soa, E.d_n, E.cap, I.soa, I.d_n, I.cap, c.vel_norm, c.DT / c.W, I.desc.mass,
+  const ParticleRef er{s->mixed, E.soa, E.mx}, ir{s->mixed, I.soa, I.mx};
+  launch_mcc(s->stream, mode, s->cs, er, E.d_n, E.cap, ir, I.d_n, I.cap, c.vel_norm, c.DT / c.W, I.desc.mass,
              I.desc.temp, d_uniforms, ustride, c.seed, s->d_step, s->mcc_ev, s->d_ncoll, s->d_flags, s->part_grid);
   s->launches += 5;
   CKL();
@@ -354,6 +412,15 @@ epic_status epic_config_from_ini(const char* path, epic_config* cfg, epic_specie
   return EPIC_OK;
 }
 
+epic_status epic_ini_get(const char* path, const char* section, const char* key, char* out, int len) {
+  if (!path || !section || !key || !out || len < 1) return fail(EPIC_ERR_INVALID, "bad argument");
+  std::string v, err;
+  int st = ini_get(path, section, key, v, err);
+  if (st) return fail((epic_status)st, "%s", err.c_str());
+  std::snprintf(out, (size_t)len, "%s", v.c_str());
+  return EPIC_OK;
+}
+
 epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   if (!cfg || !out) return fail(EPIC_ERR_INVALID, "null argument");
   *out = nullptr;
@@ -401,6 +468,11 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   guard(dalloc(&s->sum_partials, 3 * (size_t)s->part_grid));
   guard(dalloc(&s->d_sums, 4));
   guard(dalloc(&s->d_flags, 1));
+  s->mixed = cfg->precision == EPIC_PRECISION_MIXED;
+  if (s->mixed) {
+    guard(dalloc(&s->ef32, nn));
+    if (spectral_supported(s->g) && !st) guard(setup_spectral(s));
+  }
   if (st) {
     std::string e = g_err;
     epic_destroy(s);
@@ -414,10 +486,10 @@ void epic_destroy(epic_sim* s) {
   if (!s) return;
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
-  for (auto& sp : s->sp) {
-    cudaFree(sp.soa.x); cudaFree(sp.soa.y); cudaFree(sp.soa.vx); cudaFree(sp.soa.vy); cudaFree(sp.soa.vz);
-    cudaFree(sp.d_n); cudaFree(sp.den); cudaFree(sp.acc);
-  }
+  for (auto& sp : s->sp) free_species(sp);
+  void* spec[] = {s->spec.Q, s->spec.D, s->spec.t0, s->spec.t1, s->spec.r64, s->spec.partials, s->spec.state,
+                  s->ef32};
+  for (void* p : spec) cudaFree(p);
   for (auto& pe : s->prof_pending) {
     cudaEventDestroy(pe.second.first);
     cudaEventDestroy(pe.second.second);
@@ -446,6 +518,10 @@ epic_status epic_add_species(epic_sim* s, const epic_species_desc* d, int* index
   if (d->numparticle < 0 || !(d->mass > 0)) return fail(EPIC_ERR_INVALID, "bad species %s", d->name);
   epic_species_state sp;
   std::memset(&sp.soa, 0, sizeof(sp.soa));
+  std::memset(&sp.mx, 0, sizeof(sp.mx));
+  sp.d_n = nullptr;
+  sp.den = nullptr;
+  sp.acc = nullptr;
   sp.desc = *d;
   sp.desc.name[sizeof(sp.desc.name) - 1] = 0;
   sp.name = sp.desc.name;
@@ -463,18 +539,28 @@ epic_status epic_add_species(epic_sim* s, const epic_species_desc* d, int* index
     if (x && !st) st = x;
   };
   const size_t cap = (size_t)sp.cap, nn = (size_t)nnodes(s);
-  guard(dalloc(&sp.soa.x, cap));
-  guard(dalloc(&sp.soa.y, cap));
-  guard(dalloc(&sp.soa.vx, cap));
-  guard(dalloc(&sp.soa.vy, cap));
-  guard(dalloc(&sp.soa.vz, cap));
+  if (s->mixed) {
+    // 2^40 per particle in the integer CIC weights: overflow needs > 2^23
+    // particles in one node's four cells.
+    guard(dalloc(&sp.mx.cell, cap));
+    guard(dalloc(&sp.mx.ox, cap));
+    guard(dalloc(&sp.mx.oy, cap));
+    guard(dalloc(&sp.mx.vx, cap));
+    guard(dalloc(&sp.mx.vy, cap));
+    guard(dalloc(&sp.mx.vz, cap));
+  } else {
+    guard(dalloc(&sp.soa.x, cap));
+    guard(dalloc(&sp.soa.y, cap));
+    guard(dalloc(&sp.soa.vx, cap));
+    guard(dalloc(&sp.soa.vy, cap));
+    guard(dalloc(&sp.soa.vz, cap));
+  }
   guard(dalloc(&sp.d_n, 1));
   guard(dalloc(&sp.den, nn));
   guard(dalloc(&sp.acc, nn));
   guard(ensure_tile_status(s, sp.cap));
   if (st) {
-    cudaFree(sp.soa.x); cudaFree(sp.soa.y); cudaFree(sp.soa.vx); cudaFree(sp.soa.vy); cudaFree(sp.soa.vz);
-    cudaFree(sp.d_n); cudaFree(sp.den); cudaFree(sp.acc);
+    free_species(sp);
     return st;
   }
   s->sp.push_back(sp);
@@ -491,7 +577,10 @@ epic_status epic_set_particles(epic_sim* s, int i, const double* parts, int64_t 
   if (st) return st;
   if (n) {
     CK(cudaMemcpyAsync(s->staging, parts, (size_t)n * 5 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
-    k_aos_to_soa<<<s->part_grid, 256, 0, s->stream>>>((const double*)s->staging, sp.soa, n);
+    if (s->mixed)
+      launch_aos_to_mixed(s->stream, s->g, (const double*)s->staging, sp.mx, n, s->d_flags, s->part_grid);
+    else
+      k_aos_to_soa<<<s->part_grid, 256, 0, s->stream>>>((const double*)s->staging, sp.soa, n);
     s->launches += 1;
     CKL();
   }
@@ -519,7 +608,8 @@ epic_status epic_get_particles(epic_sim* s, int i, double* parts, int64_t capaci
                                   (long long)capacity, (long long)cnt);
   if (!cnt) return EPIC_OK;
   if ((st = ensure_staging(s, (size_t)cnt * 5 * sizeof(double)))) return st;
-  k_soa_to_aos<<<s->part_grid, 256, 0, s->stream>>>((double*)s->staging, s->sp[i].soa, s->sp[i].d_n);
+  if (s->mixed) launch_mixed_to_aos(s->stream, s->g, (double*)s->staging, s->sp[i].mx, s->sp[i].d_n, s->part_grid);
+  else k_soa_to_aos<<<s->part_grid, 256, 0, s->stream>>>((double*)s->staging, s->sp[i].soa, s->sp[i].d_n);
   s->launches += 1;
   CKL();
   CK(cudaMemcpyAsync(parts, s->staging, (size_t)cnt * 5 * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
@@ -592,7 +682,11 @@ epic_status epic_rewind_species(epic_sim* s, int i) {
   double qm = sp.desc.charge / sp.desc.mass;
   double K = (c.density * QE * c.L) / (EPS_0 * c.W * c.vel_norm);
   double hqmK = 0.5 * qm * K;
-  launch_rewind(s->stream, s->g, c.shape, sp.soa, sp.d_n, s->ef, hqmK, c.DT, s->d_flags, s->part_grid);
+  if (s->mixed)
+    launch_rewind_mixed(s->stream, s->g, c.shape, sp.mx, sp.d_n, s->ef32, (float)(hqmK * c.DT), s->d_flags,
+                        s->part_grid);
+  else
+    launch_rewind(s->stream, s->g, c.shape, sp.soa, sp.d_n, s->ef, hqmK, c.DT, s->d_flags, s->part_grid);
   s->launches += 1;
   CKL();
   return sync(s);
@@ -753,7 +847,11 @@ epic_status epic_run(epic_sim* s, int steps, int with_collisions, int use_graph)
 epic_status epic_compute_ke(epic_sim* s, int i, int norm, double out[3]) {
   if (!valid_species(s, i) || !valid_species(s, norm) || !out) return fail(EPIC_ERR_INVALID, "bad argument");
   epic_species_state& sp = s->sp[i];
-  launch_particle_sums(s->stream, 0, sp.soa, sp.d_n, s->cfg.vel_norm, s->sum_partials, s->d_sums, s->part_grid);
+  if (s->mixed)
+    launch_particle_sums_mixed(s->stream, 0, sp.mx, sp.d_n, s->cfg.vel_norm, s->sum_partials, s->d_sums,
+                               s->part_grid);
+  else
+    launch_particle_sums(s->stream, 0, sp.soa, sp.d_n, s->cfg.vel_norm, s->sum_partials, s->d_sums, s->part_grid);
   s->launches += 2;
   CKL();
   double k[3];
@@ -772,7 +870,11 @@ epic_status epic_compute_ke(epic_sim* s, int i, int norm, double out[3]) {
 epic_status epic_compute_momentum(epic_sim* s, int i, int norm, double out[3]) {
   if (!valid_species(s, i) || !valid_species(s, norm) || !out) return fail(EPIC_ERR_INVALID, "bad argument");
   epic_species_state& sp = s->sp[i];
-  launch_particle_sums(s->stream, 1, sp.soa, sp.d_n, s->cfg.vel_norm, s->sum_partials, s->d_sums, s->part_grid);
+  if (s->mixed)
+    launch_particle_sums_mixed(s->stream, 1, sp.mx, sp.d_n, s->cfg.vel_norm, s->sum_partials, s->d_sums,
+                               s->part_grid);
+  else
+    launch_particle_sums(s->stream, 1, sp.soa, sp.d_n, s->cfg.vel_norm, s->sum_partials, s->d_sums, s->part_grid);
   s->launches += 2;
   CKL();
   double p[3];
@@ -855,6 +957,11 @@ epic_status epic_set_grid(epic_sim* s, int which, const double* in) {
     std::vector<double2> e2(nnodes(s));
     for (long long k = 0; k < nnodes(s); k++) e2[k] = make_double2(ex[k], ey[k]);
     CK(cudaMemcpy(s->ef, e2.data(), nnodes(s) * sizeof(double2), cudaMemcpyHostToDevice));
+    if (s->ef32) {
+      std::vector<float2> f2(nnodes(s));
+      for (long long k = 0; k < nnodes(s); k++) f2[k] = make_float2((float)ex[k], (float)ey[k]);
+      CK(cudaMemcpy(s->ef32, f2.data(), nnodes(s) * sizeof(float2), cudaMemcpyHostToDevice));
+    }
   }
   return EPIC_OK;
 }

@@ -81,7 +81,8 @@ void launch_finalize(cudaStream_t st, const FinalizeArgs& a) {
 
 // ------------------------------------------------------------ E-field ---
 // FieldSolve::CalculateEfield (src/field.cpp:276-330).
-__global__ void k_efield(Geom g, int bc, const double* __restrict__ phi, double* efx, double* efy, double2* ef) {
+__global__ void k_efield(Geom g, int bc, const double* __restrict__ phi, double* efx, double* efy, double2* ef,
+                         float2* ef32) {
   const int nx = g.nx, ny = g.ny;
   const int nn = nx * ny;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
@@ -106,12 +107,14 @@ __global__ void k_efield(Geom g, int bc, const double* __restrict__ phi, double*
     efx[k] = ex;
     efy[k] = ey;
     ef[k] = make_double2(ex, ey);
+    if (ef32) ef32[k] = make_float2((float)ex, (float)ey);
   }
 }
 
-void launch_efield(cudaStream_t st, const Geom& g, int bc, const double* phi, double* efx, double* efy, double2* ef) {
+void launch_efield(cudaStream_t st, const Geom& g, int bc, const double* phi, double* efx, double* efy, double2* ef,
+                   float2* ef32) {
   int nn = g.nx * g.ny;
-  k_efield<<<(nn + 255) / 256, 256, 0, st>>>(g, bc, phi, efx, efy, ef);
+  k_efield<<<(nn + 255) / 256, 256, 0, st>>>(g, bc, phi, efx, efy, ef, ef32);
 }
 
 // ------------------------------------------------- lexicographic SOR ---

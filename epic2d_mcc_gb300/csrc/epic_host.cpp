@@ -95,6 +95,18 @@ bool to_bool(const std::string& s) {  // include/extrafun.h:6-17
 
 }  // namespace
 
+int ini_get(const char* path, const char* section, const char* key, std::string& value, std::string& err) {
+  Ini ini;
+  if (!parse_ini(path, ini, err)) return EPIC_ERR_IO;
+  auto s = ini.find(section);
+  if (s == ini.end() || s->second.find(key) == s->second.end()) {
+    err = std::string("missing key ") + key + " in [" + section + "]";
+    return EPIC_ERR_INVALID;
+  }
+  value = s->second.at(key);
+  return EPIC_OK;
+}
+
 // src/main.cpp:42-261 and Domain::set_normscheme (src/domain.cpp:123-183),
 // same operation order.  vel_norm is always L*W: main() never stores
 // vel_norm_scheme into the Domain, and set_normscheme keeps another value only
@@ -218,6 +230,8 @@ int config_from_ini(const char* path, epic_config* cfg, epic_species_desc* sp, i
     if (auto v = opt(ini, "solver", "sor_mode")) cfg->sor_mode = *v == "redblack" ? EPIC_SOR_REDBLACK : EPIC_SOR_LEXICOGRAPHIC;
     if (auto v = opt(ini, "solver", "warm_start")) cfg->warm_start = to_bool(*v);
     if (auto v = opt(ini, "simulation", "deposit_mode")) cfg->deposit_mode = *v == "fp64" ? EPIC_DEPOSIT_FP64 : EPIC_DEPOSIT_FIXED;
+    if (auto v = opt(ini, "simulation", "arithmetic"))
+      cfg->precision = *v == "mixed" ? EPIC_PRECISION_MIXED : EPIC_PRECISION_FP64;
     if (auto v = opt(ini, "collision", "mcc_mode"))
       cfg->mcc_mode = *v == "null" ? EPIC_MCC_NULL : (*v == "injected" ? EPIC_MCC_INJECTED : EPIC_MCC_PHILOX);
     if (auto v = opt(ini, "collision", "seed")) cfg->seed = std::stoull(*v);

@@ -19,6 +19,7 @@ constexpr double PI_H = 3.141592653;
 
 int config_from_ini(const char* path, epic_config* cfg, epic_species_desc* sp, int max_sp, int* nsp, int* num_ts,
                     std::string& err);
+int ini_get(const char* path, const char* section, const char* key, std::string& value, std::string& err);
 int load_particles(const epic_config& c, const std::vector<const epic_species_desc*>& sp,
                    std::vector<std::vector<double>>& out, uint32_t seed, std::string& err);
 void reference_tables(const epic_config& c, std::vector<double>& tot, std::vector<double>& ela,

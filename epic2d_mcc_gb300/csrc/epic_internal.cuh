@@ -59,6 +59,22 @@ struct SoA {
   double *x, *y, *vx, *vy, *vz;
 };
 
+// Mixed-precision particle record (24 bytes): the grid node at the lower-left
+// corner of the particle's cell (i*ny + j, so the deposit needs no index
+// arithmetic), the FP32 offset inside the cell in units of dx/dy, in [0, 1),
+// and FP32 velocities.  Position = x0 + (i + ox)*dx.
+struct MixedSoA {
+  int* cell;
+  float *ox, *oy, *vx, *vy, *vz;
+};
+
+// Particles of one species in either layout.
+struct ParticleRef {
+  int mixed;
+  SoA f;
+  MixedSoA m;
+};
+
 // Per-launch solver outcome, written by the device.
 struct SolveInfo {
   int iterations;
@@ -103,11 +119,43 @@ struct McEvents {
 };
 // d_step: device step counter (Philox counter word), advanced by every MCC
 // launch so replayed graphs draw fresh numbers.
-void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const SoA& e, long long* d_ne, long long e_cap,
-                const SoA& ion, long long* d_ni, long long i_cap, double vel_norm, double dt_phys, double ion_mass,
-                double ion_temp, const double* uniforms, int ustride, uint64_t seed, unsigned long long* d_step,
-                const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid);
+void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const ParticleRef& e, long long* d_ne,
+                long long e_cap, const ParticleRef& ion, long long* d_ni, long long i_cap, double vel_norm,
+                double dt_phys, double ion_mass, double ion_temp, const double* uniforms, int ustride, uint64_t seed,
+                unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid);
 size_t ion_event_bytes();
+
+// ---- mixed-precision particle kernels (epic_mixed.cu) ----
+void launch_aos_to_mixed(cudaStream_t st, const Geom& g, const double* aos, const MixedSoA& p, long long n,
+                         int* flags, int grid);
+void launch_mixed_to_aos(cudaStream_t st, const Geom& g, double* aos, const MixedSoA& p, const long long* d_n,
+                         int grid);
+void launch_deposit_mixed(cudaStream_t st, const Geom& g, int shape, const MixedSoA& p, const long long* d_n,
+                          unsigned long long* acc, int* flags, int grid);
+void launch_push_mixed(cudaStream_t st, const Geom& g, int shape, int bc, const MixedSoA& p, long long* d_n,
+                       const float2* ef, float qmK_dt, float cx, float cy, int* flags,
+                       unsigned long long* tile_status, unsigned int* tile_ctr, int grid);
+void launch_rewind_mixed(cudaStream_t st, const Geom& g, int shape, const MixedSoA& p, const long long* d_n,
+                         const float2* ef, float hqmK_dt, int* flags, int grid);
+void launch_particle_sums_mixed(cudaStream_t st, int what, const MixedSoA& p, const long long* d_n,
+                                double vel_norm, double* partials, double* out3, int grid);
+constexpr int MIXED_OFFSET_BITS = 20;  // deposit weights: offsets quantised to 2^-20 of a cell
+
+// ---- spectral FP32 inner solve with FP64 refinement (epic_spectral.cu) ----
+struct SolverArgs;
+struct SpectralSolver {
+  int n;          // unknowns per side (square grids only)
+  int off;        // index of the first unknown node in each direction (0: all nodes, 1: interior)
+  int gs_norm;    // 1: stop on the SOR residual L2 of src/field.cpp:118-134, 0: on |b - Ax|_2
+  float* Q;       // n x n sine transform, orthonormal and symmetric
+  float* D;       // n x n, 1/(lambda_p + lambda_q)
+  float *t0, *t1; // n x n FP32 scratch
+  double *r64;    // residual scratch (nx*ny)
+  double* partials;
+  int* state;     // [0] done flag, [1] stage, [2] converged
+};
+int spectral_supported(const Geom& g);
+void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs& a, int stages);
 void launch_particle_sums(cudaStream_t st, int what, const SoA& p, const long long* d_n, double vel_norm,
                           double* partials, double* out3, int grid);
 
@@ -132,7 +180,8 @@ struct FinalizeArgs {
   double* rho;
 };
 void launch_finalize(cudaStream_t st, const FinalizeArgs& a);
-void launch_efield(cudaStream_t st, const Geom& g, int bc, const double* phi, double* efx, double* efy, double2* ef);
+void launch_efield(cudaStream_t st, const Geom& g, int bc, const double* phi, double* efx, double* efy, double2* ef,
+                   float2* ef32);
 
 struct SolverArgs {
   Geom g;
@@ -166,7 +215,8 @@ struct epic_species_state {
   epic_species_desc desc;
   std::string name;
   long long cap;
-  epic::SoA soa;
+  epic::SoA soa;        // FP64 plain form
+  epic::MixedSoA mx;    // mixed-precision form (cell, FP32 offsets and velocities)
   long long* d_n;
   double* den;
   unsigned long long* acc;
@@ -183,6 +233,9 @@ struct epic_sim {
   std::vector<epic_species_state> sp;
   double *phi, *rho, *efx, *efy;
   double2* ef;
+  float2* ef32;                // FP32 (efx, efy) for the mixed-precision gather
+  epic::SpectralSolver spec;   // mixed-precision Poisson solve (square grids)
+  int mixed;                   // cfg.precision == EPIC_PRECISION_MIXED
   // solver workspace
   double* work[8];
   double* partials;

@@ -1,0 +1,356 @@
+// Particle kernels of the mixed-precision form.
+//
+// Record: cell (int32 node index i*ny + j of the cell's lower-left node),
+// ox, oy (FP32 offsets inside the cell, [0, 1)), vx, vy, vz (FP32) — 24 bytes.
+// The push reads and writes 20 of them (40 B per particle-step); the deposit
+// reads 12; everything runs on the FP32 and integer pipes.  Offsets keep a
+// uniform 2^-24-cell resolution over the whole domain, where FP32 absolute
+// positions would lose precision with distance from the origin.
+//
+// Compiled with contraction (FMA) enabled: this form is checked against the
+// FP64 oracle within stated tolerances, not bit for bit.
+#include <cuda_runtime.h>
+
+#include "epic_device.cuh"
+#include "epic_internal.cuh"
+
+namespace epic {
+
+// ------------------------------------------------------------ layout ---
+// Upload: FP64 records {x, y, vx, vy, vz} -> mixed.  Species::AddParticle's
+// positions become (cell, offset); a particle outside the grid raises
+// FLAG_OUT_OF_GRID (the reference would throw at its first deposit).
+__global__ void k_aos_to_mixed(Geom g, const double* __restrict__ aos, MixedSoA p, long long n, int* flags) {
+  bool bad = false;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const double* r = aos + 5 * q;
+    double lx = (r[0] - g.x0) / g.dx, ly = (r[1] - g.y0) / g.dy;
+    double fi = floor(lx), fj = floor(ly);
+    int i = (int)fi, j = (int)fj;
+    float ox = (float)(lx - fi), oy = (float)(ly - fj);
+    if (ox >= 1.f) { ox = 0.f; i++; }
+    if (oy >= 1.f) { oy = 0.f; j++; }
+    if (i < 0 || i > g.nx - 2 || j < 0 || j > g.ny - 2) {
+      bad = true;
+      i = min(max(i, 0), g.nx - 2);
+      j = min(max(j, 0), g.ny - 2);
+    }
+    p.cell[q] = i * g.ny + j;
+    p.ox[q] = ox;
+    p.oy[q] = oy;
+    p.vx[q] = (float)r[2];
+    p.vy[q] = (float)r[3];
+    p.vz[q] = (float)r[4];
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
+}
+
+__global__ void k_mixed_to_aos(Geom g, double* __restrict__ aos, MixedSoA p, const long long* __restrict__ d_n) {
+  const long long n = *d_n;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const int c = p.cell[q];
+    const int i = c / g.ny, j = c - i * g.ny;
+    double* r = aos + 5 * q;
+    r[0] = g.x0 + ((double)i + (double)p.ox[q]) * g.dx;
+    r[1] = g.y0 + ((double)j + (double)p.oy[q]) * g.dy;
+    r[2] = p.vx[q];
+    r[3] = p.vy[q];
+    r[4] = p.vz[q];
+  }
+}
+
+void launch_aos_to_mixed(cudaStream_t st, const Geom& g, const double* aos, const MixedSoA& p, long long n,
+                         int* flags, int grid) {
+  k_aos_to_mixed<<<grid, PART_THREADS, 0, st>>>(g, aos, p, n, flags);
+}
+
+void launch_mixed_to_aos(cudaStream_t st, const Geom& g, double* aos, const MixedSoA& p, const long long* d_n,
+                         int grid) {
+  k_mixed_to_aos<<<grid, PART_THREADS, 0, st>>>(g, aos, p, d_n);
+}
+
+// ----------------------------------------------------------- deposit ---
+// CIC / NGP deposit with integer weights (Domain::Scatter, src/domain.cpp:
+// 205-228): the offsets are quantised to 2^-20 of a cell and the four CIC
+// weights are exact integer products summing to 2^40, accumulated in int64
+// (deterministic: integer addition is associative).  No node can overflow
+// unless more than 2^23 particles share its four cells.  The finalisation
+// multiplies by spwt * 2^-40.
+template <int SHAPE>
+__global__ void __launch_bounds__(PART_THREADS) k_deposit_mixed(Geom g, MixedSoA p, const long long* __restrict__ d_n,
+                                                                unsigned long long* __restrict__ acc) {
+  const long long n = *d_n;
+  const long long S = 1ll << MIXED_OFFSET_BITS;
+  const float fS = (float)S;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const int c = __ldg(&p.cell[q]);
+    const float ox = __ldg(&p.ox[q]), oy = __ldg(&p.oy[q]);
+    if (SHAPE == EPIC_NGP) {
+      // round(lx) with lx = i + ox >= 0: i + (ox >= 0.5)
+      const int k = c + (ox >= 0.5f ? g.ny : 0) + (oy >= 0.5f ? 1 : 0);
+      atomicAdd(&acc[k], (unsigned long long)(S * S));
+    } else {
+      const long long a = (long long)(ox * fS), b = (long long)(oy * fS);  // truncation, in [0, 2^20)
+      atomicAdd(&acc[c], (unsigned long long)((S - a) * (S - b)));
+      atomicAdd(&acc[c + g.ny], (unsigned long long)(a * (S - b)));
+      atomicAdd(&acc[c + 1], (unsigned long long)((S - a) * b));
+      atomicAdd(&acc[c + g.ny + 1], (unsigned long long)(a * b));
+    }
+  }
+}
+
+void launch_deposit_mixed(cudaStream_t st, const Geom& g, int shape, const MixedSoA& p, const long long* d_n,
+                          unsigned long long* acc, int* flags, int grid) {
+  (void)flags;
+  if (shape == EPIC_NGP) k_deposit_mixed<EPIC_NGP><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, acc);
+  else k_deposit_mixed<EPIC_CIC><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, acc);
+}
+
+// -------------------------------------------------------------- push ---
+// Species::Push_species_serial (src/species.cpp:29-170) in cell units:
+//   v += (qm*K*DT) E;  offset += (vel_norm/(L*W)) * DT / dx * v;
+// then whole cells are carried from the offset into the cell index and the
+// boundary rule applied to the cell.  Periodic wrap is a modulo, so a
+// particle may cross any number of cells in a step.
+template <int SHAPE>
+__device__ __forceinline__ void gather32(const Geom& g, const float2* __restrict__ ef, int c, float ox, float oy,
+                                         float& ex, float& ey) {
+  if (SHAPE == EPIC_NGP) {
+    const int k = c + (ox >= 0.5f ? g.ny : 0) + (oy >= 0.5f ? 1 : 0);
+    const float2 f = __ldg(&ef[k]);
+    ex = f.x;
+    ey = f.y;
+    return;
+  }
+  const float2 f00 = __ldg(&ef[c]), f01 = __ldg(&ef[c + 1]);
+  const float2 f10 = __ldg(&ef[c + g.ny]), f11 = __ldg(&ef[c + g.ny + 1]);
+  const float w00 = (1.f - ox) * (1.f - oy), w10 = ox * (1.f - oy), w01 = (1.f - ox) * oy, w11 = ox * oy;
+  ex = f00.x * w00 + f10.x * w10 + f01.x * w01 + f11.x * w11;
+  ey = f00.y * w00 + f10.y * w10 + f01.y * w01 + f11.y * w11;
+}
+
+// Moves (cell index, offset) along one axis by `d` cells and applies the
+// boundary rule.  Returns false if the particle leaves an open boundary.
+template <int BC>
+__device__ __forceinline__ bool advance(int& idx, float& o, float& v, float d, int ncell) {
+  o += d;
+  const float f = floorf(o);
+  o -= f;
+  idx += (int)f;
+  if (o >= 1.f) {  // o was a tiny negative number
+    o = 0.f;
+    idx += 1;
+  }
+  if (BC == EPIC_PBC) {
+    if (idx < 0 || idx >= ncell) {
+      idx %= ncell;
+      if (idx < 0) idx += ncell;
+    }
+    return true;
+  } else if (BC == EPIC_OPEN) {
+    return idx >= 0 && idx < ncell;
+  } else {
+    if (idx < 0 || idx >= ncell) {
+      // mirror the position about the wall it crossed, flip the velocity
+      float pos = (float)idx + o;
+      pos = idx < 0 ? -pos : 2.f * ncell - pos;
+      const float fl = floorf(pos);
+      idx = (int)fl;
+      o = pos - fl;
+      if (o >= 1.f) {
+        o = 0.f;
+        idx += 1;
+      }
+      idx = min(max(idx, 0), ncell - 1);
+      v = -v;
+    }
+    return true;
+  }
+}
+
+template <int SHAPE, int BC>
+__device__ __forceinline__ bool push_mixed_one(const Geom& g, const float2* __restrict__ ef, float qmK_dt, float cx,
+                                               float cy, int& c, float& ox, float& oy, float& vx, float& vy) {
+  float ex, ey;
+  gather32<SHAPE>(g, ef, c, ox, oy, ex, ey);
+  vx = fmaf(qmK_dt, ex, vx);
+  vy = fmaf(qmK_dt, ey, vy);
+  int i = c / g.ny, j = c - i * g.ny;
+  bool keep = advance<BC>(i, ox, vx, cx * vx, g.nx - 1);
+  keep = advance<BC>(j, oy, vy, cy * vy, g.ny - 1) && keep;
+  c = i * g.ny + j;
+  return keep;
+}
+
+template <int SHAPE, int BC>
+__global__ void __launch_bounds__(PART_THREADS) k_push_mixed(Geom g, MixedSoA p, const long long* __restrict__ d_n,
+                                                             const float2* __restrict__ ef, float qmK_dt, float cx,
+                                                             float cy) {
+  const long long n = *d_n;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    int c = p.cell[q];
+    float ox = p.ox[q], oy = p.oy[q], vx = p.vx[q], vy = p.vy[q];
+    push_mixed_one<SHAPE, BC>(g, ef, qmK_dt, cx, cy, c, ox, oy, vx, vy);
+    p.cell[q] = c;
+    p.ox[q] = ox;
+    p.oy[q] = oy;
+    p.vx[q] = vx;
+    p.vy[q] = vy;
+  }
+}
+
+// Open boundaries: push + stable in-place compaction with ordered tiles
+// (the FP64 form's scheme; see k_push_compact in epic_particles.cu).
+template <int SHAPE>
+__global__ void __launch_bounds__(PART_THREADS) k_push_mixed_compact(Geom g, MixedSoA p, long long* d_n,
+                                                                     const float2* __restrict__ ef, float qmK_dt,
+                                                                     float cx, float cy, unsigned long long* status,
+                                                                     unsigned int* tile_ctr, int* flags) {
+  constexpr int ITEMS = SCAN_TILE / PART_THREADS;
+  __shared__ int sm[40];
+  __shared__ unsigned long long s_prefix;
+  __shared__ int s_tile;
+  const long long n = *d_n;
+  const int num_tiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(tile_ctr, 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= num_tiles) break;
+    const long long base = (long long)tile * SCAN_TILE;
+    int c[ITEMS], keep[ITEMS];
+    float ox[ITEMS], oy[ITEMS], vx[ITEMS], vy[ITEMS], vz[ITEMS];
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+      const long long q = base + (long long)k * PART_THREADS + threadIdx.x;
+      keep[k] = 0;
+      if (q < n) {
+        c[k] = p.cell[q]; ox[k] = p.ox[q]; oy[k] = p.oy[q]; vx[k] = p.vx[q]; vy[k] = p.vy[q]; vz[k] = p.vz[q];
+        keep[k] = push_mixed_one<SHAPE, EPIC_OPEN>(g, ef, qmK_dt, cx, cy, c[k], ox[k], oy[k], vx[k], vy[k]);
+      }
+    }
+    int rank[ITEMS];
+    int tile_total = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+      int row_total;
+      rank[k] = tile_total + block_exclusive_scan(keep[k], &row_total, sm);
+      tile_total += row_total;
+    }
+    if (threadIdx.x == 0) s_prefix = tile_lookback(status, tile, (unsigned long long)tile_total, flags);
+    __syncthreads();
+    const unsigned long long prefix = s_prefix;
+    if (prefix != ~0ull) {
+#pragma unroll
+      for (int k = 0; k < ITEMS; k++) {
+        if (keep[k]) {
+          const long long o = (long long)prefix + rank[k];
+          p.cell[o] = c[k]; p.ox[o] = ox[k]; p.oy[o] = oy[k]; p.vx[o] = vx[k]; p.vy[o] = vy[k]; p.vz[o] = vz[k];
+        }
+      }
+      if (tile == num_tiles - 1 && threadIdx.x == 0) *d_n = (long long)prefix + tile_total;
+    }
+    __syncthreads();
+  }
+}
+
+void launch_push_mixed(cudaStream_t st, const Geom& g, int shape, int bc, const MixedSoA& p, long long* d_n,
+                       const float2* ef, float qmK_dt, float cx, float cy, int* flags,
+                       unsigned long long* tile_status, unsigned int* tile_ctr, int grid) {
+#define PM(SH, B) k_push_mixed<SH, B><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy)
+  if (bc == EPIC_OPEN) {
+    if (shape == EPIC_NGP)
+      k_push_mixed_compact<EPIC_NGP><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy, tile_status,
+                                                                     tile_ctr, flags);
+    else
+      k_push_mixed_compact<EPIC_CIC><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy, tile_status,
+                                                                     tile_ctr, flags);
+  } else if (bc == EPIC_PBC) {
+    if (shape == EPIC_NGP) PM(EPIC_NGP, EPIC_PBC);
+    else PM(EPIC_CIC, EPIC_PBC);
+  } else {
+    if (shape == EPIC_NGP) PM(EPIC_NGP, EPIC_REFLECTIVE);
+    else PM(EPIC_CIC, EPIC_REFLECTIVE);
+  }
+#undef PM
+}
+
+// Species::Rewind_species (src/species.cpp:229-246): v -= (0.5*qm*K*DT) E.
+template <int SHAPE>
+__global__ void __launch_bounds__(PART_THREADS) k_rewind_mixed(Geom g, MixedSoA p, const long long* __restrict__ d_n,
+                                                               const float2* __restrict__ ef, float hqmK_dt) {
+  const long long n = *d_n;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    float ex, ey;
+    gather32<SHAPE>(g, ef, p.cell[q], p.ox[q], p.oy[q], ex, ey);
+    p.vx[q] = fmaf(-hqmK_dt, ex, p.vx[q]);
+    p.vy[q] = fmaf(-hqmK_dt, ey, p.vy[q]);
+  }
+}
+
+void launch_rewind_mixed(cudaStream_t st, const Geom& g, int shape, const MixedSoA& p, const long long* d_n,
+                         const float2* ef, float hqmK_dt, int* flags, int grid) {
+  (void)flags;
+  if (shape == EPIC_NGP) k_rewind_mixed<EPIC_NGP><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, hqmK_dt);
+  else k_rewind_mixed<EPIC_CIC><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, hqmK_dt);
+}
+
+// ------------------------------------------------------- reductions ---
+// Energy / momentum sums accumulated in FP64 from the FP32 velocities
+// (Species::Compute_KE / Compute_Momentum, src/species.cpp:248-297).
+__device__ __forceinline__ double warp_sum_m(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__global__ void __launch_bounds__(PART_THREADS) k_particle_sums_mixed(int what, MixedSoA p,
+                                                                      const long long* __restrict__ d_n, double vn,
+                                                                      double* partials) {
+  const long long n = *d_n;
+  double s0 = 0, s1 = 0, s2 = 0;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const double a = p.vx[q], b = p.vy[q], c = p.vz[q];
+    if (what == 0) {
+      s0 += (a * a) * vn * vn;
+      s1 += (b * b) * vn * vn;
+      s2 += (c * c) * vn * vn;
+    } else {
+      s0 += a * vn;
+      s1 += b * vn;
+      s2 += c * vn;
+    }
+  }
+  __shared__ double sm[3][PART_THREADS / 32];
+  s0 = warp_sum_m(s0);
+  s1 = warp_sum_m(s1);
+  s2 = warp_sum_m(s2);
+  if ((threadIdx.x & 31) == 0) {
+    sm[0][threadIdx.x >> 5] = s0;
+    sm[1][threadIdx.x >> 5] = s1;
+    sm[2][threadIdx.x >> 5] = s2;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double t = 0;
+    for (int w = 0; w < PART_THREADS / 32; w++) t += sm[threadIdx.x][w];
+    partials[blockIdx.x * 3 + threadIdx.x] = t;
+  }
+}
+
+__global__ void k_sum_partials3_m(const double* partials, int nblocks, double* out) {
+  const int c = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (c >= 3) return;
+  double t = 0;
+  for (int b = lane; b < nblocks; b += 32) t += partials[b * 3 + c];
+  t = warp_sum_m(t);
+  if (lane == 0) out[c] = t;
+}
+
+void launch_particle_sums_mixed(cudaStream_t st, int what, const MixedSoA& p, const long long* d_n, double vel_norm,
+                                double* partials, double* out3, int grid) {
+  k_particle_sums_mixed<<<grid, PART_THREADS, 0, st>>>(what, p, d_n, vel_norm, partials);
+  k_sum_partials3_m<<<1, 96, 0, st>>>(partials, grid, out3);
+}
+
+}  // namespace epic

@@ -1,0 +1,118 @@
+// epic2d — command-line driver of the GB300 time-step loop, the counterpart
+// of the reference's src/main.cpp: reads the same input.ini, loads particles
+// from the same mt19937 stream, runs the initial field and NUM_TS + 1 loop
+// iterations, and prints the diagnostics line of Output::diagnostics
+// (src/output.cpp:318-392) every write_diagnostics steps.  HDF5 output and
+// plotting are not part of it; `--energy FILE` writes the time history that
+// Output::storeKE_to_matrix keeps (ts*DT, KE x/y/z per species, PE) as CSV.
+//
+//   epic2d input.ini [--steps N] [--graph] [--energy energy.csv] [--quiet]
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <iomanip>
+#include <iostream>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "epic2d.hpp"
+
+using namespace epic2d;
+
+int main(int argc, char** argv) {
+  if (argc < 2) {
+    std::cout << "ERROR, at least one argument expected (the input file)." << std::endl;
+    return 1;
+  }
+  const std::string ini = argv[1];
+  int steps_override = -1;
+  bool graph = false, quiet = false;
+  std::string energy_path;
+  for (int k = 2; k < argc; k++) {
+    if (!std::strcmp(argv[k], "--steps") && k + 1 < argc) steps_override = std::atoi(argv[++k]);
+    else if (!std::strcmp(argv[k], "--graph")) graph = true;
+    else if (!std::strcmp(argv[k], "--quiet")) quiet = true;
+    else if (!std::strcmp(argv[k], "--energy") && k + 1 < argc) energy_path = argv[++k];
+  }
+  try {
+    epic_config cfg;
+    epic_species_desc descs[8];
+    int nsp = 0, num_ts = 0;
+    check(epic_config_from_ini(ini.c_str(), &cfg, descs, 8, &nsp, &num_ts));
+    if (nsp > 8) throw std::runtime_error("at most 8 species");
+    const int write_diag = INIParser::getInt(ini, "diagnostics", "write_diagnostics");
+    const int write_interval = INIParser::getInt(ini, "diagnostics", "write_interval");
+    const int precision = INIParser::getInt(ini, "diagnostics", "precision");
+    if (steps_override >= 0) num_ts = steps_override;
+    const bool collisions = cfg.elastic || cfg.excitation || cfg.ionization;
+
+    Domain domain(cfg);
+    std::vector<std::unique_ptr<Species>> species;
+    for (int s = 0; s < nsp; s++) species.emplace_back(new Species(domain, descs[s]));
+    FieldSolve fieldsolver(domain);
+    CollisionHandler coll(domain);
+    check(epic_load_particles(domain.handle(), 0));  // Init, global Rnd seeded with 0
+    // Initial field and the leapfrog half step back (src/main.cpp:366-382).
+    check(epic_initial_field(domain.handle()));
+    coll.set_electron_cross_sections();
+    coll.calc_total_cross_sections();
+    // Normalising species of Output::diagnostics (src/output.cpp:323-324).
+    const int norm = (cfg.normscheme == 2 || cfg.normscheme == 4) ? 1 : 0;
+    std::ofstream energy;
+    if (!energy_path.empty()) energy.open(energy_path);
+    auto t0 = std::chrono::steady_clock::now();
+    for (int ts = 0; ts < num_ts + 1; ts++) {
+      if (graph) check(epic_run(domain.handle(), 1, collisions, 1));
+      else check(epic_step(domain.handle(), collisions));
+      const bool diag = write_diag > 0 && ts % write_diag == 0;
+      const bool store = !energy_path.empty() && write_interval > 0 && ts % write_interval == 0;
+      if (!diag && !store) continue;
+      double ke_tot = 0;
+      std::vector<std::array<double, 3>> kes;
+      for (auto& sp : species) {
+        kes.push_back(sp->Compute_KE(*species[norm]));
+        ke_tot += kes.back()[0] + kes.back()[1] + kes.back()[2];
+      }
+      const double pe = domain.Compute_PE(norm);
+      if (store) {
+        energy << ts * cfg.DT;
+        for (auto& k : kes) energy << "," << k[0] << "," << k[1] << "," << k[2];
+        energy << "," << pe << "\n";
+      }
+      if (!diag || quiet) continue;
+      std::array<double, 3> mom{0, 0, 0};
+      for (auto& sp : species) {
+        auto p = sp->Compute_Momentum(*species[norm]);
+        for (int c = 0; c < 3; c++) mom[c] += p[c];
+      }
+      std::cout << "TS: " << ts << "\t" << "norm: " << domain.error << " delta_phi: " << std::fixed
+                << std::setprecision(2) << domain.delta_phi();
+      if (cfg.bc == EPIC_OPEN)
+        for (auto& sp : species) std::cout << " n_" << std::setw(4) << sp->name << ":" << sp->size();
+      if (cfg.bc == EPIC_PBC)
+        for (size_t s = 0; s < species.size(); s++)
+          std::cout << " KE_" << std::setw(4) << species[s]->name << ": " << std::fixed << std::setprecision(precision)
+                    << kes[s][0] + kes[s][1] + kes[s][2];
+      std::cout << " Potential_energy: " << std::fixed << std::setprecision(precision) << pe;
+      std::cout << " Kinetic_energy: " << ke_tot;
+      std::cout << " Total_energy: " << ke_tot + pe;
+      if (cfg.bc == EPIC_PBC)
+        std::cout << " p_x: " << mom[0] << " p_y: " << mom[1] << " p_z: " << mom[2];
+      std::cout << std::endl;
+      std::cout.unsetf(std::ios_base::floatfield);
+    }
+    auto t1 = std::chrono::steady_clock::now();
+    double sec = std::chrono::duration<double>(t1 - t0).count();
+    int64_t total = 0;
+    for (auto& sp : species) total += sp->size();
+    std::cout << "Elapsed time: " << sec << " seconds; " << (num_ts + 1) << " steps, " << total
+              << " particles, " << (double)total * (num_ts + 1) / sec << " particle-steps/s" << std::endl;
+  } catch (const std::exception& e) {
+    std::cerr << e.what() << std::endl;
+    return 1;
+  }
+  return 0;
+}

@@ -76,8 +76,15 @@ typedef struct {
   uint64_t seed;              /* Philox key */
   int warm_start;             /* 0: cold-start solves as the reference */
   int solver_blocks;          /* CTAs of the grid-wide solvers; 0 = automatic */
-  int reserved[15];
+  int precision;              /* EPIC_PRECISION_FP64 (the reference's arithmetic) | EPIC_PRECISION_MIXED */
+  int reserved[14];
 } epic_config;
+
+/* Mixed precision: particles as int32 cell + FP32 in-cell offsets + FP32
+ * velocities, integer CIC weights, and a Poisson solve whose inner step is
+ * FP32 (the exact sine-transform inverse of the same operator on square
+ * grids) inside FP64 defect correction to the same tolerance. */
+enum { EPIC_PRECISION_FP64 = 0, EPIC_PRECISION_MIXED = 1 };
 
 /* One [species] line of input.ini (src/main.cpp:132-149) after set-up. */
 typedef struct {
@@ -104,6 +111,11 @@ void epic_config_defaults(epic_config* cfg);
  * species lines; at most max_species descriptors are written. */
 epic_status epic_config_from_ini(const char* path, epic_config* cfg, epic_species_desc* species, int max_species,
                                  int* num_species, int* num_ts);
+
+/* INIParser::parse + getString (src/iniparser.cpp:4-66): copies the value of
+ * [section] key into out (NUL-terminated, at most len bytes).  EPIC_ERR_INVALID
+ * if the key is missing (the reference throws std::out_of_range). */
+epic_status epic_ini_get(const char* path, const char* section, const char* key, char* out, int len);
 
 /* Domain::Domain + FieldSolve::FieldSolve (src/domain.cpp:7-16, include/field.h:19). */
 epic_status epic_create(const epic_config* cfg, epic_sim** out);

@@ -1,0 +1,140 @@
+"""Mixed-precision form against the FP64 oracle.
+
+Stated errors (relative, max |a-b| / max |b|):
+* layout round trip: positions to FP32 in-cell resolution (<= 2^-23 cell),
+  velocities to FP32 rounding (<= 2^-24);
+* density: <= 1e-5 (offsets quantised to 2^-20 of a cell for the integer weights);
+* potential from the FP64-refined solve: <= 1e-5 against a tightly converged
+  FP64 solution, with the reference's own stopping norm below its tolerance;
+* one full step and ten steps: potential <= 1e-5, total energy <= 1e-5.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests import decks
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    a, b = np.asarray(a, float), np.asarray(b, float)
+    assert a.shape == b.shape
+    return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300))
+
+
+def mixed_sim(E, ini, **over):
+    return E.Simulation.from_ini(ini, precision=1, **over)
+
+
+def test_mixed_layout_round_trip(gpu_lib, tmp_path):
+    ini = decks.write(decks.deck(nx=64, ny=48, ne=50000, ni=50000, te=4), str(tmp_path))
+    orc = O.OracleSim(ini)
+    sim = mixed_sim(gpu_lib, ini)
+    for s in range(2):
+        sim.set_particles(s, orc.parts[s])
+        got = sim.particles(s)
+        assert np.max(np.abs(got[:, 0] - orc.parts[s][:, 0])) <= 2.0 ** -23 * orc.s.dx
+        assert np.max(np.abs(got[:, 1] - orc.parts[s][:, 1])) <= 2.0 ** -23 * orc.s.dy
+        assert rel(got[:, 2:], orc.parts[s][:, 2:]) <= 2.0 ** -24
+
+
+@pytest.mark.parametrize("bc", ["pbc", "open", "reflective"])
+@pytest.mark.parametrize("shape", ["CIC", "NGP"])
+def test_mixed_deposit(gpu_lib, tmp_path, bc, shape):
+    ini = decks.write(decks.deck(nx=48, ny=40, ne=60000, ni=60000, bc=bc, shape=shape), str(tmp_path))
+    orc = O.OracleSim(ini)
+    sim = mixed_sim(gpu_lib, ini)
+    for s in range(2):
+        sim.set_particles(s, orc.parts[s])
+    dens = [orc.R.scatter(orc.parts[s], orc.s.species[s].spwt) for s in range(2)]
+    for s in range(2):
+        sim.scatter_species(s)
+        assert rel(sim.den(s), dens[s]) < 1e-5
+    sim.compute_rho()
+    rho = orc.R.compute_rho(dens, [sp.charge for sp in orc.s.species])
+    assert np.max(np.abs(sim.grid("rho") - rho)) < 1e-5 * np.max(np.abs(dens[0]))
+
+
+@pytest.mark.parametrize("solver", ["cg", "gs"])
+@pytest.mark.parametrize("n", [32, 64, 128])
+def test_mixed_spectral_solve(gpu_lib, tmp_path, solver, n):
+    ini = decks.write(decks.deck(nx=n, ny=n, ne=n * n * 4, ni=n * n * 4, solver=solver, tol="1e-10",
+                                 maxit=200000), str(tmp_path))
+    orc = O.OracleSim(ini, initial_field=False)
+    orc.scatter_all()
+    sim = mixed_sim(gpu_lib, ini)
+    sim.set_grid("rho", orc.rho)
+    it, err, conv = sim.potential_solver()
+    assert conv and 1 <= it <= 5
+    if solver == "cg":
+        d = orc.R.d
+        d.tolerance = 1e-13
+        exact, _, _, _ = orc.R.pcg_solve(orc.rho)
+        assert err * (n + 1) ** 2 < 1e-10  # |Ax - b| / n, the reference's error figure
+    else:
+        d = orc.R.d
+        d.tolerance = 1e-13
+        exact, _, _, _ = orc.R.gs_solve(orc.rho, 1.9)
+        assert err < 1e-10  # SOR residual L2
+    assert rel(sim.grid("phi"), exact) < 1e-5
+
+
+def test_mixed_one_step_vs_fp64(gpu_lib, tmp_path):
+    ini = decks.write(decks.deck(nx=64, ny=64, ne=100000, ni=100000, solver="cg", tol="1e-10"), str(tmp_path))
+    orc = O.OracleSim(ini)
+    sim = mixed_sim(gpu_lib, ini)
+    for s in range(2):
+        sim.set_particles(s, orc.parts[s])
+    orc.step()
+    sim.step()
+    assert rel(sim.grid("phi"), orc.phi) < 1e-5
+    assert rel(sim.grid("efx"), orc.efx) < 1e-4
+    for s in range(2):
+        got = sim.particles(s)
+        assert np.max(np.abs(got[:, 0] - orc.parts[s][:, 0])) < 1e-5
+        assert rel(got[:, 2:4], orc.parts[s][:, 2:4]) < 1e-5
+
+
+def test_mixed_energy_tracks_fp64(gpu_lib, tmp_path):
+    """Ten loop iterations from the same start: total energy within 1e-5."""
+    ini = decks.write(decks.deck(nx=64, ny=64, ne=100000, ni=100000, solver="cg", tol="1e-10"), str(tmp_path))
+    orc = O.OracleSim(ini)
+    sim = mixed_sim(gpu_lib, ini)
+    sim.load_particles(0)
+    sim.initial_field()
+    for _ in range(10):
+        orc.step()
+        sim.step()
+    norm = orc.s.species[0]
+    ke_o = sum(orc.R.ke(sp, orc.parts[k], norm).sum() for k, sp in enumerate(orc.s.species))
+    pe_o = orc.R.pe(orc.efx, orc.efy, norm)
+    ke_g = sum(sim.compute_ke(k, 0).sum() for k in range(2))
+    pe_g = sim.compute_pe(0)
+    assert abs((ke_g + pe_g) - (ke_o + pe_o)) < 1e-5 * (ke_o + pe_o)
+    assert rel(sim.grid("phi"), orc.phi) < 1e-4
+
+
+def test_mixed_open_boundary_and_mcc(gpu_lib, tmp_path):
+    kw = dict(nx=32, ny=32, ne=30000, ni=30000, te=30, ion_mass="6.63352090e-26", collisions=True, gas="1e22",
+              bc="open", dt=0.05)
+    ini = decks.write(decks.deck(**kw), str(tmp_path))
+    orc = O.OracleSim(ini)
+    orc.step()
+    sim = mixed_sim(gpu_lib, ini, mcc_mode=1)
+    sim.set_reference_cross_sections()
+    for s in range(2):
+        sim.set_particles(s, orc.parts[s])
+    U = np.random.default_rng(7).random((len(orc.parts[0]), 16))
+    e, i, nc, kinds = orc.R.mcc(orc.parts[0], orc.parts[1], orc.s.species[1], uniforms=U)
+    got = sim.handle_collisions(0, 1, uniforms=U)
+    assert abs(got - nc) <= 2 and nc > 100
+    ge = sim.particles(0)
+    assert abs(len(ge) - len(e)) <= 2
+    # push with open walls: same survivors as the FP64 oracle
+    ex = np.random.default_rng(8).normal(size=orc.efx.shape)
+    sim.set_grid("efx", ex)
+    sim.set_grid("efy", ex)
+    ref = orc.R.push(orc.s.species[1], i, ex, ex)
+    sim.push_species(1)
+    assert abs(sim.num_particles(1) - len(ref)) <= 2
