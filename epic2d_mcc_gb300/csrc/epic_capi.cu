@@ -383,6 +383,10 @@ epic_status do_step(epic_sim* s, int with_collisions) {
 
 }  // namespace
 
+namespace epic {
+void set_last_error(const char* msg) { g_err = msg; }
+}  // namespace epic
+
 extern "C" {
 
 const char* epic_last_error(void) { return g_err.c_str(); }

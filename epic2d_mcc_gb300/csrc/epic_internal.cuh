@@ -201,6 +201,7 @@ struct SolverArgs {
   int warm;
 };
 void init_field_kernels();  // one-time kernel attributes (called by epic_create)
+void set_last_error(const char* msg);  // the message epic_last_error() returns on this thread
 void launch_sor_lex(cudaStream_t st, const SolverArgs& a);
 void launch_sor_redblack(cudaStream_t st, const SolverArgs& a, int blocks);
 void launch_pcg(cudaStream_t st, const SolverArgs& a, int blocks);

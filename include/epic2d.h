@@ -214,6 +214,28 @@ epic_status epic_set_profiling(epic_sim* sim, int enable);
 epic_status epic_get_profile(epic_sim* sim, double ms[EPIC_NUM_PHASES], int64_t counts[EPIC_NUM_PHASES],
                              int64_t* solver_iterations);
 
+/* PCG solve with no device allocation (no counterpart in the reference: its
+ * solver allocates dense matrices and vectors on every call).
+ *
+ * For callers that may not allocate GPU memory: frameworks whose memory pool
+ * or budget owns the GPU and forbids private allocations, plugins confined to
+ * the buffers their host hands them, and loops that must not meet the
+ * allocator's latency or an out-of-memory failure mid-run.  rho (input)
+ * and phi (output) are device arrays of nx*ny doubles in the reference's
+ * layout (node (i, j) at i*ny + j); K = (L/LDe)^2.  The solve is the same as
+ * epic_potential_solver with solvertype cg (same kernel and launch shape, so
+ * the same phi), with all workspace in one static device array compiled into
+ * the library: at most 257 x 257 nodes (larger grids return
+ * EPIC_ERR_CAPACITY).  Every GPU that loads the library holds that array
+ * (about 4.3 MB) until the library is unloaded.  The first call on each
+ * device looks up the array's device address; make that first call before
+ * any stream capture.  All calls share the array and leave their data in
+ * it; calls whose GPU work overlaps race, so order them on one stream.
+ * stream is a cudaStream_t (NULL: the default stream); the call waits for it. */
+epic_status epic_pcg_solve_static(const double* rho, double* phi, int nx, int ny, double dx, double K,
+                                  double tolerance, int max_iteration, void* stream, int* iterations,
+                                  double* error);
+
 #ifdef __cplusplus
 }
 #endif
