@@ -272,7 +272,9 @@ epic_status do_solve(epic_sim* s) {
     if (s->cfg.sor_mode == EPIC_SOR_LEXICOGRAPHIC) launch_sor_lex(s->stream, a);
     else launch_sor_redblack(s->stream, a, solver_blocks(s, 1024));
   } else {
-    launch_pcg(s->stream, a, solver_blocks(s, 512));
+    const int nb = s->cfg.solver_blocks > 0 ? std::min(s->cfg.solver_blocks, solver_max_blocks())
+                                            : pcg_default_blocks(nnodes(s), s->num_sms);
+    launch_pcg(s->stream, a, nb);
   }
   s->launches += 1;
   CKL();
@@ -462,7 +464,8 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   guard(dalloc(&s->efy, nn));
   guard(dalloc(&s->ef, nn));
   for (int k = 0; k < 8; k++) guard(dalloc(&s->work[k], nn));
-  guard(dalloc(&s->partials, 4 * (size_t)std::max(solver_max_blocks(), 256)));
+  // Solver partials: up to 2 parities x 48 bytes per CTA (PCG), 16 doubles per CTA.
+  guard(dalloc(&s->partials, 16 * (size_t)std::max(solver_max_blocks(), 320)));
   guard(dalloc(&s->bar, 2));
   guard(dalloc(&s->d_info, 1));
   guard(dalloc(&s->d_iter_total, 1));

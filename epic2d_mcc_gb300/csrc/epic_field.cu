@@ -6,7 +6,10 @@
 // the PCG kernel uses explicit fma() where it is documented to.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "epic_internal.cuh"
+#include "epic_xsum.cuh"
 
 namespace epic {
 
@@ -424,7 +427,10 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
   double* S[2] = {a.work[3], a.work[4]};
   double* W[2] = {a.work[5], a.work[6]};
   double* Pd = a.work[7];
-  double* P = a.partials;  // [nb][4]
+  // Partials [2][nb][4], alternating by reduction episode: a block can run
+  // at most one reduction ahead of the slowest reader.
+  int ep = 0;
+  auto Pb = [&](int e) { return a.partials + (e & 1) * 4 * nb; };
   const double minv = 1.0 / -4.0;
   const double dx2 = a.g.dx * a.g.dx;
 
@@ -452,7 +458,7 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
     pd = fma(sum, uk, pd);
     pr = fma(rk, rk, pr);
   }
-  block_partial3(pg, pd, pr, P, sw);
+  block_partial3(pg, pd, pr, Pb(ep), sw);
   if (!grid_sync(a.bar, a.flags)) return;
   unsigned int cap32 = (unsigned int)n * (unsigned int)n;
   const int maxit = (int)cap32 < a.max_iter ? (int)cap32 : a.max_iter;
@@ -477,7 +483,7 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
     s_beta = beta;
   };
   {
-    double3 t = grid_total3_t0(P, nb);
+    double3 t = grid_total3_t0(Pb(ep++), nb);
     if (threadIdx.x == 0) scalars(t);
     __syncthreads();
   }
@@ -521,12 +527,12 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
       pd = fma(sum, uk, pd);
       pr = fma(rk, rk, pr);
     }
-    block_partial3(pg, pd, pr, P, sw);
+    block_partial3(pg, pd, pr, Pb(ep), sw);
     if (!grid_sync(a.bar, a.flags)) return;
     cur ^= 1;
     it++;
     {
-      double3 t = grid_total3_t0(P, nb);
+      double3 t = grid_total3_t0(Pb(ep++), nb);
       if (threadIdx.x == 0) scalars(t);
       __syncthreads();
     }
@@ -545,9 +551,9 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
     const double e = sum - b[k];
     pe = fma(e, e, pe);
   }
-  block_partial3(pe, 0.0, 0.0, P, sw);
+  block_partial3(pe, 0.0, 0.0, Pb(ep), sw);
   if (!grid_sync(a.bar, a.flags)) return;
-  double3 e2 = grid_total3_t0(P, nb);
+  double3 e2 = grid_total3_t0(Pb(ep++), nb);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.info->iterations = it;
     a.info->converged = it < maxit;
@@ -570,10 +576,529 @@ int solver_max_blocks() {
   return g_pcg_max_blocks;
 }
 
+// ------------------------------------------------------ tiled PCG ---
+// The same Chronopoulos-Gear iteration as k_pcg, with the unknowns held in
+// registers for the whole solve.  The lattice of unknowns (R = ny rows of
+// C = nx columns, row = k / nx as in the reference's dense A) is cut into
+// one tr x tc tile per CTA; each thread owns up to NPT nodes of its tile and
+// keeps their x, r, w, p, s in registers.  The stencil reads r from a
+// shared-memory copy of the tile with a one-node halo ring: halo nodes belong
+// to neighbouring tiles, whose owners publish r, w, s of their edge nodes
+// (double-buffered by iteration parity) before the grid barrier, so after it
+// each CTA recomputes the halo's new r - alpha(w + beta s) from them.
+//
+// Exact identities of the constant Jacobi diagonal -4 remove M from the
+// loop: with u = M r = -r/4 every product with u is an exact power-of-two
+// scaling, so w = A u = fma(-1/4, sum of the neighbours' r, r), (w, u) =
+// -(w, r)/4, gamma = (r, u) = -(r, r)/4, and p is kept as p' = -4p (p' = r +
+// beta p', x += (-alpha/4) p').  All of these round exactly as the unscaled
+// forms do.  That leaves 10 FP64 operations per node and iteration, and the
+// p'/x updates (needed only for the answer) run while the CTA waits at the
+// grid barrier, so 8 are on the critical path.  The iteration's scalars need
+// one division there: beta = gamma * (1/gamma_prev), with the reciprocal
+// formed after the previous broadcast, and eta = delta - beta*gamma/alpha_prev
+// = delta - beta*(beta*eta_prev) since alpha_prev = gamma_prev/eta_prev.
+struct PcgTiling {
+  int tr, tc;          // tile rows, columns
+  int tiles_c;         // tiles per lattice row
+  int blocks;          // CTAs (tiles)
+  int npt;             // owned-node slots per thread
+};
+
+constexpr int PCG_T = 256;
+constexpr int PCG_HALO_SLOTS = 2;    // halo nodes per thread (the halo ring holds <= 512)
+constexpr int PCG_MAX_BLOCKS = 160;  // partial records read per lane: PCG_MAX_BLOCKS / 32
+
+// Split grid barrier: each CTA counts its own barrier episodes, so arriving
+// needs no returned ticket (a fire-and-forget red.release by thread 0 after a
+// __syncthreads that orders the block's writes before it), and work that no
+// other CTA needs can run between arriving and waiting.
+__device__ __forceinline__ void bar_arrive(unsigned int* bar) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(bar), "r"(1u) : "memory");
+}
+
+// Waits until `target` arrivals are in (bounded: FLAG_TIMEOUT and false on
+// giving up).  Ends with a __syncthreads.
+__device__ __forceinline__ bool bar_wait(unsigned int* bar, int* flags, unsigned int target, int* s_ok) {
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    long long spins = 0;
+    while ((int)(ld_acquire_gpu(bar) - target) < 0) {
+      if (++spins > SPIN_LIMIT) {
+        atomicOr(flags, FLAG_TIMEOUT);
+        ok = 0;
+        break;
+      }
+    }
+    *s_ok = ok;
+  }
+  __syncthreads();
+  return *s_ok;
+}
+
+// ---- exact dot-product reductions (integer pipe, see epic_xsum.cuh) ----
+// Warp total of 128-bit fixed-point values: five 26-bit limbs (the top one
+// signed) summed with redux.sync — a limb total of 32 lanes stays below 2^31
+// for |v| < 2^122 — and recombined exactly.
+__device__ __forceinline__ xs_int xs_warp_sum(xs_int v) {
+  const xs_uint u = (xs_uint)v;
+  const unsigned M = (1u << 26) - 1;
+  const int l0 = __reduce_add_sync(0xffffffffu, (int)((unsigned)u & M));
+  const int l1 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 26) & M));
+  const int l2 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 52) & M));
+  const int l3 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 78) & M));
+  const int l4 = __reduce_add_sync(0xffffffffu, (int)(v >> 104));
+  const xs_uint s = ((xs_uint)(xs_int)l4 << 104) + ((xs_uint)(unsigned)l3 << 78) + ((xs_uint)(unsigned)l2 << 52) +
+                    ((xs_uint)(unsigned)l1 << 26) + (xs_uint)(unsigned)l0;
+  return (xs_int)s;
+}
+
+// One CTA's exact partial of two dot products: V = sum * 2^(1129 - a).
+struct XPartial {
+  unsigned long long lo[2];
+  long long hi[2];
+  int a[2];
+  int pad[2];
+};
+
+struct XScratch {
+  int e[2][PCG_T / 32];
+  unsigned long long v[2][PCG_T / 32][2];
+};
+
+// Block partial of the terms t0[j], t1[j] (j < NT) of every thread; thread 0
+// stores it to *out.  Two __syncthreads (anchor exponents, warp totals).
+template <int NT>
+__device__ __forceinline__ void xs_block_partial(const double (&t0)[NT], const double (&t1)[NT], XScratch& sx,
+                                                 XPartial* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int e0 = 0, e1 = 0;
+#pragma unroll
+  for (int j = 0; j < NT; j++) {
+    e0 = max(e0, xs_exponent(t0[j]));
+    e1 = max(e1, xs_exponent(t1[j]));
+  }
+  e0 = (int)__reduce_max_sync(0xffffffffu, (unsigned)e0);
+  e1 = (int)__reduce_max_sync(0xffffffffu, (unsigned)e1);
+  if (lane == 0) {
+    sx.e[0][wid] = e0;
+    sx.e[1][wid] = e1;
+  }
+  __syncthreads();
+  int A0 = 0, A1 = 0;
+#pragma unroll
+  for (int w = 0; w < PCG_T / 32; w++) {
+    A0 = max(A0, sx.e[0][w]);
+    A1 = max(A1, sx.e[1][w]);
+  }
+  xs_int v0 = 0, v1 = 0;
+#pragma unroll
+  for (int j = 0; j < NT; j++) {
+    v0 += xs_from_double(t0[j], A0);
+    v1 += xs_from_double(t1[j], A1);
+  }
+  v0 = xs_warp_sum(v0);
+  v1 = xs_warp_sum(v1);
+  if (lane == 0) {
+    sx.v[0][wid][0] = (unsigned long long)(xs_uint)v0;
+    sx.v[0][wid][1] = (unsigned long long)((xs_uint)v0 >> 64);
+    sx.v[1][wid][0] = (unsigned long long)(xs_uint)v1;
+    sx.v[1][wid][1] = (unsigned long long)((xs_uint)v1 >> 64);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    xs_uint s0 = 0, s1 = 0;
+#pragma unroll
+    for (int w = 0; w < PCG_T / 32; w++) {
+      s0 += ((xs_uint)sx.v[0][w][1] << 64) | sx.v[0][w][0];
+      s1 += ((xs_uint)sx.v[1][w][1] << 64) | sx.v[1][w][0];
+    }
+    XPartial p;
+    p.lo[0] = (unsigned long long)s0;
+    p.hi[0] = (long long)(s0 >> 64);
+    p.lo[1] = (unsigned long long)s1;
+    p.hi[1] = (long long)(s1 >> 64);
+    p.a[0] = A0;
+    p.a[1] = A1;
+    p.pad[0] = p.pad[1] = 0;
+    *out = p;
+  }
+}
+
+// Grid totals of the nb partials, by warp 0 (all loads issued first); the
+// doubles are valid in thread 0.
+__device__ __forceinline__ void xs_grid_totals_w0(const XPartial* Pc, int nb, double* out0, double* out1) {
+  constexpr int Q = PCG_MAX_BLOCKS / 32;
+  ulonglong2 r01[Q], r23[Q];
+  int2 ra[Q];
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    const int k = threadIdx.x + 32 * q;
+    if (k < nb) {
+      const ulonglong2* rec = reinterpret_cast<const ulonglong2*>(Pc + k);
+      r01[q] = __ldcg(rec);
+      r23[q] = __ldcg(rec + 1);
+      ra[q] = __ldcg(reinterpret_cast<const int2*>(rec + 2));
+    } else {
+      r01[q] = make_ulonglong2(0, 0);
+      r23[q] = make_ulonglong2(0, 0);
+      ra[q] = make_int2(0, 0);
+    }
+  }
+  int a0 = 0, a1 = 0;
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    a0 = max(a0, ra[q].x);
+    a1 = max(a1, ra[q].y);
+  }
+  const int A0 = (int)__reduce_max_sync(0xffffffffu, (unsigned)a0);
+  const int A1 = (int)__reduce_max_sync(0xffffffffu, (unsigned)a1);
+  xs_int s0 = 0, s1 = 0;
+#pragma unroll
+  for (int q = 0; q < Q; q++) {
+    // record layout: lo[0], lo[1] | hi[0], hi[1] | a[0], a[1]
+    const xs_int v0 = (xs_int)(((xs_uint)r23[q].x << 64) | r01[q].x);
+    const xs_int v1 = (xs_int)(((xs_uint)r23[q].y << 64) | r01[q].y);
+    s0 += xs_realign(v0, ra[q].x, A0);
+    s1 += xs_realign(v1, ra[q].y, A1);
+  }
+  s0 = xs_warp_sum(s0);
+  s1 = xs_warp_sum(s1);
+  // Lanes 0 and 1 round one total each, side by side.
+  const double d = xs_to_double(threadIdx.x == 0 ? s0 : s1, threadIdx.x == 0 ? A0 : A1);
+  const double d1 = __shfl_sync(0xffffffffu, d, 1);
+  if (threadIdx.x == 0) {
+    *out0 = d;
+    *out1 = d1;
+  }
+}
+
+// 1/x by Newton-Raphson (y <- y + y(1 - m y), two steps) on the significand m
+// of x, seeded with the FP32 reciprocal of m's leading 24 bits: the ~2^-23
+// seed error squares to below FP64 rounding, so the result is within about
+// one ulp of 1/x (not correctly rounded).  The exponent is applied in the
+// integer domain.  Four dependent FP64 operations in all, against a library
+// division's longer sequence; for x and 1/x in the normal range (otherwise
+// the library division is used).
+__device__ __forceinline__ double recip_nr(double x) {
+  const uint64_t b = xs_bits(x);
+  const int e = (int)((b >> 52) & 0x7FF);
+  const uint64_t sign = b & (1ull << 63);
+  if (e == 0 || e >= 2046) return 1.0 / x;
+  const double m = xs_double((b & 0xFFFFFFFFFFFFFull) | (1023ull << 52));  // |x| scaled to [1, 2)
+  const float mf = __int_as_float(0x3F800000 | (int)((b >> 29) & 0x7FFFFF));
+  const float yf = __frcp_rn(mf);  // in (0.5, 1]
+  const unsigned yb = (unsigned)__float_as_int(yf);
+  double y = xs_double(((uint64_t)(((yb >> 23) & 0xFF) - 127 + 1023) << 52) | ((uint64_t)(yb & 0x7FFFFF) << 29));
+  double t = fma(-m, y, 1.0);
+  y = fma(y, t, y);
+  t = fma(-m, y, 1.0);
+  y = fma(y, t, y);
+  const uint64_t rb = xs_bits(y);
+  const long er = (long)((rb >> 52) & 0x7FF) + 1023 - e;
+  if (er <= 0 || er >= 2047) return 1.0 / x;
+  return xs_double(sign | ((uint64_t)er << 52) | (rb & 0xFFFFFFFFFFFFFull));
+}
+
+template <int NPT>
+__global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) {
+  extern __shared__ double sr[];  // r of the tile and its halo ring, (tr + 2) x (tc + 2)
+  __shared__ XScratch sx;
+  __shared__ double s_alpha, s_beta;
+  __shared__ int s_done, s_ok;
+  const int C = a.g.nx, R = a.g.ny;
+  const int n = C * R;
+  const int tr = t.tr, tc = t.tc, ldu = tc + 2;
+  const int br = blockIdx.x / t.tiles_c, bc = blockIdx.x - br * t.tiles_c;
+  const int r0 = br * tr, c0 = bc * tc;
+  const int nb = gridDim.x;
+  const double dx2 = a.g.dx * a.g.dx;
+  // Partials [2][nb] alternate by reduction parity (a CTA can run at most one
+  // reduction ahead of the slowest reader); published edge values likewise:
+  // work[1|2] = r, work[3|4] = w, work[5|6] = s.
+  XPartial* const P = reinterpret_cast<XPartial*>(a.partials);
+  unsigned int target = 0;
+
+  for (int m = threadIdx.x; m < (tr + 2) * ldu; m += PCG_T) sr[m] = 0.0;
+
+  // Owned slots: tile-local q = threadIdx.x + PCG_T*j, row-major in the tile.
+  int kk[NPT], si[NPT];
+  bool pub[NPT];
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    const int q = threadIdx.x + PCG_T * j;
+    const int lr = q / tc, lc = q - lr * tc;
+    const int row = r0 + lr, col = c0 + lc;
+    const bool valid = q < tr * tc && row < R && col < C;
+    kk[j] = valid ? row * C + col : -1;
+    si[j] = (lr + 1) * ldu + lc + 1;
+    pub[j] = valid && (lr == 0 || lr == tr - 1 || lc == 0 || lc == tc - 1);
+  }
+  // Halo slots: top row, bottom row, left column, right column of the ring.
+  int hk[PCG_HALO_SLOTS], hs[PCG_HALO_SLOTS];
+#pragma unroll
+  for (int j = 0; j < PCG_HALO_SLOTS; j++) {
+    const int h = threadIdx.x + PCG_T * j;
+    int row = -1, col = -1, sr_ = 0, sc = 0;
+    if (h < tc) {
+      row = r0 - 1; col = c0 + h; sr_ = 0; sc = h + 1;
+    } else if (h < 2 * tc) {
+      row = r0 + tr; col = c0 + h - tc; sr_ = tr + 1; sc = h - tc + 1;
+    } else if (h < 2 * tc + tr) {
+      row = r0 + h - 2 * tc; col = c0 - 1; sr_ = h - 2 * tc + 1; sc = 0;
+    } else if (h < 2 * tc + 2 * tr) {
+      row = r0 + h - 2 * tc - tr; col = c0 + tc; sr_ = h - 2 * tc - tr + 1; sc = tc + 1;
+    }
+    const bool valid = row >= 0 && row < R && col >= 0 && col < C;
+    hk[j] = valid ? row * C + col : -1;
+    hs[j] = sr_ * ldu + sc;
+  }
+  __syncthreads();
+
+  // set-up: x = 0, r = b, w = A(M r), p' = s = 0.
+  double x[NPT], r[NPT], w[NPT], p[NPT], s[NPT], r_old[NPT];
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    x[j] = r[j] = w[j] = p[j] = s[j] = r_old[j] = 0.0;
+    if (kk[j] >= 0) {
+      const int k = kk[j], i = k / a.g.ny;
+      r[j] = rhs_at(a, k, i, k - i * a.g.ny, dx2);
+      sr[si[j]] = r[j];
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < PCG_HALO_SLOTS; j++)
+    if (hk[j] >= 0) {
+      const int k = hk[j], i = k / a.g.ny;
+      sr[hs[j]] = rhs_at(a, k, i, k - i * a.g.ny, dx2);
+    }
+  __syncthreads();
+  // Dot-product terms of this thread's nodes: (w, r) and (r, r).
+  double td[NPT], tq[NPT];
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    td[j] = tq[j] = 0.0;
+    if (kk[j] >= 0) {
+      const double* c = sr + si[j];
+      w[j] = fma(-0.25, (c[-ldu] + c[-1]) + (c[1] + c[ldu]), r[j]);
+      td[j] = w[j] * r[j];
+      tq[j] = r[j] * r[j];
+      if (pub[j]) {
+        a.work[1][kk[j]] = r[j];
+        a.work[3][kk[j]] = w[j];
+        a.work[5][kk[j]] = 0.0;
+      }
+    }
+  }
+
+  unsigned int cap32 = (unsigned int)n * (unsigned int)n;
+  const int maxit = (int)cap32 < a.max_iter ? (int)cap32 : a.max_iter;
+  // Thread 0's scalars, in the scaled form: rr = (r, r) = -4 gamma,
+  // dr = (w, r) = -4 delta, eta_r = -4 eta; then beta = rr / rr_prev,
+  // eta_r = dr - beta*(beta*eta_r_prev), alpha = rr / eta_r.
+  double rr_cur = 0, rr_inv = 0, eta_prev = 0;
+  double be = 0, alq = 0;  // this iteration's beta and -alpha/4
+  int it = 0;
+  for (;;) {
+    XPartial* const Pc = P + (it & 1) * nb;
+    xs_block_partial<NPT>(td, tq, sx, Pc + blockIdx.x);
+    if (threadIdx.x == 0) bar_arrive(a.bar);
+    target += nb;
+    // Deferred update of the previous iteration (no other CTA needs p' or x),
+    // and the reciprocal the next beta needs.
+    if (it > 0) {
+#pragma unroll
+      for (int j = 0; j < NPT; j++)
+        if (kk[j] >= 0) {
+          p[j] = fma(be, p[j], r_old[j]);
+          x[j] = fma(alq, p[j], x[j]);
+        }
+      if (threadIdx.x == 0) rr_inv = recip_nr(rr_cur);
+    }
+    if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
+    // Halo inputs published before the barrier, loaded while warp 0 sums the
+    // partials.
+    const int cur = it & 1;
+    const double* const pr_c = cur ? a.work[2] : a.work[1];
+    const double* const pw_c = cur ? a.work[4] : a.work[3];
+    const double* const ps_c = cur ? a.work[6] : a.work[5];
+    double hr[PCG_HALO_SLOTS], hw[PCG_HALO_SLOTS], hsv[PCG_HALO_SLOTS];
+#pragma unroll
+    for (int j = 0; j < PCG_HALO_SLOTS; j++)
+      if (hk[j] >= 0) {
+        hr[j] = __ldcg(&pr_c[hk[j]]);
+        hw[j] = __ldcg(&pw_c[hk[j]]);
+        hsv[j] = __ldcg(&ps_c[hk[j]]);
+      }
+    if (threadIdx.x < 32) {
+      double dr = 0, rr = 0;
+      xs_grid_totals_w0(Pc, nb, &dr, &rr);
+      if (threadIdx.x == 0) {
+        rr_cur = rr;
+        s_done = xs_bits(rr) < a.tol_bits || it >= maxit;  // sqrt(r.r) < tol
+        double beta, eta_r;
+        if (it == 0) {
+          beta = 0;
+          eta_r = dr;
+        } else {
+          beta = rr * rr_inv;
+          eta_r = fma(-beta, beta * eta_prev, dr);
+        }
+        eta_prev = eta_r;
+        s_alpha = rr * recip_nr(eta_r);
+        s_beta = beta;
+      }
+    }
+    __syncthreads();
+    if (s_done) break;
+    const double al = s_alpha;
+    be = s_beta;
+    alq = -0.25 * al;
+#pragma unroll
+    for (int j = 0; j < NPT; j++)
+      if (kk[j] >= 0) {
+        r_old[j] = r[j];
+        s[j] = fma(be, s[j], w[j]);
+        r[j] = fma(-al, s[j], r[j]);
+        sr[si[j]] = r[j];
+      }
+#pragma unroll
+    for (int j = 0; j < PCG_HALO_SLOTS; j++)
+      if (hk[j] >= 0) sr[hs[j]] = fma(-al, fma(be, hsv[j], hw[j]), hr[j]);
+    __syncthreads();
+    double* const pr_n = cur ? a.work[1] : a.work[2];
+    double* const pw_n = cur ? a.work[3] : a.work[4];
+    double* const ps_n = cur ? a.work[5] : a.work[6];
+#pragma unroll
+    for (int j = 0; j < NPT; j++)
+      if (kk[j] >= 0) {
+        const double* c = sr + si[j];
+        w[j] = fma(-0.25, (c[-ldu] + c[-1]) + (c[1] + c[ldu]), r[j]);
+        td[j] = w[j] * r[j];
+        tq[j] = r[j] * r[j];
+        if (pub[j]) {
+          pr_n[kk[j]] = r[j];
+          pw_n[kk[j]] = w[j];
+          ps_n[kk[j]] = s[j];
+        }
+      }
+    it++;
+  }
+  // domain.error = |A x - b| / n (src/field.cpp:258-259).
+#pragma unroll
+  for (int j = 0; j < NPT; j++)
+    if (kk[j] >= 0) a.phi[kk[j]] = x[j];
+  __syncthreads();
+  if (threadIdx.x == 0) bar_arrive(a.bar);
+  target += nb;
+  if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
+#pragma unroll
+  for (int j = 0; j < NPT; j++) {
+    td[j] = tq[j] = 0.0;
+    if (kk[j] >= 0) {
+      const int k = kk[j], row = k / C, col = k - row * C, i = k / a.g.ny;
+      double sum = 0;
+      if (row > 0) sum += __ldcg(&a.phi[k - C]);
+      if (col > 0) sum += __ldcg(&a.phi[k - 1]);
+      sum = fma(-4.0, x[j], sum);
+      if (col < C - 1) sum += __ldcg(&a.phi[k + 1]);
+      if (row < R - 1) sum += __ldcg(&a.phi[k + C]);
+      const double e = sum - rhs_at(a, k, i, k - i * a.g.ny, dx2);
+      td[j] = e * e;
+    }
+  }
+  XPartial* const Pe = P + ((it + 1) & 1) * nb;
+  xs_block_partial<NPT>(td, tq, sx, Pe + blockIdx.x);
+  if (threadIdx.x == 0) bar_arrive(a.bar);
+  target += nb;
+  if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
+  if (blockIdx.x == 0 && threadIdx.x < 32) {
+    double e2 = 0, unused = 0;
+    xs_grid_totals_w0(Pe, nb, &e2, &unused);
+    if (threadIdx.x == 0) {
+      a.info->iterations = it;
+      a.info->converged = it < maxit;
+      a.info->error = sqrt(e2) / n;
+      atomicAdd(a.iter_total, (unsigned long long)it);
+    }
+  }
+}
+
+// Tile shape for at most max_blocks CTAs: the fewest FP64 operations on the
+// busiest CTA (11 per owned node, 3 per halo node), ties to fewer CTAs.
+// Returns false when no tile fits PCG_T * 8 owned nodes and a halo ring of
+// PCG_T * PCG_HALO_SLOTS nodes (then the global-memory k_pcg runs).
+static bool pcg_tiling(int R, int C, int max_blocks, PcgTiling* out) {
+  long long best = -1;
+  PcgTiling b{};
+  for (int tcb = 1; tcb <= C && tcb <= max_blocks; tcb++) {
+    const int tc = (C + tcb - 1) / tcb;
+    const int ncb = (C + tc - 1) / tc;
+    const int rb_max = max_blocks / ncb;
+    if (rb_max < 1) continue;
+    const int tr = (R + rb_max - 1) / rb_max;
+    const int nrb = (R + tr - 1) / tr;
+    const long long nodes = (long long)tr * tc;
+    if (nodes > PCG_T * 8 || 2LL * (tr + tc) > PCG_T * PCG_HALO_SLOTS) continue;
+    if (ncb * nrb > PCG_MAX_BLOCKS) continue;
+    const long long cost = 11 * nodes + 3 * 2LL * (tr + tc);
+    const int blocks = ncb * nrb;
+    if (best < 0 || cost < best || (cost == best && blocks < b.blocks)) {
+      best = cost;
+      b.tr = tr;
+      b.tc = tc;
+      b.tiles_c = ncb;
+      b.blocks = blocks;
+      const int npt = (int)((nodes + PCG_T - 1) / PCG_T);
+      b.npt = npt <= 1 ? 1 : npt <= 2 ? 2 : npt <= 4 ? 4 : 8;
+    }
+  }
+  if (best < 0) return false;
+  *out = b;
+  return true;
+}
+
+int pcg_default_blocks(long long nodes, int sms) {
+  // One CTA per SM at most (FP64 throughput is per SM; more CTAs only add
+  // barrier arrivals), and no fewer than ~384 nodes per CTA on small grids.
+  long long want = (nodes + 383) / 384;
+  return (int)std::max(1LL, std::min<long long>(want, std::min(solver_max_blocks(), sms)));
+}
+
+// Launches the tiled solve if all its CTAs can be resident at once (the
+// cooperative-launch condition); returns false otherwise.
+template <int NPT>
+static bool launch_tiled(cudaStream_t st, const SolverArgs& a, const PcgTiling& t) {
+  const int smem = (t.tr + 2) * (t.tc + 2) * (int)sizeof(double);
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg_tiled<NPT>, PCG_T, smem);
+  if (t.blocks > per_sm * sms) return false;
+  SolverArgs args = a;
+  PcgTiling tl = t;
+  void* params[] = {&args, &tl};
+  cudaLaunchCooperativeKernel((const void*)k_pcg_tiled<NPT>, dim3(t.blocks), dim3(PCG_T), params, smem, st);
+  return true;
+}
+
 void launch_pcg(cudaStream_t st, const SolverArgs& a, int blocks) {
+  cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned int), st);
+  PcgTiling t;
+  if (pcg_tiling(a.g.ny, a.g.nx, blocks, &t)) {
+    SolverArgs at = a;
+    at.tol_bits = xs_bits(xs_sqrt_threshold(a.tol));
+    bool ok;
+    switch (t.npt) {
+      case 1: ok = launch_tiled<1>(st, at, t); break;
+      case 2: ok = launch_tiled<2>(st, at, t); break;
+      case 4: ok = launch_tiled<4>(st, at, t); break;
+      default: ok = launch_tiled<8>(st, at, t); break;
+    }
+    if (ok) return;
+  }
   SolverArgs args = a;
   void* params[] = {&args};
-  cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned int), st);
   cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(blocks), dim3(256), params, 0, st);
 }
 

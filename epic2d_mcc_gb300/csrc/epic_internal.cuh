@@ -199,6 +199,7 @@ struct SolverArgs {
   double* partials;  // 4 * max_blocks
   unsigned int* bar; // grid barrier {count, generation}
   int warm;
+  unsigned long long tol_bits;  // PCG stop test: sqrt(r.r) < tol <=> bits(r.r) < tol_bits (set by launch_pcg)
 };
 void init_field_kernels();  // one-time kernel attributes (called by epic_create)
 void set_last_error(const char* msg);  // the message epic_last_error() returns on this thread
@@ -206,6 +207,9 @@ void launch_sor_lex(cudaStream_t st, const SolverArgs& a);
 void launch_sor_redblack(cudaStream_t st, const SolverArgs& a, int blocks);
 void launch_pcg(cudaStream_t st, const SolverArgs& a, int blocks);
 int solver_max_blocks();
+// CTA budget of a PCG solve on `nodes` unknowns (shared by every entry point
+// that runs it, so they all produce the same iterates).
+int pcg_default_blocks(long long nodes, int sms);
 void launch_grid_sums(cudaStream_t st, int what, const Geom& g, const double* a, const double* b, double L,
                       double* partials, double* out);
 

@@ -34,11 +34,11 @@ using namespace epic;
 
 constexpr int PCG_STATIC_MAX_NODES = 257 * 257;
 constexpr int PCG_STATIC_MAX_BLOCKS = 1024;
-// 8 node vectors + 4 partials per block + barrier counter, solve outcome,
+// 8 node vectors + 2 x 4 partials per block + barrier counter, solve outcome,
 // iteration total and error flags, each section 256-byte aligned.
 constexpr size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 constexpr size_t PCG_VEC_BYTES = align256((size_t)PCG_STATIC_MAX_NODES * sizeof(double));
-constexpr size_t PCG_PART_BYTES = align256((size_t)4 * PCG_STATIC_MAX_BLOCKS * sizeof(double));
+constexpr size_t PCG_PART_BYTES = align256((size_t)8 * PCG_STATIC_MAX_BLOCKS * sizeof(double));
 constexpr size_t PCG_STATIC_BYTES = 8 * PCG_VEC_BYTES + PCG_PART_BYTES + 4 * 256;
 
 static __device__ __align__(256) unsigned char g_pcg_scratch[PCG_STATIC_BYTES];
@@ -113,12 +113,10 @@ epic_status epic_pcg_solve_static(const double* rho, double* phi, int nx, int ny
   a.info = reinterpret_cast<SolveInfo*>(tail + 256);
   a.iter_total = reinterpret_cast<unsigned long long*>(tail + 512);
   a.flags = reinterpret_cast<int*>(tail + 768);
-  // Same CTA count as the epic_sim path (one per 512 nodes, at most one per
-  // SM), so both give identical results.
+  // Same CTA count as the epic_sim path, so both give identical results.
   int sms = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int blocks = (int)std::min<long long>(((long long)nx * ny + 511) / 512, std::min(solver_max_blocks(), sms));
-  blocks = std::max(1, std::min(blocks, PCG_STATIC_MAX_BLOCKS));
+  int blocks = std::max(1, std::min(pcg_default_blocks((long long)nx * ny, sms), PCG_STATIC_MAX_BLOCKS));
   // Zero what the kernel expects zeroed (the barrier counter is also reset
   // inside launch_pcg); the rest is written before it is read.
   if ((e = cudaMemsetAsync(a.flags, 0, sizeof(int), s)) != cudaSuccess ||
