@@ -46,7 +46,8 @@ class Config(ctypes.Structure):
                 ("elastic", ctypes.c_int), ("excitation", ctypes.c_int), ("ionization", ctypes.c_int),
                 ("sor_omega", ctypes.c_double), ("sor_mode", ctypes.c_int), ("deposit_mode", ctypes.c_int),
                 ("mcc_mode", ctypes.c_int), ("seed", ctypes.c_uint64), ("warm_start", ctypes.c_int),
-                ("solver_blocks", ctypes.c_int), ("precision", ctypes.c_int), ("reserved", ctypes.c_int * 14)]
+                ("solver_blocks", ctypes.c_int), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
+                ("reserved", ctypes.c_int * 13)]
 
 
 class SpeciesDesc(ctypes.Structure):
@@ -86,6 +87,7 @@ def lib() -> ctypes.CDLL:
         "epic_calculate_efield": ([vp], st),
         "epic_push_species": ([vp, i, i], st),
         "epic_rewind_species": ([vp, i], st),
+        "epic_sort_species": ([vp, i], st),
         "epic_set_cross_sections": ([vp, vp, vp, vp, vp, i64, d], st),
         "epic_set_reference_cross_sections": ([vp], st),
         "epic_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
@@ -224,6 +226,10 @@ class Simulation:
     def rewind_species(self, sp: int):
         _check(lib().epic_rewind_species(self._h, sp))
 
+    def sort_species(self, sp: int):
+        """Stable sort of the species' particles by cell (i*ny + j)."""
+        _check(lib().epic_sort_species(self._h, sp))
+
     def set_reference_cross_sections(self):
         _check(lib().epic_set_reference_cross_sections(self._h))
 
@@ -298,15 +304,15 @@ class Simulation:
     def stream(self) -> int:
         return lib().epic_stream(self._h) or 0
 
-    PHASES = ("deposit", "finalize", "solve", "efield", "push", "mcc")
+    PHASES = ("deposit", "finalize", "solve", "efield", "push", "mcc", "sort")
 
     def set_profiling(self, on: bool = True):
         _check(lib().epic_set_profiling(self._h, int(on)))
 
     def profile(self):
         """{phase: (ms, launches)} accumulated since the last call, plus solver iterations."""
-        ms = np.zeros(6)
-        cnt = np.zeros(6, dtype=np.int64)
+        ms = np.zeros(len(self.PHASES))
+        cnt = np.zeros(len(self.PHASES), dtype=np.int64)
         it = ctypes.c_int64()
         _check(lib().epic_get_profile(self._h, _ptr(ms), _ptr(cnt), ctypes.byref(it)))
         return {p: (float(ms[k]), int(cnt[k])) for k, p in enumerate(self.PHASES)}, it.value

@@ -19,7 +19,7 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libepic2d_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_FP64 = ["epic_particles.cu", "epic_field.cu", "epic_mcc.cu", "epic_capi.cu", "epic_noalloc.cu"]
+CU_FP64 = ["epic_particles.cu", "epic_field.cu", "epic_mcc.cu", "epic_capi.cu", "epic_noalloc.cu", "epic_sort.cu"]
 CU_FAST = ["epic_mixed.cu", "epic_spectral.cu"]
 CPP = ["epic_host.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]

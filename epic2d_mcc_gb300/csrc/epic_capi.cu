@@ -187,7 +187,9 @@ epic_status do_deposit(epic_sim* s, int i) {
   PhaseTimer t(s, 0);
   epic_species_state& sp = s->sp[i];
   CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
-  if (s->mixed)
+  if (s->mixed && s->cfg.shape == EPIC_CIC)
+    launch_deposit_mixed_sorted(s->stream, s->g, sp.mx, sp.d_n, sp.acc, s->part_grid);
+  else if (s->mixed)
     launch_deposit_mixed(s->stream, s->g, s->cfg.shape, sp.mx, sp.d_n, sp.acc, s->d_flags, s->part_grid);
   else
     launch_deposit(s->stream, s->g, s->cfg.shape, s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED, sp.soa, sp.d_n,
@@ -366,9 +368,46 @@ epic_status do_mcc(epic_sim* s, int e, int ion, const double* d_uniforms, int us
 }
 
 // The loop body of src/main.cpp:405-423 as a launch sequence.
-epic_status do_step(epic_sim* s, int with_collisions) {
+// Scratch of the cell sort, sized for the largest species (allocated before
+// any graph capture).
+epic_status ensure_sort_scratch(epic_sim* s) {
+  long long cap = 0;
+  for (auto& sp : s->sp) cap = std::max(cap, sp.cap);
+  if (s->sort_buf && s->sort_cap >= cap) return EPIC_OK;
+  if (s->sort_buf) cudaFree(s->sort_buf);
+  s->sort_buf = nullptr;
+  if (cudaMalloc(&s->sort_buf, sort_scratch_bytes(cap)) != cudaSuccess) {
+    cudaGetLastError();
+    return fail(EPIC_ERR_NOMEM, "cell sort scratch (%lld particles)", cap);
+  }
+  s->sort_cap = cap;
+  return EPIC_OK;
+}
+
+epic_status do_sort(epic_sim* s, int i) {
+  PhaseTimer t(s, 6);
+  epic_status st = ensure_sort_scratch(s);
+  if (st) return st;
+  epic_species_state& sp = s->sp[i];
+  ParticleRef p;
+  p.mixed = s->mixed;
+  p.f = sp.soa;
+  p.m = sp.mx;
+  s->launches += launch_sort(s->stream, s->g, p, sp.d_n, sp.cap, carve_sort_scratch(s->sort_buf, sp.cap),
+                             s->part_grid);
+  CKL();
+  return EPIC_OK;
+}
+
+// sort: -1 by the step counter and cfg.sort_every, 0 never, 1 always.
+epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
   epic_status st;
   const int nsp = (int)s->sp.size();
+  if (sort < 0) sort = s->cfg.sort_every > 0 && s->step_index % s->cfg.sort_every == 0;
+  s->step_index++;
+  if (sort)
+    for (int i = 0; i < nsp; i++)
+      if ((st = do_sort(s, i))) return st;
   for (int i = 0; i < nsp; i++)
     if ((st = do_deposit(s, i))) return st;
   if ((st = do_finalize(s, FINALIZE_AND_RHO, -1))) return st;
@@ -493,6 +532,8 @@ void epic_destroy(epic_sim* s) {
   if (!s) return;
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
+  if (s->sort_buf) cudaFree(s->sort_buf);
   for (auto& sp : s->sp) free_species(sp);
   void* spec[] = {s->spec.Q, s->spec.D, s->spec.t0, s->spec.t1, s->spec.r64, s->spec.partials, s->spec.state,
                   s->ef32};
@@ -572,6 +613,10 @@ epic_status epic_add_species(epic_sim* s, const epic_species_desc* d, int* index
   }
   s->sp.push_back(sp);
   if (index) *index = (int)s->sp.size() - 1;
+  // A captured step no longer covers every species.
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
+  s->graph_exec = s->graph_exec_sort = nullptr;
   return EPIC_OK;
 }
 
@@ -699,6 +744,13 @@ epic_status epic_rewind_species(epic_sim* s, int i) {
   return sync(s);
 }
 
+epic_status epic_sort_species(epic_sim* s, int i) {
+  if (!valid_species(s, i)) return fail(EPIC_ERR_INVALID, "bad species index");
+  epic_status st = do_sort(s, i);
+  if (st) return st;
+  return sync(s);
+}
+
 static epic_status upload_tables(epic_sim* s, const double* tot, const double* ela, const double* exc,
                                  const double* ion, int64_t n) {
   double** dst[4] = {&s->cs.tot, &s->cs.ela, &s->cs.exc, &s->cs.ion};
@@ -820,33 +872,46 @@ epic_status epic_run(epic_sim* s, int steps, int with_collisions, int use_graph)
       if ((st = do_step(s, with_collisions))) return st;
     return sync(s);
   }
-  if (!s->graph_exec || s->graph_collisions != with_collisions) {
-    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
-    s->graph_exec = nullptr;
-    if (with_collisions && s->sp.size() >= 2)
-      if ((st = ensure_mcc_events(s, s->sp[0].cap))) return st;
+  const bool sorting = s->cfg.sort_every > 0;
+  // One step captured as a graph (all scratch allocated first: a capture
+  // cannot allocate); with sorting on, a second graph for the sort steps.
+  auto capture = [&](int sort, cudaGraphExec_t* exec, int64_t* nlaunch) -> epic_status {
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
-    int64_t before = s->launches;
-    st = do_step(s, with_collisions);
+    const int64_t before = s->launches, step_before = s->step_index;
+    epic_status e = do_step(s, with_collisions, sort);
     cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
-    if (st || ce != cudaSuccess) {
+    s->step_index = step_before;
+    if (e || ce != cudaSuccess) {
       cudaGetLastError();  // a failed capture leaves its error pending; do not leak it to later calls
       if (ce == cudaSuccess) cudaGraphDestroy(graph);
       s->launches = before;
-      if (st) return st;
+      if (e) return e;
       return fail(EPIC_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
     }
-    s->graph_launches = s->launches - before;
+    *nlaunch = s->launches - before;
     s->launches = before;
-    ce = cudaGraphInstantiate(&s->graph_exec, graph, 0);
+    ce = cudaGraphInstantiate(exec, graph, 0);
     cudaGraphDestroy(graph);
     if (ce != cudaSuccess) return fail(EPIC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    return EPIC_OK;
+  };
+  if (!s->graph_exec || s->graph_collisions != with_collisions || (sorting && !s->graph_exec_sort)) {
+    if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+    if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
+    s->graph_exec = s->graph_exec_sort = nullptr;
+    if (with_collisions && s->sp.size() >= 2)
+      if ((st = ensure_mcc_events(s, s->sp[0].cap))) return st;
+    if (sorting && (st = ensure_sort_scratch(s))) return st;
+    if ((st = capture(0, &s->graph_exec, &s->graph_launches))) return st;
+    if (sorting && (st = capture(1, &s->graph_exec_sort, &s->graph_launches_sort))) return st;
     s->graph_collisions = with_collisions;
   }
   for (int k = 0; k < steps; k++) {
-    CK(cudaGraphLaunch(s->graph_exec, s->stream));
-    s->launches += s->graph_launches;
+    const bool srt = sorting && s->step_index % s->cfg.sort_every == 0;
+    s->step_index++;
+    CK(cudaGraphLaunch(srt ? s->graph_exec_sort : s->graph_exec, s->stream));
+    s->launches += srt ? s->graph_launches_sort : s->graph_launches;
   }
   return sync(s);
 }

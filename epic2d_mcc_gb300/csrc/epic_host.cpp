@@ -232,6 +232,10 @@ int config_from_ini(const char* path, epic_config* cfg, epic_species_desc* sp, i
     if (auto v = opt(ini, "simulation", "deposit_mode")) cfg->deposit_mode = *v == "fp64" ? EPIC_DEPOSIT_FP64 : EPIC_DEPOSIT_FIXED;
     if (auto v = opt(ini, "simulation", "arithmetic"))
       cfg->precision = *v == "mixed" ? EPIC_PRECISION_MIXED : EPIC_PRECISION_FP64;
+    // Cell sort: off for the FP64 form (keeps the reference's particle order),
+    // every 16 steps for the mixed form unless the deck says otherwise.
+    if (cfg->precision == EPIC_PRECISION_MIXED) cfg->sort_every = 16;
+    if (auto v = opt(ini, "simulation", "sort_every")) cfg->sort_every = std::stoi(*v);
     if (auto v = opt(ini, "collision", "mcc_mode"))
       cfg->mcc_mode = *v == "null" ? EPIC_MCC_NULL : (*v == "injected" ? EPIC_MCC_INJECTED : EPIC_MCC_PHILOX);
     if (auto v = opt(ini, "collision", "seed")) cfg->seed = std::stoull(*v);

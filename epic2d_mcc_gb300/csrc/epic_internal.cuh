@@ -141,6 +141,22 @@ void launch_particle_sums_mixed(cudaStream_t st, int what, const MixedSoA& p, co
                                 double vel_norm, double* partials, double* out3, int grid);
 constexpr int MIXED_OFFSET_BITS = 20;  // deposit weights: offsets quantised to 2^-20 of a cell
 
+// ---- cell sort (epic_sort.cu) ----
+struct SortScratch {
+  unsigned* keys[2];
+  unsigned* vals[2];
+  unsigned* hist;   // digit table [digit][tile], scanned in place
+  unsigned* bsum;   // scan totals
+  void* tmp;        // payload copy, 40 bytes per particle slot
+};
+size_t sort_scratch_bytes(long long cap);
+SortScratch carve_sort_scratch(void* buf, long long cap);
+// Sorts one species by cell (stable); returns the number of kernels launched.
+int launch_sort(cudaStream_t st, const Geom& g, const ParticleRef& p, const long long* d_n, long long cap,
+                const SortScratch& sc, int grid);
+void launch_deposit_mixed_sorted(cudaStream_t st, const Geom& g, const MixedSoA& p, const long long* d_n,
+                                 unsigned long long* acc, int grid);
+
 // ---- spectral FP32 inner solve with FP64 refinement (epic_spectral.cu) ----
 struct SolverArgs;
 struct SpectralSolver {
@@ -265,9 +281,14 @@ struct epic_sim {
   int* d_flags;
   epic::CrossSections cs;
   int64_t launches;
-  cudaGraphExec_t graph_exec;
-  int64_t graph_launches;
+  cudaGraphExec_t graph_exec;       // one step
+  cudaGraphExec_t graph_exec_sort;  // one step that starts with the cell sort
+  int64_t graph_launches, graph_launches_sort;
   int graph_collisions;
+  // cell sort
+  int64_t step_index;               // steps taken (decides which steps sort)
+  void* sort_buf;
+  long long sort_cap;               // largest capacity the buffer serves
   // per-phase profiling (events on `stream`)
   int profiling;
   std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;

@@ -77,7 +77,8 @@ typedef struct {
   int warm_start;             /* 0: cold-start solves as the reference */
   int solver_blocks;          /* CTAs of the grid-wide solvers; 0 = automatic */
   int precision;              /* EPIC_PRECISION_FP64 (the reference's arithmetic) | EPIC_PRECISION_MIXED */
-  int reserved[14];
+  int sort_every;             /* sort particles by cell every k steps (0: never, the reference's order) */
+  int reserved[13];
 } epic_config;
 
 /* Mixed precision: particles as int32 cell + FP32 in-cell offsets + FP32
@@ -147,6 +148,14 @@ epic_status epic_calculate_efield(epic_sim* sim);
 epic_status epic_push_species(epic_sim* sim, int species, int sub_cycle);
 /* Species::Rewind_species (src/species.cpp:229-246). */
 epic_status epic_rewind_species(epic_sim* sim, int species);
+/* Cell sort (no counterpart in the reference, which never reorders
+ * part_list): stable sort of the species' particles by the flat index
+ * i*ny + j of the lower-left node of their cell, i = (int)((x - x0)/dx),
+ * j = (int)((y - y0)/dy) (the node src/domain.cpp:207-208 deposits from).
+ * Particles of one cell keep their relative order.  epic_step sorts every
+ * species first on steps where step % sort_every == 0 (epic_config.sort_every,
+ * 0 = never). */
+epic_status epic_sort_species(epic_sim* sim, int species);
 
 /* CollisionHandler::set_electron_cross_sections + calc_total_cross_sections
  * (src/collision.cpp:12-42): per-energy tables on the linear grid
@@ -205,11 +214,11 @@ void* epic_stream(epic_sim* sim);
 /* Per-phase timing with CUDA events recorded on the handle's stream around
  * each phase of epic_step (no reference counterpart; the reference times the
  * whole run only, src/main.cpp:282,465-469).  Phases: 0 deposit, 1 density
- * finalisation + rho, 2 Poisson solve, 3 E-field, 4 push, 5 MCC.
+ * finalisation + rho, 2 Poisson solve, 3 E-field, 4 push, 5 MCC, 6 cell sort.
  * epic_get_profile waits for the stream, then returns accumulated
  * milliseconds and step counts per phase and the solver iterations summed
  * over the profiled steps; it resets the accumulators. */
-enum { EPIC_NUM_PHASES = 6 };
+enum { EPIC_NUM_PHASES = 7 };
 epic_status epic_set_profiling(epic_sim* sim, int enable);
 epic_status epic_get_profile(epic_sim* sim, double ms[EPIC_NUM_PHASES], int64_t counts[EPIC_NUM_PHASES],
                              int64_t* solver_iterations);
