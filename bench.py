@@ -41,6 +41,7 @@ WORKLOAD = "beam_mcc_256"
 METRIC = "particle-steps/s on 1 GB300 (plain FP64 time-step loop)"
 UNIT = "particle-steps/s"
 SORT_EVERY = 16  # cell-sort period of the mixed form (the mixed decks' default)
+REF_BUDGET_S = 150.0  # bound on the reference arm's timed CPU loop
 
 # Algorithmic bytes per unit of each phase (FP64 plain form).
 BYTES = {
@@ -81,7 +82,7 @@ class Clocks:
             os.close(fd)
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -163,9 +164,11 @@ def run_reference(args, rank, world):
     if rank != 0:
         return
     ini = write_deck(args.workload)
-    value, done, n, kind = cpu_port_run(ini, args.steps, args.warmup)
+    # One loop iteration of the reference takes ~1 s on this workload: at most
+    # one warm-up iteration, and the timed iterations stop at REF_BUDGET_S.
+    value, done, n, kind = cpu_port_run(ini, args.steps, min(args.warmup, 1), budget_s=REF_BUDGET_S)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": n / value * 1e3,
+            "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": n / value * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (particles loaded from mt19937 seed 0, as the reference's Init)",
             "config": {"workload": args.workload, "particles": n},
@@ -338,7 +341,17 @@ def run_ours(args, rank, world):
 
         e_ref, e_mx = energy(ref), energy(mx)
         phi_ref = ref.grid("phi")
+        # HBM roofline of the mixed particle phases: 40 B (push: cell, offsets,
+        # vx, vy read + written) and 12 B (deposit: cell + offsets read) per particle.
+        npart = 0.5 * (nb + na)
+        mroof = {}
+        for ph, per in (("push", 40), ("deposit", 12)):
+            t_ms = mprof[ph][0] / msteps
+            if t_ms > 0:
+                gbs = per * npart / (t_ms / 1e3) / 1e9
+                mroof[ph] = {"achieved_gbs": gbs, "frac": gbs / load_peaks()[0], "bytes_per_particle": per}
         mixed = {"value": mvalue, "unit": UNIT, "ms_per_step": mms / msteps, "steps": msteps,
+                 "roofline_particle_phases": mroof,
                  "speedup_vs_fp64": mvalue / value, "dtype": "f32 particles/inner solve + f64 refinement",
                  "sort_every": SORT_EVERY,
                  "phases_ms_per_step": {k: v[0] / msteps for k, v in mprof.items()},
@@ -375,16 +388,18 @@ def run_ours(args, rank, world):
 
 
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of each
-# phase's kernel from the ncu captures summarised under profiles/; None where
-# no capture exists yet.
-TRAFFIC = {}
+# phase's kernel from the ncu captures summarised under profiles/ (beam_mcc_256);
+# absent where no capture of that phase's average launch exists.  The solve's
+# vectors stay in registers and L2, so its traffic is ~2 MB against 5.8 GB of
+# algorithmic (memory-streamed) bytes.
+TRAFFIC = {"solve": 1.938688e6 + 0.08192e6}
 
 
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=10)
-    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", default=WORKLOAD)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
