@@ -88,6 +88,11 @@ def lib() -> ctypes.CDLL:
         "epic_push_species": ([vp, i, i], st),
         "epic_rewind_species": ([vp, i], st),
         "epic_sort_species": ([vp, i], st),
+        "epic_initial_field_async": ([vp], st),
+        "epic_run_async": ([vp, i, i], st),
+        "epic_poll": ([vp, ctypes.POINTER(ctypes.c_int)], st),
+        "epic_load_particles_device": ([vp, ctypes.c_uint64], st),
+        "epic_digest": ([vp, vp], st),
         "epic_set_cross_sections": ([vp, vp, vp, vp, vp, i64, d], st),
         "epic_set_reference_cross_sections": ([vp], st),
         "epic_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
@@ -106,6 +111,15 @@ def lib() -> ctypes.CDLL:
         "epic_stream": ([vp], vp),
         "epic_set_profiling": ([vp, i], st),
         "epic_get_profile": ([vp, vp, vp, ctypes.POINTER(ctypes.c_int64)], st),
+        "epic_estimate_bytes": ([vp, vp, i, i], i64),
+        "epic_server_create": ([i64, i, i, ctypes.POINTER(vp)], st),
+        "epic_server_destroy": ([vp], None),
+        "epic_server_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
+        "epic_server_submit": ([vp, vp, ctypes.POINTER(ctypes.c_int64)], st),
+        "epic_server_start": ([vp], st),
+        "epic_server_wait": ([vp, d], st),
+        "epic_server_result": ([vp, i64, vp], st),
+        "epic_server_get_stats": ([vp, vp], st),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -226,6 +240,17 @@ class Simulation:
     def rewind_species(self, sp: int):
         _check(lib().epic_rewind_species(self._h, sp))
 
+    def load_particles_device(self, seed: int = 0):
+        """Loads every species on the GPU (Philox uniforms, the reference's placement and velocity formula)."""
+        _check(lib().epic_load_particles_device(self._h, seed))
+        self.sync()
+
+    def digest(self):
+        """(phi hash, particles hash): order-independent 64-bit digests of the run's state."""
+        out = np.zeros(2, dtype=np.uint64)
+        _check(lib().epic_digest(self._h, _ptr(out)))
+        return int(out[0]), int(out[1])
+
     def sort_species(self, sp: int):
         """Stable sort of the species' particles by cell (i*ny + j)."""
         _check(lib().epic_sort_species(self._h, sp))
@@ -316,3 +341,96 @@ class Simulation:
         it = ctypes.c_int64()
         _check(lib().epic_get_profile(self._h, _ptr(ms), _ptr(cnt), ctypes.byref(it)))
         return {p: (float(ms[k]), int(cnt[k])) for k, p in enumerate(self.PHASES)}, it.value
+
+
+# ------------------------------------------------------------------ serving ---
+class Request(ctypes.Structure):
+    _fields_ = [("cfg", Config), ("species", SpeciesDesc * 8), ("num_species", ctypes.c_int),
+                ("steps", ctypes.c_int), ("collisions", ctypes.c_int), ("load_seed", ctypes.c_uint64),
+                ("arrival_s", ctypes.c_double)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("id", ctypes.c_int64), ("status", ctypes.c_int), ("arrival_s", ctypes.c_double),
+                ("admit_s", ctypes.c_double), ("finish_s", ctypes.c_double), ("particle_steps", ctypes.c_int64),
+                ("bytes", ctypes.c_int64), ("digest", ctypes.c_uint64 * 2), ("kinetic_energy", ctypes.c_double),
+                ("potential_energy", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_int64), ("completed", ctypes.c_int64), ("failed", ctypes.c_int64),
+                ("p50_latency_s", ctypes.c_double), ("p99_latency_s", ctypes.c_double),
+                ("mean_latency_s", ctypes.c_double), ("max_latency_s", ctypes.c_double),
+                ("makespan_s", ctypes.c_double), ("particle_steps_per_s", ctypes.c_double),
+                ("peak_bytes", ctypes.c_int64), ("peak_inflight", ctypes.c_int)]
+
+
+def make_request(path: str, steps: int, collisions: bool = False, seed: int = 0, arrival_s: float = 0.0,
+                 **overrides) -> Request:
+    """A serving request from an input deck (config overrides as in Simulation.from_ini)."""
+    cfg, descs, _ = config_from_ini(path)
+    for k, v in overrides.items():
+        if k == "capacity":
+            for d in descs:
+                d.capacity = int(v)
+        else:
+            setattr(cfg, k, v)
+    r = Request()
+    r.cfg = cfg
+    for k, d in enumerate(descs):
+        r.species[k] = d
+    r.num_species = len(descs)
+    r.steps = int(steps)
+    r.collisions = int(bool(collisions))
+    r.load_seed = int(seed)
+    r.arrival_s = float(arrival_s)
+    return r
+
+
+def estimate_bytes(req: Request) -> int:
+    return lib().epic_estimate_bytes(ctypes.byref(req.cfg), req.species, req.num_species, req.collisions)
+
+
+class Server:
+    """Continuous-batching serving loop (include/epic2d_serve.h)."""
+
+    def __init__(self, budget_bytes: int, max_inflight: int = 8, chunk_steps: int = 16):
+        self._h = ctypes.c_void_p()
+        _check(lib().epic_server_create(int(budget_bytes), int(max_inflight), int(chunk_steps), ctypes.byref(self._h)))
+
+    def set_log_cross_sections(self, ela, exc, ion, e_min, e_max):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (ela, exc, ion)]
+        _check(lib().epic_server_set_log_cross_sections(self._h, *[_ptr(a) for a in arrs], len(arrs[0]),
+                                                        e_min, e_max))
+
+    def submit(self, req: Request) -> int:
+        i = ctypes.c_int64()
+        _check(lib().epic_server_submit(self._h, ctypes.byref(req), ctypes.byref(i)))
+        return i.value
+
+    def start(self):
+        _check(lib().epic_server_start(self._h))
+
+    def wait(self, timeout_s: float = 600.0):
+        _check(lib().epic_server_wait(self._h, timeout_s))
+
+    def result(self, rid: int) -> Result:
+        r = Result()
+        _check(lib().epic_server_result(self._h, rid, ctypes.byref(r)))
+        return r
+
+    def stats(self) -> ServerStats:
+        s = ServerStats()
+        _check(lib().epic_server_get_stats(self._h, ctypes.byref(s)))
+        return s
+
+    def close(self):
+        if self._h:
+            lib().epic_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

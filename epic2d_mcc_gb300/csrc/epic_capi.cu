@@ -42,13 +42,21 @@ epic_status fail(epic_status st, const char* fmt, ...) {
     if (e_ != cudaSuccess) return fail(EPIC_ERR_CUDA, "kernel launch: %s", cudaGetErrorString(e_)); \
   } while (0)
 
+// Device allocations are stream-ordered on the handle's stream (and freed
+// the same way): a plain cudaMalloc, cudaFree or cudaMemset would serialise
+// the work of every other stream on the device, which stalls the other runs a
+// server keeps in flight.
 template <class T>
-epic_status dalloc(T** p, size_t count) {
+epic_status dalloc(epic_sim* s, T** p, size_t count) {
   *p = nullptr;
   if (count == 0) count = 1;
-  CK(cudaMalloc((void**)p, count * sizeof(T)));
-  CK(cudaMemset(*p, 0, count * sizeof(T)));
+  CK(cudaMallocAsync((void**)p, count * sizeof(T), s->stream));
+  CK(cudaMemsetAsync(*p, 0, count * sizeof(T), s->stream));
   return EPIC_OK;
+}
+
+void dfree(epic_sim* s, void* p) {
+  if (p) cudaFreeAsync(p, s->stream);
 }
 
 long long nnodes(const epic_sim* s) { return (long long)s->cfg.nx * s->cfg.ny; }
@@ -56,9 +64,10 @@ long long nnodes(const epic_sim* s) { return (long long)s->cfg.nx * s->cfg.ny; }
 // Reads and clears the device error flags (the stream must be idle).
 epic_status take_flags(epic_sim* s) {
   int f = 0;
-  CK(cudaMemcpy(&f, s->d_flags, sizeof(int), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&f, s->d_flags, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   if (!f) return EPIC_OK;
-  CK(cudaMemset(s->d_flags, 0, sizeof(int)));
+  CK(cudaMemsetAsync(s->d_flags, 0, sizeof(int), s->stream));
   if (f & FLAG_TIMEOUT) return fail(EPIC_ERR_TIMEOUT, "a device-side wait gave up (flags 0x%x)", f);
   if (f & FLAG_CAPACITY) return fail(EPIC_ERR_CAPACITY, "a species outgrew its particle capacity (flags 0x%x)", f);
   if (f & FLAG_OUT_OF_GRID)
@@ -76,9 +85,9 @@ bool valid_species(epic_sim* s, int i) { return s && i >= 0 && i < (int)s->sp.si
 epic_status ensure_tile_status(epic_sim* s, long long cap) {
   long long need = cap / SCAN_TILE + 2;
   if (need <= s->tile_status_len) return EPIC_OK;
-  if (s->tile_status) cudaFree(s->tile_status);
+  if (s->tile_status) dfree(s, s->tile_status);
   s->tile_status = nullptr;
-  epic_status st = dalloc(&s->tile_status, (size_t)need);
+  epic_status st = dalloc(s, &s->tile_status, (size_t)need);
   if (st) return st;
   s->tile_status_len = need;
   return EPIC_OK;
@@ -86,19 +95,18 @@ epic_status ensure_tile_status(epic_sim* s, long long cap) {
 
 epic_status ensure_staging(epic_sim* s, size_t bytes) {
   if (bytes <= s->staging_bytes) return EPIC_OK;
-  if (s->staging) cudaFree(s->staging);
+  if (s->staging) dfree(s, s->staging);
   s->staging = nullptr;
   s->staging_bytes = 0;
-  CK(cudaMalloc(&s->staging, bytes));
+  CK(cudaMallocAsync(&s->staging, bytes, s->stream));
   s->staging_bytes = bytes;
   return EPIC_OK;
 }
 
-void free_species(epic_species_state& sp) {
+void free_species(epic_sim* s, epic_species_state& sp) {
   void* ptrs[] = {sp.soa.x, sp.soa.y, sp.soa.vx, sp.soa.vy, sp.soa.vz, sp.mx.cell, sp.mx.ox, sp.mx.oy,
                   sp.mx.vx, sp.mx.vy, sp.mx.vz, sp.d_n, sp.den, sp.acc};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
+  for (void* p : ptrs) dfree(s, p);
 }
 
 // Refinement stages of the mixed-precision Poisson solve (each gains ~6
@@ -125,15 +133,16 @@ epic_status setup_spectral(epic_sim* s) {
   }
   for (int p = 0; p < n; p++)
     for (int q = 0; q < n; q++) D[(size_t)p * n + q] = (float)(1.0 / (lam[p] + lam[q]));
-  CK(cudaMalloc((void**)&sp.Q, Q.size() * sizeof(float)));
-  CK(cudaMalloc((void**)&sp.D, D.size() * sizeof(float)));
-  CK(cudaMalloc((void**)&sp.t0, Q.size() * sizeof(float)));
-  CK(cudaMalloc((void**)&sp.t1, Q.size() * sizeof(float)));
-  CK(cudaMalloc((void**)&sp.partials, 256 * sizeof(double)));
-  CK(cudaMalloc((void**)&sp.state, 4 * sizeof(int)));
-  CK(cudaMemcpy(sp.Q, Q.data(), Q.size() * sizeof(float), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(sp.D, D.data(), D.size() * sizeof(float), cudaMemcpyHostToDevice));
-  CK(cudaMemset(sp.state, 0, 4 * sizeof(int)));
+  CK(cudaMallocAsync((void**)&sp.Q, Q.size() * sizeof(float), s->stream));
+  CK(cudaMallocAsync((void**)&sp.D, D.size() * sizeof(float), s->stream));
+  CK(cudaMallocAsync((void**)&sp.t0, Q.size() * sizeof(float), s->stream));
+  CK(cudaMallocAsync((void**)&sp.t1, Q.size() * sizeof(float), s->stream));
+  CK(cudaMallocAsync((void**)&sp.partials, 256 * sizeof(double), s->stream));
+  CK(cudaMallocAsync((void**)&sp.state, 4 * sizeof(int), s->stream));
+  CK(cudaMemcpyAsync(sp.Q, Q.data(), Q.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(sp.D, D.data(), D.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaStreamSynchronize(s->stream));  // Q and D are host temporaries
+  CK(cudaMemsetAsync(sp.state, 0, 4 * sizeof(int), s->stream));
   return EPIC_OK;
 }
 
@@ -326,23 +335,23 @@ epic_status ensure_mcc_events(epic_sim* s, long long e_cap) {
   if (cudaStreamIsCapturing(s->stream, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone)
     return fail(EPIC_ERR_INVALID, "MCC scratch must be allocated before stream capture");
   McEvents& ev = s->mcc_ev;
-  cudaFree(ev.buf); cudaFree(ev.count); cudaFree(ev.slot); cudaFree(ev.tile_cnt); cudaFree(ev.tile_off);
-  cudaFree(ev.cand); cudaFree(ev.cand_count);
+  dfree(s, ev.buf); dfree(s, ev.count); dfree(s, ev.slot); dfree(s, ev.tile_cnt); dfree(s, ev.tile_off);
+  dfree(s, ev.cand); dfree(s, ev.cand_count);
   std::memset(&ev, 0, sizeof(ev));
   s->mcc_ev_for_cap = 0;
   const size_t tiles = (size_t)(e_cap / MCC_TILE + 2);
   ev.cap = (unsigned int)std::min<long long>(std::max<long long>(e_cap / 8, 65536), 1LL << 30);
-  CK(cudaMalloc((void**)&ev.buf, (size_t)ev.cap * ion_event_bytes()));
-  CK(cudaMalloc((void**)&ev.cand, (size_t)e_cap * sizeof(unsigned int)));
-  CK(cudaMalloc((void**)&ev.cand_count, sizeof(unsigned int)));
-  CK(cudaMemset(ev.cand_count, 0, sizeof(unsigned int)));
-  CK(cudaMalloc((void**)&ev.count, sizeof(unsigned int)));
-  CK(cudaMalloc((void**)&ev.slot, (size_t)e_cap * sizeof(int)));
-  CK(cudaMalloc((void**)&ev.tile_cnt, tiles * sizeof(unsigned int)));
-  CK(cudaMalloc((void**)&ev.tile_off, tiles * sizeof(unsigned int)));
-  CK(cudaMemset(ev.count, 0, sizeof(unsigned int)));
-  CK(cudaMemset(ev.slot, 0xff, (size_t)e_cap * sizeof(int)));
-  CK(cudaMemset(ev.tile_cnt, 0, tiles * sizeof(unsigned int)));
+  CK(cudaMallocAsync((void**)&ev.buf, (size_t)ev.cap * ion_event_bytes(), s->stream));
+  CK(cudaMallocAsync((void**)&ev.cand, (size_t)e_cap * sizeof(unsigned int), s->stream));
+  CK(cudaMallocAsync((void**)&ev.cand_count, sizeof(unsigned int), s->stream));
+  CK(cudaMemsetAsync(ev.cand_count, 0, sizeof(unsigned int), s->stream));
+  CK(cudaMallocAsync((void**)&ev.count, sizeof(unsigned int), s->stream));
+  CK(cudaMallocAsync((void**)&ev.slot, (size_t)e_cap * sizeof(int), s->stream));
+  CK(cudaMallocAsync((void**)&ev.tile_cnt, tiles * sizeof(unsigned int), s->stream));
+  CK(cudaMallocAsync((void**)&ev.tile_off, tiles * sizeof(unsigned int), s->stream));
+  CK(cudaMemsetAsync(ev.count, 0, sizeof(unsigned int), s->stream));
+  CK(cudaMemsetAsync(ev.slot, 0xff, (size_t)e_cap * sizeof(int), s->stream));
+  CK(cudaMemsetAsync(ev.tile_cnt, 0, tiles * sizeof(unsigned int), s->stream));
   s->mcc_ev_for_cap = e_cap;
   return EPIC_OK;
 }
@@ -374,9 +383,9 @@ epic_status ensure_sort_scratch(epic_sim* s) {
   long long cap = 0;
   for (auto& sp : s->sp) cap = std::max(cap, sp.cap);
   if (s->sort_buf && s->sort_cap >= cap) return EPIC_OK;
-  if (s->sort_buf) cudaFree(s->sort_buf);
+  if (s->sort_buf) dfree(s, s->sort_buf);
   s->sort_buf = nullptr;
-  if (cudaMalloc(&s->sort_buf, sort_scratch_bytes(cap)) != cudaSuccess) {
+  if (cudaMallocAsync(&s->sort_buf, sort_scratch_bytes(cap), s->stream) != cudaSuccess) {
     cudaGetLastError();
     return fail(EPIC_ERR_NOMEM, "cell sort scratch (%lld particles)", cap);
   }
@@ -497,28 +506,38 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
     if (x && !st) st = x;
   };
   guard(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking) == cudaSuccess ? EPIC_OK : EPIC_ERR_CUDA);
-  guard(dalloc(&s->phi, nn));
-  guard(dalloc(&s->rho, nn));
-  guard(dalloc(&s->efx, nn));
-  guard(dalloc(&s->efy, nn));
-  guard(dalloc(&s->ef, nn));
-  for (int k = 0; k < 8; k++) guard(dalloc(&s->work[k], nn));
+  {
+    // Keep freed stream-ordered memory in the device's pool (returning it to
+    // the system would synchronise); a process-local setting.
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t thr = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+    }
+  }
+  guard(dalloc(s, &s->phi, nn));
+  guard(dalloc(s, &s->rho, nn));
+  guard(dalloc(s, &s->efx, nn));
+  guard(dalloc(s, &s->efy, nn));
+  guard(dalloc(s, &s->ef, nn));
+  for (int k = 0; k < 8; k++) guard(dalloc(s, &s->work[k], nn));
   // Solver partials: up to 2 parities x 48 bytes per CTA (PCG), 16 doubles per CTA.
-  guard(dalloc(&s->partials, 16 * (size_t)std::max(solver_max_blocks(), 320)));
-  guard(dalloc(&s->bar, 2));
-  guard(dalloc(&s->d_info, 1));
-  guard(dalloc(&s->d_iter_total, 1));
-  guard(dalloc(&s->tile_ctr, 1));
-  guard(dalloc(&s->d_ncoll, 4));
-  guard(dalloc(&s->d_step, 1));
-  guard(dalloc(&s->sum_partials, 3 * (size_t)s->part_grid));
-  guard(dalloc(&s->d_sums, 4));
-  guard(dalloc(&s->d_flags, 1));
+  guard(dalloc(s, &s->partials, 16 * (size_t)std::max(solver_max_blocks(), 320)));
+  guard(dalloc(s, &s->bar, 2));
+  guard(dalloc(s, &s->d_info, 1));
+  guard(dalloc(s, &s->d_iter_total, 1));
+  guard(dalloc(s, &s->tile_ctr, 1));
+  guard(dalloc(s, &s->d_ncoll, 4));
+  guard(dalloc(s, &s->d_step, 1));
+  guard(dalloc(s, &s->sum_partials, 3 * (size_t)s->part_grid));
+  guard(dalloc(s, &s->d_sums, 4));
+  guard(dalloc(s, &s->d_flags, 1));
   s->mixed = cfg->precision == EPIC_PRECISION_MIXED;
   if (s->mixed) {
-    guard(dalloc(&s->ef32, nn));
+    guard(dalloc(s, &s->ef32, nn));
     if (spectral_supported(s->g) && !st) guard(setup_spectral(s));
   }
+  if (!st && cudaStreamSynchronize(s->stream) != cudaSuccess) st = EPIC_ERR_CUDA;
   if (st) {
     std::string e = g_err;
     epic_destroy(s);
@@ -533,29 +552,29 @@ void epic_destroy(epic_sim* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
-  if (s->sort_buf) cudaFree(s->sort_buf);
-  for (auto& sp : s->sp) free_species(sp);
+  if (s->sort_buf) dfree(s, s->sort_buf);
+  for (auto& sp : s->sp) free_species(s, sp);
   void* spec[] = {s->spec.Q, s->spec.D, s->spec.t0, s->spec.t1, s->spec.r64, s->spec.partials, s->spec.state,
                   s->ef32};
-  for (void* p : spec) cudaFree(p);
+  for (void* p : spec) dfree(s, p);
   for (auto& pe : s->prof_pending) {
     cudaEventDestroy(pe.second.first);
     cudaEventDestroy(pe.second.second);
   }
   for (auto e : s->event_pool) cudaEventDestroy(e);
-  cudaFree(s->mcc_ev.buf);
-  cudaFree(s->mcc_ev.count);
-  cudaFree(s->mcc_ev.slot);
-  cudaFree(s->mcc_ev.tile_cnt);
-  cudaFree(s->mcc_ev.tile_off);
-  cudaFree(s->mcc_ev.cand);
-  cudaFree(s->mcc_ev.cand_count);
-  for (int k = 0; k < 8; k++) cudaFree(s->work[k]);
+  dfree(s, s->mcc_ev.buf);
+  dfree(s, s->mcc_ev.count);
+  dfree(s, s->mcc_ev.slot);
+  dfree(s, s->mcc_ev.tile_cnt);
+  dfree(s, s->mcc_ev.tile_off);
+  dfree(s, s->mcc_ev.cand);
+  dfree(s, s->mcc_ev.cand_count);
+  for (int k = 0; k < 8; k++) dfree(s, s->work[k]);
   void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->partials, s->bar,
                   s->d_info, s->d_iter_total, s->tile_ctr, s->d_ncoll, s->d_step, s->sum_partials, s->d_sums, s->d_flags,
                   s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion};
   for (void* p : ptrs)
-    if (p) cudaFree(p);
+    if (p) dfree(s, p);
   if (s->stream) cudaStreamDestroy(s->stream);
   delete s;
 }
@@ -590,25 +609,25 @@ epic_status epic_add_species(epic_sim* s, const epic_species_desc* d, int* index
   if (s->mixed) {
     // 2^40 per particle in the integer CIC weights: overflow needs > 2^23
     // particles in one node's four cells.
-    guard(dalloc(&sp.mx.cell, cap));
-    guard(dalloc(&sp.mx.ox, cap));
-    guard(dalloc(&sp.mx.oy, cap));
-    guard(dalloc(&sp.mx.vx, cap));
-    guard(dalloc(&sp.mx.vy, cap));
-    guard(dalloc(&sp.mx.vz, cap));
+    guard(dalloc(s, &sp.mx.cell, cap));
+    guard(dalloc(s, &sp.mx.ox, cap));
+    guard(dalloc(s, &sp.mx.oy, cap));
+    guard(dalloc(s, &sp.mx.vx, cap));
+    guard(dalloc(s, &sp.mx.vy, cap));
+    guard(dalloc(s, &sp.mx.vz, cap));
   } else {
-    guard(dalloc(&sp.soa.x, cap));
-    guard(dalloc(&sp.soa.y, cap));
-    guard(dalloc(&sp.soa.vx, cap));
-    guard(dalloc(&sp.soa.vy, cap));
-    guard(dalloc(&sp.soa.vz, cap));
+    guard(dalloc(s, &sp.soa.x, cap));
+    guard(dalloc(s, &sp.soa.y, cap));
+    guard(dalloc(s, &sp.soa.vx, cap));
+    guard(dalloc(s, &sp.soa.vy, cap));
+    guard(dalloc(s, &sp.soa.vz, cap));
   }
-  guard(dalloc(&sp.d_n, 1));
-  guard(dalloc(&sp.den, nn));
-  guard(dalloc(&sp.acc, nn));
+  guard(dalloc(s, &sp.d_n, 1));
+  guard(dalloc(s, &sp.den, nn));
+  guard(dalloc(s, &sp.acc, nn));
   guard(ensure_tile_status(s, sp.cap));
   if (st) {
-    free_species(sp);
+    free_species(s, sp);
     return st;
   }
   s->sp.push_back(sp);
@@ -704,7 +723,8 @@ epic_status epic_potential_solver(epic_sim* s, int* iterations, double* error) {
   if (st) return st;
   if ((st = sync(s))) return st;
   SolveInfo info;
-  CK(cudaMemcpy(&info, s->d_info, sizeof(info), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&info, s->d_info, sizeof(info), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   if (iterations) *iterations = info.iterations;
   if (error) *error = info.error;
   if (!info.converged)
@@ -727,8 +747,7 @@ epic_status epic_push_species(epic_sim* s, int i, int sub_cycle) {
   return sync(s);
 }
 
-epic_status epic_rewind_species(epic_sim* s, int i) {
-  if (!valid_species(s, i)) return fail(EPIC_ERR_INVALID, "bad species index");
+static epic_status do_rewind(epic_sim* s, int i) {
   epic_species_state& sp = s->sp[i];
   const epic_config& c = s->cfg;
   double qm = sp.desc.charge / sp.desc.mass;
@@ -741,6 +760,13 @@ epic_status epic_rewind_species(epic_sim* s, int i) {
     launch_rewind(s->stream, s->g, c.shape, sp.soa, sp.d_n, s->ef, hqmK, c.DT, s->d_flags, s->part_grid);
   s->launches += 1;
   CKL();
+  return EPIC_OK;
+}
+
+epic_status epic_rewind_species(epic_sim* s, int i) {
+  if (!valid_species(s, i)) return fail(EPIC_ERR_INVALID, "bad species index");
+  epic_status st = do_rewind(s, i);
+  if (st) return st;
   return sync(s);
 }
 
@@ -756,10 +782,10 @@ static epic_status upload_tables(epic_sim* s, const double* tot, const double* e
   double** dst[4] = {&s->cs.tot, &s->cs.ela, &s->cs.exc, &s->cs.ion};
   const double* src[4] = {tot, ela, exc, ion};
   for (int k = 0; k < 4; k++) {
-    if (*dst[k]) cudaFree(*dst[k]);
+    if (*dst[k]) dfree(s, *dst[k]);
     *dst[k] = nullptr;
-    CK(cudaMalloc((void**)dst[k], (size_t)n * sizeof(double)));
-    CK(cudaMemcpy(*dst[k], src[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMallocAsync((void**)dst[k], (size_t)n * sizeof(double), s->stream));
+    CK(cudaMemcpyAsync(*dst[k], src[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice, s->stream));
   }
   s->cs.n = n;
   return EPIC_OK;
@@ -825,9 +851,9 @@ epic_status epic_handle_collisions(epic_sim* s, int e, int ion, const double* un
     if (st) return st;
     size_t len = (size_t)std::max<int64_t>(ne, 1) * ustride;
     if ((long long)len > s->uniforms_len) {
-      if (s->d_uniforms) cudaFree(s->d_uniforms);
+      if (s->d_uniforms) dfree(s, s->d_uniforms);
       s->d_uniforms = nullptr;
-      CK(cudaMalloc(&s->d_uniforms, len * sizeof(double)));
+      CK(cudaMallocAsync(&s->d_uniforms, len * sizeof(double), s->stream));
       s->uniforms_len = (long long)len;
     }
     CK(cudaMemcpyAsync(s->d_uniforms, uniforms, (size_t)ne * ustride * sizeof(double), cudaMemcpyHostToDevice,
@@ -838,7 +864,8 @@ epic_status epic_handle_collisions(epic_sim* s, int e, int ion, const double* un
   if (st) return st;
   if ((st = sync(s))) return st;
   unsigned long long nc = 0;
-  CK(cudaMemcpy(&nc, s->d_ncoll, sizeof(nc), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpyAsync(&nc, s->d_ncoll, sizeof(nc), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
   if (collisions) *collisions = (int64_t)nc;
   return EPIC_OK;
 }
@@ -850,27 +877,37 @@ epic_status epic_step(epic_sim* s, int with_collisions) {
   return sync(s);
 }
 
-epic_status epic_initial_field(epic_sim* s) {
-  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+static epic_status do_initial_field(epic_sim* s) {
   epic_status st;
   for (int i = 0; i < (int)s->sp.size(); i++)
     if ((st = do_deposit(s, i))) return st;
   if ((st = do_finalize(s, FINALIZE_AND_RHO, -1))) return st;
   if ((st = do_solve(s))) return st;
   if ((st = do_efield(s))) return st;
-  if ((st = sync(s))) return st;
   for (int i = 0; i < (int)s->sp.size(); i++)
-    if ((st = epic_rewind_species(s, i))) return st;
+    if ((st = do_rewind(s, i))) return st;
   return EPIC_OK;
 }
 
-epic_status epic_run(epic_sim* s, int steps, int with_collisions, int use_graph) {
-  if (!s || steps < 0) return fail(EPIC_ERR_INVALID, "bad argument");
+epic_status epic_initial_field(epic_sim* s) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  epic_status st = do_initial_field(s);
+  if (st) return st;
+  return sync(s);
+}
+
+epic_status epic_initial_field_async(epic_sim* s) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  return do_initial_field(s);
+}
+
+// Enqueues `steps` steps on the handle's stream without waiting.
+static epic_status enqueue_run(epic_sim* s, int steps, int with_collisions, int use_graph) {
   epic_status st;
   if (!use_graph) {
     for (int k = 0; k < steps; k++)
       if ((st = do_step(s, with_collisions))) return st;
-    return sync(s);
+    return EPIC_OK;
   }
   const bool sorting = s->cfg.sort_every > 0;
   // One step captured as a graph (all scratch allocated first: a capture
@@ -913,7 +950,84 @@ epic_status epic_run(epic_sim* s, int steps, int with_collisions, int use_graph)
     CK(cudaGraphLaunch(srt ? s->graph_exec_sort : s->graph_exec, s->stream));
     s->launches += srt ? s->graph_launches_sort : s->graph_launches;
   }
+  return EPIC_OK;
+}
+
+epic_status epic_run(epic_sim* s, int steps, int with_collisions, int use_graph) {
+  if (!s || steps < 0) return fail(EPIC_ERR_INVALID, "bad argument");
+  epic_status st = enqueue_run(s, steps, with_collisions, use_graph);
+  if (st) return st;
   return sync(s);
+}
+
+epic_status epic_run_async(epic_sim* s, int steps, int with_collisions) {
+  if (!s || steps < 0) return fail(EPIC_ERR_INVALID, "bad argument");
+  return enqueue_run(s, steps, with_collisions, 1);
+}
+
+epic_status epic_poll(epic_sim* s, int* done) {
+  if (!s || !done) return fail(EPIC_ERR_INVALID, "bad argument");
+  cudaError_t e = cudaStreamQuery(s->stream);
+  if (e == cudaErrorNotReady) {
+    *done = 0;
+    return EPIC_OK;
+  }
+  *done = 1;
+  if (e != cudaSuccess) return fail(EPIC_ERR_CUDA, "stream: %s", cudaGetErrorString(e));
+  return take_flags(s);
+}
+
+epic_status epic_load_particles_device(epic_sim* s, uint64_t seed) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  for (int i = 0; i < (int)s->sp.size(); i++) {
+    epic_species_state& sp = s->sp[i];
+    const long long n = sp.desc.numparticle;
+    if (n > sp.cap) return fail(EPIC_ERR_CAPACITY, "%lld particles exceed the capacity %lld of %s", n, sp.cap,
+                                sp.name.c_str());
+    int kind = 0, narg = 0;
+    std::string err;
+    if (parse_load_type(sp.desc.load, &kind, &narg, err)) return fail(EPIC_ERR_INVALID, "%s", err.c_str());
+    epic_status st = ensure_staging(s, std::max<size_t>(1, (size_t)n * 5 * sizeof(double)));
+    if (st) return st;
+    launch_load(s->stream, s->g, sp.desc, s->cfg, i, kind, narg, (double*)s->staging, seed, s->part_grid);
+    if (n) {
+      if (s->mixed)
+        launch_aos_to_mixed(s->stream, s->g, (const double*)s->staging, sp.mx, n, s->d_flags, s->part_grid);
+      else
+        k_aos_to_soa<<<s->part_grid, 256, 0, s->stream>>>((const double*)s->staging, sp.soa, n);
+    }
+    launch_set_count(s->stream, sp.d_n, n);
+    s->launches += n ? 3 : 1;
+    CKL();
+  }
+  return EPIC_OK;
+}
+
+epic_status epic_digest(epic_sim* s, uint64_t out[2]) {
+  if (!s || !out) return fail(EPIC_ERR_INVALID, "bad argument");
+  unsigned long long* d = reinterpret_cast<unsigned long long*>(s->d_sums);  // 4 doubles of scratch
+  CK(cudaMemsetAsync(d, 0, 2 * sizeof(unsigned long long), s->stream));
+  launch_digest(s->stream, s->phi, 8, nullptr, nnodes(s), 1, d, s->part_grid);
+  for (int i = 0; i < (int)s->sp.size(); i++) {
+    epic_species_state& sp = s->sp[i];
+    const unsigned long long tag = 16ull * (i + 1);
+    launch_digest(s->stream, sp.d_n, 8, nullptr, 1, tag, d + 1, 1);
+    if (s->mixed) {
+      const void* a[6] = {sp.mx.cell, sp.mx.ox, sp.mx.oy, sp.mx.vx, sp.mx.vy, sp.mx.vz};
+      for (int k = 0; k < 6; k++) launch_digest(s->stream, a[k], 4, sp.d_n, 0, tag + 1 + k, d + 1, s->part_grid);
+    } else {
+      const void* a[5] = {sp.soa.x, sp.soa.y, sp.soa.vx, sp.soa.vy, sp.soa.vz};
+      for (int k = 0; k < 5; k++) launch_digest(s->stream, a[k], 8, sp.d_n, 0, tag + 1 + k, d + 1, s->part_grid);
+    }
+  }
+  CKL();
+  unsigned long long h[2];
+  CK(cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, s->stream));
+  epic_status st = sync(s);
+  if (st) return st;
+  out[0] = h[0];
+  out[1] = h[1];
+  return EPIC_OK;
 }
 
 epic_status epic_compute_ke(epic_sim* s, int i, int norm, double out[3]) {
@@ -1024,16 +1138,18 @@ epic_status epic_set_grid(epic_sim* s, int which, const double* in) {
   if (which == EPIC_GRID_EFX || which == EPIC_GRID_EFY) {
     // keep the interleaved gather copy in step with the component grids
     std::vector<double> ex(nnodes(s)), ey(nnodes(s));
-    CK(cudaMemcpy(ex.data(), s->efx, nnodes(s) * sizeof(double), cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(ey.data(), s->efy, nnodes(s) * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpyAsync(ex.data(), s->efx, nnodes(s) * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaMemcpyAsync(ey.data(), s->efy, nnodes(s) * sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+    CK(cudaStreamSynchronize(s->stream));
     std::vector<double2> e2(nnodes(s));
     for (long long k = 0; k < nnodes(s); k++) e2[k] = make_double2(ex[k], ey[k]);
-    CK(cudaMemcpy(s->ef, e2.data(), nnodes(s) * sizeof(double2), cudaMemcpyHostToDevice));
+    CK(cudaMemcpyAsync(s->ef, e2.data(), nnodes(s) * sizeof(double2), cudaMemcpyHostToDevice, s->stream));
     if (s->ef32) {
       std::vector<float2> f2(nnodes(s));
       for (long long k = 0; k < nnodes(s); k++) f2[k] = make_float2((float)ex[k], (float)ey[k]);
-      CK(cudaMemcpy(s->ef32, f2.data(), nnodes(s) * sizeof(float2), cudaMemcpyHostToDevice));
+      CK(cudaMemcpyAsync(s->ef32, f2.data(), nnodes(s) * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
     }
+    CK(cudaStreamSynchronize(s->stream));  // e2, f2 are host temporaries
   }
   return EPIC_OK;
 }
@@ -1067,8 +1183,9 @@ epic_status epic_get_profile(epic_sim* s, double ms[EPIC_NUM_PHASES], int64_t co
   }
   s->prof_pending.clear();
   unsigned long long it = 0;
-  CK(cudaMemcpy(&it, s->d_iter_total, sizeof(it), cudaMemcpyDeviceToHost));
-  CK(cudaMemset(s->d_iter_total, 0, sizeof(it)));
+  CK(cudaMemcpyAsync(&it, s->d_iter_total, sizeof(it), cudaMemcpyDeviceToHost, s->stream));
+  CK(cudaStreamSynchronize(s->stream));
+  CK(cudaMemsetAsync(s->d_iter_total, 0, sizeof(it), s->stream));
   for (int k = 0; k < EPIC_NUM_PHASES; k++) {
     if (ms) ms[k] = s->prof_ms[k];
     if (counts) counts[k] = s->prof_count[k];

@@ -8,6 +8,35 @@ namespace epic {
 // ------------------------------------------------------------ helpers ---
 static __device__ __forceinline__ void set_flag(int* flags, int bit) { atomicOr(flags, bit); }
 
+// Philox-4x32-10 counter-based generator (Salmon et al., SC'11): the stream is
+// addressed by a 96-bit counter (c0, c1, c2) and a 64-bit key; draw k uses
+// 53 bits of block k/2.
+struct Philox {
+  uint32_t c0, c1, c2, key0, key1;
+  int k;
+  uint4 cur;
+  __device__ static uint4 round10(uint4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+    for (int r = 0; r < 10; r++) {
+      uint32_t hi0 = __umulhi(0xD2511F53u, c.x), lo0 = 0xD2511F53u * c.x;
+      uint32_t hi1 = __umulhi(0xCD9E8D57u, c.z), lo1 = 0xCD9E8D57u * c.z;
+      c = make_uint4(hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0);
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    return c;
+  }
+  // The k-th draw as a 53-bit integer M; the uniform is M * 2^-53 in [0, 1).
+  __device__ unsigned long long next53() {
+    if ((k & 1) == 0) cur = round10(make_uint4(c0, c1, c2, (uint32_t)(k >> 1)), key0, key1);
+    uint32_t a = (k & 1) ? cur.z : cur.x, b = (k & 1) ? cur.w : cur.y;
+    k++;
+    return ((unsigned long long)(a >> 5) << 26) | (b >> 6);
+  }
+  __device__ double next() { return (double)next53() * (1.0 / 9007199254740992.0); }
+};
+
+
 // Ordered tile scan (decoupled look-back).  Tiles are claimed in increasing
 // order through an atomic counter, so every tile a block waits on belongs to a
 // block that is already running; each wait is bounded by SPIN_LIMIT polls.

@@ -276,6 +276,25 @@ double sample_vel(Rnd& rnd, double mass, double temp) {
 }
 }  // namespace
 
+int parse_load_type(const std::string& load, int* kind, int* narg, std::string& err) {
+  std::string type = load;
+  *narg = 0;
+  size_t lp = load.find('(');
+  if (lp != std::string::npos && load.find(')', lp) != std::string::npos) {  // INIParser::loadtypeextract
+    type = load.substr(0, lp);
+    *narg = std::stoi(load.substr(lp + 1, load.find(')', lp) - lp - 1));
+  }
+  if (type == "random") *kind = 0;
+  else if (type == "uniform") *kind = 1;
+  else if (type == "sin") *kind = 2;
+  else if (type == "cos") *kind = 3;
+  else {
+    err = "load type " + load + " is not supported (random, uniform, sin(n), cos(n))";
+    return EPIC_ERR_INVALID;
+  }
+  return EPIC_OK;
+}
+
 int load_particles(const epic_config& c, const std::vector<const epic_species_desc*>& sp,
                    std::vector<std::vector<double>>& out, uint32_t seed, std::string& err) {
   Rnd rnd(seed);
@@ -283,23 +302,8 @@ int load_particles(const epic_config& c, const std::vector<const epic_species_de
   out.resize(sp.size());
   for (size_t s = 0; s < sp.size(); s++) {
     const epic_species_desc& d = *sp[s];
-    std::string load = d.load;
-    std::string type = load;
-    int narg = 0;
-    size_t lp = load.find('(');
-    if (lp != std::string::npos && load.find(')', lp) != std::string::npos) {  // INIParser::loadtypeextract
-      type = load.substr(0, lp);
-      narg = std::stoi(load.substr(lp + 1, load.find(')', lp) - lp - 1));
-    }
-    int kind;
-    if (type == "random") kind = 0;
-    else if (type == "uniform") kind = 1;
-    else if (type == "sin") kind = 2;
-    else if (type == "cos") kind = 3;
-    else {
-      err = "load type " + load + " is not supported (random, uniform, sin(n), cos(n))";
-      return EPIC_ERR_INVALID;
-    }
+    int kind = 0, narg = 0;
+    if (int st = parse_load_type(d.load, &kind, &narg, err)) return st;
     const long n = d.numparticle;
     std::vector<double>& o = out[s];
     o.resize((size_t)n * 5);

@@ -22,6 +22,9 @@ int config_from_ini(const char* path, epic_config* cfg, epic_species_desc* sp, i
 int ini_get(const char* path, const char* section, const char* key, std::string& value, std::string& err);
 int load_particles(const epic_config& c, const std::vector<const epic_species_desc*>& sp,
                    std::vector<std::vector<double>>& out, uint32_t seed, std::string& err);
+// INIParser::loadtypeextract (src/iniparser.cpp): "random" -> 0, "uniform" -> 1,
+// "sin(n)" -> 2, "cos(n)" -> 3 with *narg = n; EPIC_ERR_INVALID otherwise.
+int parse_load_type(const std::string& load, int* kind, int* narg, std::string& err);
 void reference_tables(const epic_config& c, std::vector<double>& tot, std::vector<double>& ela,
                       std::vector<double>& exc, std::vector<double>& ion);
 double cs_elastic(double energy, int on);

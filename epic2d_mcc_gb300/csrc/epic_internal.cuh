@@ -141,6 +141,14 @@ void launch_particle_sums_mixed(cudaStream_t st, int what, const MixedSoA& p, co
                                 double vel_norm, double* partials, double* out3, int grid);
 constexpr int MIXED_OFFSET_BITS = 20;  // deposit weights: offsets quantised to 2^-20 of a cell
 
+// ---- device loading and run digest (epic_load.cu) ----
+// kind: 0 random, 1 uniform, 2 sin(n), 3 cos(n) (the reference's load types).
+void launch_load(cudaStream_t st, const Geom& g, const epic_species_desc& d, const epic_config& c, int species,
+                 int kind, int narg, double* aos, unsigned long long seed, int grid);
+void launch_set_count(cudaStream_t st, long long* d_n, long long n);
+void launch_digest(cudaStream_t st, const void* a, int elem_bytes, const long long* d_n, long long n,
+                   unsigned long long tag, unsigned long long* out, int grid);
+
 // ---- cell sort (epic_sort.cu) ----
 struct SortScratch {
   unsigned* keys[2];

@@ -190,6 +190,25 @@ epic_status epic_initial_field(epic_sim* sim);
  * CUDA graph and replayed (fixed-size launches, device-side counts). */
 epic_status epic_run(epic_sim* sim, int steps, int with_collisions, int use_graph);
 
+/* Asynchronous forms for callers that keep several runs in flight (no
+ * counterpart in the reference, which runs one loop in one process).  They
+ * enqueue work on the handle's stream and return; epic_poll reports whether
+ * the stream has drained (*done = 1) and then the status the work left, as
+ * epic_sync would.  epic_run_async replays captured step graphs. */
+epic_status epic_initial_field_async(epic_sim* sim);
+epic_status epic_run_async(epic_sim* sim, int steps, int with_collisions);
+epic_status epic_poll(epic_sim* sim, int* done);
+/* Loads every species' numparticle particles on the GPU (asynchronous): the
+ * placements and velocity formula of Init::Init / Init::SampleVel
+ * (src/init.cpp:3-114) with uniforms from a Philox stream keyed by
+ * (seed, species, particle) instead of the reference's mt19937 (use
+ * epic_load_particles for the reference's own particles). */
+epic_status epic_load_particles_device(epic_sim* sim, uint64_t seed);
+/* Order-independent 64-bit hashes of the run's state: out[0] of phi, out[1]
+ * of every species' particle count and particle arrays (in the handle's
+ * layout).  Equal digests mean bit-identical state. */
+epic_status epic_digest(epic_sim* sim, uint64_t out[2]);
+
 /* Species::Compute_KE / Compute_Momentum (src/species.cpp:248-297) and
  * Domain::Compute_PE (src/domain.cpp:266-286); norm_species is the species
  * whose temperature normalises (Output::storeKE_to_matrix, src/output.cpp:291-315). */
