@@ -362,6 +362,10 @@ def run_ours(args, rank, world):
         ref.close()
         mx.close()
 
+    serving = None
+    if not args.no_serve:
+        serving = run_serving(E, workloads)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, done, n, kind = cpu_port_run(ini, None, 0, budget_s=args.cpu_seconds)
@@ -381,10 +385,72 @@ def run_ours(args, rank, world):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                         "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "mixed_precision": mixed}
+                "mixed_precision": mixed, "serving": serving}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+SERVE_BUDGET = 150e9      # device bytes the serving loop may admit
+SERVE_STEP_SCALE = 0.05   # step counts 500-5000 scaled to 25-250 so the bench ends in minutes
+SERVE_FP64_SAMPLE = 6     # requests timed one at a time in the plain FP64 form
+
+
+def run_serving(E, workloads):
+    """The serving workload (Poisson arrivals at 50 runs/s for 2 s; grids
+    {64..512}^2; 25-100 particles per cell per species; MCC on half the runs;
+    periodic or absorbing walls; step counts scaled) through the continuous-
+    batching server in the mixed form, against a sample of the same requests
+    run one at a time in the plain FP64 form."""
+    import torch
+
+    A = E.api
+    reqs = workloads.serving_requests(seed=0, step_scale=SERVE_STEP_SCALE)
+    e, ela, exc, ion = workloads.synthetic_table()
+    d = tempfile.mkdtemp(prefix="epic_serve_")
+    paths = []
+    for k, q in enumerate(reqs):
+        path = os.path.join(d, "req%03d.ini" % k)
+        with open(path, "w") as f:
+            f.write(q["ini"])
+        paths.append(path)
+    srv = A.Server(SERVE_BUDGET, max_inflight=16, chunk_steps=16)
+    srv.set_log_cross_sections(ela, exc, ion, e[0], e[-1])
+    ids = [srv.submit(A.make_request(paths[k], q["steps"], q["collisions"], q["seed"], q["arrival_s"],
+                                     precision=1, sort_every=SORT_EVERY)) for k, q in enumerate(reqs)]
+    torch.cuda.synchronize()
+    srv.start()
+    srv.wait(1800)
+    st = srv.stats()
+    fails = sum(1 for i in ids if srv.result(i).status != 0)
+    srv.close()
+    # the plain FP64 form, one request at a time (wall time from creation to the end of the last step)
+    sample = list(range(0, len(reqs), max(1, len(reqs) // SERVE_FP64_SAMPLE)))[:SERVE_FP64_SAMPLE]
+    pst, wall = 0.0, 0.0
+    for k in sample:
+        q = reqs[k]
+        t0 = time.perf_counter()
+        sim = A.Simulation.from_ini(paths[k])
+        if q["collisions"]:
+            sim.set_log_cross_sections(ela, exc, ion, e[0], e[-1])
+        sim.load_particles_device(q["seed"])
+        sim.initial_field()
+        sim.run(q["steps"], collisions=q["collisions"], graph=True)
+        wall += time.perf_counter() - t0
+        pst += q["particles"] * q["steps"]
+        sim.close()
+    fp64_rate = pst / wall if wall > 0 else None
+    return {"workload": "serving: Poisson arrivals 50/s for 2 s, grids {64,128,256,512}^2, 25-100 ppc per species, "
+                        "steps 500-5000 x %g, MCC p=0.5, pbc or open walls, %.0f GB budget, mixed form"
+                        % (SERVE_STEP_SCALE, SERVE_BUDGET / 1e9),
+            "requests": len(reqs), "completed": int(st.completed), "failed": fails,
+            "p50_latency_s": st.p50_latency_s, "p99_latency_s": st.p99_latency_s,
+            "mean_latency_s": st.mean_latency_s, "max_latency_s": st.max_latency_s,
+            "makespan_s": st.makespan_s, "particle_steps_per_s": st.particle_steps_per_s,
+            "peak_inflight": int(st.peak_inflight), "peak_bytes": int(st.peak_bytes),
+            "fp64_one_at_a_time_particle_steps_per_s": fp64_rate,
+            "fp64_sample": "%d of the %d requests, each created, loaded, initialised and run alone" % (len(sample), len(reqs)),
+            "speedup_vs_fp64_one_at_a_time": (st.particle_steps_per_s / fp64_rate) if fp64_rate else None}
 
 
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of each
@@ -405,6 +471,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision measurement")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
