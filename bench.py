@@ -180,6 +180,25 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------ GPU arm ---
+def over_ranks(x, op, dist, device):
+    """x reduced over the ranks of a replica run (max of times, sum of work);
+    x itself on a single rank.  No data-path collective: one scalar per run."""
+    if not dist:
+        return x
+    import torch
+
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def replica_value(particle_steps_rank, ms_rank, dist=None, device="cuda"):
+    """Whole-job particle-steps/s of N replicas: all ranks' particle-steps over
+    the slowest rank's time."""
+    ms_max = over_ranks(ms_rank, "max", dist, device)
+    return over_ranks(particle_steps_rank, "sum", dist, device) / (ms_max / 1e3), ms_max
+
+
 def run_ours(args, rank, world):
     import numpy as np
     import torch
@@ -202,18 +221,10 @@ def run_ours(args, rank, world):
             dist.barrier()
 
     def max_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return over_ranks(x, "max", dist, "cuda")
 
     def sum_over_ranks(x):
-        if not dist:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        return float(t.item())
+        return over_ranks(x, "sum", dist, "cuda")
 
     ini = write_deck(args.workload)
     coll = collisions_on(ini)
@@ -250,9 +261,8 @@ def run_ours(args, rank, world):
     prof, iters = sim.profile()
     sim.set_profiling(False)
     n_after = sum(sim.num_particles(s) for s in range(nsp))
-    ms_max = max_over_ranks(ms)
     pst_rank = 0.5 * (n_before + n_after) * args.steps
-    value = sum_over_ranks(pst_rank) / (ms_max / 1e3)
+    value, ms_max = replica_value(pst_rank, ms, dist, "cuda")
 
     # roofline of the dominant phase
     g = sim.cfg
