@@ -375,6 +375,9 @@ def run_ours(args, rank, world):
     serving = None
     if not args.no_serve:
         serving = run_serving(E, workloads)
+    precision_form = None
+    if not args.no_precision_form:
+        precision_form = run_precision_form(E, PRECISION_WORKLOAD, PRECISION_STEPS)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -395,10 +398,62 @@ def run_ours(args, rank, world):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                         "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "mixed_precision": mixed, "serving": serving}
+                "mixed_precision": mixed, "serving": serving, "precision_form": precision_form}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+PRECISION_WORKLOAD = "twostream_1024"
+PRECISION_STEPS = 16      # one sort period of the mixed form
+
+
+def run_precision_form(E, name, steps):
+    """The precision form's plasma (2.1e8 particles on 1024^2 periodic cells,
+    two electron streams) in the plain FP64 form and the mixed form from the
+    same particles (device loader, one seed): throughput of each over `steps`
+    steps (CUDA events, graph replay), and the mixed form's density, potential
+    and total-energy errors against the FP64 run after those steps."""
+    import numpy as np
+    import torch
+
+    A = E.api
+    ini = write_deck(name)
+    out = {"workload": name, "steps": steps}
+    sims = {}
+    for form, kw in (("fp64", {}), ("mixed", {"precision": 1, "sort_every": SORT_EVERY})):
+        sim = A.Simulation.from_ini(ini, **kw)
+        sim.load_particles_device(11)
+        sim.initial_field()
+        n = sum(sim.num_particles(k) for k in range(len(sim.species)))
+        st = torch.cuda.ExternalStream(sim.stream)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        sim.run(steps, collisions=False, graph=True)
+        e1.record(st)
+        e1.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[form + "_particle_steps_per_s"] = n * steps / (ms / 1e3)
+        out[form + "_ms_per_step"] = ms / steps
+        out["particles"] = n
+        sims[form] = sim
+    fp, mx = sims["fp64"], sims["mixed"]
+
+    def rel(a, b):
+        return float(np.max(np.abs(a - b)) / np.max(np.abs(b)))
+
+    def energy(sm):
+        return sum(sm.compute_ke(k, 0).sum() for k in range(len(sm.species))) + sm.compute_pe(0)
+
+    out["rho_rel_err_vs_fp64"] = rel(mx.grid("rho"), fp.grid("rho"))
+    out["phi_rel_err_vs_fp64"] = rel(mx.grid("phi"), fp.grid("phi"))
+    ef, em = energy(fp), energy(mx)
+    out["total_energy_rel_err_vs_fp64"] = abs(em - ef) / abs(ef)
+    out["speedup_vs_fp64"] = out["mixed_particle_steps_per_s"] / out["fp64_particle_steps_per_s"]
+    fp.close()
+    mx.close()
+    return out
 
 
 SERVE_BUDGET = 150e9      # device bytes the serving loop may admit
@@ -482,6 +537,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-precision-form", action="store_true", help="skip the 1024^2 precision-form measurement")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

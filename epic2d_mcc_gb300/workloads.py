@@ -11,6 +11,10 @@ configurations the project is measured on:
   PCG to 1e-10, MCC against 1e20 m^-3 neutrals with the synthetic 1000-point
   log-spaced table below.
 * ``periodic_1024`` — 1024x1024 cells, 100 particles per cell per species.
+* ``twostream_1024`` — the precision form's plasma: 1024x1024 periodic cells,
+  100 particles per cell per species (1.05e8 ions of 1836 m_e at 0.05 eV,
+  1.05e8 electrons at 2 eV in two halves drifting at +-3 v_th,e), dt 0.05/wpe,
+  PCG to 1e-10, no collisions (``twostream_256`` is the same on 256x256 cells).
 
 Inputs are seeded synthetic plasmas (the reference loads positions and
 velocities from mt19937 seed 0; so do these decks).
@@ -111,6 +115,19 @@ def deck(name: str) -> str:
               "beam,%.8E,%d,1,-1,%.17g,5,0,random" % (ME, beam, 1.0 / 9.0)]
         return _TEMPLATE.format(num_ts=2000, dt=0.01, n=n, solver="cg", tol="1e-10", maxit=100000,
                                 solver_extra="", bc="pbc", coll="true", gas="1e20", species="\n".join(sp))
+    if name in ("twostream_1024", "twostream_256"):
+        # two counter-streaming electron populations at +-3 v_th,e (v_th = sqrt(2 e Te / m_e));
+        # velocities are in units of vel_norm = LDe * wpe = sqrt(e Te / m_e) (norm_scheme 1), so
+        # 3 v_th,e = 3 sqrt(2) vel_norm.  Electron halves: fract_den 1 relative to the first.
+        n = 1024 if name == "twostream_1024" else 256
+        ppc = 100
+        half = n * n * ppc // 2
+        vs = 3.0 * np.sqrt(2.0)
+        sp = ["electron,%.8E,%d,2,-1,1,%.17g,0,random" % (ME, half, vs),
+              "ion,%.8E,%d,0.05,1,0,0,0,random" % (1836 * ME, n * n * ppc),
+              "beam,%.8E,%d,2,-1,1,%.17g,0,random" % (ME, half, -vs)]
+        return _TEMPLATE.format(num_ts=500, dt=0.05, n=n, solver="cg", tol="1e-10", maxit=100000,
+                                solver_extra="", bc="pbc", coll="false", gas="1e20", species="\n".join(sp))
     if name == "periodic_1024":
         n, ppc = 1024, 100
         sp = ["electron,%.8E,%d,2,-1,1,0,0,random" % (ME, n * n * ppc),
