@@ -113,36 +113,47 @@ void free_species(epic_sim* s, epic_species_state& sp) {
 // digits; the loop stops on the reference's tolerance, usually after 2-3).
 constexpr int SPECTRAL_STAGES = 6;
 
-// Sine transform and inverse eigenvalues of the reference operator for the
+// Sine transforms and inverse eigenvalues of the reference operator for the
 // mixed-precision solve: computed in FP64 on the host, stored in FP32.
-epic_status setup_spectral(epic_sim* s) {
-  SpectralSolver& sp = s->spec;
-  const bool gs = s->cfg.solver == EPIC_SOLVER_GS;
-  sp.n = gs ? s->cfg.nx - 2 : s->cfg.nx;
-  sp.off = gs ? 1 : 0;
-  sp.gs_norm = gs;
-  const int n = sp.n;
-  std::vector<float> Q((size_t)n * n), D((size_t)n * n);
-  std::vector<double> lam(n);
+static void sine_transform(int n, std::vector<float>& Q, std::vector<double>& lam) {
   const double pi = 3.14159265358979323846;
   const double c = std::sqrt(2.0 / (n + 1));
+  Q.assign((size_t)n * n, 0.f);
+  lam.assign(n, 0.0);
   for (int j = 0; j < n; j++) {
     for (int k = 0; k < n; k++) Q[(size_t)j * n + k] = (float)(c * std::sin(pi * (j + 1) * (double)(k + 1) / (n + 1)));
     const double sn = std::sin(pi * (j + 1) / (2.0 * (n + 1)));
     lam[j] = -4.0 * sn * sn;
   }
-  for (int p = 0; p < n; p++)
-    for (int q = 0; q < n; q++) D[(size_t)p * n + q] = (float)(1.0 / (lam[p] + lam[q]));
-  CK(cudaMallocAsync((void**)&sp.Q, Q.size() * sizeof(float), s->stream));
+}
+
+epic_status setup_spectral(epic_sim* s) {
+  SpectralSolver& sp = s->spec;
+  const bool gs = s->cfg.solver == EPIC_SOLVER_GS;
+  sp.flat = !gs;
+  sp.gs_norm = gs;
+  sp.R = gs ? s->cfg.nx - 2 : s->cfg.ny;
+  sp.C = gs ? s->cfg.ny - 2 : s->cfg.nx;
+  const int R = sp.R, C = sp.C;
+  std::vector<float> QR, QC, D((size_t)R * C);
+  std::vector<double> lamR, lamC;
+  sine_transform(R, QR, lamR);
+  sine_transform(C, QC, lamC);
+  for (int p = 0; p < R; p++)
+    for (int q = 0; q < C; q++) D[(size_t)p * C + q] = (float)(1.0 / (lamR[p] + lamC[q]));
+  CK(cudaMallocAsync((void**)&sp.QR, QR.size() * sizeof(float), s->stream));
+  if (C == R) sp.QC = sp.QR;
+  else CK(cudaMallocAsync((void**)&sp.QC, QC.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.D, D.size() * sizeof(float), s->stream));
-  CK(cudaMallocAsync((void**)&sp.t0, Q.size() * sizeof(float), s->stream));
-  CK(cudaMallocAsync((void**)&sp.t1, Q.size() * sizeof(float), s->stream));
+  CK(cudaMallocAsync((void**)&sp.t0, D.size() * sizeof(float), s->stream));
+  CK(cudaMallocAsync((void**)&sp.t1, D.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.partials, 256 * sizeof(double), s->stream));
   CK(cudaMallocAsync((void**)&sp.state, 4 * sizeof(int), s->stream));
-  CK(cudaMemcpyAsync(sp.Q, Q.data(), Q.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  CK(cudaMemcpyAsync(sp.QR, QR.data(), QR.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  if (C != R) CK(cudaMemcpyAsync(sp.QC, QC.data(), QC.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
   CK(cudaMemcpyAsync(sp.D, D.data(), D.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-  CK(cudaStreamSynchronize(s->stream));  // Q and D are host temporaries
   CK(cudaMemsetAsync(sp.state, 0, 4 * sizeof(int), s->stream));
+  CK(cudaStreamSynchronize(s->stream));  // host temporaries
   return EPIC_OK;
 }
 
@@ -273,7 +284,7 @@ int solver_blocks(epic_sim* s, long long nodes_per_block) {
 epic_status do_solve(epic_sim* s) {
   PhaseTimer t(s, 2);
   SolverArgs a = solver_args(s);
-  if (s->mixed && s->spec.Q) {
+  if (s->mixed && s->spec.QR) {
     launch_spectral(s->stream, s->spec, a, SPECTRAL_STAGES);
     s->launches += 3 + 6 * SPECTRAL_STAGES;
     CKL();
@@ -535,7 +546,7 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   s->mixed = cfg->precision == EPIC_PRECISION_MIXED;
   if (s->mixed) {
     guard(dalloc(s, &s->ef32, nn));
-    if (spectral_supported(s->g) && !st) guard(setup_spectral(s));
+    if (spectral_supported(s->g, cfg->solver) && !st) guard(setup_spectral(s));
   }
   if (!st && cudaStreamSynchronize(s->stream) != cudaSuccess) st = EPIC_ERR_CUDA;
   if (st) {
@@ -554,7 +565,8 @@ void epic_destroy(epic_sim* s) {
   if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
   if (s->sort_buf) dfree(s, s->sort_buf);
   for (auto& sp : s->sp) free_species(s, sp);
-  void* spec[] = {s->spec.Q, s->spec.D, s->spec.t0, s->spec.t1, s->spec.r64, s->spec.partials, s->spec.state,
+  void* spec[] = {s->spec.QR, s->spec.QC != s->spec.QR ? s->spec.QC : nullptr, s->spec.D, s->spec.t0, s->spec.t1,
+                  s->spec.r64, s->spec.partials, s->spec.state,
                   s->ef32};
   for (void* p : spec) dfree(s, p);
   for (auto& pe : s->prof_pending) {

@@ -168,17 +168,17 @@ void launch_deposit_mixed_sorted(cudaStream_t st, const Geom& g, const MixedSoA&
 // ---- spectral FP32 inner solve with FP64 refinement (epic_spectral.cu) ----
 struct SolverArgs;
 struct SpectralSolver {
-  int n;          // unknowns per side (square grids only)
-  int off;        // index of the first unknown node in each direction (0: all nodes, 1: interior)
+  int R, C;       // lattice of unknowns: R rows of C
+  int flat;       // 1: pcgsolver's lattice of the flattened vector (all nodes); 0: gssolver's interior
   int gs_norm;    // 1: stop on the SOR residual L2 of src/field.cpp:118-134, 0: on |b - Ax|_2
-  float* Q;       // n x n sine transform, orthonormal and symmetric
-  float* D;       // n x n, 1/(lambda_p + lambda_q)
-  float *t0, *t1; // n x n FP32 scratch
+  float *QR, *QC; // R x R and C x C sine transforms, orthonormal and symmetric (shared when R = C)
+  float* D;       // R x C, 1/(lambda_p + mu_q)
+  float *t0, *t1; // R x C FP32 scratch
   double *r64;    // residual scratch (nx*ny)
   double* partials;
   int* state;     // [0] done flag, [1] stage, [2] converged
 };
-int spectral_supported(const Geom& g);
+int spectral_supported(const Geom& g, int solver);
 void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs& a, int stages);
 void launch_particle_sums(cudaStream_t st, int what, const SoA& p, const long long* d_n, double vel_norm,
                           double* partials, double* out3, int grid);

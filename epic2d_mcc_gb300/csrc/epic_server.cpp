@@ -35,7 +35,10 @@ struct Run {
 // A run whose solve waits at grid-wide barriers (cooperative launches) must
 // not share the device with another such kernel.
 bool needs_exclusive(const epic_config& c) {
-  const bool spectral = c.precision == EPIC_PRECISION_MIXED && c.nx == c.ny && c.dx == c.dy;
+  // the mixed form solves with the spectral method (no grid barrier) on any
+  // grid under pcgsolver's norm and on isotropic grids under gssolver's
+  const bool spectral = c.precision == EPIC_PRECISION_MIXED && c.nx >= 3 && c.ny >= 3 &&
+                        (c.solver == EPIC_SOLVER_PCG || c.dx == c.dy);
   if (spectral) return false;
   if (c.solver == EPIC_SOLVER_PCG) return true;
   return c.solver == EPIC_SOLVER_GS && c.sor_mode == EPIC_SOR_REDBLACK;
@@ -214,8 +217,8 @@ int64_t epic_estimate_bytes(const epic_config* c, const epic_species_desc* sp, i
   const bool mixed = c->precision == EPIC_PRECISION_MIXED;
   int64_t b = N * 8 * (4 + 2 + 8) + N * 16 * nsp;  // phi rho efx efy, ef, 8 solver vectors, den + acc
   if (mixed) {
-    b += N * 8;                                       // ef32
-    if (c->nx == c->ny) b += 4 * N * 4 + N * 8;       // spectral Q, D, 2 scratch + residual
+    b += N * 8;                                                            // ef32
+    b += 3 * N * 4 + ((int64_t)c->nx * c->nx + (int64_t)c->ny * c->ny) * 4;  // spectral D, scratch, transforms
   }
   int64_t cmax = 0, nmax = 0;
   for (int k = 0; k < nsp; k++) {

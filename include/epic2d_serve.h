@@ -12,7 +12,7 @@
  * finished run is digested (epic_digest), its energies are recorded, and its
  * memory returns to the budget for the next arrivals.  Runs whose Poisson
  * solve uses a grid-wide barrier (FP64 PCG or red-black SOR, or the mixed
- * form on a non-square grid) are admitted only when nothing else is resident,
+ * form under gssolver with dx != dy) are admitted only when nothing else is resident,
  * and nothing else is admitted while they run.  Every kernel of a run is
  * deterministic, so its result is bit-identical alone and in a mix.
  *

@@ -80,6 +80,25 @@ def test_mixed_spectral_solve(gpu_lib, tmp_path, solver, n):
     assert rel(sim.grid("phi"), exact) < 1e-5
 
 
+@pytest.mark.parametrize("solver", ["cg", "gs"])
+@pytest.mark.parametrize("shape", [(64, 40), (40, 72), (97, 33)])
+def test_mixed_spectral_solve_rectangular(gpu_lib, tmp_path, solver, shape):
+    # Non-square grids: pcgsolver's lattice is the flattened vector in rows of nx
+    # (not the physical grid); gssolver's is the physical interior.
+    nx, ny = shape
+    ini = decks.write(decks.deck(nx=nx, ny=ny, ne=nx * ny * 4, ni=nx * ny * 4, solver=solver, tol="1e-10",
+                                 maxit=400000), str(tmp_path))
+    orc = O.OracleSim(ini, initial_field=False)
+    orc.scatter_all()
+    sim = mixed_sim(gpu_lib, ini)
+    sim.set_grid("rho", orc.rho)
+    it, err, conv = sim.potential_solver()
+    assert conv and 1 <= it <= 5
+    orc.R.d.tolerance = 1e-13
+    exact = orc.R.pcg_solve(orc.rho)[0] if solver == "cg" else orc.R.gs_solve(orc.rho, 1.9)[0]
+    assert rel(sim.grid("phi"), exact) < 1e-5
+
+
 def test_mixed_one_step_vs_fp64(gpu_lib, tmp_path):
     ini = decks.write(decks.deck(nx=64, ny=64, ne=100000, ni=100000, solver="cg", tol="1e-10"), str(tmp_path))
     orc = O.OracleSim(ini)
