@@ -120,6 +120,15 @@ def lib() -> ctypes.CDLL:
         "epic_server_wait": ([vp, d], st),
         "epic_server_result": ([vp, i64, vp], st),
         "epic_server_get_stats": ([vp, vp], st),
+        "epic_batch_create": ([vp, i, i, ctypes.POINTER(vp)], st),
+        "epic_batch_destroy": ([vp], None),
+        "epic_batch_initial_field": ([vp], st),
+        "epic_batch_run": ([vp, i, i], st),
+        "epic_batch_get_particles": ([vp, i, i, vp, i64, ctypes.POINTER(ctypes.c_int64)], st),
+        "epic_batch_get_grid": ([vp, i, i, vp], st),
+        "epic_batch_num_particles": ([vp, ctypes.POINTER(ctypes.c_int64)], st),
+        "epic_batch_tuning": ([vp, vp], st),
+        "epic_batch_stream": ([vp], vp),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -427,6 +436,61 @@ class Server:
     def close(self):
         if self._h:
             lib().epic_server_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------------------ batching ---
+class Batch:
+    """Many runs advanced together, one launch per phase (include/epic2d_batch.h)."""
+
+    def __init__(self, requests, sort_every: int = 16):
+        arr = (Request * len(requests))(*requests)
+        self._h = ctypes.c_void_p()
+        self.requests = list(requests)
+        _check(lib().epic_batch_create(arr, len(requests), int(sort_every), ctypes.byref(self._h)))
+
+    def initial_field(self):
+        _check(lib().epic_batch_initial_field(self._h))
+
+    def run(self, steps: int, graph: bool = True):
+        _check(lib().epic_batch_run(self._h, int(steps), int(graph)))
+
+    def particles(self, run: int, sp: int) -> np.ndarray:
+        n = self.requests[run].species[sp].numparticle
+        out = np.empty((max(n, 1), 5), dtype=np.float64)
+        got = ctypes.c_int64()
+        _check(lib().epic_batch_get_particles(self._h, run, sp, _ptr(out), len(out), ctypes.byref(got)))
+        return out[:got.value]
+
+    def grid(self, run: int, which: str = "phi") -> np.ndarray:
+        c = self.requests[run].cfg
+        out = np.empty(c.nx * c.ny, dtype=np.float64)  # node (i, j) at i*ny + j, as Simulation.grid
+        _check(lib().epic_batch_get_grid(self._h, run, GRID[which], _ptr(out)))
+        return out
+
+    def num_particles(self) -> int:
+        n = ctypes.c_int64()
+        _check(lib().epic_batch_num_particles(self._h, ctypes.byref(n)))
+        return n.value
+
+    def tuning(self):
+        t = np.zeros(4, dtype=np.int32)
+        _check(lib().epic_batch_tuning(self._h, _ptr(t)))
+        return [int(x) for x in t]
+
+    @property
+    def stream(self) -> int:
+        return lib().epic_batch_stream(self._h) or 0
+
+    def close(self):
+        if self._h:
+            lib().epic_batch_destroy(self._h)
             self._h = ctypes.c_void_p()
 
     def __del__(self):

@@ -19,8 +19,9 @@ OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libepic2d_gb300.so")
 INCLUDE = os.path.join(os.path.dirname(HERE), "include")
 
-CU_FP64 = ["epic_particles.cu", "epic_field.cu", "epic_mcc.cu", "epic_capi.cu", "epic_noalloc.cu", "epic_sort.cu", "epic_load.cu"]
-CU_FAST = ["epic_mixed.cu", "epic_spectral.cu"]
+CU_FP64 = ["epic_particles.cu", "epic_field.cu", "epic_mcc.cu", "epic_capi.cu", "epic_noalloc.cu", "epic_sort.cu", "epic_load.cu",
+           "epic_batch_grid.cu"]
+CU_FAST = ["epic_mixed.cu", "epic_spectral.cu", "epic_batch.cu"]
 CPP = ["epic_host.cpp", "epic_server.cpp"]
 GENCODE = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -55,6 +56,7 @@ def _deps():
             d.append(os.path.join(CSRC, f))
     d.append(os.path.join(INCLUDE, "epic2d.h"))
     d.append(os.path.join(INCLUDE, "epic2d_serve.h"))
+    d.append(os.path.join(INCLUDE, "epic2d_batch.h"))
     return d
 
 

@@ -1,0 +1,890 @@
+// A batch of independent runs advanced together (include/epic2d_batch.h):
+// the particle kernels, the spectral solve and the loader of the batch, and
+// the host side that lays the runs out, tunes the GEMM tiles and captures a
+// step.  Compiled like epic_mixed.cu / epic_spectral.cu (FP32 contraction
+// allowed), whose per-particle and per-lattice code it calls, so a run rounds
+// as it does alone.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/epic2d_batch.h"
+#include "epic_batch.cuh"
+#include "epic_host.h"
+#include "epic_mixed.cuh"
+#include "epic_spectral.cuh"
+
+namespace epic {
+
+constexpr int BATCH_STAGES = 6;  // refinement stages of the spectral solve (as a single run)
+
+// ------------------------------------------------------------ loading ---
+// AoS records of one run's species (epic_load.cu's loader) into the batch's
+// particle array: the single-run conversion (k_aos_to_mixed) with the cell
+// moved to the run's place in the node space.
+__global__ void k_batch_from_aos(BRun r, const double* __restrict__ aos, MixedSoA p, long long base, long long n,
+                                 int* flags) {
+  bool bad = false;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const double* a = aos + 5 * q;
+    double lx = (a[0] - r.x0) / r.dx, ly = (a[1] - r.y0) / r.dy;
+    double fi = floor(lx), fj = floor(ly);
+    int i = (int)fi, j = (int)fj;
+    float ox = (float)(lx - fi), oy = (float)(ly - fj);
+    if (ox >= 1.f) { ox = 0.f; i++; }
+    if (oy >= 1.f) { oy = 0.f; j++; }
+    if (i < 0 || i > r.nx - 2 || j < 0 || j > r.ny - 2) {
+      bad = true;
+      i = min(max(i, 0), r.nx - 2);
+      j = min(max(j, 0), r.ny - 2);
+    }
+    const long long o = base + q;
+    p.cell[o] = (int)(r.node_off + i * r.ny + j);
+    p.ox[o] = ox;
+    p.oy[o] = oy;
+    p.vx[o] = (float)a[2];
+    p.vy[o] = (float)a[3];
+    p.vz[o] = (float)a[4];
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(flags, FLAG_OUT_OF_GRID);
+}
+
+// One run's particles of a species as {x, y, vx, vy, vz} (k_mixed_to_aos).
+__global__ void k_batch_to_aos(BRun r, double* __restrict__ aos, MixedSoA p, long long base, long long n) {
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const long long o = base + q;
+    const int c = (int)(p.cell[o] - r.node_off);
+    const int i = c / r.ny, j = c - i * r.ny;
+    double* a = aos + 5 * q;
+    a[0] = __dadd_rn(r.x0, __dmul_rn(__dadd_rn((double)i, (double)p.ox[o]), r.dx));
+    a[1] = __dadd_rn(r.y0, __dmul_rn(__dadd_rn((double)j, (double)p.oy[o]), r.dy));
+    a[2] = p.vx[o];
+    a[3] = p.vy[o];
+    a[4] = p.vz[o];
+  }
+}
+
+// ---------------------------------------------------------- particles ---
+__device__ __forceinline__ Geom run_geom(const BRun& r) {
+  Geom g;
+  g.nx = r.nx;
+  g.ny = r.ny;
+  g.x0 = r.x0;
+  g.y0 = r.y0;
+  g.dx = r.dx;
+  g.dy = r.dy;
+  g.Lx = g.Ly = 0;
+  return g;
+}
+
+// The single-run push (push_mixed_one) of every particle of a species, each
+// with its run's grid, field and constants.
+__global__ void __launch_bounds__(PART_THREADS) k_batch_push(const BRun* __restrict__ runs,
+                                                             const int* __restrict__ node_run, MixedSoA p,
+                                                             const long long* __restrict__ d_n,
+                                                             const float2* __restrict__ ef32, int s) {
+  const long long n = *d_n;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const int cg = p.cell[q];
+    const BRun& r = runs[node_run[cg]];
+    const Geom g = run_geom(r);
+    const float2* ef = ef32 + r.node_off;
+    int c = (int)(cg - r.node_off);
+    float ox = p.ox[q], oy = p.oy[q], vx = p.vx[q], vy = p.vy[q];
+    if (r.bc == EPIC_PBC) push_mixed_one<EPIC_CIC, EPIC_PBC>(g, ef, r.qmK_dt[s], r.cx, r.cy, c, ox, oy, vx, vy);
+    else push_mixed_one<EPIC_CIC, EPIC_REFLECTIVE>(g, ef, r.qmK_dt[s], r.cx, r.cy, c, ox, oy, vx, vy);
+    p.cell[q] = (int)(r.node_off + c);
+    p.ox[q] = ox;
+    p.oy[q] = oy;
+    p.vx[q] = vx;
+    p.vy[q] = vy;
+  }
+}
+
+__global__ void __launch_bounds__(PART_THREADS) k_batch_rewind(const BRun* __restrict__ runs,
+                                                               const int* __restrict__ node_run, MixedSoA p,
+                                                               const long long* __restrict__ d_n,
+                                                               const float2* __restrict__ ef32, int s) {
+  const long long n = *d_n;
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
+    const int cg = p.cell[q];
+    const BRun& r = runs[node_run[cg]];
+    float ex, ey;
+    gather32<EPIC_CIC>(run_geom(r), ef32 + r.node_off, (int)(cg - r.node_off), p.ox[q], p.oy[q], ex, ey);
+    const float h = r.hqmK_dt[s];
+    p.vx[q] = fmaf(-h, ex, p.vx[q]);
+    p.vy[q] = fmaf(-h, ey, p.vy[q]);
+  }
+}
+
+// Integer CIC deposit of a species (the mixed form's weights, exact, so the
+// grid is the single runs' bit for bit).  Each CTA takes 2048 consecutive
+// particles; when the nodes they touch fit in shared memory (sorted
+// particles) runs of equal cells merge in registers and the CTA adds its
+// range once, otherwise particles add straight to the grid.
+constexpr int BDEP_PER_THREAD = 8;
+constexpr int BDEP_CHUNK = PART_THREADS * BDEP_PER_THREAD;
+constexpr int BDEP_SMEM = 3072;
+
+__global__ void __launch_bounds__(PART_THREADS) k_batch_deposit(const BRun* __restrict__ runs,
+                                                                const int* __restrict__ node_run, MixedSoA p,
+                                                                const long long* __restrict__ d_n,
+                                                                unsigned long long* __restrict__ acc) {
+  __shared__ unsigned long long sacc[BDEP_SMEM];
+  __shared__ int s_lo, s_hi;
+  const long long n = *d_n;
+  const int S = 1 << MIXED_OFFSET_BITS;
+  const float fS = (float)S;
+  if (threadIdx.x == 0) {
+    s_lo = INT_MAX;
+    s_hi = -1;
+  }
+  __syncthreads();
+  for (long long chunk = (long long)blockIdx.x * BDEP_CHUNK; chunk < n; chunk += (long long)gridDim.x * BDEP_CHUNK) {
+    const long long q0 = chunk + (long long)threadIdx.x * BDEP_PER_THREAD;
+    int c[BDEP_PER_THREAD], ny[BDEP_PER_THREAD];
+    float ox[BDEP_PER_THREAD], oy[BDEP_PER_THREAD];
+    int lo = INT_MAX, hi = -1;
+#pragma unroll
+    for (int k = 0; k < BDEP_PER_THREAD; k++) {
+      const long long q = q0 + k;
+      c[k] = q < n ? p.cell[q] : -1;
+      ox[k] = q < n ? p.ox[q] : 0.f;
+      oy[k] = q < n ? p.oy[q] : 0.f;
+      ny[k] = c[k] >= 0 ? runs[node_run[c[k]]].ny : 0;
+      if (c[k] >= 0) {
+        lo = min(lo, c[k]);
+        hi = max(hi, c[k] + ny[k] + 1);
+      }
+    }
+    lo = __reduce_min_sync(0xffffffffu, lo);
+    hi = __reduce_max_sync(0xffffffffu, hi);
+    if ((threadIdx.x & 31) == 0) {
+      atomicMin(&s_lo, lo);
+      atomicMax(&s_hi, hi);
+    }
+    __syncthreads();
+    const int blo = s_lo, bhi = s_hi;
+    const int span = bhi < 0 ? 0 : bhi + 1 - blo;
+    const bool smem = span <= BDEP_SMEM;
+    if (smem)
+      for (int m = threadIdx.x; m < span; m += PART_THREADS) sacc[m] = 0;
+    __syncthreads();
+    auto flush = [&](int cc, int nyy, unsigned long long w00, unsigned long long w10, unsigned long long w01,
+                     unsigned long long w11) {
+      if (cc < 0) return;
+      if (smem) {
+        atomicAdd(&sacc[cc - blo], w00);
+        atomicAdd(&sacc[cc - blo + nyy], w10);
+        atomicAdd(&sacc[cc - blo + 1], w01);
+        atomicAdd(&sacc[cc - blo + nyy + 1], w11);
+      } else {
+        atomicAdd(&acc[cc], w00);
+        atomicAdd(&acc[cc + nyy], w10);
+        atomicAdd(&acc[cc + 1], w01);
+        atomicAdd(&acc[cc + nyy + 1], w11);
+      }
+    };
+    int cur = -1, cur_ny = 0;
+    unsigned long long a00 = 0, a10 = 0, a01 = 0, a11 = 0;
+#pragma unroll
+    for (int k = 0; k < BDEP_PER_THREAD; k++) {
+      if (c[k] < 0) continue;
+      const unsigned long long a = (unsigned long long)(int)(ox[k] * fS), b = (unsigned long long)(int)(oy[k] * fS);
+      const unsigned long long w00 = (S - a) * (S - b), w10 = a * (S - b), w01 = (S - a) * b, w11 = a * b;
+      if (c[k] != cur) {
+        flush(cur, cur_ny, a00, a10, a01, a11);
+        cur = c[k];
+        cur_ny = ny[k];
+        a00 = w00; a10 = w10; a01 = w01; a11 = w11;
+      } else {
+        a00 += w00; a10 += w10; a01 += w01; a11 += w11;
+      }
+    }
+    flush(cur, cur_ny, a00, a10, a01, a11);
+    __syncthreads();
+    if (smem)
+      for (int m = threadIdx.x; m < span; m += PART_THREADS) {
+        const unsigned long long v = sacc[m];
+        if (v) atomicAdd(&acc[blo + m], v);
+      }
+    if (threadIdx.x == 0) {
+      s_lo = INT_MAX;
+      s_hi = -1;
+    }
+    __syncthreads();
+  }
+}
+
+// -------------------------------------------------------------- solve ---
+struct BatchSpec {
+  const BRun* runs;
+  double* phi;
+  const double* rho;
+  const float* Q;
+  const float* D;
+  float *t0, *t1;
+  double* partials;
+  int* state;  // 4 per run
+};
+
+__device__ __forceinline__ SpecLattice run_lattice(const BatchSpec& b, int ri) {
+  const BRun& r = b.runs[ri];
+  SpecLattice L;
+  L.nx = r.nx;
+  L.ny = r.ny;
+  L.I_off = 0;
+  L.NY = r.ny;
+  L.R = r.R;
+  L.C = r.C;
+  L.flat = r.flat;
+  L.gs_norm = r.gs_norm;
+  L.dx2 = r.dx * r.dx;
+  L.K = r.K;
+  L.tol = r.tol;
+  L.rho = b.rho + r.node_off;
+  L.phi = b.phi + r.node_off;
+  L.t0 = b.t0 + r.lat_off;
+  L.partials = b.partials + r.chunk_off;
+  L.state = b.state + 4 * ri;
+  L.info = nullptr;
+  L.iter_total = nullptr;
+  return L;
+}
+
+__global__ void k_batch_spec_init(BatchSpec b, const int* __restrict__ node_run, long long nodes, int nruns) {
+  for (long long k = (long long)blockIdx.x * blockDim.x + threadIdx.x; k < nodes; k += (long long)gridDim.x * blockDim.x)
+    b.phi[k] = 0;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nruns; r += gridDim.x * blockDim.x) {
+    b.state[4 * r] = 0;
+    b.state[4 * r + 1] = 0;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_batch_spec_residual(BatchSpec b, const int2* __restrict__ sched) {
+  const int2 e = sched[blockIdx.x];  // (run, chunk)
+  if (b.state[4 * e.x]) return;
+  __shared__ double sm[8];
+  spec_residual_chunk(run_lattice(b, e.x), e.y, sm);
+}
+
+__global__ void k_batch_spec_check(BatchSpec b, int nruns, int final_pass) {
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < nruns; r += gridDim.x * blockDim.x)
+    spec_check(run_lattice(b, r), final_pass);
+}
+
+// One of the four products of a refinement stage for every (run, tile) of
+// the schedule: 0 t1 = Q_R t0; 1 t0 = (t1 Q_C) o D; 2 t1 = Q_R t0; 3 phi += t1 Q_C.
+template <int PROD, int TILE>
+__global__ void __launch_bounds__(256) k_batch_spec_gemm(BatchSpec b, const int4* __restrict__ sched) {
+  const int4 e = sched[blockIdx.x];  // (run, tile row, tile col)
+  if (b.state[4 * e.x]) return;
+  __shared__ float As[32][33];
+  __shared__ float Bs[32][33];
+  const BRun& r = b.runs[e.x];
+  const SpecLattice L = run_lattice(b, e.x);
+  float* t0 = b.t0 + r.lat_off;
+  float* t1 = b.t1 + r.lat_off;
+  const float* QR = b.Q + r.qR_off;
+  const float* QC = b.Q + r.qC_off;
+  if (PROD == 0 || PROD == 2)
+    spec_gemm_tile<0, TILE>(r.R, r.C, r.R, QR, t0, t1, nullptr, &L, e.y, e.z, As, Bs);
+  else if (PROD == 1)
+    spec_gemm_tile<1, TILE>(r.R, r.C, r.C, t1, QC, t0, b.D + r.lat_off, &L, e.y, e.z, As, Bs);
+  else
+    spec_gemm_tile<2, TILE>(r.R, r.C, r.C, t1, QC, nullptr, nullptr, &L, e.y, e.z, As, Bs);
+}
+
+}  // namespace epic
+
+// ================================================================ host ===
+using namespace epic;
+
+namespace {
+
+epic_status bfail(epic_status st, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  set_last_error(buf);
+  return st;
+}
+
+#define BCK(call)                                                                                       \
+  do {                                                                                                  \
+    cudaError_t e_ = (call);                                                                            \
+    if (e_ != cudaSuccess)                                                                              \
+      return bfail(e_ == cudaErrorMemoryAllocation ? EPIC_ERR_NOMEM : EPIC_ERR_CUDA, "%s: %s", #call,  \
+                   cudaGetErrorString(e_));                                                             \
+  } while (0)
+
+int size_class(int R, int C) {
+  const int m = std::max(R, C);
+  return m <= 48 ? 0 : m <= 96 ? 1 : m <= 160 ? 2 : 3;
+}
+
+}  // namespace
+
+struct epic_batch {
+  int nruns = 0, nsp = 0, sort_every = 0;
+  long long nodes = 0;
+  int num_sms = 0, grid = 0;
+  cudaStream_t stream = nullptr;
+  std::vector<BRun> runs;
+  std::vector<epic_request> reqs;
+  std::vector<long long> poff, pn;  // [run * nsp + s]
+  BRun* d_runs = nullptr;
+  int* d_node_run = nullptr;
+  double *phi = nullptr, *rho = nullptr, *efx = nullptr, *efy = nullptr;
+  float2* ef32 = nullptr;
+  MixedSoA arena[BATCH_MAX_SPECIES];
+  long long* d_n[BATCH_MAX_SPECIES];
+  long long cap[BATCH_MAX_SPECIES];
+  unsigned long long* acc[BATCH_MAX_SPECIES];
+  float *Q = nullptr, *D = nullptr, *t0 = nullptr, *t1 = nullptr;
+  double* partials = nullptr;
+  int* state = nullptr;
+  int* flags = nullptr;
+  int2* chunk_sched = nullptr;
+  int nchunk = 0;
+  int4* tile_sched[2] = {nullptr, nullptr};  // TILE 16, 32
+  int ntile[2] = {0, 0};
+  int tiles[4] = {32, 32, 32, 32};
+  void* sort_buf = nullptr;
+  double* staging = nullptr;
+  int64_t step_index = 0;
+  cudaGraphExec_t g_plain = nullptr, g_sort = nullptr;
+  std::vector<void*> allocs;
+
+  template <class T>
+  epic_status alloc(T** p, size_t count) {
+    *p = nullptr;
+    BCK(cudaMallocAsync((void**)p, std::max<size_t>(count, 1) * sizeof(T), stream));
+    BCK(cudaMemsetAsync(*p, 0, std::max<size_t>(count, 1) * sizeof(T), stream));
+    allocs.push_back(*p);
+    return EPIC_OK;
+  }
+
+  BatchSpec spec() const {
+    BatchSpec b;
+    b.runs = d_runs;
+    b.phi = phi;
+    b.rho = rho;
+    b.Q = Q;
+    b.D = D;
+    b.t0 = t0;
+    b.t1 = t1;
+    b.partials = partials;
+    b.state = state;
+    return b;
+  }
+
+  BatchGrids grids() const {
+    BatchGrids g;
+    g.nruns = nruns;
+    g.nsp = nsp;
+    g.nodes = nodes;
+    g.runs = d_runs;
+    g.node_run = d_node_run;
+    g.phi = phi;
+    g.rho = rho;
+    g.efx = efx;
+    g.efy = efy;
+    g.ef32 = ef32;
+    for (int s = 0; s < BATCH_MAX_SPECIES; s++) g.acc[s] = s < nsp ? acc[s] : nullptr;
+    return g;
+  }
+
+  void launch_gemms(int prod, int which) {
+    const BatchSpec b = spec();
+    const int n = ntile[which];
+    if (!n) return;
+    const int4* sc = tile_sched[which];
+    if (which == 0) {
+      if (prod == 0 || prod == 2) k_batch_spec_gemm<0, 16><<<n, 256, 0, stream>>>(b, sc);
+      else if (prod == 1) k_batch_spec_gemm<1, 16><<<n, 256, 0, stream>>>(b, sc);
+      else k_batch_spec_gemm<3, 16><<<n, 256, 0, stream>>>(b, sc);
+    } else {
+      if (prod == 0 || prod == 2) k_batch_spec_gemm<0, 32><<<n, 256, 0, stream>>>(b, sc);
+      else if (prod == 1) k_batch_spec_gemm<1, 32><<<n, 256, 0, stream>>>(b, sc);
+      else k_batch_spec_gemm<3, 32><<<n, 256, 0, stream>>>(b, sc);
+    }
+  }
+
+  void solve() {
+    const BatchSpec b = spec();
+    k_batch_spec_init<<<grid, 256, 0, stream>>>(b, d_node_run, nodes, nruns);
+    for (int st = 0; st < BATCH_STAGES; st++) {
+      k_batch_spec_residual<<<nchunk, 256, 0, stream>>>(b, chunk_sched);
+      k_batch_spec_check<<<(nruns + 255) / 256, 256, 0, stream>>>(b, nruns, 0);
+      for (int prod = 0; prod < 4; prod++)
+        for (int w = 0; w < 2; w++) launch_gemms(prod, w);
+    }
+    k_batch_spec_residual<<<nchunk, 256, 0, stream>>>(b, chunk_sched);
+    k_batch_spec_check<<<(nruns + 255) / 256, 256, 0, stream>>>(b, nruns, 1);
+  }
+
+  void deposit_and_solve() {
+    for (int s = 0; s < nsp; s++) {
+      cudaMemsetAsync(acc[s], 0, nodes * sizeof(unsigned long long), stream);
+      k_batch_deposit<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], acc[s]);
+    }
+    launch_batch_finalize(stream, grids());
+    solve();
+    launch_batch_efield(stream, grids());
+  }
+
+  void sort_all() {
+    Geom g;
+    std::memset(&g, 0, sizeof(g));
+    g.nx = 1;
+    g.ny = (int)nodes;
+    for (int s = 0; s < nsp; s++) {
+      ParticleRef p;
+      std::memset(&p, 0, sizeof(p));
+      p.mixed = 1;
+      p.m = arena[s];
+      launch_sort(stream, g, p, d_n[s], cap[s], carve_sort_scratch(sort_buf, cap[s]), grid);
+    }
+  }
+
+  void step(int sort) {
+    if (sort) sort_all();
+    deposit_and_solve();
+    for (int s = 0; s < nsp; s++)
+      k_batch_push<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s);
+  }
+};
+
+namespace {
+
+// Builds the GEMM tile schedules: per size class the tile the autotuner chose.
+void build_tile_sched(epic_batch* b, std::vector<int4> (&by_tile)[2]) {
+  by_tile[0].clear();
+  by_tile[1].clear();
+  for (int r = 0; r < b->nruns; r++) {
+    const BRun& br = b->runs[r];
+    const int t = b->tiles[size_class(br.R, br.C)];
+    const int w = t == 16 ? 0 : 1;
+    for (int tr = 0; tr < (br.R + t - 1) / t; tr++)
+      for (int tc = 0; tc < (br.C + t - 1) / t; tc++) by_tile[w].push_back(make_int4(r, tr, tc, 0));
+  }
+}
+
+epic_status upload_tile_sched(epic_batch* b) {
+  std::vector<int4> by_tile[2];
+  build_tile_sched(b, by_tile);
+  for (int w = 0; w < 2; w++) {
+    if (b->tile_sched[w]) cudaFreeAsync(b->tile_sched[w], b->stream);
+    b->tile_sched[w] = nullptr;
+    b->ntile[w] = (int)by_tile[w].size();
+    if (!b->ntile[w]) continue;
+    BCK(cudaMallocAsync((void**)&b->tile_sched[w], by_tile[w].size() * sizeof(int4), b->stream));
+    BCK(cudaMemcpyAsync(b->tile_sched[w], by_tile[w].data(), by_tile[w].size() * sizeof(int4),
+                        cudaMemcpyHostToDevice, b->stream));
+  }
+  BCK(cudaStreamSynchronize(b->stream));
+  return EPIC_OK;
+}
+
+// Times one refinement stage's four products for the runs of each size class
+// with 16- and 32-wide tiles and keeps the faster per class (identical
+// results either way).  Runs before the initial field: it only writes the
+// transform scratch and phi, which every solve starts over.
+epic_status autotune(epic_batch* b) {
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best[4][2];
+  for (int cls = 0; cls < 4; cls++) best[cls][0] = best[cls][1] = 0;
+  for (int w = 0; w < 2; w++) {
+    for (int cls = 0; cls < 4; cls++) {
+      bool any = false;
+      for (int r = 0; r < b->nruns; r++) any |= size_class(b->runs[r].R, b->runs[r].C) == cls;
+      if (!any) continue;
+      int saved[4];
+      std::memcpy(saved, b->tiles, sizeof(saved));
+      for (int c = 0; c < 4; c++) b->tiles[c] = 0;  // only this class is scheduled
+      b->tiles[cls] = w ? 32 : 16;
+      std::vector<int4> by_tile[2];
+      for (int r = 0; r < b->nruns; r++) {
+        const BRun& br = b->runs[r];
+        if (size_class(br.R, br.C) != cls) continue;
+        const int t = b->tiles[cls];
+        for (int tr = 0; tr < (br.R + t - 1) / t; tr++)
+          for (int tc = 0; tc < (br.C + t - 1) / t; tc++) by_tile[w].push_back(make_int4(r, tr, tc, 0));
+      }
+      std::memcpy(b->tiles, saved, sizeof(saved));
+      int4* sc = nullptr;
+      BCK(cudaMallocAsync((void**)&sc, by_tile[w].size() * sizeof(int4), b->stream));
+      BCK(cudaMemcpyAsync(sc, by_tile[w].data(), by_tile[w].size() * sizeof(int4), cudaMemcpyHostToDevice,
+                          b->stream));
+      int4* keep[2] = {b->tile_sched[0], b->tile_sched[1]};
+      const int nkeep[2] = {b->ntile[0], b->ntile[1]};
+      b->tile_sched[0] = b->tile_sched[1] = nullptr;
+      b->ntile[0] = b->ntile[1] = 0;
+      b->tile_sched[w] = sc;
+      b->ntile[w] = (int)by_tile[w].size();
+      for (int rep = 0; rep < 2; rep++)
+        for (int prod = 0; prod < 4; prod++) b->launch_gemms(prod, w);  // warm-up
+      cudaEventRecord(e0, b->stream);
+      for (int rep = 0; rep < 5; rep++)
+        for (int prod = 0; prod < 4; prod++) b->launch_gemms(prod, w);
+      cudaEventRecord(e1, b->stream);
+      BCK(cudaEventSynchronize(e1));
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      best[cls][w] = ms;
+      cudaFreeAsync(sc, b->stream);
+      b->tile_sched[0] = keep[0];
+      b->tile_sched[1] = keep[1];
+      b->ntile[0] = nkeep[0];
+      b->ntile[1] = nkeep[1];
+    }
+  }
+  for (int cls = 0; cls < 4; cls++)
+    if (best[cls][0] > 0 && best[cls][1] > 0) b->tiles[cls] = best[cls][0] < best[cls][1] ? 16 : 32;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  BCK(cudaGetLastError());
+  return upload_tile_sched(b);
+}
+
+// Transforms of side n (orthonormal DST-I) and eigenvalues, as the single run.
+void sine_transform_h(int n, std::vector<float>& Q, std::vector<double>& lam) {
+  const double pi = 3.14159265358979323846;
+  const double c = std::sqrt(2.0 / (n + 1));
+  Q.assign((size_t)n * n, 0.f);
+  lam.assign(n, 0.0);
+  for (int j = 0; j < n; j++) {
+    for (int k = 0; k < n; k++) Q[(size_t)j * n + k] = (float)(c * std::sin(pi * (j + 1) * (double)(k + 1) / (n + 1)));
+    const double sn = std::sin(pi * (j + 1) / (2.0 * (n + 1)));
+    lam[j] = -4.0 * sn * sn;
+  }
+}
+
+epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
+  if (nruns < 1) return bfail(EPIC_ERR_INVALID, "empty batch");
+  b->nruns = nruns;
+  b->reqs.assign(reqs, reqs + nruns);
+  b->nsp = reqs[0].num_species;
+  if (b->nsp < 1 || b->nsp > BATCH_MAX_SPECIES)
+    return bfail(EPIC_ERR_INVALID, "a batch holds 1 to %d species per run", BATCH_MAX_SPECIES);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&b->num_sms, cudaDevAttrMultiProcessorCount, dev);
+  b->grid = b->num_sms * 8;
+  BCK(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  // Lay out runs, lattices, transforms.
+  b->runs.resize(nruns);
+  b->poff.assign((size_t)nruns * b->nsp, 0);
+  b->pn.assign((size_t)nruns * b->nsp, 0);
+  long long node_off = 0, lat_off = 0, qpool = 0;
+  int chunk_off = 0;
+  std::vector<long long> q_off_of_side(4096, -1);
+  std::vector<std::pair<int, long long>> sides;  // (side, offset) of each transform
+  std::vector<int2> chunks;
+  for (int r = 0; r < nruns; r++) {
+    const epic_config& c = reqs[r].cfg;
+    if (reqs[r].num_species != b->nsp) return bfail(EPIC_ERR_INVALID, "run %d: every run needs %d species", r, b->nsp);
+    if (c.precision != EPIC_PRECISION_MIXED) return bfail(EPIC_ERR_INVALID, "run %d: batches run the mixed form", r);
+    if (c.shape != EPIC_CIC) return bfail(EPIC_ERR_INVALID, "run %d: batches deposit with CIC", r);
+    if (c.bc != EPIC_PBC && c.bc != EPIC_REFLECTIVE)
+      return bfail(EPIC_ERR_INVALID, "run %d: batches take periodic or reflective walls", r);
+    if (reqs[r].collisions) return bfail(EPIC_ERR_INVALID, "run %d: batches run without collisions", r);
+    const Geom g{c.nx, c.ny, c.x0, c.y0, c.dx, c.dy, 0, 0};
+    if (!spectral_supported(g, c.solver)) return bfail(EPIC_ERR_INVALID, "run %d: grid not supported", r);
+    if (c.nx > 4095 || c.ny > 4095) return bfail(EPIC_ERR_INVALID, "run %d: grid too large for a batch", r);
+    BRun& br = b->runs[r];
+    std::memset(&br, 0, sizeof(br));
+    br.nx = c.nx;
+    br.ny = c.ny;
+    br.bc = c.bc;
+    br.node_off = node_off;
+    br.x0 = c.x0;
+    br.y0 = c.y0;
+    br.dx = c.dx;
+    br.dy = c.dy;
+    const double K = (c.density * QE * c.L) / (EPS_0 * c.W * c.vel_norm);
+    const double cc = c.vel_norm / (c.L * c.W);
+    const double dtsub = c.DT * 1;
+    br.cx = (float)(cc * dtsub / c.dx);
+    br.cy = (float)(cc * dtsub / c.dy);
+    for (int s = 0; s < b->nsp; s++) {
+      const epic_species_desc& d = reqs[r].species[s];
+      const double qm = d.charge / d.mass;
+      const double qmK = qm * K;
+      br.qmK_dt[s] = (float)(qmK * dtsub);
+      const double hqmK = 0.5 * qm * K;
+      br.hqmK_dt[s] = (float)(hqmK * c.DT);
+      br.spwt[s] = d.spwt;
+      br.charge_over_qe[s] = d.charge * (1 / QE);
+    }
+    const double cell_area = c.dx * c.dy;
+    const double L2 = c.L * c.L;
+    br.div = cell_area * L2 * c.density;
+    br.inv_scale = std::ldexp(1.0, -2 * MIXED_OFFSET_BITS);
+    br.K = (c.L * c.L) / (c.LDe * c.LDe);
+    br.tol = c.tolerance;
+    const bool gs = c.solver == EPIC_SOLVER_GS;
+    br.flat = !gs;
+    br.gs_norm = gs;
+    br.R = gs ? c.nx - 2 : c.ny;
+    br.C = gs ? c.ny - 2 : c.nx;
+    br.lat_off = lat_off;
+    for (int side : {br.R, br.C}) {
+      if (q_off_of_side[side] < 0) {
+        q_off_of_side[side] = qpool;
+        sides.push_back({side, qpool});
+        qpool += (long long)side * side;
+      }
+    }
+    br.qR_off = q_off_of_side[br.R];
+    br.qC_off = q_off_of_side[br.C];
+    br.chunk_off = chunk_off;
+    const int nch = (br.R * br.C + SPEC_CHUNK - 1) / SPEC_CHUNK;
+    for (int k = 0; k < nch; k++) chunks.push_back(make_int2(r, k));
+    chunk_off += nch;
+    lat_off += (long long)br.R * br.C;
+    node_off += (long long)c.nx * c.ny;
+  }
+  b->nodes = node_off;
+  if (b->nodes >= INT_MAX) return bfail(EPIC_ERR_INVALID, "batch node space above 2^31");
+  // Particle arrays: run r's species s at poff, in run order.
+  for (int s = 0; s < b->nsp; s++) {
+    long long off = 0;
+    for (int r = 0; r < nruns; r++) {
+      b->poff[(size_t)r * b->nsp + s] = off;
+      b->pn[(size_t)r * b->nsp + s] = reqs[r].species[s].numparticle;
+      off += reqs[r].species[s].numparticle;
+    }
+    b->cap[s] = std::max<long long>(off, 1);
+  }
+  epic_status st;
+  if ((st = b->alloc(&b->d_runs, nruns))) return st;
+  if ((st = b->alloc(&b->d_node_run, b->nodes))) return st;
+  if ((st = b->alloc(&b->phi, b->nodes))) return st;
+  if ((st = b->alloc(&b->rho, b->nodes))) return st;
+  if ((st = b->alloc(&b->efx, b->nodes))) return st;
+  if ((st = b->alloc(&b->efy, b->nodes))) return st;
+  if ((st = b->alloc(&b->ef32, b->nodes))) return st;
+  if ((st = b->alloc(&b->Q, qpool))) return st;
+  if ((st = b->alloc(&b->D, lat_off))) return st;
+  if ((st = b->alloc(&b->t0, lat_off))) return st;
+  if ((st = b->alloc(&b->t1, lat_off))) return st;
+  if ((st = b->alloc(&b->partials, chunk_off))) return st;
+  if ((st = b->alloc(&b->state, 4 * (size_t)nruns))) return st;
+  if ((st = b->alloc(&b->flags, 1))) return st;
+  if ((st = b->alloc(&b->chunk_sched, chunks.size()))) return st;
+  b->nchunk = (int)chunks.size();
+  for (int s = 0; s < b->nsp; s++) {
+    const size_t cap = (size_t)b->cap[s];
+    MixedSoA& m = b->arena[s];
+    if ((st = b->alloc(&m.cell, cap)) || (st = b->alloc(&m.ox, cap)) || (st = b->alloc(&m.oy, cap)) ||
+        (st = b->alloc(&m.vx, cap)) || (st = b->alloc(&m.vy, cap)) || (st = b->alloc(&m.vz, cap)))
+      return st;
+    if ((st = b->alloc(&b->d_n[s], 1))) return st;
+    if ((st = b->alloc(&b->acc[s], b->nodes))) return st;
+  }
+  long long cmax = 0, nmax = 1;
+  for (int s = 0; s < b->nsp; s++) cmax = std::max(cmax, b->cap[s]);
+  for (long long v : b->pn) nmax = std::max(nmax, v);
+  if (b->sort_every > 0) {
+    BCK(cudaMallocAsync(&b->sort_buf, sort_scratch_bytes(cmax), b->stream));
+    b->allocs.push_back(b->sort_buf);
+  }
+  if ((st = b->alloc(&b->staging, (size_t)nmax * 5))) return st;
+  // Host tables to the device.
+  std::vector<int> node_run(b->nodes);
+  for (int r = 0; r < nruns; r++)
+    std::fill(node_run.begin() + b->runs[r].node_off,
+              node_run.begin() + b->runs[r].node_off + (long long)b->runs[r].nx * b->runs[r].ny, r);
+  std::vector<float> Qh(std::max<long long>(qpool, 1)), Dh(std::max<long long>(lat_off, 1));
+  std::vector<std::vector<double>> lam_of_side(4096);
+  for (auto& sd : sides) {
+    std::vector<float> q;
+    sine_transform_h(sd.first, q, lam_of_side[sd.first]);
+    std::copy(q.begin(), q.end(), Qh.begin() + sd.second);
+  }
+  for (int r = 0; r < nruns; r++) {
+    const BRun& br = b->runs[r];
+    const std::vector<double>& lR = lam_of_side[br.R];
+    const std::vector<double>& lC = lam_of_side[br.C];
+    for (int p = 0; p < br.R; p++)
+      for (int q = 0; q < br.C; q++) Dh[br.lat_off + (long long)p * br.C + q] = (float)(1.0 / (lR[p] + lC[q]));
+  }
+  BCK(cudaMemcpyAsync(b->d_runs, b->runs.data(), nruns * sizeof(BRun), cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(b->d_node_run, node_run.data(), node_run.size() * sizeof(int), cudaMemcpyHostToDevice,
+                      b->stream));
+  BCK(cudaMemcpyAsync(b->Q, Qh.data(), qpool * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(b->D, Dh.data(), lat_off * sizeof(float), cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemcpyAsync(b->chunk_sched, chunks.data(), chunks.size() * sizeof(int2), cudaMemcpyHostToDevice,
+                      b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return autotune(b);
+}
+
+epic_status take_flags(epic_batch* b) {
+  int f = 0;
+  BCK(cudaMemcpyAsync(&f, b->flags, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  if (!f) return EPIC_OK;
+  cudaMemsetAsync(b->flags, 0, sizeof(int), b->stream);
+  if (f & FLAG_OUT_OF_GRID) return bfail(EPIC_ERR_DOMAIN, "a particle was loaded outside its run's grid");
+  return bfail(EPIC_ERR_CUDA, "device flags 0x%x", f);
+}
+
+}  // namespace
+
+extern "C" {
+
+epic_status epic_batch_create(const epic_request* runs, int nruns, int sort_every, epic_batch** out) {
+  if (!runs || !out || sort_every < 0) return bfail(EPIC_ERR_INVALID, "bad argument");
+  epic_batch* b = new epic_batch();
+  std::memset(b->arena, 0, sizeof(b->arena));
+  std::memset(b->d_n, 0, sizeof(b->d_n));
+  std::memset(b->acc, 0, sizeof(b->acc));
+  b->sort_every = sort_every;
+  epic_status st = build(b, runs, nruns);
+  if (st) {
+    epic_batch_destroy(b);
+    return st;
+  }
+  *out = b;
+  return EPIC_OK;
+}
+
+void epic_batch_destroy(epic_batch* b) {
+  if (!b) return;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (b->g_plain) cudaGraphExecDestroy(b->g_plain);
+  if (b->g_sort) cudaGraphExecDestroy(b->g_sort);
+  for (void* p : b->allocs) cudaFreeAsync(p, b->stream);
+  for (int w = 0; w < 2; w++)
+    if (b->tile_sched[w]) cudaFreeAsync(b->tile_sched[w], b->stream);
+  if (b->stream) {
+    cudaStreamSynchronize(b->stream);
+    cudaStreamDestroy(b->stream);
+  }
+  delete b;
+}
+
+epic_status epic_batch_initial_field(epic_batch* b) {
+  if (!b) return bfail(EPIC_ERR_INVALID, "null batch");
+  for (int r = 0; r < b->nruns; r++) {
+    const epic_request& q = b->reqs[r];
+    const Geom g{q.cfg.nx, q.cfg.ny, q.cfg.x0, q.cfg.y0, q.cfg.dx, q.cfg.dy, 0, 0};
+    for (int s = 0; s < b->nsp; s++) {
+      int kind = 0, narg = 0;
+      std::string err;
+      if (parse_load_type(q.species[s].load, &kind, &narg, err)) return bfail(EPIC_ERR_INVALID, "%s", err.c_str());
+      const long long n = b->pn[(size_t)r * b->nsp + s];
+      launch_load(b->stream, g, q.species[s], q.cfg, s, kind, narg, b->staging, q.load_seed, b->grid);
+      if (n)
+        k_batch_from_aos<<<b->grid, PART_THREADS, 0, b->stream>>>(b->runs[r], b->staging, b->arena[s],
+                                                                   b->poff[(size_t)r * b->nsp + s], n, b->flags);
+    }
+  }
+  for (int s = 0; s < b->nsp; s++) {
+    long long total = 0;
+    for (int r = 0; r < b->nruns; r++) total += b->pn[(size_t)r * b->nsp + s];
+    launch_set_count(b->stream, b->d_n[s], total);
+  }
+  b->deposit_and_solve();
+  for (int s = 0; s < b->nsp; s++)
+    k_batch_rewind<<<b->grid, PART_THREADS, 0, b->stream>>>(b->d_runs, b->d_node_run, b->arena[s], b->d_n[s],
+                                                             b->ef32, s);
+  BCK(cudaGetLastError());
+  b->step_index = 0;
+  return take_flags(b);
+}
+
+epic_status epic_batch_run(epic_batch* b, int steps, int use_graph) {
+  if (!b || steps < 0) return bfail(EPIC_ERR_INVALID, "bad argument");
+  const bool sorting = b->sort_every > 0;
+  if (!use_graph) {
+    for (int k = 0; k < steps; k++) {
+      b->step(sorting && b->step_index % b->sort_every == 0);
+      b->step_index++;
+    }
+    BCK(cudaGetLastError());
+    return take_flags(b);
+  }
+  auto capture = [&](int sort, cudaGraphExec_t* exec) -> epic_status {
+    cudaGraph_t graph;
+    BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    b->step(sort);
+    cudaError_t ce = cudaStreamEndCapture(b->stream, &graph);
+    if (ce != cudaSuccess) {
+      cudaGetLastError();
+      return bfail(EPIC_ERR_CUDA, "batch graph capture: %s", cudaGetErrorString(ce));
+    }
+    ce = cudaGraphInstantiate(exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return bfail(EPIC_ERR_CUDA, "batch graph instantiate: %s", cudaGetErrorString(ce));
+    return EPIC_OK;
+  };
+  epic_status st;
+  if (!b->g_plain && (st = capture(0, &b->g_plain))) return st;
+  if (sorting && !b->g_sort && (st = capture(1, &b->g_sort))) return st;
+  for (int k = 0; k < steps; k++) {
+    const bool srt = sorting && b->step_index % b->sort_every == 0;
+    b->step_index++;
+    BCK(cudaGraphLaunch(srt ? b->g_sort : b->g_plain, b->stream));
+  }
+  return take_flags(b);
+}
+
+epic_status epic_batch_get_particles(epic_batch* b, int run, int s, double* out, int64_t capacity, int64_t* n) {
+  if (!b || run < 0 || run >= b->nruns || s < 0 || s >= b->nsp || !out)
+    return bfail(EPIC_ERR_INVALID, "bad argument");
+  const long long cnt = b->pn[(size_t)run * b->nsp + s];
+  if (n) *n = cnt;
+  if (cnt > capacity) return bfail(EPIC_ERR_CAPACITY, "%lld particles do not fit %lld records", cnt, (long long)capacity);
+  if (cnt) {
+    k_batch_to_aos<<<b->grid, PART_THREADS, 0, b->stream>>>(b->runs[run], b->staging, b->arena[s],
+                                                             b->poff[(size_t)run * b->nsp + s], cnt);
+    BCK(cudaGetLastError());
+    BCK(cudaMemcpyAsync(out, b->staging, (size_t)cnt * 5 * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  }
+  BCK(cudaStreamSynchronize(b->stream));
+  return EPIC_OK;
+}
+
+epic_status epic_batch_get_grid(epic_batch* b, int run, int which, double* out) {
+  if (!b || run < 0 || run >= b->nruns || !out) return bfail(EPIC_ERR_INVALID, "bad argument");
+  const double* src = which == EPIC_GRID_PHI ? b->phi : which == EPIC_GRID_RHO ? b->rho : nullptr;
+  if (!src) return bfail(EPIC_ERR_INVALID, "batches keep phi and rho");
+  const BRun& r = b->runs[run];
+  BCK(cudaMemcpyAsync(out, src + r.node_off, (size_t)r.nx * r.ny * sizeof(double), cudaMemcpyDeviceToHost,
+                      b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  return EPIC_OK;
+}
+
+epic_status epic_batch_num_particles(epic_batch* b, int64_t* total) {
+  if (!b || !total) return bfail(EPIC_ERR_INVALID, "bad argument");
+  int64_t t = 0;
+  for (long long v : b->pn) t += v;
+  *total = t;
+  return EPIC_OK;
+}
+
+epic_status epic_batch_tuning(epic_batch* b, int tiles[4]) {
+  if (!b || !tiles) return bfail(EPIC_ERR_INVALID, "bad argument");
+  std::memcpy(tiles, b->tiles, sizeof(b->tiles));
+  return EPIC_OK;
+}
+
+void* epic_batch_stream(epic_batch* b) { return b ? (void*)b->stream : nullptr; }
+
+}  // extern "C"

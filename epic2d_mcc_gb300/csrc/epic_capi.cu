@@ -147,7 +147,7 @@ epic_status setup_spectral(epic_sim* s) {
   CK(cudaMallocAsync((void**)&sp.D, D.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.t0, D.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.t1, D.size() * sizeof(float), s->stream));
-  CK(cudaMallocAsync((void**)&sp.partials, 256 * sizeof(double), s->stream));
+  CK(cudaMallocAsync((void**)&sp.partials, std::max(256, spectral_chunks(sp)) * sizeof(double), s->stream));
   CK(cudaMallocAsync((void**)&sp.state, 4 * sizeof(int), s->stream));
   CK(cudaMemcpyAsync(sp.QR, QR.data(), QR.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
   if (C != R) CK(cudaMemcpyAsync(sp.QC, QC.data(), QC.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));

@@ -8,6 +8,7 @@
 
 #include <algorithm>
 
+#include "epic_grid.cuh"
 #include "epic_internal.cuh"
 #include "epic_xsum.cuh"
 
@@ -36,11 +37,6 @@ __device__ __forceinline__ double raw_den(const FinalizeArgs& a, int s, int i, i
   return v / a.div;
 }
 
-__device__ __forceinline__ double fold_y(const FinalizeArgs& a, int s, int i, int j) {
-  const int ny = a.g.ny;
-  if (j == 0 || j == ny - 1) return raw_den(a, s, i, 0) + raw_den(a, s, i, ny - 1);
-  return raw_den(a, s, i, j);
-}
 
 __global__ void k_finalize(FinalizeArgs a) {
   const int nx = a.g.nx, ny = a.g.ny;
@@ -54,15 +50,8 @@ __global__ void k_finalize(FinalizeArgs a) {
         vals[s] = a.den[s][k];
         continue;
       }
-      if (a.bc == EPIC_PBC) {
-        if (i == 0 || i == nx - 1) v = fold_y(a, s, 0, j) + fold_y(a, s, nx - 1, j);
-        else v = fold_y(a, s, i, j);
-      } else {
-        v = raw_den(a, s, i, j);
-        bool ei = (i == 0 || i == nx - 1), ej = (j == 0 || j == ny - 1);
-        if (ei && ej) v *= 0.25;
-        else if (ei || ej) v *= 0.5;
-      }
+      auto raw = [&](int ii, int jj) { return raw_den(a, s, ii, jj); };
+      v = fold_density(a.bc, nx, ny, raw, i, j);
       vals[s] = v;
     }
     double rho = 0;
@@ -91,22 +80,8 @@ __global__ void k_efield(Geom g, int bc, const double* __restrict__ phi, double*
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const int i = k / ny, j = k - i * ny;
     double ex = efx[k], ey = efy[k];
-#define PHI(a, b) phi[(a) * ny + (b)]
-    if (i >= 1 && i < nx - 1) ex = -(PHI(i + 1, j) - PHI(i - 1, j)) / (2 * g.dx);
-    else if (bc == EPIC_OPEN || bc == EPIC_REFLECTIVE) {
-      if (i == 0) ex = -(PHI(1, j) - PHI(0, j)) / g.dx;
-      else ex = -(PHI(nx - 1, j) - PHI(nx - 2, j)) / g.dx;
-    } else if (bc == EPIC_PBC) {
-      ex = -(PHI(1, j) - PHI(nx - 2, j)) / (2 * g.dx);
-    }
-    if (j >= 1 && j < ny - 1) ey = -(PHI(i, j + 1) - PHI(i, j - 1)) / (2 * g.dy);
-    else if (bc == EPIC_OPEN || bc == EPIC_REFLECTIVE) {
-      if (j == 0) ey = -(PHI(i, 1) - PHI(i, 0)) / g.dy;
-      else ey = -(PHI(i, ny - 1) - PHI(i, ny - 2)) / g.dy;
-    } else if (bc == EPIC_PBC) {
-      ey = -(PHI(i, 1) - PHI(i, ny - 2)) / (2 * g.dy);
-    }
-#undef PHI
+    auto PHI = [&](int a_, int b_) { return phi[a_ * ny + b_]; };
+    efield_node(bc, nx, ny, g.dx, g.dy, PHI, i, j, ex, ey);
     efx[k] = ex;
     efy[k] = ey;
     ef[k] = make_double2(ex, ey);

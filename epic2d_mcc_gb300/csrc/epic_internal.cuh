@@ -179,6 +179,7 @@ struct SpectralSolver {
   int* state;     // [0] done flag, [1] stage, [2] converged
 };
 int spectral_supported(const Geom& g, int solver);
+int spectral_chunks(const SpectralSolver& sp);  // residual chunks (partials needed)
 void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs& a, int stages);
 void launch_particle_sums(cudaStream_t st, int what, const SoA& p, const long long* d_n, double vel_norm,
                           double* partials, double* out3, int grid);

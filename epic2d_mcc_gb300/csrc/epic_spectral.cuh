@@ -1,0 +1,184 @@
+// Device pieces of the mixed-precision Poisson solve shared by the single-run
+// kernels (epic_spectral.cu) and the batched ones (epic_batch.cu), which must
+// give bit-identical potentials; both files are compiled with the same flags.
+//
+// The residual of a lattice is reduced in fixed chunks of SPEC_CHUNK entries
+// (one CTA each, fixed in-CTA order) and the chunk sums are added in chunk
+// order, so the stopping norm depends only on the lattice, not on how the
+// launch is shaped.  The GEMM tiles accumulate every output over k = 0..K-1
+// in order with one fma per step, so the tile shape does not change results
+// either (zero padding adds exact zeros).
+#pragma once
+
+#include "epic_internal.cuh"
+
+namespace epic {
+
+constexpr int SPEC_CHUNK = 1024;  // lattice entries per residual CTA (256 threads x 4)
+
+// One solve's lattice and where its nodes live: node (i, j) of the run's
+// nx x ny grid is at (I_off + i) * NY + j of the node arrays (I_off = 0,
+// NY = ny for a single run).
+struct SpecLattice {
+  int nx, ny, I_off, NY;
+  int R, C, flat, gs_norm;
+  double dx2, K, tol;
+  const double* rho;
+  double* phi;
+  float* t0;          // R * C residual, transform layout
+  double* partials;   // per chunk
+  int* state;         // [0] done, [1] stage
+  SolveInfo* info;    // may be null
+  unsigned long long* iter_total;  // may be null
+};
+
+__device__ __forceinline__ int spec_node(const SpecLattice& L, int i, int j) { return (L.I_off + i) * L.NY + j; }
+
+__device__ __forceinline__ double spec_warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Zero phi on the run's nodes (cold start, as both reference solvers).
+__device__ __forceinline__ void spec_init_node(const SpecLattice& L, int q) {
+  const int i = q / L.ny, j = q - i * L.ny;
+  L.phi[spec_node(L, i, j)] = 0;
+}
+
+// r = b - A x for the entries of one chunk (FP64) into t0 (FP32); the chunk's
+// sum of r^2 goes to partials[chunk].  Called by a whole CTA of 256 threads.
+__device__ __forceinline__ void spec_residual_chunk(const SpecLattice& L, int chunk, double* sm8) {
+  const int total = L.R * L.C;
+  const int nx = L.nx, ny = L.ny, R = L.R, C = L.C;
+  double acc = 0;
+#pragma unroll
+  for (int u = 0; u < SPEC_CHUNK / 256; u++) {
+    const int q = chunk * SPEC_CHUNK + u * 256 + threadIdx.x;
+    if (q < total) {
+      const int ri = q / C, cj = q - ri * C;
+      const double* x = L.phi;
+      int i, j;
+      double ax;
+      if (L.flat) {  // pcgsolver: rows of C = nx nodes of the flattened vector
+        auto nd = [&](int k) { const int ii = k / ny; return spec_node(L, ii, k - ii * ny); };
+        i = q / ny;
+        j = q - i * ny;
+        ax = -4 * x[spec_node(L, i, j)];
+        if (ri > 0) ax += x[nd(q - C)];
+        if (ri < R - 1) ax += x[nd(q + C)];
+        if (cj > 0) ax += x[nd(q - 1)];
+        if (cj < C - 1) ax += x[nd(q + 1)];
+      } else {  // gssolver: interior nodes, physical neighbours
+        i = ri + 1;
+        j = cj + 1;
+        ax = -4 * x[spec_node(L, i, j)];
+        if (i > 0) ax += x[spec_node(L, i - 1, j)];
+        if (i < nx - 1) ax += x[spec_node(L, i + 1, j)];
+        if (j > 0) ax += x[spec_node(L, i, j - 1)];
+        if (j < ny - 1) ax += x[spec_node(L, i, j + 1)];
+      }
+      const bool edge = i == 0 || i == nx - 1 || j == 0 || j == ny - 1;
+      const double b = edge ? 0.0 : -L.rho[spec_node(L, i, j)] * L.dx2 * L.K;
+      const double r = b - ax;
+      L.t0[q] = (float)r;
+      acc += r * r;
+    }
+  }
+  acc = spec_warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sm8[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < 8; w++) t += sm8[w];
+    L.partials[chunk] = t;
+  }
+}
+
+// The reference solver's stopping test on the residual just computed (one
+// thread): pcgsolver |r|_2 < tol, gssolver sqrt(sum R^2/(nx ny)) < tol with
+// R = r/dx^2.  final_pass closes an unconverged solve at the stage cap.
+__device__ __forceinline__ void spec_check(const SpecLattice& L, int final_pass) {
+  if (L.state[0]) return;
+  const int nchunks = (L.R * L.C + SPEC_CHUNK - 1) / SPEC_CHUNK;
+  double s = 0;
+  for (int b = 0; b < nchunks; b++) s += L.partials[b];
+  const double nn = (double)L.nx * L.ny;
+  double norm, err;
+  if (L.gs_norm) {
+    norm = sqrt(s / (L.dx2 * L.dx2) / nn);
+    err = norm;
+  } else {
+    norm = sqrt(s);
+    err = sqrt(s) / nn;
+  }
+  const int done = norm < L.tol;
+  if (L.info) {
+    L.info->iterations = L.state[1];
+    L.info->error = err;
+    L.info->converged = done;
+  }
+  if (done || final_pass) {
+    L.state[0] = 1;
+    if (L.iter_total) atomicAdd(L.iter_total, (unsigned long long)L.state[1]);
+  } else {
+    L.state[1] += 1;
+  }
+}
+
+// One TILE x TILE output tile of C = A B (M x K by K x N, row-major FP32) at
+// tile (tr, tc), 256 threads.  EPI 0: store; 1: store C o D; 2: add to phi
+// (FP64) at the node of lattice entry (r, c).
+template <int EPI, int TILE>
+__device__ __forceinline__ void spec_gemm_tile(int M, int N, int K, const float* __restrict__ A,
+                                               const float* __restrict__ B, float* __restrict__ Cm,
+                                               const float* __restrict__ D, const SpecLattice* L, int tr, int tc,
+                                               float (*As)[33], float (*Bs)[33]) {
+  constexpr int PT = TILE / 16;  // outputs per thread per direction (2 for 32, 1 for 16)
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int row0 = tr * TILE, col0 = tc * TILE;
+  float acc[PT][PT];
+#pragma unroll
+  for (int a = 0; a < PT; a++)
+#pragma unroll
+    for (int b = 0; b < PT; b++) acc[a][b] = 0.f;
+  for (int k0 = 0; k0 < K; k0 += TILE) {
+    for (int e = threadIdx.x; e < TILE * TILE; e += 256) {
+      const int r = e / TILE, c = e % TILE;
+      As[r][c] = (row0 + r < M && k0 + c < K) ? A[(row0 + r) * K + k0 + c] : 0.f;
+      Bs[r][c] = (k0 + r < K && col0 + c < N) ? B[(k0 + r) * N + col0 + c] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 8
+    for (int kk = 0; kk < TILE; kk++) {
+#pragma unroll
+      for (int a = 0; a < PT; a++)
+#pragma unroll
+        for (int b = 0; b < PT; b++) acc[a][b] = fmaf(As[PT * ty + a][kk], Bs[kk][PT * tx + b], acc[a][b]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < PT; a++)
+#pragma unroll
+    for (int b = 0; b < PT; b++) {
+      const int r = row0 + PT * ty + a, c = col0 + PT * tx + b;
+      if (r >= M || c >= N) continue;
+      if (EPI == 0) Cm[r * N + c] = acc[a][b];
+      else if (EPI == 1) Cm[r * N + c] = acc[a][b] * D[r * N + c];
+      else {
+        int i, j;
+        if (L->flat) {
+          const int k = r * N + c;  // N = C: the flattened vector
+          i = k / L->ny;
+          j = k - i * L->ny;
+        } else {
+          i = r + 1;
+          j = c + 1;
+        }
+        L->phi[spec_node(*L, i, j)] += (double)acc[a][b];
+      }
+    }
+}
+
+}  // namespace epic

@@ -1,0 +1,57 @@
+/* epic2d_batch.h — many independent runs advanced together, every phase of a
+ * step one launch for all of them (no counterpart in the reference, which runs
+ * one simulation per process).
+ *
+ * The runs' grids are laid end to end in one node space (run r's node (i, j)
+ * at node_off[r] + i*ny_r + j) and each species of all runs shares one
+ * particle array (a particle's stored cell is its node in that space, so it
+ * carries its run).  The deposit, finalisation, E-field, push, rewind, cell
+ * sort and the spectral mixed-precision solve (one batched GEMM schedule for
+ * all runs' transforms, with a per-run stopping test) each run as one launch
+ * over the whole batch; a step is captured as a CUDA graph.  The arithmetic
+ * per run is the single-run mixed form's, so a run gives the same particles
+ * and potential, bit for bit, in a batch as alone (epic_run with the same
+ * sort_every, loaded by epic_load_particles_device with the same seed).
+ *
+ * An autotuner picks, when the batch is built, the GEMM tile (16 or 32) for
+ * each lattice-size class by timing both on the batch's own transforms; the
+ * choice does not change results.
+ *
+ * Runs must use the mixed form with CIC deposition, periodic or reflective
+ * walls, no collisions, and the same number of species (species k plays the
+ * same role in every run). */
+#ifndef EPIC2D_BATCH_H
+#define EPIC2D_BATCH_H
+
+#include "epic2d_serve.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct epic_batch epic_batch;
+
+/* Builds a batch on the current device from nruns requests (configuration,
+ * species and load_seed of each; steps, collisions and arrival are ignored). */
+epic_status epic_batch_create(const epic_request* runs, int nruns, int sort_every, epic_batch** out);
+void epic_batch_destroy(epic_batch* b);
+/* Loads every run on the device (its load_seed) and computes its initial field
+ * and rewind (src/main.cpp:366-382). */
+epic_status epic_batch_initial_field(epic_batch* b);
+/* Advances every run by `steps` steps (use_graph: replay a captured step). */
+epic_status epic_batch_run(epic_batch* b, int steps, int use_graph);
+/* Run `run`'s particles of `species` as {x, y, vx, vy, vz} records, or a grid
+ * (EPIC_GRID_PHI / EPIC_GRID_RHO) in the run's own nx*ny layout. */
+epic_status epic_batch_get_particles(epic_batch* b, int run, int species, double* out, int64_t capacity,
+                                     int64_t* n);
+epic_status epic_batch_get_grid(epic_batch* b, int run, int which, double* out);
+epic_status epic_batch_num_particles(epic_batch* b, int64_t* total);
+/* The autotuner's choices: GEMM tile per size class (max(R, C) <= 48, <= 96,
+ * <= 160, larger). */
+epic_status epic_batch_tuning(epic_batch* b, int tiles[4]);
+void* epic_batch_stream(epic_batch* b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,58 @@
+"""Batched runs (include/epic2d_batch.h): every run of a batch gives the same
+particles and potential, bit for bit, as the same run alone in the mixed form
+(same configuration, sort period and device-loader seed) — on square and
+non-square grids, periodic and reflective walls, pcgsolver and gssolver, with
+the step replayed from a graph or launched directly."""
+import numpy as np
+import pytest
+
+from tests import decks
+
+pytestmark = pytest.mark.gpu
+
+SPECS = [dict(nx=64, ny=64, ne=60000, ni=60000, solver="cg", tol="1e-10", maxit=100000, bc="pbc", te=1),
+         dict(nx=48, ny=80, ne=50000, ni=40000, solver="cg", tol="1e-10", maxit=100000, bc="reflective", te=3),
+         dict(nx=96, ny=40, ne=70000, ni=70000, solver="gs", tol="1e-8", bc="pbc", te=0.5),
+         dict(nx=33, ny=33, ne=20000, ni=25000, solver="cg", tol="1e-10", maxit=100000, bc="pbc", te=2)]
+
+
+def _requests(A, d, sort_every):
+    out = []
+    for k, sp in enumerate(SPECS):
+        ini = decks.write(decks.deck(**sp), d)
+        out.append((ini, A.make_request(ini, steps=0, seed=50 + k, precision=1, sort_every=sort_every)))
+    return out
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_runs_equal_single_runs(gpu_lib, tmp_path, graph):
+    A = gpu_lib.api
+    sort_every, steps = 4, 10
+    reqs = _requests(A, str(tmp_path), sort_every)
+    b = A.Batch([r for _, r in reqs], sort_every=sort_every)
+    assert all(t in (16, 32) for t in b.tuning())
+    b.initial_field()
+    b.run(steps, graph=graph)
+    for k, (ini, r) in enumerate(reqs):
+        sim = A.Simulation.from_ini(ini, precision=1, sort_every=sort_every)
+        sim.load_particles_device(50 + k)
+        sim.initial_field()
+        sim.run(steps, graph=True)
+        assert np.array_equal(b.grid(k, "phi"), sim.grid("phi")), k
+        assert np.array_equal(b.grid(k, "rho"), sim.grid("rho")), k
+        for s in range(2):
+            assert np.array_equal(b.particles(k, s), sim.particles(s)), (k, s)
+        sim.close()
+    b.close()
+
+
+def test_batch_rejects_unsupported_runs(gpu_lib, tmp_path):
+    A = gpu_lib.api
+    d = str(tmp_path)
+    ok = A.make_request(decks.write(decks.deck(nx=32, ny=32, ne=1000, ni=1000), d), 0, precision=1)
+    fp64 = A.make_request(decks.write(decks.deck(nx=32, ny=32, ne=1000, ni=1000), d), 0)
+    coll = A.make_request(decks.write(decks.deck(nx=32, ny=32, ne=1000, ni=1000, collisions=True), d), 0,
+                          collisions=True, precision=1)
+    for bad in (fp64, coll):
+        with pytest.raises(A.EpicError):
+            A.Batch([ok, bad])
