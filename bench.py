@@ -375,6 +375,9 @@ def run_ours(args, rank, world):
     serving = None
     if not args.no_serve:
         serving = run_serving(E, workloads)
+    batching = None
+    if not args.no_batch:
+        batching = run_batching(E, workloads)
     precision_form = None
     if not args.no_precision_form:
         precision_form = run_precision_form(E, PRECISION_WORKLOAD, PRECISION_STEPS)
@@ -398,7 +401,8 @@ def run_ours(args, rank, world):
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                         "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
-                "mixed_precision": mixed, "serving": serving, "precision_form": precision_form}
+                "mixed_precision": mixed, "serving": serving, "batching": batching,
+                "precision_form": precision_form}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -454,6 +458,73 @@ def run_precision_form(E, name, steps):
     fp.close()
     mx.close()
     return out
+
+
+BATCH_STEPS = 32          # timed steps of the batch (two sort periods)
+BATCH_SAMPLE = 4          # runs timed one at a time for comparison
+
+
+def run_batching(E, workloads):
+    """The batching workload (512 runs, cells {32..256} per axis, 20-200
+    particles per cell, Te 0.5-5 eV) as one batch in the mixed form: every
+    phase one launch for all runs, graph-replayed steps, tuned GEMM tiles.
+    Batches run collisionless runs, so the runs drawn with MCC are left out.
+    Compared with a sample of the same runs advanced one at a time."""
+    import torch
+
+    A = E.api
+    reqs = [q for q in workloads.batching_requests(seed=0) if not q["collisions"]]
+    d = tempfile.mkdtemp(prefix="epic_batch_")
+    rq, paths = [], []
+    for k, q in enumerate(reqs):
+        path = os.path.join(d, "run%03d.ini" % k)
+        with open(path, "w") as f:
+            f.write(q["ini"])
+        paths.append(path)
+        rq.append(A.make_request(path, 0, False, q["seed"], 0.0, precision=1, sort_every=SORT_EVERY))
+    t0 = time.perf_counter()
+    b = A.Batch(rq, sort_every=SORT_EVERY)
+    b.initial_field()
+    setup_s = time.perf_counter() - t0
+    b.run(SORT_EVERY, graph=True)  # warm-up: one sort period
+    n = b.num_particles()
+    st = torch.cuda.ExternalStream(b.stream)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    b.run(BATCH_STEPS, graph=True)
+    e1.record(st)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1)
+    tiles = b.tuning()
+    b.close()
+    rate = n * BATCH_STEPS / (ms / 1e3)
+    # the same runs one at a time (mixed form, graph replay)
+    sample = list(range(0, len(reqs), max(1, len(reqs) // BATCH_SAMPLE)))[:BATCH_SAMPLE]
+    pst, t_ms = 0.0, 0.0
+    for k in sample:
+        sim = A.Simulation.from_ini(paths[k], precision=1, sort_every=SORT_EVERY)
+        sim.load_particles_device(reqs[k]["seed"])
+        sim.initial_field()
+        sim.run(SORT_EVERY, graph=True)
+        s2 = torch.cuda.ExternalStream(sim.stream)
+        a0 = torch.cuda.Event(enable_timing=True)
+        a1 = torch.cuda.Event(enable_timing=True)
+        a0.record(s2)
+        sim.run(BATCH_STEPS, graph=True)
+        a1.record(s2)
+        a1.synchronize()
+        t_ms += a0.elapsed_time(a1)
+        pst += reqs[k]["particles"] * BATCH_STEPS
+        sim.close()
+    single = pst / (t_ms / 1e3)
+    return {"workload": "batching: 512 runs drawn (cells {32,...,256} per axis, 20-200 ppc per species, Te 0.5-5 "
+                        "eV, periodic); the %d collisionless ones as one batch, mixed form" % len(reqs),
+            "runs": len(reqs), "particles": n, "steps": BATCH_STEPS, "ms_per_step": ms / BATCH_STEPS,
+            "particle_steps_per_s": rate, "setup_s": setup_s, "gemm_tiles_by_size_class": tiles,
+            "one_at_a_time_particle_steps_per_s": single,
+            "one_at_a_time_sample": "%d of the runs, each alone (mixed form, graph replay)" % len(sample),
+            "speedup_vs_one_at_a_time": rate / single}
 
 
 SERVE_BUDGET = 150e9      # device bytes the serving loop may admit
@@ -537,6 +608,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision measurement")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batching measurement")
     ap.add_argument("--no-precision-form", action="store_true", help="skip the 1024^2 precision-form measurement")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

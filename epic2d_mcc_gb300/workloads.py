@@ -178,3 +178,27 @@ def serving_requests(seed: int = 0, rate_per_s: float = 50.0, window_s: float = 
         k += 1
         t += float(rng.exponential(1.0 / rate_per_s))
     return out
+
+
+def batching_requests(seed: int = 0, nruns: int = 512, sides=tuple(range(32, 257, 16)), ppc=(20, 200),
+                      te=(0.5, 5.0), p_mcc: float = 0.5):
+    """Runs of the batching workload: per run the cell counts along x and y
+    drawn independently from `sides`, particles per cell from `ppc` (both
+    species), Te from `te` (eV; ions 1836 m_e at 0.026 eV), MCC with
+    probability `p_mcc`, periodic walls, PCG to 1e-10.  Returns a list of dicts
+    {ini, collisions, seed, nx, ny, particles}."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(nruns):
+        nx, ny = (int(rng.choice(sides)) for _ in range(2))
+        p = int(rng.integers(ppc[0], ppc[1] + 1))
+        t = float(rng.uniform(te[0], te[1]))
+        coll = bool(rng.random() < p_mcc)
+        sp = ["electron,%.8E,%d,%.6g,-1,1,0,0,random" % (ME, nx * ny * p, t),
+              "ion,%.8E,%d,0.026,1,0,0,0,random" % (1836 * ME, nx * ny * p)]
+        ini = _TEMPLATE.format(num_ts=1000, dt=0.01, n=nx, solver="cg", tol="1e-10", maxit=100000, solver_extra="",
+                               bc="pbc", coll="true" if coll else "false", gas="1e20", species="\n".join(sp))
+        ini = ini.replace("Ny       = %d" % nx, "Ny       = %d" % ny, 1)
+        out.append({"ini": ini, "collisions": coll, "seed": 2000 + k, "nx": nx, "ny": ny,
+                    "particles": 2 * nx * ny * p})
+    return out
