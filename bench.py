@@ -466,14 +466,14 @@ BATCH_SAMPLE = 4          # runs timed one at a time for comparison
 
 def run_batching(E, workloads):
     """The batching workload (512 runs, cells {32..256} per axis, 20-200
-    particles per cell, Te 0.5-5 eV) as one batch in the mixed form: every
-    phase one launch for all runs, graph-replayed steps, tuned GEMM tiles.
-    Batches run collisionless runs, so the runs drawn with MCC are left out.
-    Compared with a sample of the same runs advanced one at a time."""
+    particles per cell, Te 0.5-5 eV, MCC on half) as one batch in the mixed
+    form: every phase one launch for all runs, graph-replayed steps, tuned GEMM
+    tiles.  Compared with a sample of the same runs advanced one at a time."""
     import torch
 
     A = E.api
-    reqs = [q for q in workloads.batching_requests(seed=0) if not q["collisions"]]
+    reqs = workloads.batching_requests(seed=0)
+    e, ela, exc, ion = workloads.synthetic_table()
     d = tempfile.mkdtemp(prefix="epic_batch_")
     rq, paths = [], []
     for k, q in enumerate(reqs):
@@ -481,9 +481,10 @@ def run_batching(E, workloads):
         with open(path, "w") as f:
             f.write(q["ini"])
         paths.append(path)
-        rq.append(A.make_request(path, 0, False, q["seed"], 0.0, precision=1, sort_every=SORT_EVERY))
+        rq.append(A.make_request(path, 0, q["collisions"], q["seed"], 0.0, precision=1, sort_every=SORT_EVERY))
     t0 = time.perf_counter()
     b = A.Batch(rq, sort_every=SORT_EVERY)
+    b.set_log_cross_sections(ela, exc, ion, e[0], e[-1])
     b.initial_field()
     setup_s = time.perf_counter() - t0
     b.run(SORT_EVERY, graph=True)  # warm-up: one sort period
@@ -503,23 +504,26 @@ def run_batching(E, workloads):
     sample = list(range(0, len(reqs), max(1, len(reqs) // BATCH_SAMPLE)))[:BATCH_SAMPLE]
     pst, t_ms = 0.0, 0.0
     for k in sample:
+        coll = reqs[k]["collisions"]
         sim = A.Simulation.from_ini(paths[k], precision=1, sort_every=SORT_EVERY)
+        if coll:
+            sim.set_log_cross_sections(ela, exc, ion, e[0], e[-1])
         sim.load_particles_device(reqs[k]["seed"])
         sim.initial_field()
-        sim.run(SORT_EVERY, graph=True)
+        sim.run(SORT_EVERY, collisions=coll, graph=True)
         s2 = torch.cuda.ExternalStream(sim.stream)
         a0 = torch.cuda.Event(enable_timing=True)
         a1 = torch.cuda.Event(enable_timing=True)
         a0.record(s2)
-        sim.run(BATCH_STEPS, graph=True)
+        sim.run(BATCH_STEPS, collisions=coll, graph=True)
         a1.record(s2)
         a1.synchronize()
         t_ms += a0.elapsed_time(a1)
         pst += reqs[k]["particles"] * BATCH_STEPS
         sim.close()
     single = pst / (t_ms / 1e3)
-    return {"workload": "batching: 512 runs drawn (cells {32,...,256} per axis, 20-200 ppc per species, Te 0.5-5 "
-                        "eV, periodic); the %d collisionless ones as one batch, mixed form" % len(reqs),
+    return {"workload": "batching: 512 runs (cells {32,...,256} per axis, 20-200 ppc per species, Te 0.5-5 eV, "
+                        "MCC on %d, periodic) as one batch, mixed form" % sum(q["collisions"] for q in reqs),
             "runs": len(reqs), "particles": n, "steps": BATCH_STEPS, "ms_per_step": ms / BATCH_STEPS,
             "particle_steps_per_s": rate, "setup_s": setup_s, "gemm_tiles_by_size_class": tiles,
             "one_at_a_time_particle_steps_per_s": single,

@@ -129,6 +129,7 @@ def lib() -> ctypes.CDLL:
         "epic_batch_num_particles": ([vp, ctypes.POINTER(ctypes.c_int64)], st),
         "epic_batch_tuning": ([vp, vp], st),
         "epic_batch_stream": ([vp], vp),
+        "epic_batch_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
     }
     for name, (args, res) in sigs.items():
         fn = getattr(L, name)
@@ -455,6 +456,10 @@ class Batch:
         self.requests = list(requests)
         _check(lib().epic_batch_create(arr, len(requests), int(sort_every), ctypes.byref(self._h)))
 
+    def set_log_cross_sections(self, ela, exc, ion, e_min, e_max):
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (ela, exc, ion)]
+        _check(lib().epic_batch_set_log_cross_sections(self._h, *[_ptr(a) for a in arrs], len(arrs[0]), e_min, e_max))
+
     def initial_field(self):
         _check(lib().epic_batch_initial_field(self._h))
 
@@ -463,6 +468,8 @@ class Batch:
 
     def particles(self, run: int, sp: int) -> np.ndarray:
         n = self.requests[run].species[sp].numparticle
+        if self.requests[run].collisions:
+            n = 2 * n + 8192  # ionisation adds particles
         out = np.empty((max(n, 1), 5), dtype=np.float64)
         got = ctypes.c_int64()
         _check(lib().epic_batch_get_particles(self._h, run, sp, _ptr(out), len(out), ctypes.byref(got)))

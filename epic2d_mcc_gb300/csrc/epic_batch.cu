@@ -17,6 +17,7 @@
 
 #include "../../include/epic2d_batch.h"
 #include "epic_batch.cuh"
+#include "epic_device.cuh"
 #include "epic_host.h"
 #include "epic_mixed.cuh"
 #include "epic_spectral.cuh"
@@ -68,6 +69,54 @@ __global__ void k_batch_to_aos(BRun r, double* __restrict__ aos, MixedSoA p, lon
     a[2] = p.vx[o];
     a[3] = p.vy[o];
     a[4] = p.vz[o];
+  }
+}
+
+// Particles of one run anywhere in a species' array (after MCC appends a
+// run's particles need not be contiguous): per tile of EXTRACT_TILE slots the
+// count of the run's particles, then an ordered gather at the scanned offsets.
+constexpr int EXTRACT_TILE = 1024;
+
+__global__ void k_batch_count_run(const int* __restrict__ node_run, MixedSoA p, const long long* __restrict__ d_n,
+                                  int run, unsigned int* counts) {
+  __shared__ unsigned int c;
+  const long long n = *d_n;
+  const long long base = (long long)blockIdx.x * EXTRACT_TILE;
+  if (threadIdx.x == 0) c = 0;
+  __syncthreads();
+  unsigned int mine = 0;
+  for (int k = threadIdx.x; k < EXTRACT_TILE; k += blockDim.x) {
+    const long long q = base + k;
+    mine += q < n && node_run[p.cell[q]] == run;
+  }
+  atomicAdd(&c, mine);
+  __syncthreads();
+  if (threadIdx.x == 0) counts[blockIdx.x] = c;
+}
+
+__global__ void __launch_bounds__(256) k_batch_gather_run(BRun r, int run, const int* __restrict__ node_run, MixedSoA p,
+                                                          const long long* __restrict__ d_n,
+                                                          const unsigned int* __restrict__ offsets, double* aos) {
+  __shared__ int sm[40];
+  const long long n = *d_n;
+  const long long base = (long long)blockIdx.x * EXTRACT_TILE;
+  int rank0 = 0;
+  for (int k0 = 0; k0 < EXTRACT_TILE; k0 += 256) {
+    const long long o = base + k0 + threadIdx.x;
+    const int flag = o < n && node_run[p.cell[o]] == run;
+    int total;
+    const int rank = rank0 + block_exclusive_scan(flag, &total, sm);
+    rank0 += total;
+    if (flag) {
+      const int c = (int)(p.cell[o] - r.node_off);
+      const int i = c / r.ny, j = c - i * r.ny;
+      double* a = aos + 5 * ((long long)offsets[blockIdx.x] + rank);
+      a[0] = __dadd_rn(r.x0, __dmul_rn(__dadd_rn((double)i, (double)p.ox[o]), r.dx));
+      a[1] = __dadd_rn(r.y0, __dmul_rn(__dadd_rn((double)j, (double)p.oy[o]), r.dy));
+      a[2] = p.vx[o];
+      a[3] = p.vy[o];
+      a[4] = p.vz[o];
+    }
   }
 }
 
@@ -364,6 +413,12 @@ struct epic_batch {
   int64_t step_index = 0;
   cudaGraphExec_t g_plain = nullptr, g_sort = nullptr;
   std::vector<void*> allocs;
+  // MCC
+  bool any_mcc = false;
+  double gas_density = 0;
+  CrossSections cs;
+  McEvents ev;
+  unsigned long long *d_step = nullptr, *d_ncoll = nullptr;
 
   template <class T>
   epic_status alloc(T** p, size_t count) {
@@ -462,6 +517,9 @@ struct epic_batch {
     deposit_and_solve();
     for (int s = 0; s < nsp; s++)
       k_batch_push<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s);
+    if (any_mcc)
+      launch_batch_mcc(stream, cs, d_runs, d_node_run, arena[0], d_n[0], cap[0], arena[1], d_n[1], cap[1], d_step, ev,
+                       d_ncoll, flags, grid);
   }
 };
 
@@ -600,7 +658,13 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
     if (c.shape != EPIC_CIC) return bfail(EPIC_ERR_INVALID, "run %d: batches deposit with CIC", r);
     if (c.bc != EPIC_PBC && c.bc != EPIC_REFLECTIVE)
       return bfail(EPIC_ERR_INVALID, "run %d: batches take periodic or reflective walls", r);
-    if (reqs[r].collisions) return bfail(EPIC_ERR_INVALID, "run %d: batches run without collisions", r);
+    if (reqs[r].collisions) {
+      if (b->nsp < 2) return bfail(EPIC_ERR_INVALID, "run %d: MCC needs electrons (species 0) and ions (1)", r);
+      if (b->any_mcc && c.gas_density != b->gas_density)
+        return bfail(EPIC_ERR_INVALID, "run %d: the MCC runs of a batch share one gas density", r);
+      b->any_mcc = true;
+      b->gas_density = c.gas_density;
+    }
     const Geom g{c.nx, c.ny, c.x0, c.y0, c.dx, c.dy, 0, 0};
     if (!spectral_supported(g, c.solver)) return bfail(EPIC_ERR_INVALID, "run %d: grid not supported", r);
     if (c.nx > 4095 || c.ny > 4095) return bfail(EPIC_ERR_INVALID, "run %d: grid too large for a batch", r);
@@ -650,6 +714,16 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
     }
     br.qR_off = q_off_of_side[br.R];
     br.qC_off = q_off_of_side[br.C];
+    br.mcc = reqs[r].collisions;
+    br.vn = c.vel_norm;
+    br.dt_phys = c.DT / c.W;
+    if (b->nsp >= 2) {
+      br.ion_mass = reqs[r].species[1].mass;
+      br.ion_temp = reqs[r].species[1].temp;
+      br.F1 = ME / (ME + br.ion_mass);
+      br.F2 = br.ion_mass / (ME + br.ion_mass);
+    }
+    br.seed = c.seed ^ (reqs[r].load_seed * 0x9E3779B97F4A7C15ull);
     br.chunk_off = chunk_off;
     const int nch = (br.R * br.C + SPEC_CHUNK - 1) / SPEC_CHUNK;
     for (int k = 0; k < nch; k++) chunks.push_back(make_int2(r, k));
@@ -667,7 +741,12 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
       b->pn[(size_t)r * b->nsp + s] = reqs[r].species[s].numparticle;
       off += reqs[r].species[s].numparticle;
     }
-    b->cap[s] = std::max<long long>(off, 1);
+    // room for ionisation products: +10 % + 4096 per run (overflow raises
+    // EPIC_ERR_CAPACITY, as in a single run)
+    long long slack = 0;
+    if (b->any_mcc)
+      for (int r = 0; r < nruns; r++) slack += reqs[r].species[s].numparticle / 10 + 4096;
+    b->cap[s] = std::max<long long>(off + slack, 1);
   }
   epic_status st;
   if ((st = b->alloc(&b->d_runs, nruns))) return st;
@@ -699,10 +778,27 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
   for (int s = 0; s < b->nsp; s++) cmax = std::max(cmax, b->cap[s]);
   for (long long v : b->pn) nmax = std::max(nmax, v);
   if (b->sort_every > 0) {
-    BCK(cudaMallocAsync(&b->sort_buf, sort_scratch_bytes(cmax), b->stream));
+    BCK(cudaMallocAsync(&b->sort_buf, sort_scratch_bytes(cmax, 24), b->stream));
     b->allocs.push_back(b->sort_buf);
   }
   if ((st = b->alloc(&b->staging, (size_t)nmax * 5))) return st;
+  std::memset(&b->cs, 0, sizeof(b->cs));
+  std::memset(&b->ev, 0, sizeof(b->ev));
+  if ((st = b->alloc(&b->d_step, 1)) || (st = b->alloc(&b->d_ncoll, 4))) return st;
+  if (b->any_mcc) {
+    const long long ecap = b->cap[0];
+    McEvents& ev = b->ev;
+    ev.cap = (unsigned int)std::min<long long>(std::max<long long>(ecap / 8, 65536), 1LL << 30);
+    const size_t tiles = (size_t)(ecap / MCC_TILE + 2);
+    char* buf = nullptr;
+    if ((st = b->alloc(&buf, (size_t)ev.cap * ion_event_bytes()))) return st;
+    ev.buf = reinterpret_cast<IonEvent*>(buf);
+    if ((st = b->alloc(&ev.cand, (size_t)ecap)) || (st = b->alloc(&ev.cand_count, 1)) ||
+        (st = b->alloc(&ev.count, 1)) || (st = b->alloc(&ev.slot, (size_t)ecap)) ||
+        (st = b->alloc(&ev.tile_cnt, tiles)) || (st = b->alloc(&ev.tile_off, tiles)))
+      return st;
+    BCK(cudaMemsetAsync(ev.slot, 0xff, (size_t)ecap * sizeof(int), b->stream));
+  }
   // Host tables to the device.
   std::vector<int> node_run(b->nodes);
   for (int r = 0; r < nruns; r++)
@@ -769,6 +865,9 @@ void epic_batch_destroy(epic_batch* b) {
   if (b->g_plain) cudaGraphExecDestroy(b->g_plain);
   if (b->g_sort) cudaGraphExecDestroy(b->g_sort);
   for (void* p : b->allocs) cudaFreeAsync(p, b->stream);
+  void* tables[4] = {b->cs.tot, b->cs.ela, b->cs.exc, b->cs.ion};
+  for (void* p : tables)
+    if (p) cudaFreeAsync(p, b->stream);
   for (int w = 0; w < 2; w++)
     if (b->tile_sched[w]) cudaFreeAsync(b->tile_sched[w], b->stream);
   if (b->stream) {
@@ -810,6 +909,8 @@ epic_status epic_batch_initial_field(epic_batch* b) {
 
 epic_status epic_batch_run(epic_batch* b, int steps, int use_graph) {
   if (!b || steps < 0) return bfail(EPIC_ERR_INVALID, "bad argument");
+  if (b->any_mcc && !b->cs.tot)
+    return bfail(EPIC_ERR_INVALID, "cross sections not set (epic_batch_set_log_cross_sections)");
   const bool sorting = b->sort_every > 0;
   if (!use_graph) {
     for (int k = 0; k < steps; k++) {
@@ -847,15 +948,49 @@ epic_status epic_batch_run(epic_batch* b, int steps, int use_graph) {
 epic_status epic_batch_get_particles(epic_batch* b, int run, int s, double* out, int64_t capacity, int64_t* n) {
   if (!b || run < 0 || run >= b->nruns || s < 0 || s >= b->nsp || !out)
     return bfail(EPIC_ERR_INVALID, "bad argument");
-  const long long cnt = b->pn[(size_t)run * b->nsp + s];
-  if (n) *n = cnt;
-  if (cnt > capacity) return bfail(EPIC_ERR_CAPACITY, "%lld particles do not fit %lld records", cnt, (long long)capacity);
-  if (cnt) {
-    k_batch_to_aos<<<b->grid, PART_THREADS, 0, b->stream>>>(b->runs[run], b->staging, b->arena[s],
-                                                             b->poff[(size_t)run * b->nsp + s], cnt);
-    BCK(cudaGetLastError());
-    BCK(cudaMemcpyAsync(out, b->staging, (size_t)cnt * 5 * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  if (!b->any_mcc) {  // counts never change and each run's particles stay contiguous
+    const long long cnt = b->pn[(size_t)run * b->nsp + s];
+    if (n) *n = cnt;
+    if (cnt > capacity)
+      return bfail(EPIC_ERR_CAPACITY, "%lld particles do not fit %lld records", cnt, (long long)capacity);
+    if (cnt) {
+      k_batch_to_aos<<<b->grid, PART_THREADS, 0, b->stream>>>(b->runs[run], b->staging, b->arena[s],
+                                                               b->poff[(size_t)run * b->nsp + s], cnt);
+      BCK(cudaGetLastError());
+      BCK(cudaMemcpyAsync(out, b->staging, (size_t)cnt * 5 * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    }
+    BCK(cudaStreamSynchronize(b->stream));
+    return EPIC_OK;
   }
+  const int tiles = (int)((b->cap[s] + EXTRACT_TILE - 1) / EXTRACT_TILE);
+  unsigned int* d_counts = nullptr;
+  BCK(cudaMallocAsync((void**)&d_counts, (size_t)tiles * sizeof(unsigned int), b->stream));
+  k_batch_count_run<<<tiles, 256, 0, b->stream>>>(b->d_node_run, b->arena[s], b->d_n[s], run, d_counts);
+  std::vector<unsigned int> counts(tiles);
+  BCK(cudaMemcpyAsync(counts.data(), d_counts, (size_t)tiles * sizeof(unsigned int), cudaMemcpyDeviceToHost,
+                      b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  long long total = 0;
+  for (auto& c : counts) {
+    const unsigned int v = c;
+    c = (unsigned int)total;
+    total += v;
+  }
+  if (n) *n = total;
+  if (total > capacity) {
+    cudaFreeAsync(d_counts, b->stream);
+    return bfail(EPIC_ERR_CAPACITY, "%lld particles do not fit %lld records", total, (long long)capacity);
+  }
+  double* d_out = nullptr;
+  BCK(cudaMallocAsync((void**)&d_out, (size_t)std::max<long long>(total, 1) * 5 * sizeof(double), b->stream));
+  BCK(cudaMemcpyAsync(d_counts, counts.data(), (size_t)tiles * sizeof(unsigned int), cudaMemcpyHostToDevice,
+                      b->stream));
+  k_batch_gather_run<<<tiles, 256, 0, b->stream>>>(b->runs[run], run, b->d_node_run, b->arena[s], b->d_n[s], d_counts,
+                                                   d_out);
+  BCK(cudaGetLastError());
+  if (total) BCK(cudaMemcpyAsync(out, d_out, (size_t)total * 5 * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  cudaFreeAsync(d_out, b->stream);
+  cudaFreeAsync(d_counts, b->stream);
   BCK(cudaStreamSynchronize(b->stream));
   return EPIC_OK;
 }
@@ -874,8 +1009,56 @@ epic_status epic_batch_get_grid(epic_batch* b, int run, int which, double* out) 
 epic_status epic_batch_num_particles(epic_batch* b, int64_t* total) {
   if (!b || !total) return bfail(EPIC_ERR_INVALID, "bad argument");
   int64_t t = 0;
-  for (long long v : b->pn) t += v;
+  for (int s = 0; s < b->nsp; s++) {
+    long long v = 0;
+    BCK(cudaMemcpyAsync(&v, b->d_n[s], sizeof(v), cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    t += v;
+  }
   *total = t;
+  return EPIC_OK;
+}
+
+epic_status epic_batch_set_log_cross_sections(epic_batch* b, const double* ela, const double* exc, const double* ion,
+                                              int64_t n, double e_min, double e_max) {
+  if (!b || !ela || !exc || !ion || n < 2 || !(e_min > 0) || !(e_max > e_min))
+    return bfail(EPIC_ERR_INVALID, "bad argument");
+  // The single run's table (epic_set_log_cross_sections) for the batch's gas density.
+  std::vector<double> tot(n);
+  for (int64_t i = 0; i < n; i++) tot[i] = (ela[i] + exc[i] + ion[i]) * b->gas_density;
+  double** dst[4] = {&b->cs.tot, &b->cs.ela, &b->cs.exc, &b->cs.ion};
+  const double* src[4] = {tot.data(), ela, exc, ion};
+  for (int k = 0; k < 4; k++) {
+    if (*dst[k]) cudaFreeAsync(*dst[k], b->stream);
+    *dst[k] = nullptr;
+    BCK(cudaMallocAsync((void**)dst[k], (size_t)n * sizeof(double), b->stream));
+    BCK(cudaMemcpyAsync(*dst[k], src[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+  }
+  CrossSections& cs = b->cs;
+  cs.n = n;
+  cs.kind = 1;
+  cs.e_min = e_min;
+  cs.e_max = e_max;
+  cs.log_emin = log(e_min);
+  cs.inv_dlog = (n - 1) / (log(e_max) - log(e_min));
+  double mx = 0;
+  for (int64_t i = 0; i + 1 < n; i++) {
+    double e1 = exp(log(e_min) + (i + 1) / cs.inv_dlog);
+    mx = std::max(mx, std::max(tot[i], tot[i + 1]) * sqrt(2.0 * e1 * EV / ME));
+  }
+  mx = std::max(mx, tot[n - 1] * sqrt(2.0 * 4 * e_max * EV / ME));
+  cs.nu_max = mx;
+  for (BRun& r : b->runs) {  // the single run's early-out bound (launch_mcc)
+    const double p_null = 1 - exp(-cs.nu_max * r.dt_phys);
+    r.p_cut = fmin(1.0, p_null * (1 + 1e-9) + 1e-300);
+    r.cut53 = (unsigned long long)ceil(r.p_cut * 9007199254740992.0);
+  }
+  BCK(cudaMemcpyAsync(b->d_runs, b->runs.data(), b->runs.size() * sizeof(BRun), cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaStreamSynchronize(b->stream));
+  // captured steps hold the old table
+  if (b->g_plain) cudaGraphExecDestroy(b->g_plain);
+  if (b->g_sort) cudaGraphExecDestroy(b->g_sort);
+  b->g_plain = b->g_sort = nullptr;
   return EPIC_OK;
 }
 

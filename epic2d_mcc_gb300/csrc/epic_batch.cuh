@@ -22,7 +22,21 @@ struct BRun {
   int R, C, flat, gs_norm;
   long long lat_off, qR_off, qC_off;
   int chunk_off;  // first residual chunk slot
+  // MCC (species 0 against the gas, ions into species 1) when mcc != 0: the
+  // single run's parameters (launch_mcc), Philox keyed by this run's seed
+  int mcc;
+  double vn, dt_phys, ion_mass, ion_temp, F1, F2, p_cut;
+  unsigned long long cut53, seed;
 };
+
+struct McEvents;
+struct CrossSections;
+// Electron-neutral MCC of every run with mcc != 0, one launch sequence for the
+// batch (epic_mcc.cu).
+void launch_batch_mcc(cudaStream_t st, const CrossSections& cs, const BRun* runs, const int* node_run,
+                      const MixedSoA& e, long long* d_ne, long long e_cap, const MixedSoA& ion, long long* d_ni,
+                      long long i_cap, unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll,
+                      int* flags, int grid);
 
 struct BatchGrids {
   int nruns, nsp;

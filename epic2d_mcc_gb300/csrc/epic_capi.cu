@@ -396,7 +396,7 @@ epic_status ensure_sort_scratch(epic_sim* s) {
   if (s->sort_buf && s->sort_cap >= cap) return EPIC_OK;
   if (s->sort_buf) dfree(s, s->sort_buf);
   s->sort_buf = nullptr;
-  if (cudaMallocAsync(&s->sort_buf, sort_scratch_bytes(cap), s->stream) != cudaSuccess) {
+  if (cudaMallocAsync(&s->sort_buf, sort_scratch_bytes(cap, s->mixed ? 24 : 40), s->stream) != cudaSuccess) {
     cudaGetLastError();
     return fail(EPIC_ERR_NOMEM, "cell sort scratch (%lld particles)", cap);
   }

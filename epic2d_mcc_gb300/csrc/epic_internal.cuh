@@ -155,9 +155,9 @@ struct SortScratch {
   unsigned* vals[2];
   unsigned* hist;   // digit table [digit][tile], scanned in place
   unsigned* bsum;   // scan totals
-  void* tmp;        // payload copy, 40 bytes per particle slot
+  void* tmp;        // payload copy (24 or 40 bytes per particle slot)
 };
-size_t sort_scratch_bytes(long long cap);
+size_t sort_scratch_bytes(long long cap, int payload);
 SortScratch carve_sort_scratch(void* buf, long long cap);
 // Sorts one species by cell (stable); returns the number of kernels launched.
 int launch_sort(cudaStream_t st, const Geom& g, const ParticleRef& p, const long long* d_n, long long cap,

@@ -6,6 +6,7 @@
 // draw on injected uniforms).
 #include <cuda_runtime.h>
 
+#include "epic_batch.cuh"
 #include "epic_device.cuh"
 #include "epic_internal.cuh"
 
@@ -421,6 +422,109 @@ void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const Partic
   else
     launch_mcc_t(st, mode, cs, Fp64Particles{e.f}, d_ne, e_cap, Fp64Particles{ion.f}, d_ni, i_cap, m, uniforms,
                  ustride, seed, d_step, ev, d_ncoll, flags, grid);
+}
+
+
+// ------------------------------------------------------------ batches ---
+// The select and collide passes for a batch (include/epic2d_batch.h): every
+// electron finds its run from its cell and uses that run's parameters and
+// seed; the scan, ordered append and commit passes above serve the batch's
+// particle arrays unchanged (products carry the primary's cell, so they
+// belong to its run).
+__device__ __forceinline__ MccParams batch_mcc_params(const BRun& r) {
+  MccParams m;
+  m.vn = r.vn;
+  m.dt_phys = r.dt_phys;
+  m.ion_mass = r.ion_mass;
+  m.ion_temp = r.ion_temp;
+  m.F1 = r.F1;
+  m.F2 = r.F2;
+  m.p_cut = r.p_cut;
+  m.cut53 = r.cut53;
+  m.null_collision = 0;
+  return m;
+}
+
+__global__ void __launch_bounds__(PART_THREADS) k_batch_mcc_select(const BRun* __restrict__ runs,
+                                                                   const int* __restrict__ node_run, MixedSoA e,
+                                                                   const long long* __restrict__ d_ne,
+                                                                   const unsigned long long* __restrict__ d_step,
+                                                                   McEvents ev) {
+  const long long ne = *d_ne;
+  const unsigned long long step = *d_step;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const int lane = threadIdx.x & 31;
+  const long long nround = (ne + stride - 1) / stride;
+  for (long long rd = 0; rd < nround; rd++) {
+    const long long q = rd * stride + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    bool cand = false;
+    if (q < ne) {
+      const BRun& r = runs[node_run[e.cell[q]]];
+      if (r.mcc) {
+        Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)r.seed, (uint32_t)(r.seed >> 32), 0,
+                   make_uint4(0, 0, 0, 0)};
+        cand = src.next53() < r.cut53;
+      }
+    }
+    const unsigned int mask = __ballot_sync(0xffffffffu, cand);
+    if (mask) {
+      unsigned int base = 0;
+      if (lane == __ffs(mask) - 1) base = atomicAdd(ev.cand_count, (unsigned int)__popc(mask));
+      base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
+      if (cand) ev.cand[base + __popc(mask & ((1u << lane) - 1))] = (unsigned int)q;
+    }
+  }
+}
+
+__global__ void __launch_bounds__(PART_THREADS) k_batch_mcc_collide(CrossSections cs, const BRun* __restrict__ runs,
+                                                                    const int* __restrict__ node_run,
+                                                                    MixedParticles e,
+                                                                    const unsigned long long* __restrict__ d_step,
+                                                                    McEvents ev, unsigned long long* pending,
+                                                                    int* flags) {
+  __shared__ unsigned long long s_coll;
+  if (threadIdx.x == 0) s_coll = 0;
+  __syncthreads();
+  const unsigned int nc = *ev.cand_count;
+  const unsigned long long step = *d_step;
+  unsigned int ncoll = 0;
+  for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const long long q = ev.cand[c];
+    const BRun& r = runs[node_run[e.p.cell[q]]];
+    const MccParams m = batch_mcc_params(r);
+    IonEvent evt;
+    Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)r.seed, (uint32_t)(r.seed >> 32), 0,
+               make_uint4(0, 0, 0, 0)};
+    const unsigned long long M = src.next53();
+    const int kind = mcc_collide(cs, m, e, q, src, (double)M * (1.0 / 9007199254740992.0), evt);
+    ncoll += kind != 0;
+    if (kind == 3) {
+      unsigned int slot = atomicAdd(ev.count, 1u);
+      if (slot < ev.cap) {
+        ev.buf[slot] = evt;
+        ev.slot[q] = (int)slot;
+        atomicAdd(&ev.tile_cnt[q / MCC_TILE], 1u);
+      } else {
+        set_flag(flags, FLAG_CAPACITY);
+      }
+    }
+  }
+  if (ncoll) atomicAdd(&s_coll, (unsigned long long)ncoll);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_coll) atomicAdd(&pending[1], s_coll);
+}
+
+void launch_batch_mcc(cudaStream_t st, const CrossSections& cs, const BRun* runs, const int* node_run,
+                      const MixedSoA& e, long long* d_ne, long long e_cap, const MixedSoA& ion, long long* d_ni,
+                      long long i_cap, unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll,
+                      int* flags, int grid) {
+  unsigned long long* pending = d_ncoll + 1;
+  k_batch_mcc_select<<<grid, PART_THREADS, 0, st>>>(runs, node_run, e, d_ne, d_step, ev);
+  k_batch_mcc_collide<<<grid, PART_THREADS, 0, st>>>(cs, runs, node_run, MixedParticles{e}, d_step, ev, pending, flags);
+  k_mcc_scan<<<1, 1024, 0, st>>>(d_ne, ev, pending);
+  k_mcc_append<MixedParticles><<<grid, PART_THREADS, 0, st>>>(MixedParticles{e}, d_ne, e_cap, MixedParticles{ion}, d_ni,
+                                                              i_cap, ev, flags);
+  k_mcc_commit<<<1, 1, 0, st>>>(d_ne, e_cap, d_ni, i_cap, pending, d_ncoll, d_step, ev, flags);
 }
 
 }  // namespace epic

@@ -229,7 +229,7 @@ int64_t epic_estimate_bytes(const epic_config* c, const epic_species_desc* sp, i
     nmax = std::max(nmax, n);
   }
   b += nmax * 40;                                           // loader / upload staging
-  if (c->sort_every > 0) b += cmax * 56 + 512 * 4 * (cmax / 4096 + 1);
+  if (c->sort_every > 0) b += cmax * (16 + (mixed ? 24 : 40)) + 512 * 4 * (cmax / 4096 + 1);
   if (collisions && nsp > 0) {
     const int64_t ecap = sp[0].capacity > 0 ? sp[0].capacity : (int64_t)sp[0].numparticle * 3 / 2 + 4096;
     b += ecap * 8 + std::max<int64_t>(ecap / 8, 65536) * 80 + 4 * 1000 * 8 * 8;

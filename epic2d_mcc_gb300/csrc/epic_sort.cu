@@ -300,14 +300,16 @@ int launch_sort(cudaStream_t st, const Geom& g, const ParticleRef& p, const long
 }
 
 // One buffer: keys x2, vals x2 (4 bytes each per slot), the digit table, the
-// scan totals and the payload copy (40 bytes per slot), each 256-byte aligned.
+// scan totals and the payload copy (payload bytes per slot: 24 for the mixed
+// form's records, 40 for the FP64 form's), each 256-byte aligned.
 static size_t al256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-size_t sort_scratch_bytes(long long cap) {
+size_t sort_scratch_bytes(long long cap, int payload) {
   const long long T = sort_tiles(cap);
   const long long E = (long long)RADIX * T;
   const long long nscan = (E + SCAN_BLOCK - 1) / SCAN_BLOCK;
-  return 4 * al256(4 * (size_t)cap) + al256(4 * (size_t)E) + al256(4 * (size_t)nscan) + al256(40 * (size_t)cap);
+  return 4 * al256(4 * (size_t)cap) + al256(4 * (size_t)E) + al256(4 * (size_t)nscan) +
+         al256((size_t)payload * (size_t)cap);
 }
 
 SortScratch carve_sort_scratch(void* buf, long long cap) {

@@ -13,13 +13,20 @@
  * and potential, bit for bit, in a batch as alone (epic_run with the same
  * sort_every, loaded by epic_load_particles_device with the same seed).
  *
+ * Electron-neutral MCC (runs submitted with collisions) is one launch sequence
+ * for all colliding runs: every electron uses its own run's parameters, with
+ * Philox draws keyed by its position in the batch's array and its run's seed,
+ * so a colliding run is statistically, not bitwise, the run alone; runs
+ * without collisions stay bitwise equal to their single runs.
+ *
  * An autotuner picks, when the batch is built, the GEMM tile (16 or 32) for
  * each lattice-size class by timing both on the batch's own transforms; the
  * choice does not change results.
  *
  * Runs must use the mixed form with CIC deposition, periodic or reflective
- * walls, no collisions, and the same number of species (species k plays the
- * same role in every run). */
+ * walls, and the same number of species (species k plays the same role in
+ * every run; MCC needs electrons as species 0 and ions as species 1); the
+ * colliding runs share one gas density. */
 #ifndef EPIC2D_BATCH_H
 #define EPIC2D_BATCH_H
 
@@ -32,7 +39,7 @@ extern "C" {
 typedef struct epic_batch epic_batch;
 
 /* Builds a batch on the current device from nruns requests (configuration,
- * species and load_seed of each; steps, collisions and arrival are ignored). */
+ * species, collisions and load_seed of each; steps and arrival are ignored). */
 epic_status epic_batch_create(const epic_request* runs, int nruns, int sort_every, epic_batch** out);
 void epic_batch_destroy(epic_batch* b);
 /* Loads every run on the device (its load_seed) and computes its initial field
@@ -46,6 +53,10 @@ epic_status epic_batch_get_particles(epic_batch* b, int run, int species, double
                                      int64_t* n);
 epic_status epic_batch_get_grid(epic_batch* b, int run, int which, double* out);
 epic_status epic_batch_num_particles(epic_batch* b, int64_t* total);
+/* Cross sections of the colliding runs (epic_set_log_cross_sections), needed
+ * before the first step of a batch with collisions. */
+epic_status epic_batch_set_log_cross_sections(epic_batch* b, const double* ela, const double* exc, const double* ion,
+                                              int64_t n, double e_min, double e_max);
 /* The autotuner's choices: GEMM tile per size class (max(R, C) <= 48, <= 96,
  * <= 160, larger). */
 epic_status epic_batch_tuning(epic_batch* b, int tiles[4]);

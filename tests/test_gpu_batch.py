@@ -51,8 +51,57 @@ def test_batch_rejects_unsupported_runs(gpu_lib, tmp_path):
     d = str(tmp_path)
     ok = A.make_request(decks.write(decks.deck(nx=32, ny=32, ne=1000, ni=1000), d), 0, precision=1)
     fp64 = A.make_request(decks.write(decks.deck(nx=32, ny=32, ne=1000, ni=1000), d), 0)
-    coll = A.make_request(decks.write(decks.deck(nx=32, ny=32, ne=1000, ni=1000, collisions=True), d), 0,
-                          collisions=True, precision=1)
-    for bad in (fp64, coll):
+    open_ = A.make_request(decks.write(decks.deck(nx=32, ny=32, ne=1000, ni=1000, bc="open"), d), 0, precision=1)
+    for bad in (fp64, open_):
         with pytest.raises(A.EpicError):
             A.Batch([ok, bad])
+
+
+def _table():
+    from epic2d_mcc_gb300 import workloads
+
+    e, ela, exc, ion = workloads.synthetic_table()
+    return ela, exc, ion, e[0], e[-1]
+
+
+def test_batch_with_collisions(gpu_lib, tmp_path):
+    # Colliding runs share the batch's launches: the collisionless runs of the
+    # same batch stay bitwise equal to their single runs, and a colliding run
+    # ionises at the single run's rate (statistically: its draws are keyed by
+    # its place in the batch's array).
+    A = gpu_lib.api
+    d = str(tmp_path)
+    sort_every, steps = 8, 24
+    plain = dict(nx=64, ny=48, ne=50000, ni=50000, solver="cg", tol="1e-10", maxit=100000)
+    hot = dict(nx=64, ny=64, ne=200000, ni=200000, solver="cg", tol="1e-10", maxit=100000, te=30, gas="1e22")
+    ini_p = decks.write(decks.deck(**plain), d)
+    ini_h = decks.write(decks.deck(collisions=True, **hot), d)
+    reqs = [A.make_request(ini_p, 0, seed=7, precision=1, sort_every=sort_every),
+            A.make_request(ini_h, 0, collisions=True, seed=8, precision=1, sort_every=sort_every)]
+    b = A.Batch(reqs, sort_every=sort_every)
+    b.set_log_cross_sections(*_table())
+    b.initial_field()
+    b.run(steps, graph=True)
+    sim = A.Simulation.from_ini(ini_p, precision=1, sort_every=sort_every)
+    sim.load_particles_device(7)
+    sim.initial_field()
+    sim.run(steps, graph=True)
+    for s in range(2):
+        assert np.array_equal(b.particles(0, s), sim.particles(s))
+    sim.close()
+    n0 = 200000
+    grown_batch = len(b.particles(1, 0)) - n0
+    assert len(b.particles(1, 1)) - n0 == grown_batch  # one ion per new electron
+    grown = []
+    for seed in (8, 9, 10):
+        sim = A.Simulation.from_ini(ini_h, precision=1, sort_every=sort_every)
+        sim.set_log_cross_sections(*_table())
+        sim.load_particles_device(seed)
+        sim.initial_field()
+        sim.run(steps, collisions=True, graph=True)
+        grown.append(sim.num_particles(0) - n0)
+        sim.close()
+    mean = float(np.mean(grown))
+    assert mean > 20  # the deck ionises
+    assert abs(grown_batch - mean) <= 6 * np.sqrt(mean) + 6
+    b.close()
