@@ -110,8 +110,8 @@ def build_driver() -> str:
     """The `epic2d` command-line driver (host/main.cpp) over the C++ mirror of
     the reference classes (host/epic2d.hpp), linked to the library."""
     src = os.path.join(HERE, "host", "main.cpp")
-    hdr = os.path.join(HERE, "host", "epic2d.hpp")
-    if os.path.exists(DRIVER) and all(os.path.getmtime(DRIVER) >= os.path.getmtime(p) for p in (src, hdr, LIB)):
+    hdrs = [os.path.join(HERE, "host", h) for h in ("epic2d.hpp", "epic2d_output.hpp")]
+    if os.path.exists(DRIVER) and all(os.path.getmtime(DRIVER) >= os.path.getmtime(p) for p in [src, LIB] + hdrs):
         return DRIVER
     tmp = DRIVER + ".tmp%d" % os.getpid()
     _run(["g++", "-O2", "-std=c++17", "-I", INCLUDE, "-o", tmp, src, LIB, "-Wl,-rpath,$ORIGIN"])

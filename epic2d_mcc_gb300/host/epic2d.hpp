@@ -93,6 +93,9 @@ class Species {
     spwt = desc_.spwt;
     temp = desc_.temp;
     numparticle = desc_.numparticle;
+    fract_den = desc_.fract_den;
+    vsx = desc_.vsx;
+    vsy = desc_.vsy;
   }
   // Species::ScatterSpecies_serial (src/species.cpp:172-226).
   void ScatterSpecies_serial() { check(epic_scatter_species(domain_.handle(), index_)); }
@@ -132,6 +135,7 @@ class Species {
   std::string name;
   double mass, charge, spwt, temp;
   int numparticle;
+  double fract_den, vsx, vsy;
 
  private:
   Domain& domain_;

@@ -2,11 +2,13 @@
 // of the reference's src/main.cpp: reads the same input.ini, loads particles
 // from the same mt19937 stream, runs the initial field and NUM_TS + 1 loop
 // iterations, and prints the diagnostics line of Output::diagnostics
-// (src/output.cpp:318-392) every write_diagnostics steps.  HDF5 output and
-// plotting are not part of it; `--energy FILE` writes the time history that
-// Output::storeKE_to_matrix keeps (ts*DT, KE x/y/z per species, PE) as CSV.
+// (src/output.cpp:318-392) every write_diagnostics steps.  `--output DIR`
+// writes the reference's result.h5 tree as NPY files under DIR/result/ on the
+// reference's cadence (src/main.cpp:268-277, 426-455; epic2d_output.hpp);
+// `--energy FILE` writes the time history that Output::storeKE_to_matrix keeps
+// (ts*DT, KE x/y/z per species, PE) as CSV.  Plotting is not part of it.
 //
-//   epic2d input.ini [--steps N] [--graph] [--energy energy.csv] [--quiet]
+//   epic2d input.ini [--steps N] [--graph] [--output DIR] [--energy energy.csv] [--quiet]
 #include <chrono>
 #include <cmath>
 #include <cstdio>
@@ -19,6 +21,7 @@
 #include <vector>
 
 #include "epic2d.hpp"
+#include "epic2d_output.hpp"
 
 using namespace epic2d;
 
@@ -30,12 +33,13 @@ int main(int argc, char** argv) {
   const std::string ini = argv[1];
   int steps_override = -1;
   bool graph = false, quiet = false;
-  std::string energy_path;
+  std::string energy_path, output_dir;
   for (int k = 2; k < argc; k++) {
     if (!std::strcmp(argv[k], "--steps") && k + 1 < argc) steps_override = std::atoi(argv[++k]);
     else if (!std::strcmp(argv[k], "--graph")) graph = true;
     else if (!std::strcmp(argv[k], "--quiet")) quiet = true;
     else if (!std::strcmp(argv[k], "--energy") && k + 1 < argc) energy_path = argv[++k];
+    else if (!std::strcmp(argv[k], "--output") && k + 1 < argc) output_dir = argv[++k];
   }
   try {
     epic_config cfg;
@@ -63,10 +67,39 @@ int main(int argc, char** argv) {
     const int norm = (cfg.normscheme == 2 || cfg.normscheme == 4) ? 1 : 0;
     std::ofstream energy;
     if (!energy_path.empty()) energy.open(energy_path);
+    std::unique_ptr<Output> output;
+    int write_phase = 0, write_flag = 0;
+    if (!output_dir.empty()) {
+      write_phase = INIParser::getInt(ini, "diagnostics", "write_interval_phase");
+      write_flag = INIParser::getInt(ini, "diagnostics", "write_flag");
+      if (write_interval <= 0 || write_phase <= 0)
+        throw std::runtime_error("write_interval and write_interval_phase must be positive");
+      output.reset(new Output(output_dir, domain, num_ts, write_interval, nsp));
+      // Output::write_metadata / write_species_metadata (src/main.cpp:275-277).
+      output->write_metadata(cfg.nx, num_ts, write_interval, write_phase,
+                             INIParser::getDouble(ini, "time", "DT_coeff"), cfg.density,
+                             INIParser::getInt(ini, "diagnostics", "save_fig"), cfg.normscheme,
+                             INIParser::getInt(ini, "diagnostics", "sub_cycle_interval"), cfg.LDe, cfg.LDi, cfg.wpe,
+                             cfg.wpi, nsp, 0);
+      output->write_species_metadata(species);
+    }
     auto t0 = std::chrono::steady_clock::now();
     for (int ts = 0; ts < num_ts + 1; ts++) {
       if (graph) check(epic_run(domain.handle(), 1, collisions, 1));
       else check(epic_step(domain.handle(), collisions));
+      if (output) {
+        // src/main.cpp:431-455
+        if (ts % write_phase == 0 && ts % write_interval == 0)
+          for (auto& sp : species) output->write_particle_data(ts, *sp);
+        if (ts % write_interval == 0) {
+          output->storeKE_to_matrix(ts, species, *species[norm]);
+          if (write_flag == 1 || write_flag == 2) {
+            output->write_field_data(ts);
+            output->write_den_data(ts, *species[0]);
+            if (nsp > 1) output->write_den_data(ts, *species[1]);
+          }
+        }
+      }
       const bool diag = write_diag > 0 && ts % write_diag == 0;
       const bool store = !energy_path.empty() && write_interval > 0 && ts % write_interval == 0;
       if (!diag && !store) continue;
@@ -105,6 +138,7 @@ int main(int argc, char** argv) {
       std::cout.unsetf(std::ios_base::floatfield);
     }
     auto t1 = std::chrono::steady_clock::now();
+    if (output) output->write_ke();
     double sec = std::chrono::duration<double>(t1 - t0).count();
     int64_t total = 0;
     for (auto& sp : species) total += sp->size();
