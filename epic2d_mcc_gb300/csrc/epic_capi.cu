@@ -584,7 +584,8 @@ void epic_destroy(epic_sim* s) {
   for (int k = 0; k < 8; k++) dfree(s, s->work[k]);
   void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->partials, s->bar,
                   s->d_info, s->d_iter_total, s->tile_ctr, s->d_ncoll, s->d_step, s->sum_partials, s->d_sums, s->d_flags,
-                  s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion};
+                  s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion,
+                  s->cs.bin_cut};
   for (void* p : ptrs)
     if (p) dfree(s, p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -791,6 +792,10 @@ epic_status epic_sort_species(epic_sim* s, int i) {
 
 static epic_status upload_tables(epic_sim* s, const double* tot, const double* ela, const double* exc,
                                  const double* ion, int64_t n) {
+  // A captured step holds the old tables.
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
+  s->graph_exec = s->graph_exec_sort = nullptr;
   double** dst[4] = {&s->cs.tot, &s->cs.ela, &s->cs.exc, &s->cs.ion};
   const double* src[4] = {tot, ela, exc, ion};
   for (int k = 0; k < 4; k++) {
@@ -801,6 +806,17 @@ static epic_status upload_tables(epic_sim* s, const double* tot, const double* e
   }
   s->cs.n = n;
   return EPIC_OK;
+}
+
+// The speed-bin cuts of the MCC early-out for this run's vel_norm and dt.
+static epic_status upload_bin_cuts(epic_sim* s, const double* tot) {
+  std::vector<unsigned long long> cuts(MCC_SPEED_BINS);
+  mcc_bin_cuts(s->cs, tot, s->cfg.vel_norm, s->cfg.DT / s->cfg.W, cuts.data());
+  if (!s->cs.bin_cut)
+    CK(cudaMallocAsync((void**)&s->cs.bin_cut, MCC_SPEED_BINS * sizeof(unsigned long long), s->stream));
+  CK(cudaMemcpyAsync(s->cs.bin_cut, cuts.data(), MCC_SPEED_BINS * sizeof(unsigned long long),
+                     cudaMemcpyHostToDevice, s->stream));
+  return sync(s);  // the host vector goes out of scope
 }
 
 epic_status epic_set_cross_sections(epic_sim* s, const double* tot, const double* ela, const double* exc,
@@ -819,7 +835,7 @@ epic_status epic_set_cross_sections(epic_sim* s, const double* tot, const double
     mx = std::max(mx, tot[i] * v);
   }
   s->cs.nu_max = mx;
-  return EPIC_OK;
+  return upload_bin_cuts(s, tot);
 }
 
 epic_status epic_set_reference_cross_sections(epic_sim* s) {
@@ -849,7 +865,7 @@ epic_status epic_set_log_cross_sections(epic_sim* s, const double* ela, const do
   }
   mx = std::max(mx, tot[n - 1] * sqrt(2.0 * 4 * e_max * EV / ME));
   s->cs.nu_max = mx;
-  return EPIC_OK;
+  return upload_bin_cuts(s, tot.data());
 }
 
 epic_status epic_handle_collisions(epic_sim* s, int e, int ion, const double* uniforms, int ustride,

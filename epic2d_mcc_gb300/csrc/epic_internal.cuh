@@ -90,7 +90,19 @@ struct CrossSections {
   double de, log_emin, inv_dlog, e_min, e_max;
   double *tot, *ela, *exc, *ion;  // tot includes the gas density
   double nu_max;                  // bound of tot(E)*v(E) for null collisions
+  // First-draw cut per speed bin (MCC_SPEED_BINS entries, see mcc_speed_bin),
+  // for the direct MCC of one run's vel_norm and dt; null: the global cut.
+  unsigned long long* bin_cut = nullptr;
 };
+
+// Speed bins of the MCC early-out: bin b of |v|^2 (in vel_norm units) holds
+// the floats whose bits >> 21 equal b, i.e. quarter octaves; bins of +inf and
+// NaN (b >= 1020) always pass.
+constexpr int MCC_SPEED_BINS = 1024;
+// Host: the cut of every bin for the tables of cs (host copy tot of n
+// entries), vel_norm and dt_phys (epic_capi.cu).
+void mcc_bin_cuts(const CrossSections& cs, const double* tot, double vel_norm, double dt_phys,
+                  unsigned long long* out);
 
 // ---- kernel launchers (epic_particles.cu) ----
 void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const SoA& p, const long long* d_n,

@@ -6,6 +6,10 @@
 // draw on injected uniforms).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
 #include "epic_batch.cuh"
 #include "epic_device.cuh"
 #include "epic_internal.cuh"
@@ -64,6 +68,7 @@ __device__ __forceinline__ double sample_vel(D& src, double mass, double temp) {
 struct MccParams {
   double vn, dt_phys, ion_mass, ion_temp, F1, F2, p_cut;
   unsigned long long cut53;  // ceil(p_cut * 2^53): u < p_cut  <=>  M < cut53 for u = M * 2^-53
+  const unsigned long long* bin_cut;  // per speed bin (CrossSections::bin_cut), or null: cut53 for all
   int null_collision;
 };
 
@@ -77,6 +82,11 @@ struct IonEvent {
 // mixed form's cell index + FP32 offsets and FP32 velocities.
 struct Fp64Particles {
   SoA p;
+  // Speed bin of |v|^2 (MCC_SPEED_BINS): the float bits of the FP64 sum.
+  __device__ int speed_bin(long long q) const {
+    const double a = p.vx[q], b = p.vy[q], c = p.vz[q];
+    return (int)((__float_as_uint(__double2float_rn(a * a + b * b + c * c)) & 0x7FFFFFFFu) >> 21);
+  }
   __device__ void load_v(long long q, double& a, double& b, double& c) const { a = p.vx[q]; b = p.vy[q]; c = p.vz[q]; }
   __device__ void store_v(long long q, double a, double b, double c) const { p.vx[q] = a; p.vy[q] = b; p.vz[q] = c; }
   __device__ void load_pos(long long q, double& a, double& b, double& c) const { a = p.x[q]; b = p.y[q]; c = 0; }
@@ -87,6 +97,10 @@ struct Fp64Particles {
 
 struct MixedParticles {
   MixedSoA p;
+  __device__ int speed_bin(long long q) const {
+    const float a = p.vx[q], b = p.vy[q], c = p.vz[q];
+    return (int)((__float_as_uint(a * a + b * b + c * c) & 0x7FFFFFFFu) >> 21);
+  }
   __device__ void load_v(long long q, double& a, double& b, double& c) const { a = p.vx[q]; b = p.vy[q]; c = p.vz[q]; }
   __device__ void store_v(long long q, double a, double b, double c) const {
     p.vx[q] = (float)a; p.vy[q] = (float)b; p.vz[q] = (float)c;
@@ -193,38 +207,54 @@ __device__ int mcc_collide(const CrossSections& cs, const MccParams& m, const P&
 }
 
 // Pass 1a: every electron draws u0 (no ordering, fixed grid); the few below
-// the cut are appended, in any order, to a candidate list.  Compacting them
-// first keeps whole warps on the FP64 collision path instead of one lane in
-// 32 (divergent FP64 work costs full warp throughput).
-template <int MODE>
-__global__ void __launch_bounds__(PART_THREADS) k_mcc_select(MccParams m, const long long* __restrict__ d_ne,
+// the cut of their speed bin are appended, in any order, to a candidate list.
+// Compacting them first keeps whole warps on the FP64 collision path instead
+// of one lane in 32 (divergent FP64 work costs full warp throughput).  A bin's
+// cut bounds the collision probability of every speed in it and its two
+// neighbours from above (mcc_bin_cuts), so an electron it rejects fails the
+// reference's test p_coll > u0 as well.  One atomic per block and round
+// reserves the block's candidates.
+template <int MODE, class P>
+__global__ void __launch_bounds__(PART_THREADS) k_mcc_select(MccParams m, P e, const long long* __restrict__ d_ne,
                                                              const double* __restrict__ uniforms, int ustride,
                                                              uint64_t seed, const unsigned long long* __restrict__ d_step,
                                                              McEvents ev) {
+  __shared__ unsigned int s_cnt[PART_THREADS / 32];
+  __shared__ unsigned int s_base;
   const long long ne = *d_ne;
   const unsigned long long step = *d_step;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const long long nround = (ne + stride - 1) / stride;
   for (long long rd = 0; rd < nround; rd++) {
     const long long q = rd * stride + (long long)blockIdx.x * blockDim.x + threadIdx.x;
     bool cand = false;
     if (q < ne) {
+      const unsigned long long cut = m.bin_cut ? __ldg(&m.bin_cut[e.speed_bin(q)]) : m.cut53;
       if (MODE == EPIC_MCC_INJECTED) {
-        cand = __ldg(&uniforms[q * ustride]) < m.p_cut;
+        cand = __ldg(&uniforms[q * ustride]) * 9007199254740992.0 < (double)cut;
       } else {
         Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)seed, (uint32_t)(seed >> 32), 0,
                    make_uint4(0, 0, 0, 0)};
-        cand = src.next53() < m.cut53;
+        cand = src.next53() < cut;
       }
     }
     const unsigned int mask = __ballot_sync(0xffffffffu, cand);
-    if (mask) {
-      unsigned int base = 0;
-      if (lane == __ffs(mask) - 1) base = atomicAdd(ev.cand_count, (unsigned int)__popc(mask));
-      base = __shfl_sync(0xffffffffu, base, __ffs(mask) - 1);
-      if (cand) ev.cand[base + __popc(mask & ((1u << lane) - 1))] = (unsigned int)q;
+    if (lane == 0) s_cnt[wid] = (unsigned int)__popc(mask);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned int tot = 0;
+#pragma unroll
+      for (int w = 0; w < PART_THREADS / 32; w++) {
+        const unsigned int c = s_cnt[w];
+        s_cnt[w] = tot;
+        tot += c;
+      }
+      s_base = tot ? atomicAdd(ev.cand_count, tot) : 0u;
     }
+    __syncthreads();
+    if (cand) ev.cand[s_base + s_cnt[wid] + __popc(mask & ((1u << lane) - 1))] = (unsigned int)q;
+    __syncthreads();
   }
 }
 
@@ -381,6 +411,53 @@ __global__ void k_mcc_commit(long long* d_ne, long long e_cap, long long* d_ni, 
 
 size_t ion_event_bytes() { return sizeof(IonEvent); }
 
+// Bin b of the early-out holds |v|^2 (vel_norm units) in [lo(b), lo(b+1)),
+// lo(b) = the float with bits b << 21.  Its cut bounds 1 - exp(-nu dt) over
+// [lo(b-1), lo(b+2)) (a rounded |v|^2 may land one bin off): the largest
+// table entry the lookup of sigma_at can reach there (one index of margin
+// each side) times the largest speed, with a relative margin of 1e-9 and an
+// absolute one of 1e-15 (1 - exp(-x) carries an absolute rounding error of
+// about 1e-16).
+static double bin_lo(int b) {
+  const uint32_t u = (uint32_t)b << 21;
+  float f;
+  std::memcpy(&f, &u, sizeof f);
+  return (double)f;
+}
+
+void mcc_bin_cuts(const CrossSections& cs, const double* tot, double vn, double dt_phys, unsigned long long* out) {
+  const double two53 = 9007199254740992.0;
+  const long long n = (long long)cs.n;
+  for (int b = 0; b < MCC_SPEED_BINS; b++) {
+    if (b + 2 >= 1020) {  // reaches +inf / NaN
+      out[b] = (unsigned long long)two53;
+      continue;
+    }
+    const double s_lo = b >= 1 ? bin_lo(b - 1) : 0.0, s_hi = bin_lo(b + 2);
+    const double e_lo = 0.5 * ME * (s_lo * vn * vn) / EV * (1 - 1e-12);
+    const double e_hi = 0.5 * ME * (s_hi * vn * vn) / EV * (1 + 1e-12);
+    double tmax = 0;
+    if (cs.kind == 0) {
+      const double x0 = e_lo / cs.de + 0.5, x1 = e_hi / cs.de + 0.5;
+      long long i0 = x0 >= (double)n ? n - 1 : (long long)floor(x0) - 1;
+      long long i1 = x1 >= (double)n ? n - 1 : (long long)floor(x1) + 1;
+      i0 = std::max(0LL, std::min(i0, n - 1));
+      i1 = std::max(0LL, std::min(i1, n - 1));
+      for (long long i = i0; i <= i1; i++) tmax = std::max(tmax, tot[i]);
+    } else {
+      auto pos = [&](double e) { return (log(fmin(fmax(e, cs.e_min), cs.e_max)) - cs.log_emin) * cs.inv_dlog; };
+      long long i0 = (long long)floor(pos(e_lo)) - 1, i1 = (long long)floor(pos(e_hi)) + 1;
+      i0 = std::max(0LL, std::min(i0, n - 2));
+      i1 = std::max(0LL, std::min(i1, n - 2));
+      for (long long i = i0; i <= i1; i++) tmax = std::max(tmax, std::max(tot[i], tot[i + 1]));
+    }
+    const double v_hi = sqrt(s_hi * vn * vn) * (1 + 1e-12);
+    const double p = 1 - exp(-(tmax * v_hi) * dt_phys);
+    const double pc = fmin(1.0, p * (1 + 1e-9) + 1e-15);
+    out[b] = (unsigned long long)ceil(pc * two53);
+  }
+}
+
 template <class P>
 static void launch_mcc_t(cudaStream_t st, int mode, const CrossSections& cs, const P& e, long long* d_ne,
                          long long e_cap, const P& ion, long long* d_ni, long long i_cap, const MccParams& m,
@@ -388,11 +465,11 @@ static void launch_mcc_t(cudaStream_t st, int mode, const CrossSections& cs, con
                          const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid) {
   unsigned long long* pending = d_ncoll + 1;
   if (mode == EPIC_MCC_INJECTED) {
-    k_mcc_select<EPIC_MCC_INJECTED><<<grid, PART_THREADS, 0, st>>>(m, d_ne, uniforms, ustride, seed, d_step, ev);
+    k_mcc_select<EPIC_MCC_INJECTED, P><<<grid, PART_THREADS, 0, st>>>(m, e, d_ne, uniforms, ustride, seed, d_step, ev);
     k_mcc_collide<EPIC_MCC_INJECTED, P><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
                                                                         pending, flags);
   } else {
-    k_mcc_select<EPIC_MCC_PHILOX><<<grid, PART_THREADS, 0, st>>>(m, d_ne, uniforms, ustride, seed, d_step, ev);
+    k_mcc_select<EPIC_MCC_PHILOX, P><<<grid, PART_THREADS, 0, st>>>(m, e, d_ne, uniforms, ustride, seed, d_step, ev);
     k_mcc_collide<EPIC_MCC_PHILOX, P><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
                                                                       pending, flags);
   }
@@ -416,6 +493,7 @@ void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const Partic
   const double p_null = 1 - exp(-cs.nu_max * dt_phys);
   m.p_cut = m.null_collision ? p_null : fmin(1.0, p_null * (1 + 1e-9) + 1e-300);
   m.cut53 = (unsigned long long)ceil(m.p_cut * 9007199254740992.0);
+  m.bin_cut = m.null_collision ? nullptr : cs.bin_cut;
   if (e.mixed)
     launch_mcc_t(st, mode, cs, MixedParticles{e.m}, d_ne, e_cap, MixedParticles{ion.m}, d_ni, i_cap, m, uniforms,
                  ustride, seed, d_step, ev, d_ncoll, flags, grid);
@@ -441,6 +519,7 @@ __device__ __forceinline__ MccParams batch_mcc_params(const BRun& r) {
   m.F2 = r.F2;
   m.p_cut = r.p_cut;
   m.cut53 = r.cut53;
+  m.bin_cut = nullptr;
   m.null_collision = 0;
   return m;
 }

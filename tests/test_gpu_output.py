@@ -19,8 +19,8 @@ def test_driver_writes_the_result_tree(gpu_lib, tmp_path):
     from epic2d_mcc_gb300 import build as B
 
     drv = B.build_driver()
-    nx = ny = 33
-    ini = decks.write(decks.deck(nx=nx, ny=ny, ne=20000, ni=20000, solver="pcg", num_ts=20,
+    nx = ny = 33  # nodes: Nx + 1
+    ini = decks.write(decks.deck(nx=nx - 1, ny=ny - 1, ne=20000, ni=20000, solver="cg", num_ts=20,
                                  beam=dict(n=2000, t=1, frac=0.1, vx=5, vy=0)), str(tmp_path))
     out = tmp_path / "out"
     energy = tmp_path / "energy.csv"
