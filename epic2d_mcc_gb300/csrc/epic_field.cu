@@ -571,8 +571,16 @@ int solver_max_blocks() {
 // p'/x updates (needed only for the answer) run while the CTA waits at the
 // grid barrier, so 8 are on the critical path.  The iteration's scalars need
 // one division there: beta = gamma * (1/gamma_prev), with the reciprocal
-// formed after the previous broadcast, and eta = delta - beta*gamma/alpha_prev
-// = delta - beta*(beta*eta_prev) since alpha_prev = gamma_prev/eta_prev.
+// formed while waiting, and eta = delta - beta*gamma/alpha_prev =
+// delta - beta^2 eta_prev (alpha_prev = gamma_prev/eta_prev), formed as
+// delta - gamma^2 (eta_prev/gamma_prev^2) with the second factor also formed
+// while waiting; alpha = gamma/eta by div_nr.
+//
+// One grid-wide synchronisation per iteration carries both dot products: the
+// CTAs add their fixed-point partials into counted words of a slot (see
+// PCG_SLOT_WORDS), so the poll that ends the barrier also returns the totals.
+// The first iteration, and any whose terms outgrow the anchors, reduce
+// through block-anchored partials and the counter barrier instead.
 struct PcgTiling {
   int tr, tc;          // tile rows, columns
   int tiles_c;         // tiles per lattice row
@@ -775,6 +783,89 @@ __device__ __forceinline__ double recip_nr(double x) {
   return xs_double(sign | ((uint64_t)er << 52) | (rb & 0xFFFFFFFFFFFFFull));
 }
 
+// ---- fused grid barrier and reduction ----
+// A slot is one 128-byte line of PCG_SLOT_WORDS 64-bit words.  Every CTA adds
+// (payload << 8) + 1 to each word, so a word whose low byte has reached the
+// CTA count is complete and its upper bits hold the payload total: polling a
+// slot is the barrier and returns the reduction in the same load.  Payloads:
+// the 26-bit limb totals of the CTA's fixed-point partials of (w, r) (words
+// 0-4) and (r, r) (words 5-9) against grid-wide anchors, and whether the CTA
+// had a term beyond the anchors' range (word 10).  Slots rotate over three
+// lines: iteration k adds to slot k % 3 while CTA 0 clears slot (k + 1) % 3,
+// last read in iteration k - 2 (every CTA read it before adding to slot
+// k - 1, which CTA 0 has seen complete) and next written in iteration k + 1
+// (after the adders have seen slot k complete, including CTA 0's release).
+constexpr int PCG_SLOT_WORDS = 11;
+constexpr int PCG_SLOT_U64 = 16;
+constexpr int PCG_SLOTS = 3;
+// Byte offset of the slots in the partials buffer (after two parities of
+// XPartial records).
+constexpr size_t PCG_SLOT_OFFSET = 2 * PCG_MAX_BLOCKS * sizeof(XPartial);
+static_assert(PCG_MAX_BLOCKS < 256, "the CTA count must fit the low byte of a slot word");
+static_assert(PCG_SLOT_OFFSET % 128 == 0, "slots are 128-byte lines");
+// Anchors: (r, r) terms of iteration k+1 are converted against the exponent
+// of (r, r) of iteration k plus this headroom, (w, r) terms one higher
+// (|w_i r_i| <= 2 max r_i^2 for the diagonal -4 stencil).  A term more than
+// one binade above its anchor (a residual component that grew past about
+// 2^4 x the previous (r, r)) sends the iteration through the block-anchored
+// reduction instead.  Below the anchor, bits under 2^(A - 1129) are dropped:
+// about 2^-80 of (r, r) for 2^19 terms, far below FP64 rounding.
+constexpr int PCG_ANCHOR_HEADROOM = 3;
+
+__device__ __forceinline__ void red_add_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.relaxed.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ void red_release_add_u64(unsigned long long* p, unsigned long long v) {
+  asm volatile("red.release.gpu.global.add.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Warp totals of the five 26-bit limbs of v (top limb signed), in every lane:
+// v = sum l[k] 2^(26k).  Each limb total of 32 lanes stays below 2^31.
+__device__ __forceinline__ void xs_warp_limbs(xs_int v, int (&l)[5]) {
+  const xs_uint u = (xs_uint)v;
+  const unsigned M = (1u << 26) - 1;
+  l[0] = __reduce_add_sync(0xffffffffu, (int)((unsigned)u & M));
+  l[1] = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 26) & M));
+  l[2] = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 52) & M));
+  l[3] = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 78) & M));
+  l[4] = __reduce_add_sync(0xffffffffu, (int)(v >> 104));
+}
+
+// num / den (den normal, finite) from the FP32 reciprocal y0 of den's
+// significand m: with e = 1 - m y0 (|e| < 2^-22), num/m = num y0 (1 + e + e^2)
+// to a relative 2^-66, formed as fma(q0, fma(e, e, e), q0), q0 = num y0:
+// three dependent FP64 operations after the seed, within about two ulps.
+// The exponent is applied in the integer domain; outside the normal range (or
+// for den not normal) the library division is used.
+__device__ __forceinline__ double div_nr(double num, double den) {
+  const uint64_t b = xs_bits(den);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if (e == 0 || e >= 2046) return num / den;
+  const double m = xs_double((b & 0xFFFFFFFFFFFFFull) | (1023ull << 52));  // |den| scaled to [1, 2)
+  const float yf = __frcp_rn(__int_as_float(0x3F800000 | (int)((b >> 29) & 0x7FFFFF)));
+  const unsigned yb = (unsigned)__float_as_int(yf);
+  const double y0 =
+      xs_double(((uint64_t)(((yb >> 23) & 0xFF) - 127 + 1023) << 52) | ((uint64_t)(yb & 0x7FFFFF) << 29));
+  const double er = fma(-m, y0, 1.0);
+  const double q0 = num * y0;
+  const double q = fma(q0, fma(er, er, er), q0);
+  const uint64_t qb = xs_bits(q);
+  const long eq = (long)((qb >> 52) & 0x7FF);
+  const long en = eq - (e - 1023);
+  if (eq == 0 || eq == 0x7FF || en <= 0 || en >= 2047) return num / den;
+  return xs_double(((qb ^ b) & (1ull << 63)) | ((uint64_t)en << 52) | (qb & 0xFFFFFFFFFFFFFull));
+}
+
 template <int NPT>
 __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) {
   extern __shared__ double sr[];  // r of the tile and its halo ring, (tr + 2) x (tc + 2)
@@ -868,32 +959,139 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
 
   unsigned int cap32 = (unsigned int)n * (unsigned int)n;
   const int maxit = (int)cap32 < a.max_iter ? (int)cap32 : a.max_iter;
+  unsigned long long* const slots =
+      reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(a.partials) + PCG_SLOT_OFFSET);
+  // The counted sums hold up to 2^19 terms (the fixed-point headroom).
+  const bool fused = n < (1 << 19);
+  if (blockIdx.x == 0 && threadIdx.x < PCG_SLOTS * PCG_SLOT_U64) slots[threadIdx.x] = 0ull;
+  __shared__ int s_limb[PCG_T / 32][PCG_SLOT_WORDS];
+  __shared__ int s_aq, s_exact;
   // Thread 0's scalars, in the scaled form: rr = (r, r) = -4 gamma,
   // dr = (w, r) = -4 delta, eta_r = -4 eta; then beta = rr / rr_prev,
-  // eta_r = dr - beta*(beta*eta_r_prev), alpha = rr / eta_r.
-  double rr_cur = 0, rr_inv = 0, eta_prev = 0;
+  // eta_r = dr - beta^2 eta_r_prev = dr - rr^2 g with g = eta_r_prev / rr_prev^2
+  // (formed while waiting), alpha = rr / eta_r.
+  double rr_cur = 0, eta_prev = 0, g = 0, rr_inv = 0;
   double be = 0, alq = 0;  // this iteration's beta and -alpha/4
+  int aq = 0;              // anchor of the (r, r) terms (grid-wide); (w, r) one higher
+  int ep = 0;              // episodes of the block-anchored reduction (partials parity)
   int it = 0;
   for (;;) {
-    XPartial* const Pc = P + (it & 1) * nb;
-    xs_block_partial<NPT>(td, tq, sx, Pc + blockIdx.x);
-    if (threadIdx.x == 0) bar_arrive(a.bar);
-    target += nb;
-    // Deferred update of the previous iteration (no other CTA needs p' or x),
-    // and the reciprocal the next beta needs.
-    if (it > 0) {
+    const int cur = it & 1;
+    double dr = 0, rr = 0;  // valid in thread 0
+    bool exact = it == 0 || !fused;
+    if (!exact) {
+      // Counted sums against the anchors aq (r, r) and aq + 1 (w, r).
+      const int ad = aq + 1;
+      const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+      xs_int v0 = 0, v1 = 0;
+      bool out = false;
+#pragma unroll
+      for (int j = 0; j < NPT; j++) {
+        const int e0 = xs_exponent(td[j]), e1 = xs_exponent(tq[j]);
+        out |= e0 > ad + 1 || e1 > aq + 1;
+        if (e0 <= ad + 1) v0 += xs_from_double(td[j], ad);
+        if (e1 <= aq + 1) v1 += xs_from_double(tq[j], aq);
+      }
+      int l0[5], l1[5];
+      xs_warp_limbs(v0, l0);
+      xs_warp_limbs(v1, l1);
+      const unsigned outw = __ballot_sync(0xffffffffu, out);
+      if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+          s_limb[wid][k] = l0[k];
+          s_limb[wid][5 + k] = l1[k];
+        }
+        s_limb[wid][10] = outw != 0;
+      }
+      __syncthreads();  // also orders this CTA's published edge values before the release below
+      unsigned long long* const slot = slots + (it % PCG_SLOTS) * PCG_SLOT_U64;
+      if (wid == 0) {
+        long long S = 0;
+        if (lane < PCG_SLOT_WORDS) {
+#pragma unroll
+          for (int w = 0; w < PCG_T / 32; w++) S += s_limb[w][lane];
+          if (blockIdx.x == 0) slots[((it + 1) % PCG_SLOTS) * PCG_SLOT_U64 + lane] = 0ull;
+        }
+        __syncwarp();
+        if (lane == 0) red_release_add_u64(slot, ((unsigned long long)S << 8) + 1ull);
+        else if (lane < PCG_SLOT_WORDS) red_add_u64(slot + lane, ((unsigned long long)S << 8) + 1ull);
+      }
+      // Deferred update of the previous iteration (no other CTA needs p' or
+      // x), and the scalars the next step needs from the previous ones.
 #pragma unroll
       for (int j = 0; j < NPT; j++)
         if (kk[j] >= 0) {
           p[j] = fma(be, p[j], r_old[j]);
           x[j] = fma(alq, p[j], x[j]);
         }
-      if (threadIdx.x == 0) rr_inv = recip_nr(rr_cur);
+      if (threadIdx.x == 0) {
+        rr_inv = recip_nr(rr_cur);
+        g = eta_prev * (rr_inv * rr_inv);
+      }
+      if (wid == 0) {
+        unsigned long long wv = 0;
+        int good = 1;
+        if (lane < PCG_SLOT_WORDS) {
+          long long spins = 0;
+          for (;;) {
+            wv = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane);
+            if ((wv & 255ull) == (unsigned long long)nb) break;
+            if (++spins > SPIN_LIMIT) {
+              atomicOr(a.flags, FLAG_TIMEOUT);
+              good = 0;
+              break;
+            }
+          }
+        }
+        good = __all_sync(0xffffffffu, good);
+        const long long S = (long long)(wv - (unsigned long long)nb) >> 8;
+        const long long outc = __shfl_sync(0xffffffffu, S, 10);
+        // Lane 0 recombines (w, r), lane 1 (r, r), and each rounds its total.
+        xs_int V = 0;
+#pragma unroll
+        for (int k = 0; k < 5; k++) {
+          const long long La = __shfl_sync(0xffffffffu, S, k), Lb = __shfl_sync(0xffffffffu, S, 5 + k);
+          V += (xs_int)(lane == 0 ? La : Lb) << (26 * k);
+        }
+        const double d = xs_to_double(V, lane == 0 ? ad : aq);
+        const double d1 = __shfl_sync(0xffffffffu, d, 1);
+        if (lane == 0) {
+          dr = d;
+          rr = d1;
+          s_ok = good;
+          s_exact = outc != 0;
+        }
+      }
+      __syncthreads();
+      if (!s_ok) return;
+      exact = s_exact;
     }
-    if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
-    // Halo inputs published before the barrier, loaded while warp 0 sums the
-    // partials.
-    const int cur = it & 1;
+    if (exact) {
+      // Block-anchored reduction: partials of this episode's parity, then
+      // the grid totals after the counter barrier.
+      XPartial* const Pc = P + (ep & 1) * nb;
+      xs_block_partial<NPT>(td, tq, sx, Pc + blockIdx.x);
+      if (threadIdx.x == 0) bar_arrive(a.bar);
+      target += nb;
+      if (it > 0 && !fused) {
+#pragma unroll
+        for (int j = 0; j < NPT; j++)
+          if (kk[j] >= 0) {
+            p[j] = fma(be, p[j], r_old[j]);
+            x[j] = fma(alq, p[j], x[j]);
+          }
+        if (threadIdx.x == 0) {
+          rr_inv = recip_nr(rr_cur);
+          g = eta_prev * (rr_inv * rr_inv);
+        }
+      }
+      if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
+      if (threadIdx.x < 32) xs_grid_totals_w0(Pc, nb, &dr, &rr);
+      ep++;
+    }
+    // Halo inputs published before the barrier, loaded while thread 0 forms
+    // the scalars.
     const double* const pr_c = cur ? a.work[2] : a.work[1];
     const double* const pw_c = cur ? a.work[4] : a.work[3];
     const double* const ps_c = cur ? a.work[6] : a.work[5];
@@ -905,30 +1103,28 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
         hw[j] = __ldcg(&pw_c[hk[j]]);
         hsv[j] = __ldcg(&ps_c[hk[j]]);
       }
-    if (threadIdx.x < 32) {
-      double dr = 0, rr = 0;
-      xs_grid_totals_w0(Pc, nb, &dr, &rr);
-      if (threadIdx.x == 0) {
-        rr_cur = rr;
-        s_done = xs_bits(rr) < a.tol_bits || it >= maxit;  // sqrt(r.r) < tol
-        double beta, eta_r;
-        if (it == 0) {
-          beta = 0;
-          eta_r = dr;
-        } else {
-          beta = rr * rr_inv;
-          eta_r = fma(-beta, beta * eta_prev, dr);
-        }
-        eta_prev = eta_r;
-        s_alpha = rr * recip_nr(eta_r);
-        s_beta = beta;
+    if (threadIdx.x == 0) {
+      rr_cur = rr;
+      s_done = xs_bits(rr) < a.tol_bits || it >= maxit;  // sqrt(r.r) < tol
+      double beta, eta_r;
+      if (it == 0) {
+        beta = 0;
+        eta_r = dr;
+      } else {
+        beta = rr * rr_inv;
+        eta_r = fma(-(rr * rr), g, dr);
       }
+      eta_prev = eta_r;
+      s_alpha = div_nr(rr, eta_r);
+      s_beta = beta;
+      s_aq = xs_exponent(rr) + PCG_ANCHOR_HEADROOM;
     }
     __syncthreads();
     if (s_done) break;
     const double al = s_alpha;
     be = s_beta;
     alq = -0.25 * al;
+    aq = s_aq;
 #pragma unroll
     for (int j = 0; j < NPT; j++)
       if (kk[j] >= 0) {
@@ -982,7 +1178,7 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       td[j] = e * e;
     }
   }
-  XPartial* const Pe = P + ((it + 1) & 1) * nb;
+  XPartial* const Pe = P + (ep & 1) * nb;
   xs_block_partial<NPT>(td, tq, sx, Pe + blockIdx.x);
   if (threadIdx.x == 0) bar_arrive(a.bar);
   target += nb;
