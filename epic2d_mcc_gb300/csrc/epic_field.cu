@@ -829,6 +829,41 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   return v;
 }
 
+// PTX shifts clamp amounts of 64 or more to 64 (result 0), unlike C's.
+__device__ __forceinline__ uint64_t shl_clamp(uint64_t v, unsigned sft) {
+  uint64_t r;
+  asm("shl.b64 %0, %1, %2;" : "=l"(r) : "l"(v), "r"(sft));
+  return r;
+}
+__device__ __forceinline__ uint64_t shr_clamp(uint64_t v, unsigned sft) {
+  uint64_t r;
+  asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(v), "r"(sft));
+  return r;
+}
+
+// acc += x * 2^(1129 - A) (the fixed-point value of xs_from_double, bits
+// under 2^0 truncated toward zero) for x with biased exponent <= A + 1, branch
+// free; a term above that range adds nothing and returns false.  NONNEG: x is
+// known to be >= 0 (squares), so no conditional negation.
+template <bool NONNEG>
+__device__ __forceinline__ bool xs_add_anchored(xs_uint& acc, double x, int A) {
+  const uint64_t b = xs_bits(x);
+  const int eb = (int)((b >> 52) & 0x7FF);
+  const bool ok = eb <= A + 1;
+  const uint64_t m = ok ? ((b & 0xFFFFFFFFFFFFFull) | ((uint64_t)(eb != 0) << 52)) : 0ull;
+  const int sh = 54 + (eb ? eb : 1) - A;  // <= 55 when ok
+  const unsigned up = (unsigned)max(sh, 0), dn = (unsigned)max(-sh, 0);
+  const uint64_t lo = sh >= 0 ? shl_clamp(m, up) : shr_clamp(m, dn);
+  const uint64_t hi = shr_clamp(m, 64u - up);  // m >> (64 - sh), 0 for sh <= 0
+  xs_uint v = ((xs_uint)hi << 64) | lo;
+  if (!NONNEG) {
+    const xs_uint neg = (xs_uint)(xs_int)(-(int64_t)(b >> 63));  // all ones for a negative x
+    v = (v ^ neg) - neg;
+  }
+  acc += v;
+  return ok;
+}
+
 // Warp totals of the five 26-bit limbs of v (top limb signed), in every lane:
 // v = sum l[k] 2^(26k).  Each limb total of 32 lanes stays below 2^31.
 __device__ __forceinline__ void xs_warp_limbs(xs_int v, int (&l)[5]) {
@@ -968,9 +1003,10 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
   __shared__ int s_aq, s_exact;
   // Thread 0's scalars, in the scaled form: rr = (r, r) = -4 gamma,
   // dr = (w, r) = -4 delta, eta_r = -4 eta; then beta = rr / rr_prev,
-  // eta_r = dr - beta^2 eta_r_prev = dr - rr^2 g with g = eta_r_prev / rr_prev^2
-  // (formed while waiting), alpha = rr / eta_r.
-  double rr_cur = 0, eta_prev = 0, g = 0, rr_inv = 0;
+  // eta_r = dr - beta^2 eta_r_prev = dr - rr^2 g with g = eta_r_prev / rr_prev^2,
+  // alpha = rr / eta_r.  Thread 32 forms 1/rr_prev and g while the CTA waits.
+  __shared__ double s_rr, s_eta, s_rrinv, s_g;
+  if (threadIdx.x == 0) s_rr = s_eta = s_rrinv = s_g = 0.0;
   double be = 0, alq = 0;  // this iteration's beta and -alpha/4
   int aq = 0;              // anchor of the (r, r) terms (grid-wide); (w, r) one higher
   int ep = 0;              // episodes of the block-anchored reduction (partials parity)
@@ -983,18 +1019,17 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       // Counted sums against the anchors aq (r, r) and aq + 1 (w, r).
       const int ad = aq + 1;
       const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-      xs_int v0 = 0, v1 = 0;
-      bool out = false;
+      xs_uint v0 = 0, v1 = 0;
+      bool in = true;
 #pragma unroll
       for (int j = 0; j < NPT; j++) {
-        const int e0 = xs_exponent(td[j]), e1 = xs_exponent(tq[j]);
-        out |= e0 > ad + 1 || e1 > aq + 1;
-        if (e0 <= ad + 1) v0 += xs_from_double(td[j], ad);
-        if (e1 <= aq + 1) v1 += xs_from_double(tq[j], aq);
+        in &= xs_add_anchored<false>(v0, td[j], ad);
+        in &= xs_add_anchored<true>(v1, tq[j], aq);
       }
+      const bool out = !in;
       int l0[5], l1[5];
-      xs_warp_limbs(v0, l0);
-      xs_warp_limbs(v1, l1);
+      xs_warp_limbs((xs_int)v0, l0);
+      xs_warp_limbs((xs_int)v1, l1);
       const unsigned outw = __ballot_sync(0xffffffffu, out);
       if (lane == 0) {
 #pragma unroll
@@ -1025,9 +1060,10 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
           p[j] = fma(be, p[j], r_old[j]);
           x[j] = fma(alq, p[j], x[j]);
         }
-      if (threadIdx.x == 0) {
-        rr_inv = recip_nr(rr_cur);
-        g = eta_prev * (rr_inv * rr_inv);
+      if (threadIdx.x == 32) {
+        const double ri = recip_nr(s_rr);
+        s_rrinv = ri;
+        s_g = s_eta * (ri * ri);
       }
       if (wid == 0) {
         unsigned long long wv = 0;
@@ -1081,9 +1117,10 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
             p[j] = fma(be, p[j], r_old[j]);
             x[j] = fma(alq, p[j], x[j]);
           }
-        if (threadIdx.x == 0) {
-          rr_inv = recip_nr(rr_cur);
-          g = eta_prev * (rr_inv * rr_inv);
+        if (threadIdx.x == 32) {
+          const double ri = recip_nr(s_rr);
+          s_rrinv = ri;
+          s_g = s_eta * (ri * ri);
         }
       }
       if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
@@ -1104,17 +1141,17 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
         hsv[j] = __ldcg(&ps_c[hk[j]]);
       }
     if (threadIdx.x == 0) {
-      rr_cur = rr;
+      s_rr = rr;
       s_done = xs_bits(rr) < a.tol_bits || it >= maxit;  // sqrt(r.r) < tol
       double beta, eta_r;
       if (it == 0) {
         beta = 0;
         eta_r = dr;
       } else {
-        beta = rr * rr_inv;
-        eta_r = fma(-(rr * rr), g, dr);
+        beta = rr * s_rrinv;
+        eta_r = fma(-(rr * rr), s_g, dr);
       }
-      eta_prev = eta_r;
+      s_eta = eta_r;
       s_alpha = div_nr(rr, eta_r);
       s_beta = beta;
       s_aq = xs_exponent(rr) + PCG_ANCHOR_HEADROOM;
