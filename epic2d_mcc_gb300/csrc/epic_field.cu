@@ -1011,6 +1011,10 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
   int aq = 0;              // anchor of the (r, r) terms (grid-wide); (w, r) one higher
   int ep = 0;              // episodes of the block-anchored reduction (partials parity)
   int it = 0;
+  // This thread's fixed-point sums of its (w, r) and (r, r) terms against the
+  // anchors, accumulated as the stencil forms the terms.
+  xs_uint v0 = 0, v1 = 0;
+  bool in = true;
   for (;;) {
     const int cur = it & 1;
     double dr = 0, rr = 0;  // valid in thread 0
@@ -1019,13 +1023,6 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       // Counted sums against the anchors aq (r, r) and aq + 1 (w, r).
       const int ad = aq + 1;
       const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-      xs_uint v0 = 0, v1 = 0;
-      bool in = true;
-#pragma unroll
-      for (int j = 0; j < NPT; j++) {
-        in &= xs_add_anchored<false>(v0, td[j], ad);
-        in &= xs_add_anchored<true>(v1, tq[j], aq);
-      }
       const bool out = !in;
       int l0[5], l1[5];
       xs_warp_limbs((xs_int)v0, l0);
@@ -1041,17 +1038,19 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       }
       __syncthreads();  // also orders this CTA's published edge values before the release below
       unsigned long long* const slot = slots + (it % PCG_SLOTS) * PCG_SLOT_U64;
-      if (wid == 0) {
+      if (wid == 0 && lane >= 1 && lane < PCG_SLOT_WORDS) {
         long long S = 0;
-        if (lane < PCG_SLOT_WORDS) {
 #pragma unroll
-          for (int w = 0; w < PCG_T / 32; w++) S += s_limb[w][lane];
-          if (blockIdx.x == 0) slots[((it + 1) % PCG_SLOTS) * PCG_SLOT_U64 + lane] = 0ull;
-        }
-        __syncwarp();
-        if (lane == 0) red_release_add_u64(slot, ((unsigned long long)S << 8) + 1ull);
-        else if (lane < PCG_SLOT_WORDS) red_add_u64(slot + lane, ((unsigned long long)S << 8) + 1ull);
+        for (int w = 0; w < PCG_T / 32; w++) S += s_limb[w][lane];
+        red_add_u64(slot + lane, ((unsigned long long)S << 8) + 1ull);
+      } else if (threadIdx.x == 64) {
+        long long S = 0;
+#pragma unroll
+        for (int w = 0; w < PCG_T / 32; w++) S += s_limb[w][0];
+        red_release_add_u64(slot, ((unsigned long long)S << 8) + 1ull);
       }
+      unsigned long long wv0 = 0;
+      if (wid == 0 && lane < PCG_SLOT_WORDS) wv0 = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane);
       // Deferred update of the previous iteration (no other CTA needs p' or
       // x), and the scalars the next step needs from the previous ones.
 #pragma unroll
@@ -1070,17 +1069,20 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
         int good = 1;
         if (lane < PCG_SLOT_WORDS) {
           long long spins = 0;
+          wv = wv0;
           for (;;) {
-            wv = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane);
             if ((wv & 255ull) == (unsigned long long)nb) break;
             if (++spins > SPIN_LIMIT) {
               atomicOr(a.flags, FLAG_TIMEOUT);
               good = 0;
               break;
             }
+            wv = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane);
           }
         }
         good = __all_sync(0xffffffffu, good);
+        if (blockIdx.x == 0 && lane < PCG_SLOT_WORDS)
+          slots[((it + PCG_SLOTS - 1) % PCG_SLOTS) * PCG_SLOT_U64 + lane] = 0ull;
         const long long S = (long long)(wv - (unsigned long long)nb) >> 8;
         const long long outc = __shfl_sync(0xffffffffu, S, 10);
         // Lane 0 recombines (w, r), lane 1 (r, r), and each rounds its total.
@@ -1177,6 +1179,8 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
     double* const pr_n = cur ? a.work[1] : a.work[2];
     double* const pw_n = cur ? a.work[3] : a.work[4];
     double* const ps_n = cur ? a.work[5] : a.work[6];
+    v0 = v1 = 0;
+    in = true;
 #pragma unroll
     for (int j = 0; j < NPT; j++)
       if (kk[j] >= 0) {
@@ -1184,6 +1188,10 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
         w[j] = fma(-0.25, (c[-ldu] + c[-1]) + (c[1] + c[ldu]), r[j]);
         td[j] = w[j] * r[j];
         tq[j] = r[j] * r[j];
+        if (fused) {
+          in &= xs_add_anchored<false>(v0, td[j], aq + 1);
+          in &= xs_add_anchored<true>(v1, tq[j], aq);
+        }
         if (pub[j]) {
           pr_n[kk[j]] = r[j];
           pw_n[kk[j]] = w[j];
