@@ -50,6 +50,30 @@ __device__ __forceinline__ bool gather(const Geom& g, const double2* __restrict_
 }
 
 // ------------------------------------------------------------ deposit ---
+// Fixed-point CIC weights on the integer pipe.  For a logical coordinate
+// l in [0, 2^11) held as X = l * 2^52 (the bits of l under 2^-52 dropped:
+// below 2^-52 of the cell, far under the weight quantum), the cell is X >> 52
+// and the offset d = X mod 2^52 with 1 - d = 2^52 - d exactly; a weight
+// (1-di)(1-dj) etc. is the exact 106-bit product rounded once to the quantum
+// 2^-k, where the FP64 form rounds 1-d, the product and the scaled value
+// (so the two can differ by one quantum).  GB300 issues FP64 at 1/32 of the
+// integer rate, and these weights are most of the deposit's arithmetic.
+__device__ __forceinline__ bool fx52(double l, uint64_t& X) {
+  const uint64_t b = (uint64_t)__double_as_longlong(l);
+  const int e = (int)((b >> 52) & 0x7FF);
+  if ((b >> 63) || e >= 1023 + 11) return false;  // negative, or 2^11 and above
+  const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | ((uint64_t)(e != 0) << 52);
+  const int sh = e - 1023;
+  X = sh >= 0 ? (m << sh) : (sh > -64 ? m >> (-sh) : 0ull);
+  return true;
+}
+
+// round(a * b * 2^-s) for a, b <= 2^52 and 43 <= s < 128 (ties up).
+__device__ __forceinline__ unsigned long long fx_weight(uint64_t a, uint64_t b, int s) {
+  const unsigned __int128 p = ((unsigned __int128)__umul64hi(a, b) << 64) | (a * b);
+  return (unsigned long long)((p + ((unsigned __int128)1 << (s - 1))) >> s);
+}
+
 // Species::ScatterSpecies_serial's accumulation (src/species.cpp:174-183) with
 // Domain::Scatter (src/domain.cpp:205-228).  FIXED accumulates each CIC weight
 // rounded to an integer multiple of 2^-k (k chosen from the capacity so no
@@ -64,6 +88,8 @@ __global__ void __launch_bounds__(PART_THREADS) k_deposit(Geom g, SoA p, const l
   const long long n = *d_n;
   const long long stride = (long long)gridDim.x * blockDim.x;
   double* facc = reinterpret_cast<double*>(acc);
+  // fx_scale = 2^k: a weight product of two 52-bit offsets carries 2^104.
+  const int wshift = 104 - ((int)(((uint64_t)__double_as_longlong(fx_scale) >> 52) & 0x7FF) - 1023);
   bool bad = false;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
     double lx = to_logical<UNIT>(p.x[q], g.x0, g.dx);
@@ -78,6 +104,21 @@ __global__ void __launch_bounds__(PART_THREADS) k_deposit(Geom g, SoA p, const l
       if (FIXED) atomicAdd(&acc[k], (unsigned long long)__double2ll_rn(fx_scale));
       else atomicAdd(&facc[k], spwt);
     } else {
+      uint64_t X, Y;
+      if (FIXED && fx52(lx, X) && fx52(ly, Y)) {
+        const int i = (int)(X >> 52), j = (int)(Y >> 52);
+        if (i + 1 >= g.nx || j + 1 >= g.ny) {
+          bad = true;
+          continue;
+        }
+        const uint64_t one = 1ull << 52, di = X & (one - 1), dj = Y & (one - 1);
+        const long k = (long)i * g.ny + j;
+        atomicAdd(&acc[k], fx_weight(one - di, one - dj, wshift));
+        atomicAdd(&acc[k + g.ny], fx_weight(di, one - dj, wshift));
+        atomicAdd(&acc[k + 1], fx_weight(one - di, dj, wshift));
+        atomicAdd(&acc[k + g.ny + 1], fx_weight(di, dj, wshift));
+        continue;
+      }
       int i = (int)lx, j = (int)ly;
       if (i < 0 || i + 1 >= g.nx || j < 0 || j + 1 >= g.ny) {
         bad = true;
