@@ -95,10 +95,13 @@ struct CrossSections {
   unsigned long long* bin_cut = nullptr;
 };
 
-// Speed bins of the MCC early-out: bin b of |v|^2 (in vel_norm units) holds
-// the floats whose bits >> 21 equal b, i.e. quarter octaves; bins of +inf and
-// NaN (b >= 1020) always pass.
+// Speed bins of the MCC early-out, keyed by m = max(|vx|, |vy|, |vz|) (vel_norm
+// units, from the bits alone): bin 0 holds m < 2^-64, bin 1 + 4(e + 64) + q
+// the m in [2^e (1 + q/4), 2^e (1 + (q+1)/4)) for e in [-64, 63], and bin
+// MCC_SPEED_BINS - 1 everything from 2^64 up (infinities and NaN included),
+// which always passes.  |v|^2 lies in [m^2, 3 m^2].
 constexpr int MCC_SPEED_BINS = 1024;
+constexpr int MCC_BIN_EMIN = -64, MCC_BIN_EMAX = 63;
 // Host: the cut of every bin for the tables of cs (host copy tot of n
 // entries), vel_norm and dt_phys (epic_capi.cu).
 void mcc_bin_cuts(const CrossSections& cs, const double* tot, double vel_norm, double dt_phys,

@@ -8,7 +8,6 @@
 
 #include <algorithm>
 #include <cmath>
-#include <cstring>
 
 #include "epic_batch.cuh"
 #include "epic_device.cuh"
@@ -80,12 +79,24 @@ struct IonEvent {
 
 // Particle layouts the MCC runs on: FP64 positions and velocities, or the
 // mixed form's cell index + FP32 offsets and FP32 velocities.
+// Speed bin (MCC_SPEED_BINS) from the unbiased exponent e and the top two
+// fraction bits q of m = max |v_i|.
+__device__ __forceinline__ int speed_bin_of(int e, int q) {
+  if (e < MCC_BIN_EMIN) return 0;
+  if (e > MCC_BIN_EMAX) return MCC_SPEED_BINS - 1;
+  return 1 + 4 * (e - MCC_BIN_EMIN) + q;
+}
+
 struct Fp64Particles {
   SoA p;
-  // Speed bin of |v|^2 (MCC_SPEED_BINS): the float bits of the FP64 sum.
+  // Integer operations on the bits only (FP64 issues slowly on GB300).
   __device__ int speed_bin(long long q) const {
-    const double a = p.vx[q], b = p.vy[q], c = p.vz[q];
-    return (int)((__float_as_uint(__double2float_rn(a * a + b * b + c * c)) & 0x7FFFFFFFu) >> 21);
+    const unsigned long long M = 0x7FFFFFFFFFFFFFFFull;
+    const unsigned long long a = (unsigned long long)__double_as_longlong(p.vx[q]) & M;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(p.vy[q]) & M;
+    const unsigned long long c = (unsigned long long)__double_as_longlong(p.vz[q]) & M;
+    const unsigned long long m = max(a, max(b, c));
+    return speed_bin_of((int)(m >> 52) - 1023, (int)((m >> 50) & 3));
   }
   __device__ void load_v(long long q, double& a, double& b, double& c) const { a = p.vx[q]; b = p.vy[q]; c = p.vz[q]; }
   __device__ void store_v(long long q, double a, double b, double c) const { p.vx[q] = a; p.vy[q] = b; p.vz[q] = c; }
@@ -98,8 +109,11 @@ struct Fp64Particles {
 struct MixedParticles {
   MixedSoA p;
   __device__ int speed_bin(long long q) const {
-    const float a = p.vx[q], b = p.vy[q], c = p.vz[q];
-    return (int)((__float_as_uint(a * a + b * b + c * c) & 0x7FFFFFFFu) >> 21);
+    const unsigned a = __float_as_uint(p.vx[q]) & 0x7FFFFFFFu, b = __float_as_uint(p.vy[q]) & 0x7FFFFFFFu;
+    const unsigned c = __float_as_uint(p.vz[q]) & 0x7FFFFFFFu;
+    const unsigned m = max(a, max(b, c));
+    const int eb = (int)(m >> 23);  // 0: zero or subnormal (below 2^-126), 255: inf / NaN
+    return speed_bin_of(eb == 255 ? 1 << 20 : eb - 127, (int)((m >> 21) & 3));
   }
   __device__ void load_v(long long q, double& a, double& b, double& c) const { a = p.vx[q]; b = p.vy[q]; c = p.vz[q]; }
   __device__ void store_v(long long q, double a, double b, double c) const {
@@ -147,19 +161,37 @@ __device__ int mcc_collide(const CrossSections& cs, const MccParams& m, const P&
   double gx = vx, gy = vy, gz = vz;
   double g = sqrt(gx * gx + gy * gy + gz * gz);
   double wx = m.F1 * vx, wy = m.F1 * vy, wz = m.F1 * vz;
-  double theta, phi, chi, eta;
-  if (gx == 0) theta = 0.5 * PI_REF;
-  else theta = atan2(sqrt(gy * gy + gz * gz), gx);
-  if (gy == 0) phi = gz > 0 ? 0.5 * PI_REF : -0.5 * PI_REF;
-  else phi = atan2(gz, gy);
-  double st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+  // Euler angles theta = atan2(|(gy, gz)|, gx), phi = atan2(gz, gy) enter only
+  // through their sines and cosines, which are the direction cosines
+  // themselves (equal to the reference's sin/cos of the rounded angles to a
+  // few ulps, and far shorter dependent FP64 chains); the reference's special
+  // angles (PI_REF halves, gx or gy zero) are kept as written.
+  double st, ct, sp, cp;
+  if (gx == 0 || gy == 0) {
+    double theta, phi;
+    if (gx == 0) theta = 0.5 * PI_REF;
+    else theta = atan2(sqrt(gy * gy + gz * gz), gx);
+    if (gy == 0) phi = gz > 0 ? 0.5 * PI_REF : -0.5 * PI_REF;
+    else phi = atan2(gz, gy);
+    st = sin(theta), ct = cos(theta), sp = sin(phi), cp = cos(phi);
+  } else {
+    const double rho = sqrt(gy * gy + gz * gz);
+    st = rho / g;
+    ct = gx / g;
+    sp = gz / rho;
+    cp = gy / rho;
+  }
+  // chi enters through cos(chi) and sin(chi): for chi = acos(c) they are c and
+  // sqrt((1 - c)(1 + c)).
+  double cchi, schi, eta;
   double t0 = s.ela;
   double t1 = t0 + s.exc;
   double t2 = t1 + s.ion;
   int kind;
   if (src.next() < (t0 / t2)) {
     kind = 1;
-    chi = acos(1.0 - 2.0 * src.next());
+    cchi = 1.0 - 2.0 * src.next();
+    schi = sqrt((1.0 - cchi) * (1.0 + cchi));
     eta = 2 * PI_REF * src.next();
   } else if (src.next() < (t1 / t2)) {
     kind = 2;
@@ -167,7 +199,8 @@ __device__ int mcc_collide(const CrossSections& cs, const MccParams& m, const P&
     en = fabs(en - E_EXC_TH * EV);
     g = sqrt(2.0 * en / ME);
     g = g / m.vn;
-    chi = acos(1.0 - 2.0 * src.next());
+    cchi = 1.0 - 2.0 * src.next();
+    schi = sqrt((1.0 - cchi) * (1.0 + cchi));
     eta = 2 * PI_REF * src.next();
   } else {
     kind = 3;
@@ -179,11 +212,13 @@ __device__ int mcc_collide(const CrossSections& cs, const MccParams& m, const P&
     double g2 = sqrt(2.0 * e_ej / ME);
     g = g / m.vn;
     g2 = g2 / m.vn;
-    chi = acos(sqrt(e_sc / en));
-    double chi2 = acos(sqrt(e_ej / en));
+    // chi = acos(sqrt(e_sc/en)), chi2 = acos(sqrt(e_ej/en)) with e_sc + e_ej = en
+    // (e_ej <= en/2): sin(chi) = cos(chi2) = sqrt(e_ej/en) and the reverse.
+    cchi = sqrt(e_sc / en);
+    schi = sqrt(e_ej / en);
     eta = 2 * PI_REF * src.next();
     double eta2 = eta + PI_REF;
-    double sc = sin(chi2), cc = cos(chi2), se = sin(eta2), ce = cos(eta2);
+    double sc = cchi, cc = schi, se = sin(eta2), ce = cos(eta2);
     double hx = g2 * (ct * cc - st * sc * ce);
     double hy = g2 * (st * cp * cc + ct * cp * sc * ce - sp * sc * se);
     double hz = g2 * (st * sp * cc + ct * sp * sc * ce + cp * sc * se);
@@ -198,7 +233,7 @@ __device__ int mcc_collide(const CrossSections& cs, const MccParams& m, const P&
     pi[0] = sample_vel(src, m.ion_mass, m.ion_temp);
     e.load_pos(q, evt.x, evt.y, evt.z);
   }
-  double sc = sin(chi), cc = cos(chi), se = sin(eta), ce = cos(eta);
+  double sc = schi, cc = cchi, se = sin(eta), ce = cos(eta);
   gx = g * (ct * cc - st * sc * ce);
   gy = g * (st * cp * cc + ct * cp * sc * ce - sp * sc * se);
   gz = g * (st * sp * cc + ct * sp * sc * ce + cp * sc * se);
@@ -411,29 +446,25 @@ __global__ void k_mcc_commit(long long* d_ne, long long e_cap, long long* d_ni, 
 
 size_t ion_event_bytes() { return sizeof(IonEvent); }
 
-// Bin b of the early-out holds |v|^2 (vel_norm units) in [lo(b), lo(b+1)),
-// lo(b) = the float with bits b << 21.  Its cut bounds 1 - exp(-nu dt) over
-// [lo(b-1), lo(b+2)) (a rounded |v|^2 may land one bin off): the largest
-// table entry the lookup of sigma_at can reach there (one index of margin
-// each side) times the largest speed, with a relative margin of 1e-9 and an
-// absolute one of 1e-15 (1 - exp(-x) carries an absolute rounding error of
-// about 1e-16).
-static double bin_lo(int b) {
-  const uint32_t u = (uint32_t)b << 21;
-  float f;
-  std::memcpy(&f, &u, sizeof f);
-  return (double)f;
-}
-
+// Bin b of the early-out holds the m = max |v_i| of speed_bin_of, so |v|^2
+// (vel_norm units) lies in [m_lo^2, 3 m_hi^2] up to the rounding of the
+// collision test's own sum (relative 1e-12 of margin).  Its cut bounds
+// 1 - exp(-nu dt) there: the largest table entry the lookup of sigma_at can
+// reach (one index of margin each side) times the largest speed, with a
+// relative margin of 1e-9 and an absolute one of 1e-15 (1 - exp(-x) carries an
+// absolute rounding error of about 1e-16).
 void mcc_bin_cuts(const CrossSections& cs, const double* tot, double vn, double dt_phys, unsigned long long* out) {
   const double two53 = 9007199254740992.0;
   const long long n = (long long)cs.n;
   for (int b = 0; b < MCC_SPEED_BINS; b++) {
-    if (b + 2 >= 1020) {  // reaches +inf / NaN
+    const int e = MCC_BIN_EMIN + (b - 1) / 4, q = (b - 1) % 4;
+    if (b == MCC_SPEED_BINS - 1 || (b > 0 && e > MCC_BIN_EMAX)) {
       out[b] = (unsigned long long)two53;
       continue;
     }
-    const double s_lo = b >= 1 ? bin_lo(b - 1) : 0.0, s_hi = bin_lo(b + 2);
+    const double m_lo = b == 0 ? 0.0 : std::ldexp(1.0 + q / 4.0, e);
+    const double m_hi = b == 0 ? std::ldexp(1.0, MCC_BIN_EMIN) : std::ldexp(1.0 + (q + 1) / 4.0, e);
+    const double s_lo = m_lo * m_lo * (1 - 1e-12), s_hi = 3 * m_hi * m_hi * (1 + 1e-12);
     const double e_lo = 0.5 * ME * (s_lo * vn * vn) / EV * (1 - 1e-12);
     const double e_hi = 0.5 * ME * (s_hi * vn * vn) / EV * (1 + 1e-12);
     double tmax = 0;
