@@ -98,6 +98,8 @@ def lib() -> ctypes.CDLL:
         "epic_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
         "epic_handle_collisions": ([vp, i, i, vp, i, ctypes.POINTER(ctypes.c_int64)], st),
         "epic_step": ([vp, i], st),
+        "epic_step_host": ([vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
+                           st),
         "epic_initial_field": ([vp], st),
         "epic_run": ([vp, i, i, i], st),
         "epic_compute_ke": ([vp, i, i, vp], st),
@@ -286,6 +288,20 @@ class Simulation:
 
     def step(self, collisions: bool = False):
         _check(lib().epic_step(self._h, int(collisions)))
+
+    def step_host(self, bufs, counts, collisions: bool = False):
+        """One step of particles held in host arrays (epic_step_host): bufs[s] is a (capacity, 5)
+        float64 array whose first counts[s] rows are species s; returns the new counts.  Pinned
+        arrays (e.g. torch pin_memory) take the direct path."""
+        nsp = len(self.species)
+        for b in bufs:
+            if b.dtype != np.float64 or not b.flags["C_CONTIGUOUS"] or b.ndim != 2 or b.shape[1] != 5:
+                raise ValueError("each buffer must be a C-contiguous (capacity, 5) float64 array")
+        ptrs = (ctypes.c_void_p * nsp)(*[b.ctypes.data for b in bufs])
+        n = (ctypes.c_int64 * nsp)(*[int(c) for c in counts])
+        cap = (ctypes.c_int64 * nsp)(*[len(b) for b in bufs])
+        _check(lib().epic_step_host(self._h, int(collisions), ptrs, n, cap))
+        return [int(v) for v in n]
 
     def initial_field(self):
         _check(lib().epic_initial_field(self._h))

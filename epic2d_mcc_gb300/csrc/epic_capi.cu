@@ -905,6 +905,87 @@ epic_status epic_step(epic_sim* s, int with_collisions) {
   return sync(s);
 }
 
+// One loop iteration for particles the caller holds in host memory.  Direct
+// path (FP64 form, fixed-point deposit, periodic or reflective walls, no cell
+// sort due, every buffer pinned): the upload kernels read the records over the
+// host link and deposit on the way, the push writes the new records back as it
+// goes, and the electrons (and the ions appended by ionisation) go back after
+// the MCC; otherwise the same work runs through the staging buffer.
+epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* parts, int64_t* n,
+                           const int64_t* capacity) {
+  if (!s || !parts || !n || !capacity) return fail(EPIC_ERR_INVALID, "bad argument");
+  const int nsp = (int)s->sp.size();
+  for (int k = 0; k < nsp; k++) {
+    if (n[k] < 0 || n[k] > capacity[k] || (n[k] > 0 && !parts[k]))
+      return fail(EPIC_ERR_INVALID, "bad particle buffer for species %d", k);
+    if (n[k] > s->sp[k].cap)
+      return fail(EPIC_ERR_CAPACITY, "%lld particles exceed the capacity %lld of %s", (long long)n[k], s->sp[k].cap,
+                  s->sp[k].name.c_str());
+  }
+  const epic_config& c = s->cfg;
+  bool direct = !s->mixed && c.bc != EPIC_OPEN && c.deposit_mode == EPIC_DEPOSIT_FIXED &&
+                !(c.sort_every > 0 && s->step_index % c.sort_every == 0);
+  for (int k = 0; k < nsp && direct; k++) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, parts[k]) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+      cudaGetLastError();
+      direct = false;
+    }
+  }
+  epic_status st;
+  if (!direct) {
+    for (int k = 0; k < nsp; k++)
+      if ((st = epic_set_particles(s, k, parts[k], n[k]))) return st;
+    if ((st = epic_step(s, with_collisions))) return st;
+    for (int k = 0; k < nsp; k++) {
+      int64_t got = 0;
+      if ((st = epic_get_particles(s, k, parts[k], capacity[k], &got))) return st;
+      n[k] = got;
+    }
+    return EPIC_OK;
+  }
+  s->step_index++;
+  for (int k = 0; k < nsp; k++) {
+    epic_species_state& sp = s->sp[k];
+    CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
+    launch_upload_deposit(s->stream, s->g, c.shape, parts[k], n[k], sp.soa, sp.d_n, sp.acc, sp.fx_scale, s->d_flags,
+                          s->part_grid);
+    s->launches += 1;
+  }
+  CKL();
+  if ((st = do_finalize(s, FINALIZE_AND_RHO, -1))) return st;
+  if ((st = do_solve(s))) return st;
+  if ((st = do_efield(s))) return st;
+  const bool coll = with_collisions && nsp >= 2;
+  const double K = (c.density * QE * c.L) / (EPS_0 * c.W * c.vel_norm);
+  const double cc = (c.vel_norm) / (c.L * c.W);
+  for (int k = 0; k < nsp; k++) {
+    if (c.ionfixed == 1 && s->sp[k].name == "ion") continue;
+    if (coll && k == 0) {
+      if ((st = do_push(s, 0, 1))) return st;  // the MCC changes the electrons afterwards
+      continue;
+    }
+    epic_species_state& sp = s->sp[k];
+    launch_push_download(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, (sp.desc.charge / sp.desc.mass) * K,
+                         cc, c.DT, parts[k], s->d_flags, s->part_grid);
+    s->launches += 1;
+  }
+  CKL();
+  if (coll) {
+    if ((st = do_mcc(s, 0, 1, nullptr, 0))) return st;
+    launch_download(s->stream, s->sp[0].soa, s->sp[0].d_n, 0, capacity[0], parts[0], s->d_flags, s->part_grid);
+    launch_download(s->stream, s->sp[1].soa, s->sp[1].d_n, n[1], capacity[1], parts[1], s->d_flags, s->part_grid);
+    s->launches += 2;
+    CKL();
+  }
+  std::vector<long long> cnt(nsp);
+  for (int k = 0; k < nsp; k++)
+    CK(cudaMemcpyAsync(&cnt[k], s->sp[k].d_n, sizeof(long long), cudaMemcpyDeviceToHost, s->stream));
+  if ((st = sync(s))) return st;
+  for (int k = 0; k < nsp; k++) n[k] = cnt[k];
+  return EPIC_OK;
+}
+
 static epic_status do_initial_field(epic_sim* s) {
   epic_status st;
   for (int i = 0; i < (int)s->sp.size(); i++)

@@ -110,6 +110,15 @@ void mcc_bin_cuts(const CrossSections& cs, const double* tot, double vel_norm, d
 // ---- kernel launchers (epic_particles.cu) ----
 void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const SoA& p, const long long* d_n,
                     double spwt, double* den, unsigned long long* acc, double fx_scale, int* flags, int grid);
+// Host-resident particles (epic_step_host; FP64 form, fixed-point deposit,
+// periodic or reflective walls): `host` is mapped pinned memory of
+// {x, y, vx, vy, vz} records.
+void launch_upload_deposit(cudaStream_t st, const Geom& g, int shape, const double* host, long long n, const SoA& p,
+                           long long* d_n, unsigned long long* acc, double fx_scale, int* flags, int grid);
+void launch_push_download(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, const long long* d_n,
+                          const double2* ef, double qmK, double c, double dtsub, double* host, int* flags, int grid);
+void launch_download(cudaStream_t st, const SoA& p, const long long* d_n, long long from, long long cap, double* host,
+                     int* flags, int grid);
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
                  const double2* ef, double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
                  unsigned int* tile_ctr, int grid);

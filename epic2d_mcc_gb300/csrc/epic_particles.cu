@@ -80,6 +80,56 @@ __device__ __forceinline__ unsigned long long fx_weight(uint64_t a, uint64_t b, 
 // node can overflow): integer addition is associative, so the grid is
 // identical run to run; the weight is applied at finalisation.  Otherwise
 // FP64 atomics add spwt*w into the same accumulator buffer read as doubles.
+// One particle's deposit; false when its stencil leaves the grid.
+template <int SHAPE, bool FIXED, bool UNIT>
+__device__ __forceinline__ bool deposit_one(const Geom& g, double x, double y, double spwt,
+                                            unsigned long long* __restrict__ acc, double fx_scale, int wshift) {
+  double* facc = reinterpret_cast<double*>(acc);
+  double lx = to_logical<UNIT>(x, g.x0, g.dx);
+  double ly = to_logical<UNIT>(y, g.y0, g.dy);
+  if (SHAPE == EPIC_NGP) {
+    int gx = (int)round(lx), gy = (int)round(ly);
+    if (gx < 0 || gx >= g.nx || gy < 0 || gy >= g.ny) return false;
+    long k = (long)gx * g.ny + gy;
+    if (FIXED) atomicAdd(&acc[k], (unsigned long long)__double2ll_rn(fx_scale));
+    else atomicAdd(&facc[k], spwt);
+    return true;
+  }
+  uint64_t X, Y;
+  if (FIXED && fx52(lx, X) && fx52(ly, Y)) {
+    const int i = (int)(X >> 52), j = (int)(Y >> 52);
+    if (i + 1 >= g.nx || j + 1 >= g.ny) return false;
+    const uint64_t one = 1ull << 52, di = X & (one - 1), dj = Y & (one - 1);
+    const long k = (long)i * g.ny + j;
+    atomicAdd(&acc[k], fx_weight(one - di, one - dj, wshift));
+    atomicAdd(&acc[k + g.ny], fx_weight(di, one - dj, wshift));
+    atomicAdd(&acc[k + 1], fx_weight(one - di, dj, wshift));
+    atomicAdd(&acc[k + g.ny + 1], fx_weight(di, dj, wshift));
+    return true;
+  }
+  int i = (int)lx, j = (int)ly;
+  if (i < 0 || i + 1 >= g.nx || j < 0 || j + 1 >= g.ny) return false;
+  double di = lx - i, dj = ly - j;
+  long k = (long)i * g.ny + j;
+  if (FIXED) {
+    atomicAdd(&acc[k], (unsigned long long)__double2ll_rn((1 - di) * (1 - dj) * fx_scale));
+    atomicAdd(&acc[k + g.ny], (unsigned long long)__double2ll_rn((di) * (1 - dj) * fx_scale));
+    atomicAdd(&acc[k + 1], (unsigned long long)__double2ll_rn((1 - di) * (dj) * fx_scale));
+    atomicAdd(&acc[k + g.ny + 1], (unsigned long long)__double2ll_rn((di) * (dj) * fx_scale));
+  } else {
+    atomicAdd(&facc[k], spwt * (1 - di) * (1 - dj));
+    atomicAdd(&facc[k + g.ny], spwt * (di) * (1 - dj));
+    atomicAdd(&facc[k + 1], spwt * (1 - di) * (dj));
+    atomicAdd(&facc[k + g.ny + 1], spwt * (di) * (dj));
+  }
+  return true;
+}
+
+// fx_scale = 2^k: a weight product of two 52-bit offsets carries 2^104.
+__device__ __forceinline__ int weight_shift(double fx_scale) {
+  return 104 - ((int)(((uint64_t)__double_as_longlong(fx_scale) >> 52) & 0x7FF) - 1023);
+}
+
 template <int SHAPE, bool FIXED, bool UNIT>
 __global__ void __launch_bounds__(PART_THREADS) k_deposit(Geom g, SoA p, const long long* __restrict__ d_n,
                                                           double spwt, double* __restrict__ den,
@@ -87,58 +137,10 @@ __global__ void __launch_bounds__(PART_THREADS) k_deposit(Geom g, SoA p, const l
                                                           int* flags) {
   const long long n = *d_n;
   const long long stride = (long long)gridDim.x * blockDim.x;
-  double* facc = reinterpret_cast<double*>(acc);
-  // fx_scale = 2^k: a weight product of two 52-bit offsets carries 2^104.
-  const int wshift = 104 - ((int)(((uint64_t)__double_as_longlong(fx_scale) >> 52) & 0x7FF) - 1023);
+  const int wshift = weight_shift(fx_scale);
   bool bad = false;
-  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
-    double lx = to_logical<UNIT>(p.x[q], g.x0, g.dx);
-    double ly = to_logical<UNIT>(p.y[q], g.y0, g.dy);
-    if (SHAPE == EPIC_NGP) {
-      int gx = (int)round(lx), gy = (int)round(ly);
-      if (gx < 0 || gx >= g.nx || gy < 0 || gy >= g.ny) {
-        bad = true;
-        continue;
-      }
-      long k = (long)gx * g.ny + gy;
-      if (FIXED) atomicAdd(&acc[k], (unsigned long long)__double2ll_rn(fx_scale));
-      else atomicAdd(&facc[k], spwt);
-    } else {
-      uint64_t X, Y;
-      if (FIXED && fx52(lx, X) && fx52(ly, Y)) {
-        const int i = (int)(X >> 52), j = (int)(Y >> 52);
-        if (i + 1 >= g.nx || j + 1 >= g.ny) {
-          bad = true;
-          continue;
-        }
-        const uint64_t one = 1ull << 52, di = X & (one - 1), dj = Y & (one - 1);
-        const long k = (long)i * g.ny + j;
-        atomicAdd(&acc[k], fx_weight(one - di, one - dj, wshift));
-        atomicAdd(&acc[k + g.ny], fx_weight(di, one - dj, wshift));
-        atomicAdd(&acc[k + 1], fx_weight(one - di, dj, wshift));
-        atomicAdd(&acc[k + g.ny + 1], fx_weight(di, dj, wshift));
-        continue;
-      }
-      int i = (int)lx, j = (int)ly;
-      if (i < 0 || i + 1 >= g.nx || j < 0 || j + 1 >= g.ny) {
-        bad = true;
-        continue;
-      }
-      double di = lx - i, dj = ly - j;
-      long k = (long)i * g.ny + j;
-      if (FIXED) {
-        atomicAdd(&acc[k], (unsigned long long)__double2ll_rn((1 - di) * (1 - dj) * fx_scale));
-        atomicAdd(&acc[k + g.ny], (unsigned long long)__double2ll_rn((di) * (1 - dj) * fx_scale));
-        atomicAdd(&acc[k + 1], (unsigned long long)__double2ll_rn((1 - di) * (dj) * fx_scale));
-        atomicAdd(&acc[k + g.ny + 1], (unsigned long long)__double2ll_rn((di) * (dj) * fx_scale));
-      } else {
-        atomicAdd(&facc[k], spwt * (1 - di) * (1 - dj));
-        atomicAdd(&facc[k + g.ny], spwt * (di) * (1 - dj));
-        atomicAdd(&facc[k + 1], spwt * (1 - di) * (dj));
-        atomicAdd(&facc[k + g.ny + 1], spwt * (di) * (dj));
-      }
-    }
-  }
+  for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride)
+    bad |= !deposit_one<SHAPE, FIXED, UNIT>(g, p.x[q], p.y[q], spwt, acc, fx_scale, wshift);
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
 }
 
@@ -389,6 +391,138 @@ void launch_particle_sums(cudaStream_t st, int what, const SoA& p, const long lo
                           double* partials, double* out3, int grid) {
   k_particle_sums<<<grid, PART_THREADS, 0, st>>>(what, p, d_n, vel_norm, partials);
   k_sum_partials3<<<1, 96, 0, st>>>(partials, grid, out3);
+}
+
+// ------------------------------------------- host-resident particles ---
+// For a caller that keeps its particles in host memory, as the reference
+// keeps part_list (epic_step_host): these kernels read and write that memory
+// directly (SM loads and stores over the host link, mapped pinned memory),
+// staging tiles of HOSTIO_TILE records of {x, y, vx, vy, vz} in shared memory
+// so the host side moves as one contiguous run per tile, and do the step's
+// own work on the way, so the transfer hides it: the upload fills the device
+// arrays and deposits, the push writes the device arrays and the host records.
+constexpr int HOSTIO_TILE = PART_THREADS;
+
+template <int SHAPE, bool UNIT>
+__global__ void __launch_bounds__(PART_THREADS) k_upload_deposit(const double* __restrict__ host, long long n, SoA p,
+                                                                 long long* __restrict__ d_n, Geom g,
+                                                                 unsigned long long* __restrict__ acc,
+                                                                 double fx_scale, int* flags) {
+  __shared__ double tile[HOSTIO_TILE * 5];
+  if (blockIdx.x == 0 && threadIdx.x == 0) *d_n = n;
+  const int wshift = weight_shift(fx_scale);
+  bool bad = false;
+  for (long long base = (long long)blockIdx.x * HOSTIO_TILE; base < n;
+       base += (long long)gridDim.x * HOSTIO_TILE) {
+    const int cnt = (int)min((long long)HOSTIO_TILE, n - base);
+    const double* src = host + base * 5;
+    for (int k = threadIdx.x; k < cnt * 5; k += PART_THREADS) tile[k] = src[k];
+    __syncthreads();
+    if (threadIdx.x < cnt) {
+      const double* r = tile + threadIdx.x * 5;
+      const long long q = base + threadIdx.x;
+      p.x[q] = r[0];
+      p.y[q] = r[1];
+      p.vx[q] = r[2];
+      p.vy[q] = r[3];
+      p.vz[q] = r[4];
+      bad |= !deposit_one<SHAPE, true, UNIT>(g, r[0], r[1], 0.0, acc, fx_scale, wshift);
+    }
+    __syncthreads();
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
+}
+
+template <int SHAPE, int BC, bool UNIT>
+__global__ void __launch_bounds__(PART_THREADS) k_push_download(Geom g, SoA p, const long long* __restrict__ d_n,
+                                                                const double2* __restrict__ ef, double qmK, double c,
+                                                                double dtsub, double* __restrict__ host, int* flags) {
+  __shared__ double tile[HOSTIO_TILE * 5];
+  const long long n = *d_n;
+  bool bad = false;
+  for (long long base = (long long)blockIdx.x * HOSTIO_TILE; base < n;
+       base += (long long)gridDim.x * HOSTIO_TILE) {
+    const int cnt = (int)min((long long)HOSTIO_TILE, n - base);
+    if (threadIdx.x < cnt) {
+      const long long q = base + threadIdx.x;
+      double x = p.x[q], y = p.y[q], vx = p.vx[q], vy = p.vy[q];
+      const double vz = p.vz[q];
+      push_one<SHAPE, BC, UNIT>(g, ef, qmK, c, dtsub, x, y, vx, vy, bad);
+      p.x[q] = x;
+      p.y[q] = y;
+      p.vx[q] = vx;
+      p.vy[q] = vy;
+      double* r = tile + threadIdx.x * 5;
+      r[0] = x;
+      r[1] = y;
+      r[2] = vx;
+      r[3] = vy;
+      r[4] = vz;
+    }
+    __syncthreads();
+    double* dst = host + base * 5;
+    for (int k = threadIdx.x; k < cnt * 5; k += PART_THREADS) dst[k] = tile[k];
+    __syncthreads();
+  }
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
+}
+
+// Records [from, min(n, cap)) to host memory (FLAG_CAPACITY if n > cap).
+__global__ void __launch_bounds__(PART_THREADS) k_download(SoA p, const long long* __restrict__ d_n, long long from,
+                                                           long long cap, double* __restrict__ host, int* flags) {
+  __shared__ double tile[HOSTIO_TILE * 5];
+  long long n = *d_n;
+  if (n > cap) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) set_flag(flags, FLAG_CAPACITY);
+    n = cap;
+  }
+  for (long long base = from + (long long)blockIdx.x * HOSTIO_TILE; base < n;
+       base += (long long)gridDim.x * HOSTIO_TILE) {
+    const int cnt = (int)min((long long)HOSTIO_TILE, n - base);
+    if (threadIdx.x < cnt) {
+      const long long q = base + threadIdx.x;
+      double* r = tile + threadIdx.x * 5;
+      r[0] = p.x[q];
+      r[1] = p.y[q];
+      r[2] = p.vx[q];
+      r[3] = p.vy[q];
+      r[4] = p.vz[q];
+    }
+    __syncthreads();
+    double* dst = host + base * 5;
+    for (int k = threadIdx.x; k < cnt * 5; k += PART_THREADS) dst[k] = tile[k];
+    __syncthreads();
+  }
+}
+
+void launch_upload_deposit(cudaStream_t st, const Geom& g, int shape, const double* host, long long n, const SoA& p,
+                           long long* d_n, unsigned long long* acc, double fx_scale, int* flags, int grid) {
+#define UPD(SH, U) k_upload_deposit<SH, U><<<grid, PART_THREADS, 0, st>>>(host, n, p, d_n, g, acc, fx_scale, flags)
+  const bool u = unit_cell(g);
+  if (shape == EPIC_NGP) { if (u) UPD(EPIC_NGP, true); else UPD(EPIC_NGP, false); }
+  else { if (u) UPD(EPIC_CIC, true); else UPD(EPIC_CIC, false); }
+#undef UPD
+}
+
+void launch_push_download(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, const long long* d_n,
+                          const double2* ef, double qmK, double c, double dtsub, double* host, int* flags, int grid) {
+#define PD(SH, B, U) k_push_download<SH, B, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, host, flags)
+#define BOTH(...) do { if (u) PD(__VA_ARGS__, true); else PD(__VA_ARGS__, false); } while (0)
+  const bool u = unit_cell(g);
+  if (bc == EPIC_PBC) {
+    if (shape == EPIC_NGP) BOTH(EPIC_NGP, EPIC_PBC);
+    else BOTH(EPIC_CIC, EPIC_PBC);
+  } else {
+    if (shape == EPIC_NGP) BOTH(EPIC_NGP, EPIC_REFLECTIVE);
+    else BOTH(EPIC_CIC, EPIC_REFLECTIVE);
+  }
+#undef BOTH
+#undef PD
+}
+
+void launch_download(cudaStream_t st, const SoA& p, const long long* d_n, long long from, long long cap, double* host,
+                     int* flags, int grid) {
+  k_download<<<grid, PART_THREADS, 0, st>>>(p, d_n, from, cap, host, flags);
 }
 
 }  // namespace epic

@@ -184,6 +184,18 @@ epic_status epic_handle_collisions(epic_sim* sim, int electrons, int ions, const
  * every species (the one named "ion" is skipped if ionfixed), then
  * handle_collisions(species 0, species 1) if with_collisions. */
 epic_status epic_step(epic_sim* sim, int with_collisions);
+/* One loop iteration (as epic_step) for particles held by the caller in host
+ * memory, as the reference holds part_list (src/main.cpp:405-423 over the
+ * species' vectors): species s has n[s] records of {x, y, vx, vy, vz} at
+ * parts[s] with room for capacity[s]; on return the records are the stepped
+ * particles and n[s] their new count (ionisation appends electrons and ions).
+ * With pinned buffers (cudaHostAlloc / cudaHostRegister) in the FP64 form,
+ * with periodic or reflective walls and the fixed-point deposit, the kernels
+ * read and write the buffers directly and overlap the transfers with the
+ * deposit and the push; otherwise it is epic_set_particles + epic_step +
+ * epic_get_particles.  Same results either way. */
+epic_status epic_step_host(epic_sim* sim, int with_collisions, double* const* parts, int64_t* n,
+                           const int64_t* capacity);
 /* The prologue of src/main.cpp:366-382: scatter, rho, solve, E, rewind. */
 epic_status epic_initial_field(epic_sim* sim);
 /* Runs `steps` loop iterations; with use_graph=1 one step is captured as a
