@@ -574,6 +574,12 @@ void epic_destroy(epic_sim* s) {
     cudaEventDestroy(pe.second.second);
   }
   for (auto e : s->event_pool) cudaEventDestroy(e);
+  if (s->side) {
+    cudaStreamSynchronize(s->side);
+    cudaStreamDestroy(s->side);
+    cudaEventDestroy(s->ev_fork);
+    cudaEventDestroy(s->ev_join);
+  }
   dfree(s, s->mcc_ev.buf);
   dfree(s, s->mcc_ev.count);
   dfree(s, s->mcc_ev.slot);
@@ -959,12 +965,25 @@ epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* part
   const bool coll = with_collisions && nsp >= 2;
   const double K = (c.density * QE * c.L) / (EPS_0 * c.W * c.vel_norm);
   const double cc = (c.vel_norm) / (c.L * c.W);
-  for (int k = 0; k < nsp; k++) {
-    if (c.ionfixed == 1 && s->sp[k].name == "ion") continue;
-    if (coll && k == 0) {
-      if ((st = do_push(s, 0, 1))) return st;  // the MCC changes the electrons afterwards
-      continue;
+  const bool push_e = coll && !(c.ionfixed == 1 && s->sp[0].name == "ion");
+  if (push_e) {
+    // The MCC changes the electrons after the push, so they go back after it;
+    // their push runs on a side stream while the other species stream out.
+    if (!s->side) {
+      CK(cudaStreamCreateWithFlags(&s->side, cudaStreamNonBlocking));
+      CK(cudaEventCreateWithFlags(&s->ev_fork, cudaEventDisableTiming));
+      CK(cudaEventCreateWithFlags(&s->ev_join, cudaEventDisableTiming));
     }
+    epic_species_state& e = s->sp[0];
+    CK(cudaEventRecord(s->ev_fork, s->stream));
+    CK(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
+    launch_push(s->side, s->g, c.shape, c.bc, e.soa, e.d_n, s->ef, (e.desc.charge / e.desc.mass) * K, cc, c.DT,
+                s->d_flags, s->tile_status, s->tile_ctr, s->part_grid);
+    CK(cudaEventRecord(s->ev_join, s->side));
+    s->launches += 1;
+  }
+  for (int k = coll ? 1 : 0; k < nsp; k++) {
+    if (c.ionfixed == 1 && s->sp[k].name == "ion") continue;
     epic_species_state& sp = s->sp[k];
     launch_push_download(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, (sp.desc.charge / sp.desc.mass) * K,
                          cc, c.DT, parts[k], s->d_flags, s->part_grid);
@@ -972,6 +991,7 @@ epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* part
   }
   CKL();
   if (coll) {
+    if (push_e) CK(cudaStreamWaitEvent(s->stream, s->ev_join, 0));
     if ((st = do_mcc(s, 0, 1, nullptr, 0))) return st;
     launch_download(s->stream, s->sp[0].soa, s->sp[0].d_n, 0, capacity[0], parts[0], s->d_flags, s->part_grid);
     launch_download(s->stream, s->sp[1].soa, s->sp[1].d_n, n[1], capacity[1], parts[1], s->d_flags, s->part_grid);

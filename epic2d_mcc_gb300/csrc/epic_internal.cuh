@@ -282,6 +282,8 @@ struct epic_sim {
   epic_config cfg;
   epic::Geom g;
   cudaStream_t stream;
+  cudaStream_t side = nullptr;  // epic_step_host: electrons pushed beside the other species' transfers
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int num_sms;
   int part_grid;
   std::vector<epic_species_state> sp;
