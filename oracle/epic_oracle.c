@@ -64,9 +64,83 @@ double or_sample_vel(or_rng* r, double mass, double temp) {
   return v_th * sqrt(2) * (u1 + u2 + u3 - 1.5);
 }
 
-/* src/init.cpp:22-92 (no conductor rejection; grid_count = 0). */
+/* ------------------------------------------------------- conductors --- */
+/* Grid::IsGrid over the grids (src/grid.cpp:11-65, src/electrode.cpp:20-26):
+ * grids are OR_GRID_WORDS doubles each, {0, min_x, max_x, min_y, max_y, -, -, V}
+ * (ReactConductorGrid) or {1, x_center, y_center, electrodes, grid_radius,
+ * electrode_radius, -, V} (CircularGrid).  A circular grid has electrodes only
+ * once CircularGrid::initialize has run (inside gssolver), so circles_live = 0
+ * leaves it out. */
+static void electrode_center(const double* g, int k, double* ex, double* ey) {
+  const int num = (int)g[3];
+  const double theta = k * (2.0 * OR_M_PI / num);  /* src/grid.cpp:52-56 */
+  *ex = (int)g[1] + g[4] * cos(theta);
+  *ey = (int)g[2] + g[4] * sin(theta);
+}
+
+int or_in_conductors(const double* grids, int ng, int circles_live, double x, double y) {
+  for (int k = 0; k < ng; k++) {
+    const double* g = grids + OR_GRID_WORDS * k;
+    if (g[0] == 0) {
+      if (x >= (int)g[1] && x <= (int)g[2] && y >= (int)g[3] && y <= (int)g[4]) return 1;
+    } else if (circles_live) {
+      for (int e = 0; e < (int)g[3]; e++) {
+        double ex, ey;
+        electrode_center(g, e, &ex, &ey);
+        double dx = x - ex, dy = y - ey;
+        double distance_squared = dx * dx + dy * dy;
+        double radius_squared = g[5] * g[5];
+        if (distance_squared <= radius_squared) return 1;
+      }
+    }
+  }
+  return 0;
+}
+
+/* Grid::initialize of every grid, in order, as gssolver runs it before its
+ * iterations (src/field.cpp:100-103): ReactConductorGrid sets rho on the border
+ * of its node rectangle (src/grid.cpp:67-85), each electrode of a circular grid
+ * sets rho at 100 points of its circle (src/electrode.cpp:4-17).  Nodes outside
+ * the grid are skipped (the reference's rectangle loop does not check). */
+void or_conductor_rho(const or_domain* d, const double* grids, int ng, double* rho) {
+  const int nx = d->nx, ny = d->ny;
+  for (int k = 0; k < ng; k++) {
+    const double* g = grids + OR_GRID_WORDS * k;
+    if (g[0] == 0) {
+      int min_i = (int)((((int)g[1]) - d->x0) / d->dx), max_i = (int)((((int)g[2]) - d->x0) / d->dx);
+      int min_j = (int)((((int)g[3]) - d->y0) / d->dy), max_j = (int)((((int)g[4]) - d->y0) / d->dy);
+      for (int i = min_i; i <= max_i; i++)
+        for (int j = min_j; j <= max_j; j++)
+          if ((i == min_i || i == max_i || j == min_j || j == max_j) && i >= 0 && i < nx && j >= 0 && j < ny)
+            rho[IDX(i, j)] = g[7];
+    } else {
+      for (int e = 0; e < (int)g[3]; e++) {
+        double ex, ey;
+        electrode_center(g, e, &ex, &ey);
+        const int N = 100;
+        for (int q = 0; q < N; q++) {
+          double theta = 2.0 * q * OR_M_PI / N;
+          int x = (int)(ex + g[5] * cos(theta) + 0.5);
+          int y = (int)(ey + g[5] * sin(theta) + 0.5);
+          if (x >= 0 && x < nx && y >= 0 && y < ny) rho[IDX(x, y)] = g[7];
+        }
+      }
+    }
+  }
+}
+
+/* src/init.cpp:22-92, with the rejection of positions inside a conductor
+ * (:71-86): a rejected "random" position is drawn again; the other load types
+ * repeat the same position, where the reference loops forever (returns -2). */
+int or_load_c(const or_domain* d, or_rng* r, const char* type, int n_arg, double mass, double temp, double vsx,
+              double vsy, long n, double* out, const double* grids, int ng);
 int or_load(const or_domain* d, or_rng* r, const char* type, int n_arg, double mass, double temp, double vsx,
             double vsy, long n, double* out) {
+  return or_load_c(d, r, type, n_arg, mass, temp, vsx, vsy, n, out, 0, 0);
+}
+
+int or_load_c(const or_domain* d, or_rng* r, const char* type, int n_arg, double mass, double temp, double vsx,
+              double vsy, long n, double* out, const double* grids, int ng) {
   int kind;
   if (strcmp(type, "random") == 0) kind = 0;
   else if (strcmp(type, "uniform") == 0) kind = 1;
@@ -75,6 +149,7 @@ int or_load(const or_domain* d, or_rng* r, const char* type, int n_arg, double m
   else return -1;
   for (long p = 0; p < n; p++) {
     double x = 0, y = 0;
+    for (;;) {
     if (kind == 0) {
       x = d->x0 + d->Lx * or_rng_uniform(r);
       y = d->y0 + d->Ly * or_rng_uniform(r);
@@ -95,6 +170,9 @@ int or_load(const or_domain* d, or_rng* r, const char* type, int n_arg, double m
         x += cos(kx * x);
         y += cos(ky * y);
       }
+    }
+    if (!or_in_conductors(grids, ng, 0, x, y)) break;
+    if (kind != 0) return -2;
     }
     double vx = or_sample_vel(r, mass, temp) + vsx * d->vel_norm;
     double vy = or_sample_vel(r, mass, temp) + vsy * d->vel_norm;
@@ -336,9 +414,17 @@ static double interp(const or_domain* d, double lx, double ly, const double* f) 
          f[IDX(i + 1, j + 1)] * (di) * (dj);
 }
 
-/* Species::Push_species_serial (src/species.cpp:29-170). */
+/* Species::Push_species_serial (src/species.cpp:29-170), erasing particles
+ * that end inside a conductor (:80-97, :108-121, :150-165). */
+long or_push_c(const or_domain* d, double mass, double charge, int sub_cycle, double* part, long n,
+               const double* efx, const double* efy, const double* grids, int ng, int circles_live);
 long or_push(const or_domain* d, double mass, double charge, int sub_cycle, double* part, long n,
              const double* efx, const double* efy) {
+  return or_push_c(d, mass, charge, sub_cycle, part, n, efx, efy, 0, 0, 0);
+}
+
+long or_push_c(const or_domain* d, double mass, double charge, int sub_cycle, double* part, long n,
+               const double* efx, const double* efy, const double* grids, int ng, int circles_live) {
   long out = 0;
   for (long p = 0; p < n; p++) {
     double* q = part + 5 * p;
@@ -366,6 +452,7 @@ long or_push(const or_domain* d, double mass, double charge, int sub_cycle, doub
       if (q[1] < d->x0) { q[1] = d->x0 + (d->x0 - q[1]); q[3] = -q[3]; }
       else if (q[1] >= d->x0 + d->Ly) { q[1] = d->x0 + d->Ly - (q[1] - (d->x0 + d->Ly)); q[3] = -q[3]; }
     }
+    if (ng && or_in_conductors(grids, ng, circles_live, q[0], q[1])) continue;
     if (out != p) memmove(part + 5 * out, q, 5 * sizeof(double));
     out++;
   }

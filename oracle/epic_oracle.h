@@ -31,6 +31,8 @@ extern "C" {
 #define OR_ME 9.10938215e-31
 #define OR_K_B 1.380648e-23
 #define OR_PI 3.141592653
+#define OR_M_PI 3.14159265358979323846  /* M_PI (src/grid.cpp, src/electrode.cpp) */
+#define OR_GRID_WORDS 8
 #define OR_EV 1.602176565e-19
 #define OR_CS_RANGES 5000000
 #define OR_DE_CS 0.005
@@ -84,6 +86,13 @@ int or_pcg_solve(const or_domain* d, const double* rho, double* phi, double* err
 void or_efield(const or_domain* d, const double* phi, double* efx, double* efy);
 /* Species::Push_species_serial (src/species.cpp:29-170), no conductors.
  * Returns the new particle count (open boundaries erase, order kept). */
+/* Conductors (grids of OR_GRID_WORDS doubles, see epic_oracle.c). */
+int or_in_conductors(const double* grids, int ng, int circles_live, double x, double y);
+void or_conductor_rho(const or_domain* d, const double* grids, int ng, double* rho);
+int or_load_c(const or_domain* d, or_rng* r, const char* type, int n_arg, double mass, double temp, double vsx,
+              double vsy, long n, double* out, const double* grids, int ng);
+long or_push_c(const or_domain* d, double mass, double charge, int sub_cycle, double* part, long n,
+               const double* efx, const double* efy, const double* grids, int ng, int circles_live);
 long or_push(const or_domain* d, double mass, double charge, int sub_cycle, double* part, long n,
              const double* efx, const double* efy);
 /* Species::Rewind_species (src/species.cpp:229-246). */

@@ -142,6 +142,9 @@ class Setup:
     normscheme: int
     species: list = field(default_factory=list)
     sor_omega: float = 1.4  # optional [solver] sor_omega; 1.4 is hard-coded in src/field.cpp:114
+    # [Grids] (src/main.cpp:284-327) as rows of 8 doubles: {0, min_x, max_x, min_y, max_y, 0, 0, V}
+    # (reactconduct) or {1, x_center, y_center, electrode_number, grid_radius, electrod_radius, 0, V}
+    grids: np.ndarray = field(default_factory=lambda: np.zeros((0, 8)))
 
 
 def setup(path: str) -> Setup:
@@ -227,7 +230,26 @@ def setup(path: str) -> Setup:
                  max_iteration=_stoi(solver["max_iteration"]), gas_density=_stod(col["GAS_DENSITY"]),
                  elastic=string_to_bool(col["elastic"]), excitation=string_to_bool(col["excitation"]),
                  ionization=string_to_bool(col["ionization"]), num_ts=num_ts, ionfixed=_stoi(sim["ionfixed"]),
-                 normscheme=norm_scheme, species=species, sor_omega=_stod(solver.get("sor_omega", "1.4")))
+                 normscheme=norm_scheme, species=species, sor_omega=_stod(solver.get("sor_omega", "1.4")),
+                 grids=conductors(ini))
+
+
+def conductors(ini) -> np.ndarray:
+    """The [Grids] section as src/main.cpp:284-327 reads it (voltages scaled by eV/(k_B EV_to_K))."""
+    g = ini.get("Grids", {})
+    rows = []
+    vscale = EV / (K_B * EV_TO_K)
+    for i in range(_stoi(g.get("grid_count", "0"))):
+        pre = "grid_%d." % i
+        t = g[pre + "type"]
+        if t == "circular":
+            rows.append([1, _stoi(g[pre + "x_center"]), _stoi(g[pre + "y_center"]), _stoi(g[pre + "electrode_number"]),
+                         _stod(g[pre + "grid_radius"]), _stod(g[pre + "electrod_radius"]), 0,
+                         vscale * _stod(g[pre + "electrode_voltage"])])
+        elif t == "reactconduct":
+            rows.append([0, _stoi(g[pre + "min_x"]), _stoi(g[pre + "max_x"]), _stoi(g[pre + "min_y"]),
+                         _stoi(g[pre + "max_y"]), 0, 0, vscale * _stod(g[pre + "grid_voltage"])])
+    return np.array(rows, dtype=np.float64).reshape(-1, 8)
 
 
 def load_type(s: str):
@@ -288,6 +310,12 @@ def restatement_lib():
         L.or_rng_u32.argtypes = [vp]
         L.or_rng_u32.restype = ctypes.c_uint32
         L.or_load.argtypes = [vp, vp, ctypes.c_char_p, i, d, d, d, d, l, vp]
+        L.or_load_c.argtypes = [vp, vp, ctypes.c_char_p, i, d, d, d, d, l, vp, vp, i]
+        L.or_push_c.argtypes = [vp, d, d, i, vp, l, vp, vp, vp, i, i]
+        L.or_push_c.restype = l
+        L.or_conductor_rho.argtypes = [vp, vp, i, vp]
+        L.or_in_conductors.argtypes = [vp, i, i, d, d]
+        L.or_in_conductors.restype = i
         L.or_scatter.argtypes = [vp, vp, l, d, vp]
         L.or_scatter.restype = l
         L.or_compute_rho.argtypes = [vp, i, vp, vp, vp]
@@ -338,11 +366,21 @@ class Restatement:
     def load(self, rng: Rng, sp: SpeciesDesc) -> np.ndarray:
         t, n = load_type(sp.load)
         out = np.zeros((sp.numparticle, 5))
-        rc = self.L.or_load(ctypes.byref(self.d), ctypes.byref(rng.s), t.encode(), n, sp.mass, sp.temp, sp.vsx, sp.vsy,
-                            sp.numparticle, _p(out))
+        g = np.ascontiguousarray(self.s.grids)
+        rc = self.L.or_load_c(ctypes.byref(self.d), ctypes.byref(rng.s), t.encode(), n, sp.mass, sp.temp, sp.vsx,
+                              sp.vsy, sp.numparticle, _p(out), _p(g), len(g))
+        if rc == -2:
+            raise ValueError("load type %r puts a particle inside a conductor (the reference loops forever)" % sp.load)
         if rc != 0:
             raise ValueError("unsupported load type %r" % sp.load)
         return out
+
+    def conductor_rho(self, rho):
+        """Grid::initialize of every conductor, as gssolver runs it (src/field.cpp:100-103)."""
+        rho = np.ascontiguousarray(rho).copy()
+        g = np.ascontiguousarray(self.s.grids)
+        self.L.or_conductor_rho(ctypes.byref(self.d), _p(g), len(g), _p(rho))
+        return rho
 
     def scatter(self, part: np.ndarray, spwt: float) -> np.ndarray:
         den = self.grid()
@@ -388,9 +426,11 @@ class Restatement:
         self.L.or_efield(ctypes.byref(self.d), _p(np.ascontiguousarray(phi)), _p(efx), _p(efy))
         return efx, efy
 
-    def push(self, sp: SpeciesDesc, part, efx, efy, sub_cycle=1):
+    def push(self, sp: SpeciesDesc, part, efx, efy, sub_cycle=1, circles_live=False):
         part = np.ascontiguousarray(part).copy()
-        n = self.L.or_push(ctypes.byref(self.d), sp.mass, sp.charge, sub_cycle, _p(part), len(part), _p(efx), _p(efy))
+        g = np.ascontiguousarray(self.s.grids)
+        n = self.L.or_push_c(ctypes.byref(self.d), sp.mass, sp.charge, sub_cycle, _p(part), len(part), _p(efx),
+                             _p(efy), _p(g), len(g), int(circles_live))
         return part[:n]
 
     def rewind(self, sp: SpeciesDesc, part, efx, efy):
@@ -459,8 +499,9 @@ class Restatement:
 
 
 class OracleSim:
-    """The loop of src/main.cpp:359-423 on the restatement (no emitters or
-    conductors).  State: parts[s] (n,5) arrays, den[s], rho, phi, efx, efy."""
+    """The loop of src/main.cpp:359-423 on the restatement, conductors
+    included (no emitters).  State: parts[s] (n,5) arrays, den[s], rho, phi,
+    efx, efy."""
 
     def __init__(self, ini_path: str, load: bool = True, initial_field: bool = True, rng: Rng | None = None):
         self.s = setup(ini_path)
@@ -474,6 +515,7 @@ class OracleSim:
         self.efy = self.R.grid()
         self.error = 0.0
         self.iters = 0
+        self.circles_live = False  # circular grids have electrodes after the first gssolver call
         if load:
             self.parts = [self.R.load(self.rng, sp) for sp in self.s.species]
         if initial_field:
@@ -484,6 +526,9 @@ class OracleSim:
         self.rho = self.R.compute_rho(self.den, [sp.charge for sp in self.s.species])
 
     def field(self):
+        if self.s.solver == "gs" and len(self.s.grids):
+            self.rho = self.R.conductor_rho(self.rho)
+            self.circles_live = True
         self.phi, self.error, self.iters, _ = self.R.solve(self.rho)
         self.efx, self.efy = self.R.efield(self.phi)
 
@@ -496,7 +541,7 @@ class OracleSim:
         for k, sp in enumerate(self.s.species):
             if sp.name == "ion" and self.s.ionfixed == 1:
                 continue
-            self.parts[k] = self.R.push(sp, self.parts[k], self.efx, self.efy)
+            self.parts[k] = self.R.push(sp, self.parts[k], self.efx, self.efy, circles_live=self.circles_live)
 
     def collide(self, uniforms=None):
         e, i, nc, kinds = self.R.mcc(self.parts[0], self.parts[1], self.s.species[1],

@@ -159,7 +159,34 @@ void* ref_create(const char* ini_path, int load_particles, int initial_field) {
       s->species.emplace_back(names[i], mass[i], sign[i] * Const::QE, spwt, temps[i], nP[i], vsx[i], vsy[i],
                               frac[i], pos_init[i], *d);
     }
-    // Conductors and emitters are outside the hot path; grid_count/count must be 0.
+    // Conductors as src/main.cpp:284-327 reads them (emitters are not driven here).
+    {
+      auto& gsec = iniData["Grids"];
+      const int grid_count = INIParser::getInt(gsec, "grid_count");
+      const double vscale = Const::eV / (Const::K_b * Const::EV_to_K);
+      for (int g = 0; g < grid_count; g++) {
+        const std::string pre = "grid_" + std::to_string(g) + ".";
+        const std::string type = INIParser::getString(gsec, pre + "type");
+        GridParams cp;
+        RectangularGridParams rp;
+        if (type == "circular") {
+          cp.grid_centerx = INIParser::getInt(gsec, pre + "x_center");
+          cp.grid_centery = INIParser::getInt(gsec, pre + "y_center");
+          cp.num_electrodes = INIParser::getInt(gsec, pre + "electrode_number");
+          cp.grid_rad = INIParser::getDouble(gsec, pre + "grid_radius");
+          cp.electrode_rad = INIParser::getDouble(gsec, pre + "electrod_radius");
+          cp.voltage = vscale * INIParser::getDouble(gsec, pre + "electrode_voltage");
+          s->grids.push_back(Create_Grid(GridType::Circular, *d, cp, rp));
+        } else if (type == "reactconduct") {
+          rp.min_x = INIParser::getInt(gsec, pre + "min_x");
+          rp.min_y = INIParser::getInt(gsec, pre + "min_y");
+          rp.max_x = INIParser::getInt(gsec, pre + "max_x");
+          rp.max_y = INIParser::getInt(gsec, pre + "max_y");
+          rp.voltage = vscale * INIParser::getDouble(gsec, pre + "grid_voltage");
+          s->grids.push_back(Create_Grid(GridType::ReactConductor, *d, cp, rp));
+        }
+      }
+    }
     if (load_particles) {
       for (Species& sp : s->species) Init init(sp, *d, s->grids);
     }
@@ -188,6 +215,7 @@ void ref_destroy(void* h) {
   RefSim* s = static_cast<RefSim*>(h);
   delete s->coll;
   delete s->fs;
+  for (Grid* g : s->grids) delete g;
   s->species.clear();
   delete s->domain;
   delete s;

@@ -37,7 +37,7 @@ x0       = 0
 y0       = 0
 
 [Grids]
-grid_count = 0
+{grids}
 
 [Emitters]
 count = 0
@@ -79,7 +79,7 @@ BEAM = "beam,9.10938215E-31,{n},{t},-1,{frac},{vx},{vy},random"
 
 def deck(nx=16, ny=16, ne=2000, ni=2000, te=1, ti=0.026, ion_mass="1.6726219e-27", solver="gs", tol="1e-8",
          maxit=20000, bc="pbc", shape="CIC", dt=0.01, norm=1, density="1E13", collisions=False, gas="1e20",
-         ionfixed=0, beam=None, vdrift=(0, 0), solver_extra="", sim_extra="", coll_extra="", num_ts=10):
+         ionfixed=0, beam=None, vdrift=(0, 0), solver_extra="", sim_extra="", coll_extra="", num_ts=10, grids=None):
     sp = [ELECTRON.format(n=ne, t=te, vx=vdrift[0], vy=vdrift[1]), ION.format(m=ion_mass, n=ni, t=ti)]
     if beam:
         sp.append(BEAM.format(**beam))
@@ -87,7 +87,18 @@ def deck(nx=16, ny=16, ne=2000, ni=2000, te=1, ti=0.026, ion_mass="1.6726219e-27
     return TEMPLATE.format(num_ts=num_ts, dt=dt, nx=nx, ny=ny, norm=norm, solver=solver, tol=tol, maxit=maxit,
                            shape=shape, density=density, bc=bc, ionfixed=ionfixed, el=flag, ex=flag, io=flag,
                            gas=gas, species="\n".join(sp), solver_extra=solver_extra, sim_extra=sim_extra,
-                           coll_extra=coll_extra)
+                           coll_extra=coll_extra, grids=grid_section(grids or []))
+
+
+def grid_section(grids) -> str:
+    """[Grids] lines in the reference's keys (src/main.cpp:284-327) from dicts with a "type" of
+    "reactconduct" (min_x, max_x, min_y, max_y, grid_voltage) or "circular" (x_center, y_center,
+    electrode_number, grid_radius, electrod_radius, electrode_voltage)."""
+    lines = ["grid_count = %d" % len(grids)]
+    for i, g in enumerate(grids):
+        for k, v in g.items():
+            lines.append("grid_%d.%s = %s" % (i, k, v))
+    return "\n".join(lines)
 
 
 def write(text: str, directory: str | None = None) -> str:

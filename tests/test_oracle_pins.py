@@ -88,7 +88,18 @@ def test_mcc_injected_mode_replays_sequential_stream(tmp_path):
 
 needs_ref = pytest.mark.skipif(not O.Reference.available(), reason="reference checkout not available here")
 
+# Two conductors: a rectangle (ReactConductorGrid) and a ring of six circular
+# electrodes (CircularGrid), src/grid.cpp, src/electrode.cpp.
+CONDUCTORS = [dict(type="reactconduct", min_x=10, max_x=12, min_y=4, max_y=16, grid_voltage=10),
+              dict(type="circular", x_center=22, y_center=12, electrode_number=6, grid_radius=5,
+                   electrod_radius=1.5, electrode_voltage=-5)]
+
 LIVE = {
+    "gs_open_conductors": dict(nx=32, ny=24, ne=2000, ni=2000, te=4, solver="gs", tol="1e-8", bc="open",
+                               grids=CONDUCTORS),
+    "gs_reflective_conductors": dict(nx=32, ny=24, ne=2000, ni=2000, te=4, solver="gs", tol="1e-8",
+                                     bc="reflective", grids=CONDUCTORS),
+    "pcg_pbc_conductors": dict(nx=32, ny=24, ne=2000, ni=2000, te=4, solver="cg", tol="1e-10", grids=CONDUCTORS),
     "gs_pbc_cic_rect": dict(nx=20, ny=14, ne=1500, ni=1500, solver="gs", tol="1e-9"),
     "gs_open_ngp": dict(nx=16, ny=16, ne=1500, ni=1500, solver="gs", tol="1e-8", bc="open", shape="NGP", te=6),
     "pcg_reflective_cic": dict(nx=18, ny=18, ne=1500, ni=1500, solver="cg", tol="1e-10", bc="reflective"),
