@@ -57,6 +57,23 @@ class SpeciesDesc(ctypes.Structure):
                 ("load", ctypes.c_char * 32), ("capacity", ctypes.c_int64)]
 
 
+class Conductor(ctypes.Structure):
+    """epic_conductor: a ReactConductorGrid (type 0) or a CircularGrid (type 1), src/grid.cpp."""
+    _fields_ = [("type", ctypes.c_int), ("min_x", ctypes.c_int), ("max_x", ctypes.c_int), ("min_y", ctypes.c_int),
+                ("max_y", ctypes.c_int), ("x_center", ctypes.c_int), ("y_center", ctypes.c_int),
+                ("electrode_number", ctypes.c_int), ("grid_radius", ctypes.c_double),
+                ("electrode_radius", ctypes.c_double), ("voltage", ctypes.c_double), ("reserved", ctypes.c_int * 4)]
+
+
+def conductors_from_ini(path: str):
+    """The [Grids] section as epic_conductor records (src/main.cpp:284-327)."""
+    n = ctypes.c_int()
+    _check(lib().epic_conductors_from_ini(path.encode(), None, 0, ctypes.byref(n)))
+    out = (Conductor * max(n.value, 1))()
+    _check(lib().epic_conductors_from_ini(path.encode(), out, n.value, ctypes.byref(n)))
+    return list(out)[:n.value]
+
+
 _lib = None
 
 
@@ -98,6 +115,8 @@ def lib() -> ctypes.CDLL:
         "epic_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
         "epic_handle_collisions": ([vp, i, i, vp, i, ctypes.POINTER(ctypes.c_int64)], st),
         "epic_step": ([vp, i], st),
+        "epic_conductors_from_ini": ([ctypes.c_char_p, vp, i, ctypes.POINTER(ctypes.c_int)], st),
+        "epic_add_conductor": ([vp, vp], st),
         "epic_step_host": ([vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
                            st),
         "epic_initial_field": ([vp], st),
@@ -183,6 +202,7 @@ class Simulation:
 
     @classmethod
     def from_ini(cls, path: str, **overrides):
+        """Config, species and the [Grids] conductors of an input.ini."""
         cfg, descs, _ = config_from_ini(path)
         for k, v in overrides.items():
             if k == "capacity":
@@ -190,7 +210,13 @@ class Simulation:
                     d.capacity = int(v)
             else:
                 setattr(cfg, k, v)
-        return cls(cfg, descs)
+        sim = cls(cfg, descs)
+        for c in conductors_from_ini(path):
+            sim.add_conductor(c)
+        return sim
+
+    def add_conductor(self, c: Conductor):
+        _check(lib().epic_add_conductor(self._h, ctypes.byref(c)))
 
     def close(self):
         if self._h:

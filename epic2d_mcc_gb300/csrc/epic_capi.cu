@@ -291,6 +291,10 @@ epic_status do_solve(epic_sim* s) {
     return EPIC_OK;
   }
   if (s->cfg.solver == EPIC_SOLVER_GS) {
+    if (!s->conductors.empty()) {  // Grid::initialize inside gssolver (src/field.cpp:100-103)
+      launch_conductor_rho(s->stream, s->rho, s->d_cond_nodes, s->d_cond_vals, s->cond_nnodes, s->d_cond_live);
+      s->launches += 1;
+    }
     if (s->cfg.sor_mode == EPIC_SOR_LEXICOGRAPHIC) launch_sor_lex(s->stream, a);
     else launch_sor_redblack(s->stream, a, solver_blocks(s, 1024));
   } else {
@@ -320,11 +324,16 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle) {
   double qmK = qm * K;
   double cc = (c.vel_norm) / (c.L * c.W);
   double dtsub = c.DT * sub_cycle;
-  if (c.bc == EPIC_OPEN) {
+  const bool cond = !s->conductors.empty();
+  if (c.bc == EPIC_OPEN || cond) {
     CK(cudaMemsetAsync(s->tile_ctr, 0, sizeof(unsigned int), s->stream));
     CK(cudaMemsetAsync(s->tile_status, 0, s->tile_status_len * sizeof(unsigned long long), s->stream));
   }
-  if (s->mixed)
+  if (cond && !s->mixed) {
+    const CondSet cs{s->cond_nrect, s->cond_ncirc, s->d_cond_rect, s->d_cond_circ, s->d_cond_live};
+    launch_push_conductors(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, qmK, cc, dtsub, cs, s->d_flags,
+                           s->tile_status, s->tile_ctr, s->part_grid);
+  } else if (s->mixed)
     launch_push_mixed(s->stream, s->g, c.shape, c.bc, sp.mx, sp.d_n, s->ef32, (float)(qmK * dtsub),
                       (float)(cc * dtsub / c.dx), (float)(cc * dtsub / c.dy), s->d_flags, s->tile_status,
                       s->tile_ctr, s->part_grid);
@@ -477,6 +486,58 @@ epic_status epic_config_from_ini(const char* path, epic_config* cfg, epic_specie
   return EPIC_OK;
 }
 
+epic_status epic_conductors_from_ini(const char* path, epic_conductor* out, int max, int* count) {
+  if (!path || !count || (max > 0 && !out)) return fail(EPIC_ERR_INVALID, "bad argument");
+  std::vector<epic_conductor> v;
+  std::string err;
+  int st = conductors_from_ini(path, v, err);
+  if (st) return fail((epic_status)st, "%s", err.c_str());
+  *count = (int)v.size();
+  for (int k = 0; k < (int)v.size() && k < max; k++) out[k] = v[k];
+  return EPIC_OK;
+}
+
+epic_status epic_add_conductor(epic_sim* s, const epic_conductor* c) {
+  if (!s || !c) return fail(EPIC_ERR_INVALID, "bad argument");
+  if (s->mixed) return fail(EPIC_ERR_INVALID, "conductors are supported in the FP64 form");
+  if (c->type != EPIC_CONDUCTOR_RECT && c->type != EPIC_CONDUCTOR_CIRCULAR)
+    return fail(EPIC_ERR_INVALID, "unknown conductor type %d", c->type);
+  if (c->type == EPIC_CONDUCTOR_CIRCULAR && (c->electrode_number < 1 || c->electrode_number > 4096))
+    return fail(EPIC_ERR_INVALID, "electrode_number must be in [1, 4096]");
+  s->conductors.push_back(*c);
+  std::vector<double> rects, circles, vals;
+  std::vector<int> nodes;
+  conductor_geometry(s->cfg, s->conductors, rects, circles, nodes, vals);
+  void* old[] = {s->d_cond_rect, s->d_cond_circ, s->d_cond_nodes, s->d_cond_vals};
+  for (void* p : old)
+    if (p) dfree(s, p);
+  s->d_cond_rect = nullptr;
+  s->d_cond_circ = nullptr;
+  s->d_cond_nodes = nullptr;
+  s->d_cond_vals = nullptr;
+  s->cond_nrect = (int)(rects.size() / 4);
+  s->cond_ncirc = (int)(circles.size() / 4);
+  s->cond_nnodes = (int)nodes.size();
+  auto up = [&](void** dst, const void* src, size_t bytes) -> epic_status {
+    CK(cudaMallocAsync(dst, std::max<size_t>(bytes, 16), s->stream));
+    if (bytes) CK(cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, s->stream));
+    return EPIC_OK;
+  };
+  epic_status st;
+  if ((st = up((void**)&s->d_cond_rect, rects.data(), rects.size() * sizeof(double))) ||
+      (st = up((void**)&s->d_cond_circ, circles.data(), circles.size() * sizeof(double))) ||
+      (st = up((void**)&s->d_cond_nodes, nodes.data(), nodes.size() * sizeof(int))) ||
+      (st = up((void**)&s->d_cond_vals, vals.data(), vals.size() * sizeof(double))))
+    return st;
+  if (!s->d_cond_live) CK(cudaMallocAsync((void**)&s->d_cond_live, sizeof(int), s->stream));
+  CK(cudaMemsetAsync(s->d_cond_live, 0, sizeof(int), s->stream));
+  // A captured step holds the old geometry.
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
+  s->graph_exec = s->graph_exec_sort = nullptr;
+  return sync(s);  // the host vectors go out of scope
+}
+
 epic_status epic_ini_get(const char* path, const char* section, const char* key, char* out, int len) {
   if (!path || !section || !key || !out || len < 1) return fail(EPIC_ERR_INVALID, "bad argument");
   std::string v, err;
@@ -591,7 +652,7 @@ void epic_destroy(epic_sim* s) {
   void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->partials, s->bar,
                   s->d_info, s->d_iter_total, s->tile_ctr, s->d_ncoll, s->d_step, s->sum_partials, s->d_sums, s->d_flags,
                   s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion,
-                  s->cs.bin_cut};
+                  s->cs.bin_cut, s->d_cond_rect, s->d_cond_circ, s->d_cond_nodes, s->d_cond_vals, s->d_cond_live};
   for (void* p : ptrs)
     if (p) dfree(s, p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -712,7 +773,7 @@ epic_status epic_load_particles(epic_sim* s, uint32_t seed) {
   for (auto& sp : s->sp) d.push_back(&sp.desc);
   std::vector<std::vector<double>> parts;
   std::string err;
-  int st = load_particles(s->cfg, d, parts, seed, err);
+  int st = load_particles(s->cfg, d, parts, seed, err, s->conductors);
   if (st) return fail((epic_status)st, "%s", err.c_str());
   for (size_t i = 0; i < parts.size(); i++) {
     epic_status e = epic_set_particles(s, (int)i, parts[i].data(), (int64_t)(parts[i].size() / 5));
@@ -929,7 +990,7 @@ epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* part
                   s->sp[k].name.c_str());
   }
   const epic_config& c = s->cfg;
-  bool direct = !s->mixed && c.bc != EPIC_OPEN && c.deposit_mode == EPIC_DEPOSIT_FIXED &&
+  bool direct = !s->mixed && c.bc != EPIC_OPEN && c.deposit_mode == EPIC_DEPOSIT_FIXED && s->conductors.empty() &&
                 !(c.sort_every > 0 && s->step_index % c.sort_every == 0);
   for (int k = 0; k < nsp && direct; k++) {
     cudaPointerAttributes at;
@@ -1108,6 +1169,8 @@ epic_status epic_poll(epic_sim* s, int* done) {
 
 epic_status epic_load_particles_device(epic_sim* s, uint64_t seed) {
   if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  if (!s->conductors.empty())
+    return fail(EPIC_ERR_INVALID, "the device loader does not place particles around conductors (epic_load_particles does)");
   for (int i = 0; i < (int)s->sp.size(); i++) {
     epic_species_state& sp = s->sp[i];
     const long long n = sp.desc.numparticle;

@@ -295,8 +295,108 @@ int parse_load_type(const std::string& load, int* kind, int* narg, std::string& 
   return EPIC_OK;
 }
 
+bool in_rect_conductor(const std::vector<epic_conductor>& cond, double x, double y) {
+  for (const epic_conductor& g : cond)
+    if (g.type == EPIC_CONDUCTOR_RECT && x >= g.min_x && x <= g.max_x && y >= g.min_y && y <= g.max_y) return true;
+  return false;
+}
+
+int conductors_from_ini(const char* path, std::vector<epic_conductor>& out, std::string& err) {
+  Ini ini;
+  if (!parse_ini(path, ini, err)) return EPIC_ERR_IO;
+  out.clear();
+  auto gs = ini.find("Grids");
+  if (gs == ini.end()) return EPIC_OK;
+  const Section& g = gs->second;
+  try {
+    auto get = [&](const std::string& k) -> const std::string& {
+      auto it = g.find(k);
+      if (it == g.end()) throw std::runtime_error("missing key " + k + " in [Grids]");
+      return it->second;
+    };
+    const int count = g.count("grid_count") ? std::stoi(get("grid_count")) : 0;
+    const double vscale = QE_H / (K_B_H * (QE_H / K_B_H));  // Const::eV / (K_b * EV_to_K)
+    for (int i = 0; i < count; i++) {
+      const std::string pre = "grid_" + std::to_string(i) + ".";
+      const std::string type = get(pre + "type");
+      epic_conductor c;
+      std::memset(&c, 0, sizeof c);
+      if (type == "circular") {
+        c.type = EPIC_CONDUCTOR_CIRCULAR;
+        c.x_center = std::stoi(get(pre + "x_center"));
+        c.y_center = std::stoi(get(pre + "y_center"));
+        c.electrode_number = std::stoi(get(pre + "electrode_number"));
+        c.grid_radius = std::stod(get(pre + "grid_radius"));
+        c.electrode_radius = std::stod(get(pre + "electrod_radius"));
+        c.voltage = vscale * std::stod(get(pre + "electrode_voltage"));
+      } else if (type == "reactconduct") {
+        c.type = EPIC_CONDUCTOR_RECT;
+        c.min_x = std::stoi(get(pre + "min_x"));
+        c.min_y = std::stoi(get(pre + "min_y"));
+        c.max_x = std::stoi(get(pre + "max_x"));
+        c.max_y = std::stoi(get(pre + "max_y"));
+        c.voltage = vscale * std::stod(get(pre + "grid_voltage"));
+      } else {
+        continue;  // src/main.cpp:303-325 ignores other types
+      }
+      out.push_back(c);
+    }
+  } catch (const std::exception& e) {
+    err = e.what();
+    return EPIC_ERR_INVALID;
+  }
+  return EPIC_OK;
+}
+
+void conductor_geometry(const epic_config& c, const std::vector<epic_conductor>& cond, std::vector<double>& rects,
+                        std::vector<double>& circles, std::vector<int>& nodes, std::vector<double>& vals) {
+  rects.clear();
+  circles.clear();
+  std::map<int, double> over;  // node -> value; later conductors overwrite
+  std::vector<int> order;
+  auto set = [&](int i, int j, double v) {
+    if (i < 0 || i >= c.nx || j < 0 || j >= c.ny) return;
+    const int k = i * c.ny + j;
+    if (!over.count(k)) order.push_back(k);
+    over[k] = v;
+  };
+  const double PI_M = 3.14159265358979323846;  // M_PI (src/grid.cpp, src/electrode.cpp)
+  for (const epic_conductor& g : cond) {
+    if (g.type == EPIC_CONDUCTOR_RECT) {
+      rects.insert(rects.end(), {(double)g.min_x, (double)g.max_x, (double)g.min_y, (double)g.max_y});
+      // ReactConductorGrid::initialize: the border of the node rectangle
+      const int min_i = (int)((g.min_x - c.x0) / c.dx), max_i = (int)((g.max_x - c.x0) / c.dx);
+      const int min_j = (int)((g.min_y - c.y0) / c.dy), max_j = (int)((g.max_y - c.y0) / c.dy);
+      for (int i = min_i; i <= max_i; i++)
+        for (int j = min_j; j <= max_j; j++)
+          if (i == min_i || i == max_i || j == min_j || j == max_j) set(i, j, g.voltage);
+    } else {
+      for (int k = 0; k < g.electrode_number; k++) {
+        const double theta = k * (2.0 * PI_M / g.electrode_number);
+        const double ex = g.x_center + g.grid_radius * cos(theta);
+        const double ey = g.y_center + g.grid_radius * sin(theta);
+        const double r = g.electrode_radius;
+        circles.insert(circles.end(), {ex, ey, r * r, 0.0});
+        // Electrode::Electrode: 100 points of the circle, rounded to nodes
+        const int N = 100;
+        for (int q = 0; q < N; q++) {
+          const double t = 2.0 * q * PI_M / N;
+          set((int)(ex + r * cos(t) + 0.5), (int)(ey + r * sin(t) + 0.5), g.voltage);
+        }
+      }
+    }
+  }
+  nodes.clear();
+  vals.clear();
+  for (int k : order) {
+    nodes.push_back(k);
+    vals.push_back(over[k]);
+  }
+}
+
 int load_particles(const epic_config& c, const std::vector<const epic_species_desc*>& sp,
-                   std::vector<std::vector<double>>& out, uint32_t seed, std::string& err) {
+                   std::vector<std::vector<double>>& out, uint32_t seed, std::string& err,
+                   const std::vector<epic_conductor>& cond) {
   Rnd rnd(seed);
   const double Lx = (c.nx - 1) * c.dx, Ly = (c.ny - 1) * c.dy;
   out.resize(sp.size());
@@ -309,6 +409,7 @@ int load_particles(const epic_config& c, const std::vector<const epic_species_de
     o.resize((size_t)n * 5);
     for (long p = 0; p < n; p++) {
       double x = 0, y = 0;
+      for (;;) {  // src/init.cpp:71-86: positions inside a conductor are drawn again
       if (kind == 0) {
         x = c.x0 + Lx * rnd();
         y = c.y0 + Ly * rnd();
@@ -324,6 +425,12 @@ int load_particles(const epic_config& c, const std::vector<const epic_species_de
         double ky = 2 * PI_H * narg / Ly;
         if (kind == 2) { x += sin(kx * x); y += sin(ky * y); }
         else { x += cos(kx * x); y += cos(ky * y); }
+      }
+      if (!in_rect_conductor(cond, x, y)) break;
+      if (kind != 0) {
+        err = "load type " + std::string(d.load) + " places a particle inside a conductor (the reference loops forever)";
+        return EPIC_ERR_INVALID;
+      }
       }
       double vx = sample_vel(rnd, d.mass, d.temp) + d.vsx * c.vel_norm;
       double vy = sample_vel(rnd, d.mass, d.temp) + d.vsy * c.vel_norm;

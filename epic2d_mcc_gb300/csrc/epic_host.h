@@ -21,7 +21,17 @@ int config_from_ini(const char* path, epic_config* cfg, epic_species_desc* sp, i
                     std::string& err);
 int ini_get(const char* path, const char* section, const char* key, std::string& value, std::string& err);
 int load_particles(const epic_config& c, const std::vector<const epic_species_desc*>& sp,
-                   std::vector<std::vector<double>>& out, uint32_t seed, std::string& err);
+                   std::vector<std::vector<double>>& out, uint32_t seed, std::string& err,
+                   const std::vector<epic_conductor>& cond = {});
+int conductors_from_ini(const char* path, std::vector<epic_conductor>& out, std::string& err);
+// Conductor geometry for the device: rectangles {min_x, max_x, min_y, max_y},
+// electrodes {x0, y0, r*r, 0} (CircularGrid::initialize, src/grid.cpp:46-57),
+// and the rho override as unique (node, value) pairs, later conductors
+// winning (Grid::initialize in order, src/grid.cpp:67-85, src/electrode.cpp:4-17).
+void conductor_geometry(const epic_config& c, const std::vector<epic_conductor>& cond, std::vector<double>& rects,
+                        std::vector<double>& circles, std::vector<int>& nodes, std::vector<double>& vals);
+// Grid::IsGrid of the rectangles only (Init runs before any CircularGrid has electrodes).
+bool in_rect_conductor(const std::vector<epic_conductor>& cond, double x, double y);
 // INIParser::loadtypeextract (src/iniparser.cpp): "random" -> 0, "uniform" -> 1,
 // "sin(n)" -> 2, "cos(n)" -> 3 with *narg = n; EPIC_ERR_INVALID otherwise.
 int parse_load_type(const std::string& load, int* kind, int* narg, std::string& err);

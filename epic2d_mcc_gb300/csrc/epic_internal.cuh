@@ -59,6 +59,18 @@ struct SoA {
   double *x, *y, *vx, *vy, *vz;
 };
 
+// Conductors on the device (the reference's Grid objects, src/grid.cpp,
+// src/electrode.cpp): ReactConductorGrid rectangles {min_x, max_x, min_y,
+// max_y} and the electrodes of every CircularGrid {x0, y0, r*r, -}.  A circular
+// grid's electrodes exist only once gssolver has run CircularGrid::initialize,
+// so circles count while *live != 0 (set by the first SOR solve's override).
+struct CondSet {
+  int nrect, ncirc;
+  const double4* rect;
+  const double4* circ;
+  const int* live;
+};
+
 // Mixed-precision particle record (24 bytes): the grid node at the lower-left
 // corner of the particle's cell (i*ny + j, so the deposit needs no index
 // arithmetic), the FP32 offset inside the cell in units of dx/dy, in [0, 1),
@@ -119,6 +131,14 @@ void launch_push_download(cudaStream_t st, const Geom& g, int shape, int bc, con
                           const double2* ef, double qmK, double c, double dtsub, double* host, int* flags, int grid);
 void launch_download(cudaStream_t st, const SoA& p, const long long* d_n, long long from, long long cap, double* host,
                      int* flags, int grid);
+// The conductors' rho override before an SOR solve (Grid::initialize inside
+// gssolver, src/field.cpp:100-103): rho[nodes[k]] = vals[k], then *live = 1.
+void launch_conductor_rho(cudaStream_t st, double* rho, const int* nodes, const double* vals, int n, int* live);
+// The FP64 push erasing particles that end inside a conductor (order kept,
+// src/species.cpp:80-97, 108-121, 150-165); needs the compaction scratch.
+void launch_push_conductors(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
+                            const double2* ef, double qmK, double c, double dtsub, const CondSet& cs, int* flags,
+                            unsigned long long* tile_status, unsigned int* tile_ctr, int grid);
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
                  const double2* ef, double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
                  unsigned int* tile_ctr, int grid);
@@ -314,6 +334,14 @@ struct epic_sim {
   double* d_sums;
   double* h_sums;  // pinned
   int* d_flags;
+  // Conductors (epic_add_conductor): host list, device geometry, rho override
+  std::vector<epic_conductor> conductors;
+  double4* d_cond_rect = nullptr;
+  double4* d_cond_circ = nullptr;
+  int* d_cond_nodes = nullptr;
+  double* d_cond_vals = nullptr;
+  int* d_cond_live = nullptr;
+  int cond_nrect = 0, cond_ncirc = 0, cond_nnodes = 0;
   epic::CrossSections cs;
   int64_t launches;
   cudaGraphExec_t graph_exec;       // one step

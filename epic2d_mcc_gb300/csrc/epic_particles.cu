@@ -222,11 +222,27 @@ __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long
 // survivors written in place at (prefix of earlier tiles) + rank.  A tile's
 // writes land only at or below its own range, in slots earlier tiles have
 // already loaded before publishing their counts, so no second buffer is needed.
-template <int SHAPE, bool UNIT>
+// Grid::IsGrid of any conductor (src/grid.cpp:11-65, src/electrode.cpp:20-26).
+__device__ __forceinline__ bool in_conductor(const CondSet& cs, double x, double y) {
+  for (int k = 0; k < cs.nrect; k++) {
+    const double4 r = cs.rect[k];
+    if (x >= r.x && x <= r.y && y >= r.z && y <= r.w) return true;
+  }
+  if (cs.ncirc && *cs.live) {
+    for (int k = 0; k < cs.ncirc; k++) {
+      const double4 e = cs.circ[k];
+      const double dx = x - e.x, dy = y - e.y;
+      if (dx * dx + dy * dy <= e.z) return true;
+    }
+  }
+  return false;
+}
+
+template <int SHAPE, int BC, bool UNIT, bool COND>
 __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, long long* d_n,
                                                                const double2* __restrict__ ef, double qmK, double c,
                                                                double dtsub, unsigned long long* status,
-                                                               unsigned int* tile_ctr, int* flags) {
+                                                               unsigned int* tile_ctr, int* flags, CondSet cs) {
   constexpr int ITEMS = SCAN_TILE / PART_THREADS;
   __shared__ int sm[40];
   __shared__ unsigned long long s_prefix;
@@ -248,7 +264,10 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, lo
       keep[k] = 0;
       if (q < n) {
         x[k] = p.x[q]; y[k] = p.y[q]; vx[k] = p.vx[q]; vy[k] = p.vy[q]; vz[k] = p.vz[q];
-        keep[k] = push_one<SHAPE, EPIC_OPEN, UNIT>(g, ef, qmK, c, dtsub, x[k], y[k], vx[k], vy[k], bad) ? 1 : 0;
+        keep[k] = push_one<SHAPE, BC, UNIT>(g, ef, qmK, c, dtsub, x[k], y[k], vx[k], vy[k], bad) &&
+                          !(COND && in_conductor(cs, x[k], y[k]))
+                      ? 1
+                      : 0;
       }
     }
     int rank[ITEMS];
@@ -281,8 +300,9 @@ void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p
                  double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
                  unsigned int* tile_ctr, int grid) {
 #define PUSH(SH, B, U) k_push<SH, B, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags)
-#define COMPACT(SH, U) \
-  k_push_compact<SH, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, tile_ctr, flags)
+#define COMPACT(SH, U)                                                                                       \
+  k_push_compact<SH, EPIC_OPEN, U, false><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, \
+                                                                         tile_ctr, flags, CondSet{})
 #define BOTH(M, ...) \
   do { if (u) M(__VA_ARGS__, true); else M(__VA_ARGS__, false); } while (0)
   const bool u = unit_cell(g);
@@ -299,6 +319,34 @@ void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p
 #undef BOTH
 #undef COMPACT
 #undef PUSH
+}
+
+void launch_push_conductors(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
+                            const double2* ef, double qmK, double c, double dtsub, const CondSet& cs, int* flags,
+                            unsigned long long* tile_status, unsigned int* tile_ctr, int grid) {
+#define PC(SH, B, U)                                                                                         \
+  k_push_compact<SH, B, U, true><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, \
+                                                                tile_ctr, flags, cs)
+#define BOTH(SH, B) do { if (u) PC(SH, B, true); else PC(SH, B, false); } while (0)
+#define SHAPES(B) do { if (shape == EPIC_NGP) BOTH(EPIC_NGP, B); else BOTH(EPIC_CIC, B); } while (0)
+  const bool u = unit_cell(g);
+  if (bc == EPIC_OPEN) SHAPES(EPIC_OPEN);
+  else if (bc == EPIC_PBC) SHAPES(EPIC_PBC);
+  else SHAPES(EPIC_REFLECTIVE);
+#undef SHAPES
+#undef BOTH
+#undef PC
+}
+
+__global__ void k_conductor_rho(double* __restrict__ rho, const int* __restrict__ nodes,
+                                const double* __restrict__ vals, int n, int* live) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) rho[nodes[k]] = vals[k];
+  if (k == 0) *live = 1;
+}
+
+void launch_conductor_rho(cudaStream_t st, double* rho, const int* nodes, const double* vals, int n, int* live) {
+  k_conductor_rho<<<(n + 255) / 256 > 0 ? (n + 255) / 256 : 1, 256, 0, st>>>(rho, nodes, vals, n, live);
 }
 
 // Species::Rewind_species (src/species.cpp:229-246): v -= (0.5*qm*K) * E * DT.

@@ -73,6 +73,9 @@ class Domain {
     check(epic_delta_phi(sim_, &d));
     return d;
   }
+  // Create_Grid + grids.push_back (src/grid.cpp:88-103): a ReactConductorGrid
+  // or CircularGrid conductor, before the particles are loaded.
+  void add_conductor(const epic_conductor& c) { check(epic_add_conductor(sim_, &c)); }
   const epic_config& config() const { return cfg_; }
   epic_sim* handle() { return sim_; }
   double error = 0;  // Domain::error: last solver residual

@@ -56,6 +56,15 @@ int main(int argc, char** argv) {
     Domain domain(cfg);
     std::vector<std::unique_ptr<Species>> species;
     for (int s = 0; s < nsp; s++) species.emplace_back(new Species(domain, descs[s]));
+    // [Grids] conductors (src/main.cpp:284-327), before Init as there.
+    std::vector<epic_conductor> conds(64);
+    int ncond = 0;
+    check(epic_conductors_from_ini(ini.c_str(), conds.data(), (int)conds.size(), &ncond));
+    if (ncond > (int)conds.size()) {
+      conds.resize((size_t)ncond);
+      check(epic_conductors_from_ini(ini.c_str(), conds.data(), ncond, &ncond));
+    }
+    for (int k = 0; k < ncond; k++) domain.add_conductor(conds[(size_t)k]);
     FieldSolve fieldsolver(domain);
     CollisionHandler coll(domain);
     check(epic_load_particles(domain.handle(), 0));  // Init, global Rnd seeded with 0

@@ -230,6 +230,28 @@ epic_status epic_compute_pe(epic_sim* sim, int norm_species, double* pe);
 /* max(phi) - phi(0,0) as printed by Output::diagnostics (src/output.cpp:320-336). */
 epic_status epic_delta_phi(epic_sim* sim, double* delta_phi);
 
+/* Conductors: the reference's Grid objects (include/grid.h, src/grid.cpp,
+ * src/electrode.cpp), read from [Grids] (src/main.cpp:284-327).  A conductor
+ * overwrites rho on its nodes with its voltage before every SOR solve
+ * (Grid::initialize inside gssolver, src/field.cpp:100-103; the PCG solver
+ * does not), particles that end a push inside one are erased in order
+ * (src/species.cpp:80-165), and Init redraws random positions inside one
+ * (src/init.cpp:71-86; a CircularGrid has electrodes only after the first SOR
+ * solve, as in the reference).  FP64 form only. */
+enum { EPIC_CONDUCTOR_RECT = 0, EPIC_CONDUCTOR_CIRCULAR = 1 };
+typedef struct epic_conductor {
+  int type;                                  /* EPIC_CONDUCTOR_* ("reactconduct", "circular") */
+  int min_x, max_x, min_y, max_y;            /* RECT: ReactConductorGrid bounds */
+  int x_center, y_center, electrode_number;  /* CIRCULAR: CircularGrid */
+  double grid_radius, electrode_radius;
+  double voltage;                            /* as the reference stores it: eV/(k_B EV_to_K) x the INI volts */
+  int reserved[4];
+} epic_conductor;
+/* The [Grids] section in order (count = grid_count; at most max written). */
+epic_status epic_conductors_from_ini(const char* path, epic_conductor* out, int max, int* count);
+/* Create_Grid + grids.push_back (src/grid.cpp:88-103, src/main.cpp:312,323); before loading. */
+epic_status epic_add_conductor(epic_sim* sim, const epic_conductor* c);
+
 /* Grid download/upload (which = EPIC_GRID_*, EPIC_GRID_DEN0 + s). */
 epic_status epic_get_grid(epic_sim* sim, int which, double* out);
 epic_status epic_set_grid(epic_sim* sim, int which, const double* in);

@@ -111,3 +111,23 @@ def test_null_handle_is_rejected(E):
     L = E.lib()
     assert L.epic_step(None, 0) == 1
     assert b"null" in L.epic_last_error()
+
+
+def test_conductors_from_ini_cpu(tmp_path):
+    """[Grids] as src/main.cpp:284-327 reads it (no GPU needed)."""
+    import epic2d_mcc_gb300 as E
+    from tests import decks
+    g = [dict(type="reactconduct", min_x=0, max_x=22, min_y=30, max_y=31, grid_voltage=100),
+         dict(type="circular", x_center=22, y_center=12, electrode_number=6, grid_radius=5, electrod_radius=1.5,
+              electrode_voltage=-5),
+         dict(type="unknown_kind")]
+    ini = decks.write(decks.deck(nx=32, ny=24, grids=g), str(tmp_path))
+    cs = E.conductors_from_ini(ini)
+    assert [c.type for c in cs] == [0, 1]  # other types are ignored, as in the reference
+    assert (cs[0].min_x, cs[0].max_x, cs[0].min_y, cs[0].max_y) == (0, 22, 30, 31)
+    assert (cs[1].x_center, cs[1].y_center, cs[1].electrode_number) == (22, 12, 6)
+    assert (cs[1].grid_radius, cs[1].electrode_radius) == (5.0, 1.5)
+    # voltages scaled as the reference does: eV / (k_B * EV_to_K) * V
+    from oracle import oracle as O
+    s = O.setup(ini)
+    assert cs[0].voltage == s.grids[0][7] and cs[1].voltage == s.grids[1][7]
