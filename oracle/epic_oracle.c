@@ -186,6 +186,60 @@ int or_load_c(const or_domain* d, or_rng* r, const char* type, int n_arg, double
   return 0;
 }
 
+/* --------------------------------------------------------- emitters --- */
+/* Emitter::inject (src/emitter.cpp:5-36) of one emitter em = {x0, y0, x1, y1,
+ * temp, numparticle, vdx, vdy, species_idx1, species_idx2}.  The reference
+ * draws positions from a generator seeded by std::random_device
+ * (Domain::unirand, src/domain.cpp:288-299), so they come in as pos_u (two
+ * uniforms per point, used as std::uniform_real_distribution does:
+ * u (b - a) + a); velocities are Init::SampleVel (src/init.cpp:110-114) on the
+ * global stream r, or on vel_u when given (6 uniforms per particle, stride 12
+ * per point).  Appends to out1 (and out2 when the indices differ); returns -1
+ * when a species runs out of capacity. */
+static double sample_vel_t(or_rng* r, const double** vu, double mass, double temp) {
+  double v_th = sqrt(2 * OR_K_B * temp * (OR_QE / OR_K_B) / mass);
+  double u1, u2, u3;
+  if (*vu) {
+    u1 = (*vu)[0]; u2 = (*vu)[1]; u3 = (*vu)[2];
+    *vu += 3;
+  } else {
+    u1 = or_rng_uniform(r); u2 = or_rng_uniform(r); u3 = or_rng_uniform(r);
+  }
+  return v_th * sqrt(2) * (u1 + u2 + u3 - 1.5);
+}
+
+int or_inject(const or_domain* d, const double* em, double mass1, double mass2, or_rng* r, const double* pos_u,
+              const double* vel_u, double* out1, long* n1, long cap1, double* out2, long* n2, long cap2) {
+  const int num = (int)em[5];
+  const int two = (int)em[8] != (int)em[9];
+  for (int p = 0; p < num; p++) {
+    double x = pos_u[2 * p] * (em[2] - em[0]) + em[0];
+    double y = pos_u[2 * p + 1] * (em[3] - em[1]) + em[1];
+    const double* vu = vel_u ? vel_u + 12 * (long)p : 0;
+    double vx1 = sample_vel_t(r, &vu, mass1, em[4]) + em[6] * d->vel_norm;
+    double vy1 = sample_vel_t(r, &vu, mass1, em[4]) + em[7] * d->vel_norm;
+    double vz1 = 0.0;
+    vx1 /= d->vel_norm;
+    vy1 /= d->vel_norm;
+    vz1 /= d->vel_norm;
+    if (*n1 >= cap1) return -1;
+    double* q = out1 + 5 * (*n1)++;
+    q[0] = x; q[1] = y; q[2] = vx1; q[3] = vy1; q[4] = vz1;
+    if (two) {
+      double vx2 = sample_vel_t(r, &vu, mass2, em[4]) + em[6] * d->vel_norm;
+      double vy2 = sample_vel_t(r, &vu, mass2, em[4]) + em[7] * d->vel_norm;
+      double vz2 = 0.0;
+      vx2 /= d->vel_norm;
+      vy2 /= d->vel_norm;
+      vz2 /= d->vel_norm;
+      if (*n2 >= cap2) return -1;
+      q = out2 + 5 * (*n2)++;
+      q[0] = x; q[1] = y; q[2] = vx2; q[3] = vy2; q[4] = vz2;
+    }
+  }
+  return 0;
+}
+
 /* ----------------------------------------------------------- deposit --- */
 /* Species::ScatterSpecies_serial (src/species.cpp:172-226) with
  * Domain::Scatter (src/domain.cpp:205-228) and XtoL/YtoL (:257-264). */

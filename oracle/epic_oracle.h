@@ -86,6 +86,9 @@ int or_pcg_solve(const or_domain* d, const double* rho, double* phi, double* err
 void or_efield(const or_domain* d, const double* phi, double* efx, double* efy);
 /* Species::Push_species_serial (src/species.cpp:29-170), no conductors.
  * Returns the new particle count (open boundaries erase, order kept). */
+/* Emitter::inject of one emitter (see epic_oracle.c). */
+int or_inject(const or_domain* d, const double* em, double mass1, double mass2, or_rng* r, const double* pos_u,
+              const double* vel_u, double* out1, long* n1, long cap1, double* out2, long* n2, long cap2);
 /* Conductors (grids of OR_GRID_WORDS doubles, see epic_oracle.c). */
 int or_in_conductors(const double* grids, int ng, int circles_live, double x, double y);
 void or_conductor_rho(const or_domain* d, const double* grids, int ng, double* rho);

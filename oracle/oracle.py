@@ -145,6 +145,8 @@ class Setup:
     # [Grids] (src/main.cpp:284-327) as rows of 8 doubles: {0, min_x, max_x, min_y, max_y, 0, 0, V}
     # (reactconduct) or {1, x_center, y_center, electrode_number, grid_radius, electrod_radius, 0, V}
     grids: np.ndarray = field(default_factory=lambda: np.zeros((0, 8)))
+    # [Emitters] (src/main.cpp:330-355) as rows {x0, y0, x1, y1, temp, numparticle, vdx, vdy, idx1, idx2}
+    emitters: np.ndarray = field(default_factory=lambda: np.zeros((0, 10)))
 
 
 def setup(path: str) -> Setup:
@@ -231,7 +233,19 @@ def setup(path: str) -> Setup:
                  elastic=string_to_bool(col["elastic"]), excitation=string_to_bool(col["excitation"]),
                  ionization=string_to_bool(col["ionization"]), num_ts=num_ts, ionfixed=_stoi(sim["ionfixed"]),
                  normscheme=norm_scheme, species=species, sor_omega=_stod(solver.get("sor_omega", "1.4")),
-                 grids=conductors(ini))
+                 grids=conductors(ini), emitters=emitters(ini))
+
+
+def emitters(ini) -> np.ndarray:
+    """The [Emitters] section as src/main.cpp:330-355 reads it."""
+    e = ini.get("Emitters", {})
+    rows = []
+    for i in range(_stoi(e.get("count", "0"))):
+        pre = "emitter_%d." % i
+        rows.append([_stod(e[pre + "x0"]), _stod(e[pre + "y0"]), _stod(e[pre + "x1"]), _stod(e[pre + "y1"]),
+                     _stod(e[pre + "temp"]), _stoi(e[pre + "numparticle"]), _stod(e[pre + "vdx"]),
+                     _stod(e[pre + "vdy"]), _stoi(e[pre + "species_idx1"]), _stoi(e[pre + "species_idx2"])])
+    return np.array(rows, dtype=np.float64).reshape(-1, 10)
 
 
 def conductors(ini) -> np.ndarray:
@@ -316,6 +330,8 @@ def restatement_lib():
         L.or_conductor_rho.argtypes = [vp, vp, i, vp]
         L.or_in_conductors.argtypes = [vp, i, i, d, d]
         L.or_in_conductors.restype = i
+        L.or_inject.argtypes = [vp, vp, d, d, vp, vp, vp, vp, vp, l, vp, vp, l]
+        L.or_inject.restype = i
         L.or_scatter.argtypes = [vp, vp, l, d, vp]
         L.or_scatter.restype = l
         L.or_compute_rho.argtypes = [vp, i, vp, vp, vp]
@@ -374,6 +390,31 @@ class Restatement:
         if rc != 0:
             raise ValueError("unsupported load type %r" % sp.load)
         return out
+
+    def inject(self, em, parts, rng, pos_u, vel_u=None):
+        """Emitter::inject of one emitter row (src/emitter.cpp:5-36) appending to parts[idx1] (and
+        parts[idx2]); pos_u: 2 uniforms per point; vel_u: 12 per point, else the stream rng."""
+        i1, i2 = int(em[8]), int(em[9])
+        num = int(em[5])
+        sp = self.s.species
+        out1 = np.zeros((len(parts[i1]) + num, 5))
+        out1[:len(parts[i1])] = parts[i1]
+        n1 = ctypes.c_long(len(parts[i1]))
+        out2 = np.zeros((len(parts[i2]) + num, 5))
+        out2[:len(parts[i2])] = parts[i2]
+        n2 = ctypes.c_long(len(parts[i2]))
+        em = np.ascontiguousarray(em, dtype=np.float64)
+        pos_u = np.ascontiguousarray(pos_u, dtype=np.float64)
+        vu = None if vel_u is None else np.ascontiguousarray(vel_u, dtype=np.float64)
+        rc = self.L.or_inject(ctypes.byref(self.d), _p(em), sp[i1].mass, sp[i2].mass,
+                              None if rng is None else ctypes.byref(rng.s), _p(pos_u), None if vu is None else _p(vu),
+                              _p(out1), ctypes.byref(n1), len(out1), _p(out2), ctypes.byref(n2), len(out2))
+        assert rc == 0
+        parts = list(parts)
+        parts[i1] = out1[:n1.value]
+        if i2 != i1:
+            parts[i2] = out2[:n2.value]
+        return parts
 
     def conductor_rho(self, rho):
         """Grid::initialize of every conductor, as gssolver runs it (src/field.cpp:100-103)."""
@@ -516,6 +557,8 @@ class OracleSim:
         self.error = 0.0
         self.iters = 0
         self.circles_live = False  # circular grids have electrodes after the first gssolver call
+        # positions of emitted particles: the reference seeds their generator from std::random_device
+        self.pos_rng = np.random.default_rng(12345)
         if load:
             self.parts = [self.R.load(self.rng, sp) for sp in self.s.species]
         if initial_field:
@@ -549,7 +592,15 @@ class OracleSim:
         self.parts[0], self.parts[1] = e, i
         return nc, kinds
 
+    def inject(self, pos_u=None, vel_u=None):
+        """Every emitter, in order (src/main.cpp:397-403); pos_u / vel_u: one array per emitter."""
+        for k, em in enumerate(self.s.emitters):
+            pu = pos_u[k] if pos_u is not None else self.pos_rng.random(2 * int(em[5]))
+            self.parts = self.R.inject(em, self.parts, self.rng, pu, None if vel_u is None else vel_u[k])
+
     def step(self, collisions=False, uniforms=None):
+        if len(self.s.emitters):
+            self.inject()
         self.scatter_all()
         self.field()
         self.push_all()
@@ -592,7 +643,7 @@ class Reference:
                              ("ref_momentum", [vp, i, i, vp]), ("ref_reset_rng", [])]:
                 getattr(L, nm).argtypes = args
                 getattr(L, nm).restype = None
-            for nm, args in [("ref_scatter", [vp, i]), ("ref_solve", [vp]), ("ref_push", [vp, i, i]),
+            for nm, args in [("ref_scatter", [vp, i]), ("ref_solve", [vp]), ("ref_push", [vp, i, i]), ("ref_inject", [vp]),
                              ("ref_rewind", [vp, i]), ("ref_collide", [vp]), ("ref_step", [vp, i])]:
                 getattr(L, nm).argtypes = args
                 getattr(L, nm).restype = i
@@ -654,7 +705,7 @@ class Reference:
         self._lib.ref_species_params(self.h, sp, _p(out))
         return out
 
-    _CHECKED = ("scatter", "solve", "push", "rewind", "collide", "step")
+    _CHECKED = ("scatter", "solve", "push", "rewind", "collide", "step", "inject")
 
     def __getattr__(self, name):
         fn = getattr(self.lib(), "ref_" + name)

@@ -17,6 +17,7 @@
 #include "species.h"
 #include "collision.h"
 #include "grid.h"
+#include "emitter.h"
 #include "extrafun.h"
 
 #include <cmath>
@@ -30,6 +31,7 @@ struct RefSim {
   Domain* domain = nullptr;
   std::vector<Species> species;
   std::vector<Grid*> grids;
+  std::vector<Emitter> emitters;
   FieldSolve* fs = nullptr;
   CollisionHandler* coll = nullptr;
   double params[32];
@@ -187,6 +189,26 @@ void* ref_create(const char* ini_path, int load_particles, int initial_field) {
         }
       }
     }
+    // Emitters as src/main.cpp:330-355 reads them.
+    {
+      auto& esec = iniData["Emitters"];
+      const int count = INIParser::getInt(esec, "count");
+      for (int e = 0; e < count; e++) {
+        const std::string pre = "emitter_" + std::to_string(e) + ".";
+        EmitterParams ep;
+        ep.x0 = INIParser::getDouble(esec, pre + "x0");
+        ep.y0 = INIParser::getDouble(esec, pre + "y0");
+        ep.x1 = INIParser::getDouble(esec, pre + "x1");
+        ep.y1 = INIParser::getDouble(esec, pre + "y1");
+        ep.temp = INIParser::getDouble(esec, pre + "temp");
+        ep.numparticle = INIParser::getInt(esec, pre + "numparticle");
+        ep.vdx = INIParser::getDouble(esec, pre + "vdx");
+        ep.vdy = INIParser::getDouble(esec, pre + "vdy");
+        ep.species_idx1 = INIParser::getInt(esec, pre + "species_idx1");
+        ep.species_idx2 = INIParser::getInt(esec, pre + "species_idx2");
+        s->emitters.emplace_back(ep, *d);
+      }
+    }
     if (load_particles) {
       for (Species& sp : s->species) Init init(sp, *d, s->grids);
     }
@@ -324,6 +346,7 @@ int ref_collide(void* h) { GUARD(collide_impl(h)) }
 // One iteration of the loop body of src/main.cpp:405-423 (no emitters).
 static void step_impl(void* h, int with_collisions) {
   RefSim* s = static_cast<RefSim*>(h);
+  for (Emitter& e : s->emitters) e.inject(s->species);  // src/main.cpp:397-403
   for (Species& sp : s->species) sp.ScatterSpecies_serial();
   s->domain->ComputeRho(s->species);
   s->fs->PotentialSolver();
@@ -336,6 +359,11 @@ static void step_impl(void* h, int with_collisions) {
 }
 
 int ref_step(void* h, int with_collisions) { GUARD(step_impl(h, with_collisions)) }
+static void inject_impl(void* h) {
+  RefSim* s = static_cast<RefSim*>(h);
+  for (Emitter& e : s->emitters) e.inject(s->species);
+}
+int ref_inject(void* h) { GUARD(inject_impl(h)) }
 
 void ref_ke(void* h, int sp, int norm_sp, double* out3) {
   RefSim* s = static_cast<RefSim*>(h);

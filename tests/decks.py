@@ -40,7 +40,7 @@ y0       = 0
 {grids}
 
 [Emitters]
-count = 0
+{emitters}
 
 [normalization]
 norm_scheme = {norm}
@@ -79,7 +79,8 @@ BEAM = "beam,9.10938215E-31,{n},{t},-1,{frac},{vx},{vy},random"
 
 def deck(nx=16, ny=16, ne=2000, ni=2000, te=1, ti=0.026, ion_mass="1.6726219e-27", solver="gs", tol="1e-8",
          maxit=20000, bc="pbc", shape="CIC", dt=0.01, norm=1, density="1E13", collisions=False, gas="1e20",
-         ionfixed=0, beam=None, vdrift=(0, 0), solver_extra="", sim_extra="", coll_extra="", num_ts=10, grids=None):
+         ionfixed=0, beam=None, vdrift=(0, 0), solver_extra="", sim_extra="", coll_extra="", num_ts=10, grids=None,
+         emitters=None):
     sp = [ELECTRON.format(n=ne, t=te, vx=vdrift[0], vy=vdrift[1]), ION.format(m=ion_mass, n=ni, t=ti)]
     if beam:
         sp.append(BEAM.format(**beam))
@@ -87,7 +88,8 @@ def deck(nx=16, ny=16, ne=2000, ni=2000, te=1, ti=0.026, ion_mass="1.6726219e-27
     return TEMPLATE.format(num_ts=num_ts, dt=dt, nx=nx, ny=ny, norm=norm, solver=solver, tol=tol, maxit=maxit,
                            shape=shape, density=density, bc=bc, ionfixed=ionfixed, el=flag, ex=flag, io=flag,
                            gas=gas, species="\n".join(sp), solver_extra=solver_extra, sim_extra=sim_extra,
-                           coll_extra=coll_extra, grids=grid_section(grids or []))
+                           coll_extra=coll_extra, grids=grid_section(grids or []),
+                           emitters=emitter_section(emitters or []))
 
 
 def grid_section(grids) -> str:
@@ -107,3 +109,13 @@ def write(text: str, directory: str | None = None) -> str:
     with os.fdopen(fd, "w") as f:
         f.write(text)
     return path
+
+
+def emitter_section(emitters) -> str:
+    """[Emitters] lines in the reference's keys (src/main.cpp:330-355) from dicts of x0, y0, x1, y1,
+    temp, numparticle, vdx, vdy, species_idx1, species_idx2."""
+    lines = ["count = %d" % len(emitters)]
+    for i, e in enumerate(emitters):
+        for k, v in e.items():
+            lines.append("emitter_%d.%s = %s" % (i, k, v))
+    return "\n".join(lines)

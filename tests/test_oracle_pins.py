@@ -156,3 +156,32 @@ def test_setup_matches_reference_live(tmp_path):
         for k, sp in enumerate(s.species):
             rp = ref.species_params(k)
             assert [rp[0], rp[1], rp[2]] == [sp.mass, sp.charge, sp.spwt]
+
+
+EMITTERS = [dict(x0=1, y0=4, x1=1, y1=12, temp=0.5, numparticle=7, vdx=0.5, vdy=0, species_idx1=0, species_idx2=1),
+            dict(x0=5, y0=5, x1=9, y1=9, temp=0.02, numparticle=3, vdx=0, vdy=0.2, species_idx1=1, species_idx2=1)]
+
+
+@needs_ref
+def test_emitters_match_reference_live(tmp_path):
+    """Emitter::inject (src/emitter.cpp:5-36): counts, append order and velocities (the global mt19937
+    stream) bit for bit; positions come from a std::random_device-seeded generator in the reference, so
+    only their range is checked."""
+    ini = decks.write(decks.deck(nx=16, ny=16, ne=500, ni=500, emitters=EMITTERS), str(tmp_path))
+    ref = O.Reference(ini)
+    orc = O.OracleSim(ini)
+    loaded = [len(orc.parts[s]) for s in range(2)]
+    for _ in range(3):
+        n0 = [len(orc.parts[s]) for s in range(2)]
+        ref.inject()
+        orc.inject()
+        for s in range(2):
+            got, want = ref.particles(s), orc.parts[s]
+            assert len(got) == len(want)
+            assert np.array_equal(got[:loaded[s]], want[:loaded[s]])
+            assert np.array_equal(got[:, 2:], want[:, 2:])
+        new_e = ref.particles(0)[n0[0]:]
+        assert np.all(new_e[:, 0] == 1.0) and np.all((new_e[:, 1] >= 4) & (new_e[:, 1] < 12))
+        new_i = ref.particles(1)[n0[1]:]
+        assert len(new_i) == 7 + 3 and np.all(new_i[:7, 0] == 1.0)
+        assert np.all((new_i[7:, :2] >= 5) & (new_i[7:, :2] < 9))
