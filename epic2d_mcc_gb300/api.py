@@ -65,6 +65,23 @@ class Conductor(ctypes.Structure):
                 ("electrode_radius", ctypes.c_double), ("voltage", ctypes.c_double), ("reserved", ctypes.c_int * 4)]
 
 
+class Emitter(ctypes.Structure):
+    """epic_emitter (src/emitter.cpp, include/emitter.h EmitterParams)."""
+    _fields_ = [("x0", ctypes.c_double), ("y0", ctypes.c_double), ("x1", ctypes.c_double), ("y1", ctypes.c_double),
+                ("temp", ctypes.c_double), ("numparticle", ctypes.c_int), ("vdx", ctypes.c_double),
+                ("vdy", ctypes.c_double), ("species_idx1", ctypes.c_int), ("species_idx2", ctypes.c_int),
+                ("reserved", ctypes.c_int * 4)]
+
+
+def emitters_from_ini(path: str):
+    """The [Emitters] section as epic_emitter records (src/main.cpp:330-355)."""
+    n = ctypes.c_int()
+    _check(lib().epic_emitters_from_ini(path.encode(), None, 0, ctypes.byref(n)))
+    out = (Emitter * max(n.value, 1))()
+    _check(lib().epic_emitters_from_ini(path.encode(), out, n.value, ctypes.byref(n)))
+    return list(out)[:n.value]
+
+
 def conductors_from_ini(path: str):
     """The [Grids] section as epic_conductor records (src/main.cpp:284-327)."""
     n = ctypes.c_int()
@@ -117,6 +134,9 @@ def lib() -> ctypes.CDLL:
         "epic_step": ([vp, i], st),
         "epic_conductors_from_ini": ([ctypes.c_char_p, vp, i, ctypes.POINTER(ctypes.c_int)], st),
         "epic_add_conductor": ([vp, vp], st),
+        "epic_emitters_from_ini": ([ctypes.c_char_p, vp, i, ctypes.POINTER(ctypes.c_int)], st),
+        "epic_add_emitter": ([vp, vp], st),
+        "epic_inject": ([vp, vp], st),
         "epic_step_host": ([vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
                            st),
         "epic_initial_field": ([vp], st),
@@ -213,7 +233,17 @@ class Simulation:
         sim = cls(cfg, descs)
         for c in conductors_from_ini(path):
             sim.add_conductor(c)
+        for e in emitters_from_ini(path):
+            sim.add_emitter(e)
         return sim
+
+    def add_emitter(self, e: Emitter):
+        _check(lib().epic_add_emitter(self._h, ctypes.byref(e)))
+
+    def inject(self, uniforms: np.ndarray | None = None):
+        """Emitter::inject of every emitter (epic_inject); uniforms: rows of 14 per emitted point."""
+        u = None if uniforms is None else np.ascontiguousarray(uniforms, dtype=np.float64)
+        _check(lib().epic_inject(self._h, None if u is None else _ptr(u)))
 
     def add_conductor(self, c: Conductor):
         _check(lib().epic_add_conductor(self._h, ctypes.byref(c)))

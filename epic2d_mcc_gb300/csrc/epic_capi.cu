@@ -428,10 +428,49 @@ epic_status do_sort(epic_sim* s, int i) {
   return EPIC_OK;
 }
 
+// Emitter::inject of every emitter (src/emitter.cpp:5-36); d_uniforms: null
+// for Philox, else device rows of 14 per point, emitters in order.
+epic_status do_inject(epic_sim* s, const double* d_uniforms) {
+  const epic_config& c = s->cfg;
+  const double* u = d_uniforms;
+  for (size_t k = 0; k < s->emitters.size(); k++) {
+    const epic_emitter& m = s->emitters[k];
+    const int sp_of[2] = {m.species_idx1, m.species_idx2};
+    const int slots = m.species_idx1 != m.species_idx2 ? 2 : 1;
+    for (int slot = 0; slot < slots; slot++) {
+      epic_species_state& sp = s->sp[sp_of[slot]];
+      EmitDev e;
+      e.x0 = m.x0;
+      e.y0 = m.y0;
+      e.x1 = m.x1;
+      e.y1 = m.y1;
+      e.vth = sqrt(2 * K_B * m.temp * (QE / K_B) / sp.desc.mass);  // Init::SampleVel (src/init.cpp:112)
+      e.vdx = m.vdx * c.vel_norm;
+      e.vdy = m.vdy * c.vel_norm;
+      e.vel_norm = c.vel_norm;
+      e.num = m.numparticle;
+      e.slot = slot;
+      e.emitter = (int)k;
+      launch_emit(s->stream, sp.soa, sp.d_n, sp.cap, e, c.seed, s->d_inj, u, s->d_flags, s->part_grid);
+    }
+    for (int slot = 0; slot < slots; slot++) {
+      epic_species_state& sp = s->sp[sp_of[slot]];
+      launch_emit_commit(s->stream, sp.d_n, m.numparticle, sp.cap, s->d_flags);
+    }
+    s->launches += 2 * slots;
+    if (u) u += (size_t)m.numparticle * 14;
+  }
+  launch_inject_tick(s->stream, s->d_inj);
+  s->launches += 1;
+  CKL();
+  return EPIC_OK;
+}
+
 // sort: -1 by the step counter and cfg.sort_every, 0 never, 1 always.
 epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
   epic_status st;
   const int nsp = (int)s->sp.size();
+  if (!s->emitters.empty() && (st = do_inject(s, nullptr))) return st;  // src/main.cpp:397-403
   if (sort < 0) sort = s->cfg.sort_every > 0 && s->step_index % s->cfg.sort_every == 0;
   s->step_index++;
   if (sort)
@@ -536,6 +575,53 @@ epic_status epic_add_conductor(epic_sim* s, const epic_conductor* c) {
   if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
   s->graph_exec = s->graph_exec_sort = nullptr;
   return sync(s);  // the host vectors go out of scope
+}
+
+epic_status epic_emitters_from_ini(const char* path, epic_emitter* out, int max, int* count) {
+  if (!path || !count || (max > 0 && !out)) return fail(EPIC_ERR_INVALID, "bad argument");
+  std::vector<epic_emitter> v;
+  std::string err;
+  int st = emitters_from_ini(path, v, err);
+  if (st) return fail((epic_status)st, "%s", err.c_str());
+  *count = (int)v.size();
+  for (int k = 0; k < (int)v.size() && k < max; k++) out[k] = v[k];
+  return EPIC_OK;
+}
+
+epic_status epic_add_emitter(epic_sim* s, const epic_emitter* e) {
+  if (!s || !e) return fail(EPIC_ERR_INVALID, "bad argument");
+  if (s->mixed) return fail(EPIC_ERR_INVALID, "emitters are supported in the FP64 form");
+  const int nsp = (int)s->sp.size();
+  if (e->species_idx1 < 0 || e->species_idx1 >= nsp || e->species_idx2 < 0 || e->species_idx2 >= nsp)
+    return fail(EPIC_ERR_INVALID, "emitter species index out of range (add the species first)");
+  if (e->numparticle < 0 || e->numparticle > (1 << 28)) return fail(EPIC_ERR_INVALID, "bad numparticle");
+  if (!s->d_inj) {
+    CK(cudaMallocAsync((void**)&s->d_inj, sizeof(unsigned long long), s->stream));
+    CK(cudaMemsetAsync(s->d_inj, 0, sizeof(unsigned long long), s->stream));
+  }
+  s->emitters.push_back(*e);
+  // A captured step has no injection for it.
+  if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
+  if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
+  s->graph_exec = s->graph_exec_sort = nullptr;
+  return sync(s);
+}
+
+epic_status epic_inject(epic_sim* s, const double* uniforms) {
+  if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  if (s->emitters.empty()) return EPIC_OK;
+  const double* d_u = nullptr;
+  if (uniforms) {
+    size_t rows = 0;
+    for (const epic_emitter& m : s->emitters) rows += (size_t)m.numparticle;
+    epic_status st = ensure_staging(s, std::max<size_t>(1, rows * 14 * sizeof(double)));
+    if (st) return st;
+    CK(cudaMemcpyAsync(s->staging, uniforms, rows * 14 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    d_u = (const double*)s->staging;
+  }
+  epic_status st = do_inject(s, d_u);
+  if (st) return st;
+  return sync(s);
 }
 
 epic_status epic_ini_get(const char* path, const char* section, const char* key, char* out, int len) {
@@ -652,7 +738,8 @@ void epic_destroy(epic_sim* s) {
   void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->partials, s->bar,
                   s->d_info, s->d_iter_total, s->tile_ctr, s->d_ncoll, s->d_step, s->sum_partials, s->d_sums, s->d_flags,
                   s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion,
-                  s->cs.bin_cut, s->d_cond_rect, s->d_cond_circ, s->d_cond_nodes, s->d_cond_vals, s->d_cond_live};
+                  s->cs.bin_cut, s->d_cond_rect, s->d_cond_circ, s->d_cond_nodes, s->d_cond_vals, s->d_cond_live,
+                  s->d_inj};
   for (void* p : ptrs)
     if (p) dfree(s, p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -991,6 +1078,7 @@ epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* part
   }
   const epic_config& c = s->cfg;
   bool direct = !s->mixed && c.bc != EPIC_OPEN && c.deposit_mode == EPIC_DEPOSIT_FIXED && s->conductors.empty() &&
+                s->emitters.empty() &&
                 !(c.sort_every > 0 && s->step_index % c.sort_every == 0);
   for (int k = 0; k < nsp && direct; k++) {
     cudaPointerAttributes at;

@@ -348,6 +348,43 @@ int conductors_from_ini(const char* path, std::vector<epic_conductor>& out, std:
   return EPIC_OK;
 }
 
+int emitters_from_ini(const char* path, std::vector<epic_emitter>& out, std::string& err) {
+  Ini ini;
+  if (!parse_ini(path, ini, err)) return EPIC_ERR_IO;
+  out.clear();
+  auto es = ini.find("Emitters");
+  if (es == ini.end()) return EPIC_OK;
+  const Section& e = es->second;
+  try {
+    auto get = [&](const std::string& k) -> const std::string& {
+      auto it = e.find(k);
+      if (it == e.end()) throw std::runtime_error("missing key " + k + " in [Emitters]");
+      return it->second;
+    };
+    const int count = e.count("count") ? std::stoi(get("count")) : 0;
+    for (int i = 0; i < count; i++) {
+      const std::string pre = "emitter_" + std::to_string(i) + ".";
+      epic_emitter m;
+      std::memset(&m, 0, sizeof m);
+      m.x0 = std::stod(get(pre + "x0"));
+      m.y0 = std::stod(get(pre + "y0"));
+      m.x1 = std::stod(get(pre + "x1"));
+      m.y1 = std::stod(get(pre + "y1"));
+      m.temp = std::stod(get(pre + "temp"));
+      m.numparticle = std::stoi(get(pre + "numparticle"));
+      m.vdx = std::stod(get(pre + "vdx"));
+      m.vdy = std::stod(get(pre + "vdy"));
+      m.species_idx1 = std::stoi(get(pre + "species_idx1"));
+      m.species_idx2 = std::stoi(get(pre + "species_idx2"));
+      out.push_back(m);
+    }
+  } catch (const std::exception& ex) {
+    err = ex.what();
+    return EPIC_ERR_INVALID;
+  }
+  return EPIC_OK;
+}
+
 void conductor_geometry(const epic_config& c, const std::vector<epic_conductor>& cond, std::vector<double>& rects,
                         std::vector<double>& circles, std::vector<int>& nodes, std::vector<double>& vals) {
   rects.clear();

@@ -24,6 +24,7 @@ int load_particles(const epic_config& c, const std::vector<const epic_species_de
                    std::vector<std::vector<double>>& out, uint32_t seed, std::string& err,
                    const std::vector<epic_conductor>& cond = {});
 int conductors_from_ini(const char* path, std::vector<epic_conductor>& out, std::string& err);
+int emitters_from_ini(const char* path, std::vector<epic_emitter>& out, std::string& err);
 // Conductor geometry for the device: rectangles {min_x, max_x, min_y, max_y},
 // electrodes {x0, y0, r*r, 0} (CircularGrid::initialize, src/grid.cpp:46-57),
 // and the rho override as unique (node, value) pairs, later conductors

@@ -139,6 +139,19 @@ void launch_conductor_rho(cudaStream_t st, double* rho, const int* nodes, const 
 void launch_push_conductors(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
                             const double2* ef, double qmK, double c, double dtsub, const CondSet& cs, int* flags,
                             unsigned long long* tile_status, unsigned int* tile_ctr, int grid);
+// Emitter::inject into one species (slot 0: species_idx1, 1: species_idx2):
+// appends num particles at the live count; the count is advanced by
+// launch_emit_commit (so the two slots of one emitter read the same counts).
+struct EmitDev {
+  double x0, y0, x1, y1;
+  double vth, vdx, vdy, vel_norm;  // vth = sqrt(2 k_B T EV_to_K / m); vdx, vdy in m/s
+  int num, slot, emitter;
+};
+void launch_emit(cudaStream_t st, const SoA& p, const long long* d_n, long long cap, const EmitDev& e,
+                 unsigned long long seed, const unsigned long long* d_inj, const double* uniforms, int* flags,
+                 int grid);
+void launch_emit_commit(cudaStream_t st, long long* d_n, long long num, long long cap, int* flags);
+void launch_inject_tick(cudaStream_t st, unsigned long long* d_inj);
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
                  const double2* ef, double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
                  unsigned int* tile_ctr, int grid);
@@ -342,6 +355,9 @@ struct epic_sim {
   double* d_cond_vals = nullptr;
   int* d_cond_live = nullptr;
   int cond_nrect = 0, cond_ncirc = 0, cond_nnodes = 0;
+  // Emitters (epic_add_emitter) and the device count of injections
+  std::vector<epic_emitter> emitters;
+  unsigned long long* d_inj = nullptr;
   epic::CrossSections cs;
   int64_t launches;
   cudaGraphExec_t graph_exec;       // one step

@@ -11,6 +11,8 @@
 // count) that reads the live particle count from device memory.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "epic_internal.cuh"
 #include "epic_device.cuh"
 
@@ -348,6 +350,81 @@ __global__ void k_conductor_rho(double* __restrict__ rho, const int* __restrict_
 void launch_conductor_rho(cudaStream_t st, double* rho, const int* nodes, const double* vals, int n, int* live) {
   k_conductor_rho<<<(n + 255) / 256 > 0 ? (n + 255) / 256 : 1, 256, 0, st>>>(rho, nodes, vals, n, live);
 }
+
+// ------------------------------------------------------------- emitters ---
+// Emitter::inject (src/emitter.cpp:5-36) into one species: point q takes
+// uniforms 0-1 for its position (std::uniform_real_distribution: u (b-a) + a)
+// and 2 + 6*slot .. 7 + 6*slot for its velocity (Init::SampleVel,
+// src/init.cpp:110-114: vth sqrt(2) (u1 + u2 + u3 - 1.5), plus the drift, over
+// vel_norm), from the caller's rows of 14 or from Philox keyed by
+// (q, emitter | 2^31, injection, seed) - distinct from the MCC's keys.
+__global__ void __launch_bounds__(PART_THREADS) k_emit(SoA p, const long long* __restrict__ d_n, long long cap,
+                                                       EmitDev e, unsigned long long seed,
+                                                       const unsigned long long* __restrict__ d_inj,
+                                                       const double* __restrict__ uniforms, int* flags) {
+  const long long n0 = *d_n;
+  const unsigned long long inj = *d_inj;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < e.num; q += gridDim.x * blockDim.x) {
+    double u[8];
+    if (uniforms) {
+      const double* r = uniforms + (long long)q * 14;
+      u[0] = r[0];
+      u[1] = r[1];
+#pragma unroll
+      for (int k = 0; k < 6; k++) u[2 + k] = r[2 + 6 * e.slot + k];
+    } else {
+      Philox src{(uint32_t)q, 0x80000000u | (uint32_t)e.emitter, (uint32_t)inj, (uint32_t)seed,
+                 (uint32_t)(seed >> 32), 0, make_uint4(0, 0, 0, 0)};
+      double all[14];
+#pragma unroll
+      for (int k = 0; k < 14; k++) all[k] = src.next();
+      u[0] = all[0];
+      u[1] = all[1];
+#pragma unroll
+      for (int k = 0; k < 6; k++) u[2 + k] = e.slot ? all[8 + k] : all[2 + k];
+    }
+    const long long o = n0 + q;
+    if (o >= cap) {
+      set_flag(flags, FLAG_CAPACITY);
+      continue;
+    }
+    double vx = e.vth * sqrt(2.0) * (u[2] + u[3] + u[4] - 1.5) + e.vdx;
+    double vy = e.vth * sqrt(2.0) * (u[5] + u[6] + u[7] - 1.5) + e.vdy;
+    double vz = 0.0;
+    vx /= e.vel_norm;
+    vy /= e.vel_norm;
+    vz /= e.vel_norm;
+    p.x[o] = u[0] * (e.x1 - e.x0) + e.x0;
+    p.y[o] = u[1] * (e.y1 - e.y0) + e.y0;
+    p.vx[o] = vx;
+    p.vy[o] = vy;
+    p.vz[o] = vz;
+  }
+}
+
+__global__ void k_emit_commit(long long* d_n, long long num, long long cap, int* flags) {
+  long long n = *d_n + num;
+  if (n > cap) {
+    set_flag(flags, FLAG_CAPACITY);
+    n = cap;
+  }
+  *d_n = n;
+}
+
+__global__ void k_inject_tick(unsigned long long* d_inj) { *d_inj += 1; }
+
+void launch_emit(cudaStream_t st, const SoA& p, const long long* d_n, long long cap, const EmitDev& e,
+                 unsigned long long seed, const unsigned long long* d_inj, const double* uniforms, int* flags,
+                 int grid) {
+  const int blocks = std::max(1, std::min(grid, (e.num + PART_THREADS - 1) / PART_THREADS));
+  k_emit<<<blocks, PART_THREADS, 0, st>>>(p, d_n, cap, e, seed, d_inj, uniforms, flags);
+}
+
+void launch_emit_commit(cudaStream_t st, long long* d_n, long long num, long long cap, int* flags) {
+  k_emit_commit<<<1, 1, 0, st>>>(d_n, num, cap, flags);
+}
+
+void launch_inject_tick(cudaStream_t st, unsigned long long* d_inj) { k_inject_tick<<<1, 1, 0, st>>>(d_inj); }
 
 // Species::Rewind_species (src/species.cpp:229-246): v -= (0.5*qm*K) * E * DT.
 template <int SHAPE, bool UNIT>

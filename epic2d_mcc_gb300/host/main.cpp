@@ -65,6 +65,15 @@ int main(int argc, char** argv) {
       check(epic_conductors_from_ini(ini.c_str(), conds.data(), ncond, &ncond));
     }
     for (int k = 0; k < ncond; k++) domain.add_conductor(conds[(size_t)k]);
+    // [Emitters] (src/main.cpp:330-355); each step injects first (src/main.cpp:397-403).
+    std::vector<epic_emitter> emits(64);
+    int nemit = 0;
+    check(epic_emitters_from_ini(ini.c_str(), emits.data(), (int)emits.size(), &nemit));
+    if (nemit > (int)emits.size()) {
+      emits.resize((size_t)nemit);
+      check(epic_emitters_from_ini(ini.c_str(), emits.data(), nemit, &nemit));
+    }
+    for (int k = 0; k < nemit; k++) check(epic_add_emitter(domain.handle(), &emits[(size_t)k]));
     FieldSolve fieldsolver(domain);
     CollisionHandler coll(domain);
     check(epic_load_particles(domain.handle(), 0));  // Init, global Rnd seeded with 0

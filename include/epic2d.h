@@ -252,6 +252,31 @@ epic_status epic_conductors_from_ini(const char* path, epic_conductor* out, int 
 /* Create_Grid + grids.push_back (src/grid.cpp:88-103, src/main.cpp:312,323); before loading. */
 epic_status epic_add_conductor(epic_sim* sim, const epic_conductor* c);
 
+/* Emitters (include/emitter.h, src/emitter.cpp:5-36), read from [Emitters]
+ * (src/main.cpp:330-355): at the start of every step each emitter appends
+ * numparticle particles to species_idx1 (and the same number to
+ * species_idx2, at the same positions, when the indices differ), positions
+ * uniform on [x0, x1) x [y0, y1), velocities Init::SampleVel(temp) plus the
+ * drift.  The reference draws the positions from a std::random_device-seeded
+ * generator (not reproducible) and the velocities from its global stream;
+ * here both come from a Philox stream keyed by (point, emitter, injection,
+ * seed), or from caller uniforms (epic_inject).  FP64 form only. */
+typedef struct epic_emitter {
+  double x0, y0, x1, y1; /* injection rectangle (a segment when x0 == x1 or y0 == y1) */
+  double temp;           /* eV */
+  int numparticle;       /* particles (pairs) per step */
+  double vdx, vdy;       /* drift in units of vel_norm */
+  int species_idx1, species_idx2;
+  int reserved[4];
+} epic_emitter;
+epic_status epic_emitters_from_ini(const char* path, epic_emitter* out, int max, int* count);
+epic_status epic_add_emitter(epic_sim* sim, const epic_emitter* e);
+/* Emitter::inject of every emitter, in order (what a step does first).
+ * uniforms: null for the Philox stream, or for each emitter in order
+ * numparticle rows of 14 doubles: the x and y uniforms, 6 velocity uniforms
+ * for species_idx1 (vx then vy, three each) and 6 for species_idx2. */
+epic_status epic_inject(epic_sim* sim, const double* uniforms);
+
 /* Grid download/upload (which = EPIC_GRID_*, EPIC_GRID_DEN0 + s). */
 epic_status epic_get_grid(epic_sim* sim, int which, double* out);
 epic_status epic_set_grid(epic_sim* sim, int which, const double* in);

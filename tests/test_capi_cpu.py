@@ -131,3 +131,16 @@ def test_conductors_from_ini_cpu(tmp_path):
     from oracle import oracle as O
     s = O.setup(ini)
     assert cs[0].voltage == s.grids[0][7] and cs[1].voltage == s.grids[1][7]
+
+
+def test_emitters_from_ini_cpu(tmp_path):
+    """[Emitters] as src/main.cpp:330-355 reads it (no GPU needed)."""
+    import epic2d_mcc_gb300 as E
+    from tests import decks
+    em = [dict(x0=1, y0=20, x1=1, y1=30, temp=0, numparticle=5, vdx=0.0, vdy=0.0, species_idx1=0, species_idx2=1)]
+    ini = decks.write(decks.deck(nx=32, ny=32, emitters=em), str(tmp_path))
+    es = E.emitters_from_ini(ini)
+    assert len(es) == 1
+    e = es[0]
+    assert (e.x0, e.y0, e.x1, e.y1, e.temp, e.numparticle) == (1, 20, 1, 30, 0, 5)
+    assert (e.species_idx1, e.species_idx2) == (0, 1)
