@@ -290,7 +290,11 @@ epic_status do_solve(epic_sim* s) {
     CKL();
     return EPIC_OK;
   }
-  if (s->cfg.solver == EPIC_SOLVER_GS) {
+  if (s->cfg.solver == EPIC_SOLVER_GSHYBRID) {
+    launch_gsfluid(s->stream, a, s->rho);
+  } else if (s->cfg.solver == EPIC_SOLVER_HYBRID) {
+    launch_nrpcg(s->stream, a);
+  } else if (s->cfg.solver == EPIC_SOLVER_GS) {
     if (!s->conductors.empty()) {  // Grid::initialize inside gssolver (src/field.cpp:100-103)
       launch_conductor_rho(s->stream, s->rho, s->d_cond_nodes, s->d_cond_vals, s->cond_nnodes, s->d_cond_live);
       s->launches += 1;
@@ -642,7 +646,7 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
     return fail(EPIC_ERR_INVALID, "dx, dy, L, W, vel_norm, LDe and density must be positive");
   if (cfg->shape != EPIC_CIC && cfg->shape != EPIC_NGP) return fail(EPIC_ERR_INVALID, "bad shape");
   if (cfg->bc < EPIC_PBC || cfg->bc > EPIC_REFLECTIVE) return fail(EPIC_ERR_INVALID, "bad bc");
-  if (cfg->solver != EPIC_SOLVER_GS && cfg->solver != EPIC_SOLVER_PCG) return fail(EPIC_ERR_INVALID, "bad solver");
+  if (cfg->solver < EPIC_SOLVER_GS || cfg->solver > EPIC_SOLVER_HYBRID) return fail(EPIC_ERR_INVALID, "bad solver");
   int dev = 0;
   CK(cudaGetDevice(&dev));
   init_field_kernels();

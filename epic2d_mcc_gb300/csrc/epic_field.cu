@@ -126,6 +126,7 @@ __device__ double block_sum_1024(double v, double* sm) {
 }
 
 // Residual of src/field.cpp:121-134 over the interior (one block).
+template <bool FLUID>
 __device__ double sor_residual(const SolverArgs& a, const double* phi, double* red) {
   const int nx = a.g.nx, ny = a.g.ny;
   const double dx2 = a.g.dx * a.g.dx, dy2 = a.g.dy * a.g.dy;
@@ -135,13 +136,16 @@ __device__ double sor_residual(const SolverArgs& a, const double* phi, double* r
     int i = 1 + q / (ny - 2), j = 1 + q % (ny - 2);
     int k = i * ny + j;
     double R = ((phi[k + ny] - 2 * phi[k] + phi[k - ny]) / dx2) + ((phi[k + 1] - 2 * phi[k] + phi[k - 1]) / dy2) +
-               (a.rho[k]) * a.K;
+               (FLUID ? a.rho[k] - exp(phi[k]) : a.rho[k]) * a.K;
     sum += R * R;
   }
   sum = block_sum_1024(sum, red);
   return sqrt(sum / (nx * ny));
 }
 
+// FLUID: gsfluidsolver (src/field.cpp:7-68), Boltzmann electrons: the source
+// is (rho - exp(phi)) K and the residual is checked every 50 sweeps.
+template <bool FLUID>
 __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_smem) {
   extern __shared__ double smem[];
   __shared__ double red[40];
@@ -160,7 +164,8 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_s
   double L2 = 0;
   if (nxi > 0 && nyi > 0) {
     while (iter < a.max_iter) {
-      int S = iter == 0 ? 1 : 25;
+      constexpr int P = FLUID ? 50 : 25;
+      int S = iter == 0 ? 1 : P;
       if (S > a.max_iter - iter) S = a.max_iter - iter;
       const int T = D + 2 * (S - 1);
       for (int t = 0; t < T; t++) {
@@ -176,16 +181,16 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_s
           if (ai > a1) continue;
           int i = ai + 1, j = d - ai + 1;
           int k = i * ny + j;
-          double phi_new = inv_coeff * (a.rho[k] * a.K + ((phi[k + ny] + phi[k - ny]) / dx2) +
-                                        ((phi[k + 1] + phi[k - 1]) / dy2));
+          double phi_new = inv_coeff * ((FLUID ? a.rho[k] - exp(phi[k]) : a.rho[k]) * a.K +
+                                        ((phi[k + ny] + phi[k - ny]) / dx2) + ((phi[k + 1] + phi[k - 1]) / dy2));
           phi[k] = phi[k] + a.omega * (phi_new - phi[k]);
         }
         __syncthreads();
       }
       const int last = iter + S - 1;
       iter += S;
-      if (last % 25 == 0) {
-        L2 = sor_residual(a, phi, red);
+      if (last % P == 0) {
+        L2 = sor_residual<FLUID>(a, phi, red);
         if (L2 < a.tol) {
           converged = 1;
           break;
@@ -208,15 +213,132 @@ constexpr size_t SOR_SMEM_MAX = 200 * 1024;
 void init_field_kernels() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(k_sor_lex, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
   done = true;
 }
 
 void launch_sor_lex(cudaStream_t st, const SolverArgs& a) {
   size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
   int use_smem = bytes <= SOR_SMEM_MAX;
-  k_sor_lex<<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
+  k_sor_lex<false><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
 }
+
+// gsfluidsolver's edge values of rho (src/field.cpp:22-32): bottom 0, top
+// 10000 eV/(k_B EV_to_K), then left and right 0 (so the top corners end 0).
+__global__ void k_gsfluid_edges(Geom g, double* rho, double top) {
+  const int nx = g.nx, ny = g.ny;
+  for (int i = threadIdx.x; i < nx; i += blockDim.x) {
+    rho[i * ny] = 0;
+    rho[i * ny + ny - 1] = top;
+  }
+  __syncthreads();
+  for (int j = threadIdx.x; j < ny; j += blockDim.x) {
+    rho[j] = 0;
+    rho[(nx - 1) * ny + j] = 0;
+  }
+}
+
+void launch_gsfluid(cudaStream_t st, const SolverArgs& a, double* rho) {
+  k_gsfluid_edges<<<1, 256, 0, st>>>(a.g, rho, 10000 * (QE / (K_B * (QE / K_B))));
+  size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
+  int use_smem = bytes <= SOR_SMEM_MAX;
+  k_sor_lex<true><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
+}
+
+// ------------------------------------------------------ Newton hybrid ---
+// FieldSolve::nrpcgsolver (src/field.cpp:141-210): ten Newton steps on
+// A x - rhovec = 0 with rhovec += exp(x) K each step (the reference
+// accumulates it) and J = A - diag(exp(x)), each solved by the dense cg of
+// linearalgebra/solvers.h:33-69 (from 0, |r| < 1e-4, at most min(n, 10000)
+// iterations).  A is pcgsolver's 5-point matrix on the flattened vector (row
+// k / nx, column k % nx); the matrix-vector products sum the five entries in
+// ascending column order, which is the dense product's sum (its zero entries
+// leave it unchanged), and the dot products are summed serially in index
+// order by one thread, as vec::operator* does, so the iterates are the
+// reference's (exp aside: CUDA's and the host library's may differ in the
+// last bit).  One CTA; vectors in the solver workspace.
+__device__ __forceinline__ double nr_row(int nx, int ny, int k, double diag, const double* v) {
+  const int row = k / nx, col = k - row * nx;
+  double sum = 0;
+  if (row > 0) sum += 1.0 * v[k - nx];
+  if (col > 0) sum += 1.0 * v[k - 1];
+  sum += diag * v[k];
+  if (col < nx - 1) sum += 1.0 * v[k + 1];
+  if (row < ny - 1) sum += 1.0 * v[k + nx];
+  return sum;
+}
+
+__device__ double nr_serial_dot(const double* u, const double* v, int n, double* s_out) {
+  if (threadIdx.x == 0) {
+    double r = 0;
+    for (int i = 0; i < n; i++) r += u[i] * v[i];
+    *s_out = r;
+  }
+  __syncthreads();
+  const double r = *s_out;
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
+  __shared__ double s_dot;
+  const int nx = a.g.nx, ny = a.g.ny, n = nx * ny;
+  const double dx2 = a.g.dx * a.g.dx;
+  const double K = a.K;
+  double *rhovec = a.work[0], *x = a.work[1], *F = a.work[2], *J = a.work[3];
+  double *y = a.work[4], *r = a.work[5], *p = a.work[6], *Ap = a.work[7];
+  for (int k = threadIdx.x; k < n; k += blockDim.x) {
+    const int i = k / ny, j = k - i * ny;
+    rhovec[k] = (j == 0 || j == ny - 1 || i == 0 || i == nx - 1) ? 0.0 : -a.rho[k] * dx2 * K;
+    x[k] = 0;
+  }
+  __syncthreads();
+  const int maxit = n < 10000 ? n : 10000;
+  long long total = 0;
+  for (int it = 0; it < 10; it++) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) rhovec[k] = rhovec[k] + exp(x[k]) * K;
+    __syncthreads();
+    for (int k = threadIdx.x; k < n; k += blockDim.x) {
+      F[k] = nr_row(nx, ny, k, -4.0, x) - rhovec[k];
+      J[k] = -4 - exp(x[k]);
+      y[k] = 0;
+      r[k] = F[k] - 0.0;
+      p[k] = r[k];
+    }
+    __syncthreads();
+    double r02 = nr_serial_dot(r, r, n, &s_dot);
+    for (int i = 0; i < maxit; i++) {
+      if (sqrt(r02) < 1e-4) break;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) Ap[k] = nr_row(nx, ny, k, J[k], p);
+      __syncthreads();
+      const double pAp = nr_serial_dot(p, Ap, n, &s_dot);
+      const double alpha = r02 / pAp;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) {
+        y[k] = y[k] + p[k] * alpha;
+        r[k] = r[k] - Ap[k] * alpha;
+      }
+      __syncthreads();
+      const double r12 = nr_serial_dot(r, r, n, &s_dot);
+      const double beta = r12 / r02;
+      for (int k = threadIdx.x; k < n; k += blockDim.x) p[k] = r[k] + p[k] * beta;
+      __syncthreads();
+      r02 = r12;
+      total++;
+    }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) x[k] = x[k] - y[k];
+    __syncthreads();
+  }
+  for (int k = threadIdx.x; k < n; k += blockDim.x) a.phi[k] = x[k];
+  if (threadIdx.x == 0) {
+    a.info->iterations = (int)total;
+    a.info->converged = 1;
+    a.info->error = 0;  // domain.error = 0 (src/field.cpp:205)
+    atomicAdd(a.iter_total, (unsigned long long)total);
+  }
+}
+
+void launch_nrpcg(cudaStream_t st, const SolverArgs& a) { k_nrpcg<<<1, 1024, 0, st>>>(a); }
 
 // ------------------------------------------------------ grid barrier ---
 // Cooperative launches guarantee that all blocks are resident.  bar[0] counts

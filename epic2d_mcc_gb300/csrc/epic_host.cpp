@@ -216,7 +216,11 @@ int config_from_ini(const char* path, epic_config* cfg, epic_species_desc* sp, i
     else throw std::invalid_argument("bc must be pbc, open or reflective");
     if (solver == "gs") cfg->solver = EPIC_SOLVER_GS;
     else if (solver == "cg" || solver == "iter" || solver == "iterative") cfg->solver = EPIC_SOLVER_PCG;
-    else throw std::invalid_argument("solvertype " + solver + " is not supported (gs, cg, iter, iterative)");
+    else if (solver == "gshybrid") cfg->solver = EPIC_SOLVER_GSHYBRID;
+    else if (solver == "hybrid") cfg->solver = EPIC_SOLVER_HYBRID;
+    else
+      throw std::invalid_argument("solvertype " + solver +
+                                  " is not supported (gs, cg, iter, iterative, gshybrid, hybrid)");
     cfg->tolerance = tol;
     cfg->max_iteration = max_it;
     cfg->ionfixed = ionfixed;

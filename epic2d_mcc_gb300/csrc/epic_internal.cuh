@@ -286,6 +286,10 @@ struct SolverArgs {
 void init_field_kernels();  // one-time kernel attributes (called by epic_create)
 void set_last_error(const char* msg);  // the message epic_last_error() returns on this thread
 void launch_sor_lex(cudaStream_t st, const SolverArgs& a);
+// Boltzmann-electron solvers: gsfluidsolver ("gshybrid"; writes rho's edge
+// values, as the reference does) and nrpcgsolver ("hybrid").
+void launch_gsfluid(cudaStream_t st, const SolverArgs& a, double* rho);
+void launch_nrpcg(cudaStream_t st, const SolverArgs& a);
 void launch_sor_redblack(cudaStream_t st, const SolverArgs& a, int blocks);
 void launch_pcg(cudaStream_t st, const SolverArgs& a, int blocks);
 int solver_max_blocks();

@@ -38,7 +38,7 @@ bool needs_exclusive(const epic_config& c) {
   // the mixed form solves with the spectral method (no grid barrier) on any
   // grid under pcgsolver's norm and on isotropic grids under gssolver's
   const bool spectral = c.precision == EPIC_PRECISION_MIXED && c.nx >= 3 && c.ny >= 3 &&
-                        (c.solver == EPIC_SOLVER_PCG || c.dx == c.dy);
+                        (c.solver == EPIC_SOLVER_PCG || (c.solver == EPIC_SOLVER_GS && c.dx == c.dy));
   if (spectral) return false;
   if (c.solver == EPIC_SOLVER_PCG) return true;
   return c.solver == EPIC_SOLVER_GS && c.sor_mode == EPIC_SOR_REDBLACK;

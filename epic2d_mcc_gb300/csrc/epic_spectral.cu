@@ -34,6 +34,7 @@ namespace epic {
 
 int spectral_supported(const Geom& g, int solver) {
   if (g.nx < 3 || g.ny < 3) return 0;
+  if (solver != EPIC_SOLVER_PCG && solver != EPIC_SOLVER_GS) return 0;  // the Boltzmann solvers are nonlinear
   return solver == EPIC_SOLVER_PCG || g.dx == g.dy;  // the SOR lattice is isotropic only for dx = dy
 }
 

@@ -82,7 +82,8 @@ int main(int argc, char** argv) {
     coll.set_electron_cross_sections();
     coll.calc_total_cross_sections();
     // Normalising species of Output::diagnostics (src/output.cpp:323-324).
-    const int norm = (cfg.normscheme == 2 || cfg.normscheme == 4) ? 1 : 0;
+    const bool hybrid = cfg.solver == EPIC_SOLVER_HYBRID || cfg.solver == EPIC_SOLVER_GSHYBRID;
+    const int norm = !hybrid && (cfg.normscheme == 2 || cfg.normscheme == 4) ? 1 : 0;
     std::ofstream energy;
     if (!energy_path.empty()) energy.open(energy_path);
     std::unique_ptr<Output> output;

@@ -41,7 +41,9 @@ typedef enum {
 
 enum { EPIC_CIC = 0, EPIC_NGP = 1 };                    /* [simulation] shapefunction */
 enum { EPIC_PBC = 0, EPIC_OPEN = 1, EPIC_REFLECTIVE = 2 }; /* [simulation] bc */
-enum { EPIC_SOLVER_GS = 0, EPIC_SOLVER_PCG = 1 };       /* [solver] solvertype gs | cg/iter/iterative */
+/* [solver] solvertype gs | cg/iter/iterative | gshybrid | hybrid (the last two:
+ * Boltzmann electrons, FieldSolve::gsfluidsolver / nrpcgsolver, src/field.cpp:7-68, 141-210) */
+enum { EPIC_SOLVER_GS = 0, EPIC_SOLVER_PCG = 1, EPIC_SOLVER_GSHYBRID = 2, EPIC_SOLVER_HYBRID = 3 };
 enum { EPIC_SOR_LEXICOGRAPHIC = 0, EPIC_SOR_REDBLACK = 1 };
 enum { EPIC_DEPOSIT_FIXED = 0, EPIC_DEPOSIT_FP64 = 1 };
 enum { EPIC_MCC_PHILOX = 0, EPIC_MCC_INJECTED = 1, EPIC_MCC_NULL = 2 };
@@ -61,7 +63,7 @@ typedef struct {
   double density;             /* n0 [m^-3] */
   int shape;                  /* EPIC_CIC | EPIC_NGP */
   int bc;                     /* EPIC_PBC | EPIC_OPEN | EPIC_REFLECTIVE */
-  int solver;                 /* EPIC_SOLVER_GS | EPIC_SOLVER_PCG */
+  int solver;                 /* EPIC_SOLVER_* */
   double tolerance;
   int max_iteration;
   int ionfixed;               /* skip the push of the species named "ion" */

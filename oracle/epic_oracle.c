@@ -355,6 +355,146 @@ int or_gs_solve(const or_domain* d, double omega, const double* rho, double* phi
  * linearalgebra/linalg.h:387-432 adds A(k,j)*v(j) for j = 0..n-1 starting from
  * 0; the zero entries leave the sum unchanged, so the result is the stencil
  * terms added in increasing column order. */
+/* FieldSolve::gsfluidsolver (src/field.cpp:7-68), "gshybrid": the SOR sweep
+ * of gssolver with Boltzmann electrons, source (rho - exp(phi)) * K, after
+ * setting rho on the edges (bottom 0, top 10000 * eV/(k_B EV_to_K), then left
+ * and right 0, in that order); the residual is checked every 50 sweeps.  rho
+ * is modified in place, as domain.rho is. */
+int or_gsfluid_solve(const or_domain* d, double* rho, double* phi, double* err, int* iters) {
+  const int nx = d->nx, ny = d->ny;
+  double dx2 = d->dx * d->dx, dy2 = d->dy * d->dy;
+  memset(phi, 0, sizeof(double) * (size_t)nx * ny);
+  double L2 = 0;
+  int converged = 0;
+  double coeff = (2 / dx2) + (2 / dy2);
+  for (int i = 0; i < nx; i++) {
+    rho[IDX(i, 0)] = 0;
+    rho[IDX(i, ny - 1)] = 10000 * (OR_QE / (OR_K_B * (OR_QE / OR_K_B)));
+  }
+  for (int i = 0; i < ny; i++) {
+    rho[IDX(0, i)] = 0;
+    rho[IDX(nx - 1, i)] = 0;
+  }
+  const double K = (d->L * d->L) / (d->LDe * d->LDe);
+  int iter;
+  for (iter = 0; iter < d->max_iteration; iter++) {
+    for (int i = 1; i < nx - 1; i++) {
+      for (int j = 1; j < ny - 1; j++) {
+        double phi_new = (1 / coeff) * ((rho[IDX(i, j)] - exp(phi[IDX(i, j)])) * K +
+                                        ((phi[IDX(i + 1, j)] + phi[IDX(i - 1, j)]) / dx2) +
+                                        ((phi[IDX(i, j + 1)] + phi[IDX(i, j - 1)]) / dy2));
+        phi[IDX(i, j)] = phi[IDX(i, j)] + 1.4 * (phi_new - phi[IDX(i, j)]);
+      }
+    }
+    if (iter % 50 == 0) {
+      double sum = 0;
+      for (int i = 1; i < nx - 1; i++) {
+        for (int j = 1; j < ny - 1; j++) {
+          double R = ((phi[IDX(i + 1, j)] - 2 * phi[IDX(i, j)] + phi[IDX(i - 1, j)]) / dx2) +
+                     ((phi[IDX(i, j + 1)] - 2 * phi[IDX(i, j)] + phi[IDX(i, j - 1)]) / dy2) +
+                     (rho[IDX(i, j)] - exp(phi[IDX(i, j)])) * K;
+          sum += R * R;
+        }
+      }
+      L2 = sqrt(sum / (nx * ny));
+      *err = L2;
+      if (L2 < d->tolerance) {
+        converged = 1;
+        break;
+      }
+    }
+  }
+  *iters = converged ? iter + 1 : iter;
+  return converged;
+}
+
+/* The dense 5-point matrix of nrpcgsolver (src/field.cpp:150-161: row k / nx,
+ * column k % nx of the flattened vector, diagonal diag[k]) times v, summed in
+ * ascending column order like Matrix::operator*(vec) (linearalgebra/linalg.h:
+ * 388-430, whose zero entries leave the sum unchanged). */
+static void nr_matvec(int nx, int ny, const double* diag, double cdiag, const double* v, double* out) {
+  const long n = (long)nx * ny;
+  for (long k = 0; k < n; k++) {
+    const long row = k / nx, col = k % nx;
+    double sum = 0;
+    if (row > 0) sum += 1.0 * v[k - nx];
+    if (col > 0) sum += 1.0 * v[k - 1];
+    sum += (diag ? diag[k] : cdiag) * v[k];
+    if (col < nx - 1) sum += 1.0 * v[k + 1];
+    if (row < ny - 1) sum += 1.0 * v[k + nx];
+    out[k] = sum;
+  }
+}
+
+static double nr_dot(const double* a, const double* b, long n) {  /* vec::operator*, serial */
+  double r = 0;
+  for (long i = 0; i < n; i++) r += a[i] * b[i];
+  return r;
+}
+
+/* FieldSolve::nrpcgsolver (src/field.cpp:141-210), "hybrid": ten Newton steps
+ * on A x - rhovec with rhovec += exp(x) K every step (the reference accumulates
+ * it) and J = A - diag(exp(x)), each solved by cg (linearalgebra/solvers.h:
+ * 33-69, tolerance 1e-4, at most min(n, 10000) iterations, from x = 0).
+ * Returns the CG iterations in total; domain.error is set to 0. */
+long or_nrpcg_solve(const or_domain* d, const double* rho, double* phi, double* err) {
+  const int nx = d->nx, ny = d->ny;
+  const long n = (long)nx * ny;
+  const double dx2 = d->dx * d->dx;
+  const double K = (d->L * d->L) / (d->LDe * d->LDe);
+  double* rhovec = calloc((size_t)n, sizeof(double));
+  double* x = calloc((size_t)n, sizeof(double));
+  double* F = calloc((size_t)n, sizeof(double));
+  double* J = calloc((size_t)n, sizeof(double));
+  double* y = calloc((size_t)n, sizeof(double));
+  double* r = calloc((size_t)n, sizeof(double));
+  double* p = calloc((size_t)n, sizeof(double));
+  double* Ap = calloc((size_t)n, sizeof(double));
+  for (int i = 0; i < nx; i++)
+    for (int j = 0; j < ny; j++) {
+      double v = -rho[IDX(i, j)] * dx2 * K;
+      if (j == 0 || j == ny - 1 || i == 0 || i == nx - 1) v = 0;
+      rhovec[IDX(i, j)] = v;
+    }
+  long total = 0;
+  const long maxit = n < 10000 ? n : 10000;
+  for (int it = 0; it < 10; it++) {
+    for (long k = 0; k < n; k++) rhovec[k] = rhovec[k] + exp(x[k]) * K;
+    nr_matvec(nx, ny, 0, -4, x, F);
+    for (long k = 0; k < n; k++) {
+      F[k] = F[k] - rhovec[k];
+      J[k] = -4 - exp(x[k]);
+    }
+    /* cg(J, 0, F): r0 = F - J*0 = F */
+    for (long k = 0; k < n; k++) {
+      y[k] = 0;
+      r[k] = F[k] - 0.0;
+      p[k] = r[k];
+    }
+    double r02 = nr_dot(r, r, n);
+    for (long i = 0; i < maxit; i++) {
+      if (sqrt(r02) < 1e-4) break;
+      nr_matvec(nx, ny, J, 0, p, Ap);
+      double pAp = nr_dot(p, Ap, n);
+      double alpha = r02 / pAp;
+      for (long k = 0; k < n; k++) {
+        y[k] = y[k] + p[k] * alpha;
+        r[k] = r[k] - Ap[k] * alpha;
+      }
+      double r12 = nr_dot(r, r, n);
+      double beta = r12 / r02;
+      for (long k = 0; k < n; k++) p[k] = r[k] + p[k] * beta;
+      r02 = r12;
+      total++;
+    }
+    for (long k = 0; k < n; k++) x[k] = x[k] - y[k];
+  }
+  memcpy(phi, x, sizeof(double) * (size_t)n);
+  *err = 0;
+  free(rhovec); free(x); free(F); free(J); free(y); free(r); free(p); free(Ap);
+  return total;
+}
+
 static double pcg_row(long k, int nx, int ny, const double* v) {
   long row = k / nx, col = k % nx;
   double sum = 0;

@@ -86,6 +86,10 @@ int or_pcg_solve(const or_domain* d, const double* rho, double* phi, double* err
 void or_efield(const or_domain* d, const double* phi, double* efx, double* efy);
 /* Species::Push_species_serial (src/species.cpp:29-170), no conductors.
  * Returns the new particle count (open boundaries erase, order kept). */
+/* Boltzmann-electron solvers: gsfluidsolver ("gshybrid", rho edited in
+ * place) and nrpcgsolver ("hybrid", returns the CG iterations). */
+int or_gsfluid_solve(const or_domain* d, double* rho, double* phi, double* err, int* iters);
+long or_nrpcg_solve(const or_domain* d, const double* rho, double* phi, double* err);
 /* Emitter::inject of one emitter (see epic_oracle.c). */
 int or_inject(const or_domain* d, const double* em, double mass1, double mass2, or_rng* r, const double* pos_u,
               const double* vel_u, double* out1, long* n1, long cap1, double* out2, long* n2, long cap2);

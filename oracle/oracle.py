@@ -331,6 +331,9 @@ def restatement_lib():
         L.or_in_conductors.argtypes = [vp, i, i, d, d]
         L.or_in_conductors.restype = i
         L.or_inject.argtypes = [vp, vp, d, d, vp, vp, vp, vp, vp, l, vp, vp, l]
+        L.or_gsfluid_solve.argtypes = [vp, vp, vp, vp, vp]
+        L.or_nrpcg_solve.argtypes = [vp, vp, vp, vp]
+        L.or_nrpcg_solve.restype = l
         L.or_inject.restype = i
         L.or_scatter.argtypes = [vp, vp, l, d, vp]
         L.or_scatter.restype = l
@@ -455,11 +458,28 @@ class Restatement:
                                    ctypes.byref(it))
         return phi, err.value, it.value, bool(conv)
 
+    def gsfluid_solve(self, rho):
+        """gsfluidsolver; returns (phi, error, iterations, converged, rho with its edge values)."""
+        phi = self.grid()
+        rho = np.ascontiguousarray(rho).copy()
+        err = ctypes.c_double()
+        it = ctypes.c_int()
+        conv = self.L.or_gsfluid_solve(ctypes.byref(self.d), _p(rho), _p(phi), ctypes.byref(err), ctypes.byref(it))
+        return phi, err.value, it.value, bool(conv), rho
+
+    def nrpcg_solve(self, rho):
+        phi = self.grid()
+        err = ctypes.c_double()
+        it = self.L.or_nrpcg_solve(ctypes.byref(self.d), _p(np.ascontiguousarray(rho)), _p(phi), ctypes.byref(err))
+        return phi, err.value, it, True
+
     def solve(self, rho):
         if self.s.solver == "gs":
             return self.gs_solve(rho, self.s.sor_omega)
         if self.s.solver in ("cg", "iter", "iterative"):
             return self.pcg_solve(rho)
+        if self.s.solver == "hybrid":
+            return self.nrpcg_solve(rho)
         raise ValueError("solver %r not restated" % self.s.solver)
 
     def efield(self, phi):
@@ -572,7 +592,10 @@ class OracleSim:
         if self.s.solver == "gs" and len(self.s.grids):
             self.rho = self.R.conductor_rho(self.rho)
             self.circles_live = True
-        self.phi, self.error, self.iters, _ = self.R.solve(self.rho)
+        if self.s.solver == "gshybrid":  # gsfluidsolver edits domain.rho's edges
+            self.phi, self.error, self.iters, _, self.rho = self.R.gsfluid_solve(self.rho)
+        else:
+            self.phi, self.error, self.iters, _ = self.R.solve(self.rho)
         self.efx, self.efy = self.R.efield(self.phi)
 
     def initial_field(self):

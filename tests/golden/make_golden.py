@@ -33,6 +33,9 @@ CASES = {
                           beam=dict(n=100, t=1, frac=0.2, vx=5, vy=0)), 2, False),
     "mcc_ionizing": (dict(nx=24, ny=24, ne=500, ni=500, solver="gs", tol="1e-6", te=30,
                           ion_mass="6.63352090e-26", collisions=True, gas="1e23"), 2, True),
+    # Boltzmann-electron solvers (src/field.cpp:7-68, 141-210)
+    "gshybrid_pbc": (dict(nx=16, ny=12, ne=600, ni=600, solver="gshybrid", tol="1e-6", te=2), 2, False),
+    "hybrid_pbc": (dict(nx=12, ny=10, ne=500, ni=500, solver="hybrid", tol="1e-6", te=2), 2, False),
     # a rectangular conductor and a ring of circular electrodes (src/grid.cpp, src/electrode.cpp)
     "conductors_gs_pbc": (dict(nx=24, ny=16, ne=800, ni=800, solver="gs", tol="1e-8", te=4,
                                grids=[dict(type="reactconduct", min_x=6, max_x=8, min_y=3, max_y=11, grid_voltage=10),

@@ -100,6 +100,9 @@ LIVE = {
     "gs_reflective_conductors": dict(nx=32, ny=24, ne=2000, ni=2000, te=4, solver="gs", tol="1e-8",
                                      bc="reflective", grids=CONDUCTORS),
     "pcg_pbc_conductors": dict(nx=32, ny=24, ne=2000, ni=2000, te=4, solver="cg", tol="1e-10", grids=CONDUCTORS),
+    # Boltzmann-electron solvers (src/field.cpp:7-68, 141-210)
+    "gshybrid_pbc": dict(nx=20, ny=14, ne=1500, ni=1500, solver="gshybrid", tol="1e-6", te=2),
+    "hybrid_pbc": dict(nx=14, ny=10, ne=800, ni=800, solver="hybrid", tol="1e-6", te=2),
     "gs_pbc_cic_rect": dict(nx=20, ny=14, ne=1500, ni=1500, solver="gs", tol="1e-9"),
     "gs_open_ngp": dict(nx=16, ny=16, ne=1500, ni=1500, solver="gs", tol="1e-8", bc="open", shape="NGP", te=6),
     "pcg_reflective_cic": dict(nx=18, ny=18, ne=1500, ni=1500, solver="cg", tol="1e-10", bc="reflective"),
