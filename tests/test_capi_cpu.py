@@ -91,10 +91,14 @@ def test_errors_do_not_throw(E, tmp_path):
     with pytest.raises(E.EpicError) as ei:
         E.config_from_ini(decks.write(text, str(tmp_path)))
     assert ei.value.status == 1 and "Ny" in str(ei.value)
-    bad = decks.deck().replace("solvertype = gs", "solvertype = hybrid")
+    bad = decks.deck().replace("solvertype = gs", "solvertype = multigrid")
     with pytest.raises(E.EpicError) as ei:
         E.config_from_ini(decks.write(bad, str(tmp_path)))
-    assert "hybrid" in str(ei.value)
+    assert "multigrid" in str(ei.value)
+    for name, code in (("gshybrid", 2), ("hybrid", 3)):  # the Boltzmann-electron solvers
+        cfg, _, _ = E.config_from_ini(decks.write(decks.deck().replace("solvertype = gs", "solvertype = " + name),
+                                                  str(tmp_path)))
+        assert cfg.solver == code
 
 
 def test_reference_input_deck_parses(E):
