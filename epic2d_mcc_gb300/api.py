@@ -47,7 +47,7 @@ class Config(ctypes.Structure):
                 ("sor_omega", ctypes.c_double), ("sor_mode", ctypes.c_int), ("deposit_mode", ctypes.c_int),
                 ("mcc_mode", ctypes.c_int), ("seed", ctypes.c_uint64), ("warm_start", ctypes.c_int),
                 ("solver_blocks", ctypes.c_int), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
-                ("reserved", ctypes.c_int * 13)]
+                ("push_order", ctypes.c_int), ("reserved", ctypes.c_int * 12)]
 
 
 class SpeciesDesc(ctypes.Structure):

@@ -336,14 +336,14 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle) {
   if (cond && !s->mixed) {
     const CondSet cs{s->cond_nrect, s->cond_ncirc, s->d_cond_rect, s->d_cond_circ, s->d_cond_live};
     launch_push_conductors(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, qmK, cc, dtsub, cs, s->d_flags,
-                           s->tile_status, s->tile_ctr, s->part_grid);
+                           s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
   } else if (s->mixed)
     launch_push_mixed(s->stream, s->g, c.shape, c.bc, sp.mx, sp.d_n, s->ef32, (float)(qmK * dtsub),
                       (float)(cc * dtsub / c.dx), (float)(cc * dtsub / c.dy), s->d_flags, s->tile_status,
                       s->tile_ctr, s->part_grid);
   else
     launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, qmK, cc, dtsub, s->d_flags, s->tile_status,
-                s->tile_ctr, s->part_grid);
+                s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
   s->launches += 1;
   CKL();
   return EPIC_OK;
@@ -647,6 +647,8 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   if (cfg->shape != EPIC_CIC && cfg->shape != EPIC_NGP) return fail(EPIC_ERR_INVALID, "bad shape");
   if (cfg->bc < EPIC_PBC || cfg->bc > EPIC_REFLECTIVE) return fail(EPIC_ERR_INVALID, "bad bc");
   if (cfg->solver < EPIC_SOLVER_GS || cfg->solver > EPIC_SOLVER_HYBRID) return fail(EPIC_ERR_INVALID, "bad solver");
+  if (cfg->push_order != EPIC_PUSH_CONTRACTED && cfg->push_order != EPIC_PUSH_REFERENCE)
+    return fail(EPIC_ERR_INVALID, "bad push_order");
   int dev = 0;
   CK(cudaGetDevice(&dev));
   init_field_kernels();
@@ -1131,7 +1133,7 @@ epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* part
     CK(cudaEventRecord(s->ev_fork, s->stream));
     CK(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
     launch_push(s->side, s->g, c.shape, c.bc, e.soa, e.d_n, s->ef, (e.desc.charge / e.desc.mass) * K, cc, c.DT,
-                s->d_flags, s->tile_status, s->tile_ctr, s->part_grid);
+                s->d_flags, s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
     CK(cudaEventRecord(s->ev_join, s->side));
     s->launches += 1;
   }
@@ -1139,7 +1141,7 @@ epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* part
     if (c.ionfixed == 1 && s->sp[k].name == "ion") continue;
     epic_species_state& sp = s->sp[k];
     launch_push_download(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, (sp.desc.charge / sp.desc.mass) * K,
-                         cc, c.DT, parts[k], s->d_flags, s->part_grid);
+                         cc, c.DT, parts[k], s->d_flags, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
     s->launches += 1;
   }
   CKL();

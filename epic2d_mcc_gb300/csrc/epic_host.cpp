@@ -240,6 +240,11 @@ int config_from_ini(const char* path, epic_config* cfg, epic_species_desc* sp, i
     // every 16 steps for the mixed form unless the deck says otherwise.
     if (cfg->precision == EPIC_PRECISION_MIXED) cfg->sort_every = 16;
     if (auto v = opt(ini, "simulation", "sort_every")) cfg->sort_every = std::stoi(*v);
+    if (auto v = opt(ini, "simulation", "push_order")) {
+      if (*v == "reference") cfg->push_order = EPIC_PUSH_REFERENCE;
+      else if (*v == "contracted") cfg->push_order = EPIC_PUSH_CONTRACTED;
+      else throw std::invalid_argument("push_order " + *v + " is not supported (contracted, reference)");
+    }
     if (auto v = opt(ini, "collision", "mcc_mode"))
       cfg->mcc_mode = *v == "null" ? EPIC_MCC_NULL : (*v == "injected" ? EPIC_MCC_INJECTED : EPIC_MCC_PHILOX);
     if (auto v = opt(ini, "collision", "seed")) cfg->seed = std::stoull(*v);

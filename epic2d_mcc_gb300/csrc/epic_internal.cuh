@@ -128,7 +128,8 @@ void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const 
 void launch_upload_deposit(cudaStream_t st, const Geom& g, int shape, const double* host, long long n, const SoA& p,
                            long long* d_n, unsigned long long* acc, double fx_scale, int* flags, int grid);
 void launch_push_download(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, const long long* d_n,
-                          const double2* ef, double qmK, double c, double dtsub, double* host, int* flags, int grid);
+                          const double2* ef, double qmK, double c, double dtsub, double* host, int* flags, int grid,
+                          int contract);
 void launch_download(cudaStream_t st, const SoA& p, const long long* d_n, long long from, long long cap, double* host,
                      int* flags, int grid);
 // The conductors' rho override before an SOR solve (Grid::initialize inside
@@ -138,7 +139,7 @@ void launch_conductor_rho(cudaStream_t st, double* rho, const int* nodes, const 
 // src/species.cpp:80-97, 108-121, 150-165); needs the compaction scratch.
 void launch_push_conductors(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
                             const double2* ef, double qmK, double c, double dtsub, const CondSet& cs, int* flags,
-                            unsigned long long* tile_status, unsigned int* tile_ctr, int grid);
+                            unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract);
 // Emitter::inject into one species (slot 0: species_idx1, 1: species_idx2):
 // appends num particles at the live count; the count is advanced by
 // launch_emit_commit (so the two slots of one emitter read the same counts).
@@ -154,7 +155,7 @@ void launch_emit_commit(cudaStream_t st, long long* d_n, long long num, long lon
 void launch_inject_tick(cudaStream_t st, unsigned long long* d_inj);
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
                  const double2* ef, double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
-                 unsigned int* tile_ctr, int grid);
+                 unsigned int* tile_ctr, int grid, int contract);
 void launch_rewind(cudaStream_t st, const Geom& g, int shape, const SoA& p, const long long* d_n, const double2* ef,
                    double hqmK, double dt, int* flags, int grid);
 // Ionisation events of one MCC launch: products in `buf` (count, cap), the

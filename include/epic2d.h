@@ -44,6 +44,11 @@ enum { EPIC_PBC = 0, EPIC_OPEN = 1, EPIC_REFLECTIVE = 2 }; /* [simulation] bc */
 /* [solver] solvertype gs | cg/iter/iterative | gshybrid | hybrid (the last two:
  * Boltzmann electrons, FieldSolve::gsfluidsolver / nrpcgsolver, src/field.cpp:7-68, 141-210) */
 enum { EPIC_SOLVER_GS = 0, EPIC_SOLVER_PCG = 1, EPIC_SOLVER_GSHYBRID = 2, EPIC_SOLVER_HYBRID = 3 };
+/* FP64 push arithmetic: CONTRACTED forms the CIC weights once and uses
+ * multiply-adds (results within a few ulps of the reference's, well inside
+ * 1e-12; under half the FP64 operations); REFERENCE keeps the operation order
+ * of src/species.cpp:29-170 bit for bit.  [simulation] push_order. */
+enum { EPIC_PUSH_CONTRACTED = 0, EPIC_PUSH_REFERENCE = 1 };
 enum { EPIC_SOR_LEXICOGRAPHIC = 0, EPIC_SOR_REDBLACK = 1 };
 enum { EPIC_DEPOSIT_FIXED = 0, EPIC_DEPOSIT_FP64 = 1 };
 enum { EPIC_MCC_PHILOX = 0, EPIC_MCC_INJECTED = 1, EPIC_MCC_NULL = 2 };
@@ -80,7 +85,8 @@ typedef struct {
   int solver_blocks;          /* CTAs of the grid-wide solvers; 0 = automatic */
   int precision;              /* EPIC_PRECISION_FP64 (the reference's arithmetic) | EPIC_PRECISION_MIXED */
   int sort_every;             /* sort particles by cell every k steps (0: never, the reference's order) */
-  int reserved[13];
+  int push_order;             /* EPIC_PUSH_CONTRACTED (default) | EPIC_PUSH_REFERENCE (FP64 form) */
+  int reserved[12];
 } epic_config;
 
 /* Mixed precision: particles as int32 cell + FP32 in-cell offsets + FP32
