@@ -315,6 +315,10 @@ epic_status do_efield(epic_sim* s) {
   PhaseTimer t(s, 3);
   launch_efield(s->stream, s->g, s->cfg.bc, s->phi, s->efx, s->efy, s->ef, s->mixed ? s->ef32 : nullptr);
   s->launches += 1;
+  if (s->ef_cell) {
+    launch_cell_coef(s->stream, s->g, s->ef, s->ef_cell);
+    s->launches += 1;
+  }
   CKL();
   return EPIC_OK;
 }
@@ -335,15 +339,16 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle) {
   }
   if (cond && !s->mixed) {
     const CondSet cs{s->cond_nrect, s->cond_ncirc, s->d_cond_rect, s->d_cond_circ, s->d_cond_live};
-    launch_push_conductors(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, qmK, cc, dtsub, cs, s->d_flags,
+    launch_push_conductors(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, s->ef_cell, qmK, cc, dtsub, cs,
+                           s->d_flags,
                            s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
   } else if (s->mixed)
     launch_push_mixed(s->stream, s->g, c.shape, c.bc, sp.mx, sp.d_n, s->ef32, (float)(qmK * dtsub),
                       (float)(cc * dtsub / c.dx), (float)(cc * dtsub / c.dy), s->d_flags, s->tile_status,
                       s->tile_ctr, s->part_grid);
   else
-    launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, qmK, cc, dtsub, s->d_flags, s->tile_status,
-                s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
+    launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, s->ef_cell, qmK, cc, dtsub, s->d_flags,
+                s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
   s->launches += 1;
   CKL();
   return EPIC_OK;
@@ -700,6 +705,8 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   if (s->mixed) {
     guard(dalloc(s, &s->ef32, nn));
     if (spectral_supported(s->g, cfg->solver) && !st) guard(setup_spectral(s));
+  } else if (cfg->shape == EPIC_CIC && cfg->push_order == EPIC_PUSH_CONTRACTED) {
+    guard(dalloc(s, &s->ef_cell, 4 * (size_t)nn));
   }
   if (!st && cudaStreamSynchronize(s->stream) != cudaSuccess) st = EPIC_ERR_CUDA;
   if (st) {
@@ -741,7 +748,7 @@ void epic_destroy(epic_sim* s) {
   dfree(s, s->mcc_ev.cand);
   dfree(s, s->mcc_ev.cand_count);
   for (int k = 0; k < 8; k++) dfree(s, s->work[k]);
-  void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->partials, s->bar,
+  void* ptrs[] = {s->phi, s->rho, s->efx, s->efy, s->ef, s->ef_cell, s->partials, s->bar,
                   s->d_info, s->d_iter_total, s->tile_ctr, s->d_ncoll, s->d_step, s->sum_partials, s->d_sums, s->d_flags,
                   s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion,
                   s->cs.bin_cut, s->d_cond_rect, s->d_cond_circ, s->d_cond_nodes, s->d_cond_vals, s->d_cond_live,
@@ -1132,16 +1139,16 @@ epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* part
     epic_species_state& e = s->sp[0];
     CK(cudaEventRecord(s->ev_fork, s->stream));
     CK(cudaStreamWaitEvent(s->side, s->ev_fork, 0));
-    launch_push(s->side, s->g, c.shape, c.bc, e.soa, e.d_n, s->ef, (e.desc.charge / e.desc.mass) * K, cc, c.DT,
-                s->d_flags, s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
+    launch_push(s->side, s->g, c.shape, c.bc, e.soa, e.d_n, s->ef, s->ef_cell, (e.desc.charge / e.desc.mass) * K, cc,
+                c.DT, s->d_flags, s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
     CK(cudaEventRecord(s->ev_join, s->side));
     s->launches += 1;
   }
   for (int k = coll ? 1 : 0; k < nsp; k++) {
     if (c.ionfixed == 1 && s->sp[k].name == "ion") continue;
     epic_species_state& sp = s->sp[k];
-    launch_push_download(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, (sp.desc.charge / sp.desc.mass) * K,
-                         cc, c.DT, parts[k], s->d_flags, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
+    launch_push_download(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, s->ef_cell,
+                         (sp.desc.charge / sp.desc.mass) * K, cc, c.DT, parts[k], s->d_flags, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
     s->launches += 1;
   }
   CKL();
@@ -1430,6 +1437,7 @@ epic_status epic_set_grid(epic_sim* s, int which, const double* in) {
     std::vector<double2> e2(nnodes(s));
     for (long long k = 0; k < nnodes(s); k++) e2[k] = make_double2(ex[k], ey[k]);
     CK(cudaMemcpyAsync(s->ef, e2.data(), nnodes(s) * sizeof(double2), cudaMemcpyHostToDevice, s->stream));
+    if (s->ef_cell) launch_cell_coef(s->stream, s->g, s->ef, s->ef_cell);
     if (s->ef32) {
       std::vector<float2> f2(nnodes(s));
       for (long long k = 0; k < nnodes(s); k++) f2[k] = make_float2((float)ex[k], (float)ey[k]);

@@ -128,8 +128,8 @@ void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const 
 void launch_upload_deposit(cudaStream_t st, const Geom& g, int shape, const double* host, long long n, const SoA& p,
                            long long* d_n, unsigned long long* acc, double fx_scale, int* flags, int grid);
 void launch_push_download(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, const long long* d_n,
-                          const double2* ef, double qmK, double c, double dtsub, double* host, int* flags, int grid,
-                          int contract);
+                          const double2* ef, const double2* cell, double qmK, double c, double dtsub, double* host,
+                          int* flags, int grid, int contract);
 void launch_download(cudaStream_t st, const SoA& p, const long long* d_n, long long from, long long cap, double* host,
                      int* flags, int grid);
 // The conductors' rho override before an SOR solve (Grid::initialize inside
@@ -138,8 +138,9 @@ void launch_conductor_rho(cudaStream_t st, double* rho, const int* nodes, const 
 // The FP64 push erasing particles that end inside a conductor (order kept,
 // src/species.cpp:80-97, 108-121, 150-165); needs the compaction scratch.
 void launch_push_conductors(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
-                            const double2* ef, double qmK, double c, double dtsub, const CondSet& cs, int* flags,
-                            unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract);
+                            const double2* ef, const double2* cell, double qmK, double c, double dtsub,
+                            const CondSet& cs, int* flags, unsigned long long* tile_status, unsigned int* tile_ctr,
+                            int grid, int contract);
 // Emitter::inject into one species (slot 0: species_idx1, 1: species_idx2):
 // appends num particles at the live count; the count is advanced by
 // launch_emit_commit (so the two slots of one emitter read the same counts).
@@ -153,9 +154,14 @@ void launch_emit(cudaStream_t st, const SoA& p, const long long* d_n, long long 
                  int grid);
 void launch_emit_commit(cudaStream_t st, long long* d_n, long long num, long long cap, int* flags);
 void launch_inject_tick(cudaStream_t st, unsigned long long* d_inj);
+// The FP64 push.  ef is the node field; cell the bilinear coefficients of
+// each cell (launch_cell_coef), which the contracted CIC push reads instead.
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
-                 const double2* ef, double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
-                 unsigned int* tile_ctr, int grid, int contract);
+                 const double2* ef, const double2* cell, double qmK, double c, double dtsub, int* flags,
+                 unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract);
+// cell[4 (i ny + j) + m], m = 0..3: a0 = E00, a1 = E10 - E00, a2 = E01 - E00,
+// a3 = (E11 - E10) - (E01 - E00) of cell (i, j), from the interleaved field.
+void launch_cell_coef(cudaStream_t st, const Geom& g, const double2* ef, double2* cell);
 void launch_rewind(cudaStream_t st, const Geom& g, int shape, const SoA& p, const long long* d_n, const double2* ef,
                    double hqmK, double dt, int* flags, int grid);
 // Ionisation events of one MCC launch: products in `buf` (count, cap), the
@@ -327,6 +333,7 @@ struct epic_sim {
   std::vector<epic_species_state> sp;
   double *phi, *rho, *efx, *efy;
   double2* ef;
+  double2* ef_cell;            // bilinear coefficients per cell (contracted CIC push), or null
   float2* ef32;                // FP32 (efx, efy) for the mixed-precision gather
   epic::SpectralSolver spec;   // mixed-precision Poisson solve (square grids)
   int mixed;                   // cfg.precision == EPIC_PRECISION_MIXED

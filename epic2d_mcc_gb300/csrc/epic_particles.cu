@@ -12,6 +12,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 
 #include "epic_internal.cuh"
 #include "epic_device.cuh"
@@ -162,52 +163,141 @@ void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const 
 #undef DEP
 }
 
-// The gather with the four CIC weights formed once and the weighted sum as
-// multiply-adds: 12 FP64 operations for both components where the
-// reference's expression takes 22 (each result within a few ulps of it).
-__device__ __forceinline__ bool gather_contracted(const Geom& g, const double2* __restrict__ ef, double lx, double ly,
-                                                  double& ex, double& ey) {
-  int i = (int)lx, j = (int)ly;
+// The cell i = (int)l and offset d = l - i of a logical coordinate l, on the
+// integer pipe, giving the doubles of the FP64 forms bit for bit: for |l| < 1
+// (either sign) i = 0 and d = l; for 1 <= l < 2^31 the significand m and
+// s = exponent - 1023 give i = m >> (52 - s) and d = ((m << s) mod 2^52) 2^-52,
+// exact because l's ulp is at least 2^-52 there; for l <= -1, l >= 2^31, or
+// NaN, i = -1 (off the grid, as the reference's truncated index is).
+__device__ __forceinline__ void split_cell(double l, int& i, double& d) {
+  // Branch-free, with d selected as integer bits: a select of doubles can
+  // cost FP64 instructions.
+  const uint64_t b = (uint64_t)__double_as_longlong(l);
+  const int sh = (int)((b >> 52) & 0x7FF) - 1023;
+  const bool small = sh < 0, out = !small && ((b >> 63) || sh > 30);
+  const int s = min(max(sh, 0), 30);
+  const uint64_t m = (b & 0xFFFFFFFFFFFFFull) | (1ull << 52);
+  const uint64_t F = (m << s) & 0xFFFFFFFFFFFFFull;
+  const int t = 63 - __clzll((long long)(F | 1));  // F 2^-52, normalised by F's top bit t
+  uint64_t db = F ? (((uint64_t)(971 + t) << 52) | ((F << (52 - t)) & 0xFFFFFFFFFFFFFull)) : 0ull;
+  db = small ? b : (out ? 0ull : db);
+  i = small ? 0 : (out ? -1 : (int)(m >> (52 - s)));
+  asm("mov.b64 %0, %1;" : "=d"(d) : "l"(db));
+}
+
+// Bilinear coefficients of the node field over each cell, four double2 per
+// cell at 4 (i ny + j): E(i + di, j + dj) = a0 + a1 di + a2 dj + a3 di dj with
+// a0 = E00, a1 = E10 - E00, a2 = E01 - E00, a3 = (E11 - E10) - (E01 - E00).
+// The same function as the reference's weighted sum (src/domain.cpp:231-255)
+// up to the roundings of the differences.
+__global__ void k_cell_coef(Geom g, const double2* __restrict__ ef, double2* __restrict__ cell) {
+  const int ny = g.ny, nc = (g.nx - 1) * (ny - 1);
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+    const int i = c / (ny - 1), j = c - i * (ny - 1);
+    const long k = (long)i * ny + j;
+    const double2 f00 = ef[k], f01 = ef[k + 1], f10 = ef[k + ny], f11 = ef[k + ny + 1];
+    double2* a = cell + 4 * k;
+    a[0] = f00;
+    a[1] = make_double2(f10.x - f00.x, f10.y - f00.y);
+    a[2] = make_double2(f01.x - f00.x, f01.y - f00.y);
+    a[3] = make_double2((f11.x - f10.x) - (f01.x - f00.x), (f11.y - f10.y) - (f01.y - f00.y));
+  }
+}
+
+void launch_cell_coef(cudaStream_t st, const Geom& g, const double2* ef, double2* cell) {
+  const int nc = (g.nx - 1) * (g.ny - 1);
+  k_cell_coef<<<(nc + 255) / 256 > 0 ? (nc + 255) / 256 : 1, 256, 0, st>>>(g, ef, cell);
+}
+
+// The contracted CIC gather from the cell coefficients:
+// E = fma(dj, fma(di, a3, a2), fma(di, a1, a0)), 6 FP64 operations for both
+// components where the reference's expression takes 22 (each result within a
+// few ulps of the largest corner value of the reference's).
+__device__ __forceinline__ bool gather_cell(const Geom& g, const double2* __restrict__ cell, double lx, double ly,
+                                            double& ex, double& ey) {
+  int i, j;
+  double di, dj;
+  split_cell(lx, i, di);
+  split_cell(ly, j, dj);
   if (i < 0 || i + 1 >= g.nx || j < 0 || j + 1 >= g.ny) return false;
-  const double di = lx - i, dj = ly - j, oi = 1 - di, oj = 1 - dj;
-  const double w00 = oi * oj, w10 = di * oj, w01 = oi * dj, w11 = di * dj;
-  const long k = (long)i * g.ny + j;
-  const double2 f00 = __ldg(&ef[k]), f01 = __ldg(&ef[k + 1]);
-  const double2 f10 = __ldg(&ef[k + g.ny]), f11 = __ldg(&ef[k + g.ny + 1]);
-  ex = fma(f00.x, w00, fma(f10.x, w10, fma(f01.x, w01, f11.x * w11)));
-  ey = fma(f00.y, w00, fma(f10.y, w10, fma(f01.y, w01, f11.y * w11)));
+  const double2* a = cell + 4 * ((long)i * g.ny + j);
+  const double2 a0 = __ldg(a), a1 = __ldg(a + 1), a2 = __ldg(a + 2), a3 = __ldg(a + 3);
+  ex = fma(dj, fma(di, a3.x, a2.x), fma(di, a1.x, a0.x));
+  ey = fma(dj, fma(di, a3.y, a2.y), fma(di, a1.y, a0.y));
   return true;
 }
 
+// A signed integer that orders doubles as < does: the sign-magnitude bits as
+// two's complement, so -0 and +0 share the key 0.  NaN keys compare some way
+// where < is false both ways; the wrap then still leaves a NaN coordinate NaN.
+// The bits are taken through an opaque move: a plain reinterpretation lets
+// the compiler fold the key back into FP64 arithmetic (two additions per
+// particle on GB300's narrow FP64 pipe).
+__device__ __forceinline__ long long dkey(double v) {
+  long long b;
+  asm("mov.b64 %0, %1;" : "=l"(b) : "d"(v));
+  return b < 0 ? -(b & 0x7FFFFFFFFFFFFFFFll) : b;
+}
+
 // --------------------------------------------------------------- push ---
+// The push's logical coordinates: MAP_GENERAL (x - x0) / dx, MAP_UNIT x - x0
+// (dx = 1), MAP_ORIGIN x itself (dx = 1 and x0 = y0 = +0, where x - x0 is x
+// bit for bit).
+enum { MAP_GENERAL = 0, MAP_UNIT = 1, MAP_ORIGIN = 2 };
+static int push_map(const Geom& g) {
+  if (!unit_cell(g)) return MAP_GENERAL;
+  const bool zero = std::signbit(g.x0) == 0 && g.x0 == 0.0 && std::signbit(g.y0) == 0 && g.y0 == 0.0;
+  return zero ? MAP_ORIGIN : MAP_UNIT;
+}
+template <int MAP>
+__device__ __forceinline__ double push_logical(double x, double x0, double dx) {
+  return MAP == MAP_ORIGIN ? x : to_logical<MAP == MAP_UNIT>(x, x0, dx);
+}
+
+__device__ __forceinline__ double add_rn_volatile(double a, double b) {
+  double r;
+  asm volatile("add.rn.f64 %0, %1, %2;" : "=d"(r) : "d"(a), "d"(b));
+  return r;
+}
+
+// Per-launch constants of the contracted push, formed once per thread.
+struct PushK {
+  double kv, kx;         // qmK dt and c dt
+  long long lo, hx, hy;  // order keys of x0, x0 + Lx and x0 + Ly
+};
+__device__ __forceinline__ PushK push_consts(const Geom& g, double qmK, double c, double dtsub) {
+  return PushK{qmK * dtsub, c * dtsub, dkey(g.x0), dkey(g.x0 + g.Lx), dkey(g.x0 + g.Ly)};
+}
+
 // Species::Push_species_serial (src/species.cpp:29-170):
 //   v += (qm*K) * E * (DT*sub);  x += (vel_norm/(L*W)) * v * (DT*sub)
 // then the boundary rule.  qmK = (q/m) * (n0*e*L)/(eps0*W*vel_norm) and
 // c = vel_norm/(L*W) come from the host, computed exactly as the reference
-// evaluates the leading factors of its expressions.  contract = 0 keeps the
-// reference's operation order (bit for bit); contract = 1 (EPIC_PUSH_CONTRACTED)
-// forms the CIC weights once and uses multiply-adds, v = fma(qmK dt, E, v) and
-// x = fma(c dt, v, x): less than half the FP64 operations, each result within a
-// few ulps of the reference's.
-template <int SHAPE, int BC, bool UNIT>
+// evaluates the leading factors of its expressions.  CONTRACT = false keeps the
+// reference's operation order (bit for bit); CONTRACT (EPIC_PUSH_CONTRACTED)
+// takes E of a CIC particle from the cell coefficients (ef is then the table
+// k_cell_coef writes), splits the coordinates on the integer pipe and uses
+// multiply-adds, v = fma(qmK dt, E, v) and x = fma(c dt, v, x): about a
+// quarter of the FP64 operations, each result within a few ulps of the
+// reference's.  k holds the contracted form's per-launch constants.
+template <int SHAPE, int BC, int MAP, bool CONTRACT>
 __device__ __forceinline__ bool push_one(const Geom& g, const double2* __restrict__ ef, double qmK, double c,
-                                         double dtsub, double& x, double& y, double& vx, double& vy, bool& bad,
-                                         int contract) {
-  double lx = to_logical<UNIT>(x, g.x0, g.dx);
-  double ly = to_logical<UNIT>(y, g.y0, g.dy);
+                                         double dtsub, const PushK& k, double& x, double& y, double& vx, double& vy,
+                                         bool& bad) {
+  double lx = push_logical<MAP>(x, g.x0, g.dx);
+  double ly = push_logical<MAP>(y, g.y0, g.dy);
   double ex, ey;
-  const bool in = (SHAPE == EPIC_CIC && contract) ? gather_contracted(g, ef, lx, ly, ex, ey)
+  const bool in = (SHAPE == EPIC_CIC && CONTRACT) ? gather_cell(g, ef, lx, ly, ex, ey)
                                                   : gather<SHAPE>(g, ef, lx, ly, ex, ey);
   if (!in) {
     bad = true;
     return true;  // keep the particle untouched; the host reports FLAG_OUT_OF_GRID
   }
-  if (contract) {
-    const double kv = qmK * dtsub, kx = c * dtsub;
-    vx = fma(kv, ex, vx);
-    vy = fma(kv, ey, vy);
-    x = fma(kx, vx, x);
-    y = fma(kx, vy, y);
+  if (CONTRACT) {
+    vx = fma(k.kv, ex, vx);
+    vy = fma(k.kv, ey, vy);
+    x = fma(k.kx, vx, x);
+    y = fma(k.kx, vy, y);
   } else {
     vx += qmK * ex * dtsub;
     vy += qmK * ey * dtsub;
@@ -216,6 +306,19 @@ __device__ __forceinline__ bool push_one(const Geom& g, const double2* __restric
   }
   if (BC == EPIC_PBC) {
     // y is compared against x0 as in the reference (src/species.cpp:74-79).
+    if (CONTRACT) {
+      // The same comparisons on order-preserving integer keys; the FP64
+      // additions (x + L or x + (-L) = x - L) run only in the few warps that
+      // hold a particle to wrap: volatile, so the compiler cannot hoist them
+      // out of the branch.
+      const long long qx = dkey(x), qy = dkey(y);
+      const bool wx = qx < k.lo || qx >= k.hx, wy = qy < k.lo || qy >= k.hy;
+      if (__any_sync(__activemask(), wx || wy)) {
+        if (wx) x = add_rn_volatile(x, qx < k.lo ? g.Lx : -g.Lx);
+        if (wy) y = add_rn_volatile(y, qy < k.lo ? g.Ly : -g.Ly);
+      }
+      return true;
+    }
     if (x < g.x0) x = x + g.Lx;
     else if (x >= g.x0 + g.Lx) x = x - g.Lx;
     if (y < g.x0) y = y + g.Ly;
@@ -232,16 +335,17 @@ __device__ __forceinline__ bool push_one(const Geom& g, const double2* __restric
   }
 }
 
-template <int SHAPE, int BC, bool UNIT>
+template <int SHAPE, int BC, int MAP, bool CONTRACT>
 __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long long* __restrict__ d_n,
                                                        const double2* __restrict__ ef, double qmK, double c,
-                                                       double dtsub, int* flags, int contract) {
+                                                       double dtsub, int* flags) {
   const long long n = *d_n;
+  const PushK k = push_consts(g, qmK, c, dtsub);
   const long long stride = (long long)gridDim.x * blockDim.x;
   bool bad = false;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
     double x = p.x[q], y = p.y[q], vx = p.vx[q], vy = p.vy[q];
-    push_one<SHAPE, BC, UNIT>(g, ef, qmK, c, dtsub, x, y, vx, vy, bad, contract);
+    push_one<SHAPE, BC, MAP, CONTRACT>(g, ef, qmK, c, dtsub, k, x, y, vx, vy, bad);
     p.x[q] = x;
     p.y[q] = y;
     p.vx[q] = vx;
@@ -272,18 +376,18 @@ __device__ __forceinline__ bool in_conductor(const CondSet& cs, double x, double
   return false;
 }
 
-template <int SHAPE, int BC, bool UNIT, bool COND>
+template <int SHAPE, int BC, int MAP, bool COND, bool CONTRACT>
 __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, long long* d_n,
                                                                const double2* __restrict__ ef, double qmK, double c,
                                                                double dtsub, unsigned long long* status,
-                                                               unsigned int* tile_ctr, int* flags, CondSet cs,
-                                                               int contract) {
+                                                               unsigned int* tile_ctr, int* flags, CondSet cs) {
   constexpr int ITEMS = SCAN_TILE / PART_THREADS;
   __shared__ int sm[40];
   __shared__ unsigned long long s_prefix;
   __shared__ int s_tile;
   const long long n = *d_n;
   const int num_tiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+  const PushK pk = push_consts(g, qmK, c, dtsub);
   bool bad = false;
   for (;;) {
     if (threadIdx.x == 0) s_tile = (int)atomicAdd(tile_ctr, 1u);
@@ -299,7 +403,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, lo
       keep[k] = 0;
       if (q < n) {
         x[k] = p.x[q]; y[k] = p.y[q]; vx[k] = p.vx[q]; vy[k] = p.vy[q]; vz[k] = p.vz[q];
-        keep[k] = push_one<SHAPE, BC, UNIT>(g, ef, qmK, c, dtsub, x[k], y[k], vx[k], vy[k], bad, contract) &&
+        keep[k] = push_one<SHAPE, BC, MAP, CONTRACT>(g, ef, qmK, c, dtsub, pk, x[k], y[k], vx[k], vy[k], bad) &&
                           !(COND && in_conductor(cs, x[k], y[k]))
                       ? 1
                       : 0;
@@ -332,15 +436,22 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, lo
 }
 
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n, const double2* ef,
-                 double qmK, double c, double dtsub, int* flags, unsigned long long* tile_status,
-                 unsigned int* tile_ctr, int grid, int contract) {
-#define PUSH(SH, B, U) k_push<SH, B, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags, contract)
-#define COMPACT(SH, U)                                                                                       \
-  k_push_compact<SH, EPIC_OPEN, U, false><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, \
-                                                                         tile_ctr, flags, CondSet{}, contract)
-#define BOTH(M, ...) \
-  do { if (u) M(__VA_ARGS__, true); else M(__VA_ARGS__, false); } while (0)
-  const bool u = unit_cell(g);
+                 const double2* cell, double qmK, double c, double dtsub, int* flags,
+                 unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract) {
+  if (shape == EPIC_CIC && contract) ef = cell;
+#define PUSH1(SH, B, U, C) k_push<SH, B, U, C><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags)
+#define PUSH(SH, B, U) do { if (contract) PUSH1(SH, B, U, true); else PUSH1(SH, B, U, false); } while (0)
+#define COMPACT1(SH, U, C)                                                                                      \
+  k_push_compact<SH, EPIC_OPEN, U, false, C><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub,      \
+                                                                            tile_status, tile_ctr, flags, CondSet{})
+#define COMPACT(SH, U) do { if (contract) COMPACT1(SH, U, true); else COMPACT1(SH, U, false); } while (0)
+#define BOTH(M, ...)                          \
+  do {                                        \
+    if (map == MAP_ORIGIN) M(__VA_ARGS__, 2); \
+    else if (map == MAP_UNIT) M(__VA_ARGS__, 1); \
+    else M(__VA_ARGS__, 0);                   \
+  } while (0)
+  const int map = push_map(g);
   if (bc == EPIC_OPEN) {
     if (shape == EPIC_NGP) BOTH(COMPACT, EPIC_NGP);
     else BOTH(COMPACT, EPIC_CIC);
@@ -353,24 +464,35 @@ void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p
   }
 #undef BOTH
 #undef COMPACT
+#undef COMPACT1
 #undef PUSH
+#undef PUSH1
 }
 
 void launch_push_conductors(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
-                            const double2* ef, double qmK, double c, double dtsub, const CondSet& cs, int* flags,
-                            unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract) {
-#define PC(SH, B, U)                                                                                         \
-  k_push_compact<SH, B, U, true><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, \
-                                                                tile_ctr, flags, cs, contract)
-#define BOTH(SH, B) do { if (u) PC(SH, B, true); else PC(SH, B, false); } while (0)
+                            const double2* ef, const double2* cell, double qmK, double c, double dtsub,
+                            const CondSet& cs, int* flags, unsigned long long* tile_status, unsigned int* tile_ctr,
+                            int grid, int contract) {
+  if (shape == EPIC_CIC && contract) ef = cell;
+#define PC1(SH, B, U, C)                                                                                        \
+  k_push_compact<SH, B, U, true, C><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, \
+                                                                   tile_ctr, flags, cs)
+#define PC(SH, B, U) do { if (contract) PC1(SH, B, U, true); else PC1(SH, B, U, false); } while (0)
+#define BOTH(SH, B)                            \
+  do {                                         \
+    if (map == MAP_ORIGIN) PC(SH, B, 2);       \
+    else if (map == MAP_UNIT) PC(SH, B, 1);    \
+    else PC(SH, B, 0);                         \
+  } while (0)
 #define SHAPES(B) do { if (shape == EPIC_NGP) BOTH(EPIC_NGP, B); else BOTH(EPIC_CIC, B); } while (0)
-  const bool u = unit_cell(g);
+  const int map = push_map(g);
   if (bc == EPIC_OPEN) SHAPES(EPIC_OPEN);
   else if (bc == EPIC_PBC) SHAPES(EPIC_PBC);
   else SHAPES(EPIC_REFLECTIVE);
 #undef SHAPES
 #undef BOTH
 #undef PC
+#undef PC1
 }
 
 __global__ void k_conductor_rho(double* __restrict__ rho, const int* __restrict__ nodes,
@@ -591,13 +713,13 @@ __global__ void __launch_bounds__(PART_THREADS) k_upload_deposit(const double* _
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
 }
 
-template <int SHAPE, int BC, bool UNIT>
+template <int SHAPE, int BC, int MAP, bool CONTRACT>
 __global__ void __launch_bounds__(PART_THREADS) k_push_download(Geom g, SoA p, const long long* __restrict__ d_n,
                                                                 const double2* __restrict__ ef, double qmK, double c,
-                                                                double dtsub, double* __restrict__ host, int* flags,
-                                                                int contract) {
+                                                                double dtsub, double* __restrict__ host, int* flags) {
   __shared__ double tile[HOSTIO_TILE * 5];
   const long long n = *d_n;
+  const PushK pk = push_consts(g, qmK, c, dtsub);
   bool bad = false;
   for (long long base = (long long)blockIdx.x * HOSTIO_TILE; base < n;
        base += (long long)gridDim.x * HOSTIO_TILE) {
@@ -606,7 +728,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_download(Geom g, SoA p, c
       const long long q = base + threadIdx.x;
       double x = p.x[q], y = p.y[q], vx = p.vx[q], vy = p.vy[q];
       const double vz = p.vz[q];
-      push_one<SHAPE, BC, UNIT>(g, ef, qmK, c, dtsub, x, y, vx, vy, bad, contract);
+      push_one<SHAPE, BC, MAP, CONTRACT>(g, ef, qmK, c, dtsub, pk, x, y, vx, vy, bad);
       p.x[q] = x;
       p.y[q] = y;
       p.vx[q] = vx;
@@ -664,12 +786,19 @@ void launch_upload_deposit(cudaStream_t st, const Geom& g, int shape, const doub
 }
 
 void launch_push_download(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, const long long* d_n,
-                          const double2* ef, double qmK, double c, double dtsub, double* host, int* flags, int grid,
-                          int contract) {
-#define PD(SH, B, U) \
-  k_push_download<SH, B, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, host, flags, contract)
-#define BOTH(...) do { if (u) PD(__VA_ARGS__, true); else PD(__VA_ARGS__, false); } while (0)
-  const bool u = unit_cell(g);
+                          const double2* ef, const double2* cell, double qmK, double c, double dtsub, double* host,
+                          int* flags, int grid, int contract) {
+  if (shape == EPIC_CIC && contract) ef = cell;
+#define PD1(SH, B, U, C) \
+  k_push_download<SH, B, U, C><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, host, flags)
+#define PD(SH, B, U) do { if (contract) PD1(SH, B, U, true); else PD1(SH, B, U, false); } while (0)
+#define BOTH(...)                              \
+  do {                                         \
+    if (map == MAP_ORIGIN) PD(__VA_ARGS__, 2); \
+    else if (map == MAP_UNIT) PD(__VA_ARGS__, 1); \
+    else PD(__VA_ARGS__, 0);                   \
+  } while (0)
+  const int map = push_map(g);
   if (bc == EPIC_PBC) {
     if (shape == EPIC_NGP) BOTH(EPIC_NGP, EPIC_PBC);
     else BOTH(EPIC_CIC, EPIC_PBC);
@@ -679,6 +808,7 @@ void launch_push_download(cudaStream_t st, const Geom& g, int shape, int bc, con
   }
 #undef BOTH
 #undef PD
+#undef PD1
 }
 
 void launch_download(cudaStream_t st, const SoA& p, const long long* d_n, long long from, long long cap, double* host,

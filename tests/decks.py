@@ -33,8 +33,8 @@ species_index   = 0
 [domain]
 Nx       = {nx}
 Ny       = {ny}
-x0       = 0
-y0       = 0
+x0       = {x0}
+y0       = {x0}
 
 [Grids]
 {grids}
@@ -80,7 +80,7 @@ BEAM = "beam,9.10938215E-31,{n},{t},-1,{frac},{vx},{vy},random"
 def deck(nx=16, ny=16, ne=2000, ni=2000, te=1, ti=0.026, ion_mass="1.6726219e-27", solver="gs", tol="1e-8",
          maxit=20000, bc="pbc", shape="CIC", dt=0.01, norm=1, density="1E13", collisions=False, gas="1e20",
          ionfixed=0, beam=None, vdrift=(0, 0), solver_extra="", sim_extra="", coll_extra="", num_ts=10, grids=None,
-         emitters=None):
+         emitters=None, x0=0):
     sp = [ELECTRON.format(n=ne, t=te, vx=vdrift[0], vy=vdrift[1]), ION.format(m=ion_mass, n=ni, t=ti)]
     if beam:
         sp.append(BEAM.format(**beam))
@@ -89,7 +89,7 @@ def deck(nx=16, ny=16, ne=2000, ni=2000, te=1, ti=0.026, ion_mass="1.6726219e-27
                            shape=shape, density=density, bc=bc, ionfixed=ionfixed, el=flag, ex=flag, io=flag,
                            gas=gas, species="\n".join(sp), solver_extra=solver_extra, sim_extra=sim_extra,
                            coll_extra=coll_extra, grids=grid_section(grids or []),
-                           emitters=emitter_section(emitters or []))
+                           emitters=emitter_section(emitters or []), x0=x0)
 
 
 def grid_section(grids) -> str:

@@ -220,6 +220,30 @@ def test_push_is_exact(gpu_lib, tmp_path, shape, bc, order):
             assert parts_rel(got, ref) < 1e-14
 
 
+@pytest.mark.parametrize("bc", ["pbc", "reflective"])
+@pytest.mark.parametrize("x0", [3, 0.75])
+@pytest.mark.parametrize("order", ["reference", "contracted"])
+def test_push_offset_origin(gpu_lib, tmp_path, bc, x0, order):
+    """A domain origin x0 = y0 != 0 (the push's x - x0 kept; the boundary tests against x0 + L)."""
+    ini, orc, _ = _prepared(gpu_lib, tmp_path, nx=24, ny=20, ne=20000, ni=20000, bc=bc, te=20, dt=0.05, x0=x0)
+    assert orc.s.x0 == x0
+    sim = make_sim(gpu_lib, ini, push_order=1 if order == "reference" else 0)
+    for s in range(len(orc.parts)):
+        sim.set_particles(s, orc.parts[s])
+    rng = np.random.default_rng(5)
+    ex, ey = rng.normal(size=orc.efx.shape) * 5, rng.normal(size=orc.efy.shape) * 5
+    sim.set_grid("efx", ex)
+    sim.set_grid("efy", ey)
+    for s in range(2):
+        ref = orc.R.push(orc.s.species[s], orc.parts[s], ex, ey)
+        sim.push_species(s)
+        got = sim.particles(s)
+        if order == "reference":
+            assert np.array_equal(got, ref)
+        else:
+            assert parts_rel(got, ref) < 1e-14
+
+
 def test_rewind_is_exact(gpu_lib, tmp_path):
     ini, orc, sim = _prepared(gpu_lib, tmp_path, nx=20, ny=20, ne=5000, ni=5000)
     rng = np.random.default_rng(3)
