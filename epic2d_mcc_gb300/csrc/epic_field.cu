@@ -906,25 +906,32 @@ __device__ __forceinline__ double recip_nr(double x) {
 }
 
 // ---- fused grid barrier and reduction ----
-// A slot is one 128-byte line of PCG_SLOT_WORDS 64-bit words.  Every CTA adds
+// A slot is PCG_SLOT_WORDS 64-bit words, each on its own 128-byte line so that
+// the CTAs' additions to different words proceed in parallel in L2 instead of
+// queueing on one line.  Every CTA adds
 // (payload << 8) + 1 to each word, so a word whose low byte has reached the
 // CTA count is complete and its upper bits hold the payload total: polling a
 // slot is the barrier and returns the reduction in the same load.  Payloads:
 // the 26-bit limb totals of the CTA's fixed-point partials of (w, r) (words
 // 0-4) and (r, r) (words 5-9) against grid-wide anchors, and whether the CTA
-// had a term beyond the anchors' range (word 10).  Slots rotate over three
-// lines: iteration k adds to slot k % 3 while CTA 0 clears slot (k + 1) % 3,
-// last read in iteration k - 2 (every CTA read it before adding to slot
-// k - 1, which CTA 0 has seen complete) and next written in iteration k + 1
-// (after the adders have seen slot k complete, including CTA 0's release).
+// had a term beyond the anchors' range (word 10).  Slots rotate over three:
+// iteration k adds to slot k % 3, and once CTA 0 has seen it complete it
+// clears slot (k - 1) % 3 (every CTA read that one before adding to slot k);
+// it is next written in iteration k + 2, after the adders have seen slot
+// k + 1 complete, which includes CTA 0's addition after the clearing.
 constexpr int PCG_SLOT_WORDS = 11;
-constexpr int PCG_SLOT_U64 = 16;
+constexpr int PCG_WORD_STRIDE = 16;  // 64-bit words: one 128-byte line per slot word
+constexpr int PCG_SLOT_U64 = PCG_SLOT_WORDS * PCG_WORD_STRIDE;
 constexpr int PCG_SLOTS = 3;
 // Byte offset of the slots in the partials buffer (after two parities of
 // XPartial records).
 constexpr size_t PCG_SLOT_OFFSET = 2 * PCG_MAX_BLOCKS * sizeof(XPartial);
 static_assert(PCG_MAX_BLOCKS < 256, "the CTA count must fit the low byte of a slot word");
 static_assert(PCG_SLOT_OFFSET % 128 == 0, "slots are 128-byte lines");
+// The partials buffer holds at least 16 x 320 doubles (epic_create) and the
+// allocation-free entry's 8 x 1024.
+static_assert(PCG_SLOT_OFFSET + PCG_SLOTS * PCG_SLOT_U64 * sizeof(unsigned long long) <= 16 * 320 * sizeof(double),
+              "slots must fit the solver partials buffer");
 // Anchors: (r, r) terms of iteration k+1 are converted against the exponent
 // of (r, r) of iteration k plus this headroom, (w, r) terms one higher
 // (|w_i r_i| <= 2 max r_i^2 for the diagonal -4 stencil).  A term more than
@@ -1120,7 +1127,8 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(a.partials) + PCG_SLOT_OFFSET);
   // The counted sums hold up to 2^19 terms (the fixed-point headroom).
   const bool fused = n < (1 << 19);
-  if (blockIdx.x == 0 && threadIdx.x < PCG_SLOTS * PCG_SLOT_U64) slots[threadIdx.x] = 0ull;
+  if (blockIdx.x == 0)
+    for (int m = threadIdx.x; m < PCG_SLOTS * PCG_SLOT_U64; m += PCG_T) slots[m] = 0ull;
   __shared__ int s_limb[PCG_T / 32][PCG_SLOT_WORDS];
   __shared__ int s_aq, s_exact;
   // Thread 0's scalars, in the scaled form: rr = (r, r) = -4 gamma,
@@ -1164,7 +1172,7 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
         long long S = 0;
 #pragma unroll
         for (int w = 0; w < PCG_T / 32; w++) S += s_limb[w][lane];
-        red_add_u64(slot + lane, ((unsigned long long)S << 8) + 1ull);
+        red_add_u64(slot + lane * PCG_WORD_STRIDE, ((unsigned long long)S << 8) + 1ull);
       } else if (threadIdx.x == 64) {
         long long S = 0;
 #pragma unroll
@@ -1172,7 +1180,8 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
         red_release_add_u64(slot, ((unsigned long long)S << 8) + 1ull);
       }
       unsigned long long wv0 = 0;
-      if (wid == 0 && lane < PCG_SLOT_WORDS) wv0 = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane);
+      if (wid == 0 && lane < PCG_SLOT_WORDS)
+        wv0 = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane * PCG_WORD_STRIDE);
       // Deferred update of the previous iteration (no other CTA needs p' or
       // x), and the scalars the next step needs from the previous ones.
 #pragma unroll
@@ -1199,12 +1208,12 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
               good = 0;
               break;
             }
-            wv = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane);
+            wv = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane * PCG_WORD_STRIDE);
           }
         }
         good = __all_sync(0xffffffffu, good);
         if (blockIdx.x == 0 && lane < PCG_SLOT_WORDS)
-          slots[((it + PCG_SLOTS - 1) % PCG_SLOTS) * PCG_SLOT_U64 + lane] = 0ull;
+          slots[((it + PCG_SLOTS - 1) % PCG_SLOTS) * PCG_SLOT_U64 + lane * PCG_WORD_STRIDE] = 0ull;
         const long long S = (long long)(wv - (unsigned long long)nb) >> 8;
         const long long outc = __shfl_sync(0xffffffffu, S, 10);
         // Lane 0 recombines (w, r), lane 1 (r, r), and each rounds its total.
