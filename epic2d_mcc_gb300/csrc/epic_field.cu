@@ -1051,9 +1051,15 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
 
   for (int m = threadIdx.x; m < (tr + 2) * ldu; m += PCG_T) sr[m] = 0.0;
 
+  // Edge publication: each tile writes its boundary to an edge buffer of
+  // 2 (tc + tr) slots per tile - top row at 0, bottom row at tc, left column
+  // at 2 tc, right column at 2 tc + tr - so that a neighbour reads each side
+  // of its halo ring as one contiguous run (a column of the lattice would be
+  // one scattered load per node).  Tiles are at least 2 x 2 (pcg_tiling), so
+  // a node lies on at most one row side and one column side.
+  const int ebase = blockIdx.x * 2 * (tc + tr);
   // Owned slots: tile-local q = threadIdx.x + PCG_T*j, row-major in the tile.
-  int kk[NPT], si[NPT];
-  bool pub[NPT];
+  int kk[NPT], si[NPT], pe0[NPT], pe1[NPT];
 #pragma unroll
   for (int j = 0; j < NPT; j++) {
     const int q = threadIdx.x + PCG_T * j;
@@ -1062,25 +1068,32 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
     const bool valid = q < tr * tc && row < R && col < C;
     kk[j] = valid ? row * C + col : -1;
     si[j] = (lr + 1) * ldu + lc + 1;
-    pub[j] = valid && (lr == 0 || lr == tr - 1 || lc == 0 || lc == tc - 1);
+    const int er = lr == 0 ? ebase + lc : lr == tr - 1 ? ebase + tc + lc : -1;
+    const int ec = lc == 0 ? ebase + 2 * tc + lr : lc == tc - 1 ? ebase + 2 * tc + tr + lr : -1;
+    pe0[j] = !valid ? -1 : er >= 0 ? er : ec;
+    pe1[j] = !valid || er < 0 ? -1 : ec;
   }
-  // Halo slots: top row, bottom row, left column, right column of the ring.
-  int hk[PCG_HALO_SLOTS], hs[PCG_HALO_SLOTS];
+  // Halo slots: top row, bottom row, left column, right column of the ring,
+  // with the node (hk, for the set-up) and the neighbour's edge slot (he).
+  int hk[PCG_HALO_SLOTS], hs[PCG_HALO_SLOTS], he[PCG_HALO_SLOTS];
 #pragma unroll
   for (int j = 0; j < PCG_HALO_SLOTS; j++) {
     const int h = threadIdx.x + PCG_T * j;
-    int row = -1, col = -1, sr_ = 0, sc = 0;
-    if (h < tc) {
-      row = r0 - 1; col = c0 + h; sr_ = 0; sc = h + 1;
-    } else if (h < 2 * tc) {
-      row = r0 + tr; col = c0 + h - tc; sr_ = tr + 1; sc = h - tc + 1;
-    } else if (h < 2 * tc + tr) {
-      row = r0 + h - 2 * tc; col = c0 - 1; sr_ = h - 2 * tc + 1; sc = 0;
-    } else if (h < 2 * tc + 2 * tr) {
+    const int eb = 2 * (tc + tr);
+    int row = -1, col = -1, sr_ = 0, sc = 0, e = -1;
+    if (h < tc) {  // bottom row of the tile above
+      row = r0 - 1; col = c0 + h; sr_ = 0; sc = h + 1; e = (blockIdx.x - t.tiles_c) * eb + tc + h;
+    } else if (h < 2 * tc) {  // top row of the tile below
+      row = r0 + tr; col = c0 + h - tc; sr_ = tr + 1; sc = h - tc + 1; e = (blockIdx.x + t.tiles_c) * eb + h - tc;
+    } else if (h < 2 * tc + tr) {  // right column of the tile to the left
+      row = r0 + h - 2 * tc; col = c0 - 1; sr_ = h - 2 * tc + 1; sc = 0; e = (blockIdx.x - 1) * eb + tr + h;
+    } else if (h < 2 * tc + 2 * tr) {  // left column of the tile to the right
       row = r0 + h - 2 * tc - tr; col = c0 + tc; sr_ = h - 2 * tc - tr + 1; sc = tc + 1;
+      e = (blockIdx.x + 1) * eb + h - tr;
     }
     const bool valid = row >= 0 && row < R && col >= 0 && col < C;
     hk[j] = valid ? row * C + col : -1;
+    he[j] = valid ? e : -1;
     hs[j] = sr_ * ldu + sc;
   }
   __syncthreads();
@@ -1113,10 +1126,15 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       w[j] = fma(-0.25, (c[-ldu] + c[-1]) + (c[1] + c[ldu]), r[j]);
       td[j] = w[j] * r[j];
       tq[j] = r[j] * r[j];
-      if (pub[j]) {
-        a.work[1][kk[j]] = r[j];
-        a.work[3][kk[j]] = w[j];
-        a.work[5][kk[j]] = 0.0;
+      if (pe0[j] >= 0) {
+        a.work[1][pe0[j]] = r[j];
+        a.work[3][pe0[j]] = w[j];
+        a.work[5][pe0[j]] = 0.0;
+      }
+      if (pe1[j] >= 0) {
+        a.work[1][pe1[j]] = r[j];
+        a.work[3][pe1[j]] = w[j];
+        a.work[5][pe1[j]] = 0.0;
       }
     }
   }
@@ -1268,10 +1286,10 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
     double hr[PCG_HALO_SLOTS], hw[PCG_HALO_SLOTS], hsv[PCG_HALO_SLOTS];
 #pragma unroll
     for (int j = 0; j < PCG_HALO_SLOTS; j++)
-      if (hk[j] >= 0) {
-        hr[j] = __ldcg(&pr_c[hk[j]]);
-        hw[j] = __ldcg(&pw_c[hk[j]]);
-        hsv[j] = __ldcg(&ps_c[hk[j]]);
+      if (he[j] >= 0) {
+        hr[j] = __ldcg(&pr_c[he[j]]);
+        hw[j] = __ldcg(&pw_c[he[j]]);
+        hsv[j] = __ldcg(&ps_c[he[j]]);
       }
     if (threadIdx.x == 0) {
       s_rr = rr;
@@ -1305,7 +1323,7 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       }
 #pragma unroll
     for (int j = 0; j < PCG_HALO_SLOTS; j++)
-      if (hk[j] >= 0) sr[hs[j]] = fma(-al, fma(be, hsv[j], hw[j]), hr[j]);
+      if (he[j] >= 0) sr[hs[j]] = fma(-al, fma(be, hsv[j], hw[j]), hr[j]);
     __syncthreads();
     double* const pr_n = cur ? a.work[1] : a.work[2];
     double* const pw_n = cur ? a.work[3] : a.work[4];
@@ -1323,10 +1341,15 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
           in &= xs_add_anchored<false>(v0, td[j], aq + 1);
           in &= xs_add_anchored<true>(v1, tq[j], aq);
         }
-        if (pub[j]) {
-          pr_n[kk[j]] = r[j];
-          pw_n[kk[j]] = w[j];
-          ps_n[kk[j]] = s[j];
+        if (pe0[j] >= 0) {
+          pr_n[pe0[j]] = r[j];
+          pw_n[pe0[j]] = w[j];
+          ps_n[pe0[j]] = s[j];
+        }
+        if (pe1[j] >= 0) {
+          pr_n[pe1[j]] = r[j];
+          pw_n[pe1[j]] = w[j];
+          ps_n[pe1[j]] = s[j];
         }
       }
     it++;
@@ -1388,6 +1411,8 @@ static bool pcg_tiling(int R, int C, int max_blocks, PcgTiling* out) {
     const long long nodes = (long long)tr * tc;
     if (nodes > PCG_T * 8 || 2LL * (tr + tc) > PCG_T * PCG_HALO_SLOTS) continue;
     if (ncb * nrb > PCG_MAX_BLOCKS) continue;
+    // The edge buffers (2 (tr + tc) slots per tile) live in node-sized vectors.
+    if (tr < 2 || tc < 2 || (long long)ncb * nrb * 2 * (tr + tc) > (long long)R * C) continue;
     const long long cost = 11 * nodes + 3 * 2LL * (tr + tc);
     const int blocks = ncb * nrb;
     if (best < 0 || cost < best || (cost == best && blocks < b.blocks)) {
