@@ -203,9 +203,24 @@ struct PhaseTimer {
 };
 
 // ---- phase launchers (no synchronisation; usable inside stream capture) ----
+// The FP64 step deposits each pushed species while it moves it (k_push with
+// an accumulator) and the MCC's products after the MCC, so the next step's
+// deposit is already in the accumulators: the same fixed-point sums, without
+// a second pass over the positions.  Periodic or reflective walls, fixed-point
+// deposit, no conductors or emitters.
+static bool fused_deposit(const epic_sim* s) {
+  return !s->mixed && s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED && s->conductors.empty() && s->emitters.empty() &&
+         (s->cfg.bc == EPIC_PBC || s->cfg.bc == EPIC_REFLECTIVE);
+}
+
+static void invalidate_acc(epic_sim* s) {
+  for (auto& sp : s->sp) sp.acc_valid = false;
+}
+
 epic_status do_deposit(epic_sim* s, int i) {
   PhaseTimer t(s, 0);
   epic_species_state& sp = s->sp[i];
+  sp.acc_valid = true;
   CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
   if (s->mixed && s->cfg.shape == EPIC_CIC)
     launch_deposit_mixed_sorted(s->stream, s->g, sp.mx, sp.d_n, sp.acc, s->part_grid);
@@ -337,6 +352,7 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle) {
     CK(cudaMemsetAsync(s->tile_ctr, 0, sizeof(unsigned int), s->stream));
     CK(cudaMemsetAsync(s->tile_status, 0, s->tile_status_len * sizeof(unsigned long long), s->stream));
   }
+  sp.acc_valid = false;
   if (cond && !s->mixed) {
     const CondSet cs{s->cond_nrect, s->cond_ncirc, s->d_cond_rect, s->d_cond_circ, s->d_cond_live};
     launch_push_conductors(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, s->ef_cell, qmK, cc, dtsub, cs,
@@ -346,9 +362,14 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle) {
     launch_push_mixed(s->stream, s->g, c.shape, c.bc, sp.mx, sp.d_n, s->ef32, (float)(qmK * dtsub),
                       (float)(cc * dtsub / c.dx), (float)(cc * dtsub / c.dy), s->d_flags, s->tile_status,
                       s->tile_ctr, s->part_grid);
-  else
+  else {
+    const bool dep = fused_deposit(s);
+    if (dep) CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
     launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, s->ef_cell, qmK, cc, dtsub, s->d_flags,
-                s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
+                s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED,
+                dep ? sp.acc : nullptr, sp.fx_scale);
+    sp.acc_valid = dep;
+  }
   s->launches += 1;
   CKL();
   return EPIC_OK;
@@ -485,8 +506,10 @@ epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
   if (sort)
     for (int i = 0; i < nsp; i++)
       if ((st = do_sort(s, i))) return st;
+  const bool fused = fused_deposit(s);
   for (int i = 0; i < nsp; i++)
-    if ((st = do_deposit(s, i))) return st;
+    if (!(fused && (s->steady_capture || s->sp[i].acc_valid)))
+      if ((st = do_deposit(s, i))) return st;
   if ((st = do_finalize(s, FINALIZE_AND_RHO, -1))) return st;
   if ((st = do_solve(s))) return st;
   if ((st = do_efield(s))) return st;
@@ -494,8 +517,22 @@ epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
     if (s->cfg.ionfixed == 1 && s->sp[i].name == "ion") continue;
     if ((st = do_push(s, i, 1))) return st;
   }
-  if (with_collisions && nsp >= 2)
+  if (with_collisions && nsp >= 2) {
+    if (fused)  // counts before the MCC: its ionisation products are deposited after it
+      for (int k = 0; k < 2; k++)
+        CK(cudaMemcpyAsync(s->d_nold + k, s->sp[k].d_n, sizeof(long long), cudaMemcpyDeviceToDevice, s->stream));
     if ((st = do_mcc(s, 0, 1, nullptr, 0))) return st;
+    if (fused) {
+      PhaseTimer t(s, 0);
+      for (int k = 0; k < 2; k++) {
+        epic_species_state& sp = s->sp[k];
+        launch_deposit_range(s->stream, s->g, s->cfg.shape, sp.soa, s->d_nold + k, sp.d_n, sp.acc, sp.fx_scale,
+                             s->d_flags, s->part_grid);
+        s->launches += 1;
+      }
+      CKL();
+    }
+  }
   return EPIC_OK;
 }
 
@@ -619,6 +656,7 @@ epic_status epic_add_emitter(epic_sim* s, const epic_emitter* e) {
 epic_status epic_inject(epic_sim* s, const double* uniforms) {
   if (!s) return fail(EPIC_ERR_INVALID, "null handle");
   if (s->emitters.empty()) return EPIC_OK;
+  invalidate_acc(s);
   const double* d_u = nullptr;
   if (uniforms) {
     size_t rows = 0;
@@ -701,6 +739,7 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   guard(dalloc(s, &s->sum_partials, 3 * (size_t)s->part_grid));
   guard(dalloc(s, &s->d_sums, 4));
   guard(dalloc(s, &s->d_flags, 1));
+  guard(dalloc(s, &s->d_nold, 2));
   s->mixed = cfg->precision == EPIC_PRECISION_MIXED;
   if (s->mixed) {
     guard(dalloc(s, &s->ef32, nn));
@@ -752,7 +791,7 @@ void epic_destroy(epic_sim* s) {
                   s->d_info, s->d_iter_total, s->tile_ctr, s->d_ncoll, s->d_step, s->sum_partials, s->d_sums, s->d_flags,
                   s->tile_status, s->staging, s->d_uniforms, s->cs.tot, s->cs.ela, s->cs.exc, s->cs.ion,
                   s->cs.bin_cut, s->d_cond_rect, s->d_cond_circ, s->d_cond_nodes, s->d_cond_vals, s->d_cond_live,
-                  s->d_inj};
+                  s->d_inj, s->d_nold};
   for (void* p : ptrs)
     if (p) dfree(s, p);
   if (s->stream) cudaStreamDestroy(s->stream);
@@ -822,6 +861,7 @@ epic_status epic_add_species(epic_sim* s, const epic_species_desc* d, int* index
 epic_status epic_set_particles(epic_sim* s, int i, const double* parts, int64_t n) {
   if (!valid_species(s, i) || n < 0 || (n > 0 && !parts)) return fail(EPIC_ERR_INVALID, "bad argument");
   epic_species_state& sp = s->sp[i];
+  sp.acc_valid = false;
   if (n > sp.cap) return fail(EPIC_ERR_CAPACITY, "%lld particles exceed the capacity %lld of %s", (long long)n,
                               sp.cap, sp.name.c_str());
   epic_status st = ensure_staging(s, std::max<size_t>(1, (size_t)n * 5 * sizeof(double)));
@@ -1038,6 +1078,7 @@ epic_status epic_set_log_cross_sections(epic_sim* s, const double* ela, const do
 epic_status epic_handle_collisions(epic_sim* s, int e, int ion, const double* uniforms, int ustride,
                                    int64_t* collisions) {
   if (!valid_species(s, e) || !valid_species(s, ion) || e == ion) return fail(EPIC_ERR_INVALID, "bad species");
+  s->sp[e].acc_valid = s->sp[ion].acc_valid = false;  // products are appended
   const double* d_u = nullptr;
   if (s->cfg.mcc_mode == EPIC_MCC_INJECTED) {
     if (!uniforms || ustride < 14) return fail(EPIC_ERR_INVALID, "injected mode needs uniforms with stride >= 14");
@@ -1081,6 +1122,7 @@ epic_status epic_step(epic_sim* s, int with_collisions) {
 epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* parts, int64_t* n,
                            const int64_t* capacity) {
   if (!s || !parts || !n || !capacity) return fail(EPIC_ERR_INVALID, "bad argument");
+  invalidate_acc(s);  // the particles come from the caller and leave moved
   const int nsp = (int)s->sp.size();
   for (int k = 0; k < nsp; k++) {
     if (n[k] < 0 || n[k] > capacity[k] || (n[k] > 0 && !parts[k]))
@@ -1207,7 +1249,9 @@ static epic_status enqueue_run(epic_sim* s, int steps, int with_collisions, int 
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeThreadLocal));
     const int64_t before = s->launches, step_before = s->step_index;
+    s->steady_capture = fused_deposit(s);
     epic_status e = do_step(s, with_collisions, sort);
+    s->steady_capture = false;
     cudaError_t ce = cudaStreamEndCapture(s->stream, &graph);
     s->step_index = step_before;
     if (e || ce != cudaSuccess) {
@@ -1224,6 +1268,11 @@ static epic_status enqueue_run(epic_sim* s, int steps, int with_collisions, int 
     if (ce != cudaSuccess) return fail(EPIC_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
     return EPIC_OK;
   };
+  // The captured step takes the accumulators as deposited (the previous step's
+  // push left them so); deposit whatever another call has moved since.
+  if (fused_deposit(s))
+    for (int i = 0; i < (int)s->sp.size(); i++)
+      if (!s->sp[i].acc_valid && (st = do_deposit(s, i))) return st;
   if (!s->graph_exec || s->graph_collisions != with_collisions || (sorting && !s->graph_exec_sort)) {
     if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
     if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
@@ -1270,6 +1319,7 @@ epic_status epic_poll(epic_sim* s, int* done) {
 
 epic_status epic_load_particles_device(epic_sim* s, uint64_t seed) {
   if (!s) return fail(EPIC_ERR_INVALID, "null handle");
+  invalidate_acc(s);
   if (!s->conductors.empty())
     return fail(EPIC_ERR_INVALID, "the device loader does not place particles around conductors (epic_load_particles does)");
   for (int i = 0; i < (int)s->sp.size(); i++) {

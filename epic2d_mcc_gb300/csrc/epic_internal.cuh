@@ -156,9 +156,17 @@ void launch_emit_commit(cudaStream_t st, long long* d_n, long long num, long lon
 void launch_inject_tick(cudaStream_t st, unsigned long long* d_inj);
 // The FP64 push.  ef is the node field; cell the bilinear coefficients of
 // each cell (launch_cell_coef), which the contracted CIC push reads instead.
+// With dep_acc (periodic or reflective walls) every pushed particle is also
+// deposited at its new position into dep_acc (fixed point, fx_scale), which
+// the caller has zeroed: the next step's charge deposit, bit for bit.
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
                  const double2* ef, const double2* cell, double qmK, double c, double dtsub, int* flags,
-                 unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract);
+                 unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract,
+                 unsigned long long* dep_acc = nullptr, double fx_scale = 0.0);
+// The fixed-point deposit of particles [*d_from, *d_n) (the products an MCC
+// call appended) into acc.
+void launch_deposit_range(cudaStream_t st, const Geom& g, int shape, const SoA& p, const long long* d_from,
+                          const long long* d_n, unsigned long long* acc, double fx_scale, int* flags, int grid);
 // cell[4 (i ny + j) + m], m = 0..3: a0 = E00, a1 = E10 - E00, a2 = E01 - E00,
 // a3 = (E11 - E10) - (E01 - E00) of cell (i, j), from the interleaved field.
 void launch_cell_coef(cudaStream_t st, const Geom& g, const double2* ef, double2* cell);
@@ -320,6 +328,10 @@ struct epic_species_state {
   unsigned long long* acc;
   double fx_scale;      // 2^k
   double fx_inv_scale;  // 2^-k
+  // acc holds the fixed-point deposit of the species' current positions (set
+  // by a deposit or by a push that deposits as it moves the particles;
+  // cleared by anything that moves, adds or replaces particles otherwise).
+  bool acc_valid = false;
 };
 
 struct epic_sim {
@@ -378,6 +390,8 @@ struct epic_sim {
   int graph_collisions;
   // cell sort
   int64_t step_index;               // steps taken (decides which steps sort)
+  bool steady_capture = false;      // capturing the steady-state step (accumulators valid on entry)
+  long long* d_nold = nullptr;      // electron and ion counts before the MCC (its products are deposited)
   void* sort_buf;
   long long sort_cap;               // largest capacity the buffer serves
   // per-phase profiling (events on `stream`)

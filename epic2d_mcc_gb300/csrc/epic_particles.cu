@@ -133,6 +133,20 @@ __device__ __forceinline__ int weight_shift(double fx_scale) {
   return 104 - ((int)(((uint64_t)__double_as_longlong(fx_scale) >> 52) & 0x7FF) - 1023);
 }
 
+template <int SHAPE, bool UNIT>
+__global__ void __launch_bounds__(PART_THREADS) k_deposit_range(Geom g, SoA p, const long long* __restrict__ d_from,
+                                                                const long long* __restrict__ d_n,
+                                                                unsigned long long* __restrict__ acc, double fx_scale,
+                                                                int* flags) {
+  const long long n = *d_n;
+  const int wshift = weight_shift(fx_scale);
+  bool bad = false;
+  for (long long q = *d_from + (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x)
+    bad |= !deposit_one<SHAPE, true, UNIT>(g, p.x[q], p.y[q], 0.0, acc, fx_scale, wshift);
+  if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
+}
+
 template <int SHAPE, bool FIXED, bool UNIT>
 __global__ void __launch_bounds__(PART_THREADS) k_deposit(Geom g, SoA p, const long long* __restrict__ d_n,
                                                           double spwt, double* __restrict__ den,
@@ -161,6 +175,15 @@ void launch_deposit(cudaStream_t st, const Geom& g, int shape, int fixed, const 
     else { if (u) DEP(EPIC_CIC, false, true); else DEP(EPIC_CIC, false, false); }
   }
 #undef DEP
+}
+
+void launch_deposit_range(cudaStream_t st, const Geom& g, int shape, const SoA& p, const long long* d_from,
+                          const long long* d_n, unsigned long long* acc, double fx_scale, int* flags, int grid) {
+#define DR(SH, U) k_deposit_range<SH, U><<<grid, PART_THREADS, 0, st>>>(g, p, d_from, d_n, acc, fx_scale, flags)
+  const bool u = unit_cell(g);
+  if (shape == EPIC_NGP) { if (u) DR(EPIC_NGP, true); else DR(EPIC_NGP, false); }
+  else { if (u) DR(EPIC_CIC, true); else DR(EPIC_CIC, false); }
+#undef DR
 }
 
 // The cell i = (int)l and offset d = l - i of a logical coordinate l, on the
@@ -335,12 +358,14 @@ __device__ __forceinline__ bool push_one(const Geom& g, const double2* __restric
   }
 }
 
-template <int SHAPE, int BC, int MAP, bool CONTRACT>
+template <int SHAPE, int BC, int MAP, bool CONTRACT, bool DEP>
 __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long long* __restrict__ d_n,
                                                        const double2* __restrict__ ef, double qmK, double c,
-                                                       double dtsub, int* flags) {
+                                                       double dtsub, int* flags, unsigned long long* __restrict__ acc,
+                                                       double fx_scale) {
   const long long n = *d_n;
   const PushK k = push_consts(g, qmK, c, dtsub);
+  const int wshift = DEP ? weight_shift(fx_scale) : 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   bool bad = false;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
@@ -350,6 +375,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long
     p.y[q] = y;
     p.vx[q] = vx;
     p.vy[q] = vy;
+    if (DEP) bad |= !deposit_one<SHAPE, true, MAP != MAP_GENERAL>(g, x, y, 0.0, acc, fx_scale, wshift);
   }
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
 }
@@ -437,9 +463,12 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, lo
 
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n, const double2* ef,
                  const double2* cell, double qmK, double c, double dtsub, int* flags,
-                 unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract) {
+                 unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract,
+                 unsigned long long* dep_acc, double fx_scale) {
   if (shape == EPIC_CIC && contract) ef = cell;
-#define PUSH1(SH, B, U, C) k_push<SH, B, U, C><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags)
+#define PUSH2(SH, B, U, C, D) \
+  k_push<SH, B, U, C, D><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags, dep_acc, fx_scale)
+#define PUSH1(SH, B, U, C) do { if (dep_acc) PUSH2(SH, B, U, C, true); else PUSH2(SH, B, U, C, false); } while (0)
 #define PUSH(SH, B, U) do { if (contract) PUSH1(SH, B, U, true); else PUSH1(SH, B, U, false); } while (0)
 #define COMPACT1(SH, U, C)                                                                                      \
   k_push_compact<SH, EPIC_OPEN, U, false, C><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub,      \
@@ -467,6 +496,7 @@ void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p
 #undef COMPACT1
 #undef PUSH
 #undef PUSH1
+#undef PUSH2
 }
 
 void launch_push_conductors(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,

@@ -347,6 +347,37 @@ def test_graph_replay_equals_step_by_step(gpu_lib, tmp_path):
     assert np.array_equal(sims[0].grid("phi"), sims[1].grid("phi"))
 
 
+@pytest.mark.parametrize("bc", ["pbc", "reflective"])
+def test_deposit_in_push_equals_separate_deposit(gpu_lib, tmp_path, bc):
+    """The FP64 step deposits each species as its push moves it, and the MCC's ionisation products after
+    the MCC; reloading the particles every step forces the separate deposit pass instead. Graph replay,
+    step by step and the separate pass give the same particles and potential, bit for bit."""
+    ini = decks.write(decks.deck(nx=32, ny=32, ne=20000, ni=20000, solver="cg", tol="1e-10", bc=bc, te=30,
+                                 collisions=True, gas="1e22", ion_mass="6.63352090e-26"), str(tmp_path))
+    sims = []
+    for mode in ("graph", "step", "reload"):
+        sim = make_sim(gpu_lib, ini)
+        sim.set_reference_cross_sections()
+        sim.load_particles(0)
+        sim.initial_field()
+        if mode == "graph":
+            sim.run(3, collisions=True, graph=True)
+            sim.set_particles(1, sim.particles(1))  # moved outside the step: the next run re-deposits
+            sim.run(3, collisions=True, graph=True)
+        else:
+            for _ in range(6):
+                sim.step(collisions=True)
+                if mode == "reload":
+                    for k in range(2):
+                        sim.set_particles(k, sim.particles(k))
+        sims.append(sim)
+    assert sims[0].particles(1).shape[0] > 20000, "the MCC should ionise"
+    for other in sims[1:]:
+        for k in range(2):
+            assert np.array_equal(sims[0].particles(k), other.particles(k))
+        assert np.array_equal(sims[0].grid("phi"), other.grid("phi"))
+
+
 def test_multi_step_tracks_oracle(gpu_lib, tmp_path):
     """Ten loop iterations (GS, pbc): still within 1e-9 of the restatement."""
     ini = decks.write(decks.deck(nx=32, ny=32, ne=20000, ni=20000, tol="1e-10"), str(tmp_path))
