@@ -83,13 +83,14 @@ __device__ __forceinline__ unsigned long long fx_weight(uint64_t a, uint64_t b, 
 // node can overflow): integer addition is associative, so the grid is
 // identical run to run; the weight is applied at finalisation.  Otherwise
 // FP64 atomics add spwt*w into the same accumulator buffer read as doubles.
-// One particle's deposit; false when its stencil leaves the grid.
-template <int SHAPE, bool FIXED, bool UNIT>
+// One particle's deposit; false when its stencil leaves the grid.  ORIGIN:
+// unit cells and x0 = y0 = +0, where the logical coordinate x - x0 is x.
+template <int SHAPE, bool FIXED, bool UNIT, bool ORIGIN = false>
 __device__ __forceinline__ bool deposit_one(const Geom& g, double x, double y, double spwt,
                                             unsigned long long* __restrict__ acc, double fx_scale, int wshift) {
   double* facc = reinterpret_cast<double*>(acc);
-  double lx = to_logical<UNIT>(x, g.x0, g.dx);
-  double ly = to_logical<UNIT>(y, g.y0, g.dy);
+  double lx = ORIGIN ? x : to_logical<UNIT>(x, g.x0, g.dx);
+  double ly = ORIGIN ? y : to_logical<UNIT>(y, g.y0, g.dy);
   if (SHAPE == EPIC_NGP) {
     int gx = (int)round(lx), gy = (int)round(ly);
     if (gx < 0 || gx >= g.nx || gy < 0 || gy >= g.ny) return false;
@@ -375,7 +376,8 @@ __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long
     p.y[q] = y;
     p.vx[q] = vx;
     p.vy[q] = vy;
-    if (DEP) bad |= !deposit_one<SHAPE, true, MAP != MAP_GENERAL>(g, x, y, 0.0, acc, fx_scale, wshift);
+    if (DEP)
+      bad |= !deposit_one<SHAPE, true, MAP != MAP_GENERAL, MAP == MAP_ORIGIN>(g, x, y, 0.0, acc, fx_scale, wshift);
   }
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
 }
