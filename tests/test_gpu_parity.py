@@ -220,6 +220,36 @@ def test_push_is_exact(gpu_lib, tmp_path, shape, bc, order):
             assert parts_rel(got, ref) < 1e-14
 
 
+@pytest.mark.parametrize("order", ["reference", "contracted"])
+def test_general_cell_size(gpu_lib, tmp_path, order):
+    """dx = dy = 0.5 (a C-ABI configuration; the reference's normalisations always give 1): halved positions
+    have the same logical coordinates, so the deposit is 4x the unit-cell one and the pushed velocities equal
+    the unit-cell ones, bit for bit in both push orders (the general (x - x0)/dx path against the unit path)."""
+    ini, orc, _ = _prepared(gpu_lib, tmp_path, nx=32, ny=24, ne=30000, ni=30000, te=20, dt=0.05)
+    po = 1 if order == "reference" else 0
+    unit = make_sim(gpu_lib, ini, push_order=po)
+    half = make_sim(gpu_lib, ini, push_order=po, dx=0.5, dy=0.5)
+    rng = np.random.default_rng(4)
+    ex, ey = rng.normal(size=orc.efx.shape) * 5, rng.normal(size=orc.efy.shape) * 5
+    for s in range(2):
+        h = orc.parts[s].copy()
+        h[:, :2] *= 0.5
+        unit.set_particles(s, orc.parts[s])
+        half.set_particles(s, h)
+    for sim in (unit, half):
+        sim.set_grid("efx", ex)
+        sim.set_grid("efy", ey)
+    for s in range(2):
+        unit.scatter_species(s)
+        half.scatter_species(s)
+        assert np.array_equal(half.den(s), 4 * unit.den(s))
+        unit.push_species(s)
+        half.push_species(s)
+        a, b = unit.particles(s), half.particles(s)
+        assert a.shape == b.shape
+        assert np.array_equal(a[:, 2:], b[:, 2:])
+
+
 @pytest.mark.parametrize("bc", ["pbc", "reflective"])
 @pytest.mark.parametrize("x0", [3, 0.75])
 @pytest.mark.parametrize("order", ["reference", "contracted"])
