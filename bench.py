@@ -608,9 +608,57 @@ def run_serving(E, workloads):
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of each
 # phase's kernel from the ncu captures summarised under profiles/ (beam_mcc_256);
 # absent where no capture of that phase's average launch exists.  The solve's
-# vectors stay in registers and L2, so its traffic is ~2 MB against 5.8 GB of
+# vectors stay in registers and L2, so its traffic is ~0.7 MB against 5.5 GB of
 # algorithmic (memory-streamed) bytes.
-TRAFFIC = {"solve": 1.938688e6 + 0.08192e6}
+TRAFFIC = {"solve": 0.631296e6 + 0.080384e6}
+
+
+# ------------------------------------------------ extension-row measurements ---
+ROWS = (("conductors (SOR, absorbing walls, erase on hit)", "conductors_64"),
+        ("emitters (injection every step, absorbing walls, PCG)", "emitters_128"),
+        ("gsfluidsolver (solvertype = gshybrid)", "gshybrid_64"),
+        ("nrpcgsolver (solvertype = hybrid)", "hybrid_24"))
+
+
+def run_rows(args):
+    """Per-step throughput of each extension of the loop on its own deck: the
+    GPU loop (CUDA events on the handle's stream, FP64 form) and the oracle
+    restatement on one host core beside it.  Prints one JSON line."""
+    import torch
+
+    import epic2d_mcc_gb300 as E
+    from epic2d_mcc_gb300 import build as B
+
+    B.build()
+    out = []
+    for label, name in ROWS:
+        ini = write_deck(name)
+        sim = E.Simulation.from_ini(ini)
+        sim.load_particles(0)
+        sim.initial_field()
+        nsp = len(sim.species)
+        for _ in range(args.warmup):
+            sim.run(1, collisions=False, graph=False)
+        stream = torch.cuda.ExternalStream(sim.stream)
+        n0 = sum(sim.num_particles(s) for s in range(nsp))
+        sim.sync()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        sim.run(args.steps, collisions=False, graph=False)
+        ev1.record(stream)
+        ev1.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        n1 = sum(sim.num_particles(s) for s in range(nsp))
+        gpu = 0.5 * (n0 + n1) * args.steps / (ms * 1e-3)
+        cpu, done, n, _ = cpu_port_run(ini, None, 1, budget_s=args.cpu_seconds / len(ROWS))
+        out.append({"row": label, "workload": name, "particles": int(0.5 * (n0 + n1)), "gpu_ms_per_step": ms / args.steps,
+                    "gpu_particle_steps_per_s": gpu, "cpu_particle_steps_per_s": cpu, "cpu_steps_timed": done,
+                    "cpu_cores": 1, "speedup": gpu / cpu})
+        del sim
+    print(json.dumps({"rows": out, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
+                      "data": "synthetic (particles loaded from mt19937 seed 0, as the reference's Init)"}),
+          flush=True)
 
 
 def main():
@@ -626,7 +674,12 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching measurement")
     ap.add_argument("--no-precision-form", action="store_true", help="skip the 1024^2 precision-form measurement")
+    ap.add_argument("--rows", action="store_true",
+                    help="measure the loop's extensions (conductors, emitters, Boltzmann solvers) instead")
     args = ap.parse_args()
+    if args.rows:
+        run_rows(args)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     if args.impl == "reference":

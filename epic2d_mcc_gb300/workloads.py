@@ -11,6 +11,10 @@ configurations the project is measured on:
   PCG to 1e-10, MCC against 1e20 m^-3 neutrals with the synthetic 1000-point
   log-spaced table below.
 * ``periodic_1024`` — 1024x1024 cells, 100 particles per cell per species.
+* ``conductors_64``, ``emitters_128``, ``gshybrid_64``, ``hybrid_24`` — one deck
+  per extension of the loop (conductors with the SOR solver and absorbing walls,
+  emitters with absorbing walls and PCG, the two Boltzmann-electron solvers),
+  for their per-step measurements (``bench.py --rows``).
 * ``twostream_1024`` — the precision form's plasma: 1024x1024 periodic cells,
   100 particles per cell per species (1.05e8 ions of 1836 m_e at 0.05 eV,
   1.05e8 electrons at 2 eV in two halves drifting at +-3 v_th,e), dt 0.05/wpe,
@@ -134,6 +138,64 @@ def deck(name: str) -> str:
               "ion,%.8E,%d,0.05,1,0,0,0,random" % (1836 * ME, n * n * ppc)]
         return _TEMPLATE.format(num_ts=500, dt=0.05, n=n, solver="cg", tol="1e-10", maxit=100000,
                                 solver_extra="", bc="pbc", coll="false", gas="1e20", species="\n".join(sp))
+    if name in ROW_DECKS:
+        return row_deck(name)
+    raise KeyError(name)
+
+
+def _sections(text: str, grids=(), emitters=()) -> str:
+    """[Grids] and [Emitters] entries in the reference's keys (src/main.cpp:284-355)."""
+    g = ["grid_count = %d" % len(grids)]
+    for i, d in enumerate(grids):
+        g += ["grid_%d.%s = %s" % (i, k, v) for k, v in d.items()]
+    e = ["count = %d" % len(emitters)]
+    for i, d in enumerate(emitters):
+        e += ["emitter_%d.%s = %s" % (i, k, v) for k, v in d.items()]
+    text = text.replace("[Grids]\ngrid_count = 0", "[Grids]\n" + "\n".join(g))
+    return text.replace("[Emitters]\ncount = 0", "[Emitters]\n" + "\n".join(e))
+
+
+ROW_DECKS = ("conductors_64", "emitters_128", "gshybrid_64", "hybrid_24")
+
+
+def row_deck(name: str) -> str:
+    def plasma(n, ppc, te=1.0):
+        return ["electron,%.8E,%d,%g,-1,1,0,0,random" % (ME, n * n * ppc, te),
+                "ion,%.8E,%d,0.026,1,0,0,0,random" % (1836 * ME, n * n * ppc)]
+    if name == "conductors_64":
+        # a biased plate and a ring of six electrodes; SOR (the solver the
+        # conductors act on), absorbing walls
+        n = 64
+        grids = [dict(type="reactconduct", min_x=18, max_x=21, min_y=12, max_y=52, grid_voltage=10),
+                 dict(type="circular", x_center=42, y_center=32, electrode_number=6, grid_radius=10,
+                      electrod_radius=2, electrode_voltage=-5)]
+        text = _TEMPLATE.format(num_ts=1000, dt=0.01, n=n, solver="gs", tol="1e-6", maxit=200000,
+                                solver_extra="sor_omega = 1.8\n", bc="open", coll="false", gas="1e20",
+                                species="\n".join(plasma(n, 100, 2.0)))
+        return _sections(text, grids=grids)
+    if name == "emitters_128":
+        # an electron-ion source on the left wall and an ion source in the
+        # middle, 2,000 + 500 points a step; absorbing walls, PCG
+        n = 128
+        em = [dict(x0=1, y0=16, x1=1, y1=112, temp=0.5, numparticle=2000, vdx=0.5, vdy=0, species_idx1=0,
+                   species_idx2=1),
+              dict(x0=60, y0=60, x1=68, y1=68, temp=0.02, numparticle=500, vdx=0, vdy=0.2, species_idx1=1,
+                   species_idx2=1)]
+        text = _TEMPLATE.format(num_ts=1000, dt=0.01, n=n, solver="cg", tol="1e-10", maxit=100000,
+                                solver_extra="", bc="open", coll="false", gas="1e20",
+                                species="\n".join(plasma(n, 50)))
+        return _sections(text, emitters=em)
+    if name == "gshybrid_64":
+        n = 64
+        return _TEMPLATE.format(num_ts=1000, dt=0.01, n=n, solver="gshybrid", tol="1e-6", maxit=200000,
+                                solver_extra="sor_omega = 1.8\n", bc="pbc", coll="false", gas="1e20",
+                                species="\n".join(plasma(n, 50, 2.0)))
+    if name == "hybrid_24":
+        # nrpcgsolver builds dense n x n matrices in the reference: small grids only
+        n = 24
+        return _TEMPLATE.format(num_ts=1000, dt=0.01, n=n, solver="hybrid", tol="1e-6", maxit=100000,
+                                solver_extra="", bc="pbc", coll="false", gas="1e20",
+                                species="\n".join(plasma(n, 50, 2.0)))
     raise KeyError(name)
 
 
