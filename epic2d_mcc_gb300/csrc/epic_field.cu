@@ -269,10 +269,21 @@ __device__ __forceinline__ double nr_row(int nx, int ny, int k, double diag, con
   return sum;
 }
 
-__device__ double nr_serial_dot(const double* u, const double* v, int n, double* s_out) {
+// vec::operator* (sum += u[i] * v[i] in index order, each product rounded).
+// With prod (shared memory for n doubles) the products are formed by all
+// threads first - the same rounded values - so the one serial chain reads
+// them from shared memory instead of waiting on global loads.
+__device__ double nr_serial_dot(const double* u, const double* v, int n, double* s_out, double* prod) {
+  if (prod) {
+    for (int k = threadIdx.x; k < n; k += blockDim.x) prod[k] = u[k] * v[k];
+    __syncthreads();
+  }
   if (threadIdx.x == 0) {
     double r = 0;
-    for (int i = 0; i < n; i++) r += u[i] * v[i];
+    if (prod)
+      for (int i = 0; i < n; i++) r += prod[i];
+    else
+      for (int i = 0; i < n; i++) r += u[i] * v[i];
     *s_out = r;
   }
   __syncthreads();
@@ -281,7 +292,10 @@ __device__ double nr_serial_dot(const double* u, const double* v, int n, double*
   return r;
 }
 
+constexpr int NRPCG_SMEM_MAX = 200 * 1024;  // products staged in shared memory up to this many bytes
+
 __global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
+  extern __shared__ double s_prod[];
   __shared__ double s_dot;
   const int nx = a.g.nx, ny = a.g.ny, n = nx * ny;
   const double dx2 = a.g.dx * a.g.dx;
@@ -295,6 +309,7 @@ __global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
   }
   __syncthreads();
   const int maxit = n < 10000 ? n : 10000;
+  double* const prod = (size_t)n * sizeof(double) <= (size_t)NRPCG_SMEM_MAX ? s_prod : nullptr;
   long long total = 0;
   for (int it = 0; it < 10; it++) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) rhovec[k] = rhovec[k] + exp(x[k]) * K;
@@ -307,19 +322,19 @@ __global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
       p[k] = r[k];
     }
     __syncthreads();
-    double r02 = nr_serial_dot(r, r, n, &s_dot);
+    double r02 = nr_serial_dot(r, r, n, &s_dot, prod);
     for (int i = 0; i < maxit; i++) {
       if (sqrt(r02) < 1e-4) break;
       for (int k = threadIdx.x; k < n; k += blockDim.x) Ap[k] = nr_row(nx, ny, k, J[k], p);
       __syncthreads();
-      const double pAp = nr_serial_dot(p, Ap, n, &s_dot);
+      const double pAp = nr_serial_dot(p, Ap, n, &s_dot, prod);
       const double alpha = r02 / pAp;
       for (int k = threadIdx.x; k < n; k += blockDim.x) {
         y[k] = y[k] + p[k] * alpha;
         r[k] = r[k] - Ap[k] * alpha;
       }
       __syncthreads();
-      const double r12 = nr_serial_dot(r, r, n, &s_dot);
+      const double r12 = nr_serial_dot(r, r, n, &s_dot, prod);
       const double beta = r12 / r02;
       for (int k = threadIdx.x; k < n; k += blockDim.x) p[k] = r[k] + p[k] * beta;
       __syncthreads();
@@ -338,7 +353,12 @@ __global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
   }
 }
 
-void launch_nrpcg(cudaStream_t st, const SolverArgs& a) { k_nrpcg<<<1, 1024, 0, st>>>(a); }
+void launch_nrpcg(cudaStream_t st, const SolverArgs& a) {
+  const size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
+  const int smem = bytes <= (size_t)NRPCG_SMEM_MAX ? (int)bytes : 0;
+  if (smem > 48 * 1024) cudaFuncSetAttribute(k_nrpcg, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  k_nrpcg<<<1, 1024, smem, st>>>(a);
+}
 
 // ------------------------------------------------------ grid barrier ---
 // Cooperative launches guarantee that all blocks are resident.  bar[0] counts
