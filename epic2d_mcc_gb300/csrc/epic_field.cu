@@ -126,7 +126,7 @@ __device__ double block_sum_1024(double v, double* sm) {
 }
 
 // Residual of src/field.cpp:121-134 over the interior (one block).
-template <bool FLUID>
+template <bool FLUID, bool UNIT = false>
 __device__ double sor_residual(const SolverArgs& a, const double* phi, double* red) {
   const int nx = a.g.nx, ny = a.g.ny;
   const double dx2 = a.g.dx * a.g.dx, dy2 = a.g.dy * a.g.dy;
@@ -135,8 +135,12 @@ __device__ double sor_residual(const SolverArgs& a, const double* phi, double* r
   for (int q = threadIdx.x; q < ni; q += blockDim.x) {
     int i = 1 + q / (ny - 2), j = 1 + q % (ny - 2);
     int k = i * ny + j;
-    double R = ((phi[k + ny] - 2 * phi[k] + phi[k - ny]) / dx2) + ((phi[k + 1] - 2 * phi[k] + phi[k - 1]) / dy2) +
-               (FLUID ? a.rho[k] - exp(phi[k]) : a.rho[k]) * a.K;
+    double tx = phi[k + ny] - 2 * phi[k] + phi[k - ny], ty = phi[k + 1] - 2 * phi[k] + phi[k - 1];
+    if (!UNIT) {  // x / 1 is x: unit cells skip the divisions, bit for bit
+      tx = tx / dx2;
+      ty = ty / dy2;
+    }
+    double R = (tx + ty) + (FLUID ? a.rho[k] - exp(phi[k]) : a.rho[k]) * a.K;
     sum += R * R;
   }
   sum = block_sum_1024(sum, red);
@@ -145,13 +149,21 @@ __device__ double sor_residual(const SolverArgs& a, const double* phi, double* r
 
 // FLUID: gsfluidsolver (src/field.cpp:7-68), Boltzmann electrons: the source
 // is (rho - exp(phi)) K and the residual is checked every 50 sweeps.
-template <bool FLUID>
+// UNIT: dx = dy = 1 (every normalisation of the reference), where the
+// divisions by dx^2 and dy^2 are identities and are skipped - bit for bit the
+// same iterates, without the two FP64 divisions per node update that bound
+// this one-SM kernel.  use_smem: phi in shared memory; 2: rho K as well,
+// formed once per solve (the same product as in every sweep).
+template <bool FLUID, bool UNIT>
 __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_smem) {
   extern __shared__ double smem[];
   __shared__ double red[40];
   const int nx = a.g.nx, ny = a.g.ny;
   const int nn = nx * ny;
   double* phi = use_smem ? smem : a.phi;
+  double* const rK = !FLUID && use_smem == 2 ? smem + nn : nullptr;
+  if (rK)
+    for (int k = threadIdx.x; k < nn; k += blockDim.x) rK[k] = a.rho[k] * a.K;
   const double dx2 = a.g.dx * a.g.dx, dy2 = a.g.dy * a.g.dy;
   const double coeff = (2 / dx2) + (2 / dy2);
   const double inv_coeff = 1 / coeff;
@@ -181,8 +193,13 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_s
           if (ai > a1) continue;
           int i = ai + 1, j = d - ai + 1;
           int k = i * ny + j;
-          double phi_new = inv_coeff * ((FLUID ? a.rho[k] - exp(phi[k]) : a.rho[k]) * a.K +
-                                        ((phi[k + ny] + phi[k - ny]) / dx2) + ((phi[k + 1] + phi[k - 1]) / dy2));
+          double tx = phi[k + ny] + phi[k - ny], ty = phi[k + 1] + phi[k - 1];
+          if (!UNIT) {
+            tx = tx / dx2;
+            ty = ty / dy2;
+          }
+          const double src = FLUID ? (a.rho[k] - exp(phi[k])) * a.K : (rK ? rK[k] : a.rho[k] * a.K);
+          double phi_new = inv_coeff * ((src + tx) + ty);
           phi[k] = phi[k] + a.omega * (phi_new - phi[k]);
         }
         __syncthreads();
@@ -190,7 +207,7 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_s
       const int last = iter + S - 1;
       iter += S;
       if (last % P == 0) {
-        L2 = sor_residual<FLUID>(a, phi, red);
+        L2 = sor_residual<FLUID, UNIT>(a, phi, red);
         if (L2 < a.tol) {
           converged = 1;
           break;
@@ -213,15 +230,21 @@ constexpr size_t SOR_SMEM_MAX = 200 * 1024;
 void init_field_kernels() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(k_sor_lex<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
-  cudaFuncSetAttribute(k_sor_lex<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
   done = true;
 }
 
+static bool sor_unit(const SolverArgs& a) { return a.g.dx == 1.0 && a.g.dy == 1.0; }
+
 void launch_sor_lex(cudaStream_t st, const SolverArgs& a) {
-  size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
-  int use_smem = bytes <= SOR_SMEM_MAX;
-  k_sor_lex<false><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
+  const size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
+  const int use_smem = 2 * bytes <= SOR_SMEM_MAX ? 2 : bytes <= SOR_SMEM_MAX ? 1 : 0;
+  const size_t smem = use_smem * bytes;
+  if (sor_unit(a)) k_sor_lex<false, true><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
+  else k_sor_lex<false, false><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
 }
 
 // gsfluidsolver's edge values of rho (src/field.cpp:22-32): bottom 0, top
@@ -241,9 +264,10 @@ __global__ void k_gsfluid_edges(Geom g, double* rho, double top) {
 
 void launch_gsfluid(cudaStream_t st, const SolverArgs& a, double* rho) {
   k_gsfluid_edges<<<1, 256, 0, st>>>(a.g, rho, 10000 * (QE / (K_B * (QE / K_B))));
-  size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
-  int use_smem = bytes <= SOR_SMEM_MAX;
-  k_sor_lex<true><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
+  const size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
+  const int use_smem = bytes <= SOR_SMEM_MAX;
+  if (sor_unit(a)) k_sor_lex<true, true><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
+  else k_sor_lex<true, false><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
 }
 
 // ------------------------------------------------------ Newton hybrid ---
