@@ -19,6 +19,10 @@ the GPU-resident workload.  Prints one JSON line.
                bandwidth.
 * cpu_baseline — the oracle's C restatement of the reference loop timed on
                this host for a bounded sample of the same workload.
+* extension_rows — conductors, emitters and the two Boltzmann-electron
+               solvers, each on its own deck (10 steps after 3 warm-up), with
+               the oracle on one host core beside them (--no-rows skips;
+               --rows runs only these).
 * --impl reference — the reference's CPU implementation of the loop (the
                restatement, or the reference's own objects where they were
                compiled on this machine) on the same workload, one full loop
@@ -394,6 +398,13 @@ def run_ours(args, rank, world):
     if not args.no_precision_form:
         precision_form = run_precision_form(E, PRECISION_WORKLOAD, PRECISION_STEPS)
 
+    rows = None
+    if rank == 0 and world == 1 and not args.no_rows:
+        try:  # the extensions on their own decks (10 steps each), the oracle beside them
+            rows = measure_rows(10, 3, 12.0)
+        except Exception as exc:  # recorded, not fatal to the headline line
+            rows = {"error": repr(exc)}
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         v, done, n, kind = cpu_port_run(ini, None, 0, budget_s=args.cpu_seconds)
@@ -414,7 +425,7 @@ def run_ours(args, rank, world):
                         "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
                 "mixed_precision": mixed, "serving": serving, "batching": batching,
-                "precision_form": precision_form}
+                "precision_form": precision_form, "extension_rows": rows}
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -620,10 +631,10 @@ ROWS = (("conductors (SOR, absorbing walls, erase on hit)", "conductors_64"),
         ("nrpcgsolver (solvertype = hybrid)", "hybrid_24"))
 
 
-def run_rows(args):
+def measure_rows(steps, warmup, cpu_seconds):
     """Per-step throughput of each extension of the loop on its own deck: the
     GPU loop (CUDA events on the handle's stream, FP64 form) and the oracle
-    restatement on one host core beside it.  Prints one JSON line."""
+    restatement on one host core beside it (cpu_seconds over all rows)."""
     import torch
 
     import epic2d_mcc_gb300 as E
@@ -637,7 +648,7 @@ def run_rows(args):
         sim.load_particles(0)
         sim.initial_field()
         nsp = len(sim.species)
-        for _ in range(args.warmup):
+        for _ in range(warmup):
             sim.run(1, collisions=False, graph=False)
         stream = torch.cuda.ExternalStream(sim.stream)
         n0 = sum(sim.num_particles(s) for s in range(nsp))
@@ -645,17 +656,22 @@ def run_rows(args):
         ev0 = torch.cuda.Event(enable_timing=True)
         ev1 = torch.cuda.Event(enable_timing=True)
         ev0.record(stream)
-        sim.run(args.steps, collisions=False, graph=False)
+        sim.run(steps, collisions=False, graph=False)
         ev1.record(stream)
         ev1.synchronize()
         ms = ev0.elapsed_time(ev1)
         n1 = sum(sim.num_particles(s) for s in range(nsp))
-        gpu = 0.5 * (n0 + n1) * args.steps / (ms * 1e-3)
-        cpu, done, n, _ = cpu_port_run(ini, None, 1, budget_s=args.cpu_seconds / len(ROWS))
-        out.append({"row": label, "workload": name, "particles": int(0.5 * (n0 + n1)), "gpu_ms_per_step": ms / args.steps,
+        gpu = 0.5 * (n0 + n1) * steps / (ms * 1e-3)
+        cpu, done, n, _ = cpu_port_run(ini, None, 1, budget_s=cpu_seconds / len(ROWS))
+        out.append({"row": label, "workload": name, "particles": int(0.5 * (n0 + n1)), "gpu_ms_per_step": ms / steps,
                     "gpu_particle_steps_per_s": gpu, "cpu_particle_steps_per_s": cpu, "cpu_steps_timed": done,
                     "cpu_cores": 1, "speedup": gpu / cpu})
         del sim
+    return out
+
+
+def run_rows(args):
+    out = measure_rows(args.steps, args.warmup, args.cpu_seconds)
     print(json.dumps({"rows": out, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
                       "data": "synthetic (particles loaded from mt19937 seed 0, as the reference's Init)"}),
           flush=True)
@@ -674,6 +690,7 @@ def main():
     ap.add_argument("--no-serve", action="store_true", help="skip the serving measurement")
     ap.add_argument("--no-batch", action="store_true", help="skip the batching measurement")
     ap.add_argument("--no-precision-form", action="store_true", help="skip the 1024^2 precision-form measurement")
+    ap.add_argument("--no-rows", action="store_true", help="skip the extension-row measurements")
     ap.add_argument("--rows", action="store_true",
                     help="measure the loop's extensions (conductors, emitters, Boltzmann solvers) instead")
     args = ap.parse_args()
