@@ -338,7 +338,7 @@ epic_status do_efield(epic_sim* s) {
   return EPIC_OK;
 }
 
-epic_status do_push(epic_sim* s, int i, int sub_cycle) {
+epic_status do_push(epic_sim* s, int i, int sub_cycle, const SelectArgs* sel = nullptr) {
   PhaseTimer t(s, 4);
   epic_species_state& sp = s->sp[i];
   const epic_config& c = s->cfg;
@@ -367,7 +367,7 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle) {
     if (dep) CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
     launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, s->ef_cell, qmK, cc, dtsub, s->d_flags,
                 s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED,
-                dep ? sp.acc : nullptr, sp.fx_scale);
+                dep ? sp.acc : nullptr, sp.fx_scale, dep ? sel : nullptr);
     sp.acc_valid = dep;
   }
   s->launches += 1;
@@ -406,7 +406,7 @@ epic_status ensure_mcc_events(epic_sim* s, long long e_cap) {
   return EPIC_OK;
 }
 
-epic_status do_mcc(epic_sim* s, int e, int ion, const double* d_uniforms, int ustride) {
+epic_status do_mcc(epic_sim* s, int e, int ion, const double* d_uniforms, int ustride, int skip_select = 0) {
   PhaseTimer t(s, 5);
   if (!s->cs.tot) return fail(EPIC_ERR_INVALID, "cross sections not set (epic_set_reference_cross_sections)");
   epic_species_state& E = s->sp[e];
@@ -420,8 +420,9 @@ epic_status do_mcc(epic_sim* s, int e, int ion, const double* d_uniforms, int us
   if (mode == EPIC_MCC_INJECTED && !d_uniforms) mode = EPIC_MCC_PHILOX;
   const ParticleRef er{s->mixed, E.soa, E.mx}, ir{s->mixed, I.soa, I.mx};
   launch_mcc(s->stream, mode, s->cs, er, E.d_n, E.cap, ir, I.d_n, I.cap, c.vel_norm, c.DT / c.W, I.desc.mass,
-             I.desc.temp, d_uniforms, ustride, c.seed, s->d_step, s->mcc_ev, s->d_ncoll, s->d_flags, s->part_grid);
-  s->launches += 5;
+             I.desc.temp, d_uniforms, ustride, c.seed, s->d_step, s->mcc_ev, s->d_ncoll, s->d_flags, s->part_grid,
+             skip_select);
+  s->launches += skip_select ? 4 : 5;
   CKL();
   return EPIC_OK;
 }
@@ -513,15 +514,30 @@ epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
   if ((st = do_finalize(s, FINALIZE_AND_RHO, -1))) return st;
   if ((st = do_solve(s))) return st;
   if ((st = do_efield(s))) return st;
+  // The MCC's selection pass folded into the electrons' push (the same test on
+  // the same post-push velocities, one pass over them fewer).
+  const bool coll = with_collisions && nsp >= 2;
+  const bool presel = coll && fused && s->cfg.push_order == EPIC_PUSH_CONTRACTED && s->cs.tot &&
+                      !(s->cfg.ionfixed == 1 && s->sp[0].name == "ion");
+  SelectArgs sel{};
+  if (presel) {
+    if (s->mcc_ev_for_cap < s->sp[0].cap && (st = ensure_mcc_events(s, s->sp[0].cap))) return st;
+    const int mode = s->cfg.mcc_mode == EPIC_MCC_INJECTED ? EPIC_MCC_PHILOX : s->cfg.mcc_mode;
+    mcc_select_cut(s->cs, mode, s->cfg.DT / s->cfg.W, &sel.cut53, &sel.bin_cut);
+    sel.seed = s->cfg.seed;
+    sel.d_step = s->d_step;
+    sel.cand = s->mcc_ev.cand;
+    sel.cand_count = s->mcc_ev.cand_count;
+  }
   for (int i = 0; i < nsp; i++) {
     if (s->cfg.ionfixed == 1 && s->sp[i].name == "ion") continue;
-    if ((st = do_push(s, i, 1))) return st;
+    if ((st = do_push(s, i, 1, presel && i == 0 ? &sel : nullptr))) return st;
   }
-  if (with_collisions && nsp >= 2) {
+  if (coll) {
     if (fused)  // counts before the MCC: its ionisation products are deposited after it
       for (int k = 0; k < 2; k++)
         CK(cudaMemcpyAsync(s->d_nold + k, s->sp[k].d_n, sizeof(long long), cudaMemcpyDeviceToDevice, s->stream));
-    if ((st = do_mcc(s, 0, 1, nullptr, 0))) return st;
+    if ((st = do_mcc(s, 0, 1, nullptr, 0, presel))) return st;
     if (fused) {
       PhaseTimer t(s, 0);
       for (int k = 0; k < 2; k++) {

@@ -36,6 +36,34 @@ struct Philox {
   __device__ double next() { return (double)next53() * (1.0 / 9007199254740992.0); }
 };
 
+// Speed bin (MCC_SPEED_BINS) from the unbiased exponent e and the top two
+// fraction bits q of m = max |v_i|.
+__device__ __forceinline__ int speed_bin_of(int e, int q) {
+  if (e < MCC_BIN_EMIN) return 0;
+  if (e > MCC_BIN_EMAX) return MCC_SPEED_BINS - 1;
+  return 1 + 4 * (e - MCC_BIN_EMIN) + q;
+}
+
+// The speed bin of an FP64 velocity, on the integer pipe.
+__device__ __forceinline__ int speed_bin_fp64(double vx, double vy, double vz) {
+  const unsigned long long M = 0x7FFFFFFFFFFFFFFFull;
+  const unsigned long long a = (unsigned long long)__double_as_longlong(vx) & M;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(vy) & M;
+  const unsigned long long c = (unsigned long long)__double_as_longlong(vz) & M;
+  const unsigned long long m = max(a, max(b, c));
+  return speed_bin_of((int)(m >> 52) - 1023, (int)((m >> 50) & 3));
+}
+
+// The MCC's first pass for electron q (Philox mode): its first draw against the
+// cut of its speed bin (or cut53 for every bin without a table).
+__device__ __forceinline__ bool mcc_candidate(const SelectArgs& s, long long q, unsigned long long step, double vx,
+                                              double vy, double vz) {
+  const unsigned long long cut = s.bin_cut ? __ldg(&s.bin_cut[speed_bin_fp64(vx, vy, vz)]) : s.cut53;
+  Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)s.seed, (uint32_t)(s.seed >> 32), 0,
+             make_uint4(0, 0, 0, 0)};
+  return src.next53() < cut;
+}
+
 
 // Ordered tile scan (decoupled look-back).  Tiles are claimed in increasing
 // order through an atomic counter, so every tile a block waits on belongs to a

@@ -154,15 +154,17 @@ void launch_emit(cudaStream_t st, const SoA& p, const long long* d_n, long long 
                  int grid);
 void launch_emit_commit(cudaStream_t st, long long* d_n, long long num, long long cap, int* flags);
 void launch_inject_tick(cudaStream_t st, unsigned long long* d_inj);
+struct SelectArgs;
 // The FP64 push.  ef is the node field; cell the bilinear coefficients of
 // each cell (launch_cell_coef), which the contracted CIC push reads instead.
 // With dep_acc (periodic or reflective walls) every pushed particle is also
 // deposited at its new position into dep_acc (fixed point, fx_scale), which
-// the caller has zeroed: the next step's charge deposit, bit for bit.
+// the caller has zeroed: the next step's charge deposit, bit for bit.  With
+// sel as well (contracted push, electrons) it also runs the MCC's selection.
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n,
                  const double2* ef, const double2* cell, double qmK, double c, double dtsub, int* flags,
                  unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract,
-                 unsigned long long* dep_acc = nullptr, double fx_scale = 0.0);
+                 unsigned long long* dep_acc = nullptr, double fx_scale = 0.0, const SelectArgs* sel = nullptr);
 // The fixed-point deposit of particles [*d_from, *d_n) (the products an MCC
 // call appended) into acc.
 void launch_deposit_range(cudaStream_t st, const Geom& g, int shape, const SoA& p, const long long* d_from,
@@ -191,10 +193,27 @@ struct McEvents {
 };
 // d_step: device step counter (Philox counter word), advanced by every MCC
 // launch so replayed graphs draw fresh numbers.
+// skip_select: the candidates are already in ev (the electrons' push selected
+// them, Philox mode, FP64 form).
 void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const ParticleRef& e, long long* d_ne,
                 long long e_cap, const ParticleRef& ion, long long* d_ni, long long i_cap, double vel_norm,
                 double dt_phys, double ion_mass, double ion_temp, const double* uniforms, int ustride, uint64_t seed,
-                unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid);
+                unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid,
+                int skip_select = 0);
+// The first-draw cut of the MCC's selection: cut53 for every speed, and the
+// per-speed-bin table (or null).
+void mcc_select_cut(const CrossSections& cs, int mode, double dt_phys, unsigned long long* cut53,
+                    const unsigned long long** bin_cut);
+// The MCC's selection pass run inside the electrons' push: the candidates of
+// the step's MCC (Philox mode) appended to cand.
+struct SelectArgs {
+  const unsigned long long* bin_cut;
+  unsigned long long cut53;
+  uint64_t seed;
+  const unsigned long long* d_step;
+  unsigned int* cand;
+  unsigned int* cand_count;
+};
 size_t ion_event_bytes();
 
 // ---- mixed-precision particle kernels (epic_mixed.cu) ----

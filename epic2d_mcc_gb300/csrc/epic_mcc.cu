@@ -79,25 +79,10 @@ struct IonEvent {
 
 // Particle layouts the MCC runs on: FP64 positions and velocities, or the
 // mixed form's cell index + FP32 offsets and FP32 velocities.
-// Speed bin (MCC_SPEED_BINS) from the unbiased exponent e and the top two
-// fraction bits q of m = max |v_i|.
-__device__ __forceinline__ int speed_bin_of(int e, int q) {
-  if (e < MCC_BIN_EMIN) return 0;
-  if (e > MCC_BIN_EMAX) return MCC_SPEED_BINS - 1;
-  return 1 + 4 * (e - MCC_BIN_EMIN) + q;
-}
-
 struct Fp64Particles {
   SoA p;
   // Integer operations on the bits only (FP64 issues slowly on GB300).
-  __device__ int speed_bin(long long q) const {
-    const unsigned long long M = 0x7FFFFFFFFFFFFFFFull;
-    const unsigned long long a = (unsigned long long)__double_as_longlong(p.vx[q]) & M;
-    const unsigned long long b = (unsigned long long)__double_as_longlong(p.vy[q]) & M;
-    const unsigned long long c = (unsigned long long)__double_as_longlong(p.vz[q]) & M;
-    const unsigned long long m = max(a, max(b, c));
-    return speed_bin_of((int)(m >> 52) - 1023, (int)((m >> 50) & 3));
-  }
+  __device__ int speed_bin(long long q) const { return speed_bin_fp64(p.vx[q], p.vy[q], p.vz[q]); }
   __device__ void load_v(long long q, double& a, double& b, double& c) const { a = p.vx[q]; b = p.vy[q]; c = p.vz[q]; }
   __device__ void store_v(long long q, double a, double b, double c) const { p.vx[q] = a; p.vy[q] = b; p.vz[q] = c; }
   __device__ void load_pos(long long q, double& a, double& b, double& c) const { a = p.x[q]; b = p.y[q]; c = 0; }
@@ -493,9 +478,12 @@ template <class P>
 static void launch_mcc_t(cudaStream_t st, int mode, const CrossSections& cs, const P& e, long long* d_ne,
                          long long e_cap, const P& ion, long long* d_ni, long long i_cap, const MccParams& m,
                          const double* uniforms, int ustride, uint64_t seed, unsigned long long* d_step,
-                         const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid) {
+                         const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid, int skip_select) {
   unsigned long long* pending = d_ncoll + 1;
-  if (mode == EPIC_MCC_INJECTED) {
+  if (skip_select) {  // the push selected the candidates (mcc_candidate)
+    k_mcc_collide<EPIC_MCC_PHILOX, P><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
+                                                                      pending, flags);
+  } else if (mode == EPIC_MCC_INJECTED) {
     k_mcc_select<EPIC_MCC_INJECTED, P><<<grid, PART_THREADS, 0, st>>>(m, e, d_ne, uniforms, ustride, seed, d_step, ev);
     k_mcc_collide<EPIC_MCC_INJECTED, P><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
                                                                         pending, flags);
@@ -509,10 +497,20 @@ static void launch_mcc_t(cudaStream_t st, int mode, const CrossSections& cs, con
   k_mcc_commit<<<1, 1, 0, st>>>(d_ne, e_cap, d_ni, i_cap, pending, d_ncoll, d_step, ev, flags);
 }
 
+void mcc_select_cut(const CrossSections& cs, int mode, double dt_phys, unsigned long long* cut53,
+                    const unsigned long long** bin_cut) {
+  const double p_null = 1 - exp(-cs.nu_max * dt_phys);
+  const bool null_collision = mode == EPIC_MCC_NULL;
+  const double p_cut = null_collision ? p_null : fmin(1.0, p_null * (1 + 1e-9) + 1e-300);
+  *cut53 = (unsigned long long)ceil(p_cut * 9007199254740992.0);
+  *bin_cut = null_collision ? nullptr : cs.bin_cut;
+}
+
 void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const ParticleRef& e, long long* d_ne,
                 long long e_cap, const ParticleRef& ion, long long* d_ni, long long i_cap, double vel_norm,
                 double dt_phys, double ion_mass, double ion_temp, const double* uniforms, int ustride, uint64_t seed,
-                unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid) {
+                unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid,
+                int skip_select) {
   MccParams m;
   m.vn = vel_norm;
   m.dt_phys = dt_phys;
@@ -523,14 +521,13 @@ void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const Partic
   m.null_collision = mode == EPIC_MCC_NULL;
   const double p_null = 1 - exp(-cs.nu_max * dt_phys);
   m.p_cut = m.null_collision ? p_null : fmin(1.0, p_null * (1 + 1e-9) + 1e-300);
-  m.cut53 = (unsigned long long)ceil(m.p_cut * 9007199254740992.0);
-  m.bin_cut = m.null_collision ? nullptr : cs.bin_cut;
+  mcc_select_cut(cs, mode, dt_phys, &m.cut53, &m.bin_cut);
   if (e.mixed)
     launch_mcc_t(st, mode, cs, MixedParticles{e.m}, d_ne, e_cap, MixedParticles{ion.m}, d_ni, i_cap, m, uniforms,
-                 ustride, seed, d_step, ev, d_ncoll, flags, grid);
+                 ustride, seed, d_step, ev, d_ncoll, flags, grid, 0);
   else
     launch_mcc_t(st, mode, cs, Fp64Particles{e.f}, d_ne, e_cap, Fp64Particles{ion.f}, d_ni, i_cap, m, uniforms,
-                 ustride, seed, d_step, ev, d_ncoll, flags, grid);
+                 ustride, seed, d_step, ev, d_ncoll, flags, grid, skip_select);
 }
 
 

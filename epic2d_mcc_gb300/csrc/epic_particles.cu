@@ -359,16 +359,60 @@ __device__ __forceinline__ bool push_one(const Geom& g, const double2* __restric
   }
 }
 
-template <int SHAPE, int BC, int MAP, bool CONTRACT, bool DEP>
+// SEL: also the MCC's first pass over the pushed electrons (k_mcc_select's
+// test on the new velocities, block-aggregated appends to sel.cand), in rounds
+// that every thread of the CTA takes.
+template <int SHAPE, int BC, int MAP, bool CONTRACT, bool DEP, bool SEL>
 __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long long* __restrict__ d_n,
                                                        const double2* __restrict__ ef, double qmK, double c,
                                                        double dtsub, int* flags, unsigned long long* __restrict__ acc,
-                                                       double fx_scale) {
+                                                       double fx_scale, SelectArgs sel) {
   const long long n = *d_n;
   const PushK k = push_consts(g, qmK, c, dtsub);
   const int wshift = DEP ? weight_shift(fx_scale) : 0;
   const long long stride = (long long)gridDim.x * blockDim.x;
   bool bad = false;
+  if (SEL) {
+    __shared__ unsigned int s_cnt[PART_THREADS / 32];
+    __shared__ unsigned int s_base;
+    const unsigned long long step = *sel.d_step;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const long long nround = (n + stride - 1) / stride;
+    for (long long rd = 0; rd < nround; rd++) {
+      const long long q = rd * stride + (long long)blockIdx.x * blockDim.x + threadIdx.x;
+      bool cand = false;
+      if (q < n) {
+        double x = p.x[q], y = p.y[q], vx = p.vx[q], vy = p.vy[q];
+        push_one<SHAPE, BC, MAP, CONTRACT>(g, ef, qmK, c, dtsub, k, x, y, vx, vy, bad);
+        p.x[q] = x;
+        p.y[q] = y;
+        p.vx[q] = vx;
+        p.vy[q] = vy;
+        if (DEP)
+          bad |= !deposit_one<SHAPE, true, MAP != MAP_GENERAL, MAP == MAP_ORIGIN>(g, x, y, 0.0, acc, fx_scale,
+                                                                                  wshift);
+        cand = mcc_candidate(sel, q, step, vx, vy, p.vz[q]);
+      }
+      const unsigned int mask = __ballot_sync(0xffffffffu, cand);
+      if (lane == 0) s_cnt[wid] = (unsigned int)__popc(mask);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        unsigned int tot = 0;
+#pragma unroll
+        for (int w = 0; w < PART_THREADS / 32; w++) {
+          const unsigned int cw = s_cnt[w];
+          s_cnt[w] = tot;
+          tot += cw;
+        }
+        s_base = tot ? atomicAdd(sel.cand_count, tot) : 0u;
+      }
+      __syncthreads();
+      if (cand) sel.cand[s_base + s_cnt[wid] + __popc(mask & ((1u << lane) - 1))] = (unsigned int)q;
+      __syncthreads();
+    }
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) set_flag(flags, FLAG_OUT_OF_GRID);
+    return;
+  }
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += stride) {
     double x = p.x[q], y = p.y[q], vx = p.vx[q], vy = p.vy[q];
     push_one<SHAPE, BC, MAP, CONTRACT>(g, ef, qmK, c, dtsub, k, x, y, vx, vy, bad);
@@ -466,10 +510,28 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, lo
 void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p, long long* d_n, const double2* ef,
                  const double2* cell, double qmK, double c, double dtsub, int* flags,
                  unsigned long long* tile_status, unsigned int* tile_ctr, int grid, int contract,
-                 unsigned long long* dep_acc, double fx_scale) {
+                 unsigned long long* dep_acc, double fx_scale, const SelectArgs* sel) {
   if (shape == EPIC_CIC && contract) ef = cell;
-#define PUSH2(SH, B, U, C, D) \
-  k_push<SH, B, U, C, D><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags, dep_acc, fx_scale)
+  if (sel && dep_acc && contract && (bc == EPIC_PBC || bc == EPIC_REFLECTIVE)) {
+#define SEL3(SH, B, U) \
+  k_push<SH, B, U, true, true, true><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags, dep_acc, \
+                                                                    fx_scale, *sel)
+#define SEL2(SH, B)                                        \
+  do {                                                     \
+    const int map = push_map(g);                           \
+    if (map == MAP_ORIGIN) SEL3(SH, B, 2);                 \
+    else if (map == MAP_UNIT) SEL3(SH, B, 1);              \
+    else SEL3(SH, B, 0);                                   \
+  } while (0)
+    if (shape == EPIC_NGP) { if (bc == EPIC_PBC) SEL2(EPIC_NGP, EPIC_PBC); else SEL2(EPIC_NGP, EPIC_REFLECTIVE); }
+    else { if (bc == EPIC_PBC) SEL2(EPIC_CIC, EPIC_PBC); else SEL2(EPIC_CIC, EPIC_REFLECTIVE); }
+#undef SEL2
+#undef SEL3
+    return;
+  }
+#define PUSH2(SH, B, U, C, D)                                                                                    \
+  k_push<SH, B, U, C, D, false><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, flags, dep_acc, \
+                                                               fx_scale, SelectArgs{})
 #define PUSH1(SH, B, U, C) do { if (dep_acc) PUSH2(SH, B, U, C, true); else PUSH2(SH, B, U, C, false); } while (0)
 #define PUSH(SH, B, U) do { if (contract) PUSH1(SH, B, U, true); else PUSH1(SH, B, U, false); } while (0)
 #define COMPACT1(SH, U, C)                                                                                      \

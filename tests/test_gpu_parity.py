@@ -408,6 +408,38 @@ def test_deposit_in_push_equals_separate_deposit(gpu_lib, tmp_path, bc):
         assert np.array_equal(sims[0].grid("phi"), other.grid("phi"))
 
 
+@pytest.mark.parametrize("bc", ["pbc", "reflective"])
+def test_mcc_select_in_push_equals_separate_select(gpu_lib, tmp_path, bc):
+    """epic_step runs the MCC's selection inside the electrons' push; the same loop body through the per-phase
+    calls (scatter, rho, solve, E, push, handle_collisions) runs it as the MCC's own pass. Same particles and
+    potential, bit for bit, over steps that collide and ionise."""
+    ini = decks.write(decks.deck(nx=32, ny=32, ne=20000, ni=20000, solver="cg", tol="1e-10", bc=bc, te=30,
+                                 collisions=True, gas="1e22", ion_mass="6.63352090e-26"), str(tmp_path))
+    sims = []
+    for _ in range(2):
+        sim = make_sim(gpu_lib, ini)
+        sim.set_reference_cross_sections()
+        sim.load_particles(0)
+        sim.initial_field()
+        sims.append(sim)
+    a, b = sims
+    ncoll = 0
+    for _ in range(3):
+        a.step(collisions=True)
+        for k in range(2):
+            b.scatter_species(k)
+        b.compute_rho()
+        b.potential_solver()
+        b.calculate_efield()
+        for k in range(2):
+            b.push_species(k)
+        ncoll += b.handle_collisions()
+    assert ncoll > 0 and b.particles(1).shape[0] > 20000
+    for k in range(2):
+        assert np.array_equal(a.particles(k), b.particles(k))
+    assert np.array_equal(a.grid("phi"), b.grid("phi"))
+
+
 def test_multi_step_tracks_oracle(gpu_lib, tmp_path):
     """Ten loop iterations (GS, pbc): still within 1e-9 of the restatement."""
     ini = decks.write(decks.deck(nx=32, ny=32, ne=20000, ni=20000, tol="1e-10"), str(tmp_path))
