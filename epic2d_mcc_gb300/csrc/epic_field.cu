@@ -43,21 +43,19 @@ __global__ void k_finalize(FinalizeArgs a) {
   const int nn = nx * ny;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const int i = k / ny, j = k - i * ny;
-    double vals[8];
+    // One pass over the species: each density, then its charge added to rho
+    // in species order (no per-thread array, which would live in local memory).
+    double rho = 0;
     for (int s = 0; s < a.nsp; s++) {
       double v;
       if (a.stage == RHO_FROM_DEN || !a.active[s]) {
-        vals[s] = a.den[s][k];
-        continue;
+        v = a.den[s][k];
+      } else {
+        auto raw = [&](int ii, int jj) { return raw_den(a, s, ii, jj); };
+        v = fold_density(a.bc, nx, ny, raw, i, j);
+        a.den[s][k] = v;
       }
-      auto raw = [&](int ii, int jj) { return raw_den(a, s, ii, jj); };
-      v = fold_density(a.bc, nx, ny, raw, i, j);
-      vals[s] = v;
-    }
-    double rho = 0;
-    for (int s = 0; s < a.nsp; s++) {
-      if (a.stage != RHO_FROM_DEN && a.active[s]) a.den[s][k] = vals[s];
-      double t = vals[s] * a.charge_over_qe[s];
+      double t = v * a.charge_over_qe[s];
       rho = rho + t;
     }
     if (a.stage != FINALIZE_ONLY) a.rho[k] = rho;
