@@ -419,6 +419,7 @@ def run_ours(args, rank, world):
                 "config": {"workload": args.workload, "particles": int(0.5 * (n_before + n_after)),
                            "grid": [g.nx, g.ny], "solver": "PCG tol 1e-10 (cold start, as the reference)",
                            "mcc": "direct MCC, Philox uniforms, 1000-point log table" if coll else "off",
+                           "push": "FP64, contracted (multiply-adds; within a few ulps of the reference's order)",
                            "l2": "inputs larger than L2 (particles %.0f MB)" % (n_before * 40 / 1e6),
                            "parallelism": "replicas" if world > 1 else "single GPU"},
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
