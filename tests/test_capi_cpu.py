@@ -148,3 +148,20 @@ def test_emitters_from_ini_cpu(tmp_path):
     e = es[0]
     assert (e.x0, e.y0, e.x1, e.y1, e.temp, e.numparticle) == (1, 20, 1, 30, 0, 5)
     assert (e.species_idx1, e.species_idx2) == (0, 1)
+
+
+@pytest.mark.parametrize("name", ["conductors_64", "emitters_128", "gshybrid_64", "hybrid_24"])
+def test_row_decks_parse(E, name, tmp_path):
+    """The extension decks bench.py measures parse as the reference reads them, with the solver, walls,
+    conductors and emitters they are meant to exercise, and agree with the oracle's set-up."""
+    from epic2d_mcc_gb300 import workloads
+
+    ini = decks.write(workloads.deck(name), str(tmp_path))
+    cfg, descs, _ = E.config_from_ini(ini)
+    s = O.setup(ini)
+    assert (cfg.nx, cfg.ny) == (s.nx, s.ny) and cfg.DT == s.DT and len(descs) == 2
+    gs, pcg, gshybrid, hybrid = 0, 1, 2, 3  # EPIC_SOLVER_* (include/epic2d.h)
+    pbc, open_ = 0, 1                       # EPIC_PBC, EPIC_OPEN
+    want = {"conductors_64": (gs, open_, 2, 0), "emitters_128": (pcg, open_, 0, 2),
+            "gshybrid_64": (gshybrid, pbc, 0, 0), "hybrid_24": (hybrid, pbc, 0, 0)}[name]
+    assert (cfg.solver, cfg.bc, len(E.conductors_from_ini(ini)), len(E.emitters_from_ini(ini))) == want
