@@ -23,6 +23,7 @@ CIC, NGP = 0, 1
 PBC, OPEN, REFLECTIVE = 0, 1, 2
 SOLVER_GS, SOLVER_PCG = 0, 1
 SOR_LEXICOGRAPHIC, SOR_REDBLACK = 0, 1
+POISSON_DIRICHLET, POISSON_PERIODIC, POISSON_DIRICHLET_X = 0, 1, 2
 DEPOSIT_FIXED, DEPOSIT_FP64 = 0, 1
 MCC_PHILOX, MCC_INJECTED, MCC_NULL = 0, 1, 2
 GRID = {"phi": 0, "rho": 1, "efx": 2, "efy": 3}
@@ -47,7 +48,8 @@ class Config(ctypes.Structure):
                 ("sor_omega", ctypes.c_double), ("sor_mode", ctypes.c_int), ("deposit_mode", ctypes.c_int),
                 ("mcc_mode", ctypes.c_int), ("seed", ctypes.c_uint64), ("warm_start", ctypes.c_int),
                 ("solver_blocks", ctypes.c_int), ("precision", ctypes.c_int), ("sort_every", ctypes.c_int),
-                ("push_order", ctypes.c_int), ("reserved", ctypes.c_int * 12)]
+                ("push_order", ctypes.c_int), ("poisson_bc", ctypes.c_int), ("load_3v", ctypes.c_int),
+                ("reserved", ctypes.c_int * 10)]
 
 
 class SpeciesDesc(ctypes.Structure):

@@ -295,6 +295,8 @@ __device__ __forceinline__ SpecLattice run_lattice(const BatchSpec& b, int ri) {
   L.C = r.C;
   L.flat = r.flat;
   L.gs_norm = r.gs_norm;
+  L.mode = EPIC_POISSON_DIRICHLET;  // batches run the reference's boundary
+  L.bmean = nullptr;
   L.dx2 = r.dx * r.dx;
   L.K = r.K;
   L.tol = r.tol;
@@ -666,7 +668,7 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
       b->gas_density = c.gas_density;
     }
     const Geom g{c.nx, c.ny, c.x0, c.y0, c.dx, c.dy, 0, 0};
-    if (!spectral_supported(g, c.solver)) return bfail(EPIC_ERR_INVALID, "run %d: grid not supported", r);
+    if (c.poisson_bc != EPIC_POISSON_DIRICHLET || !spectral_supported(g, c.solver, c.poisson_bc)) return bfail(EPIC_ERR_INVALID, "run %d: grid not supported", r);
     if (c.nx > 4095 || c.ny > 4095) return bfail(EPIC_ERR_INVALID, "run %d: grid too large for a batch", r);
     BRun& br = b->runs[r];
     std::memset(&br, 0, sizeof(br));

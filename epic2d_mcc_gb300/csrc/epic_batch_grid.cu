@@ -42,7 +42,9 @@ __global__ void k_batch_efield(BatchGrids b) {
     const double* phi = b.phi + r.node_off;
     double ex = b.efx[k], ey = b.efy[k];
     auto PHI = [&](int a_, int b_) { return phi[a_ * ny + b_]; };
-    efield_node(r.bc, nx, ny, r.dx, r.dy, PHI, i, j, ex, ey);
+    int xr, yr;
+    efield_edges(r.bc, EPIC_POISSON_DIRICHLET, &xr, &yr);
+    efield_node(xr, yr, nx, ny, r.dx, r.dy, PHI, i, j, ex, ey);
     b.efx[k] = ex;
     b.efy[k] = ey;
     b.ef32[k] = make_float2((float)ex, (float)ey);

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -127,30 +128,66 @@ static void sine_transform(int n, std::vector<float>& Q, std::vector<double>& la
   }
 }
 
+// The periodic counterpart: the orthonormal, symmetric Hartley transform
+// H_jk = (cos(2 pi j k / n) + sin(2 pi j k / n)) / sqrt(n), which diagonalises
+// the circulant tridiag(1, -2, 1) with eigenvalues -4 sin^2(pi k / n) (cos
+// and sin modes of wavenumber k share the eigenvalue, so their sum is an
+// eigenvector).
+static void hartley_transform(int n, std::vector<float>& Q, std::vector<double>& lam) {
+  const double pi = 3.14159265358979323846;
+  const double c = 1.0 / std::sqrt((double)n);
+  Q.assign((size_t)n * n, 0.f);
+  lam.assign(n, 0.0);
+  for (int j = 0; j < n; j++) {
+    for (int k = 0; k < n; k++) {
+      const double t = 2.0 * pi * (double)(((long long)j * k) % n) / n;
+      Q[(size_t)j * n + k] = (float)(c * (std::cos(t) + std::sin(t)));
+    }
+    const double sn = std::sin(pi * j / n);
+    lam[j] = -4.0 * sn * sn;
+  }
+}
+
 epic_status setup_spectral(epic_sim* s) {
   SpectralSolver& sp = s->spec;
   const bool gs = s->cfg.solver == EPIC_SOLVER_GS;
+  const int mode = s->cfg.poisson_bc;
+  sp.mode = mode;
   sp.flat = !gs;
   sp.gs_norm = gs;
   sp.R = gs ? s->cfg.nx - 2 : s->cfg.ny;
   sp.C = gs ? s->cfg.ny - 2 : s->cfg.nx;
+  if (mode != EPIC_POISSON_DIRICHLET) {  // the extension lattice (Lattice), the same for both solvers
+    sp.flat = 0;
+    sp.R = mode == EPIC_POISSON_PERIODIC ? s->cfg.nx - 1 : s->cfg.nx - 2;
+    sp.C = s->cfg.ny - 1;
+  }
   const int R = sp.R, C = sp.C;
   std::vector<float> QR, QC, D((size_t)R * C);
   std::vector<double> lamR, lamC;
-  sine_transform(R, QR, lamR);
-  sine_transform(C, QC, lamC);
+  if (mode == EPIC_POISSON_PERIODIC) hartley_transform(R, QR, lamR);
+  else sine_transform(R, QR, lamR);
+  if (mode == EPIC_POISSON_DIRICHLET) sine_transform(C, QC, lamC);
+  else hartley_transform(C, QC, lamC);
   for (int p = 0; p < R; p++)
-    for (int q = 0; q < C; q++) D[(size_t)p * C + q] = (float)(1.0 / (lamR[p] + lamC[q]));
+    for (int q = 0; q < C; q++) {
+      const double l = lamR[p] + lamC[q];
+      // The constant mode of the periodic lattice is the operator's null space:
+      // the right-hand side has none (projected), the correction gets none.
+      D[(size_t)p * C + q] = l == 0.0 ? 0.f : (float)(1.0 / l);
+    }
   CK(cudaMallocAsync((void**)&sp.QR, QR.size() * sizeof(float), s->stream));
-  if (C == R) sp.QC = sp.QR;
+  if (C == R && mode != EPIC_POISSON_DIRICHLET_X) sp.QC = sp.QR;
   else CK(cudaMallocAsync((void**)&sp.QC, QC.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.D, D.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.t0, D.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.t1, D.size() * sizeof(float), s->stream));
-  CK(cudaMallocAsync((void**)&sp.partials, std::max(256, spectral_chunks(sp)) * sizeof(double), s->stream));
+  // chunk sums, then the periodic right-hand side's mean
+  CK(cudaMallocAsync((void**)&sp.partials, std::max(256, spectral_chunks(sp) + 1) * sizeof(double), s->stream));
   CK(cudaMallocAsync((void**)&sp.state, 4 * sizeof(int), s->stream));
   CK(cudaMemcpyAsync(sp.QR, QR.data(), QR.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
-  if (C != R) CK(cudaMemcpyAsync(sp.QC, QC.data(), QC.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
+  if (sp.QC != sp.QR)
+    CK(cudaMemcpyAsync(sp.QC, QC.data(), QC.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
   CK(cudaMemcpyAsync(sp.D, D.data(), D.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
   CK(cudaMemsetAsync(sp.state, 0, 4 * sizeof(int), s->stream));
   CK(cudaStreamSynchronize(s->stream));  // host temporaries
@@ -283,6 +320,7 @@ SolverArgs solver_args(epic_sim* s) {
   a.partials = s->partials;
   a.bar = s->bar;
   a.warm = s->cfg.warm_start;
+  a.poisson_bc = s->cfg.poisson_bc;
   return a;
 }
 
@@ -321,14 +359,15 @@ epic_status do_solve(epic_sim* s) {
                                             : pcg_default_blocks(nnodes(s), s->num_sms);
     launch_pcg(s->stream, a, nb);
   }
-  s->launches += 1;
+  s->launches += s->cfg.poisson_bc != EPIC_POISSON_DIRICHLET ? 2 : 1;  // + the duplicated nodes' fill
   CKL();
   return EPIC_OK;
 }
 
 epic_status do_efield(epic_sim* s) {
   PhaseTimer t(s, 3);
-  launch_efield(s->stream, s->g, s->cfg.bc, s->phi, s->efx, s->efy, s->ef, s->mixed ? s->ef32 : nullptr);
+  launch_efield(s->stream, s->g, s->cfg.bc, s->cfg.poisson_bc, s->phi, s->efx, s->efy, s->ef,
+                s->mixed ? s->ef32 : nullptr);
   s->launches += 1;
   if (s->ef_cell) {
     launch_cell_coef(s->stream, s->g, s->ef, s->ef_cell);
@@ -461,10 +500,12 @@ epic_status do_sort(epic_sim* s, int i) {
 
 // Emitter::inject of every emitter (src/emitter.cpp:5-36); d_uniforms: null
 // for Philox, else device rows of 14 per point, emitters in order.
-epic_status do_inject(epic_sim* s, const double* d_uniforms) {
+// Emitters [k0, k1) in order; tick: advance the injection counter that keys
+// their Philox streams (once per loop iteration, after the last emitter).
+epic_status do_inject_range(epic_sim* s, size_t k0, size_t k1, const double* d_uniforms, bool tick) {
   const epic_config& c = s->cfg;
   const double* u = d_uniforms;
-  for (size_t k = 0; k < s->emitters.size(); k++) {
+  for (size_t k = k0; k < k1; k++) {
     const epic_emitter& m = s->emitters[k];
     const int sp_of[2] = {m.species_idx1, m.species_idx2};
     const int slots = m.species_idx1 != m.species_idx2 ? 2 : 1;
@@ -491,10 +532,16 @@ epic_status do_inject(epic_sim* s, const double* d_uniforms) {
     s->launches += 2 * slots;
     if (u) u += (size_t)m.numparticle * 14;
   }
-  launch_inject_tick(s->stream, s->d_inj);
-  s->launches += 1;
+  if (tick) {
+    launch_inject_tick(s->stream, s->d_inj);
+    s->launches += 1;
+  }
   CKL();
   return EPIC_OK;
+}
+
+epic_status do_inject(epic_sim* s, const double* d_uniforms) {
+  return do_inject_range(s, 0, s->emitters.size(), d_uniforms, true);
 }
 
 // sort: -1 by the step counter and cfg.sort_every, 0 never, 1 always.
@@ -556,11 +603,19 @@ epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
 
 namespace epic {
 void set_last_error(const char* msg) { g_err = msg; }
+
+static std::atomic<long long> g_spin_limit{SPIN_LIMIT};
+long long spin_limit() { return g_spin_limit.load(std::memory_order_relaxed); }
 }  // namespace epic
 
 extern "C" {
 
 const char* epic_last_error(void) { return g_err.c_str(); }
+
+epic_status epic_set_spin_limit(long long polls) {
+  g_spin_limit.store(polls > 0 ? polls : SPIN_LIMIT, std::memory_order_relaxed);
+  return EPIC_OK;
+}
 
 void epic_config_defaults(epic_config* c) {
   std::memset(c, 0, sizeof(*c));
@@ -601,6 +656,8 @@ epic_status epic_conductors_from_ini(const char* path, epic_conductor* out, int 
 epic_status epic_add_conductor(epic_sim* s, const epic_conductor* c) {
   if (!s || !c) return fail(EPIC_ERR_INVALID, "bad argument");
   if (s->mixed) return fail(EPIC_ERR_INVALID, "conductors are supported in the FP64 form");
+  if (s->cfg.poisson_bc != EPIC_POISSON_DIRICHLET)
+    return fail(EPIC_ERR_INVALID, "conductors are supported with the reference's Poisson boundary");
   if (c->type != EPIC_CONDUCTOR_RECT && c->type != EPIC_CONDUCTOR_CIRCULAR)
     return fail(EPIC_ERR_INVALID, "unknown conductor type %d", c->type);
   if (c->type == EPIC_CONDUCTOR_CIRCULAR && (c->electrode_number < 1 || c->electrode_number > 4096))
@@ -687,6 +744,22 @@ epic_status epic_inject(epic_sim* s, const double* uniforms) {
   return sync(s);
 }
 
+epic_status epic_inject_emitter(epic_sim* s, int k, const double* uniforms) {
+  if (!s || k < 0 || k >= (int)s->emitters.size()) return fail(EPIC_ERR_INVALID, "bad emitter index");
+  invalidate_acc(s);
+  const double* d_u = nullptr;
+  if (uniforms) {
+    const size_t rows = (size_t)s->emitters[(size_t)k].numparticle;
+    epic_status st = ensure_staging(s, std::max<size_t>(1, rows * 14 * sizeof(double)));
+    if (st) return st;
+    CK(cudaMemcpyAsync(s->staging, uniforms, rows * 14 * sizeof(double), cudaMemcpyHostToDevice, s->stream));
+    d_u = (const double*)s->staging;
+  }
+  epic_status st = do_inject_range(s, (size_t)k, (size_t)k + 1, d_u, k + 1 == (int)s->emitters.size());
+  if (st) return st;
+  return sync(s);
+}
+
 epic_status epic_ini_get(const char* path, const char* section, const char* key, char* out, int len) {
   if (!path || !section || !key || !out || len < 1) return fail(EPIC_ERR_INVALID, "bad argument");
   std::string v, err;
@@ -708,6 +781,15 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   if (cfg->solver < EPIC_SOLVER_GS || cfg->solver > EPIC_SOLVER_HYBRID) return fail(EPIC_ERR_INVALID, "bad solver");
   if (cfg->push_order != EPIC_PUSH_CONTRACTED && cfg->push_order != EPIC_PUSH_REFERENCE)
     return fail(EPIC_ERR_INVALID, "bad push_order");
+  if (cfg->poisson_bc < EPIC_POISSON_DIRICHLET || cfg->poisson_bc > EPIC_POISSON_DIRICHLET_X)
+    return fail(EPIC_ERR_INVALID, "bad poisson_bc");
+  if (cfg->poisson_bc != EPIC_POISSON_DIRICHLET) {
+    if (cfg->nx < 5 || cfg->ny < 5) return fail(EPIC_ERR_INVALID, "poisson_bc periodic/dirichlet_x needs 5x5 nodes");
+    if (!(cfg->solver == EPIC_SOLVER_PCG ||
+          (cfg->solver == EPIC_SOLVER_GS && cfg->sor_mode == EPIC_SOR_LEXICOGRAPHIC)))
+      return fail(EPIC_ERR_INVALID, "poisson_bc periodic/dirichlet_x is supported by the cg and (lexicographic) gs "
+                                    "solvers");
+  }
   int dev = 0;
   CK(cudaGetDevice(&dev));
   init_field_kernels();
@@ -759,7 +841,7 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
   s->mixed = cfg->precision == EPIC_PRECISION_MIXED;
   if (s->mixed) {
     guard(dalloc(s, &s->ef32, nn));
-    if (spectral_supported(s->g, cfg->solver) && !st) guard(setup_spectral(s));
+    if (spectral_supported(s->g, cfg->solver, cfg->poisson_bc) && !st) guard(setup_spectral(s));
   } else if (cfg->shape == EPIC_CIC && cfg->push_order == EPIC_PUSH_CONTRACTED) {
     guard(dalloc(s, &s->ef_cell, 4 * (size_t)nn));
   }
@@ -775,6 +857,7 @@ epic_status epic_create(const epic_config* cfg, epic_sim** out) {
 
 void epic_destroy(epic_sim* s) {
   if (!s) return;
+  if (s->ref_rng) ref_stream_destroy(static_cast<RefStream*>(s->ref_rng));
   if (s->stream) cudaStreamSynchronize(s->stream);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
@@ -925,17 +1008,23 @@ epic_status epic_get_particles(epic_sim* s, int i, double* parts, int64_t capaci
 
 epic_status epic_load_particles(epic_sim* s, uint32_t seed) {
   if (!s) return fail(EPIC_ERR_INVALID, "null handle");
-  std::vector<const epic_species_desc*> d;
-  for (auto& sp : s->sp) d.push_back(&sp.desc);
-  std::vector<std::vector<double>> parts;
-  std::string err;
-  int st = load_particles(s->cfg, d, parts, seed, err, s->conductors);
-  if (st) return fail((epic_status)st, "%s", err.c_str());
-  for (size_t i = 0; i < parts.size(); i++) {
-    epic_status e = epic_set_particles(s, (int)i, parts[i].data(), (int64_t)(parts[i].size() / 5));
+  if (s->ref_rng) ref_stream_destroy(static_cast<RefStream*>(s->ref_rng));
+  s->ref_rng = ref_stream_create(seed);
+  for (size_t i = 0; i < s->sp.size(); i++) {
+    epic_status e = epic_init_species(s, (int)i);
     if (e) return e;
   }
   return EPIC_OK;
+}
+
+epic_status epic_init_species(epic_sim* s, int i) {
+  if (!valid_species(s, i)) return fail(EPIC_ERR_INVALID, "bad species index");
+  if (!s->ref_rng) s->ref_rng = ref_stream_create(0);
+  std::vector<double> parts;
+  std::string err;
+  int st = load_species(s->cfg, s->sp[i].desc, parts, static_cast<RefStream*>(s->ref_rng), err, s->conductors);
+  if (st) return fail((epic_status)st, "%s", err.c_str());
+  return epic_set_particles(s, i, parts.data(), (int64_t)(parts.size() / 5));
 }
 
 epic_status epic_scatter_species(epic_sim* s, int i) {

@@ -67,12 +67,12 @@ __device__ __forceinline__ bool mcc_candidate(const SelectArgs& s, long long q, 
 
 // Ordered tile scan (decoupled look-back).  Tiles are claimed in increasing
 // order through an atomic counter, so every tile a block waits on belongs to a
-// block that is already running; each wait is bounded by SPIN_LIMIT polls.
+// block that is already running; each wait is bounded by `limit` polls.
 // status[t] = (state << 62) | value, state 1 = tile aggregate, 2 = inclusive
 // prefix.  Called by one thread; returns the exclusive prefix of `tile`, or
 // ~0 on timeout (FLAG_TIMEOUT set).
 static __device__ unsigned long long tile_lookback(unsigned long long* status, int tile, unsigned long long count,
-                                            int* flags) {
+                                                   int* flags, long long limit) {
   const unsigned long long MASK = (1ull << 62) - 1;
   if (tile == 0) {
     __threadfence();
@@ -88,7 +88,7 @@ static __device__ unsigned long long tile_lookback(unsigned long long* status, i
     unsigned long long v = *((volatile unsigned long long*)&status[t]);
     unsigned long long st = v >> 62;
     if (st == 0) {
-      if (++spins > SPIN_LIMIT) {
+      if (++spins >= limit) {
         set_flag(flags, FLAG_TIMEOUT);
         return ~0ull;
       }

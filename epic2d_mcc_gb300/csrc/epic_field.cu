@@ -6,6 +6,8 @@
 // the PCG kernel uses explicit fma() where it is documented to.
 #include <cuda_runtime.h>
 
+#include <atomic>
+
 #include <algorithm>
 
 #include "epic_grid.cuh"
@@ -70,16 +72,17 @@ void launch_finalize(cudaStream_t st, const FinalizeArgs& a) {
 }
 
 // ------------------------------------------------------------ E-field ---
-// FieldSolve::CalculateEfield (src/field.cpp:276-330).
-__global__ void k_efield(Geom g, int bc, const double* __restrict__ phi, double* efx, double* efy, double2* ef,
-                         float2* ef32) {
+// FieldSolve::CalculateEfield (src/field.cpp:276-330), edge rules xr, yr
+// (efield_edges).
+__global__ void k_efield(Geom g, int xr, int yr, const double* __restrict__ phi, double* efx, double* efy,
+                         double2* ef, float2* ef32) {
   const int nx = g.nx, ny = g.ny;
   const int nn = nx * ny;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += gridDim.x * blockDim.x) {
     const int i = k / ny, j = k - i * ny;
     double ex = efx[k], ey = efy[k];
     auto PHI = [&](int a_, int b_) { return phi[a_ * ny + b_]; };
-    efield_node(bc, nx, ny, g.dx, g.dy, PHI, i, j, ex, ey);
+    efield_node(xr, yr, nx, ny, g.dx, g.dy, PHI, i, j, ex, ey);
     efx[k] = ex;
     efy[k] = ey;
     ef[k] = make_double2(ex, ey);
@@ -87,10 +90,12 @@ __global__ void k_efield(Geom g, int bc, const double* __restrict__ phi, double*
   }
 }
 
-void launch_efield(cudaStream_t st, const Geom& g, int bc, const double* phi, double* efx, double* efy, double2* ef,
-                   float2* ef32) {
+void launch_efield(cudaStream_t st, const Geom& g, int bc, int poisson_bc, const double* phi, double* efx,
+                   double* efy, double2* ef, float2* ef32) {
   int nn = g.nx * g.ny;
-  k_efield<<<(nn + 255) / 256, 256, 0, st>>>(g, bc, phi, efx, efy, ef, ef32);
+  int xr, yr;
+  efield_edges(bc, poisson_bc, &xr, &yr);
+  k_efield<<<(nn + 255) / 256, 256, 0, st>>>(g, xr, yr, phi, efx, efy, ef, ef32);
 }
 
 // ------------------------------------------------- lexicographic SOR ---
@@ -123,22 +128,108 @@ __device__ double block_sum_1024(double v, double* sm) {
   return t;
 }
 
-// Residual of src/field.cpp:121-134 over the interior (one block).
-template <bool FLUID, bool UNIT = false>
-__device__ double sor_residual(const SolverArgs& a, const double* phi, double* red) {
+// ---- exact dot-product reductions (integer pipe, see epic_xsum.cuh) ----
+// Warp total of 128-bit fixed-point values: five 26-bit limbs (the top one
+// signed) summed with redux.sync — a limb total of 32 lanes stays below 2^31
+// for |v| < 2^122 — and recombined exactly.
+__device__ __forceinline__ xs_int xs_warp_sum(xs_int v) {
+  const xs_uint u = (xs_uint)v;
+  const unsigned M = (1u << 26) - 1;
+  const int l0 = __reduce_add_sync(0xffffffffu, (int)((unsigned)u & M));
+  const int l1 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 26) & M));
+  const int l2 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 52) & M));
+  const int l3 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 78) & M));
+  const int l4 = __reduce_add_sync(0xffffffffu, (int)(v >> 104));
+  const xs_uint s = ((xs_uint)(xs_int)l4 << 104) + ((xs_uint)(unsigned)l3 << 78) + ((xs_uint)(unsigned)l2 << 52) +
+                    ((xs_uint)(unsigned)l1 << 26) + (xs_uint)(unsigned)l0;
+  return (xs_int)s;
+}
+
+// Exact sum of term(q), q in [0, count), over the block (each thread takes a
+// strided share), anchored on the largest exponent and rounded once
+// (epic_xsum.cuh); valid in every thread.
+template <class F>
+__device__ double block_exact_sum(int count, const F& term, double* red) {
+  __shared__ int s_e[32];
+  __shared__ unsigned long long s_v[32][2];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int e = 0;
+  for (int q = threadIdx.x; q < count; q += blockDim.x) e = max(e, xs_exponent(term(q)));
+  e = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
+  if (lane == 0) s_e[wid] = e;
+  __syncthreads();
+  int A = 0;
+  for (int w = 0; w < nw; w++) A = max(A, s_e[w]);
+  xs_int v = 0;
+  for (int q = threadIdx.x; q < count; q += blockDim.x) v += xs_from_double(term(q), A);
+  v = xs_warp_sum(v);
+  if (lane == 0) {
+    s_v[wid][0] = (unsigned long long)(xs_uint)v;
+    s_v[wid][1] = (unsigned long long)((xs_uint)v >> 64);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    xs_uint tot = 0;
+    for (int w = 0; w < nw; w++) tot += ((xs_uint)s_v[w][1] << 64) | s_v[w][0];
+    red[33] = xs_to_double((xs_int)tot, A);
+  }
+  __syncthreads();
+  const double r = red[33];
+  __syncthreads();
+  return r;
+}
+
+// The unknowns of gssolver: the interior i in [1, nx-2], j in [1, ny-2]
+// (the reference), or an extension lattice (EPIC_POISSON_*): i from i0 = 0
+// (PERIODIC) or 1 (DIRICHLET_X) to nx-2, j in [0, ny-2], with wrapped
+// neighbours.  Node indices of the four neighbours of unknown (i, j).
+struct SorLat {
+  int i0, j0, nxi, nyi, wrap_x, wrap_y;
+};
+__device__ __forceinline__ SorLat sor_lattice(int nx, int ny, int poisson_bc) {
+  SorLat l;
+  if (poisson_bc == EPIC_POISSON_DIRICHLET) {
+    l.i0 = 1; l.j0 = 1; l.nxi = nx - 2; l.nyi = ny - 2; l.wrap_x = 0; l.wrap_y = 0;
+  } else {
+    l.wrap_x = poisson_bc == EPIC_POISSON_PERIODIC;
+    l.wrap_y = 1;
+    l.i0 = l.wrap_x ? 0 : 1; l.j0 = 0; l.nxi = nx - 1 - l.i0; l.nyi = ny - 1;
+  }
+  return l;
+}
+template <bool EXT>
+__device__ __forceinline__ void sor_nbrs(const SorLat& l, int nx, int ny, int i, int j, int& kE, int& kW, int& kN,
+                                         int& kS) {
+  const int k = i * ny + j;
+  if (!EXT) {
+    kE = k + ny; kW = k - ny; kN = k + 1; kS = k - 1;
+    return;
+  }
+  kE = (i + 1 < nx - 1 || !l.wrap_x) ? k + ny : j;  // wraps to node (0, j)
+  kW = i > 0 ? k - ny : (nx - 2) * ny + j;
+  kN = j + 1 < ny - 1 ? k + 1 : i * ny;          // wraps to node (i, 0)
+  kS = j > 0 ? k - 1 : i * ny + ny - 2;
+}
+
+// Residual of src/field.cpp:121-134 over the unknowns (one block); src(k) is
+// the source term rho*K (minus its mean when periodic).
+template <bool FLUID, bool UNIT, bool EXT, class Src>
+__device__ double sor_residual(const SolverArgs& a, const SorLat& l, const double* phi, const Src& src, double* red) {
   const int nx = a.g.nx, ny = a.g.ny;
   const double dx2 = a.g.dx * a.g.dx, dy2 = a.g.dy * a.g.dy;
   double sum = 0;
-  const int ni = (nx - 2) * (ny - 2);
+  const int ni = l.nxi * l.nyi;
   for (int q = threadIdx.x; q < ni; q += blockDim.x) {
-    int i = 1 + q / (ny - 2), j = 1 + q % (ny - 2);
+    int i = l.i0 + q / l.nyi, j = l.j0 + q % l.nyi;
     int k = i * ny + j;
-    double tx = phi[k + ny] - 2 * phi[k] + phi[k - ny], ty = phi[k + 1] - 2 * phi[k] + phi[k - 1];
+    int kE, kW, kN, kS;
+    sor_nbrs<EXT>(l, nx, ny, i, j, kE, kW, kN, kS);
+    double tx = phi[kE] - 2 * phi[k] + phi[kW], ty = phi[kN] - 2 * phi[k] + phi[kS];
     if (!UNIT) {  // x / 1 is x: unit cells skip the divisions, bit for bit
       tx = tx / dx2;
       ty = ty / dy2;
     }
-    double R = (tx + ty) + (FLUID ? a.rho[k] - exp(phi[k]) : a.rho[k]) * a.K;
+    double R = (tx + ty) + (FLUID ? (a.rho[k] - exp(phi[k])) * a.K : src(k));
     sum += R * R;
   }
   sum = block_sum_1024(sum, red);
@@ -152,24 +243,47 @@ __device__ double sor_residual(const SolverArgs& a, const double* phi, double* r
 // same iterates, without the two FP64 divisions per node update that bound
 // this one-SM kernel.  use_smem: phi in shared memory; 2: rho K as well,
 // formed once per solve (the same product as in every sweep).
-template <bool FLUID, bool UNIT>
+// EXT: an extension lattice (sor_lattice).  Its wrapped neighbours couple
+// the first and last node of a periodic row or column, so sweep s may start
+// node (i, 0) only after sweep s-1 has passed node (i, nyi-1): sweeps are
+// spaced c = max(nxi or nyi of each periodic direction, 2) diagonals apart
+// instead of 2, which keeps every read at the same sweep as the
+// lexicographic order.  PERIODIC removes the source's mean before and phi's
+// mean after the sweeps (exact sums, rounded once).
+template <bool FLUID, bool UNIT, bool EXT>
 __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_smem) {
   extern __shared__ double smem[];
   __shared__ double red[40];
   const int nx = a.g.nx, ny = a.g.ny;
   const int nn = nx * ny;
+  const SorLat l = sor_lattice(nx, ny, EXT ? a.poisson_bc : EPIC_POISSON_DIRICHLET);
   double* phi = use_smem ? smem : a.phi;
   double* const rK = !FLUID && use_smem == 2 ? smem + nn : nullptr;
   if (rK)
     for (int k = threadIdx.x; k < nn; k += blockDim.x) rK[k] = a.rho[k] * a.K;
+  // PERIODIC: the mean of rho K over the unknowns, removed from the source.
+  const int ni = l.nxi * l.nyi;
+  auto unknown = [&](int q) { return (l.i0 + q / l.nyi) * ny + l.j0 + q % l.nyi; };
+  double smean = 0.0;
+  if (EXT && !FLUID && l.wrap_x) {
+    __syncthreads();
+    smean = block_exact_sum(ni, [&](int q) { const int k = unknown(q); return rK ? rK[k] : a.rho[k] * a.K; }, red) /
+            (double)ni;
+  }
+  auto src = [&](int k) -> double { return (rK ? rK[k] : a.rho[k] * a.K) - smean; };
   const double dx2 = a.g.dx * a.g.dx, dy2 = a.g.dy * a.g.dy;
   const double coeff = (2 / dx2) + (2 / dy2);
   const double inv_coeff = 1 / coeff;
   for (int k = threadIdx.x; k < nn; k += blockDim.x) phi[k] = 0;  // cold start, zero edges (src/field.cpp:78-98)
   __syncthreads();
-  const int nxi = nx - 2, nyi = ny - 2;
+  const int nxi = l.nxi, nyi = l.nyi;
   const int D = nxi + nyi - 1;
   const int Lmax = nxi < nyi ? nxi : nyi;
+  int cp = 2;  // diagonals between consecutive sweeps
+  if (EXT) {
+    if (l.wrap_x && nxi > cp) cp = nxi;
+    if (l.wrap_y && nyi > cp) cp = nyi;
+  }
   int iter = 0, converged = 0;
   double L2 = 0;
   if (nxi > 0 && nyi > 0) {
@@ -177,27 +291,29 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_s
       constexpr int P = FLUID ? 50 : 25;
       int S = iter == 0 ? 1 : P;
       if (S > a.max_iter - iter) S = a.max_iter - iter;
-      const int T = D + 2 * (S - 1);
+      const int T = D + cp * (S - 1);
       for (int t = 0; t < T; t++) {
-        int s_lo = t - D + 1 > 0 ? (t - D + 2) >> 1 : 0;
-        int s_hi = (t >> 1) < S - 1 ? (t >> 1) : S - 1;
+        int s_lo = t - D + 1 > 0 ? (t - D + cp) / cp : 0;
+        int s_hi = t / cp < S - 1 ? t / cp : S - 1;
         int items = (s_hi - s_lo + 1) * Lmax;
         for (int it = threadIdx.x; it < items; it += blockDim.x) {
           int s = s_lo + it / Lmax, q = it % Lmax;
-          int d = t - 2 * s;
+          int d = t - cp * s;
           int a0 = d - (nyi - 1) > 0 ? d - (nyi - 1) : 0;
           int a1 = d < nxi - 1 ? d : nxi - 1;
           int ai = a0 + q;
           if (ai > a1) continue;
-          int i = ai + 1, j = d - ai + 1;
+          int i = ai + l.i0, j = d - ai + l.j0;
           int k = i * ny + j;
-          double tx = phi[k + ny] + phi[k - ny], ty = phi[k + 1] + phi[k - 1];
+          int kE, kW, kN, kS;
+          sor_nbrs<EXT>(l, nx, ny, i, j, kE, kW, kN, kS);
+          double tx = phi[kE] + phi[kW], ty = phi[kN] + phi[kS];
           if (!UNIT) {
             tx = tx / dx2;
             ty = ty / dy2;
           }
-          const double src = FLUID ? (a.rho[k] - exp(phi[k])) * a.K : (rK ? rK[k] : a.rho[k] * a.K);
-          double phi_new = inv_coeff * ((src + tx) + ty);
+          const double sk = FLUID ? (a.rho[k] - exp(phi[k])) * a.K : src(k);
+          double phi_new = inv_coeff * ((sk + tx) + ty);
           phi[k] = phi[k] + a.omega * (phi_new - phi[k]);
         }
         __syncthreads();
@@ -205,13 +321,22 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_s
       const int last = iter + S - 1;
       iter += S;
       if (last % P == 0) {
-        L2 = sor_residual<FLUID, UNIT>(a, phi, red);
+        L2 = sor_residual<FLUID, UNIT, EXT>(a, l, phi, src, red);
         if (L2 < a.tol) {
           converged = 1;
           break;
         }
       }
     }
+  }
+  if (EXT && l.wrap_x) {  // zero-mean gauge over the unknowns
+    __syncthreads();
+    const double m = block_exact_sum(ni, [&](int q) { return phi[unknown(q)]; }, red) / (double)ni;
+    for (int q = threadIdx.x; q < ni; q += blockDim.x) {
+      const int k = unknown(q);
+      phi[k] = phi[k] - m;
+    }
+    __syncthreads();
   }
   if (use_smem)
     for (int k = threadIdx.x; k < nn; k += blockDim.x) a.phi[k] = phi[k];
@@ -228,10 +353,12 @@ constexpr size_t SOR_SMEM_MAX = 200 * 1024;
 void init_field_kernels() {
   static bool done = false;
   if (done) return;
-  cudaFuncSetAttribute(k_sor_lex<false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
-  cudaFuncSetAttribute(k_sor_lex<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
-  cudaFuncSetAttribute(k_sor_lex<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
-  cudaFuncSetAttribute(k_sor_lex<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<false, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<false, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<true, false, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<true, true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<false, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(k_sor_lex<false, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
   done = true;
 }
 
@@ -241,8 +368,14 @@ void launch_sor_lex(cudaStream_t st, const SolverArgs& a) {
   const size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
   const int use_smem = 2 * bytes <= SOR_SMEM_MAX ? 2 : bytes <= SOR_SMEM_MAX ? 1 : 0;
   const size_t smem = use_smem * bytes;
-  if (sor_unit(a)) k_sor_lex<false, true><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
-  else k_sor_lex<false, false><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
+  if (a.poisson_bc != EPIC_POISSON_DIRICHLET) {
+    if (sor_unit(a)) k_sor_lex<false, true, true><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
+    else k_sor_lex<false, false, true><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
+    launch_fill_poisson_nodes(st, a.g, a.poisson_bc, a.phi);
+    return;
+  }
+  if (sor_unit(a)) k_sor_lex<false, true, false><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
+  else k_sor_lex<false, false, false><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
 }
 
 // gsfluidsolver's edge values of rho (src/field.cpp:22-32): bottom 0, top
@@ -264,8 +397,8 @@ void launch_gsfluid(cudaStream_t st, const SolverArgs& a, double* rho) {
   k_gsfluid_edges<<<1, 256, 0, st>>>(a.g, rho, 10000 * (QE / (K_B * (QE / K_B))));
   const size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
   const int use_smem = bytes <= SOR_SMEM_MAX;
-  if (sor_unit(a)) k_sor_lex<true, true><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
-  else k_sor_lex<true, false><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
+  if (sor_unit(a)) k_sor_lex<true, true, false><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
+  else k_sor_lex<true, false, false><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
 }
 
 // ------------------------------------------------------ Newton hybrid ---
@@ -386,8 +519,8 @@ void launch_nrpcg(cudaStream_t st, const SolverArgs& a) {
 // Cooperative launches guarantee that all blocks are resident.  bar[0] counts
 // arrivals since the launch (zeroed before it): the blocks of barrier episode
 // e draw tickets in [e*nb, (e+1)*nb) and wait until the count reaches
-// (e+1)*nb.  Every wait gives up after SPIN_LIMIT polls (FLAG_TIMEOUT), so a
-// fault can never hang the GPU.
+// (e+1)*nb.  Every wait gives up after a bounded number of polls (the
+// launch's SolverArgs::spin; FLAG_TIMEOUT), so a fault can never hang the GPU.
 // The arrival is an atom.add with release semantics and the wait polls with
 // ld.acquire at GPU scope: the block's writes (ordered before thread 0 by
 // __syncthreads) become visible to every block that observes the count, with
@@ -405,7 +538,7 @@ __device__ __forceinline__ unsigned int ld_acquire_gpu(const unsigned int* p) {
   return v;
 }
 
-__device__ bool grid_sync(unsigned int* bar, int* flags) {
+__device__ bool grid_sync(unsigned int* bar, int* flags, long long limit) {
   __shared__ int s_ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -414,7 +547,7 @@ __device__ bool grid_sync(unsigned int* bar, int* flags) {
     int ok = 1;
     long long spins = 0;
     while ((int)(ld_acquire_gpu(bar) - target) < 0) {
-      if (++spins > SPIN_LIMIT) {
+      if (++spins >= limit) {
         atomicOr(flags, FLAG_TIMEOUT);
         ok = 0;
         break;
@@ -553,16 +686,21 @@ __device__ double3 grid_total3_t0(const double* P, int nb) {
 
 __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
   __shared__ double sw[3 * 256];
-  __shared__ double s_alpha, s_beta;
+  __shared__ double s_alpha, s_beta, s_mean;
   __shared__ int s_done;
-  const int nx = a.g.nx, ny = a.g.ny;
-  const int n = nx * ny;
+  // The unknowns as a lattice (Lattice): vectors are indexed by lattice
+  // position q = row * C + col, x lives in phi at the node of q.  For the
+  // reference's lattice q is the node index itself.
+  const Lattice lat = make_lattice(a.g.nx, a.g.ny, a.poisson_bc);
+  const int R = lat.R, C = lat.C;
+  const int n = R * C;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
   const int nb = gridDim.x;
+  const long long spin = spin_or_default(a.spin);
   double* x = a.phi;
   double* b = a.work[0];
-  double* R[2] = {a.work[1], a.work[2]};
+  double* R_[2] = {a.work[1], a.work[2]};
   double* S[2] = {a.work[3], a.work[4]};
   double* W[2] = {a.work[5], a.work[6]};
   double* Pd = a.work[7];
@@ -572,35 +710,74 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
   auto Pb = [&](int e) { return a.partials + (e & 1) * 4 * nb; };
   const double minv = 1.0 / -4.0;
   const double dx2 = a.g.dx * a.g.dx;
+  auto node = [&](int q) { const int row = q / C; return lattice_node(lat, row, q - row * C); };
+  // Lattice neighbours of q (row - 1, col - 1, col + 1, row + 1), or -1.
+  auto nbrs = [&](int q, int& up, int& lf, int& rt, int& dn) {
+    const int row = q / C, col = q - row * C;
+    const int ru = lattice_wrap(row - 1, R, lat.wrap_r), rd = lattice_wrap(row + 1, R, lat.wrap_r);
+    const int cl = lattice_wrap(col - 1, C, lat.wrap_c), cr = lattice_wrap(col + 1, C, lat.wrap_c);
+    up = ru < 0 ? -1 : ru * C + col;
+    dn = rd < 0 ? -1 : rd * C + col;
+    lf = cl < 0 ? -1 : row * C + cl;
+    rt = cr < 0 ? -1 : row * C + cr;
+  };
+
+  // b: the reference's right-hand side (zero on the grid edges) or -rho dx^2 K
+  // on every unknown of an extension lattice; PERIODIC projects it onto zero
+  // mean.
+  double pb = 0;
+  for (int q = tid; q < n; q += stride) {
+    const int k = node(q);
+    double bk;
+    if (lat.mode == EPIC_POISSON_DIRICHLET) {
+      const int i = k / a.g.ny;
+      bk = rhs_at(a, k, i, k - i * a.g.ny, dx2);
+    } else {
+      bk = -a.rho[k] * dx2 * a.K;
+    }
+    b[q] = bk;
+    pb += bk;
+  }
+  if (lat.mode == EPIC_POISSON_PERIODIC) {
+    block_partial3(pb, 0.0, 0.0, Pb(ep), sw);
+    if (!grid_sync(a.bar, a.flags, spin)) return;
+    double3 t = grid_total3_t0(Pb(ep++), nb);
+    if (threadIdx.x == 0) s_mean = t.x / (double)n;
+    __syncthreads();
+    const double bm = s_mean;
+    for (int q = tid; q < n; q += stride) b[q] = b[q] - bm;
+  }
+  if (!grid_sync(a.bar, a.flags, spin)) return;
 
   // set-up: x = 0, r = b - A*0, u = M r, w = A u, p = s = 0.
   double pg = 0, pd = 0, pr = 0;
-  for (int k = tid; k < n; k += stride) {
-    const int i = k / ny, j = k - i * ny;
-    const int row = k / nx, col = k - row * nx;
-    const double bk = rhs_at(a, k, i, j, dx2);
-    b[k] = bk;
-    x[k] = 0;
-    const double rk = bk - 0.0;
+  for (int q = tid; q < n; q += stride) {
+    x[node(q)] = 0;
+    const double rk = __ldcg(&b[q]) - 0.0;
     const double uk = minv * rk;
+    int up, lf, rt, dn;
+    nbrs(q, up, lf, rt, dn);
     double sum = 0;
-    if (row > 0) { int m = k - nx, mi = m / ny; sum += minv * rhs_at(a, m, mi, m - mi * ny, dx2); }
-    if (col > 0) { int m = k - 1, mi = m / ny; sum += minv * rhs_at(a, m, mi, m - mi * ny, dx2); }
+    if (up >= 0) sum += minv * __ldcg(&b[up]);
+    if (lf >= 0) sum += minv * __ldcg(&b[lf]);
     sum = fma(-4.0, uk, sum);
-    if (col < nx - 1) { int m = k + 1, mi = m / ny; sum += minv * rhs_at(a, m, mi, m - mi * ny, dx2); }
-    if (row < ny - 1) { int m = k + nx, mi = m / ny; sum += minv * rhs_at(a, m, mi, m - mi * ny, dx2); }
-    R[0][k] = rk;
-    W[0][k] = sum;
-    S[0][k] = 0;
-    Pd[k] = 0;
+    if (rt >= 0) sum += minv * __ldcg(&b[rt]);
+    if (dn >= 0) sum += minv * __ldcg(&b[dn]);
+    R_[0][q] = rk;
+    W[0][q] = sum;
+    S[0][q] = 0;
+    Pd[q] = 0;
     pg = fma(rk, uk, pg);
     pd = fma(sum, uk, pd);
     pr = fma(rk, rk, pr);
   }
   block_partial3(pg, pd, pr, Pb(ep), sw);
-  if (!grid_sync(a.bar, a.flags)) return;
+  if (!grid_sync(a.bar, a.flags, spin)) return;
+  // min(n*n, max_iteration) as pcg() caps it: n*n in 32-bit int arithmetic for
+  // the reference's lattice (it wraps, as there), in 64 bits for the extensions.
   unsigned int cap32 = (unsigned int)n * (unsigned int)n;
-  const int maxit = (int)cap32 < a.max_iter ? (int)cap32 : a.max_iter;
+  const long long cap = lat.mode == EPIC_POISSON_DIRICHLET ? (long long)(int)cap32 : (long long)n * n;
+  const int maxit = cap < a.max_iter ? (int)cap : a.max_iter;
   double alpha = 0, gamma_prev = 0;  // thread 0 only
   int it = 0, cur = 0;
   // Thread 0, after each reduction: the stopping test on r.r and the scalars
@@ -628,46 +805,48 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
   }
   while (it < maxit && !s_done) {
     const double al = s_alpha, be = s_beta;
-    const double* Rc = R[cur];
+    const double* Rc = R_[cur];
     const double* Sc = S[cur];
     const double* Wc = W[cur];
-    double* Rn = R[cur ^ 1];
+    double* Rn = R_[cur ^ 1];
     double* Sn = S[cur ^ 1];
     double* Wn = W[cur ^ 1];
     pg = pd = pr = 0;
-    for (int k = tid; k < n; k += stride) {
-      const int row = k / nx, col = k - row * nx;
-      const double rc = __ldcg(&Rc[k]);
-      const double sk = fma(be, __ldcg(&Sc[k]), __ldcg(&Wc[k]));
-      const double pk = fma(be, Pd[k], minv * rc);
+    for (int q = tid; q < n; q += stride) {
+      const int k = node(q);
+      const double rc = __ldcg(&Rc[q]);
+      const double sk = fma(be, __ldcg(&Sc[q]), __ldcg(&Wc[q]));
+      const double pk = fma(be, Pd[q], minv * rc);
       x[k] = fma(al, pk, x[k]);
       const double rk = fma(-al, sk, rc);
       const double uk = minv * rk;
       // w_new = A u_new; a neighbour's u_new from its previous r, w, s.  The
       // loads use clamped indices so all of them issue before the first
       // use; missing neighbours are then skipped as in the reference.
+      int up, lf, rt, dn;
+      nbrs(q, up, lf, rt, dn);
 #define UNEW(m) (minv * fma(-al, fma(be, __ldcg(&Sc[m]), __ldcg(&Wc[m])), __ldcg(&Rc[m])))
-      const double uN = UNEW(row > 0 ? k - nx : k);
-      const double uW = UNEW(col > 0 ? k - 1 : k);
-      const double uE = UNEW(col < nx - 1 ? k + 1 : k);
-      const double uS = UNEW(row < ny - 1 ? k + nx : k);
+      const double uN = UNEW(up >= 0 ? up : q);
+      const double uW = UNEW(lf >= 0 ? lf : q);
+      const double uE = UNEW(rt >= 0 ? rt : q);
+      const double uS = UNEW(dn >= 0 ? dn : q);
 #undef UNEW
       double sum = 0;
-      if (row > 0) sum += uN;
-      if (col > 0) sum += uW;
+      if (up >= 0) sum += uN;
+      if (lf >= 0) sum += uW;
       sum = fma(-4.0, uk, sum);
-      if (col < nx - 1) sum += uE;
-      if (row < ny - 1) sum += uS;
-      Pd[k] = pk;
-      Sn[k] = sk;
-      Rn[k] = rk;
-      Wn[k] = sum;
+      if (rt >= 0) sum += uE;
+      if (dn >= 0) sum += uS;
+      Pd[q] = pk;
+      Sn[q] = sk;
+      Rn[q] = rk;
+      Wn[q] = sum;
       pg = fma(rk, uk, pg);
       pd = fma(sum, uk, pd);
       pr = fma(rk, rk, pr);
     }
     block_partial3(pg, pd, pr, Pb(ep), sw);
-    if (!grid_sync(a.bar, a.flags)) return;
+    if (!grid_sync(a.bar, a.flags, spin)) return;
     cur ^= 1;
     it++;
     {
@@ -676,43 +855,60 @@ __global__ void __launch_bounds__(256) k_pcg(SolverArgs a) {
       __syncthreads();
     }
   }
-  // domain.error = |A x - b| / n (src/field.cpp:258-259); x is complete
-  // everywhere after the last barrier.
-  double pe = 0;
-  for (int k = tid; k < n; k += stride) {
-    const int row = k / nx, col = k - row * nx;
+  // domain.error = |A x - b| / n (src/field.cpp:258-259, n = nx ny); x is
+  // complete everywhere after the last barrier.  PERIODIC also totals x for
+  // the zero-mean gauge (the error is that of x before the shift).
+  double pe = 0, px = 0;
+  for (int q = tid; q < n; q += stride) {
+    int up, lf, rt, dn;
+    nbrs(q, up, lf, rt, dn);
+    const int k = node(q);
     double sum = 0;
-    if (row > 0) sum += __ldcg(&x[k - nx]);
-    if (col > 0) sum += __ldcg(&x[k - 1]);
+    if (up >= 0) sum += __ldcg(&x[node(up)]);
+    if (lf >= 0) sum += __ldcg(&x[node(lf)]);
     sum = fma(-4.0, __ldcg(&x[k]), sum);
-    if (col < nx - 1) sum += __ldcg(&x[k + 1]);
-    if (row < ny - 1) sum += __ldcg(&x[k + nx]);
-    const double e = sum - b[k];
+    if (rt >= 0) sum += __ldcg(&x[node(rt)]);
+    if (dn >= 0) sum += __ldcg(&x[node(dn)]);
+    const double e = sum - b[q];
     pe = fma(e, e, pe);
+    px += __ldcg(&x[k]);
   }
-  block_partial3(pe, 0.0, 0.0, Pb(ep), sw);
-  if (!grid_sync(a.bar, a.flags)) return;
+  block_partial3(pe, px, 0.0, Pb(ep), sw);
+  if (!grid_sync(a.bar, a.flags, spin)) return;
   double3 e2 = grid_total3_t0(Pb(ep++), nb);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     a.info->iterations = it;
     a.info->converged = it < maxit;
-    a.info->error = sqrt(e2.x) / n;
+    a.info->error = sqrt(e2.x) / (a.g.nx * a.g.ny);
     atomicAdd(a.iter_total, (unsigned long long)it);
+  }
+  if (lat.mode == EPIC_POISSON_PERIODIC) {
+    if (threadIdx.x == 0) s_mean = e2.y / (double)n;
+    __syncthreads();
+    const double xm = s_mean;
+    for (int q = tid; q < n; q += stride) {
+      const int k = node(q);
+      x[k] = x[k] - xm;
+    }
   }
 }
 
-static int g_pcg_max_blocks = 0;
+// Computed on first use (several host threads may race to do it; they all
+// store the same value).
+static std::atomic<int> g_pcg_max_blocks{0};
 
 int solver_max_blocks() {
-  if (!g_pcg_max_blocks) {
+  int v = g_pcg_max_blocks.load(std::memory_order_relaxed);
+  if (!v) {
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pcg, 256, 0);
     if (per_sm < 1) per_sm = 1;
-    g_pcg_max_blocks = sms * (per_sm < 2 ? per_sm : 2);
+    v = sms * (per_sm < 2 ? per_sm : 2);
+    g_pcg_max_blocks.store(v, std::memory_order_relaxed);
   }
-  return g_pcg_max_blocks;
+  return v;
 }
 
 // ------------------------------------------------------ tiled PCG ---
@@ -766,12 +962,13 @@ __device__ __forceinline__ void bar_arrive(unsigned int* bar) {
 
 // Waits until `target` arrivals are in (bounded: FLAG_TIMEOUT and false on
 // giving up).  Ends with a __syncthreads.
-__device__ __forceinline__ bool bar_wait(unsigned int* bar, int* flags, unsigned int target, int* s_ok) {
+__device__ __forceinline__ bool bar_wait(unsigned int* bar, int* flags, unsigned int target, int* s_ok,
+                                         long long limit) {
   if (threadIdx.x == 0) {
     int ok = 1;
     long long spins = 0;
     while ((int)(ld_acquire_gpu(bar) - target) < 0) {
-      if (++spins > SPIN_LIMIT) {
+      if (++spins >= limit) {
         atomicOr(flags, FLAG_TIMEOUT);
         ok = 0;
         break;
@@ -781,23 +978,6 @@ __device__ __forceinline__ bool bar_wait(unsigned int* bar, int* flags, unsigned
   }
   __syncthreads();
   return *s_ok;
-}
-
-// ---- exact dot-product reductions (integer pipe, see epic_xsum.cuh) ----
-// Warp total of 128-bit fixed-point values: five 26-bit limbs (the top one
-// signed) summed with redux.sync — a limb total of 32 lanes stays below 2^31
-// for |v| < 2^122 — and recombined exactly.
-__device__ __forceinline__ xs_int xs_warp_sum(xs_int v) {
-  const xs_uint u = (xs_uint)v;
-  const unsigned M = (1u << 26) - 1;
-  const int l0 = __reduce_add_sync(0xffffffffu, (int)((unsigned)u & M));
-  const int l1 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 26) & M));
-  const int l2 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 52) & M));
-  const int l3 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 78) & M));
-  const int l4 = __reduce_add_sync(0xffffffffu, (int)(v >> 104));
-  const xs_uint s = ((xs_uint)(xs_int)l4 << 104) + ((xs_uint)(unsigned)l3 << 78) + ((xs_uint)(unsigned)l2 << 52) +
-                    ((xs_uint)(unsigned)l1 << 26) + (xs_uint)(unsigned)l0;
-  return (xs_int)s;
 }
 
 // One CTA's exact partial of two dot products: V = sum * 2^(1129 - a).
@@ -1078,27 +1258,44 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
   __shared__ XScratch sx;
   __shared__ double s_alpha, s_beta;
   __shared__ int s_done, s_ok;
-  const int C = a.g.nx, R = a.g.ny;
+  __shared__ double s_mean;
+  const Lattice lat = make_lattice(a.g.nx, a.g.ny, a.poisson_bc);
+  const int C = lat.C, R = lat.R;
   const int n = C * R;
   const int tr = t.tr, tc = t.tc, ldu = tc + 2;
   const int br = blockIdx.x / t.tiles_c, bc = blockIdx.x - br * t.tiles_c;
   const int r0 = br * tr, c0 = bc * tc;
+  // Valid extent of this tile (the last tile row and column may be partial).
+  const int vr = min(tr, R - r0), vc = min(tc, C - c0);
   const int nb = gridDim.x;
   const double dx2 = a.g.dx * a.g.dx;
+  const long long spin = spin_or_default(a.spin);
   // Partials [2][nb] alternate by reduction parity (a CTA can run at most one
   // reduction ahead of the slowest reader); published edge values likewise:
   // work[1|2] = r, work[3|4] = w, work[5|6] = s.
   XPartial* const P = reinterpret_cast<XPartial*>(a.partials);
   unsigned int target = 0;
+  int ep = 0;  // episodes of the block-anchored reduction (partials parity)
+  // The right-hand side at node k: the reference's (zero on the grid edges),
+  // or -rho dx^2 K on every unknown of an extension lattice.
+  auto rhs = [&](int k) -> double {
+    if (lat.mode == EPIC_POISSON_DIRICHLET) {
+      const int i = k / a.g.ny;
+      return rhs_at(a, k, i, k - i * a.g.ny, dx2);
+    }
+    return -a.rho[k] * dx2 * a.K;
+  };
 
   for (int m = threadIdx.x; m < (tr + 2) * ldu; m += PCG_T) sr[m] = 0.0;
 
   // Edge publication: each tile writes its boundary to an edge buffer of
   // 2 (tc + tr) slots per tile - top row at 0, bottom row at tc, left column
-  // at 2 tc, right column at 2 tc + tr - so that a neighbour reads each side
-  // of its halo ring as one contiguous run (a column of the lattice would be
-  // one scattered load per node).  Tiles are at least 2 x 2 (pcg_tiling), so
-  // a node lies on at most one row side and one column side.
+  // at 2 tc, right column at 2 tc + tr, the bottom row and right column being
+  // the last valid ones - so that a neighbour reads each side of its halo
+  // ring as one contiguous run (a column of the lattice would be one
+  // scattered load per node).  Tiles span at least 2 x 2 valid nodes where a
+  // neighbour can lie beyond them (pcg_tiling), so a node lies on at most one
+  // row side and one column side.
   const int ebase = blockIdx.x * 2 * (tc + tr);
   // Owned slots: tile-local q = threadIdx.x + PCG_T*j, row-major in the tile.
   int kk[NPT], si[NPT], pe0[NPT], pe1[NPT];
@@ -1108,55 +1305,88 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
     const int lr = q / tc, lc = q - lr * tc;
     const int row = r0 + lr, col = c0 + lc;
     const bool valid = q < tr * tc && row < R && col < C;
-    kk[j] = valid ? row * C + col : -1;
+    kk[j] = valid ? lattice_node(lat, row, col) : -1;
     si[j] = (lr + 1) * ldu + lc + 1;
-    const int er = lr == 0 ? ebase + lc : lr == tr - 1 ? ebase + tc + lc : -1;
-    const int ec = lc == 0 ? ebase + 2 * tc + lr : lc == tc - 1 ? ebase + 2 * tc + tr + lr : -1;
+    const int er = lr == 0 ? ebase + lc : lr == vr - 1 ? ebase + tc + lc : -1;
+    const int ec = lc == 0 ? ebase + 2 * tc + lr : lc == vc - 1 ? ebase + 2 * tc + tr + lr : -1;
     pe0[j] = !valid ? -1 : er >= 0 ? er : ec;
     pe1[j] = !valid || er < 0 ? -1 : ec;
   }
-  // Halo slots: top row, bottom row, left column, right column of the ring,
-  // with the node (hk, for the set-up) and the neighbour's edge slot (he).
+  // Halo slots: the ring around the valid extent - above, below, left, right
+  // - with the node (hk, for the set-up) and the neighbour tile's edge slot
+  // (he): the neighbour above publishes its bottom row, the one below its top
+  // row, and so on.  Neighbours wrap around where the lattice is periodic.
   int hk[PCG_HALO_SLOTS], hs[PCG_HALO_SLOTS], he[PCG_HALO_SLOTS];
 #pragma unroll
   for (int j = 0; j < PCG_HALO_SLOTS; j++) {
     const int h = threadIdx.x + PCG_T * j;
-    const int eb = 2 * (tc + tr);
-    int row = -1, col = -1, sr_ = 0, sc = 0, e = -1;
-    if (h < tc) {  // bottom row of the tile above
-      row = r0 - 1; col = c0 + h; sr_ = 0; sc = h + 1; e = (blockIdx.x - t.tiles_c) * eb + tc + h;
-    } else if (h < 2 * tc) {  // top row of the tile below
-      row = r0 + tr; col = c0 + h - tc; sr_ = tr + 1; sc = h - tc + 1; e = (blockIdx.x + t.tiles_c) * eb + h - tc;
-    } else if (h < 2 * tc + tr) {  // right column of the tile to the left
-      row = r0 + h - 2 * tc; col = c0 - 1; sr_ = h - 2 * tc + 1; sc = 0; e = (blockIdx.x - 1) * eb + tr + h;
-    } else if (h < 2 * tc + 2 * tr) {  // left column of the tile to the right
-      row = r0 + h - 2 * tc - tr; col = c0 + tc; sr_ = h - 2 * tc - tr + 1; sc = tc + 1;
-      e = (blockIdx.x + 1) * eb + h - tr;
+    int row = -1, col = -1, side = -1, sr_ = 0, sc = 0;
+    if (h < vc) {
+      side = 0; row = r0 - 1; col = c0 + h; sr_ = 0; sc = h + 1;
+    } else if (h < 2 * vc) {
+      side = 1; row = r0 + vr; col = c0 + h - vc; sr_ = vr + 1; sc = h - vc + 1;
+    } else if (h < 2 * vc + vr) {
+      side = 2; row = r0 + h - 2 * vc; col = c0 - 1; sr_ = h - 2 * vc + 1; sc = 0;
+    } else if (h < 2 * vc + 2 * vr) {
+      side = 3; row = r0 + h - 2 * vc - vr; col = c0 + vc; sr_ = h - 2 * vc - vr + 1; sc = vc + 1;
     }
-    const bool valid = row >= 0 && row < R && col >= 0 && col < C;
-    hk[j] = valid ? row * C + col : -1;
-    he[j] = valid ? e : -1;
+    if (side >= 0) {
+      row = lattice_wrap(row, R, lat.wrap_r);
+      col = lattice_wrap(col, C, lat.wrap_c);
+    }
+    const bool valid = side >= 0 && row >= 0 && col >= 0;
+    int e = -1;
+    if (valid) {
+      const int nbr = row / tr, nbc = col / tc;
+      const int nlr = row - nbr * tr, nlc = col - nbc * tc;
+      const int eslot = side == 0 ? tc + nlc : side == 1 ? nlc : side == 2 ? 2 * tc + tr + nlr : 2 * tc + nlr;
+      e = (nbr * t.tiles_c + nbc) * 2 * (tc + tr) + eslot;
+    }
+    hk[j] = valid ? lattice_node(lat, row, col) : -1;
+    he[j] = e;
     hs[j] = sr_ * ldu + sc;
   }
-  __syncthreads();
 
   // set-up: x = 0, r = b, w = A(M r), p' = s = 0.
   double x[NPT], r[NPT], w[NPT], p[NPT], s[NPT], r_old[NPT];
 #pragma unroll
   for (int j = 0; j < NPT; j++) {
     x[j] = r[j] = w[j] = p[j] = s[j] = r_old[j] = 0.0;
-    if (kk[j] >= 0) {
-      const int k = kk[j], i = k / a.g.ny;
-      r[j] = rhs_at(a, k, i, k - i * a.g.ny, dx2);
-      sr[si[j]] = r[j];
+    if (kk[j] >= 0) r[j] = rhs(kk[j]);
+  }
+  // PERIODIC: b projected onto zero mean (the mean of the exact total,
+  // rounded once; the singular system is then consistent).
+  double bmean = 0.0;
+  if (lat.mode == EPIC_POISSON_PERIODIC) {
+    double t0[NPT], t1[NPT];
+#pragma unroll
+    for (int j = 0; j < NPT; j++) {
+      t0[j] = kk[j] >= 0 ? r[j] : 0.0;
+      t1[j] = 0.0;
     }
+    XPartial* const Pc = P + (ep & 1) * nb;
+    xs_block_partial<NPT>(t0, t1, sx, Pc + blockIdx.x);
+    if (threadIdx.x == 0) bar_arrive(a.bar);
+    target += nb;
+    if (!bar_wait(a.bar, a.flags, target, &s_ok, spin)) return;
+    if (threadIdx.x < 32) {
+      double tot = 0, unused = 0;
+      xs_grid_totals_w0(Pc, nb, &tot, &unused);
+      if (threadIdx.x == 0) s_mean = tot / (double)n;
+    }
+    ep++;
+    __syncthreads();
+    bmean = s_mean;
+#pragma unroll
+    for (int j = 0; j < NPT; j++)
+      if (kk[j] >= 0) r[j] = r[j] - bmean;
   }
 #pragma unroll
+  for (int j = 0; j < NPT; j++)
+    if (kk[j] >= 0) sr[si[j]] = r[j];
+#pragma unroll
   for (int j = 0; j < PCG_HALO_SLOTS; j++)
-    if (hk[j] >= 0) {
-      const int k = hk[j], i = k / a.g.ny;
-      sr[hs[j]] = rhs_at(a, k, i, k - i * a.g.ny, dx2);
-    }
+    if (hk[j] >= 0) sr[hs[j]] = rhs(hk[j]) - bmean;
   __syncthreads();
   // Dot-product terms of this thread's nodes: (w, r) and (r, r).
   double td[NPT], tq[NPT];
@@ -1181,8 +1411,11 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
     }
   }
 
+  // min(n*n, max_iteration) as pcg() caps it: n*n in 32-bit int arithmetic for
+  // the reference's lattice (it wraps, as there), in 64 bits for the extensions.
   unsigned int cap32 = (unsigned int)n * (unsigned int)n;
-  const int maxit = (int)cap32 < a.max_iter ? (int)cap32 : a.max_iter;
+  const long long cap = lat.mode == EPIC_POISSON_DIRICHLET ? (long long)(int)cap32 : (long long)n * n;
+  const int maxit = cap < a.max_iter ? (int)cap : a.max_iter;
   unsigned long long* const slots =
       reinterpret_cast<unsigned long long*>(reinterpret_cast<char*>(a.partials) + PCG_SLOT_OFFSET);
   // The counted sums hold up to 2^19 terms (the fixed-point headroom).
@@ -1199,7 +1432,6 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
   if (threadIdx.x == 0) s_rr = s_eta = s_rrinv = s_g = 0.0;
   double be = 0, alq = 0;  // this iteration's beta and -alpha/4
   int aq = 0;              // anchor of the (r, r) terms (grid-wide); (w, r) one higher
-  int ep = 0;              // episodes of the block-anchored reduction (partials parity)
   int it = 0;
   // This thread's fixed-point sums of its (w, r) and (r, r) terms against the
   // anchors, accumulated as the stencil forms the terms.
@@ -1263,7 +1495,7 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
           wv = wv0;
           for (;;) {
             if ((wv & 255ull) == (unsigned long long)nb) break;
-            if (++spins > SPIN_LIMIT) {
+            if (++spins >= spin) {
               atomicOr(a.flags, FLAG_TIMEOUT);
               good = 0;
               break;
@@ -1316,7 +1548,7 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
           s_g = s_eta * (ri * ri);
         }
       }
-      if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
+      if (!bar_wait(a.bar, a.flags, target, &s_ok, spin)) return;
       if (threadIdx.x < 32) xs_grid_totals_w0(Pc, nb, &dr, &rr);
       ep++;
     }
@@ -1396,43 +1628,60 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       }
     it++;
   }
-  // domain.error = |A x - b| / n (src/field.cpp:258-259).
+  // domain.error = |A x - b| / n (src/field.cpp:258-259), n = nx ny.  With
+  // PERIODIC the same reduction also totals x, whose mean is then removed
+  // (the zero-mean gauge; the error is that of x before the shift).
 #pragma unroll
   for (int j = 0; j < NPT; j++)
     if (kk[j] >= 0) a.phi[kk[j]] = x[j];
   __syncthreads();
   if (threadIdx.x == 0) bar_arrive(a.bar);
   target += nb;
-  if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
+  if (!bar_wait(a.bar, a.flags, target, &s_ok, spin)) return;
+  const bool gauge = lat.mode == EPIC_POISSON_PERIODIC;
 #pragma unroll
   for (int j = 0; j < NPT; j++) {
     td[j] = tq[j] = 0.0;
     if (kk[j] >= 0) {
-      const int k = kk[j], row = k / C, col = k - row * C, i = k / a.g.ny;
+      const int q = threadIdx.x + PCG_T * j, lr = q / tc, lc = q - lr * tc;
+      const int row = r0 + lr, col = c0 + lc;
+      const int up = lattice_wrap(row - 1, R, lat.wrap_r), dn = lattice_wrap(row + 1, R, lat.wrap_r);
+      const int lf = lattice_wrap(col - 1, C, lat.wrap_c), rt = lattice_wrap(col + 1, C, lat.wrap_c);
       double sum = 0;
-      if (row > 0) sum += __ldcg(&a.phi[k - C]);
-      if (col > 0) sum += __ldcg(&a.phi[k - 1]);
+      if (up >= 0) sum += __ldcg(&a.phi[lattice_node(lat, up, col)]);
+      if (lf >= 0) sum += __ldcg(&a.phi[lattice_node(lat, row, lf)]);
       sum = fma(-4.0, x[j], sum);
-      if (col < C - 1) sum += __ldcg(&a.phi[k + 1]);
-      if (row < R - 1) sum += __ldcg(&a.phi[k + C]);
-      const double e = sum - rhs_at(a, k, i, k - i * a.g.ny, dx2);
+      if (rt >= 0) sum += __ldcg(&a.phi[lattice_node(lat, row, rt)]);
+      if (dn >= 0) sum += __ldcg(&a.phi[lattice_node(lat, dn, col)]);
+      const double e = sum - (rhs(kk[j]) - bmean);
       td[j] = e * e;
+      if (gauge) tq[j] = x[j];
     }
   }
   XPartial* const Pe = P + (ep & 1) * nb;
   xs_block_partial<NPT>(td, tq, sx, Pe + blockIdx.x);
   if (threadIdx.x == 0) bar_arrive(a.bar);
   target += nb;
-  if (!bar_wait(a.bar, a.flags, target, &s_ok)) return;
-  if (blockIdx.x == 0 && threadIdx.x < 32) {
-    double e2 = 0, unused = 0;
-    xs_grid_totals_w0(Pe, nb, &e2, &unused);
+  if (!bar_wait(a.bar, a.flags, target, &s_ok, spin)) return;
+  if ((gauge || blockIdx.x == 0) && threadIdx.x < 32) {
+    double e2 = 0, xsum = 0;
+    xs_grid_totals_w0(Pe, nb, &e2, &xsum);
     if (threadIdx.x == 0) {
-      a.info->iterations = it;
-      a.info->converged = it < maxit;
-      a.info->error = sqrt(e2) / n;
-      atomicAdd(a.iter_total, (unsigned long long)it);
+      s_mean = xsum / (double)n;
+      if (blockIdx.x == 0) {
+        a.info->iterations = it;
+        a.info->converged = it < maxit;
+        a.info->error = sqrt(e2) / (a.g.nx * a.g.ny);
+        atomicAdd(a.iter_total, (unsigned long long)it);
+      }
     }
+  }
+  if (gauge) {
+    __syncthreads();
+    const double xm = s_mean;
+#pragma unroll
+    for (int j = 0; j < NPT; j++)
+      if (kk[j] >= 0) a.phi[kk[j]] = x[j] - xm;
   }
 }
 
@@ -1440,7 +1689,7 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
 // busiest CTA (11 per owned node, 3 per halo node), ties to fewer CTAs.
 // Returns false when no tile fits PCG_T * 8 owned nodes and a halo ring of
 // PCG_T * PCG_HALO_SLOTS nodes (then the global-memory k_pcg runs).
-static bool pcg_tiling(int R, int C, int max_blocks, PcgTiling* out) {
+static bool pcg_tiling(int R, int C, int wrap_r, int wrap_c, int max_blocks, PcgTiling* out) {
   long long best = -1;
   PcgTiling b{};
   for (int tcb = 1; tcb <= C && tcb <= max_blocks; tcb++) {
@@ -1453,6 +1702,10 @@ static bool pcg_tiling(int R, int C, int max_blocks, PcgTiling* out) {
     const long long nodes = (long long)tr * tc;
     if (nodes > PCG_T * 8 || 2LL * (tr + tc) > PCG_T * PCG_HALO_SLOTS) continue;
     if (ncb * nrb > PCG_MAX_BLOCKS) continue;
+    // Where the lattice wraps, the last tile's valid extent has a neighbour
+    // beyond both of its sides and must span two nodes (so that its first
+    // and last rows / columns are different nodes).
+    if ((wrap_r && R - (nrb - 1) * tr < 2) || (wrap_c && C - (ncb - 1) * tc < 2)) continue;
     // The edge buffers (2 (tr + tc) slots per tile) live in node-sized vectors.
     if (tr < 2 || tc < 2 || (long long)ncb * nrb * 2 * (tr + tc) > (long long)R * C) continue;
     const long long cost = 11 * nodes + 3 * 2LL * (tr + tc);
@@ -1496,10 +1749,13 @@ static bool launch_tiled(cudaStream_t st, const SolverArgs& a, const PcgTiling& 
   return true;
 }
 
-void launch_pcg(cudaStream_t st, const SolverArgs& a, int blocks) {
-  cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned int), st);
+void launch_pcg(cudaStream_t st, const SolverArgs& a_in, int blocks) {
+  cudaMemsetAsync(a_in.bar, 0, 2 * sizeof(unsigned int), st);
+  SolverArgs a = a_in;
+  a.spin = spin_limit();
+  const Lattice lat = make_lattice(a.g.nx, a.g.ny, a.poisson_bc);
   PcgTiling t;
-  if (pcg_tiling(a.g.ny, a.g.nx, blocks, &t)) {
+  if (pcg_tiling(lat.R, lat.C, lat.wrap_r, lat.wrap_c, blocks, &t)) {
     SolverArgs at = a;
     at.tol_bits = xs_bits(xs_sqrt_threshold(a.tol));
     bool ok;
@@ -1509,11 +1765,33 @@ void launch_pcg(cudaStream_t st, const SolverArgs& a, int blocks) {
       case 4: ok = launch_tiled<4>(st, at, t); break;
       default: ok = launch_tiled<8>(st, at, t); break;
     }
-    if (ok) return;
+    if (ok) {
+      if (a.poisson_bc != EPIC_POISSON_DIRICHLET) launch_fill_poisson_nodes(st, a.g, a.poisson_bc, a.phi);
+      return;
+    }
   }
   SolverArgs args = a;
   void* params[] = {&args};
   cudaLaunchCooperativeKernel((const void*)k_pcg, dim3(blocks), dim3(256), params, 0, st);
+  if (a.poisson_bc != EPIC_POISSON_DIRICHLET) launch_fill_poisson_nodes(st, a.g, a.poisson_bc, a.phi);
+}
+
+__global__ void k_fill_poisson_nodes(Geom g, int mode, double* phi) {
+  const int nx = g.nx, ny = g.ny;
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx * ny; k += gridDim.x * blockDim.x) {
+    const int i = k / ny, j = k - i * ny;
+    if (mode == EPIC_POISSON_DIRICHLET_X && (i == 0 || i == nx - 1)) {
+      phi[k] = 0.0;
+    } else if (j == ny - 1 || (mode == EPIC_POISSON_PERIODIC && i == nx - 1)) {
+      const int si = mode == EPIC_POISSON_PERIODIC && i == nx - 1 ? 0 : i;
+      phi[k] = phi[si * ny + (j == ny - 1 ? 0 : j)];  // an unknown: never written here
+    }
+  }
+}
+
+void launch_fill_poisson_nodes(cudaStream_t st, const Geom& g, int poisson_bc, double* phi) {
+  const int nn = g.nx * g.ny;
+  k_fill_poisson_nodes<<<(nn + 255) / 256, 256, 0, st>>>(g, poisson_bc, phi);
 }
 
 // -------------------------------------------------- red-black SOR ---
@@ -1539,7 +1817,7 @@ __global__ void __launch_bounds__(256) k_sor_rb(SolverArgs a) {
     const int i = k / ny, j = k - i * ny;
     if (!a.warm || i == 0 || i == nx - 1 || j == 0 || j == ny - 1) phi[k] = 0;
   }
-  if (!grid_sync(a.bar, a.flags)) return;
+  if (!grid_sync(a.bar, a.flags, spin_or_default(a.spin))) return;
   const int ni = (nx - 2) * (ny - 2);
   int iter = 0, converged = 0;
   double L2 = 0;
@@ -1554,7 +1832,7 @@ __global__ void __launch_bounds__(256) k_sor_rb(SolverArgs a) {
         double phi_new = inv_coeff * (a.rho[k] * a.K + ((pE + pW) / dx2) + ((pN + pS) / dy2));
         phi[k] = pk + a.omega * (phi_new - pk);
       }
-      if (!grid_sync(a.bar, a.flags)) return;
+      if (!grid_sync(a.bar, a.flags, spin_or_default(a.spin))) return;
     }
     const int last = iter;
     iter++;
@@ -1569,7 +1847,7 @@ __global__ void __launch_bounds__(256) k_sor_rb(SolverArgs a) {
         sum += R * R;
       }
       block_partial2(sum, 0.0, P, sw);
-      if (!grid_sync(a.bar, a.flags)) return;
+      if (!grid_sync(a.bar, a.flags, spin_or_default(a.spin))) return;
       double2 tot = grid_total2_t0(P, nb, sw);
       if (threadIdx.x == 0) {
         s_l2 = sqrt(tot.x / (nx * ny));
@@ -1577,7 +1855,7 @@ __global__ void __launch_bounds__(256) k_sor_rb(SolverArgs a) {
       }
       __syncthreads();
       L2 = s_l2;
-      if (!grid_sync(a.bar, a.flags)) return;  // partials are rewritten at the next check
+      if (!grid_sync(a.bar, a.flags, spin_or_default(a.spin))) return;  // partials are rewritten at the next check
       if (s_done) {
         converged = 1;
         break;
@@ -1594,6 +1872,7 @@ __global__ void __launch_bounds__(256) k_sor_rb(SolverArgs a) {
 
 void launch_sor_redblack(cudaStream_t st, const SolverArgs& a, int blocks) {
   SolverArgs args = a;
+  args.spin = spin_limit();
   void* params[] = {&args};
   cudaMemsetAsync(a.bar, 0, 2 * sizeof(unsigned int), st);
   cudaLaunchCooperativeKernel((const void*)k_sor_rb, dim3(blocks), dim3(256), params, 0, st);

@@ -233,6 +233,13 @@ int config_from_ini(const char* path, epic_config* cfg, epic_species_desc* sp, i
     if (auto v = opt(ini, "solver", "sor_omega")) cfg->sor_omega = std::stod(*v);
     if (auto v = opt(ini, "solver", "sor_mode")) cfg->sor_mode = *v == "redblack" ? EPIC_SOR_REDBLACK : EPIC_SOR_LEXICOGRAPHIC;
     if (auto v = opt(ini, "solver", "warm_start")) cfg->warm_start = to_bool(*v);
+    if (auto v = opt(ini, "solver", "poisson_bc")) {
+      if (*v == "dirichlet") cfg->poisson_bc = EPIC_POISSON_DIRICHLET;
+      else if (*v == "periodic") cfg->poisson_bc = EPIC_POISSON_PERIODIC;
+      else if (*v == "dirichlet_x") cfg->poisson_bc = EPIC_POISSON_DIRICHLET_X;
+      else throw std::invalid_argument("poisson_bc " + *v + " is not supported (dirichlet, periodic, dirichlet_x)");
+    }
+    if (auto v = opt(ini, "simulation", "load_3v")) cfg->load_3v = to_bool(*v);
     if (auto v = opt(ini, "simulation", "deposit_mode")) cfg->deposit_mode = *v == "fp64" ? EPIC_DEPOSIT_FP64 : EPIC_DEPOSIT_FIXED;
     if (auto v = opt(ini, "simulation", "arithmetic"))
       cfg->precision = *v == "mixed" ? EPIC_PRECISION_MIXED : EPIC_PRECISION_FP64;
@@ -440,18 +447,31 @@ void conductor_geometry(const epic_config& c, const std::vector<epic_conductor>&
   }
 }
 
+struct RefStream {
+  Rnd rnd;
+  explicit RefStream(uint32_t seed) : rnd(seed) {}
+};
+RefStream* ref_stream_create(uint32_t seed) { return new RefStream(seed); }
+void ref_stream_destroy(RefStream* r) { delete r; }
+
 int load_particles(const epic_config& c, const std::vector<const epic_species_desc*>& sp,
                    std::vector<std::vector<double>>& out, uint32_t seed, std::string& err,
                    const std::vector<epic_conductor>& cond) {
-  Rnd rnd(seed);
-  const double Lx = (c.nx - 1) * c.dx, Ly = (c.ny - 1) * c.dy;
+  RefStream rs(seed);
   out.resize(sp.size());
-  for (size_t s = 0; s < sp.size(); s++) {
-    const epic_species_desc& d = *sp[s];
+  for (size_t s = 0; s < sp.size(); s++)
+    if (int st = load_species(c, *sp[s], out[s], &rs, err, cond)) return st;
+  return EPIC_OK;
+}
+
+int load_species(const epic_config& c, const epic_species_desc& d, std::vector<double>& o, RefStream* rs,
+                 std::string& err, const std::vector<epic_conductor>& cond) {
+  Rnd& rnd = rs->rnd;
+  const double Lx = (c.nx - 1) * c.dx, Ly = (c.ny - 1) * c.dy;
+  {
     int kind = 0, narg = 0;
     if (int st = parse_load_type(d.load, &kind, &narg, err)) return st;
     const long n = d.numparticle;
-    std::vector<double>& o = out[s];
     o.resize((size_t)n * 5);
     for (long p = 0; p < n; p++) {
       double x = 0, y = 0;
@@ -480,7 +500,9 @@ int load_particles(const epic_config& c, const std::vector<const epic_species_de
       }
       double vx = sample_vel(rnd, d.mass, d.temp) + d.vsx * c.vel_norm;
       double vy = sample_vel(rnd, d.mass, d.temp) + d.vsy * c.vel_norm;
-      double vz = 0;
+      // The reference loads vz = 0 (src/init.cpp:88); load_3v draws it like
+      // vx and vy (no drift), after them.
+      double vz = c.load_3v ? sample_vel(rnd, d.mass, d.temp) : 0;
       vx /= c.vel_norm;
       vy /= c.vel_norm;
       vz /= c.vel_norm;

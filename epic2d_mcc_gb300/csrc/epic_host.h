@@ -23,6 +23,14 @@ int ini_get(const char* path, const char* section, const char* key, std::string&
 int load_particles(const epic_config& c, const std::vector<const epic_species_desc*>& sp,
                    std::vector<std::vector<double>>& out, uint32_t seed, std::string& err,
                    const std::vector<epic_conductor>& cond = {});
+// The reference's global generator (Rnd rnd, include/domain.h:218-231 and
+// src/domain.cpp:4): one mt19937 seeded once and continued by every Init.
+struct RefStream;
+RefStream* ref_stream_create(uint32_t seed);
+void ref_stream_destroy(RefStream* r);
+// Init::Init of one species (src/init.cpp:3-101) drawing from *rs.
+int load_species(const epic_config& c, const epic_species_desc& d, std::vector<double>& out, RefStream* rs,
+                 std::string& err, const std::vector<epic_conductor>& cond = {});
 int conductors_from_ini(const char* path, std::vector<epic_conductor>& out, std::string& err);
 int emitters_from_ini(const char* path, std::vector<epic_emitter>& out, std::string& err);
 // Conductor geometry for the device: rectangles {min_x, max_x, min_y, max_y},

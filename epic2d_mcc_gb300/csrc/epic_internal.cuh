@@ -44,8 +44,12 @@ enum : int {
   FLAG_BAD_TABLE = 8,
 };
 
-// Bounded spin: polls of a device-side wait before it reports FLAG_TIMEOUT.
+// Bounded spin: polls of a device-side wait before it reports FLAG_TIMEOUT
+// (the default).  spin_limit() is the limit the launchers pass to their
+// kernels: SPIN_LIMIT unless epic_set_spin_limit chose another.
 constexpr long long SPIN_LIMIT = 1ll << 24;
+long long spin_limit();
+__host__ __device__ inline long long spin_or_default(long long v) { return v > 0 ? v : SPIN_LIMIT; }
 
 constexpr int PART_THREADS = 256;
 constexpr int SCAN_TILE = 1024;  // particles per ordered tile (push+compact, MCC append)
@@ -261,6 +265,7 @@ struct SolverArgs;
 struct SpectralSolver {
   int R, C;       // lattice of unknowns: R rows of C
   int flat;       // 1: pcgsolver's lattice of the flattened vector (all nodes); 0: gssolver's interior
+  int mode;       // EPIC_POISSON_* (an extension lattice: rows i = r + i0, columns j, see Lattice)
   int gs_norm;    // 1: stop on the SOR residual L2 of src/field.cpp:118-134, 0: on |b - Ax|_2
   float *QR, *QC; // R x R and C x C sine transforms, orthonormal and symmetric (shared when R = C)
   float* D;       // R x C, 1/(lambda_p + mu_q)
@@ -269,7 +274,7 @@ struct SpectralSolver {
   double* partials;
   int* state;     // [0] done flag, [1] stage, [2] converged
 };
-int spectral_supported(const Geom& g, int solver);
+int spectral_supported(const Geom& g, int solver, int poisson_bc);
 int spectral_chunks(const SpectralSolver& sp);  // residual chunks (partials needed)
 void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs& a, int stages);
 void launch_particle_sums(cudaStream_t st, int what, const SoA& p, const long long* d_n, double vel_norm,
@@ -296,8 +301,8 @@ struct FinalizeArgs {
   double* rho;
 };
 void launch_finalize(cudaStream_t st, const FinalizeArgs& a);
-void launch_efield(cudaStream_t st, const Geom& g, int bc, const double* phi, double* efx, double* efy, double2* ef,
-                   float2* ef32);
+void launch_efield(cudaStream_t st, const Geom& g, int bc, int poisson_bc, const double* phi, double* efx,
+                   double* efy, double2* ef, float2* ef32);
 
 struct SolverArgs {
   Geom g;
@@ -316,7 +321,48 @@ struct SolverArgs {
   unsigned int* bar; // grid barrier {count, generation}
   int warm;
   unsigned long long tol_bits;  // PCG stop test: sqrt(r.r) < tol <=> bits(r.r) < tol_bits (set by launch_pcg)
+  long long spin;               // poll limit of the grid-wide waits (set by the launchers; 0 = SPIN_LIMIT)
+  int poisson_bc;               // EPIC_POISSON_* (the extensions' lattices, see Lattice)
 };
+
+// The unknowns of a PCG / SOR solve as a lattice of R rows of C columns.
+// EPIC_POISSON_DIRICHLET (the reference's pcgsolver): the flattened node
+// vector in rows of nx (row = k / nx, col = k % nx, src/field.cpp:221-232),
+// neighbours outside the lattice contribute nothing.  The extensions: rows
+// are the x index i = row + i0, columns the y index j, node (row, col) at
+// (row + i0) * ny + col; DIRICHLET_X has i0 = 1, R = nx - 2 (the walls are
+// not unknowns) and wraps columns (C = ny - 1, node ny-1 is node 0);
+// PERIODIC has i0 = 0, R = nx - 1 and wraps rows and columns.
+struct Lattice {
+  int R, C;
+  int rs, k0;  // node of (row, col) = k0 + row * rs + col
+  int wrap_r, wrap_c;
+  int mode;    // EPIC_POISSON_*
+};
+__host__ __device__ inline Lattice make_lattice(int nx, int ny, int poisson_bc) {
+  Lattice l;
+  l.mode = poisson_bc;
+  if (poisson_bc == EPIC_POISSON_PERIODIC) {
+    l.R = nx - 1; l.C = ny - 1; l.rs = ny; l.k0 = 0; l.wrap_r = 1; l.wrap_c = 1;
+  } else if (poisson_bc == EPIC_POISSON_DIRICHLET_X) {
+    l.R = nx - 2; l.C = ny - 1; l.rs = ny; l.k0 = ny; l.wrap_r = 0; l.wrap_c = 1;
+  } else {
+    l.R = ny; l.C = nx; l.rs = nx; l.k0 = 0; l.wrap_r = 0; l.wrap_c = 0;
+  }
+  return l;
+}
+__host__ __device__ inline int lattice_node(const Lattice& l, int row, int col) { return l.k0 + row * l.rs + col; }
+// Lattice position of a neighbour row / column index that may lie one step
+// outside: wrapped where the lattice is periodic, else -1 (no neighbour).
+__host__ __device__ inline int lattice_wrap(int v, int n, int wrap) {
+  if (v >= 0 && v < n) return v;
+  if (!wrap) return -1;
+  return v < 0 ? v + n : v - n;
+}
+// The solve's duplicated nodes after an extension solve: periodic copies
+// (node nx-1 from node 0, node ny-1 from node 0) and the zero x walls of
+// DIRICHLET_X (epic_field.cu).
+void launch_fill_poisson_nodes(cudaStream_t st, const Geom& g, int poisson_bc, double* phi);
 void init_field_kernels();  // one-time kernel attributes (called by epic_create)
 void set_last_error(const char* msg);  // the message epic_last_error() returns on this thread
 void launch_sor_lex(cudaStream_t st, const SolverArgs& a);
@@ -401,6 +447,9 @@ struct epic_sim {
   // Emitters (epic_add_emitter) and the device count of injections
   std::vector<epic_emitter> emitters;
   unsigned long long* d_inj = nullptr;
+  // The reference's global mt19937 for per-species Init (epic_init_species);
+  // created on first use with seed 0, reseeded by epic_load_particles.
+  void* ref_rng = nullptr;
   epic::CrossSections cs;
   int64_t launches;
   cudaGraphExec_t graph_exec;       // one step

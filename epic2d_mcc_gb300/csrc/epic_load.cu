@@ -4,7 +4,8 @@
 // The loader places particles exactly as Init::Init (src/init.cpp:3-114) and
 // Init::SampleVel do — uniform random, uniform lattice, or sin/cos(n)
 // positions, and v = v_th*sqrt(2)*(u1 + u2 + u3 - 1.5) + drift per component
-// (vz = 0), normalised by vel_norm — but draws its uniforms from Philox keyed
+// (vz = 0, or drawn like vx and vy with load_3v), normalised by vel_norm — but
+// draws its uniforms from Philox keyed
 // by (seed, species, particle) on the GPU instead of the host mt19937 stream,
 // so a run can be loaded without a host-side pass over its particles (the
 // serving loop admits runs of ~10^7 particles while others are in flight).
@@ -30,6 +31,7 @@ struct LoadSpec {
   double x0, y0, Lx, Ly;
   double v_th, vsx, vsy, vel_norm;
   double pi;
+  int load_3v;
 };
 
 __global__ void k_load(LoadSpec L, double* __restrict__ aos, unsigned long long seed) {
@@ -72,7 +74,12 @@ __global__ void k_load(LoadSpec L, double* __restrict__ aos, unsigned long long 
     q[1] = y;
     q[2] = vx / L.vel_norm;
     q[3] = vy / L.vel_norm;
-    q[4] = 0.0;
+    double vz = 0.0;
+    if (L.load_3v) {
+      u1 = r.next(); u2 = r.next(); u3 = r.next();
+      vz = L.v_th * s2 * (u1 + u2 + u3 - 1.5);
+    }
+    q[4] = vz / L.vel_norm;
   }
 }
 
@@ -94,6 +101,7 @@ void launch_load(cudaStream_t st, const Geom& g, const epic_species_desc& d, con
   L.vsy = d.vsy;
   L.vel_norm = c.vel_norm;
   L.pi = PI_REF;
+  L.load_3v = c.load_3v;
   if (L.n > 0) k_load<<<grid, PART_THREADS, 0, st>>>(L, aos, seed);
   (void)g;
 }

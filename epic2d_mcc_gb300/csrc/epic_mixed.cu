@@ -133,7 +133,8 @@ template <int SHAPE>
 __global__ void __launch_bounds__(PART_THREADS) k_push_mixed_compact(Geom g, MixedSoA p, long long* d_n,
                                                                      const float2* __restrict__ ef, float qmK_dt,
                                                                      float cx, float cy, unsigned long long* status,
-                                                                     unsigned int* tile_ctr, int* flags) {
+                                                                     unsigned int* tile_ctr, int* flags,
+                                                                     long long spin) {
   constexpr int ITEMS = SCAN_TILE / PART_THREADS;
   __shared__ int sm[40];
   __shared__ unsigned long long s_prefix;
@@ -165,7 +166,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_mixed_compact(Geom g, Mix
       rank[k] = tile_total + block_exclusive_scan(keep[k], &row_total, sm);
       tile_total += row_total;
     }
-    if (threadIdx.x == 0) s_prefix = tile_lookback(status, tile, (unsigned long long)tile_total, flags);
+    if (threadIdx.x == 0) s_prefix = tile_lookback(status, tile, (unsigned long long)tile_total, flags, spin);
     __syncthreads();
     const unsigned long long prefix = s_prefix;
     if (prefix != ~0ull) {
@@ -189,10 +190,10 @@ void launch_push_mixed(cudaStream_t st, const Geom& g, int shape, int bc, const 
   if (bc == EPIC_OPEN) {
     if (shape == EPIC_NGP)
       k_push_mixed_compact<EPIC_NGP><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy, tile_status,
-                                                                     tile_ctr, flags);
+                                                                     tile_ctr, flags, spin_limit());
     else
       k_push_mixed_compact<EPIC_CIC><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy, tile_status,
-                                                                     tile_ctr, flags);
+                                                                     tile_ctr, flags, spin_limit());
   } else if (bc == EPIC_PBC) {
     if (shape == EPIC_NGP) PM(EPIC_NGP, EPIC_PBC);
     else PM(EPIC_CIC, EPIC_PBC);

@@ -24,7 +24,6 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 
 #include "epic_internal.cuh"
 
@@ -43,29 +42,25 @@ constexpr size_t PCG_STATIC_BYTES = 8 * PCG_VEC_BYTES + PCG_PART_BYTES + 4 * 256
 
 static __device__ __align__(256) unsigned char g_pcg_scratch[PCG_STATIC_BYTES];
 
-constexpr int MAX_DEVICES = 64;
-std::mutex g_mu;
-unsigned char* g_scratch_ptr[MAX_DEVICES] = {nullptr};  // device address of g_pcg_scratch per device
 epic_status fail_na(epic_status st, const char* msg) {
   set_last_error(msg);  // reported by epic_last_error(), as for every entry point
   return st;
 }
 
-// Device address of the static array on the current device (looked up once
-// per device; the lookup is not a stream operation).
-epic_status scratch_address(int dev, unsigned char** out) {
-  std::lock_guard<std::mutex> lk(g_mu);
-  if (!g_scratch_ptr[dev]) {
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_pcg_scratch);
-    if (e != cudaSuccess) {
-      char buf[256];
-      std::snprintf(buf, sizeof(buf), "cudaGetSymbolAddress(g_pcg_scratch): %s", cudaGetErrorString(e));
-      return fail_na(EPIC_ERR_CUDA, buf);
-    }
-    g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
+// Device address of the static array on the current device.  Looked up on
+// every call (a host-side query, not a stream operation): the address belongs
+// to the context that loaded this library's device code, and a caller that
+// resets the device (cudaDeviceReset) gets a new context in which the array
+// may sit elsewhere, so an address kept from an earlier call could be stale.
+epic_status scratch_address(unsigned char** out) {
+  void* p = nullptr;
+  cudaError_t e = cudaGetSymbolAddress(&p, g_pcg_scratch);
+  if (e != cudaSuccess || !p) {
+    char buf[256];
+    std::snprintf(buf, sizeof(buf), "cudaGetSymbolAddress(g_pcg_scratch): %s", cudaGetErrorString(e));
+    return fail_na(EPIC_ERR_CUDA, buf);
   }
-  *out = g_scratch_ptr[dev];
+  *out = static_cast<unsigned char*>(p);
   return EPIC_OK;
 }
 
@@ -88,9 +83,9 @@ epic_status epic_pcg_solve_static(const double* rho, double* phi, int nx, int ny
   }
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= MAX_DEVICES) return fail_na(EPIC_ERR_CUDA, "no usable CUDA device");
+  if (e != cudaSuccess) return fail_na(EPIC_ERR_CUDA, "no usable CUDA device");
   unsigned char* base = nullptr;
-  epic_status st = scratch_address(dev, &base);
+  epic_status st = scratch_address(&base);
   if (st) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 

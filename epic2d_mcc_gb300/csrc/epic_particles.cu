@@ -452,7 +452,8 @@ template <int SHAPE, int BC, int MAP, bool COND, bool CONTRACT>
 __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, long long* d_n,
                                                                const double2* __restrict__ ef, double qmK, double c,
                                                                double dtsub, unsigned long long* status,
-                                                               unsigned int* tile_ctr, int* flags, CondSet cs) {
+                                                               unsigned int* tile_ctr, int* flags, CondSet cs,
+                                                               long long spin) {
   constexpr int ITEMS = SCAN_TILE / PART_THREADS;
   __shared__ int sm[40];
   __shared__ unsigned long long s_prefix;
@@ -489,7 +490,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, lo
       rank[k] = tile_total + block_exclusive_scan(keep[k], &row_total, sm);
       tile_total += row_total;
     }
-    if (threadIdx.x == 0) s_prefix = tile_lookback(status, tile, (unsigned long long)tile_total, flags);
+    if (threadIdx.x == 0) s_prefix = tile_lookback(status, tile, (unsigned long long)tile_total, flags, spin);
     __syncthreads();
     const unsigned long long prefix = s_prefix;
     if (prefix != ~0ull) {
@@ -536,7 +537,8 @@ void launch_push(cudaStream_t st, const Geom& g, int shape, int bc, const SoA& p
 #define PUSH(SH, B, U) do { if (contract) PUSH1(SH, B, U, true); else PUSH1(SH, B, U, false); } while (0)
 #define COMPACT1(SH, U, C)                                                                                      \
   k_push_compact<SH, EPIC_OPEN, U, false, C><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub,      \
-                                                                            tile_status, tile_ctr, flags, CondSet{})
+                                                                            tile_status, tile_ctr, flags, CondSet{},      \
+                                                                            spin_limit())
 #define COMPACT(SH, U) do { if (contract) COMPACT1(SH, U, true); else COMPACT1(SH, U, false); } while (0)
 #define BOTH(M, ...)                          \
   do {                                        \
@@ -570,7 +572,7 @@ void launch_push_conductors(cudaStream_t st, const Geom& g, int shape, int bc, c
   if (shape == EPIC_CIC && contract) ef = cell;
 #define PC1(SH, B, U, C)                                                                                        \
   k_push_compact<SH, B, U, true, C><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK, c, dtsub, tile_status, \
-                                                                   tile_ctr, flags, cs)
+                                                                   tile_ctr, flags, cs, spin_limit())
 #define PC(SH, B, U) do { if (contract) PC1(SH, B, U, true); else PC1(SH, B, U, false); } while (0)
 #define BOTH(SH, B)                            \
   do {                                         \

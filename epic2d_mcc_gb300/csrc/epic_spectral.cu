@@ -32,9 +32,12 @@
 
 namespace epic {
 
-int spectral_supported(const Geom& g, int solver) {
+int spectral_supported(const Geom& g, int solver, int poisson_bc) {
   if (g.nx < 3 || g.ny < 3) return 0;
   if (solver != EPIC_SOLVER_PCG && solver != EPIC_SOLVER_GS) return 0;  // the Boltzmann solvers are nonlinear
+  // The extension lattices (both solvers' unknowns are the same there) are
+  // isotropic only for dx = dy.
+  if (poisson_bc != EPIC_POISSON_DIRICHLET) return g.dx == g.dy;
   return solver == EPIC_SOLVER_PCG || g.dx == g.dy;  // the SOR lattice is isotropic only for dx = dy
 }
 
@@ -48,6 +51,8 @@ static SpecLattice lattice_of(const SpectralSolver& sp, const SolverArgs& a) {
   L.C = sp.C;
   L.flat = sp.flat;
   L.gs_norm = sp.gs_norm;
+  L.mode = sp.mode;
+  L.bmean = sp.partials + spectral_chunks(sp);
   L.dx2 = a.g.dx * a.g.dx;
   L.K = a.K;
   L.tol = a.tol;
@@ -67,13 +72,62 @@ __global__ void k_spec_init(SpecLattice L, int warm) {
   const int nx = L.nx, ny = L.ny;
   for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nx * ny; k += gridDim.x * blockDim.x) {
     const int i = k / ny, j = k - i * ny;
-    const bool unknown = L.flat || (i >= 1 && i < nx - 1 && j >= 1 && j < ny - 1);
+    const bool unknown = L.mode == EPIC_POISSON_PERIODIC   ? i < nx - 1 && j < ny - 1
+                         : L.mode == EPIC_POISSON_DIRICHLET_X ? i >= 1 && i < nx - 1 && j < ny - 1
+                         : L.flat || (i >= 1 && i < nx - 1 && j >= 1 && j < ny - 1);
     if (!warm || !unknown) spec_init_node(L, k);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     L.state[0] = 0;
     L.state[1] = 0;
     L.state[2] = 0;
+  }
+}
+
+// PERIODIC: the mean of b = -rho dx^2 K over the unknowns (one CTA, fixed
+// order), subtracted from b so that the singular system is consistent.  The
+// periodic lattice's entry (r, c) is node (r, c).
+__global__ void __launch_bounds__(1024) k_spec_bmean(SpecLattice L) {
+  __shared__ double sm[32];
+  const int n = L.R * L.C;
+  double acc = 0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int i = q / L.C, j = q - i * L.C;
+    acc += -L.rho[spec_node(L, i, j)] * L.dx2 * L.K;
+  }
+  acc = spec_warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w];
+    *const_cast<double*>(L.bmean) = t / n;
+  }
+}
+
+// PERIODIC: phi shifted to zero mean over the unknowns (the FP64 solver's
+// gauge); the FP32 corrections leave a rounding-level mean.
+__global__ void __launch_bounds__(1024) k_spec_gauge(SpecLattice L) {
+  __shared__ double sm[33];
+  const int n = L.R * L.C;
+  double acc = 0;
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int i = q / L.C, j = q - i * L.C;
+    acc += L.phi[spec_node(L, i, j)];
+  }
+  acc = spec_warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w];
+    sm[32] = t / n;
+  }
+  __syncthreads();
+  const double m = sm[32];
+  for (int q = threadIdx.x; q < n; q += blockDim.x) {
+    const int i = q / L.C, j = q - i * L.C;
+    L.phi[spec_node(L, i, j)] -= m;
   }
 }
 
@@ -102,6 +156,7 @@ void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs
   const SpecLattice L = lattice_of(sp, a);
   const int nch = spectral_chunks(sp);
   k_spec_init<<<(a.g.nx * a.g.ny + 255) / 256, 256, 0, st>>>(L, a.warm);
+  if (sp.mode == EPIC_POISSON_PERIODIC) k_spec_bmean<<<1, 1024, 0, st>>>(L);
   dim3 g2((C + 31) / 32, (R + 31) / 32);
   for (int s = 0; s < stages; s++) {
     k_spec_residual<<<nch, 256, 0, st>>>(L);
@@ -113,6 +168,8 @@ void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs
   }
   k_spec_residual<<<nch, 256, 0, st>>>(L);
   k_spec_check<<<1, 1, 0, st>>>(L, 1);
+  if (sp.mode == EPIC_POISSON_PERIODIC) k_spec_gauge<<<1, 1024, 0, st>>>(L);
+  if (sp.mode != EPIC_POISSON_DIRICHLET) launch_fill_poisson_nodes(st, a.g, sp.mode, a.phi);
 }
 
 }  // namespace epic

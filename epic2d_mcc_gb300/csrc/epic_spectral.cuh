@@ -22,6 +22,11 @@ constexpr int SPEC_CHUNK = 1024;  // lattice entries per residual CTA (256 threa
 struct SpecLattice {
   int nx, ny, I_off, NY;
   int R, C, flat, gs_norm;
+  // EPIC_POISSON_* : with an extension the unknowns are rows i = r + i0
+  // (i0 = 1 for DIRICHLET_X, 0 for PERIODIC) of columns j = c, neighbours
+  // wrapped where periodic, and PERIODIC subtracts *bmean from b.
+  int mode;
+  const double* bmean;
   double dx2, K, tol;
   const double* rho;
   double* phi;
@@ -60,7 +65,18 @@ __device__ __forceinline__ void spec_residual_chunk(const SpecLattice& L, int ch
       const double* x = L.phi;
       int i, j;
       double ax;
-      if (L.flat) {  // pcgsolver: rows of C = nx nodes of the flattened vector
+      if (L.mode != EPIC_POISSON_DIRICHLET) {  // extension lattice: rows i = ri + i0, wrapped neighbours
+        const int i0 = L.mode == EPIC_POISSON_PERIODIC ? 0 : 1;
+        i = ri + i0;
+        j = cj;
+        const int ru = lattice_wrap(ri - 1, R, L.mode == EPIC_POISSON_PERIODIC);
+        const int rd = lattice_wrap(ri + 1, R, L.mode == EPIC_POISSON_PERIODIC);
+        ax = -4 * x[spec_node(L, i, j)];
+        if (ru >= 0) ax += x[spec_node(L, ru + i0, j)];
+        if (rd >= 0) ax += x[spec_node(L, rd + i0, j)];
+        ax += x[spec_node(L, i, cj > 0 ? cj - 1 : C - 1)];
+        ax += x[spec_node(L, i, cj < C - 1 ? cj + 1 : 0)];
+      } else if (L.flat) {  // pcgsolver: rows of C = nx nodes of the flattened vector
         auto nd = [&](int k) { const int ii = k / ny; return spec_node(L, ii, k - ii * ny); };
         i = q / ny;
         j = q - i * ny;
@@ -78,8 +94,9 @@ __device__ __forceinline__ void spec_residual_chunk(const SpecLattice& L, int ch
         if (j > 0) ax += x[spec_node(L, i, j - 1)];
         if (j < ny - 1) ax += x[spec_node(L, i, j + 1)];
       }
-      const bool edge = i == 0 || i == nx - 1 || j == 0 || j == ny - 1;
-      const double b = edge ? 0.0 : -L.rho[spec_node(L, i, j)] * L.dx2 * L.K;
+      const bool edge = L.mode == EPIC_POISSON_DIRICHLET && (i == 0 || i == nx - 1 || j == 0 || j == ny - 1);
+      double b = edge ? 0.0 : -L.rho[spec_node(L, i, j)] * L.dx2 * L.K;
+      if (L.mode == EPIC_POISSON_PERIODIC) b = b - *L.bmean;
       const double r = b - ax;
       L.t0[q] = (float)r;
       acc += r * r;
@@ -168,7 +185,10 @@ __device__ __forceinline__ void spec_gemm_tile(int M, int N, int K, const float*
       else if (EPI == 1) Cm[r * N + c] = acc[a][b] * D[r * N + c];
       else {
         int i, j;
-        if (L->flat) {
+        if (L->mode != EPIC_POISSON_DIRICHLET) {
+          i = r + (L->mode == EPIC_POISSON_PERIODIC ? 0 : 1);
+          j = c;
+        } else if (L->flat) {
           const int k = r * N + c;  // N = C: the flattened vector
           i = k / L->ny;
           j = k - i * L->ny;

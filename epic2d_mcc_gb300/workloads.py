@@ -5,11 +5,14 @@ configurations the project is measured on:
 
 * ``periodic_64`` — 64x64 cells, 50 particles per cell per species
   (204,800 electrons + 204,800 ions), Te 1 eV, Ti 0.026 eV, ion mass 1836 m_e,
-  n0 1e13 m^-3, dt 0.01/wpe, CIC, SOR (omega 1.8, tolerance 1e-8), no collisions.
+  n0 1e13 m^-3, dt 0.01/wpe, CIC, SOR (omega 1.8, tolerance 1e-8), no
+  collisions; periodic particles and a periodic Poisson problem
+  (poisson_bc = periodic), velocities drawn in 3V (load_3v).
 * ``beam_mcc_256`` — 256x256 cells, 100 particles per cell: 6,553,600 ions
   (40 amu) and 6,553,600 electrons of which 10 % are a beam drifting at 5 v_th,e,
   PCG to 1e-10, MCC against 1e20 m^-3 neutrals with the synthetic 1000-point
-  log-spaced table below.
+  log-spaced table below; phi = 0 on the x walls and periodic in y
+  (poisson_bc = dirichlet_x), particles periodic.
 * ``periodic_1024`` — 1024x1024 cells, 100 particles per cell per species.
 * ``conductors_64``, ``emitters_128``, ``gshybrid_64``, ``hybrid_24`` — one deck
   per extension of the loop (conductors with the SOR solver and absorbing walls,
@@ -18,7 +21,8 @@ configurations the project is measured on:
 * ``twostream_1024`` — the precision form's plasma: 1024x1024 periodic cells,
   100 particles per cell per species (1.05e8 ions of 1836 m_e at 0.05 eV,
   1.05e8 electrons at 2 eV in two halves drifting at +-3 v_th,e), dt 0.05/wpe,
-  PCG to 1e-10, no collisions (``twostream_256`` is the same on 256x256 cells).
+  PCG to 1e-10 on a periodic Poisson problem, no collisions (``twostream_256``
+  is the same on 256x256 cells).
 
 Inputs are seeded synthetic plasmas (the reference loads positions and
 velocities from mt19937 seed 0; so do these decks).
@@ -104,9 +108,10 @@ def deck(name: str) -> str:
         n, ppc = 64, 50
         sp = ["electron,%.8E,%d,1,-1,1,0,0,random" % (ME, n * n * ppc),
               "ion,%.8E,%d,0.026,1,0,0,0,random" % (1836 * ME, n * n * ppc)]
-        return _TEMPLATE.format(num_ts=1000, dt=0.01, n=n, solver="gs", tol="1e-8", maxit=200000,
-                                solver_extra="sor_omega = 1.8\n", bc="pbc", coll="false", gas="1e20",
-                                species="\n".join(sp))
+        text = _TEMPLATE.format(num_ts=1000, dt=0.01, n=n, solver="gs", tol="1e-8", maxit=200000,
+                                solver_extra="sor_omega = 1.8\npoisson_bc = periodic\n", bc="pbc", coll="false",
+                                gas="1e20", species="\n".join(sp))
+        return text.replace("ionfixed = 0\n", "ionfixed = 0\nload_3v = true\n")
     if name in ("beam_mcc_256", "beam_mcc_160"):
         # beam_mcc_160 is the same plasma on 160x160 cells (5.1 M particles,
         # 205 MB: still larger than L2) for profiler captures.
@@ -118,7 +123,8 @@ def deck(name: str) -> str:
               "ion,%.8E,%d,0.026,1,0,0,0,random" % (40 * AMU, total_e),
               "beam,%.8E,%d,1,-1,%.17g,5,0,random" % (ME, beam, 1.0 / 9.0)]
         return _TEMPLATE.format(num_ts=2000, dt=0.01, n=n, solver="cg", tol="1e-10", maxit=100000,
-                                solver_extra="", bc="pbc", coll="true", gas="1e20", species="\n".join(sp))
+                                solver_extra="poisson_bc = dirichlet_x\n", bc="pbc", coll="true", gas="1e20",
+                                species="\n".join(sp))
     if name in ("twostream_1024", "twostream_256"):
         # two counter-streaming electron populations at +-3 v_th,e (v_th = sqrt(2 e Te / m_e));
         # velocities are in units of vel_norm = LDe * wpe = sqrt(e Te / m_e) (norm_scheme 1), so
@@ -131,7 +137,8 @@ def deck(name: str) -> str:
               "ion,%.8E,%d,0.05,1,0,0,0,random" % (1836 * ME, n * n * ppc),
               "beam,%.8E,%d,2,-1,1,%.17g,0,random" % (ME, half, -vs)]
         return _TEMPLATE.format(num_ts=500, dt=0.05, n=n, solver="cg", tol="1e-10", maxit=100000,
-                                solver_extra="", bc="pbc", coll="false", gas="1e20", species="\n".join(sp))
+                                solver_extra="poisson_bc = periodic\n", bc="pbc", coll="false", gas="1e20",
+                                species="\n".join(sp))
     if name == "periodic_1024":
         n, ppc = 1024, 100
         sp = ["electron,%.8E,%d,2,-1,1,0,0,random" % (ME, n * n * ppc),

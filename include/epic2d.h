@@ -31,7 +31,7 @@ typedef enum {
   EPIC_ERR_INVALID = 1,       /* bad argument or configuration */
   EPIC_ERR_CUDA = 2,          /* CUDA runtime error */
   EPIC_ERR_NOMEM = 3,         /* device allocation failed */
-  EPIC_ERR_CAPACITY = 4,      /* a species outgrew its particle capacity */
+  EPIC_ERR_CAPACITY = 4,      /* a species outgrew its particle capacity, or a grid exceeds a fixed scratch limit */
   EPIC_WARN_NOT_CONVERGED = 5,/* Poisson solve hit max_iteration (the reference prints to cerr) */
   EPIC_ERR_DOMAIN = 6,        /* a particle left the grid (the reference throws std::out_of_range) */
   EPIC_ERR_TIMEOUT = 7,       /* a device-side wait gave up */
@@ -86,8 +86,23 @@ typedef struct {
   int precision;              /* EPIC_PRECISION_FP64 (the reference's arithmetic) | EPIC_PRECISION_MIXED */
   int sort_every;             /* sort particles by cell every k steps (0: never, the reference's order) */
   int push_order;             /* EPIC_PUSH_CONTRACTED (default) | EPIC_PUSH_REFERENCE (FP64 form) */
-  int reserved[12];
+  int poisson_bc;             /* EPIC_POISSON_* ([solver] poisson_bc); DIRICHLET is the reference */
+  int load_3v;                /* 1: Init draws vz like vx, vy ([simulation] load_3v; the reference loads vz = 0) */
+  int reserved[10];
 } epic_config;
+
+/* Boundary of the Poisson problem (extension; no reference counterpart
+ * except DIRICHLET).  DIRICHLET: the reference's solvers (gssolver holds
+ * phi = 0 on every edge node, pcgsolver zeroes the right-hand side there).
+ * PERIODIC: unknowns i in [0, nx-2], j in [0, ny-2], periodic in x and y
+ * (node nx-1 is node 0, node ny-1 is node 0); the right-hand side is
+ * projected onto zero mean and phi has zero mean over the unknowns.
+ * DIRICHLET_X: phi = 0 on the x walls i = 0 and i = nx-1, periodic in y;
+ * unknowns i in [1, nx-2], j in [0, ny-2].  The extensions keep each solver's
+ * update, scaling, stopping test and residual norm, and the E-field takes
+ * the periodic edge formula in periodic directions and the one-sided one at
+ * the x walls.  Solvers: gs (lexicographic) and cg, both forms. */
+enum { EPIC_POISSON_DIRICHLET = 0, EPIC_POISSON_PERIODIC = 1, EPIC_POISSON_DIRICHLET_X = 2 };
 
 /* Mixed precision: particles as int32 cell + FP32 in-cell offsets + FP32
  * velocities, integer CIC weights, and a Poisson solve whose inner step is
@@ -115,8 +130,8 @@ void epic_config_defaults(epic_config* cfg);
 
 /* INIParser::parse + the set-up of src/main.cpp:34-261 (normalisation, species
  * densities and weights; src/iniparser.cpp:4-113).  Also reads the optional
- * keys sor_omega, sor_mode, deposit_mode, mcc_mode, seed, warm_start from
- * [solver]/[simulation]/[collision].  *num_species is set to the number of
+ * keys sor_omega, sor_mode, poisson_bc, deposit_mode, mcc_mode, seed,
+ * warm_start, load_3v from [solver]/[simulation]/[collision].  *num_species is set to the number of
  * species lines; at most max_species descriptors are written. */
 epic_status epic_config_from_ini(const char* path, epic_config* cfg, epic_species_desc* species, int max_species,
                                  int* num_species, int* num_ts);
@@ -137,6 +152,14 @@ epic_status epic_add_species(epic_sim* sim, const epic_species_desc* desc, int* 
  * with `seed` (src/init.cpp:3-101; the reference seeds its global Rnd with 0,
  * include/domain.h:223).  Host-side start-up, as in the reference. */
 epic_status epic_load_particles(epic_sim* sim, uint32_t seed);
+
+/* Init::Init of one species (src/init.cpp:3-101), drawing from the handle's
+ * copy of the reference's global generator (Rnd rnd, include/domain.h:218-231:
+ * one mt19937 seeded with 0 when the handle is created and continued by every
+ * call, reseeded by epic_load_particles).  Calling it for species 0, 1, ... in
+ * order is epic_load_particles(sim, 0), as main runs Init per species
+ * (src/main.cpp:359-362). */
+epic_status epic_init_species(epic_sim* sim, int species);
 
 /* Particle upload/download in the Particle layout (5 doubles per particle). */
 epic_status epic_set_particles(epic_sim* sim, int species, const double* particles, int64_t n);
@@ -284,6 +307,12 @@ epic_status epic_add_emitter(epic_sim* sim, const epic_emitter* e);
  * numparticle rows of 14 doubles: the x and y uniforms, 6 velocity uniforms
  * for species_idx1 (vx then vy, three each) and 6 for species_idx2. */
 epic_status epic_inject(epic_sim* sim, const double* uniforms);
+/* Emitter::inject of emitter k alone (src/emitter.cpp:5-36), as the loop calls
+ * it per emitter (src/main.cpp:397-403); uniforms: its numparticle rows of 14
+ * or null.  The injection counter that keys the Philox streams advances after
+ * the last emitter, so calling it for every emitter in order equals one
+ * epic_inject. */
+epic_status epic_inject_emitter(epic_sim* sim, int k, const double* uniforms);
 
 /* Grid download/upload (which = EPIC_GRID_*, EPIC_GRID_DEN0 + s). */
 epic_status epic_get_grid(epic_sim* sim, int which, double* out);
@@ -309,6 +338,17 @@ epic_status epic_set_profiling(epic_sim* sim, int enable);
 epic_status epic_get_profile(epic_sim* sim, double ms[EPIC_NUM_PHASES], int64_t counts[EPIC_NUM_PHASES],
                              int64_t* solver_iterations);
 
+/* Poll limit of the device-side waits (no counterpart in the reference,
+ * which has no device waits): the grid barriers of the PCG and red-black SOR
+ * solvers and the ordered tile look-back of the compacting pushes give up at
+ * the `polls`-th unsuccessful poll and return, and the call that waited on the
+ * kernel reports EPIC_ERR_TIMEOUT (the results of that kernel are void).
+ * polls <= 0 restores the default (2^24 polls, far longer than any healthy
+ * wait).  Process-wide; applies to launches made after the call (a step graph
+ * keeps the limit it was captured with).  Meant for tests of the timeout
+ * path: a limit of a few polls makes a healthy wait give up. */
+epic_status epic_set_spin_limit(long long polls);
+
 /* PCG solve with no device allocation (no counterpart in the reference: its
  * solver allocates dense matrices and vectors on every call).
  *
@@ -322,11 +362,14 @@ epic_status epic_get_profile(epic_sim* sim, double ms[EPIC_NUM_PHASES], int64_t 
  * the same phi), with all workspace in one static device array compiled into
  * the library: at most 257 x 257 nodes (larger grids return
  * EPIC_ERR_CAPACITY).  Every GPU that loads the library holds that array
- * (about 4.3 MB) until the library is unloaded.  The first call on each
- * device looks up the array's device address; make that first call before
- * any stream capture.  All calls share the array and leave their data in
- * it; calls whose GPU work overlaps race, so order them on one stream.
- * stream is a cudaStream_t (NULL: the default stream); the call waits for it. */
+ * (about 4.3 MB) until the library is unloaded.  Every call looks up the
+ * array's device address on the current device (a host-side query; it stays
+ * right after a device reset); the first call on a device also loads the
+ * library's device code there, so make that first call before any stream
+ * capture.  All calls share the array and leave their data in it; calls whose
+ * GPU work overlaps race, so order them on one stream.  stream is a
+ * cudaStream_t (NULL: the default stream); the call waits for the stream to
+ * finish the solve, then reads the outcome back. */
 epic_status epic_pcg_solve_static(const double* rho, double* phi, int nx, int ny, double dx, double K,
                                   double tolerance, int max_iteration, void* stream, int* iterations,
                                   double* error);

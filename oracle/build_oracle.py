@@ -24,7 +24,9 @@ from concurrent.futures import ThreadPoolExecutor
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-REFERENCE = os.environ.get("EPIC_REFERENCE_DIR", "/root/reference")
+# The reference checkout: EPIC_REFERENCE_DIR, else a "reference" directory
+# beside this repository's root.
+REFERENCE = os.environ.get("EPIC_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 REF_SOURCES = ["domain", "species", "field", "collision", "cross_section", "init",
                "grid", "electrode", "iniparser", "emitter"]
 

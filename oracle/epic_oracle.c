@@ -8,6 +8,7 @@
 #include "epic_oracle.h"
 
 #include <math.h>
+#include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -176,7 +177,9 @@ int or_load_c(const or_domain* d, or_rng* r, const char* type, int n_arg, double
     }
     double vx = or_sample_vel(r, mass, temp) + vsx * d->vel_norm;
     double vy = or_sample_vel(r, mass, temp) + vsy * d->vel_norm;
-    double vz = 0;
+    /* The reference loads vz = 0 (src/init.cpp:88, with SampleVel commented
+     * out there); the 3V extension draws it like vx and vy, after them. */
+    double vz = d->load_3v ? or_sample_vel(r, mass, temp) : 0;
     vx /= d->vel_norm;
     vy /= d->vel_norm;
     vz /= d->vel_norm;
@@ -307,11 +310,260 @@ void or_compute_rho(const or_domain* d, int nsp, const double* const* dens, cons
   }
 }
 
+static double dot(const double* a, const double* b, long n);
+
+/* ------------------------------------------------ Poisson extensions --- */
+/* Extensions with no reference counterpart (restatements of this project's
+ * own definitions; the tests pin them against direct solves).  The reference
+ * solves with phi = 0 on all four edges; these put the Poisson problem on
+ *   periodic:     unknowns i in [0, nx-2], j in [0, ny-2], both directions
+ *                 periodic (node nx-1 is node 0, node ny-1 is node 0); the
+ *                 right-hand side is projected onto zero mean and phi is
+ *                 returned with zero mean over the unknowns;
+ *   dirichlet_x:  unknowns i in [1, nx-2], j in [0, ny-2]; phi = 0 on the
+ *                 x walls i = 0 and i = nx-1, periodic in y.
+ * The lattice of unknowns has R rows (x index i = row + i0) of C = ny - 1
+ * columns (y index j = col), index q = row * C + col. */
+
+/* Correctly rounded sum: a long accumulator of 32-bit digits, digit k worth
+ * 2^(32k - 1100), so every finite double is at most three shifted digits and
+ * the total is exact until the single rounding at the end. */
+#define OR_ACC_DIGITS 72
+double or_exact_sum(const double* x, long n) {
+  int64_t acc[OR_ACC_DIGITS];
+  memset(acc, 0, sizeof(acc));
+  for (long t = 0; t < n; t++) {
+    uint64_t b;
+    memcpy(&b, &x[t], 8);
+    int e = (int)((b >> 52) & 0x7FF);
+    uint64_t m = b & 0xFFFFFFFFFFFFFull;
+    if (e == 0x7FF) return NAN;
+    if (e) m |= 1ull << 52;
+    else e = 1;
+    if (!m) continue;
+    const int p = e + 25; /* m * 2^(e - 1075) = m * 2^(p - 1100) */
+    const int k = p / 32, sft = p % 32;
+    const unsigned __int128 v = (unsigned __int128)m << sft;
+    const int64_t d0 = (int64_t)(uint32_t)v, d1 = (int64_t)(uint32_t)(v >> 32), d2 = (int64_t)(uint32_t)(v >> 64);
+    if (b >> 63) {
+      acc[k] -= d0; acc[k + 1] -= d1; acc[k + 2] -= d2;
+    } else {
+      acc[k] += d0; acc[k + 1] += d1; acc[k + 2] += d2;
+    }
+  }
+  /* digits to [0, 2^32) with the carries moved up; the top digit keeps the sign */
+  for (int k = 0; k < OR_ACC_DIGITS - 1; k++) {
+    const int64_t c = acc[k] >> 32;
+    acc[k] -= c * ((int64_t)1 << 32);
+    acc[k + 1] += c;
+  }
+  const int neg = acc[OR_ACC_DIGITS - 1] < 0;
+  if (neg) {
+    for (int k = 0; k < OR_ACC_DIGITS; k++) acc[k] = -acc[k];
+    for (int k = 0; k < OR_ACC_DIGITS - 1; k++) {
+      const int64_t c = acc[k] >> 32;
+      acc[k] -= c * ((int64_t)1 << 32);
+      acc[k + 1] += c;
+    }
+  }
+  int h = OR_ACC_DIGITS - 1;
+  while (h >= 0 && acc[h] == 0) h--;
+  if (h < 0) return 0.0;
+  /* 128-bit window of the top four digits, and whether anything lies below */
+  unsigned __int128 W = 0;
+  for (int k = h; k >= h - 3; k--) W = (W << 32) | (uint64_t)(k >= 0 ? acc[k] : 0);
+  int sticky = 0;
+  for (int k = h - 4; k >= 0; k--) sticky |= acc[k] != 0;
+  int len = 0;
+  for (unsigned __int128 t = W; t; t >>= 1) len++;
+  const int drop = len - 53;
+  uint64_t mant = (uint64_t)(W >> drop);
+  const unsigned __int128 rem = W & (((unsigned __int128)1 << drop) - 1);
+  const unsigned __int128 half = (unsigned __int128)1 << (drop - 1);
+  if (rem > half || (rem == half && (sticky || (mant & 1)))) mant++;
+  const double res = ldexp((double)mant, drop + 32 * (h - 3) - 1100);
+  return neg ? -res : res;
+}
+
+typedef struct {
+  int R, C, i0, wrap_x;
+} or_lattice;
+
+static or_lattice lattice_of(const or_domain* d) {
+  or_lattice L;
+  L.i0 = d->poisson_bc == OR_POISSON_PERIODIC ? 0 : 1;
+  L.wrap_x = d->poisson_bc == OR_POISSON_PERIODIC;
+  L.R = d->nx - 1 - L.i0;
+  L.C = d->ny - 1;
+  return L;
+}
+
+/* The duplicated nodes after a solve: periodic copies (x first, so the corner
+ * takes node (0, 0)) and zero x walls. */
+static void fill_periodic_nodes(const or_domain* d, double* phi) {
+  const int nx = d->nx, ny = d->ny;
+  if (d->poisson_bc == OR_POISSON_PERIODIC)
+    for (int j = 0; j < ny - 1; j++) phi[IDX(nx - 1, j)] = phi[IDX(0, j)];
+  for (int i = 0; i < nx; i++) phi[IDX(i, ny - 1)] = phi[IDX(i, 0)];
+  if (d->poisson_bc == OR_POISSON_DIRICHLET_X)
+    for (int j = 0; j < ny; j++) phi[IDX(0, j)] = phi[IDX(nx - 1, j)] = 0;
+}
+
+/* Subtracts the (correctly rounded) mean of the unknowns' values v[q]. */
+static void remove_mean(double* v, long m) {
+  const double mean = or_exact_sum(v, m) / (double)m;
+  for (long q = 0; q < m; q++) v[q] = v[q] - mean;
+}
+
+/* gssolver's sweep on the extension lattices: lexicographic (i outer, j
+ * inner) in-place SOR of the same update with wrapped neighbours, the source
+ * rho*K (minus its mean when periodic), the L2 residual over the unknowns
+ * checked after sweeps 0, 25, 50, ... as sqrt(sum / (nx*ny)). */
+static int gs_solve_ext(const or_domain* d, double omega, const double* rho, double* phi, double* err, int* iters) {
+  const int nx = d->nx, ny = d->ny;
+  const or_lattice L = lattice_of(d);
+  const long m = (long)L.R * L.C;
+  double dx2 = d->dx * d->dx, dy2 = d->dy * d->dy;
+  const double K = (d->L * d->L) / (d->LDe * d->LDe);
+  double* src = (double*)malloc(sizeof(double) * m);
+  for (int r = 0; r < L.R; r++)
+    for (int c = 0; c < L.C; c++) src[(long)r * L.C + c] = rho[IDX(r + L.i0, c)] * K;
+  if (L.wrap_x) remove_mean(src, m);
+  memset(phi, 0, sizeof(double) * (size_t)nx * ny);
+  double L2 = 0;
+  int converged = 0;
+  double coeff = (2 / dx2) + (2 / dy2);
+  int iter;
+#define XE(i) ((i) + 1 < nx - 1 || !L.wrap_x ? (i) + 1 : 0)
+#define XW(i) ((i) > 0 ? (i) - 1 : nx - 2)
+#define YN(j) ((j) + 1 < ny - 1 ? (j) + 1 : 0)
+#define YS(j) ((j) > 0 ? (j) - 1 : ny - 2)
+  for (iter = 0; iter < d->max_iteration; iter++) {
+    for (int r = 0; r < L.R; r++) {
+      const int i = r + L.i0;
+      for (int j = 0; j < L.C; j++) {
+        double phi_new = (1 / coeff) * (src[(long)r * L.C + j] + ((phi[IDX(XE(i), j)] + phi[IDX(XW(i), j)]) / dx2) +
+                                        ((phi[IDX(i, YN(j))] + phi[IDX(i, YS(j))]) / dy2));
+        phi[IDX(i, j)] = phi[IDX(i, j)] + omega * (phi_new - phi[IDX(i, j)]);
+      }
+    }
+    if (iter % 25 == 0) {
+      double sum = 0;
+      for (int r = 0; r < L.R; r++) {
+        const int i = r + L.i0;
+        for (int j = 0; j < L.C; j++) {
+          double R = ((phi[IDX(XE(i), j)] - 2 * phi[IDX(i, j)] + phi[IDX(XW(i), j)]) / dx2) +
+                     ((phi[IDX(i, YN(j))] - 2 * phi[IDX(i, j)] + phi[IDX(i, YS(j))]) / dy2) + src[(long)r * L.C + j];
+          sum += R * R;
+        }
+      }
+      L2 = sqrt(sum / (nx * ny));
+      *err = L2;
+      if (L2 < d->tolerance) {
+        converged = 1;
+        break;
+      }
+    }
+  }
+#undef XE
+#undef XW
+#undef YN
+#undef YS
+  *iters = converged ? iter + 1 : iter;
+  if (L.wrap_x) {
+    double* u = (double*)malloc(sizeof(double) * m);
+    for (int r = 0; r < L.R; r++)
+      for (int c = 0; c < L.C; c++) u[(long)r * L.C + c] = phi[IDX(r + L.i0, c)];
+    remove_mean(u, m);
+    for (int r = 0; r < L.R; r++)
+      for (int c = 0; c < L.C; c++) phi[IDX(r + L.i0, c)] = u[(long)r * L.C + c];
+    free(u);
+  }
+  fill_periodic_nodes(d, phi);
+  free(src);
+  return converged;
+}
+
+/* Row q of the extension operator (diagonal -4, wrapped neighbours; beyond
+ * the x walls nothing), terms added as the reference's pcg_row adds them:
+ * x neighbour below, y neighbour below, the diagonal, y above, x above. */
+static double lat_row(const or_lattice* L, const double* v, int r, int c) {
+  const int R = L->R, C = L->C;
+  double sum = 0;
+  if (r > 0) sum += v[(long)(r - 1) * C + c];
+  else if (L->wrap_x) sum += v[(long)(R - 1) * C + c];
+  sum += v[(long)r * C + (c > 0 ? c - 1 : C - 1)];
+  sum += -4 * v[(long)r * C + c];
+  sum += v[(long)r * C + (c < C - 1 ? c + 1 : 0)];
+  if (r < R - 1) sum += v[(long)(r + 1) * C + c];
+  else if (L->wrap_x) sum += v[c];
+  return sum;
+}
+
+/* pcgsolver's right-hand side -rho*dx^2*K on the extension lattices (minus
+ * its mean when periodic), then pcg() of linearalgebra/solvers.h:73-100 as
+ * or_pcg_solve runs it; phi with zero mean when periodic; *err =
+ * |A x - b| / (nx*ny). */
+static int pcg_solve_ext(const or_domain* d, const double* rho, double* phi, double* err, int* iters) {
+  const int nx = d->nx, ny = d->ny;
+  const or_lattice L = lattice_of(d);
+  const long m = (long)L.R * L.C;
+  double dx2 = d->dx * d->dx;
+  const double K = (d->L * d->L) / (d->LDe * d->LDe);
+  double* b = (double*)calloc(m, sizeof(double));
+  double* x = (double*)calloc(m, sizeof(double));
+  double* r = (double*)calloc(m, sizeof(double));
+  double* w = (double*)calloc(m, sizeof(double));
+  double* v = (double*)calloc(m, sizeof(double));
+  double* u = (double*)calloc(m, sizeof(double));
+  for (int rr = 0; rr < L.R; rr++)
+    for (int c = 0; c < L.C; c++) b[(long)rr * L.C + c] = -rho[IDX(rr + L.i0, c)] * dx2 * K;
+  if (L.wrap_x) remove_mean(b, m);
+  for (long k = 0; k < m; k++) r[k] = b[k] - 0.0;
+  double minv = 1.0 / -4.0;
+  for (long k = 0; k < m; k++) { w[k] = minv * r[k]; v[k] = w[k]; }
+  double alpha = dot(w, r, m);
+  /* min(m*m, max_iteration) as pcg() caps it, with m*m in 64 bits (the
+   * reference's 32-bit product wraps negative for lattices this size). */
+  const long long cap = (long long)m * m;
+  int maxit = cap < d->max_iteration ? (int)cap : d->max_iteration;
+  int it = 0;
+  for (it = 0; it < maxit; it++) {
+    if (sqrt(dot(r, r, m)) < d->tolerance) break;
+    for (int rr = 0; rr < L.R; rr++)
+      for (int c = 0; c < L.C; c++) u[(long)rr * L.C + c] = lat_row(&L, v, rr, c);
+    double t = alpha / dot(v, u, m);
+    for (long k = 0; k < m; k++) x[k] = x[k] + v[k] * t;
+    for (long k = 0; k < m; k++) r[k] = r[k] - u[k] * t;
+    for (long k = 0; k < m; k++) w[k] = minv * r[k];
+    double beta = dot(w, r, m);
+    double s = beta / alpha;
+    for (long k = 0; k < m; k++) v[k] = w[k] + v[k] * s;
+    alpha = beta;
+  }
+  double e2 = 0;
+  for (int rr = 0; rr < L.R; rr++)
+    for (int c = 0; c < L.C; c++) {
+      double e = lat_row(&L, x, rr, c) - b[(long)rr * L.C + c];
+      e2 += e * e;
+    }
+  *err = sqrt(e2) / ((long)nx * ny);
+  *iters = it;
+  if (L.wrap_x) remove_mean(x, m);
+  memset(phi, 0, sizeof(double) * (size_t)nx * ny);
+  for (int rr = 0; rr < L.R; rr++)
+    for (int c = 0; c < L.C; c++) phi[IDX(rr + L.i0, c)] = x[(long)rr * L.C + c];
+  fill_periodic_nodes(d, phi);
+  free(b); free(x); free(r); free(w); free(v); free(u);
+  return it < maxit;
+}
+
 /* ------------------------------------------------------------ solvers --- */
 /* FieldSolve::gssolver (src/field.cpp:70-139): cold start, phi = 0 on every
  * edge, lexicographic (i outer, j inner) in-place SOR, L2 residual check
  * after sweeps 0, 25, 50, ... */
 int or_gs_solve(const or_domain* d, double omega, const double* rho, double* phi, double* err, int* iters) {
+  if (d->poisson_bc != OR_POISSON_REFERENCE) return gs_solve_ext(d, omega, rho, phi, err, iters);
   const int nx = d->nx, ny = d->ny;
   double dx2 = d->dx * d->dx, dy2 = d->dy * d->dy;
   memset(phi, 0, sizeof(double) * (size_t)nx * ny);
@@ -517,6 +769,7 @@ static double dot(const double* a, const double* b, long n) {
  * function.h:97-105 (1/(-4) on the diagonal).  The iteration cap is
  * min(n*n, max_iteration) with n*n in 32-bit int arithmetic, as the reference. */
 int or_pcg_solve(const or_domain* d, const double* rho, double* phi, double* err, int* iters) {
+  if (d->poisson_bc != OR_POISSON_REFERENCE) return pcg_solve_ext(d, rho, phi, err, iters);
   const int nx = d->nx, ny = d->ny;
   const long n = (long)nx * ny;
   double dx2 = d->dx * d->dx;
@@ -563,19 +816,32 @@ int or_pcg_solve(const or_domain* d, const double* rho, double* phi, double* err
   return it < maxit;
 }
 
-/* FieldSolve::CalculateEfield (src/field.cpp:276-330). */
+/* FieldSolve::CalculateEfield (src/field.cpp:276-330).  The edge formulas
+ * follow bc as there (periodic central for pbc, one-sided otherwise); with a
+ * Poisson extension they follow the field's boundary instead: periodic
+ * directions take the periodic central formula, the x walls of dirichlet_x
+ * the one-sided one. */
 void or_efield(const or_domain* d, const double* phi, double* efx, double* efy) {
   const int nx = d->nx, ny = d->ny;
   const double dx = d->dx, dy = d->dy;
+  int x_periodic = d->bc == OR_PBC, x_onesided = d->bc == OR_OPEN || d->bc == OR_REFLECTIVE;
+  int y_periodic = x_periodic, y_onesided = x_onesided;
+  if (d->poisson_bc == OR_POISSON_PERIODIC) {
+    x_periodic = y_periodic = 1;
+    x_onesided = y_onesided = 0;
+  } else if (d->poisson_bc == OR_POISSON_DIRICHLET_X) {
+    x_periodic = 0; x_onesided = 1;
+    y_periodic = 1; y_onesided = 0;
+  }
   for (int i = 1; i < nx - 1; i++)
     for (int j = 0; j < ny; j++) efx[IDX(i, j)] = -(phi[IDX(i + 1, j)] - phi[IDX(i - 1, j)]) / (2 * dx);
-  if (d->bc == OR_OPEN || d->bc == OR_REFLECTIVE) {
+  if (x_onesided) {
     for (int j = 0; j < ny; j++) {
       efx[IDX(0, j)] = -(phi[IDX(1, j)] - phi[IDX(0, j)]) / dx;
       efx[IDX(nx - 1, j)] = -(phi[IDX(nx - 1, j)] - phi[IDX(nx - 2, j)]) / dx;
     }
   }
-  if (d->bc == OR_PBC) {
+  if (x_periodic) {
     for (int j = 0; j < ny; j++) {
       efx[IDX(0, j)] = -(phi[IDX(1, j)] - phi[IDX(nx - 2, j)]) / (2 * dx);
       efx[IDX(nx - 1, j)] = efx[IDX(0, j)];
@@ -583,13 +849,13 @@ void or_efield(const or_domain* d, const double* phi, double* efx, double* efy) 
   }
   for (int i = 0; i < nx; i++)
     for (int j = 1; j < ny - 1; j++) efy[IDX(i, j)] = -(phi[IDX(i, j + 1)] - phi[IDX(i, j - 1)]) / (2 * dy);
-  if (d->bc == OR_OPEN || d->bc == OR_REFLECTIVE) {
+  if (y_onesided) {
     for (int i = 0; i < nx; i++) {
       efy[IDX(i, 0)] = -(phi[IDX(i, 1)] - phi[IDX(i, 0)]) / dy;
       efy[IDX(i, ny - 1)] = -(phi[IDX(i, ny - 1)] - phi[IDX(i, ny - 2)]) / dy;
     }
   }
-  if (d->bc == OR_PBC) {
+  if (y_periodic) {
     for (int i = 0; i < nx; i++) {
       efy[IDX(i, 0)] = -(phi[IDX(i, 1)] - phi[IDX(i, ny - 2)]) / (2 * dy);
       efy[IDX(i, ny - 1)] = efy[IDX(i, 0)];

@@ -56,7 +56,15 @@ typedef struct {
   int max_iteration;
   double gas_density;
   int elastic, excitation, ionization;
+  /* Extensions with no reference counterpart (0 = the reference's behaviour):
+   * poisson_bc 0 = the reference's solvers (zero on every edge), 1 = periodic
+   * in x and y, 2 = phi = 0 on the x walls and periodic in y; load_3v 1 =
+   * vz drawn like vx and vy (the reference loads vz = 0). */
+  int poisson_bc;
+  int load_3v;
 } or_domain;
+
+enum { OR_POISSON_REFERENCE = 0, OR_POISSON_PERIODIC = 1, OR_POISSON_DIRICHLET_X = 2 };
 
 /* mt19937 + std::generate_canonical<double, 53> (two 32-bit draws per double). */
 void or_rng_seed(or_rng* r, uint32_t seed);
@@ -82,6 +90,8 @@ int or_gs_solve(const or_domain* d, double omega, const double* rho, double* phi
 /* FieldSolve::pcgsolver (src/field.cpp:212-264) with pcg() of
  * linearalgebra/solvers.h:73-100; *err = |A x - b| / n as the reference. */
 int or_pcg_solve(const or_domain* d, const double* rho, double* phi, double* err, int* iters);
+/* Correctly rounded sum of n doubles (any order gives the same result). */
+double or_exact_sum(const double* x, long n);
 /* FieldSolve::CalculateEfield (src/field.cpp:276-330). */
 void or_efield(const or_domain* d, const double* phi, double* efx, double* efy);
 /* Species::Push_species_serial (src/species.cpp:29-170), no conductors.

@@ -35,6 +35,9 @@ EV = 1.602176565e-19
 CS_RANGES = 5_000_000
 
 BC_CODES = {"pbc": 0, "open": 1, "reflective": 2}
+# [solver] poisson_bc (extension): the reference's zero edges, periodic, or
+# zero on the x walls and periodic in y
+POISSON_BC_CODES = {"dirichlet": 0, "periodic": 1, "dirichlet_x": 2}
 SHAPE_CODES = {"CIC": 0, "NGP": 1}
 
 
@@ -142,6 +145,8 @@ class Setup:
     normscheme: int
     species: list = field(default_factory=list)
     sor_omega: float = 1.4  # optional [solver] sor_omega; 1.4 is hard-coded in src/field.cpp:114
+    poisson_bc: str = "dirichlet"  # optional [solver] poisson_bc (extension)
+    load_3v: bool = False  # optional [simulation] load_3v: vz drawn like vx, vy (the reference loads 0)
     # [Grids] (src/main.cpp:284-327) as rows of 8 doubles: {0, min_x, max_x, min_y, max_y, 0, 0, V}
     # (reactconduct) or {1, x_center, y_center, electrode_number, grid_radius, electrod_radius, 0, V}
     grids: np.ndarray = field(default_factory=lambda: np.zeros((0, 8)))
@@ -233,6 +238,8 @@ def setup(path: str) -> Setup:
                  elastic=string_to_bool(col["elastic"]), excitation=string_to_bool(col["excitation"]),
                  ionization=string_to_bool(col["ionization"]), num_ts=num_ts, ionfixed=_stoi(sim["ionfixed"]),
                  normscheme=norm_scheme, species=species, sor_omega=_stod(solver.get("sor_omega", "1.4")),
+                 poisson_bc=solver.get("poisson_bc", "dirichlet"),
+                 load_3v=string_to_bool(sim.get("load_3v", "false")),
                  grids=conductors(ini), emitters=emitters(ini))
 
 
@@ -285,7 +292,8 @@ class _Domain(ctypes.Structure):
                 ("shape", ctypes.c_int), ("bc", ctypes.c_int),
                 ("tolerance", ctypes.c_double), ("max_iteration", ctypes.c_int),
                 ("gas_density", ctypes.c_double),
-                ("elastic", ctypes.c_int), ("excitation", ctypes.c_int), ("ionization", ctypes.c_int)]
+                ("elastic", ctypes.c_int), ("excitation", ctypes.c_int), ("ionization", ctypes.c_int),
+                ("poisson_bc", ctypes.c_int), ("load_3v", ctypes.c_int)]
 
 
 class _Rng(ctypes.Structure):
@@ -306,7 +314,8 @@ def _p(a):
 def domain_struct(s: Setup) -> _Domain:
     return _Domain(s.nx, s.ny, s.x0, s.y0, s.dx, s.dy, s.Lx, s.Ly, s.DT, s.L, s.W, s.vel_norm, s.LDe, s.wpe,
                    s.density, SHAPE_CODES[s.shape], BC_CODES.get(s.bc, -1), s.tolerance, s.max_iteration,
-                   s.gas_density, int(s.elastic), int(s.excitation), int(s.ionization))
+                   s.gas_density, int(s.elastic), int(s.excitation), int(s.ionization),
+                   POISSON_BC_CODES[s.poisson_bc], int(s.load_3v))
 
 
 _LIB = None
@@ -341,6 +350,8 @@ def restatement_lib():
         L.or_gs_solve.argtypes = [vp, d, vp, vp, vp, vp]
         L.or_pcg_solve.argtypes = [vp, vp, vp, vp, vp]
         L.or_efield.argtypes = [vp, vp, vp, vp]
+        L.or_exact_sum.argtypes = [vp, l]
+        L.or_exact_sum.restype = d
         L.or_push.argtypes = [vp, d, d, i, vp, l, vp, vp]
         L.or_push.restype = l
         L.or_rewind.argtypes = [vp, d, d, vp, l, vp, vp]
