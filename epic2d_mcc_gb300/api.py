@@ -142,6 +142,11 @@ def lib() -> ctypes.CDLL:
         "epic_step_host": ([vp, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
                            st),
         "epic_initial_field": ([vp], st),
+        "epic_run_host": ([vp, i, i, ctypes.POINTER(vp), ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)],
+                          st),
+        "epic_init_species": ([vp, i], st),
+        "epic_inject_emitter": ([vp, i, vp], st),
+        "epic_set_spin_limit": ([ctypes.c_longlong], st),
         "epic_run": ([vp, i, i, i], st),
         "epic_compute_ke": ([vp, i, i, vp], st),
         "epic_compute_momentum": ([vp, i, i, vp], st),
@@ -360,6 +365,24 @@ class Simulation:
         cap = (ctypes.c_int64 * nsp)(*[len(b) for b in bufs])
         _check(lib().epic_step_host(self._h, int(collisions), ptrs, n, cap))
         return [int(v) for v in n]
+
+    def run_host(self, bufs, counts, steps: int, collisions: bool = False):
+        """`steps` steps of particles held in host arrays (epic_run_host): bufs[s] is a (capacity, 5)
+        float64 array whose first counts[s] rows are species s; every step's records go to the
+        arrays and back; returns the final counts.  Pinned arrays take the copy-engine path."""
+        nsp = len(self.species)
+        for b in bufs:
+            if b.dtype != np.float64 or not b.flags["C_CONTIGUOUS"] or b.ndim != 2 or b.shape[1] != 5:
+                raise ValueError("each buffer must be a C-contiguous (capacity, 5) float64 array")
+        ptrs = (ctypes.c_void_p * nsp)(*[b.ctypes.data for b in bufs])
+        n = (ctypes.c_int64 * nsp)(*[int(c) for c in counts])
+        cap = (ctypes.c_int64 * nsp)(*[len(b) for b in bufs])
+        _check(lib().epic_run_host(self._h, int(steps), int(collisions), ptrs, n, cap))
+        return [int(v) for v in n]
+
+    def init_species(self, sp: int):
+        """Init of one species from the handle's copy of the reference's generator (epic_init_species)."""
+        _check(lib().epic_init_species(self._h, sp))
 
     def initial_field(self):
         _check(lib().epic_initial_field(self._h))

@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstdarg>
@@ -545,7 +546,9 @@ epic_status do_inject(epic_sim* s, const double* d_uniforms) {
 }
 
 // sort: -1 by the step counter and cfg.sort_every, 0 never, 1 always.
-epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
+// A step is do_step_field (emitters, cell sort, deposit, rho, solve, E-field)
+// then do_step_move (push, MCC, deposit of the MCC's products).
+epic_status do_step_field(epic_sim* s, int sort = -1) {
   epic_status st;
   const int nsp = (int)s->sp.size();
   if (!s->emitters.empty() && (st = do_inject(s, nullptr))) return st;  // src/main.cpp:397-403
@@ -560,7 +563,13 @@ epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
       if ((st = do_deposit(s, i))) return st;
   if ((st = do_finalize(s, FINALIZE_AND_RHO, -1))) return st;
   if ((st = do_solve(s))) return st;
-  if ((st = do_efield(s))) return st;
+  return do_efield(s);
+}
+
+epic_status do_step_move(epic_sim* s, int with_collisions) {
+  epic_status st;
+  const int nsp = (int)s->sp.size();
+  const bool fused = fused_deposit(s);
   // The MCC's selection pass folded into the electrons' push (the same test on
   // the same post-push velocities, one pass over them fewer).
   const bool coll = with_collisions && nsp >= 2;
@@ -597,6 +606,12 @@ epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
     }
   }
   return EPIC_OK;
+}
+
+epic_status do_step(epic_sim* s, int with_collisions, int sort = -1) {
+  epic_status st = do_step_field(s, sort);
+  if (st) return st;
+  return do_step_move(s, with_collisions);
 }
 
 }  // namespace
@@ -859,6 +874,16 @@ void epic_destroy(epic_sim* s) {
   if (!s) return;
   if (s->ref_rng) ref_stream_destroy(static_cast<RefStream*>(s->ref_rng));
   if (s->stream) cudaStreamSynchronize(s->stream);
+  if (s->xfer_out) {
+    cudaStreamSynchronize(s->xfer_out);
+    cudaStreamSynchronize(s->xfer_in);
+    cudaStreamDestroy(s->xfer_out);
+    cudaStreamDestroy(s->xfer_in);
+  }
+  for (cudaEvent_t e : s->xfer_ev) cudaEventDestroy(e);
+  if (s->h_counts) cudaFreeHost(s->h_counts);
+  if (s->host_in) dfree(s, s->host_in);
+  if (s->host_out) dfree(s, s->host_out);
   if (s->graph_exec) cudaGraphExecDestroy(s->graph_exec);
   if (s->graph_exec_sort) cudaGraphExecDestroy(s->graph_exec_sort);
   if (s->sort_buf) dfree(s, s->sort_buf);
@@ -1313,6 +1338,144 @@ epic_status epic_step_host(epic_sim* s, int with_collisions, double* const* part
   if ((st = sync(s))) return st;
   for (int k = 0; k < nsp; k++) n[k] = cnt[k];
   return EPIC_OK;
+}
+
+// Several loop iterations for particles the caller holds in host memory,
+// with every step's records going to the host and back: after each step the
+// stepped records are copied device-to-host into the caller's buffers, and
+// the next step's push takes its input records copied host-to-device from
+// those buffers.  The copies run on two copy-engine streams, chunk by chunk
+// (the host-to-device copy of a chunk follows its device-to-host copy, so the
+// two directions of the link work at once), while the SMs run the next
+// step's deposit, Poisson solve and E-field, which need no particle records
+// (the push deposited the new positions as it moved them).
+constexpr size_t RUN_HOST_CHUNK_BYTES = 32u << 20;
+
+static epic_status run_host_streams(epic_sim* s, size_t doubles, int nevents) {
+  if (!s->xfer_out) {
+    CK(cudaStreamCreateWithFlags(&s->xfer_out, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&s->xfer_in, cudaStreamNonBlocking));
+  }
+  while ((int)s->xfer_ev.size() < nevents) {
+    cudaEvent_t e;
+    CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    s->xfer_ev.push_back(e);
+  }
+  if (!s->h_counts) CK(cudaMallocHost((void**)&s->h_counts, 8 * sizeof(long long)));
+  if (doubles > s->host_stage_doubles) {
+    if (s->host_in) dfree(s, s->host_in);
+    if (s->host_out) dfree(s, s->host_out);
+    s->host_in = s->host_out = nullptr;
+    s->host_stage_doubles = 0;
+    CK(cudaMallocAsync((void**)&s->host_in, doubles * sizeof(double), s->stream));
+    CK(cudaMallocAsync((void**)&s->host_out, doubles * sizeof(double), s->stream));
+    s->host_stage_doubles = doubles;
+  }
+  return EPIC_OK;
+}
+
+epic_status epic_run_host(epic_sim* s, int steps, int with_collisions, double* const* parts, int64_t* n,
+                          const int64_t* capacity) {
+  if (!s || !parts || !n || !capacity || steps < 0) return fail(EPIC_ERR_INVALID, "bad argument");
+  const int nsp = (int)s->sp.size();
+  for (int k = 0; k < nsp; k++) {
+    if (n[k] < 0 || n[k] > capacity[k] || (n[k] > 0 && !parts[k]))
+      return fail(EPIC_ERR_INVALID, "bad particle buffer for species %d", k);
+    if (n[k] > s->sp[k].cap)
+      return fail(EPIC_ERR_CAPACITY, "%lld particles exceed the capacity %lld of %s", (long long)n[k], s->sp[k].cap,
+                  s->sp[k].name.c_str());
+  }
+  if (steps == 0) return EPIC_OK;
+  const epic_config& c = s->cfg;
+  bool direct = !s->mixed && fused_deposit(s) && c.sort_every == 0 && nsp <= 8;
+  for (int k = 0; k < nsp && direct; k++) {
+    cudaPointerAttributes at;
+    if (cudaPointerGetAttributes(&at, parts[k]) != cudaSuccess || at.type != cudaMemoryTypeHost) {
+      cudaGetLastError();
+      direct = false;
+    }
+  }
+  epic_status st;
+  if (!direct) {  // the same round trips, step by step
+    for (int t = 0; t < steps; t++)
+      if ((st = epic_step_host(s, with_collisions, parts, n, capacity))) return st;
+    return EPIC_OK;
+  }
+  std::vector<size_t> off(nsp + 1, 0);
+  for (int k = 0; k < nsp; k++) off[k + 1] = off[k] + (size_t)s->sp[k].cap * 5;
+  const int max_chunks = 256;
+  if ((st = run_host_streams(s, off[nsp], max_chunks + 2))) return st;
+  cudaEvent_t ev_out_ready = s->xfer_ev[0], ev_in_done = s->xfer_ev[1];
+  std::vector<long long> cnt(n, n + nsp);
+  // Chunks of the records of every species: (species, first record, records).
+  auto chunks = [&](std::vector<std::array<long long, 3>>& out) {
+    out.clear();
+    long long total = 0;
+    for (int k = 0; k < nsp; k++) total += cnt[k];
+    const long long per = std::max<long long>(
+        std::max<long long>(1, (long long)(RUN_HOST_CHUNK_BYTES / 40)), (total + max_chunks - nsp - 1) / (max_chunks - nsp));
+    for (int k = 0; k < nsp; k++)
+      for (long long a = 0; a < cnt[k]; a += per) out.push_back({k, a, std::min(per, cnt[k] - a)});
+  };
+  auto soa_from_stage = [&]() -> epic_status {
+    for (int k = 0; k < nsp; k++) {
+      if (cnt[k] > 0)
+        k_aos_to_soa<<<s->part_grid, 256, 0, s->stream>>>(s->host_in + off[k], s->sp[k].soa, cnt[k]);
+      launch_set_count(s->stream, s->sp[k].d_n, cnt[k]);
+      s->launches += 2;
+    }
+    CKL();
+    return EPIC_OK;
+  };
+  // Inputs of the first step.
+  invalidate_acc(s);
+  for (int k = 0; k < nsp; k++)
+    if (cnt[k] > 0)
+      CK(cudaMemcpyAsync(s->host_in + off[k], parts[k], (size_t)cnt[k] * 40, cudaMemcpyHostToDevice, s->stream));
+  if ((st = soa_from_stage())) return st;
+  if ((st = do_step_field(s))) return st;
+  std::vector<std::array<long long, 3>> ch;
+  for (int t = 0; t < steps; t++) {
+    if (t > 0) {  // this step's input records, back from the host
+      CK(cudaStreamWaitEvent(s->stream, ev_in_done, 0));
+      if ((st = soa_from_stage())) return st;
+    }
+    if ((st = do_step_move(s, with_collisions))) return st;
+    for (int k = 0; k < nsp; k++) {
+      k_soa_to_aos<<<s->part_grid, 256, 0, s->stream>>>(s->host_out + off[k], s->sp[k].soa, s->sp[k].d_n);
+      CK(cudaMemcpyAsync(s->h_counts + k, s->sp[k].d_n, sizeof(long long), cudaMemcpyDeviceToHost, s->stream));
+      s->launches += 1;
+    }
+    CKL();
+    CK(cudaEventRecord(ev_out_ready, s->stream));
+    if (t + 1 < steps && (st = do_step_field(s))) return st;  // the SMs go on while the records travel
+    CK(cudaEventSynchronize(ev_out_ready));
+    bool over = false;
+    for (int k = 0; k < nsp; k++) {
+      cnt[k] = s->h_counts[k];
+      over |= cnt[k] > capacity[k];
+    }
+    if (over) {
+      cudaStreamSynchronize(s->stream);
+      return fail(EPIC_ERR_CAPACITY, "a species outgrew the caller's buffer");
+    }
+    chunks(ch);
+    CK(cudaStreamWaitEvent(s->xfer_out, ev_out_ready, 0));
+    for (size_t q = 0; q < ch.size(); q++) {
+      const int k = (int)ch[q][0];
+      const size_t a = (size_t)ch[q][1] * 5, b = (size_t)ch[q][2] * 40;
+      CK(cudaMemcpyAsync(parts[k] + a, s->host_out + off[k] + a, b, cudaMemcpyDeviceToHost, s->xfer_out));
+      if (t + 1 < steps) {
+        CK(cudaEventRecord(s->xfer_ev[2 + q], s->xfer_out));
+        CK(cudaStreamWaitEvent(s->xfer_in, s->xfer_ev[2 + q], 0));
+        CK(cudaMemcpyAsync(s->host_in + off[k] + a, parts[k] + a, b, cudaMemcpyHostToDevice, s->xfer_in));
+      }
+    }
+    if (t + 1 < steps) CK(cudaEventRecord(ev_in_done, s->xfer_in));
+  }
+  CK(cudaStreamSynchronize(s->xfer_out));
+  for (int k = 0; k < nsp; k++) n[k] = cnt[k];
+  return sync(s);
 }
 
 static epic_status do_initial_field(epic_sim* s) {

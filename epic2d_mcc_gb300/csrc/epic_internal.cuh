@@ -405,6 +405,14 @@ struct epic_sim {
   cudaStream_t stream;
   cudaStream_t side = nullptr;  // epic_step_host: electrons pushed beside the other species' transfers
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  // epic_run_host: copy-engine streams for each step's host round trip, their
+  // events, and the records of every species staged in HBM on the way in and out.
+  cudaStream_t xfer_out = nullptr, xfer_in = nullptr;
+  std::vector<cudaEvent_t> xfer_ev;
+  double* host_in = nullptr;
+  double* host_out = nullptr;
+  long long* h_counts = nullptr;  // pinned
+  size_t host_stage_doubles = 0;
   int num_sms;
   int part_grid;
   std::vector<epic_species_state> sp;

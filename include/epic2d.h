@@ -227,6 +227,17 @@ epic_status epic_step(epic_sim* sim, int with_collisions);
  * epic_get_particles.  Same results either way. */
 epic_status epic_step_host(epic_sim* sim, int with_collisions, double* const* parts, int64_t* n,
                            const int64_t* capacity);
+/* `steps` loop iterations (as epic_step_host, step after step) for particles
+ * held in the caller's host buffers, which the caller leaves alone until the
+ * call returns: after every step the stepped records are copied into the
+ * buffers, and every step's push reads its input records copied from them.
+ * With pinned buffers in the FP64 form (periodic or reflective walls, the
+ * fixed-point deposit, no conductors, emitters or cell sort) the copies run
+ * on copy engines, the two directions at once, while the SMs run the next
+ * step's deposit, Poisson solve and E-field; otherwise each step is one
+ * epic_step_host.  On return n[s] holds the counts (ionisation appends). */
+epic_status epic_run_host(epic_sim* sim, int steps, int with_collisions, double* const* parts, int64_t* n,
+                          const int64_t* capacity);
 /* The prologue of src/main.cpp:366-382: scatter, rho, solve, E, rewind. */
 epic_status epic_initial_field(epic_sim* sim);
 /* Runs `steps` loop iterations; with use_graph=1 one step is captured as a
