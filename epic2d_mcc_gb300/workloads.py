@@ -219,15 +219,17 @@ def synthetic_table(n: int = 1000, e_min: float = 0.01, e_max: float = 1000.0):
     return e, ela, exc, ion
 
 
-def serving_requests(seed: int = 0, rate_per_s: float = 50.0, window_s: float = 2.0, sides=(64, 128, 256, 512),
+def serving_requests(seed: int = 0, rate_per_s: float = 50.0, window_s: float = 60.0, sides=(64, 128, 256, 512),
                      ppc=(25, 100), steps=(500, 5000), step_scale: float = 1.0, p_mcc: float = 0.5):
     """Requests of the serving workload: Poisson arrivals at `rate_per_s` over
     `window_s` seconds; per request a square grid side drawn from `sides`,
     particles per cell per species drawn from `ppc`, a step count drawn from
     `steps` and multiplied by `step_scale`, MCC with probability `p_mcc`
-    (synthetic table), and periodic or absorbing (open) walls.  Electrons
-    Te = 1 eV, ions 40 amu at 0.026 eV, PCG to 1e-10.  Returns a list of
-    dicts {ini, steps, collisions, seed, arrival_s, side, particles}."""
+    (synthetic table), and a periodic system (periodic walls and Poisson
+    problem) or a Dirichlet one (phi = 0 on the edges, absorbing walls), each
+    with probability 0.5.  Electrons Te = 1 eV, ions 40 amu at 0.026 eV, PCG
+    to 1e-10.  Returns a list of dicts {ini, steps, collisions, seed,
+    arrival_s, side, particles}."""
     rng = np.random.default_rng(seed)
     out = []
     t = float(rng.exponential(1.0 / rate_per_s))
@@ -237,11 +239,13 @@ def serving_requests(seed: int = 0, rate_per_s: float = 50.0, window_s: float = 
         pe, pi = (int(rng.integers(ppc[0], ppc[1] + 1)) for _ in range(2))
         st = max(1, int(round(int(rng.integers(steps[0], steps[1] + 1)) * step_scale)))
         coll = bool(rng.random() < p_mcc)
-        bc = "pbc" if rng.random() < 0.5 else "open"
+        periodic = rng.random() < 0.5
+        bc = "pbc" if periodic else "open"
         sp = ["electron,%.8E,%d,1,-1,1,0,0,random" % (ME, n * n * pe),
               "ion,%.8E,%d,0.026,1,0,0,0,random" % (40 * AMU, n * n * pi)]
-        ini = _TEMPLATE.format(num_ts=st, dt=0.01, n=n, solver="cg", tol="1e-10", maxit=100000, solver_extra="",
-                               bc=bc, coll="true" if coll else "false", gas="1e20", species="\n".join(sp))
+        ini = _TEMPLATE.format(num_ts=st, dt=0.01, n=n, solver="cg", tol="1e-10", maxit=100000,
+                               solver_extra="poisson_bc = periodic\n" if periodic else "", bc=bc,
+                               coll="true" if coll else "false", gas="1e20", species="\n".join(sp))
         out.append({"ini": ini, "steps": st, "collisions": coll, "seed": 1000 + k, "arrival_s": t, "side": n,
                     "particles": n * n * (pe + pi)})
         k += 1
