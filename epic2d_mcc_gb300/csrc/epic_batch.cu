@@ -35,17 +35,11 @@ __global__ void k_batch_from_aos(BRun r, const double* __restrict__ aos, MixedSo
   bool bad = false;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
     const double* a = aos + 5 * q;
-    double lx = (a[0] - r.x0) / r.dx, ly = (a[1] - r.y0) / r.dy;
-    double fi = floor(lx), fj = floor(ly);
-    int i = (int)fi, j = (int)fj;
-    float ox = (float)(lx - fi), oy = (float)(ly - fj);
-    if (ox >= 1.f) { ox = 0.f; i++; }
-    if (oy >= 1.f) { oy = 0.f; j++; }
-    if (i < 0 || i > r.nx - 2 || j < 0 || j > r.ny - 2) {
-      bad = true;
-      i = min(max(i, 0), r.nx - 2);
-      j = min(max(j, 0), r.ny - 2);
-    }
+    int i, j;
+    float ox, oy;
+    const bool in_x = cell_offset((a[0] - r.x0) / r.dx, r.nx - 1, i, ox);
+    const bool in_y = cell_offset((a[1] - r.y0) / r.dy, r.ny - 1, j, oy);
+    bad |= !(in_x && in_y);
     const long long o = base + q;
     p.cell[o] = (int)(r.node_off + i * r.ny + j);
     p.ox[o] = ox;

@@ -241,14 +241,16 @@ struct PhaseTimer {
 };
 
 // ---- phase launchers (no synchronisation; usable inside stream capture) ----
-// The FP64 step deposits each pushed species while it moves it (k_push with
-// an accumulator) and the MCC's products after the MCC, so the next step's
-// deposit is already in the accumulators: the same fixed-point sums, without
-// a second pass over the positions.  Periodic or reflective walls, fixed-point
-// deposit, no conductors or emitters.
+// The step deposits each pushed species while it moves it (the push kernel
+// with an accumulator) and the MCC's products after the MCC, so the next
+// step's deposit is already in the accumulators: the same integer sums,
+// without a second pass over the positions.  Periodic or reflective walls, no
+// conductors or emitters; the FP64 form with the fixed-point deposit, the
+// mixed form with CIC.
 static bool fused_deposit(const epic_sim* s) {
-  return !s->mixed && s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED && s->conductors.empty() && s->emitters.empty() &&
-         (s->cfg.bc == EPIC_PBC || s->cfg.bc == EPIC_REFLECTIVE);
+  if (!s->conductors.empty() || !s->emitters.empty() || (s->cfg.bc != EPIC_PBC && s->cfg.bc != EPIC_REFLECTIVE))
+    return false;
+  return s->mixed ? s->cfg.shape == EPIC_CIC : s->cfg.deposit_mode == EPIC_DEPOSIT_FIXED;
 }
 
 static void invalidate_acc(epic_sim* s) {
@@ -398,11 +400,14 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle, const SelectArgs* sel = n
     launch_push_conductors(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, s->ef_cell, qmK, cc, dtsub, cs,
                            s->d_flags,
                            s->tile_status, s->tile_ctr, s->part_grid, c.push_order == EPIC_PUSH_CONTRACTED);
-  } else if (s->mixed)
+  } else if (s->mixed) {
+    const bool dep = fused_deposit(s);
+    if (dep) CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
     launch_push_mixed(s->stream, s->g, c.shape, c.bc, sp.mx, sp.d_n, s->ef32, (float)(qmK * dtsub),
                       (float)(cc * dtsub / c.dx), (float)(cc * dtsub / c.dy), s->d_flags, s->tile_status,
-                      s->tile_ctr, s->part_grid);
-  else {
+                      s->tile_ctr, s->part_grid, dep ? sp.acc : nullptr, dep ? sel : nullptr);
+    sp.acc_valid = dep;
+  } else {
     const bool dep = fused_deposit(s);
     if (dep) CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
     launch_push(s->stream, s->g, c.shape, c.bc, sp.soa, sp.d_n, s->ef, s->ef_cell, qmK, cc, dtsub, s->d_flags,
@@ -573,7 +578,7 @@ epic_status do_step_move(epic_sim* s, int with_collisions) {
   // The MCC's selection pass folded into the electrons' push (the same test on
   // the same post-push velocities, one pass over them fewer).
   const bool coll = with_collisions && nsp >= 2;
-  const bool presel = coll && fused && s->cfg.push_order == EPIC_PUSH_CONTRACTED && s->cs.tot &&
+  const bool presel = coll && fused && (s->mixed || s->cfg.push_order == EPIC_PUSH_CONTRACTED) && s->cs.tot &&
                       !(s->cfg.ionfixed == 1 && s->sp[0].name == "ion");
   SelectArgs sel{};
   if (presel) {
@@ -598,8 +603,11 @@ epic_status do_step_move(epic_sim* s, int with_collisions) {
       PhaseTimer t(s, 0);
       for (int k = 0; k < 2; k++) {
         epic_species_state& sp = s->sp[k];
-        launch_deposit_range(s->stream, s->g, s->cfg.shape, sp.soa, s->d_nold + k, sp.d_n, sp.acc, sp.fx_scale,
-                             s->d_flags, s->part_grid);
+        if (s->mixed)
+          launch_deposit_mixed_range(s->stream, s->g, sp.mx, s->d_nold + k, sp.d_n, sp.acc, s->part_grid);
+        else
+          launch_deposit_range(s->stream, s->g, s->cfg.shape, sp.soa, s->d_nold + k, sp.d_n, sp.acc, sp.fx_scale,
+                               s->d_flags, s->part_grid);
         s->launches += 1;
       }
       CKL();

@@ -54,14 +54,34 @@ __device__ __forceinline__ int speed_bin_fp64(double vx, double vy, double vz) {
   return speed_bin_of((int)(m >> 52) - 1023, (int)((m >> 50) & 3));
 }
 
+// The speed bin of an FP32 velocity (the mixed form), on the integer pipe.
+__device__ __forceinline__ int speed_bin_fp32(float vx, float vy, float vz) {
+  const unsigned a = __float_as_uint(vx) & 0x7FFFFFFFu, b = __float_as_uint(vy) & 0x7FFFFFFFu;
+  const unsigned c = __float_as_uint(vz) & 0x7FFFFFFFu;
+  const unsigned m = max(a, max(b, c));
+  const int eb = (int)(m >> 23);  // 0: zero or subnormal (below 2^-126), 255: inf / NaN
+  return speed_bin_of(eb == 255 ? 1 << 20 : eb - 127, (int)((m >> 21) & 3));
+}
+
 // The MCC's first pass for electron q (Philox mode): its first draw against the
 // cut of its speed bin (or cut53 for every bin without a table).
-__device__ __forceinline__ bool mcc_candidate(const SelectArgs& s, long long q, unsigned long long step, double vx,
-                                              double vy, double vz) {
-  const unsigned long long cut = s.bin_cut ? __ldg(&s.bin_cut[speed_bin_fp64(vx, vy, vz)]) : s.cut53;
+__device__ __forceinline__ bool mcc_first_draw_passes(const SelectArgs& s, long long q, unsigned long long step,
+                                                      unsigned long long cut) {
   Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)s.seed, (uint32_t)(s.seed >> 32), 0,
              make_uint4(0, 0, 0, 0)};
   return src.next53() < cut;
+}
+
+__device__ __forceinline__ bool mcc_candidate(const SelectArgs& s, long long q, unsigned long long step, double vx,
+                                              double vy, double vz) {
+  const unsigned long long cut = s.bin_cut ? __ldg(&s.bin_cut[speed_bin_fp64(vx, vy, vz)]) : s.cut53;
+  return mcc_first_draw_passes(s, q, step, cut);
+}
+
+__device__ __forceinline__ bool mcc_candidate(const SelectArgs& s, long long q, unsigned long long step, float vx,
+                                              float vy, float vz) {
+  const unsigned long long cut = s.bin_cut ? __ldg(&s.bin_cut[speed_bin_fp32(vx, vy, vz)]) : s.cut53;
+  return mcc_first_draw_passes(s, q, step, cut);
 }
 
 

@@ -227,9 +227,26 @@ void launch_mixed_to_aos(cudaStream_t st, const Geom& g, double* aos, const Mixe
                          int grid);
 void launch_deposit_mixed(cudaStream_t st, const Geom& g, int shape, const MixedSoA& p, const long long* d_n,
                           unsigned long long* acc, int* flags, int grid);
+// CTAs of `kernel` (threads per CTA, no dynamic shared memory) resident at once
+// on the current device: a grid of one full wave.
+template <class K>
+int resident_grid(K kernel, int threads) {
+  int dev = 0, sms = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
+  return (per > 0 ? per : 1) * (sms > 0 ? sms : 1);
+}
+
+// With dep_acc (CIC, periodic or reflective walls) every pushed particle is
+// also deposited at its new position into dep_acc (integer weights), and with
+// sel the electrons' MCC candidates are appended to sel->cand.
 void launch_push_mixed(cudaStream_t st, const Geom& g, int shape, int bc, const MixedSoA& p, long long* d_n,
                        const float2* ef, float qmK_dt, float cx, float cy, int* flags,
-                       unsigned long long* tile_status, unsigned int* tile_ctr, int grid);
+                       unsigned long long* tile_status, unsigned int* tile_ctr, int grid,
+                       unsigned long long* dep_acc = nullptr, const SelectArgs* sel = nullptr);
+void launch_deposit_mixed_range(cudaStream_t st, const Geom& g, const MixedSoA& p, const long long* d_from,
+                                const long long* d_n, unsigned long long* acc, int grid);
 void launch_rewind_mixed(cudaStream_t st, const Geom& g, int shape, const MixedSoA& p, const long long* d_n,
                          const float2* ef, float hqmK_dt, int* flags, int grid);
 void launch_particle_sums_mixed(cudaStream_t st, int what, const MixedSoA& p, const long long* d_n,

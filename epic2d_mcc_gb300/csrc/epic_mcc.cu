@@ -93,13 +93,7 @@ struct Fp64Particles {
 
 struct MixedParticles {
   MixedSoA p;
-  __device__ int speed_bin(long long q) const {
-    const unsigned a = __float_as_uint(p.vx[q]) & 0x7FFFFFFFu, b = __float_as_uint(p.vy[q]) & 0x7FFFFFFFu;
-    const unsigned c = __float_as_uint(p.vz[q]) & 0x7FFFFFFFu;
-    const unsigned m = max(a, max(b, c));
-    const int eb = (int)(m >> 23);  // 0: zero or subnormal (below 2^-126), 255: inf / NaN
-    return speed_bin_of(eb == 255 ? 1 << 20 : eb - 127, (int)((m >> 21) & 3));
-  }
+  __device__ int speed_bin(long long q) const { return speed_bin_fp32(p.vx[q], p.vy[q], p.vz[q]); }
   __device__ void load_v(long long q, double& a, double& b, double& c) const { a = p.vx[q]; b = p.vy[q]; c = p.vz[q]; }
   __device__ void store_v(long long q, double a, double b, double c) const {
     p.vx[q] = (float)a; p.vy[q] = (float)b; p.vz[q] = (float)c;
@@ -524,7 +518,7 @@ void launch_mcc(cudaStream_t st, int mode, const CrossSections& cs, const Partic
   mcc_select_cut(cs, mode, dt_phys, &m.cut53, &m.bin_cut);
   if (e.mixed)
     launch_mcc_t(st, mode, cs, MixedParticles{e.m}, d_ne, e_cap, MixedParticles{ion.m}, d_ni, i_cap, m, uniforms,
-                 ustride, seed, d_step, ev, d_ncoll, flags, grid, 0);
+                 ustride, seed, d_step, ev, d_ncoll, flags, grid, skip_select);
   else
     launch_mcc_t(st, mode, cs, Fp64Particles{e.f}, d_ne, e_cap, Fp64Particles{ion.f}, d_ni, i_cap, m, uniforms,
                  ustride, seed, d_step, ev, d_ncoll, flags, grid, skip_select);

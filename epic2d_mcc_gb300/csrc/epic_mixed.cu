@@ -25,17 +25,11 @@ __global__ void k_aos_to_mixed(Geom g, const double* __restrict__ aos, MixedSoA 
   bool bad = false;
   for (long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n; q += (long long)gridDim.x * blockDim.x) {
     const double* r = aos + 5 * q;
-    double lx = (r[0] - g.x0) / g.dx, ly = (r[1] - g.y0) / g.dy;
-    double fi = floor(lx), fj = floor(ly);
-    int i = (int)fi, j = (int)fj;
-    float ox = (float)(lx - fi), oy = (float)(ly - fj);
-    if (ox >= 1.f) { ox = 0.f; i++; }
-    if (oy >= 1.f) { oy = 0.f; j++; }
-    if (i < 0 || i > g.nx - 2 || j < 0 || j > g.ny - 2) {
-      bad = true;
-      i = min(max(i, 0), g.nx - 2);
-      j = min(max(j, 0), g.ny - 2);
-    }
+    int i, j;
+    float ox, oy;
+    const bool in_x = cell_offset((r[0] - g.x0) / g.dx, g.nx - 1, i, ox);
+    const bool in_y = cell_offset((r[1] - g.y0) / g.dy, g.ny - 1, j, oy);
+    bad |= !(in_x && in_y);
     p.cell[q] = i * g.ny + j;
     p.ox[q] = ox;
     p.oy[q] = oy;
@@ -108,6 +102,31 @@ void launch_deposit_mixed(cudaStream_t st, const Geom& g, int shape, const Mixed
   else k_deposit_mixed<EPIC_CIC><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, acc);
 }
 
+// CIC deposit of the particles [*d_from, *d_n) (the MCC's ionisation
+// products, appended after the push deposited the rest).
+__global__ void __launch_bounds__(PART_THREADS) k_deposit_mixed_range(Geom g, MixedSoA p,
+                                                                      const long long* __restrict__ d_from,
+                                                                      const long long* __restrict__ d_n,
+                                                                      unsigned long long* __restrict__ acc) {
+  const long long from = *d_from, n = *d_n;
+  const long long S = 1ll << MIXED_OFFSET_BITS;
+  const float fS = (float)S;
+  for (long long q = from + (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int c = p.cell[q];
+    const long long a = (long long)(p.ox[q] * fS), b = (long long)(p.oy[q] * fS);
+    atomicAdd(&acc[c], (unsigned long long)((S - a) * (S - b)));
+    atomicAdd(&acc[c + g.ny], (unsigned long long)(a * (S - b)));
+    atomicAdd(&acc[c + 1], (unsigned long long)((S - a) * b));
+    atomicAdd(&acc[c + g.ny + 1], (unsigned long long)(a * b));
+  }
+}
+
+void launch_deposit_mixed_range(cudaStream_t st, const Geom& g, const MixedSoA& p, const long long* d_from,
+                                const long long* d_n, unsigned long long* acc, int grid) {
+  k_deposit_mixed_range<<<grid, PART_THREADS, 0, st>>>(g, p, d_from, d_n, acc);
+}
+
 // -------------------------------------------------------------- push ---
 // gather32 / advance / push_mixed_one: epic_mixed.cuh (shared with the batch).
 template <int SHAPE, int BC>
@@ -124,6 +143,109 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_mixed(Geom g, MixedSoA p,
     p.oy[q] = oy;
     p.vx[q] = vx;
     p.vy[q] = vy;
+  }
+}
+
+// Periodic or reflective walls, CIC: the push, the deposit of the new
+// positions into acc (deposit_warp_sorted) and, with SEL, the MCC's first
+// pass over the pushed electrons (mcc_candidate on the new velocities,
+// CTA-aggregated appends to sel.cand) in one pass over the particles.  Each
+// thread takes DEP_PER_THREAD consecutive particles with vector loads and
+// stores.  The particles, the integer sums and the candidate set (in another
+// order, which the MCC does not depend on) equal those of k_push_mixed +
+// k_deposit_mixed_sorted + k_mcc_select.
+template <int BC, bool SEL>
+__global__ void __launch_bounds__(PART_THREADS, 3) k_push_mixed_dep(Geom g, MixedSoA p, const long long* __restrict__ d_n,
+                                                                 const float2* __restrict__ ef, float qmK_dt,
+                                                                 float cx, float cy, unsigned long long* __restrict__ acc,
+                                                                 SelectArgs sel) {
+  constexpr int P = DEP_PER_THREAD;
+  __shared__ DepWarp tables[PART_THREADS / 32];
+  DepWarp& w = tables[threadIdx.x >> 5];
+  const long long n = *d_n;
+  const unsigned long long step = SEL ? *sel.d_step : 0ull;
+  const int lane = threadIdx.x & 31;
+  dep_init(w);
+  for (long long chunk = (long long)blockIdx.x * DEP_CHUNK; chunk < n; chunk += (long long)gridDim.x * DEP_CHUNK) {
+    const long long q0 = chunk + (long long)threadIdx.x * P;
+    const bool full = q0 + P <= n;
+    int c[P];
+    float ox[P], oy[P], vx[P], vy[P], vz[P];
+    if (full) {
+#pragma unroll
+      for (int h = 0; h < P / 4; h++) {
+        const int4 cc = reinterpret_cast<const int4*>(p.cell + q0)[h];
+        const float4 a = reinterpret_cast<const float4*>(p.ox + q0)[h];
+        const float4 b = reinterpret_cast<const float4*>(p.oy + q0)[h];
+        const float4 u = reinterpret_cast<const float4*>(p.vx + q0)[h];
+        const float4 v = reinterpret_cast<const float4*>(p.vy + q0)[h];
+        c[4 * h] = cc.x; c[4 * h + 1] = cc.y; c[4 * h + 2] = cc.z; c[4 * h + 3] = cc.w;
+        ox[4 * h] = a.x; ox[4 * h + 1] = a.y; ox[4 * h + 2] = a.z; ox[4 * h + 3] = a.w;
+        oy[4 * h] = b.x; oy[4 * h + 1] = b.y; oy[4 * h + 2] = b.z; oy[4 * h + 3] = b.w;
+        vx[4 * h] = u.x; vx[4 * h + 1] = u.y; vx[4 * h + 2] = u.z; vx[4 * h + 3] = u.w;
+        vy[4 * h] = v.x; vy[4 * h + 1] = v.y; vy[4 * h + 2] = v.z; vy[4 * h + 3] = v.w;
+        if (SEL) {
+          const float4 w = reinterpret_cast<const float4*>(p.vz + q0)[h];
+          vz[4 * h] = w.x; vz[4 * h + 1] = w.y; vz[4 * h + 2] = w.z; vz[4 * h + 3] = w.w;
+        }
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < P; k++) {
+        const long long q = q0 + k;
+        const bool in = q < n;
+        c[k] = in ? p.cell[q] : -1;
+        ox[k] = in ? p.ox[q] : 0.f;
+        oy[k] = in ? p.oy[q] : 0.f;
+        vx[k] = in ? p.vx[q] : 0.f;
+        vy[k] = in ? p.vy[q] : 0.f;
+        vz[k] = (SEL && in) ? p.vz[q] : 0.f;
+      }
+    }
+    unsigned int cand = 0;
+#pragma unroll
+    for (int k = 0; k < P; k++)
+      if (c[k] >= 0) {
+        push_mixed_one<EPIC_CIC, BC>(g, ef, qmK_dt, cx, cy, c[k], ox[k], oy[k], vx[k], vy[k]);
+        if (SEL && mcc_candidate(sel, q0 + k, step, vx[k], vy[k], vz[k])) cand |= 1u << k;
+      }
+    if (full) {
+#pragma unroll
+      for (int h = 0; h < P / 4; h++) {
+        reinterpret_cast<int4*>(p.cell + q0)[h] = make_int4(c[4 * h], c[4 * h + 1], c[4 * h + 2], c[4 * h + 3]);
+        reinterpret_cast<float4*>(p.ox + q0)[h] = make_float4(ox[4 * h], ox[4 * h + 1], ox[4 * h + 2], ox[4 * h + 3]);
+        reinterpret_cast<float4*>(p.oy + q0)[h] = make_float4(oy[4 * h], oy[4 * h + 1], oy[4 * h + 2], oy[4 * h + 3]);
+        reinterpret_cast<float4*>(p.vx + q0)[h] = make_float4(vx[4 * h], vx[4 * h + 1], vx[4 * h + 2], vx[4 * h + 3]);
+        reinterpret_cast<float4*>(p.vy + q0)[h] = make_float4(vy[4 * h], vy[4 * h + 1], vy[4 * h + 2], vy[4 * h + 3]);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < P; k++)
+        if (c[k] >= 0) {
+          const long long q = q0 + k;
+          p.cell[q] = c[k];
+          p.ox[q] = ox[k];
+          p.oy[q] = oy[k];
+          p.vx[q] = vx[k];
+          p.vy[q] = vy[k];
+        }
+    }
+    if (SEL && __any_sync(0xffffffffu, cand != 0)) {  // one atomic per warp with candidates
+      const unsigned int mine = __popc(cand);
+      unsigned int incl = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      unsigned int base = 0;
+      if (lane == 31) base = atomicAdd(sel.cand_count, incl);
+      unsigned int o = __shfl_sync(0xffffffffu, base, 31) + incl - mine;
+#pragma unroll
+      for (int k = 0; k < P; k++)
+        if (cand & (1u << k)) sel.cand[o++] = (unsigned int)(q0 + k);
+    }
+    deposit_warp_sorted(acc, w, g.ny, c, ox, oy);
   }
 }
 
@@ -185,8 +307,20 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_mixed_compact(Geom g, Mix
 
 void launch_push_mixed(cudaStream_t st, const Geom& g, int shape, int bc, const MixedSoA& p, long long* d_n,
                        const float2* ef, float qmK_dt, float cx, float cy, int* flags,
-                       unsigned long long* tile_status, unsigned int* tile_ctr, int grid) {
+                       unsigned long long* tile_status, unsigned int* tile_ctr, int grid,
+                       unsigned long long* dep_acc, const SelectArgs* sel) {
 #define PM(SH, B) k_push_mixed<SH, B><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy)
+  if (dep_acc && shape == EPIC_CIC && (bc == EPIC_PBC || bc == EPIC_REFLECTIVE)) {
+    const SelectArgs a = sel ? *sel : SelectArgs{};
+    // one wave of resident CTAs (the kernel strides over the chunks)
+#define PD(B, S)                                                                                       \
+  k_push_mixed_dep<B, S><<<resident_grid(k_push_mixed_dep<B, S>, PART_THREADS), PART_THREADS, 0, st>>>( \
+      g, p, d_n, ef, qmK_dt, cx, cy, dep_acc, a)
+    if (bc == EPIC_PBC) { if (sel) PD(EPIC_PBC, true); else PD(EPIC_PBC, false); }
+    else { if (sel) PD(EPIC_REFLECTIVE, true); else PD(EPIC_REFLECTIVE, false); }
+#undef PD
+    return;
+  }
   if (bc == EPIC_OPEN) {
     if (shape == EPIC_NGP)
       k_push_mixed_compact<EPIC_NGP><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy, tile_status,

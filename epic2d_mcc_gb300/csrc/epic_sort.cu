@@ -23,6 +23,7 @@
 #include <climits>
 
 #include "epic_internal.cuh"
+#include "epic_mixed.cuh"
 
 namespace epic {
 
@@ -334,48 +335,16 @@ SortScratch carve_sort_scratch(void* buf, long long cap) {
 
 // ----------------------------------------------- deposit of sorted particles ---
 // CIC deposit of the mixed form for particles sorted by cell (or nearly so,
-// between sorts): each CTA takes a contiguous chunk of 2048 particles, finds
-// the node range the chunk touches, and if it fits in shared memory adds the
-// integer weights there — each thread first merges runs of consecutive
-// particles in the same cell in registers — then adds the range to the grid
-// with one global atomic per touched node.  A chunk whose range does not fit
-// (unsorted input) adds straight to the grid.  The sums are integers, so the
-// result is identical to k_deposit_mixed's.
-constexpr int DEP_PER_THREAD = 8;
-constexpr int DEP_CHUNK = PART_THREADS * DEP_PER_THREAD;
-constexpr int DEP_SMEM_NODES = 3072;
-
-__device__ __forceinline__ void dep_flush(unsigned long long* __restrict__ acc, unsigned long long* sacc, bool smem,
-                                          int lo, int ny, int c, unsigned long long w00, unsigned long long w10,
-                                          unsigned long long w01, unsigned long long w11) {
-  if (c < 0) return;
-  if (smem) {
-    atomicAdd(&sacc[c - lo], w00);
-    atomicAdd(&sacc[c - lo + ny], w10);
-    atomicAdd(&sacc[c - lo + 1], w01);
-    atomicAdd(&sacc[c - lo + ny + 1], w11);
-  } else {
-    atomicAdd(&acc[c], w00);
-    atomicAdd(&acc[c + ny], w10);
-    atomicAdd(&acc[c + 1], w01);
-    atomicAdd(&acc[c + ny + 1], w11);
-  }
-}
-
+// between sorts): each warp takes a contiguous chunk of DEP_WARP_CHUNK
+// particles and deposits it with deposit_warp_sorted (epic_mixed.cuh).  The sums are
+// integers, so the result is identical to k_deposit_mixed's.
 __global__ void __launch_bounds__(PART_THREADS) k_deposit_mixed_sorted(Geom g, MixedSoA p,
                                                                        const long long* __restrict__ d_n,
                                                                        unsigned long long* __restrict__ acc) {
-  __shared__ unsigned long long sacc[DEP_SMEM_NODES];
-  __shared__ int s_lo, s_hi;
+  __shared__ DepWarp tables[PART_THREADS / 32];
+  DepWarp& w = tables[threadIdx.x >> 5];
   const long long n = *d_n;
-  const int S = 1 << MIXED_OFFSET_BITS;
-  const float fS = (float)S;
-  const int ny = g.ny;
-  if (threadIdx.x == 0) {
-    s_lo = INT_MAX;
-    s_hi = -1;
-  }
-  __syncthreads();
+  dep_init(w);
   for (long long chunk = (long long)blockIdx.x * DEP_CHUNK; chunk < n; chunk += (long long)gridDim.x * DEP_CHUNK) {
     const long long q0 = chunk + (long long)threadIdx.x * DEP_PER_THREAD;
     int c[DEP_PER_THREAD];
@@ -401,53 +370,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_deposit_mixed_sorted(Geom g, M
         oy[k] = q < n ? __ldg(&p.oy[q]) : 0.f;
       }
     }
-    int lo = INT_MAX, hi = -1;
-#pragma unroll
-    for (int k = 0; k < DEP_PER_THREAD; k++)
-      if (c[k] >= 0) {
-        lo = min(lo, c[k]);
-        hi = max(hi, c[k]);
-      }
-    lo = __reduce_min_sync(0xffffffffu, lo);
-    hi = __reduce_max_sync(0xffffffffu, hi);
-    if ((threadIdx.x & 31) == 0) {
-      atomicMin(&s_lo, lo);
-      atomicMax(&s_hi, hi);
-    }
-    __syncthreads();
-    const int blo = s_lo, bhi = s_hi;
-    const int span = bhi < 0 ? 0 : bhi + ny + 2 - blo;
-    const bool smem = span <= DEP_SMEM_NODES;
-    if (smem)
-      for (int m = threadIdx.x; m < span; m += PART_THREADS) sacc[m] = 0;
-    __syncthreads();
-    int cur = -1;
-    unsigned long long a00 = 0, a10 = 0, a01 = 0, a11 = 0;
-#pragma unroll
-    for (int k = 0; k < DEP_PER_THREAD; k++) {
-      if (c[k] < 0) continue;
-      const unsigned long long a = (unsigned long long)(int)(ox[k] * fS), b = (unsigned long long)(int)(oy[k] * fS);
-      const unsigned long long w00 = (S - a) * (S - b), w10 = a * (S - b), w01 = (S - a) * b, w11 = a * b;
-      if (c[k] != cur) {
-        dep_flush(acc, sacc, smem, blo, ny, cur, a00, a10, a01, a11);
-        cur = c[k];
-        a00 = w00; a10 = w10; a01 = w01; a11 = w11;
-      } else {
-        a00 += w00; a10 += w10; a01 += w01; a11 += w11;
-      }
-    }
-    dep_flush(acc, sacc, smem, blo, ny, cur, a00, a10, a01, a11);
-    __syncthreads();
-    if (smem)
-      for (int m = threadIdx.x; m < span; m += PART_THREADS) {
-        const unsigned long long v = sacc[m];
-        if (v) atomicAdd(&acc[blo + m], v);
-      }
-    if (threadIdx.x == 0) {
-      s_lo = INT_MAX;
-      s_hi = -1;
-    }
-    __syncthreads();
+    deposit_warp_sorted(acc, w, g.ny, c, ox, oy);
   }
 }
 

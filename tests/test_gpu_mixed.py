@@ -157,3 +157,31 @@ def test_mixed_open_boundary_and_mcc(gpu_lib, tmp_path):
     ref = orc.R.push(orc.s.species[1], i, ex, ex)
     sim.push_species(1)
     assert abs(sim.num_particles(1) - len(ref)) <= 2
+
+
+def test_mixed_upload_keeps_particles_by_the_far_walls(gpu_lib, tmp_path):
+    """A particle a hair inside the far walls, whose FP32 offset in the last cell rounds up to 1, stays in the
+    last cell at the largest offset below 1 (2^-24 cell from the wall); one on the wall itself is outside the
+    grid, as for the reference's deposit."""
+    E = gpu_lib
+    ini = decks.write(decks.deck(nx=32, ny=24, ne=100, ni=100), str(tmp_path))
+    orc = O.OracleSim(ini, initial_field=False)
+    s = orc.s
+    sim = mixed_sim(E, ini)
+    e = orc.parts[0].copy()
+    far_x, far_y = s.x0 + s.Lx * (1 - 2.0 ** -40), s.y0 + s.Ly * (1 - 2.0 ** -40)
+    e[0, :2] = far_x, far_y
+    e[1, 0] = far_x
+    e[2, 1] = far_y
+    sim.set_particles(0, e)
+    got = sim.particles(0)
+    for k, c, far, L in ((0, 0, far_x, s.Lx), (0, 1, far_y, s.Ly), (1, 0, far_x, s.Lx), (2, 1, far_y, s.Ly)):
+        d = s.dx if c == 0 else s.dy
+        assert s.x0 + L - 2.0 ** -23 * d < got[k, c] < s.x0 + L, (k, c)
+    sim.set_particles(1, orc.parts[1])
+    sim.scatter_species(0)
+    assert rel(sim.den(0), orc.R.scatter(e, s.species[0].spwt)) < 1e-5
+    e[3, 0] = s.x0 + s.Lx
+    with pytest.raises(E.EpicError) as ei:
+        sim.set_particles(0, e)
+    assert ei.value.status == 6  # EPIC_ERR_DOMAIN
