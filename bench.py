@@ -487,6 +487,15 @@ def run_precision_form(E, name, steps):
     ef, em = energy(fp), energy(mx)
     out["total_energy_rel_err_vs_fp64"] = abs(em - ef) / abs(ef)
     out["speedup_vs_fp64"] = out["mixed_particle_steps_per_s"] / out["fp64_particle_steps_per_s"]
+    # Phase split of each form: one more sort period, launched step by step
+    # with the phase timers on (after the comparison above).
+    for form, sim in (("fp64", fp), ("mixed", mx)):
+        sim.set_profiling(True)
+        sim.profile()
+        sim.run(SORT_EVERY, collisions=False, graph=False)
+        prof, _ = sim.profile()
+        sim.set_profiling(False)
+        out[form + "_phases_ms_per_step"] = {k: v[0] / SORT_EVERY for k, v in prof.items()}
     fp.close()
     mx.close()
     return out

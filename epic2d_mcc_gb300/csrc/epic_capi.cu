@@ -342,7 +342,10 @@ epic_status do_solve(epic_sim* s) {
   SolverArgs a = solver_args(s);
   if (s->mixed && s->spec.QR) {
     launch_spectral(s->stream, s->spec, a, SPECTRAL_STAGES);
-    s->launches += 3 + 6 * SPECTRAL_STAGES;
+    // set-up, the cooperative solve; the mean of b and the gauge (periodic),
+    // the duplicated nodes (extensions)
+    s->launches += 2 + (s->spec.mode == EPIC_POISSON_PERIODIC ? 2 : 0) +
+                   (s->spec.mode != EPIC_POISSON_DIRICHLET ? 1 : 0);
     CKL();
     return EPIC_OK;
   }

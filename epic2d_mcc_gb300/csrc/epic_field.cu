@@ -1180,18 +1180,6 @@ __device__ __forceinline__ unsigned long long ld_relaxed_u64(const unsigned long
   return v;
 }
 
-// PTX shifts clamp amounts of 64 or more to 64 (result 0), unlike C's.
-__device__ __forceinline__ uint64_t shl_clamp(uint64_t v, unsigned sft) {
-  uint64_t r;
-  asm("shl.b64 %0, %1, %2;" : "=l"(r) : "l"(v), "r"(sft));
-  return r;
-}
-__device__ __forceinline__ uint64_t shr_clamp(uint64_t v, unsigned sft) {
-  uint64_t r;
-  asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(v), "r"(sft));
-  return r;
-}
-
 // acc += x * 2^(1129 - A) (the fixed-point value of xs_from_double, bits
 // under 2^0 truncated toward zero) for x with biased exponent <= A + 1, branch
 // free; a term above that range adds nothing and returns false.  NONNEG: x is
@@ -1204,8 +1192,8 @@ __device__ __forceinline__ bool xs_add_anchored(xs_uint& acc, double x, int A) {
   const uint64_t m = ok ? ((b & 0xFFFFFFFFFFFFFull) | ((uint64_t)(eb != 0) << 52)) : 0ull;
   const int sh = 54 + (eb ? eb : 1) - A;  // <= 55 when ok
   const unsigned up = (unsigned)max(sh, 0), dn = (unsigned)max(-sh, 0);
-  const uint64_t lo = sh >= 0 ? shl_clamp(m, up) : shr_clamp(m, dn);
-  const uint64_t hi = shr_clamp(m, 64u - up);  // m >> (64 - sh), 0 for sh <= 0
+  const uint64_t lo = sh >= 0 ? xs_shl(m, up) : xs_shr(m, dn);
+  const uint64_t hi = xs_shr(m, 64u - up);  // m >> (64 - sh), 0 for sh <= 0
   xs_uint v = ((xs_uint)hi << 64) | lo;
   if (!NONNEG) {
     const xs_uint neg = (xs_uint)(xs_int)(-(int64_t)(b >> 63));  // all ones for a negative x
@@ -1471,9 +1459,13 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
         for (int w = 0; w < PCG_T / 32; w++) S += s_limb[w][0];
         red_release_add_u64(slot, ((unsigned long long)S << 8) + 1ull);
       }
+      // Warp 0 polls: lanes 0-4 the (w, r) limb words 0-4, lanes 8-12 the
+      // (r, r) words 5-9, lane 16 word 10 (so that each total gathers in an
+      // 8-lane group).
+      const int pword = lane < 5 ? lane : (lane >= 8 && lane < 13) ? lane - 3 : lane == 16 ? 10 : -1;
       unsigned long long wv0 = 0;
-      if (wid == 0 && lane < PCG_SLOT_WORDS)
-        wv0 = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane * PCG_WORD_STRIDE);
+      if (wid == 0 && pword >= 0)
+        wv0 = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + pword * PCG_WORD_STRIDE);
       // Deferred update of the previous iteration (no other CTA needs p' or
       // x), and the scalars the next step needs from the previous ones.
 #pragma unroll
@@ -1490,7 +1482,7 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
       if (wid == 0) {
         unsigned long long wv = 0;
         int good = 1;
-        if (lane < PCG_SLOT_WORDS) {
+        if (pword >= 0) {
           long long spins = 0;
           wv = wv0;
           for (;;) {
@@ -1500,23 +1492,26 @@ __global__ void __launch_bounds__(PCG_T) k_pcg_tiled(SolverArgs a, PcgTiling t) 
               good = 0;
               break;
             }
-            wv = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + lane * PCG_WORD_STRIDE);
+            wv = lane == 0 ? ld_acquire_u64(slot) : ld_relaxed_u64(slot + pword * PCG_WORD_STRIDE);
           }
         }
         good = __all_sync(0xffffffffu, good);
-        if (blockIdx.x == 0 && lane < PCG_SLOT_WORDS)
-          slots[((it + PCG_SLOTS - 1) % PCG_SLOTS) * PCG_SLOT_U64 + lane * PCG_WORD_STRIDE] = 0ull;
-        const long long S = (long long)(wv - (unsigned long long)nb) >> 8;
-        const long long outc = __shfl_sync(0xffffffffu, S, 10);
-        // Lane 0 recombines (w, r), lane 1 (r, r), and each rounds its total.
-        xs_int V = 0;
+        if (blockIdx.x == 0 && pword >= 0)
+          slots[((it + PCG_SLOTS - 1) % PCG_SLOTS) * PCG_SLOT_U64 + pword * PCG_WORD_STRIDE] = 0ull;
+        const long long S = pword >= 0 ? (long long)(wv - (unsigned long long)nb) >> 8 : 0;
+        const long long outc = __shfl_sync(0xffffffffu, S, 16);
+        // Each 8-lane group sums its limbs shifted to their weights (a
+        // butterfly of 128-bit adds): lane 0 holds (w, r), lane 8 (r, r);
+        // both round their totals at once.
+        xs_int V = (lane & 7) < 5 && lane < 16 ? (xs_int)S << (26 * (lane & 7)) : (xs_int)0;
 #pragma unroll
-        for (int k = 0; k < 5; k++) {
-          const long long La = __shfl_sync(0xffffffffu, S, k), Lb = __shfl_sync(0xffffffffu, S, 5 + k);
-          V += (xs_int)(lane == 0 ? La : Lb) << (26 * k);
+        for (int o = 4; o >= 1; o >>= 1) {
+          const uint64_t vlo = (uint64_t)(xs_uint)V, vhi = (uint64_t)((xs_uint)V >> 64);
+          const uint64_t olo = __shfl_xor_sync(0xffffffffu, vlo, o), ohi = __shfl_xor_sync(0xffffffffu, vhi, o);
+          V += (xs_int)(((xs_uint)ohi << 64) | olo);
         }
         const double d = xs_to_double(V, lane == 0 ? ad : aq);
-        const double d1 = __shfl_sync(0xffffffffu, d, 1);
+        const double d1 = __shfl_sync(0xffffffffu, d, 8);
         if (lane == 0) {
           dr = d;
           rr = d1;

@@ -19,11 +19,12 @@
 // once the reference's own stopping norm is below its tolerance (|r|_2 for
 // pcgsolver; the SOR residual L2 = sqrt(sum R^2 / (nx ny)), R = r/dx^2, for
 // gssolver), and otherwise adds the FP32 correction A^-1 r to x in FP64.
-// Every kernel reads a device-side done flag and returns at once after
-// convergence, so a fixed launch sequence (graph-capturable) serves any
-// number of stages up to the cap.
+// The stages run in one cooperative launch (k_spec_solve) that stops as soon
+// as the test passes, so one fixed launch sequence (graph-capturable) serves
+// any number of stages up to the cap.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -131,43 +132,111 @@ __global__ void __launch_bounds__(1024) k_spec_gauge(SpecLattice L) {
   }
 }
 
-__global__ void __launch_bounds__(256) k_spec_residual(SpecLattice L) {
-  if (L.state[0]) return;
-  __shared__ double sm[8];
-  spec_residual_chunk(L, blockIdx.x, sm);
+int spectral_chunks(const SpectralSolver& sp) { return (sp.R * sp.C + SPEC_CHUNK - 1) / SPEC_CHUNK; }
+
+// Grid barrier of a cooperative launch (counter zeroed before the launch):
+// release add, acquire poll, bounded by `limit` polls (FLAG_TIMEOUT).
+__device__ bool spec_grid_sync(unsigned int* bar, int* flags, long long limit) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    unsigned int ticket;
+    asm volatile("atom.add.release.gpu.global.u32 %0, [%1], 1;" : "=r"(ticket) : "l"(bar) : "memory");
+    const unsigned int target = (ticket / gridDim.x + 1) * gridDim.x;
+    int ok = 1;
+    long long spins = 0;
+    for (;;) {
+      unsigned int v;
+      asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(bar) : "memory");
+      if ((int)(v - target) >= 0) break;
+      if (++spins >= limit) {
+        atomicOr(flags, FLAG_TIMEOUT);
+        ok = 0;
+        break;
+      }
+    }
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok;
 }
 
-__global__ void k_spec_check(SpecLattice L, int final_pass) { spec_check(L, final_pass); }
-
-template <int EPI>
-__global__ void __launch_bounds__(256) k_spec_gemm(int M, int N, int K, const float* __restrict__ A,
-                                                   const float* __restrict__ B, float* __restrict__ C,
-                                                   const float* __restrict__ D, SpecLattice L) {
-  if (L.state[0]) return;
+// The whole defect-correction loop in one cooperative launch: the CTAs take
+// the residual chunks in turn; after a grid barrier every CTA forms the
+// stopping norm from the chunk sums in chunk order (so every CTA decides
+// alike; CTA 0 records it as spec_check); then the four products, the CTAs
+// taking TILE x TILE output tiles in turn, with a grid barrier after each.
+// Each output accumulates over k in order whatever the tile, so the
+// potentials equal those of the batched solve bit for bit.
+template <int TILE>
+__global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* __restrict__ QR,
+                                                    const float* __restrict__ QC, const float* __restrict__ D,
+                                                    float* t1, int stages, unsigned int* bar, int* flags,
+                                                    long long spin) {
   __shared__ float As[32][33];
   __shared__ float Bs[32][33];
-  spec_gemm_tile<EPI, 32>(M, N, K, A, B, C, D, &L, blockIdx.y, blockIdx.x, As, Bs);
+  __shared__ double sm8[8];
+  __shared__ int s_stop;
+  const int R = L.R, C = L.C;
+  const int nch = (R * C + SPEC_CHUNK - 1) / SPEC_CHUNK;
+  const int tiles_c = (C + TILE - 1) / TILE, ntiles = tiles_c * ((R + TILE - 1) / TILE);
+  for (int s = 0;; s++) {
+    for (int ch = blockIdx.x; ch < nch; ch += gridDim.x) {
+      spec_residual_chunk(L, ch, sm8);
+      __syncthreads();
+    }
+    if (!spec_grid_sync(bar, flags, spin)) return;
+    if (threadIdx.x == 0) {
+      double sum = 0, norm, err;
+      for (int b = 0; b < nch; b++) sum += __ldcg(&L.partials[b]);
+      spec_norm(L, sum, norm, err);
+      const int done = norm < L.tol;
+      if (blockIdx.x == 0) spec_record(L, done, s == stages, err);
+      s_stop = done || s == stages;
+    }
+    __syncthreads();
+    if (s_stop) return;
+#define SPEC_PASS(EPI, K_, A_, B_, C_, D_)                                                             \
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x)                                                  \
+    spec_gemm_tile<EPI, TILE>(R, C, K_, A_, B_, C_, D_, &L, t / tiles_c, t - (t / tiles_c) * tiles_c, As, Bs); \
+  if (!spec_grid_sync(bar, flags, spin)) return;
+    SPEC_PASS(0, R, QR, L.t0, t1, nullptr)
+    SPEC_PASS(1, C, t1, QC, L.t0, D)
+    SPEC_PASS(0, R, QR, L.t0, t1, nullptr)
+    SPEC_PASS(2, C, t1, QC, nullptr, nullptr)
+#undef SPEC_PASS
+  }
 }
-
-int spectral_chunks(const SpectralSolver& sp) { return (sp.R * sp.C + SPEC_CHUNK - 1) / SPEC_CHUNK; }
 
 void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs& a, int stages) {
   const int R = sp.R, C = sp.C;
   const SpecLattice L = lattice_of(sp, a);
-  const int nch = spectral_chunks(sp);
   k_spec_init<<<(a.g.nx * a.g.ny + 255) / 256, 256, 0, st>>>(L, a.warm);
   if (sp.mode == EPIC_POISSON_PERIODIC) k_spec_bmean<<<1, 1024, 0, st>>>(L);
-  dim3 g2((C + 31) / 32, (R + 31) / 32);
-  for (int s = 0; s < stages; s++) {
-    k_spec_residual<<<nch, 256, 0, st>>>(L);
-    k_spec_check<<<1, 1, 0, st>>>(L, 0);
-    k_spec_gemm<0><<<g2, 256, 0, st>>>(R, C, R, sp.QR, sp.t0, sp.t1, nullptr, L);
-    k_spec_gemm<1><<<g2, 256, 0, st>>>(R, C, C, sp.t1, sp.QC, sp.t0, sp.D, L);
-    k_spec_gemm<0><<<g2, 256, 0, st>>>(R, C, R, sp.QR, sp.t0, sp.t1, nullptr, L);
-    k_spec_gemm<2><<<g2, 256, 0, st>>>(R, C, C, sp.t1, sp.QC, nullptr, nullptr, L);
-  }
-  k_spec_residual<<<nch, 256, 0, st>>>(L);
-  k_spec_check<<<1, 1, 0, st>>>(L, 1);
+  // One wave of co-resident CTAs, at most one per output tile.
+  int dev = 0, sms = 0, per16 = 0, per32 = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per16, k_spec_solve<16>, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per32, k_spec_solve<32>, 256, 0);
+  const long long t32 = (long long)((R + 31) / 32) * ((C + 31) / 32);
+  const long long t16 = (long long)((R + 15) / 16) * ((C + 15) / 16);
+  const bool big = t32 >= 2LL * sms;  // enough 32 x 32 tiles to fill the GPU
+  const int per = std::max(1, std::min(2, big ? per32 : per16));
+  const int grid = (int)std::max(1LL, std::min<long long>(big ? t32 : t16, (long long)per * sms));
+  cudaMemsetAsync(a.bar, 0, sizeof(unsigned int), st);
+  SpecLattice Lk = L;
+  const float *qr = sp.QR, *qc = sp.QC, *d = sp.D;
+  float* t1 = sp.t1;
+  int stg = stages;
+  unsigned int* bar = a.bar;
+  int* flags = a.flags;
+  long long spin = spin_limit();
+  void* params[] = {&Lk, &qr, &qc, &d, &t1, &stg, &bar, &flags, &spin};
+  if (big)
+    cudaLaunchCooperativeKernel((const void*)k_spec_solve<32>, dim3(grid), dim3(256), params, 0, st);
+  else
+    cudaLaunchCooperativeKernel((const void*)k_spec_solve<16>, dim3(grid), dim3(256), params, 0, st);
   if (sp.mode == EPIC_POISSON_PERIODIC) k_spec_gauge<<<1, 1024, 0, st>>>(L);
   if (sp.mode != EPIC_POISSON_DIRICHLET) launch_fill_poisson_nodes(st, a.g, sp.mode, a.phi);
 }

@@ -115,13 +115,9 @@ __device__ __forceinline__ void spec_residual_chunk(const SpecLattice& L, int ch
 // The reference solver's stopping test on the residual just computed (one
 // thread): pcgsolver |r|_2 < tol, gssolver sqrt(sum R^2/(nx ny)) < tol with
 // R = r/dx^2.  final_pass closes an unconverged solve at the stage cap.
-__device__ __forceinline__ void spec_check(const SpecLattice& L, int final_pass) {
-  if (L.state[0]) return;
-  const int nchunks = (L.R * L.C + SPEC_CHUNK - 1) / SPEC_CHUNK;
-  double s = 0;
-  for (int b = 0; b < nchunks; b++) s += L.partials[b];
+// The stopping norm and the reported error from the sum of r^2.
+__device__ __forceinline__ void spec_norm(const SpecLattice& L, double s, double& norm, double& err) {
   const double nn = (double)L.nx * L.ny;
-  double norm, err;
   if (L.gs_norm) {
     norm = sqrt(s / (L.dx2 * L.dx2) / nn);
     err = norm;
@@ -129,7 +125,10 @@ __device__ __forceinline__ void spec_check(const SpecLattice& L, int final_pass)
     norm = sqrt(s);
     err = sqrt(s) / nn;
   }
-  const int done = norm < L.tol;
+}
+
+// Records the test's outcome (done: converged; final_pass: the stage cap).
+__device__ __forceinline__ void spec_record(const SpecLattice& L, int done, int final_pass, double err) {
   if (L.info) {
     L.info->iterations = L.state[1];
     L.info->error = err;
@@ -141,6 +140,16 @@ __device__ __forceinline__ void spec_check(const SpecLattice& L, int final_pass)
   } else {
     L.state[1] += 1;
   }
+}
+
+__device__ __forceinline__ void spec_check(const SpecLattice& L, int final_pass) {
+  if (L.state[0]) return;
+  const int nchunks = (L.R * L.C + SPEC_CHUNK - 1) / SPEC_CHUNK;
+  double s = 0;
+  for (int b = 0; b < nchunks; b++) s += L.partials[b];
+  double norm, err;
+  spec_norm(L, s, norm, err);
+  spec_record(L, norm < L.tol, final_pass, err);
 }
 
 // One TILE x TILE output tile of C = A B (M x K by K x N, row-major FP32) at

@@ -91,34 +91,63 @@ XS_HD xs_int xs_realign(xs_int v, int A, int A2) {
 }
 
 // The double nearest to V * 2^(A - 1129) (ties to even); results below the
-// normal range flush to zero, above it give infinity.
+// normal range flush to zero, above it give infinity.  The magnitude's top 64
+// bits are rounded to 53 with the bits under them as a sticky bit: a few
+// dependent integer operations, no 128-bit shifts by variable amounts.
 XS_HD double xs_to_double(xs_int v, int A) {
   if (v == 0) return 0.0;
   const uint64_t sign = v < 0 ? 1u : 0u;
   const xs_uint u = sign ? (xs_uint)(-v) : (xs_uint)v;
   const uint64_t hi = (uint64_t)(u >> 64), lo = (uint64_t)u;
-  const int p = hi ? 127 - xs_clz64(hi) : 63 - xs_clz64(lo);
-  long E = (long)p + A - 106;
-  uint64_t q;
-  if (p <= 52) {
-    q = (uint64_t)(u << (52 - p));
+  const int lz = hi ? xs_clz64(hi) : 64 + xs_clz64(lo);
+  uint64_t w, rest;
+  if (lz >= 64) {
+    w = lo << (lz - 64);
+    rest = 0;
+  } else if (lz == 0) {
+    w = hi;
+    rest = lo;
   } else {
-    const int d = p - 52;
-    q = (uint64_t)(u >> d);
-    const xs_uint rem = u & (((xs_uint)1 << d) - 1);
-    const xs_uint half = (xs_uint)1 << (d - 1);
-    if (rem > half || (rem == half && (q & 1))) {
-      q++;
-      if (q >> 53) {
-        q >>= 1;
-        E++;
-      }
+    w = (hi << lz) | (lo >> (64 - lz));
+    rest = lo << lz;
+  }
+  uint64_t q = w >> 11;  // 53 bits, the top one set
+  long E = (long)(127 - lz) + A - 106;
+  const bool guard = (w >> 10) & 1, sticky = (w & 0x3FFull) != 0 || rest != 0;
+  if (guard && (sticky || (q & 1))) {
+    q++;
+    if (q >> 53) {
+      q >>= 1;
+      E++;
     }
   }
   if (E <= 0) return sign ? -0.0 : 0.0;
   if (E >= 2047) return xs_double((sign << 63) | (0x7FFull << 52));
   return xs_double((sign << 63) | ((uint64_t)E << 52) | (q & 0xFFFFFFFFFFFFFull));
 }
+
+// v << s and v >> s, 0 for s >= 64 (s is unsigned, so a negative amount
+// converted to it is also 0); on the device the PTX shifts, which clamp the
+// amount to the width.
+XS_HD uint64_t xs_shl(uint64_t v, unsigned s) {
+#if defined(__CUDA_ARCH__)
+  uint64_t r;
+  asm("shl.b64 %0, %1, %2;" : "=l"(r) : "l"(v), "r"(s));
+  return r;
+#else
+  return s >= 64 ? 0 : v << s;
+#endif
+}
+XS_HD uint64_t xs_shr(uint64_t v, unsigned s) {
+#if defined(__CUDA_ARCH__)
+  uint64_t r;
+  asm("shr.b64 %0, %1, %2;" : "=l"(r) : "l"(v), "r"(s));
+  return r;
+#else
+  return s >= 64 ? 0 : v >> s;
+#endif
+}
+
 
 }  // namespace epic
 

@@ -117,3 +117,4 @@ def test_sqrt_stop_threshold(X):
         below = math.nextafter(T, 0.0)
         assert math.sqrt(below) < tol
     assert X.xs_threshold(0.0) == 0.0
+
