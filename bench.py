@@ -493,9 +493,10 @@ def run_precision_form(E, name, steps):
         sim.set_profiling(True)
         sim.profile()
         sim.run(SORT_EVERY, collisions=False, graph=False)
-        prof, _ = sim.profile()
+        prof, iters = sim.profile()
         sim.set_profiling(False)
         out[form + "_phases_ms_per_step"] = {k: v[0] / SORT_EVERY for k, v in prof.items()}
+        out[form + ("_pcg_iterations_per_step" if form == "fp64" else "_solve_stages_per_step")] = iters / SORT_EVERY
     fp.close()
     mx.close()
     return out

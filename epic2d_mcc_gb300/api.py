@@ -421,8 +421,13 @@ class Simulation:
         return self.grid(10 + sp)
 
     def set_grid(self, which, arr):
+        """Sets a node grid (nx * ny values, i-major) from the host; an array of another size is refused (the C
+        entry point copies nx * ny values)."""
         code = GRID.get(which, which)
         a = np.ascontiguousarray(arr, dtype=np.float64).reshape(-1)
+        if a.size != self.cfg.nx * self.cfg.ny:
+            raise ValueError("grid %r needs %d x %d = %d values, got %d" % (which, self.cfg.nx, self.cfg.ny,
+                                                                        self.cfg.nx * self.cfg.ny, a.size))
         _check(lib().epic_set_grid(self._h, code, _ptr(a)))
 
     def sync(self):

@@ -135,7 +135,9 @@ __global__ void __launch_bounds__(1024) k_spec_gauge(SpecLattice L) {
 int spectral_chunks(const SpectralSolver& sp) { return (sp.R * sp.C + SPEC_CHUNK - 1) / SPEC_CHUNK; }
 
 // Grid barrier of a cooperative launch (counter zeroed before the launch):
-// release add, acquire poll, bounded by `limit` polls (FLAG_TIMEOUT).
+// the CTA barrier orders the CTA's writes before thread 0's release add, and
+// the acquire poll followed by the CTA barrier orders every later read after
+// the other CTAs' writes; bounded by `limit` polls (FLAG_TIMEOUT).
 __device__ bool spec_grid_sync(unsigned int* bar, int* flags, long long limit) {
   __shared__ int s_ok;
   __syncthreads();
@@ -173,8 +175,9 @@ __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* 
                                                     const float* __restrict__ QC, const float* __restrict__ D,
                                                     float* t1, int stages, unsigned int* bar, int* flags,
                                                     long long spin) {
-  __shared__ float As[32][33];
-  __shared__ float Bs[32][33];
+  __shared__ __align__(16) float As[TILE == 64 ? 1 : 32][33];
+  __shared__ float Bs[TILE == 64 ? 1 : 32][33];
+  __shared__ __align__(16) SpecGemmSmem sg[TILE == 64 ? 1 : 0 + 1];
   __shared__ double sm8[8];
   __shared__ int s_stop;
   const int R = L.R, C = L.C;
@@ -196,9 +199,14 @@ __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* 
     }
     __syncthreads();
     if (s_stop) return;
-#define SPEC_PASS(EPI, K_, A_, B_, C_, D_)                                                             \
-  for (int t = blockIdx.x; t < ntiles; t += gridDim.x)                                                  \
-    spec_gemm_tile<EPI, TILE>(R, C, K_, A_, B_, C_, D_, &L, t / tiles_c, t - (t / tiles_c) * tiles_c, As, Bs); \
+#define SPEC_PASS(EPI, K_, A_, B_, C_, D_)                                                                    \
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {                                                       \
+    if (TILE == 64)                                                                                          \
+      spec_gemm_tile64<EPI>(R, C, K_, A_, B_, C_, D_, &L, t / tiles_c, t - (t / tiles_c) * tiles_c, sg[0]);  \
+    else                                                                                                     \
+      spec_gemm_tile<EPI, TILE == 64 ? 32 : TILE>(R, C, K_, A_, B_, C_, D_, &L, t / tiles_c,                 \
+                                                  t - (t / tiles_c) * tiles_c, As, Bs);                      \
+  }                                                                                                          \
   if (!spec_grid_sync(bar, flags, spin)) return;
     SPEC_PASS(0, R, QR, L.t0, t1, nullptr)
     SPEC_PASS(1, C, t1, QC, L.t0, D)
@@ -214,16 +222,21 @@ void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs
   k_spec_init<<<(a.g.nx * a.g.ny + 255) / 256, 256, 0, st>>>(L, a.warm);
   if (sp.mode == EPIC_POISSON_PERIODIC) k_spec_bmean<<<1, 1024, 0, st>>>(L);
   // One wave of co-resident CTAs, at most one per output tile.
-  int dev = 0, sms = 0, per16 = 0, per32 = 0;
+  // Output tiles: 64 x 64 (register-blocked) once there are enough of them
+  // for every SM, else 32 x 32 with two per SM, else 16 x 16.
+  int dev = 0, sms = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per16, k_spec_solve<16>, 256, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per32, k_spec_solve<32>, 256, 0);
+  const long long t64 = (long long)((R + 63) / 64) * ((C + 63) / 64);
   const long long t32 = (long long)((R + 31) / 32) * ((C + 31) / 32);
   const long long t16 = (long long)((R + 15) / 16) * ((C + 15) / 16);
-  const bool big = t32 >= 2LL * sms;  // enough 32 x 32 tiles to fill the GPU
-  const int per = std::max(1, std::min(2, big ? per32 : per16));
-  const int grid = (int)std::max(1LL, std::min<long long>(big ? t32 : t16, (long long)per * sms));
+  const int tile = t64 >= sms ? 64 : t32 >= 2LL * sms ? 32 : 16;
+  const void* kern = tile == 64 ? (const void*)k_spec_solve<64>
+                     : tile == 32 ? (const void*)k_spec_solve<32> : (const void*)k_spec_solve<16>;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, 0);
+  per = std::max(1, std::min(2, per));
+  const long long tiles = tile == 64 ? t64 : tile == 32 ? t32 : t16;
+  const int grid = (int)std::max(1LL, std::min<long long>(tiles, (long long)per * sms));
   cudaMemsetAsync(a.bar, 0, sizeof(unsigned int), st);
   SpecLattice Lk = L;
   const float *qr = sp.QR, *qc = sp.QC, *d = sp.D;
@@ -233,10 +246,7 @@ void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs
   int* flags = a.flags;
   long long spin = spin_limit();
   void* params[] = {&Lk, &qr, &qc, &d, &t1, &stg, &bar, &flags, &spin};
-  if (big)
-    cudaLaunchCooperativeKernel((const void*)k_spec_solve<32>, dim3(grid), dim3(256), params, 0, st);
-  else
-    cudaLaunchCooperativeKernel((const void*)k_spec_solve<16>, dim3(grid), dim3(256), params, 0, st);
+  cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(256), params, 0, st);
   if (sp.mode == EPIC_POISSON_PERIODIC) k_spec_gauge<<<1, 1024, 0, st>>>(L);
   if (sp.mode != EPIC_POISSON_DIRICHLET) launch_fill_poisson_nodes(st, a.g, sp.mode, a.phi);
 }

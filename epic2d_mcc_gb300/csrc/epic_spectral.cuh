@@ -53,6 +53,9 @@ __device__ __forceinline__ void spec_init_node(const SpecLattice& L, int q) {
 
 // r = b - A x for the entries of one chunk (FP64) into t0 (FP32); the chunk's
 // sum of r^2 goes to partials[chunk].  Called by a whole CTA of 256 threads.
+// x and the products' operands are read through L2 (__ldcg): inside the
+// cooperative solve other CTAs wrote them since this SM last read them, and
+// its L1 is not coherent.
 __device__ __forceinline__ void spec_residual_chunk(const SpecLattice& L, int chunk, double* sm8) {
   const int total = L.R * L.C;
   const int nx = L.nx, ny = L.ny, R = L.R, C = L.C;
@@ -71,28 +74,28 @@ __device__ __forceinline__ void spec_residual_chunk(const SpecLattice& L, int ch
         j = cj;
         const int ru = lattice_wrap(ri - 1, R, L.mode == EPIC_POISSON_PERIODIC);
         const int rd = lattice_wrap(ri + 1, R, L.mode == EPIC_POISSON_PERIODIC);
-        ax = -4 * x[spec_node(L, i, j)];
-        if (ru >= 0) ax += x[spec_node(L, ru + i0, j)];
-        if (rd >= 0) ax += x[spec_node(L, rd + i0, j)];
-        ax += x[spec_node(L, i, cj > 0 ? cj - 1 : C - 1)];
-        ax += x[spec_node(L, i, cj < C - 1 ? cj + 1 : 0)];
+        ax = -4 * __ldcg(&x[spec_node(L, i, j)]);
+        if (ru >= 0) ax += __ldcg(&x[spec_node(L, ru + i0, j)]);
+        if (rd >= 0) ax += __ldcg(&x[spec_node(L, rd + i0, j)]);
+        ax += __ldcg(&x[spec_node(L, i, cj > 0 ? cj - 1 : C - 1)]);
+        ax += __ldcg(&x[spec_node(L, i, cj < C - 1 ? cj + 1 : 0)]);
       } else if (L.flat) {  // pcgsolver: rows of C = nx nodes of the flattened vector
         auto nd = [&](int k) { const int ii = k / ny; return spec_node(L, ii, k - ii * ny); };
         i = q / ny;
         j = q - i * ny;
-        ax = -4 * x[spec_node(L, i, j)];
-        if (ri > 0) ax += x[nd(q - C)];
-        if (ri < R - 1) ax += x[nd(q + C)];
-        if (cj > 0) ax += x[nd(q - 1)];
-        if (cj < C - 1) ax += x[nd(q + 1)];
+        ax = -4 * __ldcg(&x[spec_node(L, i, j)]);
+        if (ri > 0) ax += __ldcg(&x[nd(q - C)]);
+        if (ri < R - 1) ax += __ldcg(&x[nd(q + C)]);
+        if (cj > 0) ax += __ldcg(&x[nd(q - 1)]);
+        if (cj < C - 1) ax += __ldcg(&x[nd(q + 1)]);
       } else {  // gssolver: interior nodes, physical neighbours
         i = ri + 1;
         j = cj + 1;
-        ax = -4 * x[spec_node(L, i, j)];
-        if (i > 0) ax += x[spec_node(L, i - 1, j)];
-        if (i < nx - 1) ax += x[spec_node(L, i + 1, j)];
-        if (j > 0) ax += x[spec_node(L, i, j - 1)];
-        if (j < ny - 1) ax += x[spec_node(L, i, j + 1)];
+        ax = -4 * __ldcg(&x[spec_node(L, i, j)]);
+        if (i > 0) ax += __ldcg(&x[spec_node(L, i - 1, j)]);
+        if (i < nx - 1) ax += __ldcg(&x[spec_node(L, i + 1, j)]);
+        if (j > 0) ax += __ldcg(&x[spec_node(L, i, j - 1)]);
+        if (j < ny - 1) ax += __ldcg(&x[spec_node(L, i, j + 1)]);
       }
       const bool edge = L.mode == EPIC_POISSON_DIRICHLET && (i == 0 || i == nx - 1 || j == 0 || j == ny - 1);
       double b = edge ? 0.0 : -L.rho[spec_node(L, i, j)] * L.dx2 * L.K;
@@ -152,6 +155,24 @@ __device__ __forceinline__ void spec_check(const SpecLattice& L, int final_pass)
   spec_record(L, norm < L.tol, final_pass, err);
 }
 
+// The output element (r, c) of the last product goes to phi at its node.
+__device__ __forceinline__ void spec_add_phi(const SpecLattice* L, int N, int r, int c, float v) {
+  int i, j;
+  if (L->mode != EPIC_POISSON_DIRICHLET) {
+    i = r + (L->mode == EPIC_POISSON_PERIODIC ? 0 : 1);
+    j = c;
+  } else if (L->flat) {
+    const int k = r * N + c;  // N = C: the flattened vector
+    i = k / L->ny;
+    j = k - i * L->ny;
+  } else {
+    i = r + 1;
+    j = c + 1;
+  }
+  double* const ph = &L->phi[spec_node(*L, i, j)];
+  *ph = __ldcg(ph) + (double)v;
+}
+
 // One TILE x TILE output tile of C = A B (M x K by K x N, row-major FP32) at
 // tile (tr, tc), 256 threads.  EPI 0: store; 1: store C o D; 2: add to phi
 // (FP64) at the node of lattice entry (r, c).
@@ -171,8 +192,8 @@ __device__ __forceinline__ void spec_gemm_tile(int M, int N, int K, const float*
   for (int k0 = 0; k0 < K; k0 += TILE) {
     for (int e = threadIdx.x; e < TILE * TILE; e += 256) {
       const int r = e / TILE, c = e % TILE;
-      As[r][c] = (row0 + r < M && k0 + c < K) ? A[(row0 + r) * K + k0 + c] : 0.f;
-      Bs[r][c] = (k0 + r < K && col0 + c < N) ? B[(k0 + r) * N + col0 + c] : 0.f;
+      As[r][c] = (row0 + r < M && k0 + c < K) ? __ldcg(&A[(row0 + r) * K + k0 + c]) : 0.f;
+      Bs[r][c] = (k0 + r < K && col0 + c < N) ? __ldcg(&B[(k0 + r) * N + col0 + c]) : 0.f;
     }
     __syncthreads();
 #pragma unroll 8
@@ -192,21 +213,90 @@ __device__ __forceinline__ void spec_gemm_tile(int M, int N, int K, const float*
       if (r >= M || c >= N) continue;
       if (EPI == 0) Cm[r * N + c] = acc[a][b];
       else if (EPI == 1) Cm[r * N + c] = acc[a][b] * D[r * N + c];
-      else {
-        int i, j;
-        if (L->mode != EPIC_POISSON_DIRICHLET) {
-          i = r + (L->mode == EPIC_POISSON_PERIODIC ? 0 : 1);
-          j = c;
-        } else if (L->flat) {
-          const int k = r * N + c;  // N = C: the flattened vector
-          i = k / L->ny;
-          j = k - i * L->ny;
-        } else {
-          i = r + 1;
-          j = c + 1;
-        }
-        L->phi[spec_node(*L, i, j)] += (double)acc[a][b];
-      }
+      else spec_add_phi(L, N, r, c, acc[a][b]);
+    }
+}
+
+// A 64 x 64 output tile of C = A B for large lattices, 256 threads with 4 x 4
+// outputs each (register blocking: two 16-byte shared loads feed 16 fmas),
+// k in steps of 16 with the next step's operands loaded into registers while
+// the current one is multiplied (double-buffered shared memory, one barrier
+// per step).  Every output accumulates over k = 0, 1, ... in order with one
+// fma per step, as spec_gemm_tile: the same results.
+constexpr int SG_BM = 64, SG_BK = 16, SG_LDA = SG_BM + 4;
+struct SpecGemmSmem {
+  float A[2][SG_BK][SG_LDA];  // k-major (transposed) A tile
+  float B[2][SG_BK][SG_BM];
+};
+
+template <int EPI>
+__device__ __forceinline__ void spec_gemm_tile64(int M, int N, int K, const float* __restrict__ A,
+                                                 const float* __restrict__ B, float* __restrict__ Cm,
+                                                 const float* __restrict__ D, const SpecLattice* L, int tr, int tc,
+                                                 SpecGemmSmem& sm) {
+  const int t = threadIdx.x;
+  const int tx = t & 15, ty = t >> 4;
+  const int row0 = tr * SG_BM, col0 = tc * SG_BM;
+  // loader coordinates: A row t/4, k quad (t%4)*4; B k row t/16, column quad (t%16)*4
+  const int la_r = t >> 2, la_k = (t & 3) * 4, lb_k = t >> 4, lb_c = (t & 15) * 4;
+  const bool vec = (K & 3) == 0 && (N & 3) == 0;
+  float ra[4], rb[4];
+  auto load = [&](int k0) {
+    const int ar = row0 + la_r, ak = k0 + la_k, bk = k0 + lb_k, bc = col0 + lb_c;
+    if (vec && ar < M && ak + 3 < K) {
+      const float4 v = __ldcg(reinterpret_cast<const float4*>(A + (size_t)ar * K + ak));
+      ra[0] = v.x; ra[1] = v.y; ra[2] = v.z; ra[3] = v.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) ra[q] = (ar < M && ak + q < K) ? __ldcg(A + (size_t)ar * K + ak + q) : 0.f;
+    }
+    if (vec && bk < K && bc + 3 < N) {
+      const float4 v = __ldcg(reinterpret_cast<const float4*>(B + (size_t)bk * N + bc));
+      rb[0] = v.x; rb[1] = v.y; rb[2] = v.z; rb[3] = v.w;
+    } else {
+#pragma unroll
+      for (int q = 0; q < 4; q++) rb[q] = (bk < K && bc + q < N) ? __ldcg(B + (size_t)bk * N + bc + q) : 0.f;
+    }
+  };
+  auto store = [&](int buf) {
+#pragma unroll
+    for (int q = 0; q < 4; q++) sm.A[buf][la_k + q][la_r] = ra[q];
+    *reinterpret_cast<float4*>(&sm.B[buf][lb_k][lb_c]) = make_float4(rb[0], rb[1], rb[2], rb[3]);
+  };
+  float acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) acc[a][b] = 0.f;
+  const int nk = (K + SG_BK - 1) / SG_BK;
+  load(0);
+  store(0);
+  __syncthreads();
+  for (int s = 0; s < nk; s++) {
+    const int cur = s & 1;
+    if (s + 1 < nk) load((s + 1) * SG_BK);
+#pragma unroll
+    for (int kk = 0; kk < SG_BK; kk++) {
+      const float4 a4 = *reinterpret_cast<const float4*>(&sm.A[cur][kk][ty * 4]);
+      const float4 b4 = *reinterpret_cast<const float4*>(&sm.B[cur][kk][tx * 4]);
+      const float av[4] = {a4.x, a4.y, a4.z, a4.w}, bv[4] = {b4.x, b4.y, b4.z, b4.w};
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = fmaf(av[a], bv[b], acc[a][b]);
+    }
+    if (s + 1 < nk) store(cur ^ 1);
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int r = row0 + ty * 4 + a, c = col0 + tx * 4 + b;
+      if (r >= M || c >= N) continue;
+      if (EPI == 0) Cm[r * N + c] = acc[a][b];
+      else if (EPI == 1) Cm[r * N + c] = acc[a][b] * D[r * N + c];
+      else spec_add_phi(L, N, r, c, acc[a][b]);
     }
 }
 
