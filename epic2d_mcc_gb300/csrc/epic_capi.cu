@@ -183,8 +183,8 @@ epic_status setup_spectral(epic_sim* s) {
   CK(cudaMallocAsync((void**)&sp.D, D.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.t0, D.size() * sizeof(float), s->stream));
   CK(cudaMallocAsync((void**)&sp.t1, D.size() * sizeof(float), s->stream));
-  // chunk sums, then the periodic right-hand side's mean
-  CK(cudaMallocAsync((void**)&sp.partials, std::max(256, spectral_chunks(sp) + 1) * sizeof(double), s->stream));
+  // the residual's chunk sums, then (periodic) those of b and of phi
+  CK(cudaMallocAsync((void**)&sp.partials, std::max(256, 2 * spectral_chunks(sp)) * sizeof(double), s->stream));
   CK(cudaMallocAsync((void**)&sp.state, 4 * sizeof(int), s->stream));
   CK(cudaMemcpyAsync(sp.QR, QR.data(), QR.size() * sizeof(float), cudaMemcpyHostToDevice, s->stream));
   if (sp.QC != sp.QR)
@@ -342,10 +342,8 @@ epic_status do_solve(epic_sim* s) {
   SolverArgs a = solver_args(s);
   if (s->mixed && s->spec.QR) {
     launch_spectral(s->stream, s->spec, a, SPECTRAL_STAGES);
-    // set-up, the cooperative solve; the mean of b and the gauge (periodic),
-    // the duplicated nodes (extensions)
-    s->launches += 2 + (s->spec.mode == EPIC_POISSON_PERIODIC ? 2 : 0) +
-                   (s->spec.mode != EPIC_POISSON_DIRICHLET ? 1 : 0);
+    // set-up, the cooperative solve, the duplicated nodes (extensions)
+    s->launches += 2 + (s->spec.mode != EPIC_POISSON_DIRICHLET ? 1 : 0);
     CKL();
     return EPIC_OK;
   }

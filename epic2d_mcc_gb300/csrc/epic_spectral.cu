@@ -53,7 +53,7 @@ static SpecLattice lattice_of(const SpectralSolver& sp, const SolverArgs& a) {
   L.flat = sp.flat;
   L.gs_norm = sp.gs_norm;
   L.mode = sp.mode;
-  L.bmean = sp.partials + spectral_chunks(sp);
+  L.bmean = nullptr;  // PERIODIC: set inside the solve
   L.dx2 = a.g.dx * a.g.dx;
   L.K = a.K;
   L.tol = a.tol;
@@ -82,53 +82,6 @@ __global__ void k_spec_init(SpecLattice L, int warm) {
     L.state[0] = 0;
     L.state[1] = 0;
     L.state[2] = 0;
-  }
-}
-
-// PERIODIC: the mean of b = -rho dx^2 K over the unknowns (one CTA, fixed
-// order), subtracted from b so that the singular system is consistent.  The
-// periodic lattice's entry (r, c) is node (r, c).
-__global__ void __launch_bounds__(1024) k_spec_bmean(SpecLattice L) {
-  __shared__ double sm[32];
-  const int n = L.R * L.C;
-  double acc = 0;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int i = q / L.C, j = q - i * L.C;
-    acc += -L.rho[spec_node(L, i, j)] * L.dx2 * L.K;
-  }
-  acc = spec_warp_sum(acc);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w];
-    *const_cast<double*>(L.bmean) = t / n;
-  }
-}
-
-// PERIODIC: phi shifted to zero mean over the unknowns (the FP64 solver's
-// gauge); the FP32 corrections leave a rounding-level mean.
-__global__ void __launch_bounds__(1024) k_spec_gauge(SpecLattice L) {
-  __shared__ double sm[33];
-  const int n = L.R * L.C;
-  double acc = 0;
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int i = q / L.C, j = q - i * L.C;
-    acc += L.phi[spec_node(L, i, j)];
-  }
-  acc = spec_warp_sum(acc);
-  if ((threadIdx.x & 31) == 0) sm[threadIdx.x >> 5] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double t = 0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += sm[w];
-    sm[32] = t / n;
-  }
-  __syncthreads();
-  const double m = sm[32];
-  for (int q = threadIdx.x; q < n; q += blockDim.x) {
-    const int i = q / L.C, j = q - i * L.C;
-    L.phi[spec_node(L, i, j)] -= m;
   }
 }
 
@@ -170,6 +123,40 @@ __device__ bool spec_grid_sync(unsigned int* bar, int* flags, long long limit) {
 // taking TILE x TILE output tiles in turn, with a grid barrier after each.
 // Each output accumulates over k in order whatever the tile, so the
 // potentials equal those of the batched solve bit for bit.
+// PERIODIC: a fixed-order sum over the lattice entries [ch * SPEC_CHUNK, ...)
+// of b = -rho dx^2 K (what = 0) or of phi (what = 1); entry (r, c) is node
+// (r, c).  Called by a whole CTA of 256 threads; the sum goes to out[ch].
+__device__ void spec_chunk_sum(const SpecLattice& L, int what, int ch, double* out, double* sm8) {
+  const int total = L.R * L.C;
+  double acc = 0;
+#pragma unroll
+  for (int u = 0; u < SPEC_CHUNK / 256; u++) {
+    const int q = ch * SPEC_CHUNK + u * 256 + threadIdx.x;
+    if (q < total) {
+      const int r = q / L.C, c = q - r * L.C;
+      const int k = spec_node(L, r, c);
+      acc += what ? __ldcg(&L.phi[k]) : -L.rho[k] * L.dx2 * L.K;
+    }
+  }
+  acc = spec_warp_sum(acc);
+  if ((threadIdx.x & 31) == 0) sm8[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0;
+    for (int w = 0; w < 8; w++) t += sm8[w];
+    out[ch] = t;
+  }
+  __syncthreads();
+}
+
+// The mean over the lattice from the chunk sums, in chunk order (every CTA
+// forms the same value).
+__device__ double spec_chunk_mean(const SpecLattice& L, const double* sums, int nch) {
+  double t = 0;
+  for (int b = 0; b < nch; b++) t += __ldcg(&sums[b]);
+  return t / ((double)L.R * L.C);
+}
+
 template <int TILE>
 __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* __restrict__ QR,
                                                     const float* __restrict__ QC, const float* __restrict__ D,
@@ -179,10 +166,21 @@ __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* 
   __shared__ float Bs[TILE == 64 ? 1 : 32][33];
   __shared__ __align__(16) SpecGemmSmem sg[TILE == 64 ? 1 : 0 + 1];
   __shared__ double sm8[8];
+  __shared__ double s_mean;
   __shared__ int s_stop;
   const int R = L.R, C = L.C;
   const int nch = (R * C + SPEC_CHUNK - 1) / SPEC_CHUNK;
   const int tiles_c = (C + TILE - 1) / TILE, ntiles = tiles_c * ((R + TILE - 1) / TILE);
+  // PERIODIC: the chunk sums of b and of phi go after the residual's.
+  double* const sums = L.partials + nch;
+  const bool periodic = L.mode == EPIC_POISSON_PERIODIC;
+  if (periodic) {  // b projected onto zero mean: the mean of b over the unknowns
+    for (int ch = blockIdx.x; ch < nch; ch += gridDim.x) spec_chunk_sum(L, 0, ch, sums, sm8);
+    if (!spec_grid_sync(bar, flags, spin)) return;
+    if (threadIdx.x == 0) s_mean = spec_chunk_mean(L, sums, nch);
+    __syncthreads();
+    L.bmean = &s_mean;
+  }
   for (int s = 0;; s++) {
     for (int ch = blockIdx.x; ch < nch; ch += gridDim.x) {
       spec_residual_chunk(L, ch, sm8);
@@ -198,7 +196,7 @@ __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* 
       s_stop = done || s == stages;
     }
     __syncthreads();
-    if (s_stop) return;
+    if (s_stop) break;
 #define SPEC_PASS(EPI, K_, A_, B_, C_, D_)                                                                    \
   for (int t = blockIdx.x; t < ntiles; t += gridDim.x) {                                                       \
     if (TILE == 64)                                                                                          \
@@ -214,13 +212,27 @@ __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* 
     SPEC_PASS(2, C, t1, QC, nullptr, nullptr)
 #undef SPEC_PASS
   }
+  if (periodic) {  // phi shifted to zero mean over the unknowns (the FP64 solver's gauge)
+    for (int ch = blockIdx.x; ch < nch; ch += gridDim.x) spec_chunk_sum(L, 1, ch, sums, sm8);
+    if (!spec_grid_sync(bar, flags, spin)) return;
+    if (threadIdx.x == 0) s_mean = spec_chunk_mean(L, sums, nch);
+    __syncthreads();
+    const double m = s_mean;
+    for (int ch = blockIdx.x; ch < nch; ch += gridDim.x)
+      for (int u = 0; u < SPEC_CHUNK / 256; u++) {
+        const int q = ch * SPEC_CHUNK + u * 256 + threadIdx.x;
+        if (q < R * C) {
+          const int r = q / C, c = q - r * C;
+          L.phi[spec_node(L, r, c)] -= m;
+        }
+      }
+  }
 }
 
 void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs& a, int stages) {
   const int R = sp.R, C = sp.C;
   const SpecLattice L = lattice_of(sp, a);
   k_spec_init<<<(a.g.nx * a.g.ny + 255) / 256, 256, 0, st>>>(L, a.warm);
-  if (sp.mode == EPIC_POISSON_PERIODIC) k_spec_bmean<<<1, 1024, 0, st>>>(L);
   // One wave of co-resident CTAs, at most one per output tile.
   // Output tiles: 64 x 64 (register-blocked) once there are enough of them
   // for every SM, else 32 x 32 with two per SM, else 16 x 16.
@@ -247,7 +259,6 @@ void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs
   long long spin = spin_limit();
   void* params[] = {&Lk, &qr, &qc, &d, &t1, &stg, &bar, &flags, &spin};
   cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(256), params, 0, st);
-  if (sp.mode == EPIC_POISSON_PERIODIC) k_spec_gauge<<<1, 1024, 0, st>>>(L);
   if (sp.mode != EPIC_POISSON_DIRICHLET) launch_fill_poisson_nodes(st, a.g, sp.mode, a.phi);
 }
 
