@@ -109,7 +109,16 @@ struct CrossSections {
   // First-draw cut per speed bin (MCC_SPEED_BINS entries, see mcc_speed_bin),
   // for the direct MCC of one run's vel_norm and dt; null: the global cut.
   unsigned long long* bin_cut = nullptr;
+  // Device code only: the logarithmic table staged in shared memory as
+  // {tot, ela, exc, ion} per entry (mcc_stage_table), or null.
+  const double4* stab = nullptr;
 };
+// A logarithmic table of at most this many entries is staged in shared memory
+// by the collision kernels (32 bytes per entry).
+constexpr int MCC_SMEM_TABLE = 1536;
+inline int mcc_table_smem(const CrossSections& cs) {
+  return cs.kind == 1 && cs.n <= MCC_SMEM_TABLE ? (int)cs.n * 32 : 0;
+}
 
 // Speed bins of the MCC early-out, keyed by m = max(|vx|, |vy|, |vz|) (vel_norm
 // units, from the bits alone): bin 0 holds m < 2^-64, bin 1 + 4(e + 64) + q

@@ -46,12 +46,31 @@ __device__ __forceinline__ Sigma sigma_at(const CrossSections& cs, double energy
     if (i > (int)cs.n - 2) i = (int)cs.n - 2;
     if (i < 0) i = 0;
     double f = u - i;
-    s.ela = __ldg(&cs.ela[i]) * (1 - f) + __ldg(&cs.ela[i + 1]) * f;
-    s.exc = __ldg(&cs.exc[i]) * (1 - f) + __ldg(&cs.exc[i + 1]) * f;
-    s.ion = __ldg(&cs.ion[i]) * (1 - f) + __ldg(&cs.ion[i + 1]) * f;
-    s.tot = __ldg(&cs.tot[i]) * (1 - f) + __ldg(&cs.tot[i + 1]) * f;
+    if (cs.stab) {  // the same interpolation from the shared-memory copy
+      const double4 a = cs.stab[i], b = cs.stab[i + 1];
+      s.ela = a.y * (1 - f) + b.y * f;
+      s.exc = a.z * (1 - f) + b.z * f;
+      s.ion = a.w * (1 - f) + b.w * f;
+      s.tot = a.x * (1 - f) + b.x * f;
+    } else {
+      s.ela = __ldg(&cs.ela[i]) * (1 - f) + __ldg(&cs.ela[i + 1]) * f;
+      s.exc = __ldg(&cs.exc[i]) * (1 - f) + __ldg(&cs.exc[i + 1]) * f;
+      s.ion = __ldg(&cs.ion[i]) * (1 - f) + __ldg(&cs.ion[i + 1]) * f;
+      s.tot = __ldg(&cs.tot[i]) * (1 - f) + __ldg(&cs.tot[i + 1]) * f;
+    }
   }
   return s;
+}
+
+// The logarithmic table into shared memory (the whole CTA; ends with a
+// barrier) when it fits: every lookup of the collision pass then reads
+// shared memory instead of L2.
+__device__ __forceinline__ void mcc_stage_table(CrossSections& cs, double4* s_tab) {
+  if (cs.kind != 1 || cs.n > MCC_SMEM_TABLE) return;
+  for (int i = threadIdx.x; i < (int)cs.n; i += blockDim.x)
+    s_tab[i] = make_double4(__ldg(&cs.tot[i]), __ldg(&cs.ela[i]), __ldg(&cs.exc[i]), __ldg(&cs.ion[i]));
+  __syncthreads();
+  cs.stab = s_tab;
 }
 
 // Init::SampleVel (src/init.cpp:104-114).
@@ -282,10 +301,13 @@ __global__ void __launch_bounds__(PART_THREADS) k_mcc_collide(CrossSections cs, 
                                                               uint64_t seed,
                                                               const unsigned long long* __restrict__ d_step,
                                                               McEvents ev, unsigned long long* pending, int* flags) {
+  extern __shared__ double4 s_tab[];
   __shared__ unsigned long long s_coll;
-  if (threadIdx.x == 0) s_coll = 0;
-  __syncthreads();
   const unsigned int nc = *ev.cand_count;
+  if ((unsigned long long)blockIdx.x * blockDim.x >= nc) return;  // no candidates for this CTA
+  if (threadIdx.x == 0) s_coll = 0;
+  mcc_stage_table(cs, s_tab);
+  __syncthreads();
   const unsigned long long step = *d_step;
   unsigned int ncoll = 0;
   for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
@@ -475,15 +497,15 @@ static void launch_mcc_t(cudaStream_t st, int mode, const CrossSections& cs, con
                          const McEvents& ev, unsigned long long* d_ncoll, int* flags, int grid, int skip_select) {
   unsigned long long* pending = d_ncoll + 1;
   if (skip_select) {  // the push selected the candidates (mcc_candidate)
-    k_mcc_collide<EPIC_MCC_PHILOX, P><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
+    k_mcc_collide<EPIC_MCC_PHILOX, P><<<grid, PART_THREADS, mcc_table_smem(cs), st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
                                                                       pending, flags);
   } else if (mode == EPIC_MCC_INJECTED) {
     k_mcc_select<EPIC_MCC_INJECTED, P><<<grid, PART_THREADS, 0, st>>>(m, e, d_ne, uniforms, ustride, seed, d_step, ev);
-    k_mcc_collide<EPIC_MCC_INJECTED, P><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
+    k_mcc_collide<EPIC_MCC_INJECTED, P><<<grid, PART_THREADS, mcc_table_smem(cs), st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
                                                                         pending, flags);
   } else {
     k_mcc_select<EPIC_MCC_PHILOX, P><<<grid, PART_THREADS, 0, st>>>(m, e, d_ne, uniforms, ustride, seed, d_step, ev);
-    k_mcc_collide<EPIC_MCC_PHILOX, P><<<grid, PART_THREADS, 0, st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
+    k_mcc_collide<EPIC_MCC_PHILOX, P><<<grid, PART_THREADS, mcc_table_smem(cs), st>>>(cs, m, e, uniforms, ustride, seed, d_step, ev,
                                                                       pending, flags);
   }
   k_mcc_scan<<<1, 1024, 0, st>>>(d_ne, ev, pending);
@@ -583,10 +605,13 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_mcc_collide(CrossSection
                                                                     const unsigned long long* __restrict__ d_step,
                                                                     McEvents ev, unsigned long long* pending,
                                                                     int* flags) {
+  extern __shared__ double4 s_tab[];
   __shared__ unsigned long long s_coll;
-  if (threadIdx.x == 0) s_coll = 0;
-  __syncthreads();
   const unsigned int nc = *ev.cand_count;
+  if ((unsigned long long)blockIdx.x * blockDim.x >= nc) return;  // no candidates for this CTA
+  if (threadIdx.x == 0) s_coll = 0;
+  mcc_stage_table(cs, s_tab);
+  __syncthreads();
   const unsigned long long step = *d_step;
   unsigned int ncoll = 0;
   for (unsigned int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
@@ -621,7 +646,7 @@ void launch_batch_mcc(cudaStream_t st, const CrossSections& cs, const BRun* runs
                       int* flags, int grid) {
   unsigned long long* pending = d_ncoll + 1;
   k_batch_mcc_select<<<grid, PART_THREADS, 0, st>>>(runs, node_run, e, d_ne, d_step, ev);
-  k_batch_mcc_collide<<<grid, PART_THREADS, 0, st>>>(cs, runs, node_run, MixedParticles{e}, d_step, ev, pending, flags);
+  k_batch_mcc_collide<<<grid, PART_THREADS, mcc_table_smem(cs), st>>>(cs, runs, node_run, MixedParticles{e}, d_step, ev, pending, flags);
   k_mcc_scan<<<1, 1024, 0, st>>>(d_ne, ev, pending);
   k_mcc_append<MixedParticles><<<grid, PART_THREADS, 0, st>>>(MixedParticles{e}, d_ne, e_cap, MixedParticles{ion}, d_ni,
                                                               i_cap, ev, flags);
