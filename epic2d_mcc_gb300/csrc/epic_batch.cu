@@ -167,6 +167,148 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_rewind(const BRun* __res
   }
 }
 
+// The batch's step push: the single-run push of every particle with its run's
+// grid, field and constants, the CIC deposit of the new positions into acc
+// (deposit_warp_sorted with each cell's run's row stride) and, with SEL, the
+// MCC's first pass of k_batch_mcc_select on the pushed electrons of colliding
+// runs (appended to ev.cand, one atomic per warp with candidates).  Particles,
+// integer sums and the candidate set equal k_batch_push + k_batch_deposit +
+// k_batch_mcc_select.
+struct RunNy {
+  const BRun* runs;
+  const int* node_run;
+  __device__ __forceinline__ int operator()(int cg) const { return runs[__ldg(&node_run[cg])].ny; }
+};
+
+template <bool SEL>
+__global__ void __launch_bounds__(PART_THREADS, 3) k_batch_push_dep(const BRun* __restrict__ runs,
+                                                                    const int* __restrict__ node_run, MixedSoA p,
+                                                                    const long long* __restrict__ d_n,
+                                                                    const float2* __restrict__ ef32, int s,
+                                                                    unsigned long long* __restrict__ acc,
+                                                                    const unsigned long long* __restrict__ d_step,
+                                                                    McEvents ev) {
+  constexpr int P = DEP_PER_THREAD;
+  __shared__ DepWarp tables[PART_THREADS / 32];
+  DepWarp& w = tables[threadIdx.x >> 5];
+  const long long n = *d_n;
+  const unsigned long long step = SEL ? *d_step : 0ull;
+  const int lane = threadIdx.x & 31;
+  const RunNy ny_of{runs, node_run};
+  dep_init(w);
+  for (long long chunk = (long long)blockIdx.x * DEP_CHUNK; chunk < n; chunk += (long long)gridDim.x * DEP_CHUNK) {
+    const long long q0 = chunk + (long long)threadIdx.x * P;
+    const bool full = q0 + P <= n;
+    int c[P];
+    float ox[P], oy[P], vx[P], vy[P];
+    if (full) {
+#pragma unroll
+      for (int h = 0; h < P / 4; h++) {
+        const int4 cc = reinterpret_cast<const int4*>(p.cell + q0)[h];
+        const float4 a = reinterpret_cast<const float4*>(p.ox + q0)[h];
+        const float4 b = reinterpret_cast<const float4*>(p.oy + q0)[h];
+        const float4 u = reinterpret_cast<const float4*>(p.vx + q0)[h];
+        const float4 v = reinterpret_cast<const float4*>(p.vy + q0)[h];
+        c[4 * h] = cc.x; c[4 * h + 1] = cc.y; c[4 * h + 2] = cc.z; c[4 * h + 3] = cc.w;
+        ox[4 * h] = a.x; ox[4 * h + 1] = a.y; ox[4 * h + 2] = a.z; ox[4 * h + 3] = a.w;
+        oy[4 * h] = b.x; oy[4 * h + 1] = b.y; oy[4 * h + 2] = b.z; oy[4 * h + 3] = b.w;
+        vx[4 * h] = u.x; vx[4 * h + 1] = u.y; vx[4 * h + 2] = u.z; vx[4 * h + 3] = u.w;
+        vy[4 * h] = v.x; vy[4 * h + 1] = v.y; vy[4 * h + 2] = v.z; vy[4 * h + 3] = v.w;
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < P; k++) {
+        const long long q = q0 + k;
+        const bool in = q < n;
+        c[k] = in ? p.cell[q] : -1;
+        ox[k] = in ? p.ox[q] : 0.f;
+        oy[k] = in ? p.oy[q] : 0.f;
+        vx[k] = in ? p.vx[q] : 0.f;
+        vy[k] = in ? p.vy[q] : 0.f;
+      }
+    }
+    unsigned int cand = 0;
+#pragma unroll
+    for (int k = 0; k < P; k++)
+      if (c[k] >= 0) {
+        const BRun& r = runs[__ldg(&node_run[c[k]])];
+        const Geom g = run_geom(r);
+        const float2* ef = ef32 + r.node_off;
+        int cl = (int)(c[k] - r.node_off);
+        if (r.bc == EPIC_PBC)
+          push_mixed_one<EPIC_CIC, EPIC_PBC>(g, ef, r.qmK_dt[s], r.cx, r.cy, cl, ox[k], oy[k], vx[k], vy[k]);
+        else
+          push_mixed_one<EPIC_CIC, EPIC_REFLECTIVE>(g, ef, r.qmK_dt[s], r.cx, r.cy, cl, ox[k], oy[k], vx[k], vy[k]);
+        c[k] = (int)(r.node_off + cl);
+        if (SEL && r.mcc) {
+          const long long q = q0 + k;
+          Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)r.seed, (uint32_t)(r.seed >> 32), 0,
+                     make_uint4(0, 0, 0, 0)};
+          if (src.next53() < r.cut53) cand |= 1u << k;
+        }
+      }
+    if (full) {
+#pragma unroll
+      for (int h = 0; h < P / 4; h++) {
+        reinterpret_cast<int4*>(p.cell + q0)[h] = make_int4(c[4 * h], c[4 * h + 1], c[4 * h + 2], c[4 * h + 3]);
+        reinterpret_cast<float4*>(p.ox + q0)[h] = make_float4(ox[4 * h], ox[4 * h + 1], ox[4 * h + 2], ox[4 * h + 3]);
+        reinterpret_cast<float4*>(p.oy + q0)[h] = make_float4(oy[4 * h], oy[4 * h + 1], oy[4 * h + 2], oy[4 * h + 3]);
+        reinterpret_cast<float4*>(p.vx + q0)[h] = make_float4(vx[4 * h], vx[4 * h + 1], vx[4 * h + 2], vx[4 * h + 3]);
+        reinterpret_cast<float4*>(p.vy + q0)[h] = make_float4(vy[4 * h], vy[4 * h + 1], vy[4 * h + 2], vy[4 * h + 3]);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < P; k++)
+        if (c[k] >= 0) {
+          const long long q = q0 + k;
+          p.cell[q] = c[k];
+          p.ox[q] = ox[k];
+          p.oy[q] = oy[k];
+          p.vx[q] = vx[k];
+          p.vy[q] = vy[k];
+        }
+    }
+    if (SEL && __any_sync(0xffffffffu, cand != 0)) {
+      const unsigned int mine = __popc(cand);
+      unsigned int incl = mine;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      unsigned int base = 0;
+      if (lane == 31) base = atomicAdd(ev.cand_count, incl);
+      unsigned int o = __shfl_sync(0xffffffffu, base, 31) + incl - mine;
+#pragma unroll
+      for (int k = 0; k < P; k++)
+        if (cand & (1u << k)) ev.cand[o++] = (unsigned int)(q0 + k);
+    }
+    deposit_warp_sorted(acc, w, ny_of, c, ox, oy);
+  }
+}
+
+// CIC deposit of the particles [*d_from, *d_n) of a species (the MCC's
+// ionisation products, appended after the push deposited the rest).
+__global__ void __launch_bounds__(PART_THREADS) k_batch_deposit_range(const BRun* __restrict__ runs,
+                                                                      const int* __restrict__ node_run, MixedSoA p,
+                                                                      const long long* __restrict__ d_from,
+                                                                      const long long* __restrict__ d_n,
+                                                                      unsigned long long* __restrict__ acc) {
+  const long long from = *d_from, n = *d_n;
+  const long long S = 1ll << MIXED_OFFSET_BITS;
+  const float fS = (float)S;
+  for (long long q = from + (long long)blockIdx.x * blockDim.x + threadIdx.x; q < n;
+       q += (long long)gridDim.x * blockDim.x) {
+    const int c = p.cell[q];
+    const int ny = runs[node_run[c]].ny;
+    const long long a = (long long)(p.ox[q] * fS), b = (long long)(p.oy[q] * fS);
+    atomicAdd(&acc[c], (unsigned long long)((S - a) * (S - b)));
+    atomicAdd(&acc[c + ny], (unsigned long long)(a * (S - b)));
+    atomicAdd(&acc[c + 1], (unsigned long long)((S - a) * b));
+    atomicAdd(&acc[c + ny + 1], (unsigned long long)(a * b));
+  }
+}
+
 // Integer CIC deposit of a species (the mixed form's weights, exact, so the
 // grid is the single runs' bit for bit).  Each CTA takes 2048 consecutive
 // particles; when the nodes they touch fit in shared memory (sorted
@@ -408,6 +550,10 @@ struct epic_batch {
   double* staging = nullptr;
   int64_t step_index = 0;
   cudaGraphExec_t g_plain = nullptr, g_sort = nullptr;
+  // acc holds the deposit of the current positions (the step's push leaves it
+  // so); the counts before the MCC, whose products are deposited after it
+  bool acc_valid = false;
+  long long* d_nold = nullptr;
   std::vector<void*> allocs;
   // MCC
   bool any_mcc = false;
@@ -484,11 +630,16 @@ struct epic_batch {
     k_batch_spec_check<<<(nruns + 255) / 256, 256, 0, stream>>>(b, nruns, 1);
   }
 
-  void deposit_and_solve() {
+  void deposit_all() {
     for (int s = 0; s < nsp; s++) {
       cudaMemsetAsync(acc[s], 0, nodes * sizeof(unsigned long long), stream);
       k_batch_deposit<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], acc[s]);
     }
+    acc_valid = true;
+  }
+
+  void deposit_and_solve() {
+    if (!acc_valid) deposit_all();
     launch_batch_finalize(stream, grids());
     solve();
     launch_batch_efield(stream, grids());
@@ -508,14 +659,32 @@ struct epic_batch {
     }
   }
 
+  // A step: (sort,) field phase from the accumulators, then each species'
+  // push deposits its new positions (and the electrons' push selects the MCC's
+  // candidates), the MCC, and the deposit of its ionisation products.
   void step(int sort) {
-    if (sort) sort_all();
+    if (sort) sort_all();  // the accumulators do not depend on the order
     deposit_and_solve();
-    for (int s = 0; s < nsp; s++)
-      k_batch_push<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s);
-    if (any_mcc)
+    const int grid_dep = resident_grid(k_batch_push_dep<true>, PART_THREADS);
+    for (int s = 0; s < nsp; s++) {
+      cudaMemsetAsync(acc[s], 0, nodes * sizeof(unsigned long long), stream);
+      if (any_mcc && s == 0)
+        k_batch_push_dep<true><<<grid_dep, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s,
+                                                                      acc[s], d_step, ev);
+      else
+        k_batch_push_dep<false><<<grid_dep, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s,
+                                                                       acc[s], d_step, ev);
+    }
+    if (any_mcc) {
+      for (int k = 0; k < 2; k++)
+        cudaMemcpyAsync(d_nold + k, d_n[k], sizeof(long long), cudaMemcpyDeviceToDevice, stream);
       launch_batch_mcc(stream, cs, d_runs, d_node_run, arena[0], d_n[0], cap[0], arena[1], d_n[1], cap[1], d_step, ev,
-                       d_ncoll, flags, grid);
+                       d_ncoll, flags, grid, 1);
+      for (int k = 0; k < 2; k++)
+        k_batch_deposit_range<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[k], d_nold + k, d_n[k],
+                                                                 acc[k]);
+    }
+    acc_valid = true;
   }
 };
 
@@ -759,6 +928,7 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
   if ((st = b->alloc(&b->partials, chunk_off))) return st;
   if ((st = b->alloc(&b->state, 4 * (size_t)nruns))) return st;
   if ((st = b->alloc(&b->flags, 1))) return st;
+  if ((st = b->alloc(&b->d_nold, 2))) return st;
   if ((st = b->alloc(&b->chunk_sched, chunks.size()))) return st;
   b->nchunk = (int)chunks.size();
   for (int s = 0; s < b->nsp; s++) {
@@ -931,6 +1101,7 @@ epic_status epic_batch_run(epic_batch* b, int steps, int use_graph) {
     return EPIC_OK;
   };
   epic_status st;
+  if (!b->acc_valid) b->deposit_all();  // the captured steps take the accumulators as deposited
   if (!b->g_plain && (st = capture(0, &b->g_plain))) return st;
   if (sorting && !b->g_sort && (st = capture(1, &b->g_sort))) return st;
   for (int k = 0; k < steps; k++) {

@@ -36,7 +36,7 @@ struct CrossSections;
 void launch_batch_mcc(cudaStream_t st, const CrossSections& cs, const BRun* runs, const int* node_run,
                       const MixedSoA& e, long long* d_ne, long long e_cap, const MixedSoA& ion, long long* d_ni,
                       long long i_cap, unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll,
-                      int* flags, int grid);
+                      int* flags, int grid, int skip_select = 0);
 
 struct BatchGrids {
   int nruns, nsp;

@@ -643,9 +643,10 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_mcc_collide(CrossSection
 void launch_batch_mcc(cudaStream_t st, const CrossSections& cs, const BRun* runs, const int* node_run,
                       const MixedSoA& e, long long* d_ne, long long e_cap, const MixedSoA& ion, long long* d_ni,
                       long long i_cap, unsigned long long* d_step, const McEvents& ev, unsigned long long* d_ncoll,
-                      int* flags, int grid) {
+                      int* flags, int grid, int skip_select) {
   unsigned long long* pending = d_ncoll + 1;
-  k_batch_mcc_select<<<grid, PART_THREADS, 0, st>>>(runs, node_run, e, d_ne, d_step, ev);
+  if (!skip_select)  // else the electrons' push selected the candidates (k_batch_push_dep)
+    k_batch_mcc_select<<<grid, PART_THREADS, 0, st>>>(runs, node_run, e, d_ne, d_step, ev);
   k_batch_mcc_collide<<<grid, PART_THREADS, mcc_table_smem(cs), st>>>(cs, runs, node_run, MixedParticles{e}, d_step, ev, pending, flags);
   k_mcc_scan<<<1, 1024, 0, st>>>(d_ne, ev, pending);
   k_mcc_append<MixedParticles><<<grid, PART_THREADS, 0, st>>>(MixedParticles{e}, d_ne, e_cap, MixedParticles{ion}, d_ni,

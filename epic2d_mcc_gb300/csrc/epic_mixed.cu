@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(PART_THREADS, 3) k_push_mixed_dep(Geom g, Mixe
       for (int k = 0; k < P; k++)
         if (cand & (1u << k)) sel.cand[o++] = (unsigned int)(q0 + k);
     }
-    deposit_warp_sorted(acc, w, g.ny, c, ox, oy);
+    deposit_warp_sorted(acc, w, ConstNy{g.ny}, c, ox, oy);
   }
 }
 

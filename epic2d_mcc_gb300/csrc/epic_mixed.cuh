@@ -184,8 +184,16 @@ __device__ __forceinline__ void dep_node_weights(unsigned long long* __restrict_
   atomicAdd(&acc[c + ny + 1], AB);
 }
 
-__device__ __forceinline__ void dep_run(unsigned long long* __restrict__ acc, DepWarp& w, int ny, int c, unsigned N,
-                                        unsigned A, unsigned B, unsigned ab_lo, unsigned ab_hi) {
+// The row stride (nodes per grid row) of a cell's grid: one grid, or a batch's
+// runs laid end to end (the stride of the run that holds the cell).
+struct ConstNy {
+  int ny;
+  __device__ __forceinline__ int operator()(int) const { return ny; }
+};
+
+template <class NY>
+__device__ __forceinline__ void dep_run(unsigned long long* __restrict__ acc, DepWarp& w, const NY& ny_of, int c,
+                                        unsigned N, unsigned A, unsigned B, unsigned ab_lo, unsigned ab_hi) {
   if (c < 0) return;
   const int m = (int)(((unsigned)c * 0x9E3779B1u) >> 25);  // 7-bit multiplicative hash
   int t = *(volatile int*)&w.tag[m];
@@ -198,7 +206,7 @@ __device__ __forceinline__ void dep_run(unsigned long long* __restrict__ acc, De
       }
     }
     if (t != c) {
-      dep_node_weights(acc, ny, c, N, A, B, ab_lo, ab_hi);
+      dep_node_weights(acc, ny_of(c), c, N, A, B, ab_lo, ab_hi);
       return;
     }
   }
@@ -210,8 +218,9 @@ __device__ __forceinline__ void dep_run(unsigned long long* __restrict__ acc, De
 }
 
 // Every lane of the warp calls this once per chunk with its particles
-// (c[k] < 0: no particle).
-__device__ __forceinline__ void deposit_warp_sorted(unsigned long long* __restrict__ acc, DepWarp& w, int ny,
+// (c[k] < 0: no particle); ny_of(cell) gives the cell's row stride.
+template <class NY>
+__device__ __forceinline__ void deposit_warp_sorted(unsigned long long* __restrict__ acc, DepWarp& w, const NY& ny_of,
                                                     const int (&c)[DEP_PER_THREAD],
                                                     const float (&ox)[DEP_PER_THREAD],
                                                     const float (&oy)[DEP_PER_THREAD]) {
@@ -226,7 +235,7 @@ __device__ __forceinline__ void deposit_warp_sorted(unsigned long long* __restri
     const unsigned a = (unsigned)(int)(ox[k] * fS), b = (unsigned)(int)(oy[k] * fS);
     const unsigned long long ab = (unsigned long long)a * b;
     if (c[k] != cur) {
-      dep_run(acc, w, ny, cur, N, A, B, L, H);
+      dep_run(acc, w, ny_of, cur, N, A, B, L, H);
       cur = c[k];
       N = 0; A = 0; B = 0; L = 0; H = 0;
     }
@@ -236,14 +245,15 @@ __device__ __forceinline__ void deposit_warp_sorted(unsigned long long* __restri
     L += (unsigned)ab & DEP_LIMB;
     H += (unsigned)(ab >> 20);
   }
-  dep_run(acc, w, ny, cur, N, A, B, L, H);
+  dep_run(acc, w, ny_of, cur, N, A, B, L, H);
   __syncwarp();
   const int cnt = *(volatile int*)&w.count;
   __syncwarp();
   if (lane == 0) w.count = 0;  // every lane has read it; the next appends follow the last __syncwarp
   for (int e = lane; e < cnt; e += 32) {
     const int m = w.list[e];
-    dep_node_weights(acc, ny, w.tag[m], w.n[m], w.a[m], w.b[m], w.ab_lo[m], w.ab_hi[m]);
+    const int cm = w.tag[m];
+    dep_node_weights(acc, ny_of(cm), cm, w.n[m], w.a[m], w.b[m], w.ab_lo[m], w.ab_hi[m]);
     w.n[m] = w.a[m] = w.b[m] = w.ab_lo[m] = w.ab_hi[m] = 0;
     w.tag[m] = -1;
   }

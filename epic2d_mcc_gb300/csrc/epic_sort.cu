@@ -370,7 +370,7 @@ __global__ void __launch_bounds__(PART_THREADS) k_deposit_mixed_sorted(Geom g, M
         oy[k] = q < n ? __ldg(&p.oy[q]) : 0.f;
       }
     }
-    deposit_warp_sorted(acc, w, g.ny, c, ox, oy);
+    deposit_warp_sorted(acc, w, ConstNy{g.ny}, c, ox, oy);
   }
 }
 
