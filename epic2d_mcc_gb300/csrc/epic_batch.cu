@@ -287,6 +287,76 @@ __global__ void __launch_bounds__(PART_THREADS, 3) k_batch_push_dep(const BRun* 
   }
 }
 
+// The batch's push when some run has absorbing walls: each particle with its
+// run's constants and wall rule; a particle that leaves an open run is erased
+// and the rest keep their order (std::vector::erase, src/species.cpp:100-112),
+// through the single run's ordered tile scan (k_push_mixed_compact) over the
+// whole shared array, so every run's particles stay contiguous and in order.
+__global__ void __launch_bounds__(PART_THREADS) k_batch_push_compact(const BRun* __restrict__ runs,
+                                                                     const int* __restrict__ node_run, MixedSoA p,
+                                                                     long long* d_n, const float2* __restrict__ ef32,
+                                                                     int s, unsigned long long* status,
+                                                                     unsigned int* tile_ctr, int* flags, long long spin) {
+  constexpr int ITEMS = SCAN_TILE / PART_THREADS;
+  __shared__ int sm[40];
+  __shared__ unsigned long long s_prefix;
+  __shared__ int s_tile;
+  const long long n = *d_n;
+  const int num_tiles = (int)((n + SCAN_TILE - 1) / SCAN_TILE);
+  for (;;) {
+    if (threadIdx.x == 0) s_tile = (int)atomicAdd(tile_ctr, 1u);
+    __syncthreads();
+    const int tile = s_tile;
+    if (tile >= num_tiles) break;
+    const long long base = (long long)tile * SCAN_TILE;
+    int c[ITEMS], keep[ITEMS];
+    float ox[ITEMS], oy[ITEMS], vx[ITEMS], vy[ITEMS], vz[ITEMS];
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+      const long long q = base + (long long)k * PART_THREADS + threadIdx.x;
+      keep[k] = 0;
+      if (q < n) {
+        const int cg = p.cell[q];
+        ox[k] = p.ox[q]; oy[k] = p.oy[q]; vx[k] = p.vx[q]; vy[k] = p.vy[q]; vz[k] = p.vz[q];
+        const BRun& r = runs[__ldg(&node_run[cg])];
+        const Geom g = run_geom(r);
+        const float2* ef = ef32 + r.node_off;
+        int cl = (int)(cg - r.node_off);
+        if (r.bc == EPIC_OPEN)
+          keep[k] = push_mixed_one<EPIC_CIC, EPIC_OPEN>(g, ef, r.qmK_dt[s], r.cx, r.cy, cl, ox[k], oy[k], vx[k], vy[k]);
+        else if (r.bc == EPIC_PBC)
+          keep[k] = push_mixed_one<EPIC_CIC, EPIC_PBC>(g, ef, r.qmK_dt[s], r.cx, r.cy, cl, ox[k], oy[k], vx[k], vy[k]);
+        else
+          keep[k] = push_mixed_one<EPIC_CIC, EPIC_REFLECTIVE>(g, ef, r.qmK_dt[s], r.cx, r.cy, cl, ox[k], oy[k], vx[k],
+                                                              vy[k]);
+        c[k] = (int)(r.node_off + cl);
+      }
+    }
+    int rank[ITEMS];
+    int tile_total = 0;
+#pragma unroll
+    for (int k = 0; k < ITEMS; k++) {
+      int row_total;
+      rank[k] = tile_total + block_exclusive_scan(keep[k], &row_total, sm);
+      tile_total += row_total;
+    }
+    if (threadIdx.x == 0) s_prefix = tile_lookback(status, tile, (unsigned long long)tile_total, flags, spin);
+    __syncthreads();
+    const unsigned long long prefix = s_prefix;
+    if (prefix != ~0ull) {
+#pragma unroll
+      for (int k = 0; k < ITEMS; k++) {
+        if (keep[k]) {
+          const long long o = (long long)prefix + rank[k];
+          p.cell[o] = c[k]; p.ox[o] = ox[k]; p.oy[o] = oy[k]; p.vx[o] = vx[k]; p.vy[o] = vy[k]; p.vz[o] = vz[k];
+        }
+      }
+      if (tile == num_tiles - 1 && threadIdx.x == 0) *d_n = (long long)prefix + tile_total;
+    }
+    __syncthreads();
+  }
+}
+
 // CIC deposit of the particles [*d_from, *d_n) of a species (the MCC's
 // ionisation products, appended after the push deposited the rest).
 __global__ void __launch_bounds__(PART_THREADS) k_batch_deposit_range(const BRun* __restrict__ runs,
@@ -310,101 +380,29 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_deposit_range(const BRun
 }
 
 // Integer CIC deposit of a species (the mixed form's weights, exact, so the
-// grid is the single runs' bit for bit).  Each CTA takes 2048 consecutive
-// particles; when the nodes they touch fit in shared memory (sorted
-// particles) runs of equal cells merge in registers and the CTA adds its
-// range once, otherwise particles add straight to the grid.
-constexpr int BDEP_PER_THREAD = 8;
-constexpr int BDEP_CHUNK = PART_THREADS * BDEP_PER_THREAD;
-constexpr int BDEP_SMEM = 3072;
-
+// grid is the single runs' bit for bit): deposit_warp_sorted over chunks of
+// consecutive particles, each cell with its run's row stride.
 __global__ void __launch_bounds__(PART_THREADS) k_batch_deposit(const BRun* __restrict__ runs,
                                                                 const int* __restrict__ node_run, MixedSoA p,
                                                                 const long long* __restrict__ d_n,
                                                                 unsigned long long* __restrict__ acc) {
-  __shared__ unsigned long long sacc[BDEP_SMEM];
-  __shared__ int s_lo, s_hi;
+  __shared__ DepWarp tables[PART_THREADS / 32];
+  DepWarp& w = tables[threadIdx.x >> 5];
   const long long n = *d_n;
-  const int S = 1 << MIXED_OFFSET_BITS;
-  const float fS = (float)S;
-  if (threadIdx.x == 0) {
-    s_lo = INT_MAX;
-    s_hi = -1;
-  }
-  __syncthreads();
-  for (long long chunk = (long long)blockIdx.x * BDEP_CHUNK; chunk < n; chunk += (long long)gridDim.x * BDEP_CHUNK) {
-    const long long q0 = chunk + (long long)threadIdx.x * BDEP_PER_THREAD;
-    int c[BDEP_PER_THREAD], ny[BDEP_PER_THREAD];
-    float ox[BDEP_PER_THREAD], oy[BDEP_PER_THREAD];
-    int lo = INT_MAX, hi = -1;
+  const RunNy ny_of{runs, node_run};
+  dep_init(w);
+  for (long long chunk = (long long)blockIdx.x * DEP_CHUNK; chunk < n; chunk += (long long)gridDim.x * DEP_CHUNK) {
+    const long long q0 = chunk + (long long)threadIdx.x * DEP_PER_THREAD;
+    int c[DEP_PER_THREAD];
+    float ox[DEP_PER_THREAD], oy[DEP_PER_THREAD];
 #pragma unroll
-    for (int k = 0; k < BDEP_PER_THREAD; k++) {
+    for (int k = 0; k < DEP_PER_THREAD; k++) {
       const long long q = q0 + k;
-      c[k] = q < n ? p.cell[q] : -1;
-      ox[k] = q < n ? p.ox[q] : 0.f;
-      oy[k] = q < n ? p.oy[q] : 0.f;
-      ny[k] = c[k] >= 0 ? runs[node_run[c[k]]].ny : 0;
-      if (c[k] >= 0) {
-        lo = min(lo, c[k]);
-        hi = max(hi, c[k] + ny[k] + 1);
-      }
+      c[k] = q < n ? __ldg(&p.cell[q]) : -1;
+      ox[k] = q < n ? __ldg(&p.ox[q]) : 0.f;
+      oy[k] = q < n ? __ldg(&p.oy[q]) : 0.f;
     }
-    lo = __reduce_min_sync(0xffffffffu, lo);
-    hi = __reduce_max_sync(0xffffffffu, hi);
-    if ((threadIdx.x & 31) == 0) {
-      atomicMin(&s_lo, lo);
-      atomicMax(&s_hi, hi);
-    }
-    __syncthreads();
-    const int blo = s_lo, bhi = s_hi;
-    const int span = bhi < 0 ? 0 : bhi + 1 - blo;
-    const bool smem = span <= BDEP_SMEM;
-    if (smem)
-      for (int m = threadIdx.x; m < span; m += PART_THREADS) sacc[m] = 0;
-    __syncthreads();
-    auto flush = [&](int cc, int nyy, unsigned long long w00, unsigned long long w10, unsigned long long w01,
-                     unsigned long long w11) {
-      if (cc < 0) return;
-      if (smem) {
-        atomicAdd(&sacc[cc - blo], w00);
-        atomicAdd(&sacc[cc - blo + nyy], w10);
-        atomicAdd(&sacc[cc - blo + 1], w01);
-        atomicAdd(&sacc[cc - blo + nyy + 1], w11);
-      } else {
-        atomicAdd(&acc[cc], w00);
-        atomicAdd(&acc[cc + nyy], w10);
-        atomicAdd(&acc[cc + 1], w01);
-        atomicAdd(&acc[cc + nyy + 1], w11);
-      }
-    };
-    int cur = -1, cur_ny = 0;
-    unsigned long long a00 = 0, a10 = 0, a01 = 0, a11 = 0;
-#pragma unroll
-    for (int k = 0; k < BDEP_PER_THREAD; k++) {
-      if (c[k] < 0) continue;
-      const unsigned long long a = (unsigned long long)(int)(ox[k] * fS), b = (unsigned long long)(int)(oy[k] * fS);
-      const unsigned long long w00 = (S - a) * (S - b), w10 = a * (S - b), w01 = (S - a) * b, w11 = a * b;
-      if (c[k] != cur) {
-        flush(cur, cur_ny, a00, a10, a01, a11);
-        cur = c[k];
-        cur_ny = ny[k];
-        a00 = w00; a10 = w10; a01 = w01; a11 = w11;
-      } else {
-        a00 += w00; a10 += w10; a01 += w01; a11 += w11;
-      }
-    }
-    flush(cur, cur_ny, a00, a10, a01, a11);
-    __syncthreads();
-    if (smem)
-      for (int m = threadIdx.x; m < span; m += PART_THREADS) {
-        const unsigned long long v = sacc[m];
-        if (v) atomicAdd(&acc[blo + m], v);
-      }
-    if (threadIdx.x == 0) {
-      s_lo = INT_MAX;
-      s_hi = -1;
-    }
-    __syncthreads();
+    deposit_warp_sorted(acc, w, ny_of, c, ox, oy);
   }
 }
 
@@ -554,6 +552,11 @@ struct epic_batch {
   // so); the counts before the MCC, whose products are deposited after it
   bool acc_valid = false;
   long long* d_nold = nullptr;
+  // some run has absorbing walls: the compacting push, its ordered tile scan
+  bool has_open = false;
+  unsigned long long* tile_status = nullptr;
+  unsigned int* tile_ctr = nullptr;
+  long long tile_status_len = 0;
   std::vector<void*> allocs;
   // MCC
   bool any_mcc = false;
@@ -664,6 +667,21 @@ struct epic_batch {
   // candidates), the MCC, and the deposit of its ionisation products.
   void step(int sort) {
     if (sort) sort_all();  // the accumulators do not depend on the order
+    if (has_open) {  // erasing pushes: deposit, field, compacting push, MCC with its own selection
+      deposit_all();
+      deposit_and_solve();
+      for (int s = 0; s < nsp; s++) {
+        cudaMemsetAsync(tile_ctr, 0, sizeof(unsigned int), stream);
+        cudaMemsetAsync(tile_status, 0, tile_status_len * sizeof(unsigned long long), stream);
+        k_batch_push_compact<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s,
+                                                                tile_status, tile_ctr, flags, spin_limit());
+      }
+      if (any_mcc)
+        launch_batch_mcc(stream, cs, d_runs, d_node_run, arena[0], d_n[0], cap[0], arena[1], d_n[1], cap[1], d_step,
+                         ev, d_ncoll, flags, grid);
+      acc_valid = false;
+      return;
+    }
     deposit_and_solve();
     const int grid_dep = resident_grid(k_batch_push_dep<true>, PART_THREADS);
     for (int s = 0; s < nsp; s++) {
@@ -821,8 +839,9 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
     if (reqs[r].num_species != b->nsp) return bfail(EPIC_ERR_INVALID, "run %d: every run needs %d species", r, b->nsp);
     if (c.precision != EPIC_PRECISION_MIXED) return bfail(EPIC_ERR_INVALID, "run %d: batches run the mixed form", r);
     if (c.shape != EPIC_CIC) return bfail(EPIC_ERR_INVALID, "run %d: batches deposit with CIC", r);
-    if (c.bc != EPIC_PBC && c.bc != EPIC_REFLECTIVE)
-      return bfail(EPIC_ERR_INVALID, "run %d: batches take periodic or reflective walls", r);
+    if (c.bc != EPIC_PBC && c.bc != EPIC_REFLECTIVE && c.bc != EPIC_OPEN)
+      return bfail(EPIC_ERR_INVALID, "run %d: bad wall rule", r);
+    if (c.bc == EPIC_OPEN) b->has_open = true;
     if (reqs[r].collisions) {
       if (b->nsp < 2) return bfail(EPIC_ERR_INVALID, "run %d: MCC needs electrons (species 0) and ions (1)", r);
       if (b->any_mcc && c.gas_density != b->gas_density)
@@ -942,6 +961,10 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
   }
   long long cmax = 0, nmax = 1;
   for (int s = 0; s < b->nsp; s++) cmax = std::max(cmax, b->cap[s]);
+  if (b->has_open) {
+    b->tile_status_len = cmax / SCAN_TILE + 2;
+    if ((st = b->alloc(&b->tile_status, (size_t)b->tile_status_len)) || (st = b->alloc(&b->tile_ctr, 1))) return st;
+  }
   for (long long v : b->pn) nmax = std::max(nmax, v);
   if (b->sort_every > 0) {
     BCK(cudaMallocAsync(&b->sort_buf, sort_scratch_bytes(cmax, 24), b->stream));
@@ -1115,7 +1138,7 @@ epic_status epic_batch_run(epic_batch* b, int steps, int use_graph) {
 epic_status epic_batch_get_particles(epic_batch* b, int run, int s, double* out, int64_t capacity, int64_t* n) {
   if (!b || run < 0 || run >= b->nruns || s < 0 || s >= b->nsp || !out)
     return bfail(EPIC_ERR_INVALID, "bad argument");
-  if (!b->any_mcc) {  // counts never change and each run's particles stay contiguous
+  if (!b->any_mcc && !b->has_open) {  // counts never change and each run's particles stay where they were loaded
     const long long cnt = b->pn[(size_t)run * b->nsp + s];
     if (n) *n = cnt;
     if (cnt > capacity)

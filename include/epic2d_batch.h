@@ -23,10 +23,13 @@
  * each lattice-size class by timing both on the batch's own transforms; the
  * choice does not change results.
  *
- * Runs must use the mixed form with CIC deposition, periodic or reflective
- * walls, and the same number of species (species k plays the same role in
- * every run; MCC needs electrons as species 0 and ions as species 1); the
- * colliding runs share one gas density. */
+ * Runs must use the mixed form with CIC deposition and the same number of
+ * species (species k plays the same role in every run; MCC needs electrons as
+ * species 0 and ions as species 1); the colliding runs share one gas density.
+ * Walls may be periodic, reflective or absorbing, mixed within a batch; with
+ * an absorbing run in the batch the push erases leaving particles in order
+ * (as a single run) and the deposit and the MCC's selection run as their own
+ * passes. */
 #ifndef EPIC2D_BATCH_H
 #define EPIC2D_BATCH_H
 
