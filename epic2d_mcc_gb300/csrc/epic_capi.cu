@@ -341,6 +341,12 @@ epic_status do_solve(epic_sim* s) {
   PhaseTimer t(s, 2);
   SolverArgs a = solver_args(s);
   if (s->mixed && s->spec.QR) {
+    if (s->cfg.solver == EPIC_SOLVER_GS && !s->conductors.empty()) {
+      // Grid::initialize inside gssolver (src/field.cpp:100-103): the same
+      // right-hand side for the spectral solve of the same operator
+      launch_conductor_rho(s->stream, s->rho, s->d_cond_nodes, s->d_cond_vals, s->cond_nnodes, s->d_cond_live);
+      s->launches += 1;
+    }
     launch_spectral(s->stream, s->spec, a, SPECTRAL_STAGES);
     // set-up, the cooperative solve, the duplicated nodes (extensions)
     s->launches += 2 + (s->spec.mode != EPIC_POISSON_DIRICHLET ? 1 : 0);
@@ -404,9 +410,10 @@ epic_status do_push(epic_sim* s, int i, int sub_cycle, const SelectArgs* sel = n
   } else if (s->mixed) {
     const bool dep = fused_deposit(s);
     if (dep) CK(cudaMemsetAsync(sp.acc, 0, nnodes(s) * sizeof(unsigned long long), s->stream));
+    const CondSet cs{s->cond_nrect, s->cond_ncirc, s->d_cond_rect, s->d_cond_circ, s->d_cond_live};
     launch_push_mixed(s->stream, s->g, c.shape, c.bc, sp.mx, sp.d_n, s->ef32, (float)(qmK * dtsub),
                       (float)(cc * dtsub / c.dx), (float)(cc * dtsub / c.dy), s->d_flags, s->tile_status,
-                      s->tile_ctr, s->part_grid, dep ? sp.acc : nullptr, dep ? sel : nullptr);
+                      s->tile_ctr, s->part_grid, dep ? sp.acc : nullptr, dep ? sel : nullptr, cond ? &cs : nullptr);
     sp.acc_valid = dep;
   } else {
     const bool dep = fused_deposit(s);
@@ -530,7 +537,8 @@ epic_status do_inject_range(epic_sim* s, size_t k0, size_t k1, const double* d_u
       e.num = m.numparticle;
       e.slot = slot;
       e.emitter = (int)k;
-      launch_emit(s->stream, sp.soa, sp.d_n, sp.cap, e, c.seed, s->d_inj, u, s->d_flags, s->part_grid);
+      launch_emit(s->stream, ParticleRef{s->mixed, sp.soa, sp.mx}, s->g, sp.d_n, sp.cap, e, c.seed, s->d_inj, u,
+                  s->d_flags, s->part_grid);
     }
     for (int slot = 0; slot < slots; slot++) {
       epic_species_state& sp = s->sp[sp_of[slot]];
@@ -679,7 +687,6 @@ epic_status epic_conductors_from_ini(const char* path, epic_conductor* out, int 
 
 epic_status epic_add_conductor(epic_sim* s, const epic_conductor* c) {
   if (!s || !c) return fail(EPIC_ERR_INVALID, "bad argument");
-  if (s->mixed) return fail(EPIC_ERR_INVALID, "conductors are supported in the FP64 form");
   if (s->cfg.poisson_bc != EPIC_POISSON_DIRICHLET)
     return fail(EPIC_ERR_INVALID, "conductors are supported with the reference's Poisson boundary");
   if (c->type != EPIC_CONDUCTOR_RECT && c->type != EPIC_CONDUCTOR_CIRCULAR)
@@ -733,7 +740,6 @@ epic_status epic_emitters_from_ini(const char* path, epic_emitter* out, int max,
 
 epic_status epic_add_emitter(epic_sim* s, const epic_emitter* e) {
   if (!s || !e) return fail(EPIC_ERR_INVALID, "bad argument");
-  if (s->mixed) return fail(EPIC_ERR_INVALID, "emitters are supported in the FP64 form");
   const int nsp = (int)s->sp.size();
   if (e->species_idx1 < 0 || e->species_idx1 >= nsp || e->species_idx2 < 0 || e->species_idx2 >= nsp)
     return fail(EPIC_ERR_INVALID, "emitter species index out of range (add the species first)");

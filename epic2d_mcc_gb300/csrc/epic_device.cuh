@@ -151,4 +151,21 @@ static __device__ __forceinline__ int block_exclusive_scan(int v, int* total, in
   return warp_prefix + x - v;
 }
 
+// Grid::IsGrid of any conductor (src/grid.cpp:11-65, src/electrode.cpp:20-26),
+// for the FP64 and the mixed push.
+__device__ __forceinline__ bool in_conductor(const CondSet& cs, double x, double y) {
+  for (int k = 0; k < cs.nrect; k++) {
+    const double4 r = cs.rect[k];
+    if (x >= r.x && x <= r.y && y >= r.z && y <= r.w) return true;
+  }
+  if (cs.ncirc && *cs.live) {
+    for (int k = 0; k < cs.ncirc; k++) {
+      const double4 e = cs.circ[k];
+      const double dx = __dsub_rn(x, e.x), dy = __dsub_rn(y, e.y);
+      if (__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)) <= e.z) return true;  // uncontracted in every file
+    }
+  }
+  return false;
+}
+
 }  // namespace epic

@@ -162,9 +162,10 @@ struct EmitDev {
   double vth, vdx, vdy, vel_norm;  // vth = sqrt(2 k_B T EV_to_K / m); vdx, vdy in m/s
   int num, slot, emitter;
 };
-void launch_emit(cudaStream_t st, const SoA& p, const long long* d_n, long long cap, const EmitDev& e,
-                 unsigned long long seed, const unsigned long long* d_inj, const double* uniforms, int* flags,
-                 int grid);
+struct ParticleRef;
+void launch_emit(cudaStream_t st, const ParticleRef& p, const Geom& g, const long long* d_n, long long cap,
+                 const EmitDev& e, unsigned long long seed, const unsigned long long* d_inj, const double* uniforms,
+                 int* flags, int grid);
 void launch_emit_commit(cudaStream_t st, long long* d_n, long long num, long long cap, int* flags);
 void launch_inject_tick(cudaStream_t st, unsigned long long* d_inj);
 struct SelectArgs;
@@ -249,11 +250,13 @@ int resident_grid(K kernel, int threads) {
 
 // With dep_acc (CIC, periodic or reflective walls) every pushed particle is
 // also deposited at its new position into dep_acc (integer weights), and with
-// sel the electrons' MCC candidates are appended to sel->cand.
+// sel the electrons' MCC candidates are appended to sel->cand.  With cond,
+// particles that end inside a conductor are erased (compacting push).
 void launch_push_mixed(cudaStream_t st, const Geom& g, int shape, int bc, const MixedSoA& p, long long* d_n,
                        const float2* ef, float qmK_dt, float cx, float cy, int* flags,
                        unsigned long long* tile_status, unsigned int* tile_ctr, int grid,
-                       unsigned long long* dep_acc = nullptr, const SelectArgs* sel = nullptr);
+                       unsigned long long* dep_acc = nullptr, const SelectArgs* sel = nullptr,
+                       const CondSet* cond = nullptr);
 void launch_deposit_mixed_range(cudaStream_t st, const Geom& g, const MixedSoA& p, const long long* d_from,
                                 const long long* d_n, unsigned long long* acc, int grid);
 void launch_rewind_mixed(cudaStream_t st, const Geom& g, int shape, const MixedSoA& p, const long long* d_n,

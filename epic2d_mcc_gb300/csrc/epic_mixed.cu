@@ -249,14 +249,17 @@ __global__ void __launch_bounds__(PART_THREADS, 3) k_push_mixed_dep(Geom g, Mixe
   }
 }
 
-// Open boundaries: push + stable in-place compaction with ordered tiles
-// (the FP64 form's scheme; see k_push_compact in epic_particles.cu).
-template <int SHAPE>
+// Open boundaries or conductors: push + stable in-place compaction with
+// ordered tiles (the FP64 form's scheme; see k_push_compact in
+// epic_particles.cu).  COND: a particle that ends inside a conductor, its
+// position taken as x0 + (i + ox) dx in FP64, is erased too
+// (src/species.cpp:80-165).
+template <int SHAPE, int BC, bool COND>
 __global__ void __launch_bounds__(PART_THREADS) k_push_mixed_compact(Geom g, MixedSoA p, long long* d_n,
                                                                      const float2* __restrict__ ef, float qmK_dt,
                                                                      float cx, float cy, unsigned long long* status,
                                                                      unsigned int* tile_ctr, int* flags,
-                                                                     long long spin) {
+                                                                     long long spin, CondSet cs) {
   constexpr int ITEMS = SCAN_TILE / PART_THREADS;
   __shared__ int sm[40];
   __shared__ unsigned long long s_prefix;
@@ -277,7 +280,14 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_mixed_compact(Geom g, Mix
       keep[k] = 0;
       if (q < n) {
         c[k] = p.cell[q]; ox[k] = p.ox[q]; oy[k] = p.oy[q]; vx[k] = p.vx[q]; vy[k] = p.vy[q]; vz[k] = p.vz[q];
-        keep[k] = push_mixed_one<SHAPE, EPIC_OPEN>(g, ef, qmK_dt, cx, cy, c[k], ox[k], oy[k], vx[k], vy[k]);
+        keep[k] = push_mixed_one<SHAPE, BC>(g, ef, qmK_dt, cx, cy, c[k], ox[k], oy[k], vx[k], vy[k]);
+        if (COND && keep[k]) {
+          int i, j;
+          split_cell(c[k], g.ny, i, j);
+          const double x = __dadd_rn(g.x0, __dmul_rn(__dadd_rn((double)i, (double)ox[k]), g.dx));
+          const double y = __dadd_rn(g.y0, __dmul_rn(__dadd_rn((double)j, (double)oy[k]), g.dy));
+          keep[k] = !in_conductor(cs, x, y);
+        }
       }
     }
     int rank[ITEMS];
@@ -308,7 +318,23 @@ __global__ void __launch_bounds__(PART_THREADS) k_push_mixed_compact(Geom g, Mix
 void launch_push_mixed(cudaStream_t st, const Geom& g, int shape, int bc, const MixedSoA& p, long long* d_n,
                        const float2* ef, float qmK_dt, float cx, float cy, int* flags,
                        unsigned long long* tile_status, unsigned int* tile_ctr, int grid,
-                       unsigned long long* dep_acc, const SelectArgs* sel) {
+                       unsigned long long* dep_acc, const SelectArgs* sel, const CondSet* cond) {
+  if (cond) {  // the compacting push with the conductor test, for any wall rule
+#define PC(SH, B) \
+  k_push_mixed_compact<SH, B, true><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy, tile_status, tile_ctr, \
+                                                                   flags, spin_limit(), *cond)
+#define PCB(SH)                          \
+  do {                                   \
+    if (bc == EPIC_OPEN) PC(SH, EPIC_OPEN); \
+    else if (bc == EPIC_PBC) PC(SH, EPIC_PBC); \
+    else PC(SH, EPIC_REFLECTIVE);        \
+  } while (0)
+    if (shape == EPIC_NGP) PCB(EPIC_NGP);
+    else PCB(EPIC_CIC);
+#undef PCB
+#undef PC
+    return;
+  }
 #define PM(SH, B) k_push_mixed<SH, B><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy)
   if (dep_acc && shape == EPIC_CIC && (bc == EPIC_PBC || bc == EPIC_REFLECTIVE)) {
     const SelectArgs a = sel ? *sel : SelectArgs{};
@@ -323,11 +349,11 @@ void launch_push_mixed(cudaStream_t st, const Geom& g, int shape, int bc, const 
   }
   if (bc == EPIC_OPEN) {
     if (shape == EPIC_NGP)
-      k_push_mixed_compact<EPIC_NGP><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy, tile_status,
-                                                                     tile_ctr, flags, spin_limit());
+      k_push_mixed_compact<EPIC_NGP, EPIC_OPEN, false><<<grid, PART_THREADS, 0, st>>>(
+          g, p, d_n, ef, qmK_dt, cx, cy, tile_status, tile_ctr, flags, spin_limit(), CondSet{});
     else
-      k_push_mixed_compact<EPIC_CIC><<<grid, PART_THREADS, 0, st>>>(g, p, d_n, ef, qmK_dt, cx, cy, tile_status,
-                                                                     tile_ctr, flags, spin_limit());
+      k_push_mixed_compact<EPIC_CIC, EPIC_OPEN, false><<<grid, PART_THREADS, 0, st>>>(
+          g, p, d_n, ef, qmK_dt, cx, cy, tile_status, tile_ctr, flags, spin_limit(), CondSet{});
   } else if (bc == EPIC_PBC) {
     if (shape == EPIC_NGP) PM(EPIC_NGP, EPIC_PBC);
     else PM(EPIC_CIC, EPIC_PBC);

@@ -15,6 +15,7 @@
 #include <cmath>
 
 #include "epic_internal.cuh"
+#include "epic_mixed.cuh"
 #include "epic_device.cuh"
 
 namespace epic {
@@ -432,21 +433,6 @@ __global__ void __launch_bounds__(PART_THREADS) k_push(Geom g, SoA p, const long
 // survivors written in place at (prefix of earlier tiles) + rank.  A tile's
 // writes land only at or below its own range, in slots earlier tiles have
 // already loaded before publishing their counts, so no second buffer is needed.
-// Grid::IsGrid of any conductor (src/grid.cpp:11-65, src/electrode.cpp:20-26).
-__device__ __forceinline__ bool in_conductor(const CondSet& cs, double x, double y) {
-  for (int k = 0; k < cs.nrect; k++) {
-    const double4 r = cs.rect[k];
-    if (x >= r.x && x <= r.y && y >= r.z && y <= r.w) return true;
-  }
-  if (cs.ncirc && *cs.live) {
-    for (int k = 0; k < cs.ncirc; k++) {
-      const double4 e = cs.circ[k];
-      const double dx = x - e.x, dy = y - e.y;
-      if (dx * dx + dy * dy <= e.z) return true;
-    }
-  }
-  return false;
-}
 
 template <int SHAPE, int BC, int MAP, bool COND, bool CONTRACT>
 __global__ void __launch_bounds__(PART_THREADS) k_push_compact(Geom g, SoA p, long long* d_n,
@@ -609,8 +595,11 @@ void launch_conductor_rho(cudaStream_t st, double* rho, const int* nodes, const 
 // src/init.cpp:110-114: vth sqrt(2) (u1 + u2 + u3 - 1.5), plus the drift, over
 // vel_norm), from the caller's rows of 14 or from Philox keyed by
 // (q, emitter | 2^31, injection, seed) - distinct from the MCC's keys.
-__global__ void __launch_bounds__(PART_THREADS) k_emit(SoA p, const long long* __restrict__ d_n, long long cap,
-                                                       EmitDev e, unsigned long long seed,
+// MIXED: the record goes to the mixed form's layout (cell and FP32 offsets of
+// the FP64 position, FP32 velocities), as the upload converts it.
+template <bool MIXED>
+__global__ void __launch_bounds__(PART_THREADS) k_emit(SoA p, MixedSoA m, Geom g, const long long* __restrict__ d_n,
+                                                       long long cap, EmitDev e, unsigned long long seed,
                                                        const unsigned long long* __restrict__ d_inj,
                                                        const double* __restrict__ uniforms, int* flags) {
   const long long n0 = *d_n;
@@ -645,11 +634,27 @@ __global__ void __launch_bounds__(PART_THREADS) k_emit(SoA p, const long long* _
     vx /= e.vel_norm;
     vy /= e.vel_norm;
     vz /= e.vel_norm;
-    p.x[o] = u[0] * (e.x1 - e.x0) + e.x0;
-    p.y[o] = u[1] * (e.y1 - e.y0) + e.y0;
-    p.vx[o] = vx;
-    p.vy[o] = vy;
-    p.vz[o] = vz;
+    const double x = u[0] * (e.x1 - e.x0) + e.x0;
+    const double y = u[1] * (e.y1 - e.y0) + e.y0;
+    if (MIXED) {
+      int i, j;
+      float ox, oy;
+      const bool in_x = cell_offset((x - g.x0) / g.dx, g.nx - 1, i, ox);
+      const bool in_y = cell_offset((y - g.y0) / g.dy, g.ny - 1, j, oy);
+      if (!(in_x && in_y)) set_flag(flags, FLAG_OUT_OF_GRID);
+      m.cell[o] = i * g.ny + j;
+      m.ox[o] = ox;
+      m.oy[o] = oy;
+      m.vx[o] = (float)vx;
+      m.vy[o] = (float)vy;
+      m.vz[o] = (float)vz;
+    } else {
+      p.x[o] = x;
+      p.y[o] = y;
+      p.vx[o] = vx;
+      p.vy[o] = vy;
+      p.vz[o] = vz;
+    }
   }
 }
 
@@ -664,11 +669,12 @@ __global__ void k_emit_commit(long long* d_n, long long num, long long cap, int*
 
 __global__ void k_inject_tick(unsigned long long* d_inj) { *d_inj += 1; }
 
-void launch_emit(cudaStream_t st, const SoA& p, const long long* d_n, long long cap, const EmitDev& e,
-                 unsigned long long seed, const unsigned long long* d_inj, const double* uniforms, int* flags,
-                 int grid) {
+void launch_emit(cudaStream_t st, const ParticleRef& p, const Geom& g, const long long* d_n, long long cap,
+                 const EmitDev& e, unsigned long long seed, const unsigned long long* d_inj, const double* uniforms,
+                 int* flags, int grid) {
   const int blocks = std::max(1, std::min(grid, (e.num + PART_THREADS - 1) / PART_THREADS));
-  k_emit<<<blocks, PART_THREADS, 0, st>>>(p, d_n, cap, e, seed, d_inj, uniforms, flags);
+  if (p.mixed) k_emit<true><<<blocks, PART_THREADS, 0, st>>>(p.f, p.m, g, d_n, cap, e, seed, d_inj, uniforms, flags);
+  else k_emit<false><<<blocks, PART_THREADS, 0, st>>>(p.f, p.m, g, d_n, cap, e, seed, d_inj, uniforms, flags);
 }
 
 void launch_emit_commit(cudaStream_t st, long long* d_n, long long num, long long cap, int* flags) {

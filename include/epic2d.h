@@ -279,7 +279,9 @@ epic_status epic_delta_phi(epic_sim* sim, double* delta_phi);
  * does not), particles that end a push inside one are erased in order
  * (src/species.cpp:80-165), and Init redraws random positions inside one
  * (src/init.cpp:71-86; a CircularGrid has electrodes only after the first SOR
- * solve, as in the reference).  FP64 form only. */
+ * solve, as in the reference).  Both forms (the mixed push tests the FP64
+ * position rebuilt from cell and offset); load with epic_load_particles (the
+ * device loader does not place particles around conductors). */
 enum { EPIC_CONDUCTOR_RECT = 0, EPIC_CONDUCTOR_CIRCULAR = 1 };
 typedef struct epic_conductor {
   int type;                                  /* EPIC_CONDUCTOR_* ("reactconduct", "circular") */
@@ -302,7 +304,7 @@ epic_status epic_add_conductor(epic_sim* sim, const epic_conductor* c);
  * drift.  The reference draws the positions from a std::random_device-seeded
  * generator (not reproducible) and the velocities from its global stream;
  * here both come from a Philox stream keyed by (point, emitter, injection,
- * seed), or from caller uniforms (epic_inject).  FP64 form only. */
+ * seed), or from caller uniforms (epic_inject).  Both forms. */
 typedef struct epic_emitter {
   double x0, y0, x1, y1; /* injection rectangle (a segment when x0 == x1 or y0 == y1) */
   double temp;           /* eV */
