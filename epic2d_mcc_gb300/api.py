@@ -456,10 +456,15 @@ class Simulation:
 
 
 # ------------------------------------------------------------------ serving ---
+REQUEST_MAX_CONDUCTORS = REQUEST_MAX_EMITTERS = 8
+
+
 class Request(ctypes.Structure):
     _fields_ = [("cfg", Config), ("species", SpeciesDesc * 8), ("num_species", ctypes.c_int),
                 ("steps", ctypes.c_int), ("collisions", ctypes.c_int), ("load_seed", ctypes.c_uint64),
-                ("arrival_s", ctypes.c_double)]
+                ("arrival_s", ctypes.c_double), ("num_conductors", ctypes.c_int),
+                ("conductors", Conductor * REQUEST_MAX_CONDUCTORS), ("num_emitters", ctypes.c_int),
+                ("emitters", Emitter * REQUEST_MAX_EMITTERS)]
 
 
 class Result(ctypes.Structure):
@@ -496,6 +501,16 @@ def make_request(path: str, steps: int, collisions: bool = False, seed: int = 0,
     r.collisions = int(bool(collisions))
     r.load_seed = int(seed)
     r.arrival_s = float(arrival_s)
+    conds, ems = conductors_from_ini(path), emitters_from_ini(path)
+    if len(conds) > REQUEST_MAX_CONDUCTORS or len(ems) > REQUEST_MAX_EMITTERS:
+        raise ValueError("a request carries at most %d conductors and %d emitters" % (REQUEST_MAX_CONDUCTORS,
+                                                                                     REQUEST_MAX_EMITTERS))
+    r.num_conductors = len(conds)
+    for k, c in enumerate(conds):
+        r.conductors[k] = c
+    r.num_emitters = len(ems)
+    for k, e in enumerate(ems):
+        r.emitters[k] = e
     return r
 
 

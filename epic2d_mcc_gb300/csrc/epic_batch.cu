@@ -838,6 +838,8 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
     const epic_config& c = reqs[r].cfg;
     if (reqs[r].num_species != b->nsp) return bfail(EPIC_ERR_INVALID, "run %d: every run needs %d species", r, b->nsp);
     if (c.precision != EPIC_PRECISION_MIXED) return bfail(EPIC_ERR_INVALID, "run %d: batches run the mixed form", r);
+    if (reqs[r].num_conductors || reqs[r].num_emitters)
+      return bfail(EPIC_ERR_INVALID, "run %d: conductors and emitters run in the server and the single-run form", r);
     if (c.shape != EPIC_CIC) return bfail(EPIC_ERR_INVALID, "run %d: batches deposit with CIC", r);
     if (c.bc != EPIC_PBC && c.bc != EPIC_REFLECTIVE && c.bc != EPIC_OPEN)
       return bfail(EPIC_ERR_INVALID, "run %d: bad wall rule", r);

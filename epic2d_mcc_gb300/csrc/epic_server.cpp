@@ -32,11 +32,13 @@ struct Run {
   bool done = false;
 };
 
-// A run whose solve waits at grid-wide barriers (cooperative launches) must
-// not share the device with another such kernel.
+// Runs admitted alone: those whose FP64 solve is a cooperative launch with one
+// CTA per SM (the PCG, red-black SOR), which would wait for the whole GPU
+// beside other runs.  The mixed form's spectral solve is a cooperative launch
+// too, sized to its lattice's tiles (at most two CTAs per SM); served runs
+// share the GPU with it.  Every grid-wide wait is bounded (a run whose wait
+// gives up fails with EPIC_ERR_TIMEOUT instead of hanging).
 bool needs_exclusive(const epic_config& c) {
-  // the mixed form solves with the spectral method (no grid barrier) on any
-  // grid under pcgsolver's norm and on isotropic grids under gssolver's
   const bool spectral = c.precision == EPIC_PRECISION_MIXED && c.nx >= 3 && c.ny >= 3 &&
                         (c.solver == EPIC_SOLVER_PCG || (c.solver == EPIC_SOLVER_GS && c.dx == c.dy));
   if (spectral) return false;
@@ -98,9 +100,14 @@ struct epic_server {
     int st = epic_create(&q.cfg, &r->sim);
     if (st) return st;
     for (int k = 0; k < q.num_species && !st; k++) st = epic_add_species(r->sim, &q.species[k], nullptr);
+    for (int k = 0; k < q.num_conductors && !st; k++) st = epic_add_conductor(r->sim, &q.conductors[k]);
+    for (int k = 0; k < q.num_emitters && !st; k++) st = epic_add_emitter(r->sim, &q.emitters[k]);
     if (!st && q.collisions && !ela.empty())
       st = epic_set_log_cross_sections(r->sim, ela.data(), exc.data(), ion.data(), (int64_t)ela.size(), e_min, e_max);
-    if (!st) st = epic_load_particles_device(r->sim, q.load_seed);
+    // the host loader keeps particles out of conductors (it blocks the
+    // scheduler for the load); the device loader places the rest
+    if (!st) st = q.num_conductors ? epic_load_particles(r->sim, (uint32_t)q.load_seed)
+                                   : epic_load_particles_device(r->sim, q.load_seed);
     if (!st) st = epic_initial_field_async(r->sim);
     return st;
   }
@@ -280,8 +287,34 @@ epic_status epic_server_set_log_cross_sections(epic_server* s, const double* ela
 
 epic_status epic_server_submit(epic_server* s, const epic_request* q, int64_t* id) {
   if (!s || !q || q->num_species < 1 || q->num_species > 8 || q->steps < 0) return EPIC_ERR_INVALID;
+  if (q->num_conductors < 0 || q->num_conductors > EPIC_REQUEST_MAX_CONDUCTORS || q->num_emitters < 0 ||
+      q->num_emitters > EPIC_REQUEST_MAX_EMITTERS)
+    return EPIC_ERR_INVALID;
   Run* r = new Run();
   r->req = *q;
+  // Room for the injections: a species that emitters feed gets the default
+  // capacity plus every particle they add over the run.
+  for (int e = 0; e < q->num_emitters; e++) {
+    const epic_emitter& m = q->emitters[e];
+    if (m.species_idx1 < 0 || m.species_idx1 >= q->num_species || m.species_idx2 < 0 ||
+        m.species_idx2 >= q->num_species || m.numparticle < 0) {
+      delete r;
+      return EPIC_ERR_INVALID;
+    }
+  }
+  for (int k = 0; k < q->num_species; k++) {
+    int64_t inj = 0;
+    for (int e = 0; e < q->num_emitters; e++) {
+      const epic_emitter& m = q->emitters[e];
+      if (m.species_idx1 == k || m.species_idx2 == k) inj += (int64_t)m.numparticle * q->steps;
+    }
+    epic_species_desc& d = r->req.species[k];
+    if (inj > 0) {
+      const int64_t base = d.capacity > 0 ? d.capacity : d.numparticle + d.numparticle / 2 + 4096;
+      d.capacity = base + inj;
+    }
+  }
+  q = &r->req;
   std::memset(&r->res, 0, sizeof(r->res));
   r->res.arrival_s = q->arrival_s;
   r->bytes = epic_estimate_bytes(&q->cfg, q->species, q->num_species, q->collisions);

@@ -29,6 +29,8 @@ extern "C" {
 
 typedef struct epic_server epic_server;
 
+enum { EPIC_REQUEST_MAX_CONDUCTORS = 8, EPIC_REQUEST_MAX_EMITTERS = 8 };
+
 typedef struct {
   epic_config cfg;
   epic_species_desc species[8];
@@ -37,6 +39,14 @@ typedef struct {
   int collisions;       /* MCC every step (species 0 against the gas, ions into species 1) */
   uint64_t load_seed;   /* Philox seed of the device loader */
   double arrival_s;     /* arrival, seconds after epic_server_start */
+  /* The deck's [Grids] and [Emitters] (epic_conductors_from_ini,
+   * epic_emitters_from_ini).  A run with conductors is loaded on the host
+   * (epic_load_particles with load_seed), whose loader keeps particles out of
+   * them; a run with emitters gets the room its injections need. */
+  int num_conductors;
+  epic_conductor conductors[EPIC_REQUEST_MAX_CONDUCTORS];
+  int num_emitters;
+  epic_emitter emitters[EPIC_REQUEST_MAX_EMITTERS];
 } epic_request;
 
 typedef struct {

@@ -113,6 +113,41 @@ def test_served_run_equals_the_plain_api(gpu_lib, tmp_path):
     assert sim.digest() == tuple(res.digest)
 
 
+@pytest.mark.parametrize("precision", [0, 1])
+def test_served_conductors_and_emitters_equal_the_plain_api(gpu_lib, tmp_path, precision):
+    """A request carries its deck's [Grids] and [Emitters]: loaded on the host
+    around the conductors, with room for the injections, and stepped in chunks
+    beside another run, it ends bit for bit where the plain API ends."""
+    A = gpu_lib.api
+    grids = [dict(type="reactconduct", min_x=10, max_x=12, min_y=4, max_y=16, grid_voltage=10),
+             dict(type="circular", x_center=40, y_center=30, electrode_number=6, grid_radius=6,
+                  electrod_radius=1.5, electrode_voltage=-5)]
+    em = [dict(x0=2, y0=20, x1=2, y1=30, temp=0.5, numparticle=400, vdx=0.2, vdy=0, species_idx1=0,
+               species_idx2=1)]
+    ini = decks.write(decks.deck(nx=64, ny=48, ne=20000, ni=20000, te=1, bc="open", solver="gs", tol="1e-8",
+                                 grids=grids, emitters=em), str(tmp_path))
+    steps = 40
+    req = A.make_request(ini, steps=steps, seed=9, precision=precision)
+    assert req.num_conductors == 2 and req.num_emitters == 1
+    other = A.make_request(ini, steps=12, seed=3, precision=1)
+    other.num_conductors = other.num_emitters = 0
+    srv = A.Server(budget_bytes=4 << 30, max_inflight=2, chunk_steps=7)
+    i = srv.submit(req)
+    srv.submit(other)
+    srv.start()
+    srv.wait(300)
+    res = srv.result(i)
+    srv.close()
+    assert res.status == 0
+    # the server's capacity: the default plus the emitter's particles over the run
+    sim = A.Simulation.from_ini(ini, precision=precision, capacity=20000 + 10000 + 4096 + 400 * steps)
+    sim.load_particles(9)
+    sim.initial_field()
+    sim.run(steps, graph=True)
+    assert sim.num_particles(1) > 20000 + 400 * steps // 2  # the emitter fed the ions
+    assert sim.digest() == tuple(res.digest)
+
+
 def test_admission_budget_exclusive_and_rejection(gpu_lib, tmp_path):
     A = gpu_lib.api
     d = str(tmp_path)
