@@ -4,9 +4,13 @@
 //
 // Built with -fmad=false so every expression rounds as the reference's does;
 // the PCG kernel uses explicit fma() where it is documented to.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <map>
+#include <mutex>
+#include <tuple>
 
 #include <algorithm>
 
@@ -350,6 +354,308 @@ __global__ void __launch_bounds__(SOR_THREADS) k_sor_lex(SolverArgs a, int use_s
 
 constexpr size_t SOR_SMEM_MAX = 200 * 1024;
 
+// ---- lexicographic SOR over a thread-block cluster ----
+// The pipelined wavefront of k_sor_lex spread over the C CTAs of one cluster
+// (C <= 16): CTA c owns node rows [c R, c R + R) and keeps their phi (and
+// rho K) in its shared memory.  At time step t every CTA updates the active
+// nodes of its own rows; the rows beside its band, and the wrapped rows of a
+// periodic lattice, are read from the owning CTA's shared memory through the
+// cluster's distributed shared memory, and a cluster barrier (release /
+// acquire) separates the time steps.  A node update is the same arithmetic
+// as in k_sor_lex, in the same wavefront order, so the iterates are the same
+// bit for bit.  The residual and the periodic means are exact sums over the
+// cluster, rounded once, so every CTA takes the same convergence decision.
+// The barrier is the hardware's cluster barrier: all CTAs of a cluster are
+// resident together and run the same number of time steps.
+constexpr int SORC_THREADS = 512;
+constexpr int SORC_MAX = 16;
+namespace cgx = cooperative_groups;
+
+struct SorcXs {  // a CTA's share of an exact cluster sum
+  int e;
+  unsigned long long v[2];
+};
+
+// Exact sum of term(q), q in [0, count) of this CTA, over the cluster;
+// the same value in every thread of every CTA.  Three cluster barriers.
+template <class F>
+__device__ double cluster_exact_sum(const cgx::cluster_group& cl, int count, const F& term, SorcXs* mine,
+                                    double* red) {
+  __shared__ int s_e[32];
+  __shared__ unsigned long long s_v[32][2];
+  __shared__ int s_A;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int C = (int)cl.num_blocks();
+  int e = 0;
+  for (int q = threadIdx.x; q < count; q += blockDim.x) e = max(e, xs_exponent(term(q)));
+  e = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
+  if (lane == 0) s_e[wid] = e;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int m = 0;
+    for (int w = 0; w < nw; w++) m = max(m, s_e[w]);
+    mine->e = m;
+  }
+  cl.sync();
+  if (threadIdx.x == 0) {
+    int m = 0;
+    for (int r = 0; r < C; r++) m = max(m, cl.map_shared_rank(mine, r)->e);
+    s_A = m;
+  }
+  __syncthreads();
+  const int A = s_A;
+  xs_int v = 0;
+  for (int q = threadIdx.x; q < count; q += blockDim.x) v += xs_from_double(term(q), A);
+  v = xs_warp_sum(v);
+  if (lane == 0) {
+    s_v[wid][0] = (unsigned long long)(xs_uint)v;
+    s_v[wid][1] = (unsigned long long)((xs_uint)v >> 64);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    xs_uint tot = 0;
+    for (int w = 0; w < nw; w++) tot += ((xs_uint)s_v[w][1] << 64) | s_v[w][0];
+    mine->v[0] = (unsigned long long)tot;
+    mine->v[1] = (unsigned long long)(tot >> 64);
+  }
+  cl.sync();
+  if (threadIdx.x == 0) {
+    xs_uint tot = 0;
+    for (int r = 0; r < C; r++) {
+      const SorcXs* o = cl.map_shared_rank(mine, r);
+      tot += ((xs_uint)o->v[1] << 64) | o->v[0];
+    }
+    red[33] = xs_to_double((xs_int)tot, A);
+  }
+  cl.sync();  // the shares are read before they are rewritten; red[33] visible
+  return red[33];
+}
+
+// with_rk: rho K of the band kept in shared memory after phi (not FLUID).
+template <bool FLUID, bool UNIT, bool EXT>
+__global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int R, int with_rk) {
+  extern __shared__ double smem[];
+  __shared__ double red[40];
+  __shared__ double* s_row0[SORC_MAX];  // phi of each CTA's band (distributed shared memory)
+  __shared__ SorcXs s_xs;
+  const cgx::cluster_group cl = cgx::this_cluster();
+  const int me = (int)cl.block_rank(), C = (int)cl.num_blocks();
+  const int nx = a.g.nx, ny = a.g.ny;
+  const SorLat l = sor_lattice(nx, ny, EXT ? a.poisson_bc : EPIC_POISSON_DIRICHLET);
+  const int r_lo = me * R, r_hi = min(nx, r_lo + R);
+  const int nloc = max(r_hi - r_lo, 0) * ny;
+  double* const phi = smem;  // rows [r_lo, r_hi)
+  double* const rK = with_rk ? smem + (size_t)R * ny : nullptr;
+  if (threadIdx.x < C) s_row0[threadIdx.x] = threadIdx.x == me ? phi : cl.map_shared_rank(phi, (int)threadIdx.x);
+  for (int q = threadIdx.x; q < nloc; q += blockDim.x) {
+    phi[q] = 0;  // cold start, zero edges (src/field.cpp:78-98)
+    if (rK) rK[q] = a.rho[(size_t)r_lo * ny + q] * a.K;
+  }
+  // this CTA's unknowns: lattice rows ai in [u_lo, u_hi)
+  const int u_lo = max(r_lo, l.i0) - l.i0, u_hi = min(r_hi, l.i0 + l.nxi) - l.i0;
+  const int Ru = max(u_hi - u_lo, 0);
+  const int nu = Ru * l.nyi;
+  auto unknown_local = [&](int q) { return (u_lo + l.i0 - r_lo + q / l.nyi) * ny + l.j0 + q % l.nyi; };
+  cl.sync();  // every band initialised (and every CTA running) before remote reads
+  auto row_of = [&](int i) -> const double* {
+    if (i >= r_lo && i < r_hi) return phi + (size_t)(i - r_lo) * ny;
+    const int o = i / R;
+    return s_row0[o] + (size_t)(i - o * R) * ny;
+  };
+  double smean = 0.0;
+  if (EXT && !FLUID && l.wrap_x)
+    smean = cluster_exact_sum(
+                cl, nu,
+                [&](int q) {
+                  const int kl = unknown_local(q);
+                  return rK ? rK[kl] : a.rho[(size_t)r_lo * ny + kl] * a.K;
+                },
+                &s_xs, red) /
+            (double)(l.nxi * l.nyi);
+  auto src = [&](int i, int j, int kl) -> double {
+    if (FLUID) return (a.rho[(size_t)i * ny + j] - exp(phi[kl])) * a.K;
+    return (rK ? rK[kl] : a.rho[(size_t)i * ny + j] * a.K) - smean;
+  };
+  // neighbours of unknown (i, j): rows iE, iW and columns jN, jS (sor_nbrs)
+  auto nbrs = [&](int i, int j, int& iE, int& iW, int& jN, int& jS) {
+    iE = i + 1; iW = i - 1; jN = j + 1; jS = j - 1;
+    if (EXT) {
+      if (!(i + 1 < nx - 1 || !l.wrap_x)) iE = 0;
+      if (i <= 0) iW = nx - 2;
+      if (!(j + 1 < ny - 1)) jN = 0;
+      if (j <= 0) jS = ny - 2;
+    }
+  };
+  const double dx2 = a.g.dx * a.g.dx, dy2 = a.g.dy * a.g.dy;
+  const double coeff = (2 / dx2) + (2 / dy2);
+  const double inv_coeff = 1 / coeff;
+  auto residual = [&]() -> double {
+    const double sum = cluster_exact_sum(
+        cl, nu,
+        [&](int q) {
+          const int i = u_lo + l.i0 + q / l.nyi, j = l.j0 + q % l.nyi;
+          const int kl = (i - r_lo) * ny + j;
+          int iE, iW, jN, jS;
+          nbrs(i, j, iE, iW, jN, jS);
+          double tx = row_of(iE)[j] - 2 * phi[kl] + row_of(iW)[j];
+          double ty = phi[kl - j + jN] - 2 * phi[kl] + phi[kl - j + jS];
+          if (!UNIT) {
+            tx = tx / dx2;
+            ty = ty / dy2;
+          }
+          const double Rv = (tx + ty) + src(i, j, kl);
+          return Rv * Rv;
+        },
+        &s_xs, red);
+    return sqrt(sum / (nx * ny));
+  };
+  const int nxi = l.nxi, nyi = l.nyi;
+  const int D = nxi + nyi - 1;
+  int cp = 2;
+  if (EXT) {
+    if (l.wrap_x && nxi > cp) cp = nxi;
+    if (l.wrap_y && nyi > cp) cp = nyi;
+  }
+  int iter = 0, converged = 0;
+  double L2 = 0;
+  if (nxi > 0 && nyi > 0) {
+    while (iter < a.max_iter) {
+      constexpr int P = FLUID ? 50 : 25;
+      int S = iter == 0 ? 1 : P;
+      if (S > a.max_iter - iter) S = a.max_iter - iter;
+      const int T = D + cp * (S - 1);
+      for (int t = 0; t < T; t++) {
+        const int s_lo = t - D + 1 > 0 ? (t - D + cp) / cp : 0;
+        const int s_hi = t / cp < S - 1 ? t / cp : S - 1;
+        const int items = (s_hi - s_lo + 1) * Ru;
+        for (int it = threadIdx.x; it < items; it += blockDim.x) {
+          const int s = s_lo + it / Ru, ai = u_lo + it % Ru;
+          const int d = t - cp * s;
+          const int a0 = d - (nyi - 1) > 0 ? d - (nyi - 1) : 0;
+          const int a1 = d < nxi - 1 ? d : nxi - 1;
+          if (ai < a0 || ai > a1) continue;
+          const int i = ai + l.i0, j = d - ai + l.j0;
+          const int kl = (i - r_lo) * ny + j;
+          int iE, iW, jN, jS;
+          nbrs(i, j, iE, iW, jN, jS);
+          double tx = row_of(iE)[j] + row_of(iW)[j], ty = phi[kl - j + jN] + phi[kl - j + jS];
+          if (!UNIT) {
+            tx = tx / dx2;
+            ty = ty / dy2;
+          }
+          const double sk = src(i, j, kl);
+          double phi_new = inv_coeff * ((sk + tx) + ty);
+          phi[kl] = phi[kl] + a.omega * (phi_new - phi[kl]);
+        }
+        cl.sync();
+      }
+      const int last = iter + S - 1;
+      iter += S;
+      if (last % P == 0) {
+        L2 = residual();
+        if (L2 < a.tol) {
+          converged = 1;
+          break;
+        }
+      }
+    }
+  }
+  if (EXT && l.wrap_x) {  // zero-mean gauge over the unknowns
+    const double m =
+        cluster_exact_sum(cl, nu, [&](int q) { return phi[unknown_local(q)]; }, &s_xs, red) / (double)(nxi * nyi);
+    for (int q = threadIdx.x; q < nu; q += blockDim.x) {
+      const int kl = unknown_local(q);
+      phi[kl] = phi[kl] - m;
+    }
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < nloc; q += blockDim.x) a.phi[(size_t)r_lo * ny + q] = phi[q];
+  if (me == 0 && threadIdx.x == 0) {
+    a.info->iterations = iter;
+    a.info->converged = converged;
+    a.info->error = L2;
+    atomicAdd(a.iter_total, (unsigned long long)iter);
+  }
+  cl.sync();  // no CTA leaves while another may still read its band
+}
+
+// Whether the device can co-schedule a cluster of C CTAs of this kernel with
+// this shared memory (asked once per kernel, size and shared memory).
+static bool cluster_fits(const void* kern, int C, int threads, size_t smem) {
+  static std::mutex mu;
+  static std::map<std::tuple<const void*, int, size_t>, bool> known;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(kern, C, smem);
+  const auto f = known.find(key);
+  if (f != known.end()) return f->second;
+  cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SOR_SMEM_MAX);
+  cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(C);
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  const bool ok = cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters >= 1;
+  if (!ok) cudaGetLastError();
+  known[key] = ok;
+  return ok;
+}
+
+// The cluster for a lattice: about min(16, nx / 4) CTAs of R rows each, phi (and rho K when it fits) in shared memory; 0 when the lattice is
+// too small, too large for the cluster's shared memory, or the device cannot
+// co-schedule the cluster (k_sor_lex then runs it on one CTA).
+struct SorCluster {
+  int C, R, with_rk;
+  size_t smem;
+};
+
+template <bool FLUID, bool UNIT, bool EXT>
+static SorCluster sor_cluster_shape(const SolverArgs& a) {
+  SorCluster c{0, 0, 0, 0};
+  const int nx = a.g.nx, ny = a.g.ny;
+  int C = std::min(SORC_MAX, nx / 4);
+  if (C < 2 || ny < 3) return c;
+  const int R = (nx + C - 1) / C;
+  C = (nx + R - 1) / R;  // no CTA without rows
+  const size_t band = (size_t)R * ny * sizeof(double);
+  if (band > SOR_SMEM_MAX) return c;
+  const int with_rk = !FLUID && 2 * band <= SOR_SMEM_MAX;
+  const size_t smem = band * (with_rk ? 2 : 1);
+  if (!cluster_fits((const void*)k_sor_cluster<FLUID, UNIT, EXT>, C, SORC_THREADS, smem)) return c;
+  c.C = C;
+  c.R = R;
+  c.with_rk = with_rk;
+  c.smem = smem;
+  return c;
+}
+
+// Launches the cluster form when the lattice suits it; false otherwise.
+template <bool FLUID, bool UNIT, bool EXT>
+static bool launch_sor_cluster(cudaStream_t st, const SolverArgs& a) {
+  const SorCluster c = sor_cluster_shape<FLUID, UNIT, EXT>(a);
+  if (!c.C) return false;
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = c.C;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3(c.C);
+  cfg.blockDim = dim3(SORC_THREADS);
+  cfg.dynamicSmemBytes = c.smem;
+  cfg.stream = st;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k_sor_cluster<FLUID, UNIT, EXT>, a, c.R, c.with_rk) == cudaSuccess;
+}
+
 void init_field_kernels() {
   static bool done = false;
   if (done) return;
@@ -369,11 +675,17 @@ void launch_sor_lex(cudaStream_t st, const SolverArgs& a) {
   const int use_smem = 2 * bytes <= SOR_SMEM_MAX ? 2 : bytes <= SOR_SMEM_MAX ? 1 : 0;
   const size_t smem = use_smem * bytes;
   if (a.poisson_bc != EPIC_POISSON_DIRICHLET) {
-    if (sor_unit(a)) k_sor_lex<false, true, true><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
-    else k_sor_lex<false, false, true><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
+    const bool cl = sor_unit(a) ? launch_sor_cluster<false, true, true>(st, a)
+                                : launch_sor_cluster<false, false, true>(st, a);
+    if (!cl) {
+      if (sor_unit(a)) k_sor_lex<false, true, true><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
+      else k_sor_lex<false, false, true><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
+    }
     launch_fill_poisson_nodes(st, a.g, a.poisson_bc, a.phi);
     return;
   }
+  if (sor_unit(a) ? launch_sor_cluster<false, true, false>(st, a) : launch_sor_cluster<false, false, false>(st, a))
+    return;
   if (sor_unit(a)) k_sor_lex<false, true, false><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
   else k_sor_lex<false, false, false><<<1, SOR_THREADS, smem, st>>>(a, use_smem);
 }
@@ -397,6 +709,8 @@ void launch_gsfluid(cudaStream_t st, const SolverArgs& a, double* rho) {
   k_gsfluid_edges<<<1, 256, 0, st>>>(a.g, rho, 10000 * (QE / (K_B * (QE / K_B))));
   const size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
   const int use_smem = bytes <= SOR_SMEM_MAX;
+  if (sor_unit(a) ? launch_sor_cluster<true, true, false>(st, a) : launch_sor_cluster<true, false, false>(st, a))
+    return;
   if (sor_unit(a)) k_sor_lex<true, true, false><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
   else k_sor_lex<true, false, false><<<1, SOR_THREADS, use_smem ? bytes : 0, st>>>(a, use_smem);
 }
@@ -409,10 +723,12 @@ void launch_gsfluid(cudaStream_t st, const SolverArgs& a, double* rho) {
 // iterations).  A is pcgsolver's 5-point matrix on the flattened vector (row
 // k / nx, column k % nx); the matrix-vector products sum the five entries in
 // ascending column order, which is the dense product's sum (its zero entries
-// leave it unchanged), and the dot products are summed serially in index
-// order by one thread, as vec::operator* does, so the iterates are the
-// reference's (exp aside: CUDA's and the host library's may differ in the
-// last bit).  One CTA; vectors in the solver workspace.
+// leave it unchanged).  vec::operator* sums its rounded products serially in
+// index order; here the same rounded products are summed exactly over the
+// CTA and rounded once (block_exact_sum), which differs from the serial sum
+// only by that sum's own rounding errors - a serial chain of dependent FP64
+// additions, one per node, would bound every CG iteration.  One CTA; vectors
+// in the solver workspace.
 __device__ __forceinline__ double nr_row(int nx, int ny, int k, double diag, const double* v) {
   const int row = k / nx, col = k - row * nx;
   double sum = 0;
@@ -424,34 +740,14 @@ __device__ __forceinline__ double nr_row(int nx, int ny, int k, double diag, con
   return sum;
 }
 
-// vec::operator* (sum += u[i] * v[i] in index order, each product rounded).
-// With prod (shared memory for n doubles) the products are formed by all
-// threads first - the same rounded values - so the one serial chain reads
-// them from shared memory instead of waiting on global loads.
-__device__ double nr_serial_dot(const double* u, const double* v, int n, double* s_out, double* prod) {
-  if (prod) {
-    for (int k = threadIdx.x; k < n; k += blockDim.x) prod[k] = u[k] * v[k];
-    __syncthreads();
-  }
-  if (threadIdx.x == 0) {
-    double r = 0;
-    if (prod)
-      for (int i = 0; i < n; i++) r += prod[i];
-    else
-      for (int i = 0; i < n; i++) r += u[i] * v[i];
-    *s_out = r;
-  }
-  __syncthreads();
-  const double r = *s_out;
-  __syncthreads();
-  return r;
+// (u, v): the rounded products u[i] * v[i] (the kernel is built without
+// contraction), summed exactly and rounded once.
+__device__ __forceinline__ double nr_dot(const double* u, const double* v, int n, double* red) {
+  return block_exact_sum(n, [&](int k) { return u[k] * v[k]; }, red);
 }
 
-constexpr int NRPCG_SMEM_MAX = 200 * 1024;  // products staged in shared memory up to this many bytes
-
 __global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
-  extern __shared__ double s_prod[];
-  __shared__ double s_dot;
+  __shared__ double red[40];
   const int nx = a.g.nx, ny = a.g.ny, n = nx * ny;
   const double dx2 = a.g.dx * a.g.dx;
   const double K = a.K;
@@ -464,7 +760,6 @@ __global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
   }
   __syncthreads();
   const int maxit = n < 10000 ? n : 10000;
-  double* const prod = (size_t)n * sizeof(double) <= (size_t)NRPCG_SMEM_MAX ? s_prod : nullptr;
   long long total = 0;
   for (int it = 0; it < 10; it++) {
     for (int k = threadIdx.x; k < n; k += blockDim.x) rhovec[k] = rhovec[k] + exp(x[k]) * K;
@@ -477,19 +772,19 @@ __global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
       p[k] = r[k];
     }
     __syncthreads();
-    double r02 = nr_serial_dot(r, r, n, &s_dot, prod);
+    double r02 = nr_dot(r, r, n, red);
     for (int i = 0; i < maxit; i++) {
       if (sqrt(r02) < 1e-4) break;
       for (int k = threadIdx.x; k < n; k += blockDim.x) Ap[k] = nr_row(nx, ny, k, J[k], p);
       __syncthreads();
-      const double pAp = nr_serial_dot(p, Ap, n, &s_dot, prod);
+      const double pAp = nr_dot(p, Ap, n, red);
       const double alpha = r02 / pAp;
       for (int k = threadIdx.x; k < n; k += blockDim.x) {
         y[k] = y[k] + p[k] * alpha;
         r[k] = r[k] - Ap[k] * alpha;
       }
       __syncthreads();
-      const double r12 = nr_serial_dot(r, r, n, &s_dot, prod);
+      const double r12 = nr_dot(r, r, n, red);
       const double beta = r12 / r02;
       for (int k = threadIdx.x; k < n; k += blockDim.x) p[k] = r[k] + p[k] * beta;
       __syncthreads();
@@ -508,11 +803,192 @@ __global__ void __launch_bounds__(1024) k_nrpcg(SolverArgs a) {
   }
 }
 
+// The same solve over a thread-block cluster: CTA c owns the nodes
+// [c per, c per + per) of the flattened vector and updates them; the
+// matrix-vector products read the neighbours' p (and x) from L2 after a
+// cluster barrier.  A dot product is summed exactly per CTA against the
+// CTA's own anchor, and the C CTA totals are aligned to the largest anchor
+// (bits below 2^-106 of the largest term dropped, a fixed rule) and added in
+// every warp after one cluster barrier: each CTA obtains the same value, so
+// every CTA takes the same CG and Newton decisions.
+constexpr int NRC_THREADS = 128;
+struct NrSlot {
+  int e;
+  unsigned long long v[2];
+};
+
+// mine: this call's slot; successive calls alternate between two slots, so a
+// slot is rewritten only after every CTA has passed the barrier of the call
+// in between, i.e. after every CTA has read it.
+template <class F>
+__device__ __forceinline__ double nrc_sum(const cgx::cluster_group& cl, int lo, int hi, const F& term, NrSlot* mine) {
+  __shared__ int s_e[NRC_THREADS / 32];
+  __shared__ unsigned long long s_v[NRC_THREADS / 32][2];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int C = (int)cl.num_blocks();
+  int e = 0;
+  for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) e = max(e, xs_exponent(term(k)));
+  e = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
+  if (lane == 0) s_e[wid] = e;
+  __syncthreads();
+  int Ac = 0;
+  for (int w = 0; w < NRC_THREADS / 32; w++) Ac = max(Ac, s_e[w]);
+  xs_int v = 0;
+  for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) v += xs_from_double(term(k), Ac);
+  v = xs_warp_sum(v);
+  if (lane == 0) {
+    s_v[wid][0] = (unsigned long long)(xs_uint)v;
+    s_v[wid][1] = (unsigned long long)((xs_uint)v >> 64);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    xs_uint tot = 0;
+    for (int w = 0; w < NRC_THREADS / 32; w++) tot += ((xs_uint)s_v[w][1] << 64) | s_v[w][0];
+    mine->e = Ac;
+    mine->v[0] = (unsigned long long)tot;
+    mine->v[1] = (unsigned long long)(tot >> 64);
+  }
+  cl.sync();
+  int er = 0;
+  xs_int vr = 0;
+  if (lane < C) {
+    const NrSlot* o = cl.map_shared_rank(mine, lane);
+    er = o->e;
+    vr = (xs_int)(((xs_uint)o->v[1] << 64) | o->v[0]);
+  }
+  const int A = (int)__reduce_max_sync(0xffffffffu, (unsigned)er);
+  vr >>= min(A - er, 127);
+  const xs_int tot = xs_warp_sum(vr);
+  return xs_to_double(tot, A);
+}
+
+// Row k of the matrix-vector product with v distributed over the cluster's
+// shared memory: node q lives in CTA q / per at index q % per (base[] holds
+// each CTA's array in the distributed shared memory window).
+__device__ __forceinline__ double nr_row_dsm(int nx, int ny, int k, double diag, double* const* base, int per,
+                                             int lo, int hi, const double* own) {
+  auto at = [&](int q) -> double {
+    if (q >= lo && q < hi) return own[q - lo];
+    const int o = q / per;
+    return base[o][q - o * per];
+  };
+  const int row = k / nx, col = k - row * nx;
+  double sum = 0;
+  if (row > 0) sum += 1.0 * at(k - nx);
+  if (col > 0) sum += 1.0 * at(k - 1);
+  sum += diag * own[k - lo];
+  if (col < nx - 1) sum += 1.0 * at(k + 1);
+  if (row < ny - 1) sum += 1.0 * at(k + nx);
+  return sum;
+}
+
+// Shared memory of a CTA: seven arrays of per doubles (rhovec, x, J, y, r,
+// p, Ap); x and p are read by the other CTAs for their products.
+constexpr int NRC_ARRAYS = 7;
+
+__global__ void __launch_bounds__(NRC_THREADS) k_nrpcg_cluster(SolverArgs a, int per) {
+  extern __shared__ double sv[];
+  __shared__ NrSlot s_slots[2];
+  __shared__ double* s_xb[SORC_MAX];
+  __shared__ double* s_pb[SORC_MAX];
+  const cgx::cluster_group cl = cgx::this_cluster();
+  const int me = (int)cl.block_rank(), C = (int)cl.num_blocks();
+  const int nx = a.g.nx, ny = a.g.ny, n = nx * ny;
+  const int lo = me * per, hi = min(n, lo + per);
+  const double dx2 = a.g.dx * a.g.dx;
+  const double K = a.K;
+  double *rhovec = sv, *x = sv + per, *J = sv + 2 * per, *y = sv + 3 * per;
+  double *r = sv + 4 * per, *p = sv + 5 * per, *Ap = sv + 6 * per;
+  if (threadIdx.x < C) {
+    s_xb[threadIdx.x] = cl.map_shared_rank(x, (int)threadIdx.x);
+    s_pb[threadIdx.x] = cl.map_shared_rank(p, (int)threadIdx.x);
+  }
+  int parity = 0;
+  // every thread touches the same nodes k = lo + threadIdx.x + m blockDim in
+  // every loop, so an array read only at its own nodes needs no barrier
+  for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+    const int i = k / ny, j = k - i * ny;
+    rhovec[k - lo] = (j == 0 || j == ny - 1 || i == 0 || i == nx - 1) ? 0.0 : -a.rho[k] * dx2 * K;
+    x[k - lo] = 0;
+  }
+  cl.sync();
+  const int maxit = n < 10000 ? n : 10000;
+  long long total = 0;
+  for (int it = 0; it < 10; it++) {
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+      const int q = k - lo;
+      const double xk = x[q];
+      rhovec[q] = rhovec[q] + exp(xk) * K;
+      const double F = nr_row_dsm(nx, ny, k, -4.0, s_xb, per, lo, hi, x) - rhovec[q];
+      J[q] = -4 - exp(xk);
+      y[q] = 0;
+      r[q] = F - 0.0;
+    }
+    // p = r: the other CTAs last read p before the barrier of the previous
+    // step's last sum
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) p[k - lo] = r[k - lo];
+    double r02 = nrc_sum(cl, lo, hi, [&](int k) { return r[k - lo] * r[k - lo]; }, s_slots + parity);
+    parity ^= 1;  // the barrier above: p visible, x reads done
+    for (int i = 0; i < maxit; i++) {
+      if (sqrt(r02) < 1e-4) break;
+      for (int k = lo + threadIdx.x; k < hi; k += blockDim.x)
+        Ap[k - lo] = nr_row_dsm(nx, ny, k, J[k - lo], s_pb, per, lo, hi, p);
+      const double pAp = nrc_sum(cl, lo, hi, [&](int k) { return p[k - lo] * Ap[k - lo]; }, s_slots + parity);
+      parity ^= 1;  // the barrier above: every CTA's reads of p done
+      const double alpha = r02 / pAp;
+      for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) {
+        const int q = k - lo;
+        y[q] = y[q] + p[q] * alpha;
+        r[q] = r[q] - Ap[q] * alpha;
+      }
+      const double r12 = nrc_sum(cl, lo, hi, [&](int k) { return r[k - lo] * r[k - lo]; }, s_slots + parity);
+      parity ^= 1;
+      const double beta = r12 / r02;
+      for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) p[k - lo] = r[k - lo] + p[k - lo] * beta;
+      cl.sync();  // p of every CTA visible to the next product
+      r02 = r12;
+      total++;
+    }
+    for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) x[k - lo] = x[k - lo] - y[k - lo];
+    cl.sync();  // x of every CTA visible to the next Newton step
+  }
+  for (int k = lo + threadIdx.x; k < hi; k += blockDim.x) a.phi[k] = x[k - lo];
+  if (me == 0 && threadIdx.x == 0) {
+    a.info->iterations = (int)total;
+    a.info->converged = 1;
+    a.info->error = 0;  // domain.error = 0 (src/field.cpp:205)
+    atomicAdd(a.iter_total, (unsigned long long)total);
+  }
+  cl.sync();  // no CTA leaves while another may still read its arrays
+}
+
+// Cluster of about n / 40 CTAs (2 to 16) when its arrays fit the CTAs'
+// shared memory and the device can co-schedule it; one CTA otherwise.
 void launch_nrpcg(cudaStream_t st, const SolverArgs& a) {
-  const size_t bytes = (size_t)a.g.nx * a.g.ny * sizeof(double);
-  const int smem = bytes <= (size_t)NRPCG_SMEM_MAX ? (int)bytes : 0;
-  if (smem > 48 * 1024) cudaFuncSetAttribute(k_nrpcg, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  k_nrpcg<<<1, 1024, smem, st>>>(a);
+  const int n = a.g.nx * a.g.ny;
+  int C = std::min(SORC_MAX, n / 40);
+  const int per = C >= 2 ? (n + C - 1) / C : 0;
+  const size_t smem = (size_t)NRC_ARRAYS * per * sizeof(double);
+  if (C >= 2 && smem <= SOR_SMEM_MAX) {
+    C = (n + per - 1) / per;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(NRC_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    if (cluster_fits((const void*)k_nrpcg_cluster, C, NRC_THREADS, smem) &&
+        cudaLaunchKernelEx(&cfg, k_nrpcg_cluster, a, per) == cudaSuccess)
+      return;
+    cudaGetLastError();
+  }
+  k_nrpcg<<<1, 1024, 0, st>>>(a);
 }
 
 // ------------------------------------------------------ grid barrier ---
