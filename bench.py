@@ -540,6 +540,7 @@ def run_batching(E, workloads):
     e1.synchronize()
     ms = e0.elapsed_time(e1)
     tiles = b.tuning()
+    shapes = b.particle_tuning()
     b.close()
     rate = n * BATCH_STEPS / (ms / 1e3)
     # the same runs one at a time (mixed form, graph replay)
@@ -568,6 +569,7 @@ def run_batching(E, workloads):
                         "MCC on %d, periodic) as one batch, mixed form" % sum(q["collisions"] for q in reqs),
             "runs": len(reqs), "particles": n, "steps": BATCH_STEPS, "ms_per_step": ms / BATCH_STEPS,
             "particle_steps_per_s": rate, "setup_s": setup_s, "gemm_tiles_by_size_class": tiles,
+            "particle_launch_shapes": shapes,
             "one_at_a_time_particle_steps_per_s": single,
             "one_at_a_time_sample": "%d of the runs, each alone (mixed form, graph replay)" % len(sample),
             "speedup_vs_one_at_a_time": rate / single}

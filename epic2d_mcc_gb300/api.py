@@ -176,6 +176,7 @@ def lib() -> ctypes.CDLL:
         "epic_batch_get_grid": ([vp, i, i, vp], st),
         "epic_batch_num_particles": ([vp, ctypes.POINTER(ctypes.c_int64)], st),
         "epic_batch_tuning": ([vp, vp], st),
+        "epic_batch_particle_tuning": ([vp, vp, vp, vp], st),
         "epic_batch_stream": ([vp], vp),
         "epic_batch_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
     }
@@ -607,6 +608,19 @@ class Batch:
         t = np.zeros(4, dtype=np.int32)
         _check(lib().epic_batch_tuning(self._h, _ptr(t)))
         return [int(x) for x in t]
+
+    def particle_tuning(self):
+        """The autotuner's launch shapes of the fused push and the deposit pass, with the timings behind them."""
+        sh = np.zeros(4, dtype=np.int32)
+        pm = np.zeros(5, dtype=np.float32)
+        dm = np.zeros(6, dtype=np.float32)
+        _check(lib().epic_batch_particle_tuning(self._h, _ptr(sh), _ptr(pm), _ptr(dm)))
+        return {"push_threads": int(sh[0]), "push_blocks": int(sh[1]), "deposit_threads": int(sh[2]),
+                "deposit_blocks": int(sh[3]),
+                "push_ms_by_shape": dict(zip(["128 resident", "256 resident", "256 x 1/SM", "256 x 2/SM",
+                                              "128 x 3/SM"], [round(float(x), 4) for x in pm])),
+                "deposit_ms_by_shape": dict(zip(["128 resident", "256 resident", "256 x 4/SM", "256 x 8/SM",
+                                                 "256 x 16/SM", "128 x 8/SM"], [round(float(x), 4) for x in dm]))}
 
     @property
     def stream(self) -> int:

@@ -180,8 +180,10 @@ struct RunNy {
   __device__ __forceinline__ int operator()(int cg) const { return runs[__ldg(&node_run[cg])].ny; }
 };
 
-template <bool SEL>
-__global__ void __launch_bounds__(PART_THREADS, 3) k_batch_push_dep(const BRun* __restrict__ runs,
+// T threads per CTA (128 or 256; the autotuner picks the shape), each taking
+// DEP_PER_THREAD consecutive particles per round.
+template <bool SEL, int T>
+__global__ void __launch_bounds__(T, 768 / T) k_batch_push_dep(const BRun* __restrict__ runs,
                                                                     const int* __restrict__ node_run, MixedSoA p,
                                                                     const long long* __restrict__ d_n,
                                                                     const float2* __restrict__ ef32, int s,
@@ -189,14 +191,15 @@ __global__ void __launch_bounds__(PART_THREADS, 3) k_batch_push_dep(const BRun* 
                                                                     const unsigned long long* __restrict__ d_step,
                                                                     McEvents ev) {
   constexpr int P = DEP_PER_THREAD;
-  __shared__ DepWarp tables[PART_THREADS / 32];
+  constexpr int CHUNK = T * P;
+  __shared__ DepWarp tables[T / 32];
   DepWarp& w = tables[threadIdx.x >> 5];
   const long long n = *d_n;
   const unsigned long long step = SEL ? *d_step : 0ull;
   const int lane = threadIdx.x & 31;
   const RunNy ny_of{runs, node_run};
   dep_init(w);
-  for (long long chunk = (long long)blockIdx.x * DEP_CHUNK; chunk < n; chunk += (long long)gridDim.x * DEP_CHUNK) {
+  for (long long chunk = (long long)blockIdx.x * CHUNK; chunk < n; chunk += (long long)gridDim.x * CHUNK) {
     const long long q0 = chunk + (long long)threadIdx.x * P;
     const bool full = q0 + P <= n;
     int c[P];
@@ -382,16 +385,17 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_deposit_range(const BRun
 // Integer CIC deposit of a species (the mixed form's weights, exact, so the
 // grid is the single runs' bit for bit): deposit_warp_sorted over chunks of
 // consecutive particles, each cell with its run's row stride.
-__global__ void __launch_bounds__(PART_THREADS) k_batch_deposit(const BRun* __restrict__ runs,
-                                                                const int* __restrict__ node_run, MixedSoA p,
-                                                                const long long* __restrict__ d_n,
-                                                                unsigned long long* __restrict__ acc) {
-  __shared__ DepWarp tables[PART_THREADS / 32];
+template <int T>
+__global__ void __launch_bounds__(T) k_batch_deposit(const BRun* __restrict__ runs, const int* __restrict__ node_run,
+                                                     MixedSoA p, const long long* __restrict__ d_n,
+                                                     unsigned long long* __restrict__ acc) {
+  constexpr int CHUNK = T * DEP_PER_THREAD;
+  __shared__ DepWarp tables[T / 32];
   DepWarp& w = tables[threadIdx.x >> 5];
   const long long n = *d_n;
   const RunNy ny_of{runs, node_run};
   dep_init(w);
-  for (long long chunk = (long long)blockIdx.x * DEP_CHUNK; chunk < n; chunk += (long long)gridDim.x * DEP_CHUNK) {
+  for (long long chunk = (long long)blockIdx.x * CHUNK; chunk < n; chunk += (long long)gridDim.x * CHUNK) {
     const long long q0 = chunk + (long long)threadIdx.x * DEP_PER_THREAD;
     int c[DEP_PER_THREAD];
     float ox[DEP_PER_THREAD], oy[DEP_PER_THREAD];
@@ -544,6 +548,11 @@ struct epic_batch {
   int4* tile_sched[2] = {nullptr, nullptr};  // TILE 16, 32
   int ntile[2] = {0, 0};
   int tiles[4] = {32, 32, 32, 32};
+  // Launch shapes of the particle passes (the autotuner's choice): threads
+  // per CTA and CTAs of the fused push and of the deposit pass.
+  int push_threads = PART_THREADS, push_blocks = 0, dep_threads = PART_THREADS, dep_blocks = 0;
+  float push_ms[5] = {0, 0, 0, 0, 0}, dep_ms[6] = {0, 0, 0, 0, 0, 0};
+  bool particles_tuned = false;
   void* sort_buf = nullptr;
   double* staging = nullptr;
   int64_t step_index = 0;
@@ -636,9 +645,23 @@ struct epic_batch {
   void deposit_all() {
     for (int s = 0; s < nsp; s++) {
       cudaMemsetAsync(acc[s], 0, nodes * sizeof(unsigned long long), stream);
-      k_batch_deposit<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], acc[s]);
+      launch_deposit(arena[s], d_n[s], acc[s], dep_threads, dep_blocks ? dep_blocks : grid);
     }
     acc_valid = true;
+  }
+
+  void launch_deposit(const MixedSoA& a, const long long* dn, unsigned long long* out, int T, int blocks) {
+    if (T == 128) k_batch_deposit<128><<<blocks, 128, 0, stream>>>(d_runs, d_node_run, a, dn, out);
+    else k_batch_deposit<256><<<blocks, 256, 0, stream>>>(d_runs, d_node_run, a, dn, out);
+  }
+
+  template <bool SEL>
+  void launch_push(const MixedSoA& a, const long long* dn, const float2* ef, int s, unsigned long long* out, int T,
+                   int blocks) {
+    if (T == 128)
+      k_batch_push_dep<SEL, 128><<<blocks, 128, 0, stream>>>(d_runs, d_node_run, a, dn, ef, s, out, d_step, ev);
+    else
+      k_batch_push_dep<SEL, 256><<<blocks, 256, 0, stream>>>(d_runs, d_node_run, a, dn, ef, s, out, d_step, ev);
   }
 
   void deposit_and_solve() {
@@ -683,15 +706,11 @@ struct epic_batch {
       return;
     }
     deposit_and_solve();
-    const int grid_dep = resident_grid(k_batch_push_dep<true>, PART_THREADS);
+    const int grid_dep = push_blocks ? push_blocks : resident_grid(k_batch_push_dep<true, PART_THREADS>, PART_THREADS);
     for (int s = 0; s < nsp; s++) {
       cudaMemsetAsync(acc[s], 0, nodes * sizeof(unsigned long long), stream);
-      if (any_mcc && s == 0)
-        k_batch_push_dep<true><<<grid_dep, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s,
-                                                                      acc[s], d_step, ev);
-      else
-        k_batch_push_dep<false><<<grid_dep, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s,
-                                                                       acc[s], d_step, ev);
+      if (any_mcc && s == 0) launch_push<true>(arena[s], d_n[s], ef32, s, acc[s], push_threads, grid_dep);
+      else launch_push<false>(arena[s], d_n[s], ef32, s, acc[s], push_threads, grid_dep);
     }
     if (any_mcc) {
       for (int k = 0; k < 2; k++)
@@ -798,6 +817,96 @@ epic_status autotune(epic_batch* b) {
   cudaEventDestroy(e1);
   BCK(cudaGetLastError());
   return upload_tile_sched(b);
+}
+
+// Launch shapes of the particle passes, timed on a sample: a copy of the
+// first 2^24 particles of species 0 pushed through a zero field and deposited
+// into a scratch accumulator (the batch's own particles, runs and node table;
+// the copy is discarded), one warm-up and three timed launches per shape.  The
+// shapes change neither the push nor the integer deposit, so results do not
+// depend on the choice.  Runs after the particles are loaded.
+epic_status tune_particle_passes(epic_batch* b) {
+  const long long n0 = b->pn.empty() ? 0 : [&] {
+    long long t = 0;
+    for (int r = 0; r < b->nruns; r++) t += b->pn[(size_t)r * b->nsp];
+    return t;
+  }();
+  const long long ns = std::min<long long>(n0, 1ll << 24);
+  if (ns < 1) return EPIC_OK;
+  const int sms = b->num_sms;
+  MixedSoA sm;
+  std::memset(&sm, 0, sizeof(sm));
+  long long* dns = nullptr;
+  unsigned long long* sacc = nullptr;
+  float2* zef = nullptr;
+  BCK(cudaMallocAsync((void**)&sm.cell, ns * sizeof(int), b->stream));
+  BCK(cudaMallocAsync((void**)&sm.ox, ns * sizeof(float), b->stream));
+  BCK(cudaMallocAsync((void**)&sm.oy, ns * sizeof(float), b->stream));
+  BCK(cudaMallocAsync((void**)&sm.vx, ns * sizeof(float), b->stream));
+  BCK(cudaMallocAsync((void**)&sm.vy, ns * sizeof(float), b->stream));
+  BCK(cudaMallocAsync((void**)&sm.vz, ns * sizeof(float), b->stream));
+  BCK(cudaMallocAsync((void**)&dns, sizeof(long long), b->stream));
+  BCK(cudaMallocAsync((void**)&sacc, b->nodes * sizeof(unsigned long long), b->stream));
+  BCK(cudaMallocAsync((void**)&zef, b->nodes * sizeof(float2), b->stream));
+  const MixedSoA& a = b->arena[0];
+  BCK(cudaMemcpyAsync(sm.cell, a.cell, ns * sizeof(int), cudaMemcpyDeviceToDevice, b->stream));
+  BCK(cudaMemcpyAsync(sm.ox, a.ox, ns * sizeof(float), cudaMemcpyDeviceToDevice, b->stream));
+  BCK(cudaMemcpyAsync(sm.oy, a.oy, ns * sizeof(float), cudaMemcpyDeviceToDevice, b->stream));
+  BCK(cudaMemcpyAsync(sm.vx, a.vx, ns * sizeof(float), cudaMemcpyDeviceToDevice, b->stream));
+  BCK(cudaMemcpyAsync(sm.vy, a.vy, ns * sizeof(float), cudaMemcpyDeviceToDevice, b->stream));
+  BCK(cudaMemcpyAsync(sm.vz, a.vz, ns * sizeof(float), cudaMemcpyDeviceToDevice, b->stream));
+  BCK(cudaMemcpyAsync(dns, &ns, sizeof(long long), cudaMemcpyHostToDevice, b->stream));
+  BCK(cudaMemsetAsync(zef, 0, b->nodes * sizeof(float2), b->stream));
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  auto time_it = [&](auto&& launch) -> float {
+    float tot = 0;
+    for (int rep = 0; rep < 4; rep++) {
+      cudaMemsetAsync(sacc, 0, b->nodes * sizeof(unsigned long long), b->stream);
+      cudaEventRecord(e0, b->stream);
+      launch();
+      cudaEventRecord(e1, b->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (rep) tot += ms;  // the first launch warms up
+    }
+    return tot / 3;
+  };
+  // push: 128 and 256 threads with every CTA resident, 256 with 1 and 2 CTAs
+  // per SM, 128 with 3
+  const int pT[5] = {128, 256, 256, 256, 128};
+  const int pB[5] = {resident_grid(k_batch_push_dep<false, 128>, 128),
+                     resident_grid(k_batch_push_dep<false, 256>, 256), sms, 2 * sms, 3 * sms};
+  int best = -1;
+  if (!b->has_open) {
+    for (int v = 0; v < 5; v++) {
+      b->push_ms[v] = time_it([&] { b->launch_push<false>(sm, dns, zef, 0, sacc, pT[v], pB[v]); });
+      if (best < 0 || b->push_ms[v] < b->push_ms[best]) best = v;
+    }
+    b->push_threads = pT[best];
+    b->push_blocks = pB[best];
+  }
+  // deposit: 128 and 256 threads at full occupancy, 256 with 4, 8 and 16
+  // CTAs per SM, 128 with 8
+  const int dT[6] = {128, 256, 256, 256, 256, 128};
+  const int dB[6] = {resident_grid(k_batch_deposit<128>, 128), resident_grid(k_batch_deposit<256>, 256), 4 * sms,
+                     8 * sms, 16 * sms, 8 * sms};
+  best = -1;
+  for (int v = 0; v < 6; v++) {
+    b->dep_ms[v] = time_it([&] { b->launch_deposit(sm, dns, sacc, dT[v], dB[v]); });
+    if (best < 0 || b->dep_ms[v] < b->dep_ms[best]) best = v;
+  }
+  b->dep_threads = dT[best];
+  b->dep_blocks = dB[best];
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  void* bufs[9] = {sm.cell, sm.ox, sm.oy, sm.vx, sm.vy, sm.vz, dns, sacc, zef};
+  for (void* q : bufs) cudaFreeAsync(q, b->stream);
+  BCK(cudaStreamSynchronize(b->stream));
+  BCK(cudaGetLastError());
+  return EPIC_OK;
 }
 
 // Transforms of side n (orthonormal DST-I) and eigenvalues, as the single run.
@@ -1089,6 +1198,12 @@ epic_status epic_batch_initial_field(epic_batch* b) {
     for (int r = 0; r < b->nruns; r++) total += b->pn[(size_t)r * b->nsp + s];
     launch_set_count(b->stream, b->d_n[s], total);
   }
+  epic_status tst = take_flags(b);
+  if (tst) return tst;
+  if (!b->particles_tuned) {
+    if ((tst = tune_particle_passes(b))) return tst;
+    b->particles_tuned = true;
+  }
   b->deposit_and_solve();
   for (int s = 0; s < b->nsp; s++)
     k_batch_rewind<<<b->grid, PART_THREADS, 0, b->stream>>>(b->d_runs, b->d_node_run, b->arena[s], b->d_n[s],
@@ -1257,6 +1372,17 @@ epic_status epic_batch_set_log_cross_sections(epic_batch* b, const double* ela, 
 epic_status epic_batch_tuning(epic_batch* b, int tiles[4]) {
   if (!b || !tiles) return bfail(EPIC_ERR_INVALID, "bad argument");
   std::memcpy(tiles, b->tiles, sizeof(b->tiles));
+  return EPIC_OK;
+}
+
+epic_status epic_batch_particle_tuning(epic_batch* b, int shapes[4], float push_ms[5], float deposit_ms[6]) {
+  if (!b || !shapes) return bfail(EPIC_ERR_INVALID, "bad argument");
+  shapes[0] = b->push_threads;
+  shapes[1] = b->push_blocks;
+  shapes[2] = b->dep_threads;
+  shapes[3] = b->dep_blocks;
+  if (push_ms) std::memcpy(push_ms, b->push_ms, sizeof(b->push_ms));
+  if (deposit_ms) std::memcpy(deposit_ms, b->dep_ms, sizeof(b->dep_ms));
   return EPIC_OK;
 }
 

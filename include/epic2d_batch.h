@@ -63,6 +63,15 @@ epic_status epic_batch_set_log_cross_sections(epic_batch* b, const double* ela, 
 /* The autotuner's choices: GEMM tile per size class (max(R, C) <= 48, <= 96,
  * <= 160, larger). */
 epic_status epic_batch_tuning(epic_batch* b, int tiles[4]);
+/* The autotuner's launch shapes of the particle passes, chosen when the
+ * particles are loaded (epic_batch_initial_field) by timing a sample of them:
+ * shapes = {push threads per CTA, push CTAs, deposit threads per CTA, deposit
+ * CTAs}; push_ms (5) and deposit_ms (6), when not NULL, receive the sample's
+ * time per launch of each shape tried (push: 128 and 256 threads with every
+ * CTA resident, 256 with 1 and 2 CTAs per SM, 128 with 3; deposit: 128 and
+ * 256 at full occupancy, 256 with 4, 8 and 16 CTAs per SM, 128 with 8).  No
+ * shape changes results. */
+epic_status epic_batch_particle_tuning(epic_batch* b, int shapes[4], float push_ms[5], float deposit_ms[6]);
 void* epic_batch_stream(epic_batch* b);
 
 #ifdef __cplusplus

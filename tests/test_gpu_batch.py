@@ -2,7 +2,8 @@
 particles and potential, bit for bit, as the same run alone in the mixed form
 (same configuration, sort period and device-loader seed) — on square and
 non-square grids, periodic and reflective walls, pcgsolver and gssolver, with
-the step replayed from a graph or launched directly."""
+the step replayed from a graph or launched directly, whatever launch shapes
+the autotuner chose for the GEMM tiles and the particle passes."""
 import numpy as np
 import pytest
 
@@ -32,6 +33,12 @@ def test_batch_runs_equal_single_runs(gpu_lib, tmp_path, graph):
     b = A.Batch([r for _, r in reqs], sort_every=sort_every)
     assert all(t in (16, 32) for t in b.tuning())
     b.initial_field()
+    # the particle passes' launch shapes were timed on a sample and one kept
+    sh = b.particle_tuning()
+    assert sh["push_threads"] in (128, 256) and sh["deposit_threads"] in (128, 256)
+    assert sh["push_blocks"] > 0 and sh["deposit_blocks"] > 0
+    assert all(v > 0 for v in sh["push_ms_by_shape"].values())
+    assert all(v > 0 for v in sh["deposit_ms_by_shape"].values())
     b.run(steps, graph=graph)
     for k, (ini, r) in enumerate(reqs):
         sim = A.Simulation.from_ini(ini, precision=1, sort_every=sort_every)
