@@ -433,7 +433,7 @@ __device__ double cluster_exact_sum(const cgx::cluster_group& cl, int count, con
 
 // with_rk: rho K of the band kept in shared memory after phi (not FLUID).
 template <bool FLUID, bool UNIT, bool EXT>
-__global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int R, int with_rk) {
+__global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int R, int with_rk, int K) {
   extern __shared__ double smem[];
   __shared__ double red[40];
   __shared__ double* s_row0[SORC_MAX];  // phi of each CTA's band (distributed shared memory)
@@ -444,12 +444,15 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
   const SorLat l = sor_lattice(nx, ny, EXT ? a.poisson_bc : EPIC_POISSON_DIRICHLET);
   const int r_lo = me * R, r_hi = min(nx, r_lo + R);
   const int nloc = max(r_hi - r_lo, 0) * ny;
+  const size_t band = (size_t)R * ny;
   double* const phi = smem;  // rows [r_lo, r_hi)
-  double* const rK = with_rk ? smem + (size_t)R * ny : nullptr;
+  double* const rK = with_rk ? smem + band : nullptr;
+  double* const snaps = smem + band * (with_rk ? 2 : 1);  // K snapshot bands (undrained pipeline)
   if (threadIdx.x < C) s_row0[threadIdx.x] = threadIdx.x == me ? phi : cl.map_shared_rank(phi, (int)threadIdx.x);
   for (int q = threadIdx.x; q < nloc; q += blockDim.x) {
     phi[q] = 0;  // cold start, zero edges (src/field.cpp:78-98)
     if (rK) rK[q] = a.rho[(size_t)r_lo * ny + q] * a.K;
+    for (int k = 0; k < K; k++) snaps[k * band + q] = 0;
   }
   // this CTA's unknowns: lattice rows ai in [u_lo, u_hi)
   const int u_lo = max(r_lo, l.i0) - l.i0, u_hi = min(r_hi, l.i0 + l.nxi) - l.i0;
@@ -472,8 +475,9 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
                 },
                 &s_xs, red) /
             (double)(l.nxi * l.nyi);
-  auto src = [&](int i, int j, int kl) -> double {
-    if (FLUID) return (a.rho[(size_t)i * ny + j] - exp(phi[kl])) * a.K;
+  // the source at node (i, j) whose potential is v
+  auto src = [&](int i, int j, int kl, double v) -> double {
+    if (FLUID) return (a.rho[(size_t)i * ny + j] - exp(v)) * a.K;
     return (rK ? rK[kl] : a.rho[(size_t)i * ny + j] * a.K) - smean;
   };
   // neighbours of unknown (i, j): rows iE, iW and columns jN, jS (sor_nbrs)
@@ -489,7 +493,14 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
   const double dx2 = a.g.dx * a.g.dx, dy2 = a.g.dy * a.g.dy;
   const double coeff = (2 / dx2) + (2 / dy2);
   const double inv_coeff = 1 / coeff;
-  auto residual = [&]() -> double {
+  // L2 residual (src/field.cpp:121-134) of the band array buf (phi or a
+  // snapshot; the other CTAs' bands at the same offset of their shared memory)
+  auto residual = [&](double* buf) -> double {
+    auto brow = [&](int i) -> const double* {
+      if (i >= r_lo && i < r_hi) return buf + (size_t)(i - r_lo) * ny;
+      const int o = i / R;
+      return cl.map_shared_rank(buf, o) + (size_t)(i - o * R) * ny;
+    };
     const double sum = cluster_exact_sum(
         cl, nu,
         [&](int q) {
@@ -497,13 +508,13 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
           const int kl = (i - r_lo) * ny + j;
           int iE, iW, jN, jS;
           nbrs(i, j, iE, iW, jN, jS);
-          double tx = row_of(iE)[j] - 2 * phi[kl] + row_of(iW)[j];
-          double ty = phi[kl - j + jN] - 2 * phi[kl] + phi[kl - j + jS];
+          double tx = brow(iE)[j] - 2 * buf[kl] + brow(iW)[j];
+          double ty = buf[kl - j + jN] - 2 * buf[kl] + buf[kl - j + jS];
           if (!UNIT) {
             tx = tx / dx2;
             ty = ty / dy2;
           }
-          const double Rv = (tx + ty) + src(i, j, kl);
+          const double Rv = (tx + ty) + src(i, j, kl, buf[kl]);
           return Rv * Rv;
         },
         &s_xs, red);
@@ -516,11 +527,71 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
     if (l.wrap_x && nxi > cp) cp = nxi;
     if (l.wrap_y && nyi > cp) cp = nyi;
   }
+  constexpr int P = FLUID ? 50 : 25;  // residual after sweeps 0, P, 2P, ... (src/field.cpp:118)
+  // sweep g's update of the node at lattice row ai on diagonal d (snap: also
+  // store the new value there)
+  auto update = [&](int d, int ai, double* snap) {
+    const int i = ai + l.i0, j = d - ai + l.j0;
+    const int kl = (i - r_lo) * ny + j;
+    int iE, iW, jN, jS;
+    nbrs(i, j, iE, iW, jN, jS);
+    double tx = row_of(iE)[j] + row_of(iW)[j], ty = phi[kl - j + jN] + phi[kl - j + jS];
+    if (!UNIT) {
+      tx = tx / dx2;
+      ty = ty / dy2;
+    }
+    const double sk = src(i, j, kl, phi[kl]);
+    double phi_new = inv_coeff * ((sk + tx) + ty);
+    const double v = phi[kl] + a.omega * (phi_new - phi[kl]);
+    phi[kl] = v;
+    if (snap) snap[kl] = v;
+  };
   int iter = 0, converged = 0;
   double L2 = 0;
-  if (nxi > 0 && nyi > 0) {
+  double* out = phi;
+  if (nxi > 0 && nyi > 0 && K > 0) {
+    // Undrained: one wavefront over all sweeps g < max_iter (sweep g on
+    // diagonal d at step d + cp g).  The sweeps the reference checks write
+    // their values into snapshot (g / P) % K as well; a checked sweep's
+    // residual is taken from its snapshot at the step after its last
+    // diagonal, and if it converged the snapshot is the result.  A snapshot
+    // is rewritten cp K P >= D steps after its sweep started, i.e. after it
+    // was checked.
+    const long long G = a.max_iter;
+    const long long t_end = (long long)D - 1 + (long long)cp * (G - 1);
+    long long chk = 0;  // next checked sweep
+    for (long long t = 0; t <= t_end + 1; t++) {
+      if (chk < G && t == (long long)D + cp * chk) {
+        double* sn = snaps + (size_t)((chk / P) % K) * band;
+        L2 = residual(sn);
+        iter = (int)(chk + 1);
+        if (L2 < a.tol) {
+          converged = 1;
+          out = sn;
+          break;
+        }
+        chk += P;
+      }
+      if (t > t_end) break;
+      const long long g_lo = t - D + 1 > 0 ? (t - D + cp) / cp : 0;
+      const long long g_hi = t / cp < G - 1 ? t / cp : G - 1;
+      const int items = (int)(g_hi - g_lo + 1) * Ru;
+      for (int it = threadIdx.x; it < items; it += blockDim.x) {
+        const long long g = g_lo + it / Ru;
+        const int ai = u_lo + it % Ru;
+        const int d = (int)(t - cp * g);
+        const int a0 = d - (nyi - 1) > 0 ? d - (nyi - 1) : 0;
+        const int a1 = d < nxi - 1 ? d : nxi - 1;
+        if (ai < a0 || ai > a1) continue;
+        update(d, ai, g % P == 0 ? snaps + (size_t)((g / P) % K) * band : nullptr);
+      }
+      cl.sync();
+    }
+    if (!converged) iter = (int)G;
+  } else if (nxi > 0 && nyi > 0) {
+    // Drained: chunks of sweeps up to the next check, each chunk's wavefront
+    // emptied before its residual
     while (iter < a.max_iter) {
-      constexpr int P = FLUID ? 50 : 25;
       int S = iter == 0 ? 1 : P;
       if (S > a.max_iter - iter) S = a.max_iter - iter;
       const int T = D + cp * (S - 1);
@@ -534,25 +605,14 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
           const int a0 = d - (nyi - 1) > 0 ? d - (nyi - 1) : 0;
           const int a1 = d < nxi - 1 ? d : nxi - 1;
           if (ai < a0 || ai > a1) continue;
-          const int i = ai + l.i0, j = d - ai + l.j0;
-          const int kl = (i - r_lo) * ny + j;
-          int iE, iW, jN, jS;
-          nbrs(i, j, iE, iW, jN, jS);
-          double tx = row_of(iE)[j] + row_of(iW)[j], ty = phi[kl - j + jN] + phi[kl - j + jS];
-          if (!UNIT) {
-            tx = tx / dx2;
-            ty = ty / dy2;
-          }
-          const double sk = src(i, j, kl);
-          double phi_new = inv_coeff * ((sk + tx) + ty);
-          phi[kl] = phi[kl] + a.omega * (phi_new - phi[kl]);
+          update(d, ai, nullptr);
         }
         cl.sync();
       }
       const int last = iter + S - 1;
       iter += S;
       if (last % P == 0) {
-        L2 = residual();
+        L2 = residual(phi);
         if (L2 < a.tol) {
           converged = 1;
           break;
@@ -562,14 +622,14 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
   }
   if (EXT && l.wrap_x) {  // zero-mean gauge over the unknowns
     const double m =
-        cluster_exact_sum(cl, nu, [&](int q) { return phi[unknown_local(q)]; }, &s_xs, red) / (double)(nxi * nyi);
+        cluster_exact_sum(cl, nu, [&](int q) { return out[unknown_local(q)]; }, &s_xs, red) / (double)(nxi * nyi);
     for (int q = threadIdx.x; q < nu; q += blockDim.x) {
       const int kl = unknown_local(q);
-      phi[kl] = phi[kl] - m;
+      out[kl] = out[kl] - m;
     }
   }
   __syncthreads();
-  for (int q = threadIdx.x; q < nloc; q += blockDim.x) a.phi[(size_t)r_lo * ny + q] = phi[q];
+  for (int q = threadIdx.x; q < nloc; q += blockDim.x) a.phi[(size_t)r_lo * ny + q] = out[q];
   if (me == 0 && threadIdx.x == 0) {
     a.info->iterations = iter;
     a.info->converged = converged;
@@ -612,13 +672,13 @@ static bool cluster_fits(const void* kern, int C, int threads, size_t smem) {
 // too small, too large for the cluster's shared memory, or the device cannot
 // co-schedule the cluster (k_sor_lex then runs it on one CTA).
 struct SorCluster {
-  int C, R, with_rk;
+  int C, R, with_rk, K;
   size_t smem;
 };
 
 template <bool FLUID, bool UNIT, bool EXT>
 static SorCluster sor_cluster_shape(const SolverArgs& a) {
-  SorCluster c{0, 0, 0, 0};
+  SorCluster c{0, 0, 0, 0, 0};
   const int nx = a.g.nx, ny = a.g.ny;
   int C = std::min(SORC_MAX, nx / 4);
   if (C < 2 || ny < 3) return c;
@@ -626,12 +686,34 @@ static SorCluster sor_cluster_shape(const SolverArgs& a) {
   C = (nx + R - 1) / R;  // no CTA without rows
   const size_t band = (size_t)R * ny * sizeof(double);
   if (band > SOR_SMEM_MAX) return c;
-  const int with_rk = !FLUID && 2 * band <= SOR_SMEM_MAX;
-  const size_t smem = band * (with_rk ? 2 : 1);
+  // the lattice's wavefront (sor_lattice): D diagonals, sweeps cp apart
+  const int pbc = EXT ? a.poisson_bc : EPIC_POISSON_DIRICHLET;
+  const bool ext = pbc != EPIC_POISSON_DIRICHLET, wrap_x = pbc == EPIC_POISSON_PERIODIC;
+  const int nxi = ext ? nx - 1 - (wrap_x ? 0 : 1) : nx - 2, nyi = ext ? ny - 1 : ny - 2;
+  const int D = nxi + nyi - 1;
+  int cp = 2;
+  if (ext) {
+    if (wrap_x && nxi > cp) cp = nxi;
+    if (nyi > cp) cp = nyi;
+  }
+  const int P = FLUID ? 50 : 25;
+  // snapshots for the undrained pipeline: a checked sweep's snapshot must
+  // outlive the D steps until its check, cp K P >= D
+  const int K = std::max(1, (D + cp * P - 1) / (cp * P));
+  int with_rk = !FLUID && 2 * band <= SOR_SMEM_MAX;
+  int k = 0;
+  if (band * (1 + with_rk + K) <= SOR_SMEM_MAX) {
+    k = K;
+  } else if (band * (1 + K) <= SOR_SMEM_MAX) {
+    k = K;
+    with_rk = 0;
+  }
+  const size_t smem = band * (1 + with_rk + k);
   if (!cluster_fits((const void*)k_sor_cluster<FLUID, UNIT, EXT>, C, SORC_THREADS, smem)) return c;
   c.C = C;
   c.R = R;
   c.with_rk = with_rk;
+  c.K = k;
   c.smem = smem;
   return c;
 }
@@ -653,7 +735,7 @@ static bool launch_sor_cluster(cudaStream_t st, const SolverArgs& a) {
   cfg.stream = st;
   cfg.attrs = attr;
   cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, k_sor_cluster<FLUID, UNIT, EXT>, a, c.R, c.with_rk) == cudaSuccess;
+  return cudaLaunchKernelEx(&cfg, k_sor_cluster<FLUID, UNIT, EXT>, a, c.R, c.with_rk, c.K) == cudaSuccess;
 }
 
 void init_field_kernels() {
