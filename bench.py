@@ -709,6 +709,79 @@ def measure_rows(steps, warmup, cpu_seconds):
     return out
 
 
+def run_serving_unscaled(cutoff_s):
+    """The serving configuration as stated: Poisson arrivals at 50 runs/s for
+    60 s with the unscaled step counts (500-5000).  The arrivals offer about
+    100 times the particle-steps per second the GPU serves, so the queue grows
+    without bound; the server runs until cutoff_s after its start and is then
+    stopped.  Reported: what arrived, completed and was still queued or in
+    service at the cutoff; the latencies of the completed requests; and the
+    latencies of every request that had arrived, an unfinished one counted as
+    (cutoff - arrival), i.e. lower bounds."""
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import epic2d_mcc_gb300 as E
+    from epic2d_mcc_gb300 import build as B
+    from epic2d_mcc_gb300 import workloads
+
+    B.build()
+    A = E.api
+    reqs = workloads.serving_requests(seed=0, step_scale=1.0)
+    e, ela, exc, ion = workloads.synthetic_table()
+    d = tempfile.mkdtemp(prefix="epic_serve_full_")
+    srv = A.Server(SERVE_BUDGET, max_inflight=16, chunk_steps=16)
+    srv.set_log_cross_sections(ela, exc, ion, e[0], e[-1])
+    ids = []
+    for k, q in enumerate(reqs):
+        path = os.path.join(d, "req%03d.ini" % k)
+        with open(path, "w") as f:
+            f.write(q["ini"])
+        ids.append(srv.submit(A.make_request(path, q["steps"], q["collisions"], q["seed"], q["arrival_s"],
+                                             precision=1, sort_every=SORT_EVERY)))
+    torch.cuda.synchronize()
+    srv.start()
+    t0 = time.perf_counter()
+    try:
+        srv.wait(cutoff_s)
+    except E.EpicError:
+        pass  # the cutoff came first (the expected outcome at this load)
+    cutoff = time.perf_counter() - t0
+    done_lat, all_lat, work, failed = [], [], 0.0, 0
+    arrived = 0
+    for k, i in enumerate(ids):
+        q = reqs[k]
+        if q["arrival_s"] > cutoff:
+            continue
+        arrived += 1
+        r = A.Result()
+        ok = A.lib().epic_server_result(srv._h, i, ctypes.byref(r)) == 0
+        if ok and r.status == 0:
+            lat = r.finish_s - r.arrival_s
+            done_lat.append(lat)
+            all_lat.append(lat)
+            work += q["particles"] * q["steps"]
+        else:
+            failed += int(ok)
+            all_lat.append(cutoff - q["arrival_s"])
+    srv.close()
+    offered = sum(q["particles"] * q["steps"] for q in reqs) / 60.0
+    pct = lambda v, p: float(np.percentile(v, p)) if v else None
+    print(json.dumps({
+        "workload": "serving as configured: Poisson arrivals 50/s for 60 s, grids {64,128,256,512}^2, 25-100 ppc "
+                    "per species, steps 500-5000 (unscaled), MCC p=0.5, periodic or Dirichlet systems, mixed form",
+        "requests": len(reqs), "cutoff_s": cutoff, "arrived_by_cutoff": arrived, "completed": len(done_lat),
+        "failed": failed, "queued_or_in_service_at_cutoff": arrived - len(done_lat) - failed,
+        "completed_p50_latency_s": pct(done_lat, 50), "completed_p99_latency_s": pct(done_lat, 99),
+        "arrived_p50_latency_s_lower_bound": pct(all_lat, 50), "arrived_p99_latency_s_lower_bound": pct(all_lat, 99),
+        "offered_particle_steps_per_s": offered,
+        "completed_particle_steps_per_s_lower_bound": work / cutoff,
+        "note": "unfinished requests count as (cutoff - arrival); work of runs still in service is not counted"}),
+        flush=True)
+
+
 def run_rows(args):
     out = measure_rows(args.steps, args.warmup, args.cpu_seconds)
     print(json.dumps({"rows": out, "steps": args.steps, "warmup": args.warmup, "dtype": "f64",
@@ -734,9 +807,15 @@ def main():
     ap.add_argument("--no-rows", action="store_true", help="skip the extension-row measurements")
     ap.add_argument("--rows", action="store_true",
                     help="measure the loop's extensions (conductors, emitters, Boltzmann solvers) instead")
+    ap.add_argument("--serve-unscaled", type=float, default=0.0, metavar="SECONDS",
+                    help="run the serving configuration with unscaled step counts for SECONDS, then stop it "
+                         "and report the queue (instead of the default measurements)")
     args = ap.parse_args()
     if args.rows:
         run_rows(args)
+        return
+    if args.serve_unscaled > 0:
+        run_serving_unscaled(args.serve_unscaled)
         return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
