@@ -1012,7 +1012,7 @@ __global__ void __launch_bounds__(NRC_THREADS) k_nrpcg_cluster(SolverArgs a, int
     double r02 = nrc_sum(cl, lo, hi, [&](int k) { return r[k - lo] * r[k - lo]; }, s_slots + parity);
     parity ^= 1;  // the barrier above: p visible, x reads done
     for (int i = 0; i < maxit; i++) {
-      if (sqrt(r02) < 1e-4) break;
+      if (xs_bits(r02) < a.tol_bits) break;  // sqrt(r02) < 1e-4 (r02 >= 0: bit order is value order)
       for (int k = lo + threadIdx.x; k < hi; k += blockDim.x)
         Ap[k - lo] = nr_row_dsm(nx, ny, k, J[k - lo], s_pb, per, lo, hi, p);
       const double pAp = nrc_sum(cl, lo, hi, [&](int k) { return p[k - lo] * Ap[k - lo]; }, s_slots + parity);
@@ -1065,8 +1065,10 @@ void launch_nrpcg(cudaStream_t st, const SolverArgs& a) {
     cfg.stream = st;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
+    SolverArgs an = a;
+    an.tol_bits = xs_bits(xs_sqrt_threshold(1e-4));  // the cg's stop test, |r| < 1e-4
     if (cluster_fits((const void*)k_nrpcg_cluster, C, NRC_THREADS, smem) &&
-        cudaLaunchKernelEx(&cfg, k_nrpcg_cluster, a, per) == cudaSuccess)
+        cudaLaunchKernelEx(&cfg, k_nrpcg_cluster, an, per) == cudaSuccess)
       return;
     cudaGetLastError();
   }
