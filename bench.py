@@ -165,6 +165,48 @@ def cpu_port_run(ini, steps, warmup, budget_s=None):
     return n_acc / el, done, n_acc // done, "port"
 
 
+def _cpu_run_worker(job):
+    """One reference loop (oracle restatement, one thread) on one deck for
+    budget_s seconds after its load and initial field: (particle-steps, s)."""
+    ini, coll, budget_s = job
+    from epic2d_mcc_gb300 import workloads
+    from oracle import oracle as O
+
+    sim = O.OracleSim(ini)
+    if coll:
+        e, ela, exc, ion = workloads.synthetic_table()
+        sim.R.set_log_table(ela, exc, ion, e[0], e[-1])
+    n_acc, t0 = 0, time.perf_counter()
+    while True:
+        n_acc += sum(len(p) for p in sim.parts)
+        sim.step(collisions=coll)
+        if time.perf_counter() - t0 >= budget_s:
+            break
+    return n_acc, time.perf_counter() - t0
+
+
+def cpu_multi_run(jobs, budget_s):
+    """Many runs on the host cores at once, one reference loop per core (the
+    reference is serial, so concurrent runs are how a CPU serves many):
+    aggregate particle-steps/s of len(jobs) concurrent processes.  A spawned
+    pool (this process has already used the GPU)."""
+    import multiprocessing as mp
+
+    with mp.get_context("spawn").Pool(len(jobs)) as pool:
+        res = pool.map(_cpu_run_worker, [(ini, coll, budget_s) for ini, coll in jobs])
+    return sum(r[0] / r[1] for r in res)
+
+
+def cpu_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+CPU_MULTI_SECONDS = 8.0  # per process, after its load and initial field
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -565,6 +607,9 @@ def run_batching(E, workloads):
         pst += reqs[k]["particles"] * BATCH_STEPS
         sim.close()
     single = pst / (t_ms / 1e3)
+    procs = min(cpu_cores(), len(reqs), 16)
+    cpu_sample = list(range(0, len(reqs), max(1, len(reqs) // procs)))[:procs]
+    cpu_rate = cpu_multi_run([(paths[k], reqs[k]["collisions"]) for k in cpu_sample], CPU_MULTI_SECONDS)
     return {"workload": "batching: 512 runs (cells {32,...,256} per axis, 20-200 ppc per species, Te 0.5-5 eV, "
                         "MCC on %d, periodic) as one batch, mixed form" % sum(q["collisions"] for q in reqs),
             "runs": len(reqs), "particles": n, "steps": BATCH_STEPS, "ms_per_step": ms / BATCH_STEPS,
@@ -572,7 +617,11 @@ def run_batching(E, workloads):
             "particle_launch_shapes": shapes,
             "one_at_a_time_particle_steps_per_s": single,
             "one_at_a_time_sample": "%d of the runs, each alone (mixed form, graph replay)" % len(sample),
-            "speedup_vs_one_at_a_time": rate / single}
+            "speedup_vs_one_at_a_time": rate / single,
+            "cpu_baseline": {"value": cpu_rate, "unit": "particle-steps/s", "cores": procs, "kind": "port",
+                             "sample": "%d of the runs at once, one reference loop (oracle restatement) per host "
+                                       "core, %g s each after load and initial field" % (procs, CPU_MULTI_SECONDS)},
+            "speedup_vs_cpu_cores": rate / cpu_rate if cpu_rate else None}
 
 
 SERVE_BUDGET = 150e9      # device bytes the serving loop may admit
@@ -636,6 +685,9 @@ def run_serving(E, workloads, step_scale=SERVE_STEP_SCALE):
         pst += q["particles"] * q["steps"]
         sim.close()
     fp64_rate = pst / wall if wall > 0 else None
+    procs = min(cpu_cores(), len(reqs), 16)
+    cpu_sample = list(range(0, len(reqs), max(1, len(reqs) // procs)))[:procs]
+    cpu_rate = cpu_multi_run([(paths[k], reqs[k]["collisions"]) for k in cpu_sample], CPU_MULTI_SECONDS)
     offered = sum(q["particles"] * q["steps"] for q in reqs) / window
     offered_unscaled = sum(q["particles"] * q["steps"] for q in unscaled) / window
     return {"workload": "serving: Poisson arrivals 50/s for 60 s, grids {64,128,256,512}^2, 25-100 ppc per species, "
@@ -652,7 +704,11 @@ def run_serving(E, workloads, step_scale=SERVE_STEP_SCALE):
             "peak_inflight": int(st.peak_inflight), "peak_bytes": int(st.peak_bytes),
             "fp64_one_at_a_time_particle_steps_per_s": fp64_rate,
             "fp64_sample": "%d of the %d requests, each created, loaded, initialised and run alone" % (len(sample), len(reqs)),
-            "speedup_vs_fp64_one_at_a_time": (st.particle_steps_per_s / fp64_rate) if fp64_rate else None}
+            "speedup_vs_fp64_one_at_a_time": (st.particle_steps_per_s / fp64_rate) if fp64_rate else None,
+            "cpu_baseline": {"value": cpu_rate, "unit": "particle-steps/s", "cores": procs, "kind": "port",
+                             "sample": "%d of the requests at once, one reference loop (oracle restatement) per "
+                                       "host core, %g s each after load and initial field" % (procs, CPU_MULTI_SECONDS)},
+            "speedup_vs_cpu_cores": (st.particle_steps_per_s / cpu_rate) if cpu_rate else None}
 
 
 # Per-launch DRAM traffic (dram__bytes_read.sum + dram__bytes_write.sum) of each
