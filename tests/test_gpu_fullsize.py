@@ -18,6 +18,8 @@
   particles still agree within 1e-10 relative (the two runs differ only in
   the rounding of the fixed-point deposit, ~2^-38 of a particle's weight, and
   the contracted push, a few ulps, so the trajectories separate slowly).
+* the lexicographic SOR on 200^2 and 256^2 cells (the clustered wavefront,
+  undrained with snapshots and drained): the oracle's iterates bit for bit.
 """
 import os
 
@@ -144,3 +146,36 @@ def test_periodic_64_sor_omega_18_fifty_steps_track_oracle(gpu_lib, tmp_path):
     assert rel(sim.grid("phi"), orc.phi) < 1e-10
     for s in range(nsp):
         assert parts_rel(sim.particles(s), orc.parts[s]) < 1e-10
+
+
+@pytest.mark.parametrize("n", [200, 256])
+def test_large_lattice_sor_is_iterate_exact(gpu_lib, tmp_path, n):
+    """The clustered lexicographic SOR on large lattices: 200^2 cells runs the
+    undrained wavefront with four snapshot bands per CTA, 256^2 (whose
+    snapshots do not fit) drains at every check.  Capped at 60 sweeps, and
+    converging at the check after sweep 275 (a tolerance just above the
+    oracle's residual there): the oracle's iteration count and phi bit for
+    bit."""
+    from tests import decks
+
+    d = str(tmp_path)
+    ini = decks.write(decks.deck(nx=n, ny=n, ne=n * n * 4, ni=n * n * 4, solver="gs", tol="1e-30", maxit=276), d)
+    orc = O.OracleSim(ini, initial_field=False)
+    orc.scatter_all()
+    phi275, err275, it_o, conv_o = orc.R.gs_solve(orc.rho)
+    assert it_o == 276 and not conv_o
+    cases = [("1e-30", 60, 60, False), (repr(err275 * 1.0001), 400, 276, True)]
+    for tol, maxit, it_want, conv_want in cases:
+        ini = decks.write(decks.deck(nx=n, ny=n, ne=n * n * 4, ni=n * n * 4, solver="gs", tol=tol, maxit=maxit), d)
+        o = O.OracleSim(ini, initial_field=False)
+        o.scatter_all()
+        phi_o, err_o, it_o, conv_o = o.R.gs_solve(o.rho)
+        assert it_o == it_want and bool(conv_o) == conv_want
+        sim = gpu_lib.Simulation.from_ini(ini)
+        sim.set_grid("rho", o.rho)
+        it, err, conv = sim.potential_solver()
+        assert it == it_o and bool(conv) == conv_want
+        assert np.array_equal(sim.grid("phi"), phi_o)
+        if conv_want:
+            assert np.array_equal(phi_o, phi275)
+        sim.close()
