@@ -151,8 +151,9 @@ def test_periodic_64_sor_omega_18_fifty_steps_track_oracle(gpu_lib, tmp_path):
 @pytest.mark.parametrize("n", [200, 256])
 def test_large_lattice_sor_is_iterate_exact(gpu_lib, tmp_path, n):
     """The clustered lexicographic SOR on large lattices: 200^2 cells runs the
-    undrained wavefront with four snapshot bands per CTA, 256^2 (whose
-    snapshots do not fit) drains at every check.  Capped at 60 sweeps, and
+    undrained wavefront with eight snapshot bands per CTA (rho K read from
+    global memory to make room), 256^2 (whose snapshots do not fit) drains at
+    every check.  Capped at 60 sweeps, and
     converging at the check after sweep 275 (a tolerance just above the
     oracle's residual there): the oracle's iteration count and phi bit for
     bit."""
