@@ -999,6 +999,11 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
     br.gs_norm = gs;
     br.R = gs ? c.nx - 2 : c.ny;
     br.C = gs ? c.ny - 2 : c.nx;
+    // a single run solves lattices with a side of 512 or more unknowns by FFT
+    // passes (where its sides allow), the batch by the dense products: such a
+    // run would not equal its single run bit for bit, so it runs alone
+    if (std::max(br.R, br.C) >= 512)
+      return bfail(EPIC_ERR_INVALID, "run %d: lattices with a side of 512 or more unknowns run alone", r);
     br.lat_off = lat_off;
     for (int side : {br.R, br.C}) {
       if (q_off_of_side[side] < 0) {

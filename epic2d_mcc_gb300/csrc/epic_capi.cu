@@ -114,6 +114,9 @@ void free_species(epic_sim* s, epic_species_state& sp) {
 // Refinement stages of the mixed-precision Poisson solve (each gains ~6
 // digits; the loop stops on the reference's tolerance, usually after 2-3).
 constexpr int SPECTRAL_STAGES = 6;
+// Lattices with a side of at least this many unknowns use FFT passes where
+// their sides allow (SpecFFT); a batch holds only smaller ones.
+constexpr int SPECTRAL_FFT_MIN = 512;
 
 // Sine transforms and inverse eigenvalues of the reference operator for the
 // mixed-precision solve: computed in FP64 on the host, stored in FP32.
@@ -177,6 +180,41 @@ epic_status setup_spectral(epic_sim* s) {
       // the right-hand side has none (projected), the correction gets none.
       D[(size_t)p * C + q] = l == 0.0 ? 0.f : (float)(1.0 / l);
     }
+  // FFT passes for large lattices whose sides allow them: the Hartley
+  // direction (periodic) of n a power of two, FFT length n; the sine
+  // direction of n + 1 a power of two, FFT length 2 (n + 1).  Smaller lattices
+  // keep the dense products, whose cost there is the grid barriers' anyway.
+  std::memset(&sp.fft, 0, sizeof(sp.fft));
+  {
+    auto pow2 = [](long long v) { return v >= 2 && (v & (v - 1)) == 0; };
+    const int sineR = mode != EPIC_POISSON_PERIODIC, sineC = mode == EPIC_POISSON_DIRICHLET;
+    const long long mR = sineR ? 2LL * (R + 1) : R, mC = sineC ? 2LL * (C + 1) : C;
+    if (std::max(R, C) >= SPECTRAL_FFT_MIN && pow2(mR) && pow2(mC) && mR <= 4096 && mC <= 4096) {
+      SpecFFT& F = sp.fft;
+      F.on = 1;
+      F.mR = (int)mR;
+      F.mC = (int)mC;
+      F.lgR = __builtin_ctzll(mR);
+      F.lgC = __builtin_ctzll(mC);
+      F.sineR = sineR;
+      F.sineC = sineC;
+      F.scaleR = (float)(sineR ? std::sqrt(2.0 / (R + 1)) : 1.0 / std::sqrt((double)R));
+      F.scaleC = (float)(sineC ? std::sqrt(2.0 / (C + 1)) : 1.0 / std::sqrt((double)C));
+      const double pi = 3.14159265358979323846;
+      for (int d = 0; d < 2; d++) {
+        const long long m = d ? mC : mR;
+        std::vector<float2> tw((size_t)m / 2);
+        for (long long k = 0; k < m / 2; k++)
+          tw[(size_t)k] = make_float2((float)std::cos(2.0 * pi * (double)k / (double)m),
+                                      (float)-std::sin(2.0 * pi * (double)k / (double)m));
+        float2* dt = nullptr;
+        CK(cudaMallocAsync((void**)&dt, tw.size() * sizeof(float2), s->stream));
+        CK(cudaMemcpyAsync(dt, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice, s->stream));
+        CK(cudaStreamSynchronize(s->stream));  // tw is a host temporary
+        (d ? F.twC : F.twR) = dt;
+      }
+    }
+  }
   CK(cudaMallocAsync((void**)&sp.QR, QR.size() * sizeof(float), s->stream));
   if (C == R && mode != EPIC_POISSON_DIRICHLET_X) sp.QC = sp.QR;
   else CK(cudaMallocAsync((void**)&sp.QC, QC.size() * sizeof(float), s->stream));
@@ -904,7 +942,7 @@ void epic_destroy(epic_sim* s) {
   if (s->sort_buf) dfree(s, s->sort_buf);
   for (auto& sp : s->sp) free_species(s, sp);
   void* spec[] = {s->spec.QR, s->spec.QC != s->spec.QR ? s->spec.QC : nullptr, s->spec.D, s->spec.t0, s->spec.t1,
-                  s->spec.r64, s->spec.partials, s->spec.state,
+                  s->spec.r64, s->spec.partials, s->spec.state, (void*)s->spec.fft.twR, (void*)s->spec.fft.twC,
                   s->ef32};
   for (void* p : spec) dfree(s, p);
   for (auto& pe : s->prof_pending) {

@@ -291,6 +291,19 @@ void launch_deposit_mixed_sorted(cudaStream_t st, const Geom& g, const MixedSoA&
 
 // ---- spectral FP32 inner solve with FP64 refinement (epic_spectral.cu) ----
 struct SolverArgs;
+// Fast transforms of the mixed solve for lattices whose sides allow them
+// (epic_spectral.cuh, spec_fft_unit): a line of n unknowns is transformed by
+// a complex radix-2 FFT of length m, m = n for the Hartley transform
+// (periodic direction, n a power of two) and m = 2 (n + 1) for the sine
+// transform (DST-I by odd extension, n + 1 a power of two).
+struct SpecFFT {
+  int on;                  // 1: the solve's four products per stage are FFT passes
+  int mR, mC, lgR, lgC;    // FFT lengths of the two directions and their log2
+  int sineR, sineC;        // 1: sine transform, 0: Hartley
+  float scaleR, scaleC;    // orthonormal scaling: sqrt(2 / (n + 1)) or 1 / sqrt(n)
+  const float2* twR;       // e^(-2 pi i k / mR), k < mR / 2
+  const float2* twC;
+};
 struct SpectralSolver {
   int R, C;       // lattice of unknowns: R rows of C
   int flat;       // 1: pcgsolver's lattice of the flattened vector (all nodes); 0: gssolver's interior
@@ -302,6 +315,7 @@ struct SpectralSolver {
   double *r64;    // residual scratch (nx*ny)
   double* partials;
   int* state;     // [0] done flag, [1] stage, [2] converged
+  SpecFFT fft;    // fft.on: FFT passes instead of the dense products (large lattices)
 };
 int spectral_supported(const Geom& g, int solver, int poisson_bc);
 int spectral_chunks(const SpectralSolver& sp);  // residual chunks (partials needed)

@@ -15,7 +15,8 @@
 // eigenvalues lambda_k = -4 sin^2(pi (k+1)/(2(n+1))), so
 // A^-1 X = Q_R ((Q_R X Q_C) o D) Q_C with D_pq = 1/(lambda_p + mu_q): four dense
 // products, done here in FP32 (each inner solve is accurate to ~1e-6
-// relative).  Each stage computes the FP64 residual r = b - A x, stops
+// relative); on large lattices whose sides allow it (SpecFFT) the four
+// products are FFT passes instead, O(n^2 log n) against O(n^3).  Each stage computes the FP64 residual r = b - A x, stops
 // once the reference's own stopping norm is below its tolerance (|r|_2 for
 // pcgsolver; the SOR residual L2 = sqrt(sum R^2 / (nx ny)), R = r/dx^2, for
 // gssolver), and otherwise adds the FP32 correction A^-1 r to x in FP64.
@@ -118,8 +119,8 @@ __device__ bool spec_grid_sync(unsigned int* bar, int* flags, long long limit) {
 
 // The whole defect-correction loop in one cooperative launch: the CTAs take
 // the residual chunks in turn; after a grid barrier every CTA forms the
-// stopping norm from the chunk sums in chunk order (so every CTA decides
-// alike; CTA 0 records it as spec_check); then the four products, the CTAs
+// stopping norm from the exact sum of the chunk sums (so every CTA decides
+// alike, and as spec_check; CTA 0 records it); then the four products, the CTAs
 // taking TILE x TILE output tiles in turn, with a grid barrier after each.
 // Each output accumulates over k in order whatever the tile, so the
 // potentials equal those of the batched solve bit for bit.
@@ -149,35 +150,51 @@ __device__ void spec_chunk_sum(const SpecLattice& L, int what, int ch, double* o
   __syncthreads();
 }
 
-// The mean over the lattice from the chunk sums, in chunk order (every CTA
-// forms the same value).
-__device__ double spec_chunk_mean(const SpecLattice& L, const double* sums, int nch) {
-  double t = 0;
-  for (int b = 0; b < nch; b++) t += __ldcg(&sums[b]);
-  return t / ((double)L.R * L.C);
+// The mean over the lattice from the chunk sums, added exactly by the whole
+// CTA (every CTA forms the same value).
+__device__ double spec_chunk_mean(const SpecLattice& L, const double* sums, int nch, int* s_e,
+                                  unsigned long long (*s_v)[2], double* s_out) {
+  return spec_exact_sum_cta(sums, nch, s_e, s_v, s_out) / ((double)L.R * L.C);
 }
 
+// TILE 16, 32, 64: the dense products in output tiles of that side; TILE 0:
+// FFT passes (F), units of SPEC_FFT_LINES lines, the sequences in dynamic
+// shared memory.
 template <int TILE>
 __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* __restrict__ QR,
                                                     const float* __restrict__ QC, const float* __restrict__ D,
                                                     float* t1, int stages, unsigned int* bar, int* flags,
-                                                    long long spin) {
-  __shared__ __align__(16) float As[TILE == 64 ? 1 : 32][33];
-  __shared__ float Bs[TILE == 64 ? 1 : 32][33];
+                                                    long long spin, SpecFFT F) {
+  extern __shared__ float2 fbuf[];
+  __shared__ __align__(16) float As[TILE == 64 || TILE == 0 ? 1 : 32][33];
+  __shared__ float Bs[TILE == 64 || TILE == 0 ? 1 : 32][33];
   __shared__ __align__(16) SpecGemmSmem sg[TILE == 64 ? 1 : 0 + 1];
   __shared__ double sm8[8];
-  __shared__ double s_mean;
+  __shared__ double s_mean, s_sum;
   __shared__ int s_stop;
+  __shared__ int s_xe[8];
+  __shared__ unsigned long long s_xv[8][2];
   const int R = L.R, C = L.C;
   const int nch = (R * C + SPEC_CHUNK - 1) / SPEC_CHUNK;
-  const int tiles_c = (C + TILE - 1) / TILE, ntiles = tiles_c * ((R + TILE - 1) / TILE);
+  const int TL = TILE ? TILE : 1;
+  const int tiles_c = (C + TL - 1) / TL, ntiles = tiles_c * ((R + TL - 1) / TL);
+  const int ucols = (C + SPEC_FFT_LINES - 1) / SPEC_FFT_LINES, urows = (R + SPEC_FFT_LINES - 1) / SPEC_FFT_LINES;
   // PERIODIC: the chunk sums of b and of phi go after the residual's.
   double* const sums = L.partials + nch;
   const bool periodic = L.mode == EPIC_POISSON_PERIODIC;
+  // FFT: the twiddle tables in shared memory after the sequences
+  float2* const s_twR = fbuf + (TILE == 0 ? (SPEC_FFT_LINES / 2) * max(F.mR, F.mC) : 0);
+  float2* const s_twC = s_twR + (TILE == 0 ? F.mR / 2 : 0);
+  if (TILE == 0) {
+    for (int k = threadIdx.x; k < F.mR / 2; k += blockDim.x) s_twR[k] = F.twR[k];
+    for (int k = threadIdx.x; k < F.mC / 2; k += blockDim.x) s_twC[k] = F.twC[k];
+    __syncthreads();
+  }
   if (periodic) {  // b projected onto zero mean: the mean of b over the unknowns
     for (int ch = blockIdx.x; ch < nch; ch += gridDim.x) spec_chunk_sum(L, 0, ch, sums, sm8);
     if (!spec_grid_sync(bar, flags, spin)) return;
-    if (threadIdx.x == 0) s_mean = spec_chunk_mean(L, sums, nch);
+    const double m = spec_chunk_mean(L, sums, nch, s_xe, s_xv, &s_sum);
+    if (threadIdx.x == 0) s_mean = m;
     __syncthreads();
     L.bmean = &s_mean;
   }
@@ -187,9 +204,9 @@ __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* 
       __syncthreads();
     }
     if (!spec_grid_sync(bar, flags, spin)) return;
+    const double sum = spec_exact_sum_cta(L.partials, nch, s_xe, s_xv, &s_sum);
     if (threadIdx.x == 0) {
-      double sum = 0, norm, err;
-      for (int b = 0; b < nch; b++) sum += __ldcg(&L.partials[b]);
+      double norm, err;
       spec_norm(L, sum, norm, err);
       const int done = norm < L.tol;
       if (blockIdx.x == 0) spec_record(L, done, s == stages, err);
@@ -206,18 +223,28 @@ __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* 
                                                   t - (t / tiles_c) * tiles_c, As, Bs);                      \
   }                                                                                                          \
   if (!spec_grid_sync(bar, flags, spin)) return;
-    SPEC_PASS(0, R, QR, L.t0, t1, nullptr)
-    SPEC_PASS(1, C, t1, QC, L.t0, D)
-    SPEC_PASS(0, R, QR, L.t0, t1, nullptr)
-    SPEC_PASS(2, C, t1, QC, nullptr, nullptr)
+#define SPEC_FFT(EPI, DIR, IN_, OUT_, D_)                                                         \
+  for (int u = blockIdx.x; u < (DIR == 0 ? ucols : urows); u += gridDim.x)                          \
+    spec_fft_unit<EPI>(L, F, DIR, u * SPEC_FFT_LINES, IN_, OUT_, D_, fbuf, s_twR, s_twC);           \
+  if (!spec_grid_sync(bar, flags, spin)) return;
+    if constexpr (TILE == 0) {  // the same four products as FFT passes: along r, along c (o D), along r, along c (+= phi)
+      SPEC_FFT(0, 0, L.t0, t1, nullptr)
+      SPEC_FFT(1, 1, t1, L.t0, D)
+      SPEC_FFT(0, 0, L.t0, t1, nullptr)
+      SPEC_FFT(2, 1, t1, nullptr, nullptr)
+    } else {
+      SPEC_PASS(0, R, QR, L.t0, t1, nullptr)
+      SPEC_PASS(1, C, t1, QC, L.t0, D)
+      SPEC_PASS(0, R, QR, L.t0, t1, nullptr)
+      SPEC_PASS(2, C, t1, QC, nullptr, nullptr)
+    }
 #undef SPEC_PASS
+#undef SPEC_FFT
   }
   if (periodic) {  // phi shifted to zero mean over the unknowns (the FP64 solver's gauge)
     for (int ch = blockIdx.x; ch < nch; ch += gridDim.x) spec_chunk_sum(L, 1, ch, sums, sm8);
     if (!spec_grid_sync(bar, flags, spin)) return;
-    if (threadIdx.x == 0) s_mean = spec_chunk_mean(L, sums, nch);
-    __syncthreads();
-    const double m = s_mean;
+    const double m = spec_chunk_mean(L, sums, nch, s_xe, s_xv, &s_sum);
     for (int ch = blockIdx.x; ch < nch; ch += gridDim.x)
       for (int u = 0; u < SPEC_CHUNK / 256; u++) {
         const int q = ch * SPEC_CHUNK + u * 256 + threadIdx.x;
@@ -242,12 +269,21 @@ void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs
   const long long t64 = (long long)((R + 63) / 64) * ((C + 63) / 64);
   const long long t32 = (long long)((R + 31) / 32) * ((C + 31) / 32);
   const long long t16 = (long long)((R + 15) / 16) * ((C + 15) / 16);
-  const int tile = t64 >= sms ? 64 : t32 >= 2LL * sms ? 32 : 16;
-  const void* kern = tile == 64 ? (const void*)k_spec_solve<64>
+  // FFT passes (sp.fft.on): units of SPEC_FFT_LINES lines per direction.
+  const int tile = sp.fft.on ? 0 : t64 >= sms ? 64 : t32 >= 2LL * sms ? 32 : 16;
+  const void* kern = tile == 0    ? (const void*)k_spec_solve<0>
+                     : tile == 64 ? (const void*)k_spec_solve<64>
                      : tile == 32 ? (const void*)k_spec_solve<32> : (const void*)k_spec_solve<16>;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, 0);
+  const int fft_smem =
+      tile == 0 ? (int)(((SPEC_FFT_LINES / 2) * std::max(sp.fft.mR, sp.fft.mC) + sp.fft.mR / 2 + sp.fft.mC / 2) *
+                        sizeof(float2))
+                : 0;
+  if (fft_smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, fft_smem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kern, 256, fft_smem);
   per = std::max(1, std::min(2, per));
-  const long long tiles = tile == 64 ? t64 : tile == 32 ? t32 : t16;
+  const long long units =
+      (long long)std::max((C + SPEC_FFT_LINES - 1) / SPEC_FFT_LINES, (R + SPEC_FFT_LINES - 1) / SPEC_FFT_LINES);
+  const long long tiles = tile == 0 ? units : tile == 64 ? t64 : tile == 32 ? t32 : t16;
   const int grid = (int)std::max(1LL, std::min<long long>(tiles, (long long)per * sms));
   cudaMemsetAsync(a.bar, 0, sizeof(unsigned int), st);
   SpecLattice Lk = L;
@@ -257,8 +293,9 @@ void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs
   unsigned int* bar = a.bar;
   int* flags = a.flags;
   long long spin = spin_limit();
-  void* params[] = {&Lk, &qr, &qc, &d, &t1, &stg, &bar, &flags, &spin};
-  cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(256), params, 0, st);
+  SpecFFT F = sp.fft;
+  void* params[] = {&Lk, &qr, &qc, &d, &t1, &stg, &bar, &flags, &spin, &F};
+  cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(256), params, fft_smem, st);
   if (sp.mode != EPIC_POISSON_DIRICHLET) launch_fill_poisson_nodes(st, a.g, sp.mode, a.phi);
 }
 

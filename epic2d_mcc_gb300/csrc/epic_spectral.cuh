@@ -3,16 +3,58 @@
 // give bit-identical potentials; both files are compiled with the same flags.
 //
 // The residual of a lattice is reduced in fixed chunks of SPEC_CHUNK entries
-// (one CTA each, fixed in-CTA order) and the chunk sums are added in chunk
-// order, so the stopping norm depends only on the lattice, not on how the
-// launch is shaped.  The GEMM tiles accumulate every output over k = 0..K-1
+// (one CTA each, fixed in-CTA order) and the chunk sums are added exactly
+// (fixed point, rounded once), so the stopping norm depends only on the
+// lattice, not on how the launch is shaped or who adds the chunk sums.  The GEMM tiles accumulate every output over k = 0..K-1
 // in order with one fma per step, so the tile shape does not change results
 // either (zero padding adds exact zeros).
 #pragma once
 
 #include "epic_internal.cuh"
+#include "epic_xsum.cuh"
 
 namespace epic {
+
+// Exact sum of v[0..n) rounded once (epic_xsum.cuh), by one thread: the
+// batched solve's per-run test.
+__device__ __forceinline__ double spec_exact_sum_serial(const double* v, int n) {
+  int A = 0;
+  for (int b = 0; b < n; b++) A = max(A, xs_exponent(__ldcg(&v[b])));
+  xs_int acc = 0;
+  for (int b = 0; b < n; b++) acc += xs_from_double(__ldcg(&v[b]), A);
+  return xs_to_double(acc, A);
+}
+
+// The same sum by a whole CTA of 256 threads (the same value: exact, then
+// rounded once), in every thread; s_e and s_v: shared scratch of 8 entries.
+__device__ __forceinline__ double spec_exact_sum_cta(const double* v, int n, int* s_e, unsigned long long (*s_v)[2],
+                                                     double* s_out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int e = 0;
+  for (int b = threadIdx.x; b < n; b += 256) e = max(e, xs_exponent(__ldcg(&v[b])));
+  e = (int)__reduce_max_sync(0xffffffffu, (unsigned)e);
+  if (lane == 0) s_e[wid] = e;
+  __syncthreads();
+  int A = 0;
+  for (int w = 0; w < 8; w++) A = max(A, s_e[w]);
+  xs_int acc = 0;
+  for (int b = threadIdx.x; b < n; b += 256) acc += xs_from_double(__ldcg(&v[b]), A);
+  acc = xs_warp_sum(acc);
+  if (lane == 0) {
+    s_v[wid][0] = (unsigned long long)(xs_uint)acc;
+    s_v[wid][1] = (unsigned long long)((xs_uint)acc >> 64);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    xs_uint tot = 0;
+    for (int w = 0; w < 8; w++) tot += ((xs_uint)s_v[w][1] << 64) | s_v[w][0];
+    *s_out = xs_to_double((xs_int)tot, A);
+  }
+  __syncthreads();
+  const double r = *s_out;
+  __syncthreads();
+  return r;
+}
 
 constexpr int SPEC_CHUNK = 1024;  // lattice entries per residual CTA (256 threads x 4)
 
@@ -148,8 +190,7 @@ __device__ __forceinline__ void spec_record(const SpecLattice& L, int done, int 
 __device__ __forceinline__ void spec_check(const SpecLattice& L, int final_pass) {
   if (L.state[0]) return;
   const int nchunks = (L.R * L.C + SPEC_CHUNK - 1) / SPEC_CHUNK;
-  double s = 0;
-  for (int b = 0; b < nchunks; b++) s += L.partials[b];
+  const double s = spec_exact_sum_serial(L.partials, nchunks);
   double norm, err;
   spec_norm(L, s, norm, err);
   spec_record(L, norm < L.tol, final_pass, err);
@@ -298,6 +339,131 @@ __device__ __forceinline__ void spec_gemm_tile64(int M, int N, int K, const floa
       else if (EPI == 1) Cm[r * N + c] = acc[a][b] * D[r * N + c];
       else spec_add_phi(L, N, r, c, acc[a][b]);
     }
+}
+
+// ---- FFT passes (SpecFFT) ----
+// Lines per unit of work: two complex FFTs, each carrying two real lines (one
+// in the real part, one in the imaginary part).
+constexpr int SPEC_FFT_LINES = 4;
+
+// One unit of an FFT pass: lines [l0, l0 + SPEC_FFT_LINES) of `in`, transformed
+// along direction dir (0: along r, a line per column c; 1: along c, a line per
+// row r), the results (r, c) through the epilogue EPI as in spec_gemm_tile:
+// 0 store to out, 1 store times D, 2 add to phi.  buf: shared memory for
+// SPEC_FFT_LINES / 2 sequences of the FFT length.  Decimation in time from
+// bit-reversed loads, radix 2 taken two stages at a time.  Hartley: Z = FFT(x + i y), H_k = (Re X_k - Im X_k)
+// with X_k = (Z_k + conj Z_(m-k)) / 2 (and Y likewise).  Sine: the odd
+// extension of length m = 2 (n + 1) has FFT -2i S'(x) + 2 S'(y), with S' the
+// unnormalised DST-I at index k + 1.
+template <int EPI>
+__device__ __forceinline__ void spec_fft_unit(const SpecLattice& L, const SpecFFT& F, int dir, int l0,
+                                              const float* in, float* out, const float* __restrict__ D,
+                                              float2* buf, const float2* twR, const float2* twC) {
+  constexpr int NF = SPEC_FFT_LINES / 2, LN = SPEC_FFT_LINES, U = 4;
+  static_assert(LN == 4, "element q of a unit is line q & 3, index q >> 2");
+  const int R = L.R, C = L.C;
+  const int n = dir == 0 ? R : C, nl = dir == 0 ? C : R;
+  const int m = dir == 0 ? F.mR : F.mC, lg = dir == 0 ? F.lgR : F.lgC;
+  const int sine = dir == 0 ? F.sineR : F.sineC;
+  const float sc = dir == 0 ? F.scaleR : F.scaleC;
+  const float2* tw = dir == 0 ? twR : twC;  // shared memory
+  float* const bf = reinterpret_cast<float*>(buf);
+  // Element q of the unit: line q & 3, index q >> 2 along it (a warp reads
+  // eight 16-byte runs: adjacent columns along r, or eight adjacent values of
+  // four rows along c - the same sectors as one 128-byte run).
+  auto at = [&](int line, int e) { return dir == 0 ? e * C + line : line * C + e; };
+  auto slot = [&](int f, int pos, int comp) {
+    return 2 * (f * m + (int)(__brev((unsigned)pos) >> (32 - lg))) + comp;
+  };
+  if (sine && threadIdx.x < 2 * NF * 2) {  // the odd extension's zeros at 0 and n + 1
+    const int f = threadIdx.x >> 2, which = (threadIdx.x >> 1) & 1, comp = threadIdx.x & 1;
+    bf[slot(f, which ? n + 1 : 0, comp)] = 0.f;
+  }
+  // loads: U per thread in flight, then their shared-memory stores
+  for (int q0 = threadIdx.x; q0 < LN * n; q0 += U * blockDim.x) {
+    float v[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * blockDim.x, l = q & (LN - 1), e = q >> 2;
+      v[u] = q < LN * n && l0 + l < nl ? __ldcg(&in[at(l0 + l, e)]) : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int q = q0 + u * blockDim.x, l = q & (LN - 1), e = q >> 2;
+      if (q >= LN * n) continue;
+      const int f = l >> 1, comp = l & 1;
+      if (sine) {
+        bf[slot(f, e + 1, comp)] = v[u];
+        bf[slot(f, m - 1 - e, comp)] = -v[u];
+      } else {
+        bf[slot(f, e, comp)] = v[u];
+      }
+    }
+  }
+  __syncthreads();
+  // Stages s = 0 .. lg-1 (half-span 2^s) two at a time: a thread takes the
+  // four elements g 4h + j + {0, h, 2h, 3h} (j < h = 2^s) through stage s
+  // (pairs at distance h, twiddle j) and stage s + 1 (pairs at distance 2h,
+  // twiddles j and j + h) in registers - one barrier and one shared-memory
+  // round trip per two stages; an odd last stage alone.
+  auto bfly = [](float2& a, float2& c, float2 w) {
+    const float2 t = make_float2(w.x * c.x - w.y * c.y, w.x * c.y + w.y * c.x);
+    c = make_float2(a.x - t.x, a.y - t.y);
+    a = make_float2(a.x + t.x, a.y + t.y);
+  };
+  int st = 0;
+  for (; st + 1 < lg; st += 2) {
+    const int h = 1 << st, quarter = m >> 2;
+    for (int q = threadIdx.x; q < NF * quarter; q += blockDim.x) {
+      const int f = q >> (lg - 2), b = q & (quarter - 1);
+      const int j = b & (h - 1), i0 = ((b >> st) << (st + 2)) + j;
+      float2* x = buf + f * m;
+      float2 a0 = x[i0], a1 = x[i0 + h], a2 = x[i0 + 2 * h], a3 = x[i0 + 3 * h];
+      const float2 w1 = tw[j << (lg - 1 - st)];
+      bfly(a0, a1, w1);
+      bfly(a2, a3, w1);
+      bfly(a0, a2, tw[j << (lg - 2 - st)]);
+      bfly(a1, a3, tw[(j + h) << (lg - 2 - st)]);
+      x[i0] = a0;
+      x[i0 + h] = a1;
+      x[i0 + 2 * h] = a2;
+      x[i0 + 3 * h] = a3;
+    }
+    __syncthreads();
+  }
+  if (st < lg) {
+    const int h = 1 << st, half = m >> 1;
+    for (int q = threadIdx.x; q < NF * half; q += blockDim.x) {
+      const int f = q >> (lg - 1), b = q & (half - 1);
+      const int j = b & (h - 1), i1 = ((b >> st) << (st + 1)) + j;
+      float2* x = buf + f * m;
+      float2 a = x[i1], c = x[i1 + h];
+      bfly(a, c, tw[j << (lg - 1 - st)]);
+      x[i1] = a;
+      x[i1 + h] = c;
+    }
+    __syncthreads();
+  }
+  for (int q = threadIdx.x; q < LN * n; q += blockDim.x) {
+    const int l = q & (LN - 1), k = q >> 2, line = l0 + l;
+    if (line >= nl) continue;
+    const int f = l >> 1, comp = l & 1;
+    const float2* Z = buf + f * m;
+    float y;
+    if (sine) {
+      const float2 z = Z[k + 1];
+      y = comp ? 0.5f * z.x : -0.5f * z.y;
+    } else {
+      const float2 z = Z[k], zc = Z[(m - k) & (m - 1)];
+      y = comp ? 0.5f * ((z.y + zc.y) + (z.x - zc.x)) : 0.5f * ((z.x + zc.x) - (z.y - zc.y));
+    }
+    y *= sc;
+    const int r = dir == 0 ? k : line, c = dir == 0 ? line : k;
+    if (EPI == 0) out[r * C + c] = y;
+    else if (EPI == 1) out[r * C + c] = y * __ldg(&D[r * C + c]);
+    else spec_add_phi(&L, C, r, c, y);
+  }
+  __syncthreads();  // buf is reused by the next unit
 }
 
 }  // namespace epic

@@ -148,6 +148,23 @@ XS_HD uint64_t xs_shr(uint64_t v, unsigned s) {
 #endif
 }
 
+#if defined(__CUDACC__)
+// Warp total of 128-bit fixed-point values: five 26-bit limbs (the top one
+// signed) summed with redux.sync — a limb total of 32 lanes stays below 2^31
+// for |v| < 2^122 — and recombined exactly.
+__device__ __forceinline__ xs_int xs_warp_sum(xs_int v) {
+  const xs_uint u = (xs_uint)v;
+  const unsigned M = (1u << 26) - 1;
+  const int l0 = __reduce_add_sync(0xffffffffu, (int)((unsigned)u & M));
+  const int l1 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 26) & M));
+  const int l2 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 52) & M));
+  const int l3 = __reduce_add_sync(0xffffffffu, (int)((unsigned)(u >> 78) & M));
+  const int l4 = __reduce_add_sync(0xffffffffu, (int)(v >> 104));
+  const xs_uint s = ((xs_uint)(xs_int)l4 << 104) + ((xs_uint)(unsigned)l3 << 78) + ((xs_uint)(unsigned)l2 << 52) +
+                    ((xs_uint)(unsigned)l1 << 26) + (xs_uint)(unsigned)l0;
+  return (xs_int)s;
+}
+#endif
 
 }  // namespace epic
 

@@ -26,6 +26,9 @@
  * Runs must use the mixed form with CIC deposition and the same number of
  * species (species k plays the same role in every run; MCC needs electrons as
  * species 0 and ions as species 1); the colliding runs share one gas density.
+ * Lattices with a side of 512 or more unknowns run alone (a single run solves
+ * them by FFT passes where their sides allow, so a batch could not equal it);
+ * conductors and emitters run in the server and the single-run form.
  * Walls may be periodic, reflective or absorbing, mixed within a batch; with
  * an absorbing run in the batch the push erases leaving particles in order
  * (as a single run) and the deposit and the MCC's selection run as their own

@@ -110,6 +110,53 @@ def test_mixed_spectral_solve_large_lattice(gpu_lib, tmp_path, n, bc):
         assert rel(mx.grid("phi"), ref.grid("phi")) < 1e-5
 
 
+@pytest.mark.parametrize("n, bc, solver", [(1024, "periodic", "cg"), (512, "dirichlet_x", "cg"), (512, "dirichlet", "gs")])
+def test_mixed_spectral_solve_fft_lattice(gpu_lib, tmp_path, n, bc, solver):
+    """Lattices with a side of 512 or more unknowns whose sides allow it take FFT passes instead of the
+    dense products: the Hartley transform of a periodic direction (1024 or 512 points), the sine transform
+    of a Dirichlet one by the odd extension (2 x 512 points).  The solve converges within a few stages to
+    the reference's stopping norm, and phi agrees within 1e-6 with the FP64 solution of the same rho: a
+    tightly converged FP64 PCG on the periodic and x-Dirichlet lattices, the exact discrete solution by
+    orthonormal DST-I in FP64 (scipy) on the Dirichlet interior."""
+    E = gpu_lib
+    extra = "" if bc == "dirichlet" else "poisson_bc = %s\n" % bc
+    ini = decks.write(decks.deck(nx=n, ny=n, ne=1000, ni=1000, solver=solver, tol="1", maxit=1000000,
+                                 solver_extra=extra), str(tmp_path))
+    s = O.setup(ini)
+    N = s.nx
+    x = np.linspace(0, 1, N)
+    rho = (np.sin(3 * np.pi * x)[:, None] * np.cos(2 * np.pi * x)[None, :]).ravel()
+    rho += 0.1 * np.random.default_rng(7).normal(size=N * N)
+    K = (s.L / s.LDe) ** 2
+    if solver == "cg":
+        bnorm = np.linalg.norm(rho) * s.dx * s.dx * K
+        tol = 1e-9 * bnorm
+    else:
+        tol = 1e-9 * np.sqrt(np.sum((rho * K) ** 2) / (N * N))  # the SOR residual's norm, relative 1e-9
+    mx = mixed_sim(E, ini, tolerance=tol)
+    mx.set_grid("rho", rho)
+    it, err, conv = mx.potential_solver()
+    assert conv and 1 <= it <= 4, (it, err)
+    phi = mx.grid("phi")
+    if solver == "cg":
+        ref = E.Simulation.from_ini(ini, tolerance=0.05 * tol)
+        ref.set_grid("rho", rho)
+        assert ref.potential_solver()[2]
+        want = ref.grid("phi")
+    else:
+        from scipy import fft as sfft
+
+        m = N - 2
+        lam = -4.0 * np.sin(np.pi * np.arange(1, m + 1) / (2.0 * (m + 1))) ** 2
+        # A phi = -rho K dx^2 on the interior (dx = dy), phi = 0 on the edges
+        b = -(rho.reshape(N, N)[1:-1, 1:-1] * K) * s.dx * s.dx
+        inner = sfft.dstn(sfft.dstn(b, type=1, norm="ortho") / (lam[:, None] + lam[None, :]), type=1, norm="ortho")
+        want = np.zeros((N, N))
+        want[1:-1, 1:-1] = inner
+        want = want.ravel()
+    assert rel(phi, want) < 1e-6
+
+
 @pytest.mark.parametrize("solver", ["cg", "gs"])
 @pytest.mark.parametrize("shape", [(64, 40), (40, 72), (97, 33)])
 def test_mixed_spectral_solve_rectangular(gpu_lib, tmp_path, solver, shape):
