@@ -183,7 +183,7 @@ __global__ void __launch_bounds__(256) k_spec_solve(SpecLattice L, const float* 
   double* const sums = L.partials + nch;
   const bool periodic = L.mode == EPIC_POISSON_PERIODIC;
   // FFT: the twiddle tables in shared memory after the sequences
-  float2* const s_twR = fbuf + (TILE == 0 ? (SPEC_FFT_LINES / 2) * max(F.mR, F.mC) : 0);
+  float2* const s_twR = fbuf + (TILE == 0 ? (SPEC_FFT_LINES / 2) * spec_fft_seq(max(F.mR, F.mC)) : 0);
   float2* const s_twC = s_twR + (TILE == 0 ? F.mR / 2 : 0);
   if (TILE == 0) {
     for (int k = threadIdx.x; k < F.mR / 2; k += blockDim.x) s_twR[k] = F.twR[k];
@@ -275,7 +275,8 @@ void launch_spectral(cudaStream_t st, const SpectralSolver& sp, const SolverArgs
                      : tile == 64 ? (const void*)k_spec_solve<64>
                      : tile == 32 ? (const void*)k_spec_solve<32> : (const void*)k_spec_solve<16>;
   const int fft_smem =
-      tile == 0 ? (int)(((SPEC_FFT_LINES / 2) * std::max(sp.fft.mR, sp.fft.mC) + sp.fft.mR / 2 + sp.fft.mC / 2) *
+      tile == 0 ? (int)(((SPEC_FFT_LINES / 2) * spec_fft_seq(std::max(sp.fft.mR, sp.fft.mC)) + sp.fft.mR / 2 +
+                         sp.fft.mC / 2) *
                         sizeof(float2))
                 : 0;
   if (fft_smem > 48 * 1024) cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, fft_smem);

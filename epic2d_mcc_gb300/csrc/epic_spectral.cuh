@@ -345,13 +345,19 @@ __device__ __forceinline__ void spec_gemm_tile64(int M, int N, int K, const floa
 // Lines per unit of work: two complex FFTs, each carrying two real lines (one
 // in the real part, one in the imaginary part).
 constexpr int SPEC_FFT_LINES = 4;
+// Shared-memory slots of one FFT sequence of length m (padded).
+__host__ __device__ __forceinline__ int spec_fft_seq(int m) { return m + (m >> 5); }
+__device__ __forceinline__ int spec_fft_pad(int i) { return i + (i >> 5); }
 
 // One unit of an FFT pass: lines [l0, l0 + SPEC_FFT_LINES) of `in`, transformed
 // along direction dir (0: along r, a line per column c; 1: along c, a line per
 // row r), the results (r, c) through the epilogue EPI as in spec_gemm_tile:
 // 0 store to out, 1 store times D, 2 add to phi.  buf: shared memory for
-// SPEC_FFT_LINES / 2 sequences of the FFT length.  Decimation in time from
-// bit-reversed loads, radix 2 taken two stages at a time.  Hartley: Z = FFT(x + i y), H_k = (Re X_k - Im X_k)
+// SPEC_FFT_LINES / 2 sequences of the FFT length, each element i of a
+// sequence at i + i / 32 (spec_fft_pad: one spare slot per 32, so that the
+// bit-reversed stores and the short-span butterflies spread over the
+// banks).  Decimation in time from bit-reversed loads, radix 2 taken two
+// stages at a time.  Hartley: Z = FFT(x + i y), H_k = (Re X_k - Im X_k)
 // with X_k = (Z_k + conj Z_(m-k)) / 2 (and Y likewise).  Sine: the odd
 // extension of length m = 2 (n + 1) has FFT -2i S'(x) + 2 S'(y), with S' the
 // unnormalised DST-I at index k + 1.
@@ -372,8 +378,9 @@ __device__ __forceinline__ void spec_fft_unit(const SpecLattice& L, const SpecFF
   // eight 16-byte runs: adjacent columns along r, or eight adjacent values of
   // four rows along c - the same sectors as one 128-byte run).
   auto at = [&](int line, int e) { return dir == 0 ? e * C + line : line * C + e; };
+  const int seq = spec_fft_seq(m);
   auto slot = [&](int f, int pos, int comp) {
-    return 2 * (f * m + (int)(__brev((unsigned)pos) >> (32 - lg))) + comp;
+    return 2 * (f * seq + spec_fft_pad((int)(__brev((unsigned)pos) >> (32 - lg)))) + comp;
   };
   if (sine && threadIdx.x < 2 * NF * 2) {  // the odd extension's zeros at 0 and n + 1
     const int f = threadIdx.x >> 2, which = (threadIdx.x >> 1) & 1, comp = threadIdx.x & 1;
@@ -417,17 +424,19 @@ __device__ __forceinline__ void spec_fft_unit(const SpecLattice& L, const SpecFF
     for (int q = threadIdx.x; q < NF * quarter; q += blockDim.x) {
       const int f = q >> (lg - 2), b = q & (quarter - 1);
       const int j = b & (h - 1), i0 = ((b >> st) << (st + 2)) + j;
-      float2* x = buf + f * m;
-      float2 a0 = x[i0], a1 = x[i0 + h], a2 = x[i0 + 2 * h], a3 = x[i0 + 3 * h];
+      float2* x = buf + f * seq;
+      const int p0 = spec_fft_pad(i0), p1 = spec_fft_pad(i0 + h), p2 = spec_fft_pad(i0 + 2 * h),
+                p3 = spec_fft_pad(i0 + 3 * h);
+      float2 a0 = x[p0], a1 = x[p1], a2 = x[p2], a3 = x[p3];
       const float2 w1 = tw[j << (lg - 1 - st)];
       bfly(a0, a1, w1);
       bfly(a2, a3, w1);
       bfly(a0, a2, tw[j << (lg - 2 - st)]);
       bfly(a1, a3, tw[(j + h) << (lg - 2 - st)]);
-      x[i0] = a0;
-      x[i0 + h] = a1;
-      x[i0 + 2 * h] = a2;
-      x[i0 + 3 * h] = a3;
+      x[p0] = a0;
+      x[p1] = a1;
+      x[p2] = a2;
+      x[p3] = a3;
     }
     __syncthreads();
   }
@@ -436,11 +445,12 @@ __device__ __forceinline__ void spec_fft_unit(const SpecLattice& L, const SpecFF
     for (int q = threadIdx.x; q < NF * half; q += blockDim.x) {
       const int f = q >> (lg - 1), b = q & (half - 1);
       const int j = b & (h - 1), i1 = ((b >> st) << (st + 1)) + j;
-      float2* x = buf + f * m;
-      float2 a = x[i1], c = x[i1 + h];
+      float2* x = buf + f * seq;
+      const int p1 = spec_fft_pad(i1), p2 = spec_fft_pad(i1 + h);
+      float2 a = x[p1], c = x[p2];
       bfly(a, c, tw[j << (lg - 1 - st)]);
-      x[i1] = a;
-      x[i1 + h] = c;
+      x[p1] = a;
+      x[p2] = c;
     }
     __syncthreads();
   }
@@ -448,13 +458,13 @@ __device__ __forceinline__ void spec_fft_unit(const SpecLattice& L, const SpecFF
     const int l = q & (LN - 1), k = q >> 2, line = l0 + l;
     if (line >= nl) continue;
     const int f = l >> 1, comp = l & 1;
-    const float2* Z = buf + f * m;
+    const float2* Z = buf + f * seq;
     float y;
     if (sine) {
-      const float2 z = Z[k + 1];
+      const float2 z = Z[spec_fft_pad(k + 1)];
       y = comp ? 0.5f * z.x : -0.5f * z.y;
     } else {
-      const float2 z = Z[k], zc = Z[(m - k) & (m - 1)];
+      const float2 z = Z[spec_fft_pad(k)], zc = Z[spec_fft_pad((m - k) & (m - 1))];
       y = comp ? 0.5f * ((z.y + zc.y) + (z.x - zc.x)) : 0.5f * ((z.x + zc.x) - (z.y - zc.y));
     }
     y *= sc;
