@@ -595,6 +595,12 @@ def run_batching(E, workloads):
     ms = e0.elapsed_time(e1)
     tiles = b.tuning()
     shapes = b.particle_tuning()
+    # phase split: one more sort period launched step by step with the phase timers on
+    b.set_profiling(True)
+    b.profile()
+    b.run(SORT_EVERY, graph=False)
+    phases = {k: v[0] / SORT_EVERY for k, v in b.profile().items()}
+    b.set_profiling(False)
     b.close()
     rate = n * BATCH_STEPS / (ms / 1e3)
     # the same runs one at a time (mixed form, graph replay)
@@ -626,7 +632,7 @@ def run_batching(E, workloads):
                         "MCC on %d, periodic) as one batch, mixed form" % sum(q["collisions"] for q in reqs),
             "runs": len(reqs), "particles": n, "steps": BATCH_STEPS, "ms_per_step": ms / BATCH_STEPS,
             "particle_steps_per_s": rate, "setup_s": setup_s, "gemm_tiles_by_size_class": tiles,
-            "particle_launch_shapes": shapes,
+            "particle_launch_shapes": shapes, "phases_ms_per_step": phases,
             "one_at_a_time_particle_steps_per_s": single,
             "one_at_a_time_sample": "%d of the runs, each alone (mixed form, graph replay)" % len(sample),
             "speedup_vs_one_at_a_time": rate / single,

@@ -177,6 +177,8 @@ def lib() -> ctypes.CDLL:
         "epic_batch_num_particles": ([vp, ctypes.POINTER(ctypes.c_int64)], st),
         "epic_batch_tuning": ([vp, vp], st),
         "epic_batch_particle_tuning": ([vp, vp, vp, vp], st),
+        "epic_batch_set_profiling": ([vp, i], st),
+        "epic_batch_get_profile": ([vp, vp, vp], st),
         "epic_batch_stream": ([vp], vp),
         "epic_batch_set_log_cross_sections": ([vp, vp, vp, vp, i64, d, d], st),
     }
@@ -608,6 +610,16 @@ class Batch:
         t = np.zeros(4, dtype=np.int32)
         _check(lib().epic_batch_tuning(self._h, _ptr(t)))
         return [int(x) for x in t]
+
+    def set_profiling(self, on: bool = True):
+        _check(lib().epic_batch_set_profiling(self._h, 1 if on else 0))
+
+    def profile(self):
+        """{phase: (ms, count)} accumulated since the last call (directly launched steps only)."""
+        ms = np.zeros(7, dtype=np.float64)
+        cnt = np.zeros(7, dtype=np.int64)
+        _check(lib().epic_batch_get_profile(self._h, _ptr(ms), _ptr(cnt)))
+        return {name: (float(ms[k]), int(cnt[k])) for k, name in enumerate(Simulation.PHASES)}
 
     def particle_tuning(self):
         """The autotuner's launch shapes of the fused push and the deposit pass, with the timings behind them."""

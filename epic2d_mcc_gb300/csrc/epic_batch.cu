@@ -553,6 +553,42 @@ struct epic_batch {
   int push_threads = PART_THREADS, push_blocks = 0, dep_threads = PART_THREADS, dep_blocks = 0;
   float push_ms[5] = {0, 0, 0, 0, 0}, dep_ms[6] = {0, 0, 0, 0, 0, 0};
   bool particles_tuned = false;
+  // Phase timers (epic_batch_set_profiling): events around each phase of a
+  // step launched directly (not while a graph is being captured).
+  bool profiling = false;
+  std::vector<cudaEvent_t> event_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> prof_pending;
+  double prof_ms[7] = {0, 0, 0, 0, 0, 0, 0};
+  long long prof_count[7] = {0, 0, 0, 0, 0, 0, 0};
+
+  struct Phase {  // phases as epic_get_profile: 0 deposit .. 6 sort
+    epic_batch* b;
+    int phase;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    Phase(epic_batch* b_, int p) : b(b_), phase(p) {
+      if (!b->profiling) return;
+      cudaStreamCaptureStatus cs;
+      if (cudaStreamIsCapturing(b->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+      e0 = b->take_event();
+      e1 = b->take_event();
+      cudaEventRecord(e0, b->stream);
+    }
+    ~Phase() {
+      if (!e0) return;
+      cudaEventRecord(e1, b->stream);
+      b->prof_pending.push_back({phase, {e0, e1}});
+    }
+  };
+  cudaEvent_t take_event() {
+    if (!event_pool.empty()) {
+      cudaEvent_t e = event_pool.back();
+      event_pool.pop_back();
+      return e;
+    }
+    cudaEvent_t e = nullptr;
+    cudaEventCreate(&e);
+    return e;
+  }
   void* sort_buf = nullptr;
   double* staging = nullptr;
   int64_t step_index = 0;
@@ -665,9 +701,19 @@ struct epic_batch {
   }
 
   void deposit_and_solve() {
-    if (!acc_valid) deposit_all();
-    launch_batch_finalize(stream, grids());
-    solve();
+    if (!acc_valid) {
+      Phase ph(this, 0);
+      deposit_all();
+    }
+    {
+      Phase ph(this, 1);
+      launch_batch_finalize(stream, grids());
+    }
+    {
+      Phase ph(this, 2);
+      solve();
+    }
+    Phase ph(this, 3);
     launch_batch_efield(stream, grids());
   }
 
@@ -689,34 +735,53 @@ struct epic_batch {
   // push deposits its new positions (and the electrons' push selects the MCC's
   // candidates), the MCC, and the deposit of its ionisation products.
   void step(int sort) {
-    if (sort) sort_all();  // the accumulators do not depend on the order
+    if (sort) {
+      Phase ph(this, 6);
+      sort_all();  // the accumulators do not depend on the order
+    }
     if (has_open) {  // erasing pushes: deposit, field, compacting push, MCC with its own selection
-      deposit_all();
-      deposit_and_solve();
-      for (int s = 0; s < nsp; s++) {
-        cudaMemsetAsync(tile_ctr, 0, sizeof(unsigned int), stream);
-        cudaMemsetAsync(tile_status, 0, tile_status_len * sizeof(unsigned long long), stream);
-        k_batch_push_compact<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s,
-                                                                tile_status, tile_ctr, flags, spin_limit());
+      {
+        Phase ph(this, 0);
+        deposit_all();
       }
-      if (any_mcc)
+      deposit_and_solve();
+      {
+        Phase ph(this, 4);
+        for (int s = 0; s < nsp; s++) {
+          cudaMemsetAsync(tile_ctr, 0, sizeof(unsigned int), stream);
+          cudaMemsetAsync(tile_status, 0, tile_status_len * sizeof(unsigned long long), stream);
+          k_batch_push_compact<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s,
+                                                                  tile_status, tile_ctr, flags, spin_limit());
+        }
+      }
+      if (any_mcc) {
+        Phase ph(this, 5);
         launch_batch_mcc(stream, cs, d_runs, d_node_run, arena[0], d_n[0], cap[0], arena[1], d_n[1], cap[1], d_step,
                          ev, d_ncoll, flags, grid);
+      }
       acc_valid = false;
       return;
     }
     deposit_and_solve();
-    const int grid_dep = push_blocks ? push_blocks : resident_grid(k_batch_push_dep<true, PART_THREADS>, PART_THREADS);
-    for (int s = 0; s < nsp; s++) {
-      cudaMemsetAsync(acc[s], 0, nodes * sizeof(unsigned long long), stream);
-      if (any_mcc && s == 0) launch_push<true>(arena[s], d_n[s], ef32, s, acc[s], push_threads, grid_dep);
-      else launch_push<false>(arena[s], d_n[s], ef32, s, acc[s], push_threads, grid_dep);
+    {
+      Phase ph(this, 4);
+      const int grid_dep =
+          push_blocks ? push_blocks : resident_grid(k_batch_push_dep<true, PART_THREADS>, PART_THREADS);
+      for (int s = 0; s < nsp; s++) {
+        cudaMemsetAsync(acc[s], 0, nodes * sizeof(unsigned long long), stream);
+        if (any_mcc && s == 0) launch_push<true>(arena[s], d_n[s], ef32, s, acc[s], push_threads, grid_dep);
+        else launch_push<false>(arena[s], d_n[s], ef32, s, acc[s], push_threads, grid_dep);
+      }
     }
     if (any_mcc) {
-      for (int k = 0; k < 2; k++)
-        cudaMemcpyAsync(d_nold + k, d_n[k], sizeof(long long), cudaMemcpyDeviceToDevice, stream);
-      launch_batch_mcc(stream, cs, d_runs, d_node_run, arena[0], d_n[0], cap[0], arena[1], d_n[1], cap[1], d_step, ev,
-                       d_ncoll, flags, grid, 1);
+      {
+        Phase ph(this, 5);
+        for (int k = 0; k < 2; k++)
+          cudaMemcpyAsync(d_nold + k, d_n[k], sizeof(long long), cudaMemcpyDeviceToDevice, stream);
+        launch_batch_mcc(stream, cs, d_runs, d_node_run, arena[0], d_n[0], cap[0], arena[1], d_n[1], cap[1], d_step,
+                         ev, d_ncoll, flags, grid, 1);
+      }
+      Phase ph(this, 0);
       for (int k = 0; k < 2; k++)
         k_batch_deposit_range<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[k], d_nold + k, d_n[k],
                                                                  acc[k]);
@@ -1167,6 +1232,11 @@ epic_status epic_batch_create(const epic_request* runs, int nruns, int sort_ever
 void epic_batch_destroy(epic_batch* b) {
   if (!b) return;
   if (b->stream) cudaStreamSynchronize(b->stream);
+  for (auto& pe : b->prof_pending) {
+    cudaEventDestroy(pe.second.first);
+    cudaEventDestroy(pe.second.second);
+  }
+  for (cudaEvent_t e : b->event_pool) cudaEventDestroy(e);
   if (b->g_plain) cudaGraphExecDestroy(b->g_plain);
   if (b->g_sort) cudaGraphExecDestroy(b->g_sort);
   for (void* p : b->allocs) cudaFreeAsync(p, b->stream);
@@ -1377,6 +1447,33 @@ epic_status epic_batch_set_log_cross_sections(epic_batch* b, const double* ela, 
 epic_status epic_batch_tuning(epic_batch* b, int tiles[4]) {
   if (!b || !tiles) return bfail(EPIC_ERR_INVALID, "bad argument");
   std::memcpy(tiles, b->tiles, sizeof(b->tiles));
+  return EPIC_OK;
+}
+
+epic_status epic_batch_set_profiling(epic_batch* b, int enable) {
+  if (!b) return bfail(EPIC_ERR_INVALID, "null batch");
+  b->profiling = enable != 0;
+  return EPIC_OK;
+}
+
+epic_status epic_batch_get_profile(epic_batch* b, double ms[7], int64_t counts[7]) {
+  if (!b) return bfail(EPIC_ERR_INVALID, "null batch");
+  BCK(cudaStreamSynchronize(b->stream));
+  for (auto& pe : b->prof_pending) {
+    float t = 0;
+    BCK(cudaEventElapsedTime(&t, pe.second.first, pe.second.second));
+    b->prof_ms[pe.first] += t;
+    b->prof_count[pe.first] += 1;
+    b->event_pool.push_back(pe.second.first);
+    b->event_pool.push_back(pe.second.second);
+  }
+  b->prof_pending.clear();
+  for (int k = 0; k < 7; k++) {
+    if (ms) ms[k] = b->prof_ms[k];
+    if (counts) counts[k] = b->prof_count[k];
+    b->prof_ms[k] = 0;
+    b->prof_count[k] = 0;
+  }
   return EPIC_OK;
 }
 

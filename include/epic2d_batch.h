@@ -75,6 +75,13 @@ epic_status epic_batch_tuning(epic_batch* b, int tiles[4]);
  * 256 at full occupancy, 256 with 4, 8 and 16 CTAs per SM, 128 with 8).  No
  * shape changes results. */
 epic_status epic_batch_particle_tuning(epic_batch* b, int shapes[4], float push_ms[5], float deposit_ms[6]);
+/* Per-phase timing of directly launched steps (epic_batch_run with
+ * use_graph = 0), as epic_set_profiling / epic_get_profile for one run:
+ * phases 0 deposit, 1 finalisation + rho, 2 Poisson solve, 3 E-field, 4 push,
+ * 5 MCC, 6 cell sort; get_profile waits for the stream, returns accumulated
+ * milliseconds and counts and resets them. */
+epic_status epic_batch_set_profiling(epic_batch* b, int enable);
+epic_status epic_batch_get_profile(epic_batch* b, double ms[7], int64_t counts[7]);
 void* epic_batch_stream(epic_batch* b);
 
 #ifdef __cplusplus

@@ -39,7 +39,14 @@ def test_batch_runs_equal_single_runs(gpu_lib, tmp_path, graph):
     assert sh["push_blocks"] > 0 and sh["deposit_blocks"] > 0
     assert all(v > 0 for v in sh["push_ms_by_shape"].values())
     assert all(v > 0 for v in sh["deposit_ms_by_shape"].values())
+    if not graph:  # the phase timers of directly launched steps (they change no result)
+        b.set_profiling(True)
+        b.profile()
     b.run(steps, graph=graph)
+    if not graph:
+        prof = b.profile()
+        assert prof["push"][1] == steps and prof["solve"][1] == steps and prof["sort"][1] == (steps + 3) // 4
+        assert all(prof[k][0] > 0 for k in ("push", "solve", "sort"))
     for k, (ini, r) in enumerate(reqs):
         sim = A.Simulation.from_ini(ini, precision=1, sort_every=sort_every)
         sim.load_particles_device(50 + k)
