@@ -231,23 +231,45 @@ __global__ void __launch_bounds__(T, 768 / T) k_batch_push_dep(const BRun* __res
       }
     }
     unsigned int cand = 0;
+    // A thread's particles are consecutive in the cell-sorted array, so they
+    // nearly always share a run: its parameters are loaded once and kept
+    // while the run stays the same.
+    int rid = -1, rbc = 0, rmcc = 0;
+    long long roff = 0;
+    float rqm = 0.f, rcx = 0.f, rcy = 0.f;
+    unsigned long long rcut = 0, rseed = 0;
+    Geom g;
 #pragma unroll
     for (int k = 0; k < P; k++)
       if (c[k] >= 0) {
-        const BRun& r = runs[__ldg(&node_run[c[k]])];
-        const Geom g = run_geom(r);
-        const float2* ef = ef32 + r.node_off;
-        int cl = (int)(c[k] - r.node_off);
-        if (r.bc == EPIC_PBC)
-          push_mixed_one<EPIC_CIC, EPIC_PBC>(g, ef, r.qmK_dt[s], r.cx, r.cy, cl, ox[k], oy[k], vx[k], vy[k]);
+        const int ri = __ldg(&node_run[c[k]]);
+        if (ri != rid) {
+          const BRun& r = runs[ri];
+          g = run_geom(r);
+          roff = r.node_off;
+          rbc = r.bc;
+          rqm = r.qmK_dt[s];
+          rcx = r.cx;
+          rcy = r.cy;
+          if (SEL) {
+            rmcc = r.mcc;
+            rcut = r.cut53;
+            rseed = r.seed;
+          }
+          rid = ri;
+        }
+        const float2* ef = ef32 + roff;
+        int cl = (int)(c[k] - roff);
+        if (rbc == EPIC_PBC)
+          push_mixed_one<EPIC_CIC, EPIC_PBC>(g, ef, rqm, rcx, rcy, cl, ox[k], oy[k], vx[k], vy[k]);
         else
-          push_mixed_one<EPIC_CIC, EPIC_REFLECTIVE>(g, ef, r.qmK_dt[s], r.cx, r.cy, cl, ox[k], oy[k], vx[k], vy[k]);
-        c[k] = (int)(r.node_off + cl);
-        if (SEL && r.mcc) {
+          push_mixed_one<EPIC_CIC, EPIC_REFLECTIVE>(g, ef, rqm, rcx, rcy, cl, ox[k], oy[k], vx[k], vy[k]);
+        c[k] = (int)(roff + cl);
+        if (SEL && rmcc) {
           const long long q = q0 + k;
-          Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)r.seed, (uint32_t)(r.seed >> 32), 0,
+          Philox src{(uint32_t)q, (uint32_t)(q >> 32), (uint32_t)step, (uint32_t)rseed, (uint32_t)(rseed >> 32), 0,
                      make_uint4(0, 0, 0, 0)};
-          if (src.next53() < r.cut53) cand |= 1u << k;
+          if (src.next53() < rcut) cand |= 1u << k;
         }
       }
     if (full) {
