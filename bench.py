@@ -637,7 +637,8 @@ def run_batching(E, workloads):
     cpu_rate = cpu_multi_run([(paths[k], reqs[k]["collisions"]) for k in cpu_sample], CPU_MULTI_SECONDS)
     return {"workload": "batching: 512 runs (cells {32,...,256} per axis, 20-200 ppc per species, Te 0.5-5 eV, "
                         "MCC on %d, periodic) as one batch, mixed form" % sum(q["collisions"] for q in reqs),
-            "runs": len(reqs), "particles": n, "steps": BATCH_STEPS, "ms_per_step": ms / BATCH_STEPS,
+            "runs": len(reqs), "particles": n, "steps": BATCH_STEPS, "sort_every": BATCH_SORT_EVERY,
+            "ms_per_step": ms / BATCH_STEPS,
             "particle_steps_per_s": rate, "setup_s": setup_s, "gemm_tiles_by_size_class": tiles,
             "particle_launch_shapes": shapes, "phases_ms_per_step": phases,
             "one_at_a_time_particle_steps_per_s": single,
