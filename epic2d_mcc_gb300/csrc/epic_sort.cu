@@ -166,12 +166,19 @@ __global__ void __launch_bounds__(SORT_T) k_radix_scatter(const unsigned* __rest
   const unsigned lt = (1u << lane) - 1u;
   constexpr int R = SORT_PER_WARP / 32;
   unsigned key[R], val[R], rank[R];
+  // All of the warp's loads first: the ranking rounds below are ordered by
+  // __syncwarp, which loads issued inside them could not cross.
 #pragma unroll
   for (int r = 0; r < R; r++) {
     const long long q = base + r * 32 + lane;
     const bool valid = q < n;
-    key[r] = valid ? keys_in[q] : 0xFFFFFFFFu;
-    val[r] = valid ? (vals_in ? vals_in[q] : (unsigned)q) : 0u;
+    key[r] = valid ? __ldg(&keys_in[q]) : 0xFFFFFFFFu;
+    val[r] = valid ? (vals_in ? __ldg(&vals_in[q]) : (unsigned)q) : 0u;
+  }
+#pragma unroll
+  for (int r = 0; r < R; r++) {
+    const long long q = base + r * 32 + lane;
+    const bool valid = q < n;
     const unsigned d = valid ? (key[r] >> shift) & (RADIX - 1) : (unsigned)RADIX;
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const unsigned pos = __popc(peers & lt);
