@@ -341,22 +341,29 @@ __global__ void __launch_bounds__(PART_THREADS) k_mcc_collide(CrossSections cs, 
   if (threadIdx.x == 0 && s_coll) atomicAdd(&pending[1], s_coll);
 }
 
-// Pass 2 (one block): exclusive scan of the per-tile event counts.
+// Pass 2 (one block): exclusive scan of the per-tile event counts, 4,096
+// tiles (four per thread) per round.
 __global__ void __launch_bounds__(1024) k_mcc_scan(const long long* __restrict__ d_ne, McEvents ev,
                                                    unsigned long long* pending) {
   __shared__ unsigned int warp_tot[32];
   __shared__ unsigned int carry;
   const long long ne = *d_ne;
   const int tiles = (int)((ne + MCC_TILE - 1) / MCC_TILE);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
-  for (int base = 0; base < tiles; base += blockDim.x) {
-    const int t = base + threadIdx.x;
-    unsigned int v = t < tiles ? ev.tile_cnt[t] : 0u, x = v;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int base = 0; base < tiles; base += 4 * blockDim.x) {
+    const int t0 = base + 4 * threadIdx.x;
+    unsigned int v[4], s = 0;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      v[k] = t0 + k < tiles ? ev.tile_cnt[t0 + k] : 0u;
+      s += v[k];
+    }
+    unsigned int x = s;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
+      const unsigned int y = __shfl_up_sync(0xffffffffu, x, o);
       if (lane >= o) x += y;
     }
     if (lane == 31) warp_tot[w] = x;
@@ -365,16 +372,21 @@ __global__ void __launch_bounds__(1024) k_mcc_scan(const long long* __restrict__
       unsigned int y = warp_tot[lane];
 #pragma unroll
       for (int o = 1; o < 32; o <<= 1) {
-        unsigned int z = __shfl_up_sync(0xffffffffu, y, o);
+        const unsigned int z = __shfl_up_sync(0xffffffffu, y, o);
         if (lane >= o) y += z;
       }
       warp_tot[lane] = y;
     }
     __syncthreads();
-    const unsigned int excl = carry + (w ? warp_tot[w - 1] : 0u) + x - v;
-    if (t < tiles) ev.tile_off[t] = excl;
-    __syncthreads();
-    if (threadIdx.x == blockDim.x - 1) carry = excl + v;
+    const unsigned int c0 = carry;
+    unsigned int run = c0 + (w ? warp_tot[w - 1] : 0u) + x - s;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+      if (t0 + k < tiles) ev.tile_off[t0 + k] = run;
+      run += v[k];
+    }
+    __syncthreads();  // every thread has read carry and warp_tot
+    if (threadIdx.x == blockDim.x - 1) carry = run;
     __syncthreads();
   }
   if (threadIdx.x == 0) pending[0] = carry;
@@ -390,10 +402,21 @@ __global__ void __launch_bounds__(PART_THREADS) k_mcc_append(P e, const long lon
                                                              McEvents ev, int* flags) {
   constexpr int ITEMS = MCC_TILE / PART_THREADS;
   __shared__ int sm[40];
+  __shared__ int s_list[PART_THREADS];
+  __shared__ int s_nlist;
   const long long ne = *d_ne, ni = *d_ni;
   const int tiles = (int)((ne + MCC_TILE - 1) / MCC_TILE);
-  for (int t = blockIdx.x; t < tiles; t += gridDim.x) {
-    if (ev.tile_cnt[t] == 0) continue;  // block-uniform
+  // Each CTA takes PART_THREADS consecutive tiles at a time, finds those
+  // with events in one pass (a load per thread) and appends them in turn.
+  for (int t0 = blockIdx.x * PART_THREADS; t0 < tiles; t0 += gridDim.x * PART_THREADS) {
+    if (threadIdx.x == 0) s_nlist = 0;
+    __syncthreads();
+    const int tt = t0 + threadIdx.x;
+    if (tt < tiles && ev.tile_cnt[tt] != 0) s_list[atomicAdd(&s_nlist, 1)] = tt;
+    __syncthreads();
+    const int nlist = s_nlist;
+    for (int li = 0; li < nlist; li++) {
+    const int t = s_list[li];
     const long long base = (long long)t * MCC_TILE;
     int slot[ITEMS], flag[ITEMS];
 #pragma unroll
@@ -422,6 +445,8 @@ __global__ void __launch_bounds__(PART_THREADS) k_mcc_append(P e, const long lon
     }
     __syncthreads();
     if (threadIdx.x == 0) ev.tile_cnt[t] = 0;
+    }
+    __syncthreads();  // s_list and s_nlist are rewritten for the next tiles
   }
 }
 
