@@ -3,8 +3,11 @@ the reference live and by tests/golden/{gshybrid,hybrid}_pbc.npz):
 gsfluidsolver ("gshybrid", src/field.cpp:7-68: the SOR sweep with source
 (rho - exp(phi)) K, rho's edges overwritten, residual every 50 sweeps) and
 nrpcgsolver ("hybrid", src/field.cpp:141-210: ten Newton steps, each a dense
-CG to 1e-4, summed in the reference's order).  The device exp and the host
-library's may differ in the last bit, hence 1e-12 rather than bit equality."""
+CG to 1e-4; the oracle sums its dot products in the reference's order, the
+GPU exactly).  The device exp and the host library's may differ in the last
+bit, hence 1e-12 rather than bit equality.  The smallest grids (6 cells
+across: too few node rows or nodes for a thread-block cluster) take the
+one-CTA kernels, the others the clustered ones."""
 import numpy as np
 import pytest
 
@@ -22,8 +25,8 @@ def rel(a, b):
     return float(np.max(np.abs(a - b)) / max(np.max(np.abs(b)), 1e-300)) if b.size else 0.0
 
 
-@pytest.mark.parametrize("solver,nx,ny", [("gshybrid", 20, 14), ("gshybrid", 24, 24), ("hybrid", 14, 10),
-                                          ("hybrid", 16, 16)])
+@pytest.mark.parametrize("solver,nx,ny", [("gshybrid", 20, 14), ("gshybrid", 24, 24), ("gshybrid", 6, 16),
+                                          ("hybrid", 14, 10), ("hybrid", 16, 16), ("hybrid", 6, 8)])
 def test_boltzmann_solvers_track_oracle(gpu_lib, tmp_path, solver, nx, ny):
     ini = decks.write(decks.deck(nx=nx, ny=ny, ne=1500, ni=1500, te=2, solver=solver, tol="1e-6"), str(tmp_path))
     orc = O.OracleSim(ini)
