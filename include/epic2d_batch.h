@@ -19,9 +19,9 @@
  * so a colliding run is statistically, not bitwise, the run alone; runs
  * without collisions stay bitwise equal to their single runs.
  *
- * An autotuner picks, when the batch is built, the GEMM tile (16 or 32) for
- * each lattice-size class by timing both on the batch's own transforms; the
- * choice does not change results.
+ * An autotuner picks, when the batch is built, the GEMM tile (16, 32, or 64
+ * register-blocked) for each lattice-size class by timing them on the
+ * batch's own transforms; the choice does not change results.
  *
  * Runs must use the mixed form with CIC deposition and the same number of
  * species (species k plays the same role in every run; MCC needs electrons as
@@ -72,8 +72,10 @@ epic_status epic_batch_tuning(epic_batch* b, int tiles[4]);
  * CTAs}; push_ms (5) and deposit_ms (6), when not NULL, receive the sample's
  * time per launch of each shape tried (push: 128 and 256 threads with every
  * CTA resident, 256 with 1 and 2 CTAs per SM, 128 with 3; deposit: 128 and
- * 256 at full occupancy, 256 with 4, 8 and 16 CTAs per SM, 128 with 8).  No
- * shape changes results. */
+ * 256 at full occupancy, 256 with 4, 8 and 16 CTAs per SM, 128 with 8); a
+ * shape replaces the default (push: 256 resident; deposit: 256 with 8 per SM)
+ * only when it is at least 5 % faster on the sample.  No shape changes
+ * results. */
 epic_status epic_batch_particle_tuning(epic_batch* b, int shapes[4], float push_ms[5], float deposit_ms[6]);
 /* Per-phase timing of directly launched steps (epic_batch_run with
  * use_graph = 0), as epic_set_profiling / epic_get_profile for one run:
