@@ -533,7 +533,7 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
   int iter = 0, converged = 0;
   double L2 = 0;
   double* out = phi;
-  if (nxi > 0 && nyi > 0 && K > 0) {
+  if (nxi > 0 && nyi > 0 && K > 0 && a.max_iter > 0) {
     // Undrained: one wavefront over all sweeps g < max_iter (sweep g on
     // diagonal d at step d + cp g).  The sweeps the reference checks write
     // their values into snapshot (g / P) % K as well; a checked sweep's
@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(SORC_THREADS) k_sor_cluster(SolverArgs a, int 
       cl.sync();
     }
     if (!converged) iter = (int)G;
-  } else if (nxi > 0 && nyi > 0) {
+  } else if (nxi > 0 && nyi > 0 && K == 0) {
     // Drained: chunks of sweeps up to the next check, each chunk's wavefront
     // emptied before its residual
     while (iter < a.max_iter) {
