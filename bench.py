@@ -165,6 +165,25 @@ def cpu_port_run(ini, steps, warmup, budget_s=None):
     return n_acc / el, done, n_acc // done, "port"
 
 
+def workload_config(ini, name, world=1):
+    """The workload as both arms report it (from the deck: the same dict for
+    the GPU arm and the reference arm)."""
+    from oracle import oracle as O
+
+    s = O.setup(ini)
+    coll = bool(s.elastic or s.excitation or s.ionization)
+    solver = {"cg": "PCG", "gs": "SOR"}.get(s.solver, s.solver)
+    n = int(sum(sp.numparticle for sp in s.species))
+    return {"workload": name, "particles": n, "grid": [s.nx, s.ny],
+            "solver": "%s tol %g (cold start, as the reference)" % (solver, s.tolerance),
+            "field_bc": {"dirichlet": "phi = 0 on all edges (the reference's)", "periodic": "periodic",
+                         "dirichlet_x": "phi = 0 on the x walls, periodic in y"}.get(s.poisson_bc, s.poisson_bc),
+            "particle_bc": {"pbc": "periodic", "open": "absorbing", "reflective": "reflecting"}.get(s.bc, s.bc),
+            "mcc": "direct MCC, 1000-point log table" if coll else "off",
+            "l2": "inputs larger than L2 (particles %.0f MB)" % (n * 40 / 1e6),
+            "parallelism": "replicas" if world > 1 else "single run"}
+
+
 def _cpu_run_worker(job):
     """One reference loop (oracle restatement, one thread) on one deck for
     budget_s seconds after its load and initial field: (particle-steps, s)."""
@@ -218,7 +237,8 @@ def run_reference(args, rank, world):
             "steps": done, "warmup": min(args.warmup, 1), "ms_per_step": n / value * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (particles loaded from mt19937 seed 0, as the reference's Init)",
-            "config": {"workload": args.workload, "particles": n},
+            "config": workload_config(ini, args.workload),
+            "particles_stepped": n,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": kind,
                              "sample": "%d full loop iterations of %s (%d particles), single thread; the "
                                        "reference loop is serial" % (done, args.workload, n)},
@@ -463,15 +483,10 @@ def run_ours(args, rank, world):
                 "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (particles loaded from mt19937 seed 0, as the reference's Init)",
-                "config": {"workload": args.workload, "particles": int(0.5 * (n_before + n_after)),
-                           "grid": [g.nx, g.ny], "solver": "PCG tol 1e-10 (cold start, as the reference)",
-                           "field_bc": {0: "phi = 0 on all edges (the reference's)", 1: "periodic",
-                                        2: "phi = 0 on the x walls, periodic in y"}[g.poisson_bc],
-                           "particle_bc": {0: "periodic", 1: "absorbing", 2: "reflecting"}[g.bc],
-                           "mcc": "direct MCC, Philox uniforms, 1000-point log table" if coll else "off",
-                           "push": "FP64, contracted (multiply-adds; within a few ulps of the reference's order)",
-                           "l2": "inputs larger than L2 (particles %.0f MB)" % (n_before * 40 / 1e6),
-                           "parallelism": "replicas" if world > 1 else "single GPU"},
+                "config": workload_config(ini, args.workload, world),
+                "particles_stepped": int(0.5 * (n_before + n_after)),
+                "push": "FP64, contracted (multiply-adds; within a few ulps of the reference's order)",
+                "mcc_uniforms": "Philox" if coll else None,
                 "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                         "d2h_bytes_per_step": d2h // e2e_steps, "steps": e2e_steps},
                 "gpu_launches": int(launches), "roofline": roofline, "cpu_baseline": cpu, "clocks": clk,
