@@ -12,6 +12,8 @@
 #include <string>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "epic_host.h"
 #include "epic_internal.cuh"
 
@@ -248,11 +250,20 @@ __global__ void k_soa_to_aos(double* __restrict__ aos, SoA p, const long long* d
   }
 }
 
-// Per-phase CUDA events on the handle's stream (epic_set_profiling).
+// Per-phase CUDA events on the handle's stream (epic_set_profiling), and an
+// NVTX range per phase on the calling thread (always; free without a tool
+// attached), so that profilers can attribute and filter the phases.
+static const char* const kPhaseNames[EPIC_NUM_PHASES] = {"epic deposit", "epic finalize", "epic solve",
+                                                         "epic efield",  "epic push",     "epic mcc",
+                                                         "epic sort"};
 struct PhaseTimer {
   epic_sim* s;
   int phase;
   cudaEvent_t a = nullptr, b = nullptr;
+  struct Nvtx {
+    explicit Nvtx(int p) { nvtxRangePushA(kPhaseNames[p]); }
+    ~Nvtx() { nvtxRangePop(); }
+  } nvtx;
   static cudaEvent_t take(epic_sim* s) {
     if (!s->event_pool.empty()) {
       cudaEvent_t e = s->event_pool.back();
@@ -263,7 +274,7 @@ struct PhaseTimer {
     cudaEventCreate(&e);
     return e;
   }
-  PhaseTimer(epic_sim* s_, int p) : s(s_), phase(p) {
+  PhaseTimer(epic_sim* s_, int p) : s(s_), phase(p), nvtx(p) {
     if (!s->profiling) return;
     cudaStreamCaptureStatus cs;
     if (cudaStreamIsCapturing(s->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
