@@ -590,10 +590,15 @@ class Batch:
         n = self.requests[run].species[sp].numparticle
         if self.requests[run].collisions:
             n = 2 * n + 8192  # ionisation adds particles
-        out = np.empty((max(n, 1), 5), dtype=np.float64)
-        got = ctypes.c_int64()
-        _check(lib().epic_batch_get_particles(self._h, run, sp, _ptr(out), len(out), ctypes.byref(got)))
-        return out[:got.value]
+        while True:
+            out = np.empty((max(n, 1), 5), dtype=np.float64)
+            got = ctypes.c_int64()
+            st = lib().epic_batch_get_particles(self._h, run, sp, _ptr(out), len(out), ctypes.byref(got))
+            if st == 4 and got.value > len(out):  # CAPACITY: emitters added more; the count came back
+                n = got.value
+                continue
+            _check(st)
+            return out[:got.value]
 
     def grid(self, run: int, which: str = "phi") -> np.ndarray:
         c = self.requests[run].cfg

@@ -18,6 +18,7 @@
 #include "../../include/epic2d_batch.h"
 #include "epic_batch.cuh"
 #include "epic_device.cuh"
+#include "epic_emit.cuh"
 #include "epic_host.h"
 #include "epic_mixed.cuh"
 #include "epic_spectral.cuh"
@@ -382,8 +383,61 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_push_compact(const BRun*
   }
 }
 
+// Emitter::inject of every run (src/emitter.cpp:5-36) into one species: CTA
+// row y is emitter em[y]; its points are emit_point's draws (the run alone
+// writes the same), written past the live count in (run, emitter) order, so
+// each run's new particles follow its others in its own emitters' order.
+__global__ void __launch_bounds__(PART_THREADS) k_batch_emit(const BRun* __restrict__ runs,
+                                                             const BEmit* __restrict__ em, MixedSoA p,
+                                                             const long long* __restrict__ d_n, long long cap,
+                                                             const unsigned long long* __restrict__ d_inj,
+                                                             int* flags) {
+  const BEmit b = em[blockIdx.y];
+  const BRun& r = runs[b.run];
+  const long long n0 = *d_n + b.off;
+  const unsigned long long inj = *d_inj;
+  bool bad = false, over = false;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < b.e.num; q += gridDim.x * blockDim.x) {
+    const long long o = n0 + q;
+    if (o >= cap) {
+      over = true;
+      continue;
+    }
+    double x, y, vx, vy, vz;
+    emit_point(b.e, q, b.seed, inj, nullptr, x, y, vx, vy, vz);
+    int i, j;
+    float ox, oy;
+    const bool in_x = cell_offset((x - r.x0) / r.dx, r.nx - 1, i, ox);
+    const bool in_y = cell_offset((y - r.y0) / r.dy, r.ny - 1, j, oy);
+    bad |= !(in_x && in_y);
+    p.cell[o] = (int)(r.node_off + i * r.ny + j);
+    p.ox[o] = ox;
+    p.oy[o] = oy;
+    p.vx[o] = (float)vx;
+    p.vy[o] = (float)vy;
+    p.vz[o] = (float)vz;
+  }
+  if (over) atomicOr(flags, FLAG_CAPACITY);
+  if (bad) atomicOr(flags, FLAG_OUT_OF_GRID);
+}
+
+// Advances a species' count past one step's injections (capped at the
+// capacity, which raises EPIC_ERR_CAPACITY) and keeps the old count as the
+// start of the range to deposit.
+__global__ void k_batch_emit_commit(long long* d_n, long long* d_from, long long total, long long cap, int* flags) {
+  const long long n0 = *d_n;
+  long long n = n0 + total;
+  if (n > cap) {
+    atomicOr(flags, FLAG_CAPACITY);
+    n = cap;
+  }
+  *d_from = n0;
+  *d_n = n;
+}
+
 // CIC deposit of the particles [*d_from, *d_n) of a species (the MCC's
-// ionisation products, appended after the push deposited the rest).
+// ionisation products, appended after the push deposited the rest, or an
+// injection's particles).
 __global__ void __launch_bounds__(PART_THREADS) k_batch_deposit_range(const BRun* __restrict__ runs,
                                                                       const int* __restrict__ node_run, MixedSoA p,
                                                                       const long long* __restrict__ d_from,
@@ -634,6 +688,16 @@ struct epic_batch {
   unsigned int* tile_ctr = nullptr;
   long long tile_status_len = 0;
   std::vector<void*> allocs;
+  // Emitters (src/emitter.cpp:5-36): per species the (run, emitter) rows that
+  // feed it, its points per step and the largest emitter; the injection count
+  // that keys the draws; each species' count before a step's injections
+  BEmit* d_emit[BATCH_MAX_SPECIES] = {};
+  int nemit[BATCH_MAX_SPECIES] = {};
+  int emit_max[BATCH_MAX_SPECIES] = {};
+  long long emit_total[BATCH_MAX_SPECIES] = {};
+  bool any_emit = false;
+  unsigned long long* d_inj = nullptr;
+  long long* d_efrom = nullptr;
   // MCC
   bool any_mcc = false;
   double gas_density = 0;
@@ -766,10 +830,32 @@ struct epic_batch {
     }
   }
 
-  // A step: (sort,) field phase from the accumulators, then each species'
-  // push deposits its new positions (and the electrons' push selects the MCC's
-  // candidates), the MCC, and the deposit of its ionisation products.
+  // A step's injections, first in the step as in the run alone
+  // (src/main.cpp:397-403): each species' emitters in one launch, its count
+  // advanced past them, and their deposit added to the accumulators when these
+  // hold the others' (with absorbing walls the step deposits everything).
+  void inject() {
+    for (int s = 0; s < nsp; s++) {
+      if (!nemit[s]) continue;
+      const int bx = std::max(1, std::min((emit_max[s] + PART_THREADS - 1) / PART_THREADS, grid / nemit[s]));
+      k_batch_emit<<<dim3(bx, nemit[s]), PART_THREADS, 0, stream>>>(d_runs, d_emit[s], arena[s], d_n[s], cap[s],
+                                                                   d_inj, flags);
+      k_batch_emit_commit<<<1, 1, 0, stream>>>(d_n[s], d_efrom + s, emit_total[s], cap[s], flags);
+      if (acc_valid && !has_open)
+        k_batch_deposit_range<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_efrom + s, d_n[s],
+                                                                 acc[s]);
+    }
+    launch_inject_tick(stream, d_inj);
+  }
+
+  // A step: (injections, sort,) field phase from the accumulators, then each
+  // species' push deposits its new positions (and the electrons' push selects
+  // the MCC's candidates), the MCC, and the deposit of its ionisation products.
   void step(int sort) {
+    if (any_emit) {
+      Phase ph(this, 0);
+      inject();
+    }
     if (sort) {
       Phase ph(this, 6);
       sort_all();  // the accumulators do not depend on the order
@@ -1060,8 +1146,17 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
     const epic_config& c = reqs[r].cfg;
     if (reqs[r].num_species != b->nsp) return bfail(EPIC_ERR_INVALID, "run %d: every run needs %d species", r, b->nsp);
     if (c.precision != EPIC_PRECISION_MIXED) return bfail(EPIC_ERR_INVALID, "run %d: batches run the mixed form", r);
-    if (reqs[r].num_conductors || reqs[r].num_emitters)
-      return bfail(EPIC_ERR_INVALID, "run %d: conductors and emitters run in the server and the single-run form", r);
+    if (reqs[r].num_conductors)
+      return bfail(EPIC_ERR_INVALID, "run %d: conductors run in the server and the single-run form", r);
+    if (reqs[r].num_emitters < 0 || reqs[r].num_emitters > EPIC_REQUEST_MAX_EMITTERS)
+      return bfail(EPIC_ERR_INVALID, "run %d: bad emitter count", r);
+    for (int k = 0; k < reqs[r].num_emitters; k++) {
+      const epic_emitter& m = reqs[r].emitters[k];
+      if (m.species_idx1 < 0 || m.species_idx1 >= b->nsp || m.species_idx2 < 0 || m.species_idx2 >= b->nsp)
+        return bfail(EPIC_ERR_INVALID, "run %d: emitter %d: species index out of range", r, k);
+      if (m.numparticle < 0 || m.numparticle > (1 << 28))
+        return bfail(EPIC_ERR_INVALID, "run %d: emitter %d: bad numparticle", r, k);
+    }
     if (c.shape != EPIC_CIC) return bfail(EPIC_ERR_INVALID, "run %d: batches deposit with CIC", r);
     if (c.bc != EPIC_PBC && c.bc != EPIC_REFLECTIVE && c.bc != EPIC_OPEN)
       return bfail(EPIC_ERR_INVALID, "run %d: bad wall rule", r);
@@ -1154,11 +1249,18 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
       b->pn[(size_t)r * b->nsp + s] = reqs[r].species[s].numparticle;
       off += reqs[r].species[s].numparticle;
     }
-    // room for ionisation products: +10 % + 4096 per run (overflow raises
-    // EPIC_ERR_CAPACITY, as in a single run)
+    // room for ionisation products: +10 % + 4096 per run, and for a run's
+    // injections over its request's steps (overflow raises EPIC_ERR_CAPACITY,
+    // as in a single run)
     long long slack = 0;
-    if (b->any_mcc)
-      for (int r = 0; r < nruns; r++) slack += reqs[r].species[s].numparticle / 10 + 4096;
+    for (int r = 0; r < nruns; r++) {
+      if (b->any_mcc) slack += reqs[r].species[s].numparticle / 10 + 4096;
+      for (int k = 0; k < reqs[r].num_emitters; k++) {
+        const epic_emitter& m = reqs[r].emitters[k];
+        if (m.species_idx1 == s || m.species_idx2 == s)
+          slack += (long long)m.numparticle * std::max(reqs[r].steps, 0);
+      }
+    }
     b->cap[s] = std::max<long long>(off + slack, 1);
   }
   epic_status st;
@@ -1217,6 +1319,50 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
       return st;
     BCK(cudaMemsetAsync(ev.slot, 0xff, (size_t)ecap * sizeof(int), b->stream));
   }
+  // Emitter rows: per species, its (run, emitter) rows in run order, each
+  // emitter's slot for that species (Emitter::inject's two species), with the
+  // single run's parameters (do_inject_range).
+  std::vector<BEmit> em[BATCH_MAX_SPECIES];
+  for (int r = 0; r < nruns; r++) {
+    const epic_config& c = reqs[r].cfg;
+    for (int k = 0; k < reqs[r].num_emitters; k++) {
+      const epic_emitter& m = reqs[r].emitters[k];
+      const int sp_of[2] = {m.species_idx1, m.species_idx2};
+      const int slots = m.species_idx1 != m.species_idx2 ? 2 : 1;
+      for (int slot = 0; slot < slots; slot++) {
+        const int s = sp_of[slot];
+        BEmit e;
+        std::memset(&e, 0, sizeof(e));
+        e.e.x0 = m.x0;
+        e.e.y0 = m.y0;
+        e.e.x1 = m.x1;
+        e.e.y1 = m.y1;
+        e.e.vth = sqrt(2 * K_B * m.temp * (QE / K_B) / reqs[r].species[s].mass);  // Init::SampleVel (src/init.cpp:112)
+        e.e.vdx = m.vdx * c.vel_norm;
+        e.e.vdy = m.vdy * c.vel_norm;
+        e.e.vel_norm = c.vel_norm;
+        e.e.num = m.numparticle;
+        e.e.slot = slot;
+        e.e.emitter = k;
+        e.seed = c.seed;
+        e.off = b->emit_total[s];
+        e.run = r;
+        b->emit_total[s] += m.numparticle;
+        b->emit_max[s] = std::max(b->emit_max[s], m.numparticle);
+        em[s].push_back(e);
+      }
+    }
+  }
+  for (int s = 0; s < b->nsp; s++) {
+    if (em[s].empty()) continue;
+    if (em[s].size() > 65535) return bfail(EPIC_ERR_INVALID, "more than 65535 emitters feed species %d", s);
+    b->nemit[s] = (int)em[s].size();
+    b->any_emit = true;
+    if ((st = b->alloc(&b->d_emit[s], em[s].size()))) return st;
+    BCK(cudaMemcpyAsync(b->d_emit[s], em[s].data(), em[s].size() * sizeof(BEmit), cudaMemcpyHostToDevice,
+                        b->stream));
+  }
+  if ((st = b->alloc(&b->d_inj, 1)) || (st = b->alloc(&b->d_efrom, BATCH_MAX_SPECIES))) return st;
   // Host tables to the device.
   std::vector<int> node_run(b->nodes);
   for (int r = 0; r < nruns; r++)
@@ -1378,7 +1524,7 @@ epic_status epic_batch_run(epic_batch* b, int steps, int use_graph) {
 epic_status epic_batch_get_particles(epic_batch* b, int run, int s, double* out, int64_t capacity, int64_t* n) {
   if (!b || run < 0 || run >= b->nruns || s < 0 || s >= b->nsp || !out)
     return bfail(EPIC_ERR_INVALID, "bad argument");
-  if (!b->any_mcc && !b->has_open) {  // counts never change and each run's particles stay where they were loaded
+  if (!b->any_mcc && !b->has_open && !b->any_emit) {  // counts never change: each run's particles stay where loaded
     const long long cnt = b->pn[(size_t)run * b->nsp + s];
     if (n) *n = cnt;
     if (cnt > capacity)

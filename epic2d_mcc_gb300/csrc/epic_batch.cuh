@@ -29,6 +29,17 @@ struct BRun {
   unsigned long long cut53, seed;
 };
 
+// One emitter of one run feeding one species (e.slot 0: its species_idx1, 1:
+// species_idx2): its points go to records off .. off + e.num past the
+// species' live count, Philox keyed by the run's configuration seed (as the
+// run alone).
+struct BEmit {
+  EmitDev e;
+  unsigned long long seed;
+  long long off;
+  int run;
+};
+
 struct McEvents;
 struct CrossSections;
 // Electron-neutral MCC of every run with mcc != 0, one launch sequence for the

@@ -17,6 +17,7 @@
 #include "epic_internal.cuh"
 #include "epic_mixed.cuh"
 #include "epic_device.cuh"
+#include "epic_emit.cuh"
 
 namespace epic {
 
@@ -589,12 +590,8 @@ void launch_conductor_rho(cudaStream_t st, double* rho, const int* nodes, const 
 }
 
 // ------------------------------------------------------------- emitters ---
-// Emitter::inject (src/emitter.cpp:5-36) into one species: point q takes
-// uniforms 0-1 for its position (std::uniform_real_distribution: u (b-a) + a)
-// and 2 + 6*slot .. 7 + 6*slot for its velocity (Init::SampleVel,
-// src/init.cpp:110-114: vth sqrt(2) (u1 + u2 + u3 - 1.5), plus the drift, over
-// vel_norm), from the caller's rows of 14 or from Philox keyed by
-// (q, emitter | 2^31, injection, seed) - distinct from the MCC's keys.
+// Emitter::inject (src/emitter.cpp:5-36) into one species: point q's draws
+// from emit_point (epic_emit.cuh), written at the live count.
 // MIXED: the record goes to the mixed form's layout (cell and FP32 offsets of
 // the FP64 position, FP32 velocities), as the upload converts it.
 template <bool MIXED>
@@ -605,37 +602,13 @@ __global__ void __launch_bounds__(PART_THREADS) k_emit(SoA p, MixedSoA m, Geom g
   const long long n0 = *d_n;
   const unsigned long long inj = *d_inj;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < e.num; q += gridDim.x * blockDim.x) {
-    double u[8];
-    if (uniforms) {
-      const double* r = uniforms + (long long)q * 14;
-      u[0] = r[0];
-      u[1] = r[1];
-#pragma unroll
-      for (int k = 0; k < 6; k++) u[2 + k] = r[2 + 6 * e.slot + k];
-    } else {
-      Philox src{(uint32_t)q, 0x80000000u | (uint32_t)e.emitter, (uint32_t)inj, (uint32_t)seed,
-                 (uint32_t)(seed >> 32), 0, make_uint4(0, 0, 0, 0)};
-      double all[14];
-#pragma unroll
-      for (int k = 0; k < 14; k++) all[k] = src.next();
-      u[0] = all[0];
-      u[1] = all[1];
-#pragma unroll
-      for (int k = 0; k < 6; k++) u[2 + k] = e.slot ? all[8 + k] : all[2 + k];
-    }
     const long long o = n0 + q;
     if (o >= cap) {
       set_flag(flags, FLAG_CAPACITY);
       continue;
     }
-    double vx = e.vth * sqrt(2.0) * (u[2] + u[3] + u[4] - 1.5) + e.vdx;
-    double vy = e.vth * sqrt(2.0) * (u[5] + u[6] + u[7] - 1.5) + e.vdy;
-    double vz = 0.0;
-    vx /= e.vel_norm;
-    vy /= e.vel_norm;
-    vz /= e.vel_norm;
-    const double x = u[0] * (e.x1 - e.x0) + e.x0;
-    const double y = u[1] * (e.y1 - e.y0) + e.y0;
+    double x, y, vx, vy, vz;
+    emit_point(e, q, seed, inj, uniforms, x, y, vx, vy, vz);
     if (MIXED) {
       int i, j;
       float ox, oy;

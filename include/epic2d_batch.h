@@ -28,7 +28,10 @@
  * species 0 and ions as species 1); the colliding runs share one gas density.
  * Lattices with a side of 512 or more unknowns run alone (a single run solves
  * them by FFT passes where their sides allow, so a batch could not equal it);
- * conductors and emitters run in the server and the single-run form.
+ * conductors run in the server and the single-run form.  A run's emitters
+ * (its request's [Emitters]) inject first in every step with the run alone's
+ * draws, and get room for the request's `steps` steps of injections (past it
+ * epic_batch_run returns EPIC_ERR_CAPACITY).
  * Walls may be periodic, reflective or absorbing, mixed within a batch; with
  * an absorbing run in the batch the push erases leaving particles in order
  * (as a single run) and the deposit and the MCC's selection run as their own
@@ -45,7 +48,8 @@ extern "C" {
 typedef struct epic_batch epic_batch;
 
 /* Builds a batch on the current device from nruns requests (configuration,
- * species, collisions and load_seed of each; steps and arrival are ignored). */
+ * species, collisions, load_seed and emitters of each; steps sizes the room
+ * for a run's injections; arrival is ignored). */
 epic_status epic_batch_create(const epic_request* runs, int nruns, int sort_every, epic_batch** out);
 void epic_batch_destroy(epic_batch* b);
 /* Loads every run on the device (its load_seed) and computes its initial field

@@ -105,6 +105,64 @@ def test_batch_with_absorbing_walls_equals_single_runs(gpu_lib, tmp_path, graph)
     b.close()
 
 
+EMIT_A = [dict(x0=1, y0=7, x1=1, y1=9, temp=0.1, numparticle=50, vdx=0.2, vdy=0, species_idx1=0, species_idx2=1),
+          dict(x0=20, y0=3, x1=26, y1=12, temp=0.5, numparticle=40, vdx=0, vdy=0.1, species_idx1=1, species_idx2=1)]
+EMIT_B = [dict(x0=30, y0=20, x1=34, y1=28, temp=1, numparticle=300, vdx=0, vdy=0, species_idx1=0, species_idx2=0)]
+
+
+@pytest.mark.parametrize("walls", ["closed", "with_absorbing"])
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_with_emitters_equals_single_runs(gpu_lib, tmp_path, walls, graph):
+    """Emitters in a batch (src/emitter.cpp:5-36, first in every step as src/main.cpp:397-403): each run's
+    injections are the run alone's Philox draws (keyed by its own seed), appended after its other particles in
+    its emitters' order, so every run — emitting or not — equals the same run alone bit for bit (particles,
+    counts, rho, phi), with the cell sort on; with closed walls the injected particles are deposited into the
+    accumulators the push left, beside an absorbing run the step deposits everything."""
+    A = gpu_lib.api
+    sort_every, steps = 4, 10
+    open_bc = "open" if walls == "with_absorbing" else "pbc"
+    specs = [(dict(nx=48, ny=32, ne=30000, ni=30000, solver="cg", tol="1e-10", maxit=100000, bc=open_bc, te=2),
+              EMIT_A),
+             (dict(nx=40, ny=40, ne=20000, ni=20000, solver="cg", tol="1e-10", maxit=100000, bc="pbc", te=1), []),
+             (dict(nx=64, ny=48, ne=40000, ni=40000, solver="gs", tol="1e-8", bc="reflective", te=3), EMIT_B)]
+    d = str(tmp_path)
+    reqs = []
+    for k, (sp, em) in enumerate(specs):
+        ini = decks.write(decks.deck(emitters=em, **sp), d)
+        reqs.append((ini, A.make_request(ini, steps=steps, seed=90 + k, precision=1, sort_every=sort_every)))
+    assert [r.num_emitters for _, r in reqs] == [2, 0, 1]
+    b = A.Batch([r for _, r in reqs], sort_every=sort_every)
+    b.initial_field()
+    n0 = b.num_particles()
+    b.run(steps, graph=graph)
+    if walls == "closed":  # 50 pairs + 40 ions + 300 electrons a step
+        assert b.num_particles() == n0 + steps * (100 + 40 + 300)
+    for k, (ini, r) in enumerate(reqs):
+        sim = A.Simulation.from_ini(ini, precision=1, sort_every=sort_every)
+        sim.load_particles_device(90 + k)
+        sim.initial_field()
+        sim.run(steps, graph=True)
+        assert np.array_equal(b.grid(k, "phi"), sim.grid("phi")), k
+        assert np.array_equal(b.grid(k, "rho"), sim.grid("rho")), k
+        for s in range(2):
+            assert np.array_equal(b.particles(k, s), sim.particles(s)), (k, s)
+        sim.close()
+    b.close()
+
+
+def test_batch_emitter_room_is_the_request_steps(gpu_lib, tmp_path):
+    """A run's injections get room for its request's steps; running past it raises EPIC_ERR_CAPACITY (as a
+    single run outgrowing its capacity) rather than writing past the arrays."""
+    A = gpu_lib.api
+    d = str(tmp_path)
+    ini = decks.write(decks.deck(nx=32, ny=32, ne=2000, ni=2000, emitters=EMIT_A), d)
+    b = A.Batch([A.make_request(ini, steps=2, seed=3, precision=1, sort_every=0)], sort_every=0)
+    b.initial_field()
+    with pytest.raises(A.EpicError):
+        b.run(400, graph=False)
+    b.close()
+
+
 def _table():
     from epic2d_mcc_gb300 import workloads
 
