@@ -313,16 +313,19 @@ __global__ void __launch_bounds__(T, 768 / T) k_batch_push_dep(const BRun* __res
   }
 }
 
-// The batch's push when some run has absorbing walls: each particle with its
-// run's constants and wall rule; a particle that leaves an open run is erased
-// and the rest keep their order (std::vector::erase, src/species.cpp:100-112),
-// through the single run's ordered tile scan (k_push_mixed_compact) over the
-// whole shared array, so every run's particles stay contiguous and in order.
+// The batch's push when some run has absorbing walls or conductors: each
+// particle with its run's constants and wall rule; a particle that leaves an
+// open run, or ends inside one of its run's conductors (its position taken as
+// x0 + (i + ox) dx in FP64, as k_push_mixed_compact<..., COND>), is erased and
+// the rest keep their order (std::vector::erase, src/species.cpp:80-165),
+// through the single run's ordered tile scan over the whole shared array, so
+// every run's particles stay contiguous and in order.
 __global__ void __launch_bounds__(PART_THREADS) k_batch_push_compact(const BRun* __restrict__ runs,
                                                                      const int* __restrict__ node_run, MixedSoA p,
                                                                      long long* d_n, const float2* __restrict__ ef32,
                                                                      int s, unsigned long long* status,
-                                                                     unsigned int* tile_ctr, int* flags, long long spin) {
+                                                                     unsigned int* tile_ctr, int* flags, long long spin,
+                                                                     BatchConductors cd) {
   constexpr int ITEMS = SCAN_TILE / PART_THREADS;
   __shared__ int sm[40];
   __shared__ unsigned long long s_prefix;
@@ -344,7 +347,8 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_push_compact(const BRun*
       if (q < n) {
         const int cg = p.cell[q];
         ox[k] = p.ox[q]; oy[k] = p.oy[q]; vx[k] = p.vx[q]; vy[k] = p.vy[q]; vz[k] = p.vz[q];
-        const BRun& r = runs[__ldg(&node_run[cg])];
+        const int run = __ldg(&node_run[cg]);
+        const BRun& r = runs[run];
         const Geom g = run_geom(r);
         const float2* ef = ef32 + r.node_off;
         int cl = (int)(cg - r.node_off);
@@ -355,6 +359,14 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_push_compact(const BRun*
         else
           keep[k] = push_mixed_one<EPIC_CIC, EPIC_REFLECTIVE>(g, ef, r.qmK_dt[s], r.cx, r.cy, cl, ox[k], oy[k], vx[k],
                                                               vy[k]);
+        if (keep[k] && (r.nrect | r.ncirc)) {
+          int i, j;
+          split_cell(cl, r.ny, i, j);
+          const double x = __dadd_rn(g.x0, __dmul_rn(__dadd_rn((double)i, (double)ox[k]), g.dx));
+          const double y = __dadd_rn(g.y0, __dmul_rn(__dadd_rn((double)j, (double)oy[k]), g.dy));
+          const CondSet cs{r.nrect, r.ncirc, cd.rect + r.rect_off, cd.circ + r.circ_off, cd.live + run};
+          keep[k] = !in_conductor(cs, x, y);
+        }
         c[k] = (int)(r.node_off + cl);
       }
     }
@@ -381,6 +393,18 @@ __global__ void __launch_bounds__(PART_THREADS) k_batch_push_compact(const BRun*
     }
     __syncthreads();
   }
+}
+
+// Grid::initialize inside gssolver (src/field.cpp:100-103) for every run that
+// solves with SOR and has conductors: their voltages into rho at the listed
+// nodes of the batch's node space (a run's later conductors win, as the host
+// list is built), and the runs' electrodes marked as existing.
+__global__ void k_batch_conductor_rho(double* __restrict__ rho, const int* __restrict__ nodes,
+                                      const double* __restrict__ vals, int n, const int* __restrict__ live_runs,
+                                      int nlive, int* live) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int k = t; k < n; k += stride) rho[nodes[k]] = vals[k];
+  for (int k = t; k < nlive; k += stride) live[live_runs[k]] = 1;
 }
 
 // Emitter::inject of every run (src/emitter.cpp:5-36) into one species: CTA
@@ -698,6 +722,16 @@ struct epic_batch {
   bool any_emit = false;
   unsigned long long* d_inj = nullptr;
   long long* d_efrom = nullptr;
+  // Conductors: every run's rectangles and electrodes, whether its electrodes
+  // exist yet, the rho override of the runs that solve with SOR (nodes of the
+  // batch's node space) and those runs; each run's list for the host loader
+  double4 *d_cond_rect = nullptr, *d_cond_circ = nullptr;
+  int* d_cond_live = nullptr;
+  int* d_cond_nodes = nullptr;
+  double* d_cond_vals = nullptr;
+  int* d_cond_runs = nullptr;
+  int cond_nnodes = 0, cond_nruns = 0;
+  std::vector<std::vector<epic_conductor>> conductors;
   // MCC
   bool any_mcc = false;
   double gas_density = 0;
@@ -764,8 +798,15 @@ struct epic_batch {
     }
   }
 
+  BatchConductors cond_view() const { return BatchConductors{d_cond_rect, d_cond_circ, d_cond_live}; }
+
   void solve() {
     const BatchSpec b = spec();
+    if (cond_nnodes || cond_nruns) {  // the SOR runs' Grid::initialize: the same right-hand side for the spectral solve
+      const int m = std::max(cond_nnodes, cond_nruns);
+      k_batch_conductor_rho<<<std::max(1, std::min(grid, (m + 255) / 256)), 256, 0, stream>>>(
+          rho, d_cond_nodes, d_cond_vals, cond_nnodes, d_cond_runs, cond_nruns, d_cond_live);
+    }
     k_batch_spec_init<<<grid, 256, 0, stream>>>(b, d_node_run, nodes, nruns);
     for (int st = 0; st < BATCH_STAGES; st++) {
       k_batch_spec_residual<<<nchunk, 256, 0, stream>>>(b, chunk_sched);
@@ -872,7 +913,8 @@ struct epic_batch {
           cudaMemsetAsync(tile_ctr, 0, sizeof(unsigned int), stream);
           cudaMemsetAsync(tile_status, 0, tile_status_len * sizeof(unsigned long long), stream);
           k_batch_push_compact<<<grid, PART_THREADS, 0, stream>>>(d_runs, d_node_run, arena[s], d_n[s], ef32, s,
-                                                                  tile_status, tile_ctr, flags, spin_limit());
+                                                                  tile_status, tile_ctr, flags, spin_limit(),
+                                                                  cond_view());
         }
       }
       if (any_mcc) {
@@ -1146,8 +1188,17 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
     const epic_config& c = reqs[r].cfg;
     if (reqs[r].num_species != b->nsp) return bfail(EPIC_ERR_INVALID, "run %d: every run needs %d species", r, b->nsp);
     if (c.precision != EPIC_PRECISION_MIXED) return bfail(EPIC_ERR_INVALID, "run %d: batches run the mixed form", r);
-    if (reqs[r].num_conductors)
-      return bfail(EPIC_ERR_INVALID, "run %d: conductors run in the server and the single-run form", r);
+    if (reqs[r].num_conductors < 0 || reqs[r].num_conductors > EPIC_REQUEST_MAX_CONDUCTORS)
+      return bfail(EPIC_ERR_INVALID, "run %d: bad conductor count", r);
+    for (int k = 0; k < reqs[r].num_conductors; k++) {  // epic_add_conductor's checks
+      const epic_conductor& g = reqs[r].conductors[k];
+      if (g.type != EPIC_CONDUCTOR_RECT && g.type != EPIC_CONDUCTOR_CIRCULAR)
+        return bfail(EPIC_ERR_INVALID, "run %d: unknown conductor type %d", r, g.type);
+      if (g.type == EPIC_CONDUCTOR_CIRCULAR && (g.electrode_number < 1 || g.electrode_number > 4096))
+        return bfail(EPIC_ERR_INVALID, "run %d: electrode_number must be in [1, 4096]", r);
+    }
+    // conductors erase particles: the batch's push is then the compacting one
+    if (reqs[r].num_conductors) b->has_open = true;
     if (reqs[r].num_emitters < 0 || reqs[r].num_emitters > EPIC_REQUEST_MAX_EMITTERS)
       return bfail(EPIC_ERR_INVALID, "run %d: bad emitter count", r);
     for (int k = 0; k < reqs[r].num_emitters; k++) {
@@ -1363,6 +1414,49 @@ epic_status build(epic_batch* b, const epic_request* reqs, int nruns) {
                         b->stream));
   }
   if ((st = b->alloc(&b->d_inj, 1)) || (st = b->alloc(&b->d_efrom, BATCH_MAX_SPECIES))) return st;
+  // Conductor tables (conductor_geometry, as epic_add_conductor builds them per run).
+  std::vector<double> all_rect, all_circ, all_vals;
+  std::vector<int> all_nodes, live_runs;
+  b->conductors.assign(nruns, {});
+  for (int r = 0; r < nruns; r++) {
+    const epic_request& q = reqs[r];
+    if (!q.num_conductors) continue;
+    std::vector<epic_conductor> cv(q.conductors, q.conductors + q.num_conductors);
+    std::vector<double> rects, circles, vals;
+    std::vector<int> cnodes;
+    conductor_geometry(q.cfg, cv, rects, circles, cnodes, vals);
+    BRun& br = b->runs[r];
+    br.nrect = (int)(rects.size() / 4);
+    br.ncirc = (int)(circles.size() / 4);
+    br.rect_off = (int)(all_rect.size() / 4);
+    br.circ_off = (int)(all_circ.size() / 4);
+    all_rect.insert(all_rect.end(), rects.begin(), rects.end());
+    all_circ.insert(all_circ.end(), circles.begin(), circles.end());
+    if (q.cfg.solver == EPIC_SOLVER_GS) {  // gssolver calls Grid::initialize (src/field.cpp:100-103), pcgsolver not
+      for (size_t k = 0; k < cnodes.size(); k++) {
+        all_nodes.push_back((int)(br.node_off + cnodes[k]));
+        all_vals.push_back(vals[k]);
+      }
+      live_runs.push_back(r);
+    }
+    b->conductors[r] = std::move(cv);
+  }
+  b->cond_nnodes = (int)all_nodes.size();
+  b->cond_nruns = (int)live_runs.size();
+  if ((st = b->alloc(&b->d_cond_rect, all_rect.size() / 4)) || (st = b->alloc(&b->d_cond_circ, all_circ.size() / 4)) ||
+      (st = b->alloc(&b->d_cond_live, nruns)) || (st = b->alloc(&b->d_cond_nodes, all_nodes.size())) ||
+      (st = b->alloc(&b->d_cond_vals, all_vals.size())) || (st = b->alloc(&b->d_cond_runs, live_runs.size())))
+    return st;
+  auto up = [&](void* dst, const void* src, size_t bytes) -> epic_status {
+    if (bytes) BCK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, b->stream));
+    return EPIC_OK;
+  };
+  if ((st = up(b->d_cond_rect, all_rect.data(), all_rect.size() * sizeof(double))) ||
+      (st = up(b->d_cond_circ, all_circ.data(), all_circ.size() * sizeof(double))) ||
+      (st = up(b->d_cond_nodes, all_nodes.data(), all_nodes.size() * sizeof(int))) ||
+      (st = up(b->d_cond_vals, all_vals.data(), all_vals.size() * sizeof(double))) ||
+      (st = up(b->d_cond_runs, live_runs.data(), live_runs.size() * sizeof(int))))
+    return st;
   // Host tables to the device.
   std::vector<int> node_run(b->nodes);
   for (int r = 0; r < nruns; r++)
@@ -1451,6 +1545,35 @@ epic_status epic_batch_initial_field(epic_batch* b) {
   for (int r = 0; r < b->nruns; r++) {
     const epic_request& q = b->reqs[r];
     const Geom g{q.cfg.nx, q.cfg.ny, q.cfg.x0, q.cfg.y0, q.cfg.dx, q.cfg.dy, 0, 0};
+    if (q.num_conductors) {
+      // the host loader, as epic_load_particles with load_seed: Init's mt19937
+      // stream continued across the species, positions inside a conductor
+      // drawn again (the device loader does not place particles around them)
+      RefStream* rs = ref_stream_create((uint32_t)q.load_seed);
+      epic_status st = EPIC_OK;
+      for (int s = 0; s < b->nsp && !st; s++) {
+        std::vector<double> parts;
+        std::string err;
+        const long long n = b->pn[(size_t)r * b->nsp + s];
+        if (int e = load_species(q.cfg, q.species[s], parts, rs, err, b->conductors[r])) {
+          st = bfail((epic_status)e, "run %d: %s", r, err.c_str());
+        } else if ((long long)(parts.size() / 5) != n) {
+          st = bfail(EPIC_ERR_INVALID, "run %d: the loader gave %lld particles", r, (long long)(parts.size() / 5));
+        } else if (n) {
+          cudaError_t ce = cudaMemcpyAsync(b->staging, parts.data(), (size_t)n * 5 * sizeof(double),
+                                           cudaMemcpyHostToDevice, b->stream);
+          if (ce == cudaSuccess) {
+            k_batch_from_aos<<<b->grid, PART_THREADS, 0, b->stream>>>(b->runs[r], b->staging, b->arena[s],
+                                                                       b->poff[(size_t)r * b->nsp + s], n, b->flags);
+            ce = cudaStreamSynchronize(b->stream);  // parts goes out of scope
+          }
+          if (ce != cudaSuccess) st = bfail(EPIC_ERR_CUDA, "run %d: load: %s", r, cudaGetErrorString(ce));
+        }
+      }
+      ref_stream_destroy(rs);
+      if (st) return st;
+      continue;
+    }
     for (int s = 0; s < b->nsp; s++) {
       int kind = 0, narg = 0;
       std::string err;

@@ -27,6 +27,18 @@ struct BRun {
   int mcc;
   double vn, dt_phys, ion_mass, ion_temp, F1, F2, p_cut;
   unsigned long long cut53, seed;
+  // conductors (src/grid.cpp, src/electrode.cpp): rectangles and electrodes
+  // at rect_off / circ_off of the batch's conductor tables (BatchConductors)
+  int nrect, ncirc, rect_off, circ_off;
+};
+
+// The conductors of every run: rectangles {min_x, max_x, min_y, max_y},
+// electrodes {x, y, r*r, 0}, and per run whether its electrodes exist yet (a
+// CircularGrid has none until the first SOR solve's Grid::initialize).
+struct BatchConductors {
+  const double4* rect;
+  const double4* circ;
+  const int* live;
 };
 
 // One emitter of one run feeding one species (e.slot 0: its species_idx1, 1:

@@ -33,14 +33,17 @@ __device__ __forceinline__ void emit_point(const EmitDev& e, int q, unsigned lon
 #pragma unroll
     for (int k = 0; k < 6; k++) u[2 + k] = e.slot ? all[8 + k] : all[2 + k];
   }
-  vx = e.vth * sqrt(2.0) * (u[2] + u[3] + u[4] - 1.5) + e.vdx;
-  vy = e.vth * sqrt(2.0) * (u[5] + u[6] + u[7] - 1.5) + e.vdy;
+  // uncontracted in every file (the files including this one build with and
+  // without FMA contraction): ((vth sqrt2) ((u1 + u2) + u3 - 1.5)) + drift
+  const double vs = __dmul_rn(e.vth, sqrt(2.0));
+  vx = __dadd_rn(__dmul_rn(vs, __dsub_rn(__dadd_rn(__dadd_rn(u[2], u[3]), u[4]), 1.5)), e.vdx);
+  vy = __dadd_rn(__dmul_rn(vs, __dsub_rn(__dadd_rn(__dadd_rn(u[5], u[6]), u[7]), 1.5)), e.vdy);
   vz = 0.0;
   vx /= e.vel_norm;
   vy /= e.vel_norm;
   vz /= e.vel_norm;
-  x = u[0] * (e.x1 - e.x0) + e.x0;
-  y = u[1] * (e.y1 - e.y0) + e.y0;
+  x = __dadd_rn(__dmul_rn(u[0], __dsub_rn(e.x1, e.x0)), e.x0);
+  y = __dadd_rn(__dmul_rn(u[1], __dsub_rn(e.y1, e.y0)), e.y0);
 }
 
 }  // namespace epic

@@ -27,13 +27,15 @@
  * species (species k plays the same role in every run; MCC needs electrons as
  * species 0 and ions as species 1); the colliding runs share one gas density.
  * Lattices with a side of 512 or more unknowns run alone (a single run solves
- * them by FFT passes where their sides allow, so a batch could not equal it);
- * conductors run in the server and the single-run form.  A run's emitters
- * (its request's [Emitters]) inject first in every step with the run alone's
- * draws, and get room for the request's `steps` steps of injections (past it
- * epic_batch_run returns EPIC_ERR_CAPACITY).
+ * them by FFT passes where their sides allow, so a batch could not equal it).
+ * A run's emitters (its request's [Emitters]) inject first in every step with
+ * the run alone's draws, and get room for the request's `steps` steps of
+ * injections (past it epic_batch_run returns EPIC_ERR_CAPACITY).  A run with
+ * conductors (its request's [Grids]) is loaded by the host loader, as
+ * epic_load_particles with load_seed; its SOR solves get the rho override and
+ * the push erases the particles that end inside them.
  * Walls may be periodic, reflective or absorbing, mixed within a batch; with
- * an absorbing run in the batch the push erases leaving particles in order
+ * an absorbing run or conductors in the batch the push erases particles in order
  * (as a single run) and the deposit and the MCC's selection run as their own
  * passes. */
 #ifndef EPIC2D_BATCH_H
@@ -48,8 +50,8 @@ extern "C" {
 typedef struct epic_batch epic_batch;
 
 /* Builds a batch on the current device from nruns requests (configuration,
- * species, collisions, load_seed and emitters of each; steps sizes the room
- * for a run's injections; arrival is ignored). */
+ * species, collisions, load_seed, conductors and emitters of each; steps sizes
+ * the room for a run's injections; arrival is ignored). */
 epic_status epic_batch_create(const epic_request* runs, int nruns, int sort_every, epic_batch** out);
 void epic_batch_destroy(epic_batch* b);
 /* Loads every run on the device (its load_seed) and computes its initial field

@@ -150,6 +150,53 @@ def test_batch_with_emitters_equals_single_runs(gpu_lib, tmp_path, walls, graph)
     b.close()
 
 
+GRIDS = [dict(type="reactconduct", min_x=10, max_x=12, min_y=4, max_y=16, grid_voltage=10),
+         dict(type="circular", x_center=22, y_center=12, electrode_number=6, grid_radius=5, electrod_radius=1.5,
+              electrode_voltage=-5)]
+
+
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_with_conductors_equals_single_runs(gpu_lib, tmp_path, graph):
+    """Conductors in a batch (src/grid.cpp, src/electrode.cpp): a run with conductors is loaded by the host
+    loader (positions inside a conductor drawn again, as the run alone with the same seed); its SOR solves get
+    Grid::initialize's rho override (src/field.cpp:100-103), which also brings its electrodes into existence, its
+    PCG solves do not; and the push erases, in order, the particles that end inside one. Every run (SOR and PCG
+    with a rectangle and a ring, periodic, reflective and absorbing walls, one also emitting, and a plain run
+    beside them) equals the same run alone bit for bit (particles, counts, rho, phi), with the cell sort on."""
+    A = gpu_lib.api
+    sort_every, steps = 4, 8
+    specs = [(dict(nx=32, ny=24, ne=20000, ni=20000, solver="gs", tol="1e-6", bc="pbc", te=2, grids=GRIDS), []),
+             (dict(nx=40, ny=40, ne=20000, ni=20000, solver="cg", tol="1e-10", maxit=100000, bc="pbc", te=1), []),
+             (dict(nx=32, ny=24, ne=20000, ni=20000, solver="cg", tol="1e-10", maxit=100000, bc="reflective", te=2,
+                   grids=GRIDS), []),
+             (dict(nx=32, ny=24, ne=15000, ni=15000, solver="gs", tol="1e-6", bc="open", te=1, grids=GRIDS[:1]),
+              EMIT_A)]
+    d = str(tmp_path)
+    reqs = []
+    for k, (sp, em) in enumerate(specs):
+        ini = decks.write(decks.deck(emitters=em, **sp), d)
+        reqs.append((ini, A.make_request(ini, steps=steps, seed=110 + k, precision=1, sort_every=sort_every)))
+    assert [r.num_conductors for _, r in reqs] == [2, 0, 2, 1]
+    b = A.Batch([r for _, r in reqs], sort_every=sort_every)
+    b.initial_field()
+    b.run(steps, graph=graph)
+    assert len(b.particles(0, 0)) < 20000  # electrons ended inside run 0's conductors
+    for k, (ini, r) in enumerate(reqs):
+        sim = A.Simulation.from_ini(ini, precision=1, sort_every=sort_every)
+        if r.num_conductors:
+            sim.load_particles(110 + k)
+        else:
+            sim.load_particles_device(110 + k)
+        sim.initial_field()
+        sim.run(steps, graph=True)
+        assert np.array_equal(b.grid(k, "phi"), sim.grid("phi")), k
+        assert np.array_equal(b.grid(k, "rho"), sim.grid("rho")), k
+        for s in range(2):
+            assert np.array_equal(b.particles(k, s), sim.particles(s)), (k, s)
+        sim.close()
+    b.close()
+
+
 def test_batch_emitter_room_is_the_request_steps(gpu_lib, tmp_path):
     """A run's injections get room for its request's steps; running past it raises EPIC_ERR_CAPACITY (as a
     single run outgrowing its capacity) rather than writing past the arrays."""
