@@ -1,9 +1,10 @@
 """Batched runs (include/epic2d_batch.h): every run of a batch gives the same
 particles and potential, bit for bit, as the same run alone in the mixed form
 (same configuration, sort period and device-loader seed) — on square and
-non-square grids, periodic and reflective walls, pcgsolver and gssolver, with
-the step replayed from a graph or launched directly, whatever launch shapes
-the autotuner chose for the GEMM tiles and the particle passes."""
+non-square grids, periodic, reflective and absorbing walls, pcgsolver and
+gssolver, conductors and emitters, with the step replayed from a graph or
+launched directly, whatever launch shapes the autotuner chose for the GEMM
+tiles and the particle passes."""
 import numpy as np
 import pytest
 
