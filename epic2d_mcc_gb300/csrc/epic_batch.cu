@@ -1493,6 +1493,8 @@ epic_status take_flags(epic_batch* b) {
   BCK(cudaStreamSynchronize(b->stream));
   if (!f) return EPIC_OK;
   cudaMemsetAsync(b->flags, 0, sizeof(int), b->stream);
+  if (f & FLAG_TIMEOUT) return bfail(EPIC_ERR_TIMEOUT, "a device-side wait gave up (flags 0x%x)", f);
+  if (f & FLAG_CAPACITY) return bfail(EPIC_ERR_CAPACITY, "a species outgrew the batch's capacity (flags 0x%x)", f);
   if (f & FLAG_OUT_OF_GRID) return bfail(EPIC_ERR_DOMAIN, "a particle was loaded outside its run's grid");
   return bfail(EPIC_ERR_CUDA, "device flags 0x%x", f);
 }

@@ -74,6 +74,8 @@ epic_status take_flags(epic_sim* s) {
   CK(cudaMemsetAsync(s->d_flags, 0, sizeof(int), s->stream));
   if (f & FLAG_TIMEOUT) return fail(EPIC_ERR_TIMEOUT, "a device-side wait gave up (flags 0x%x)", f);
   if (f & FLAG_CAPACITY) return fail(EPIC_ERR_CAPACITY, "a species outgrew its particle capacity (flags 0x%x)", f);
+  if (f & FLAG_LOAD_IN_CONDUCTOR)
+    return fail(EPIC_ERR_INVALID, "the load type places a particle inside a conductor (the reference loops forever)");
   if (f & FLAG_OUT_OF_GRID)
     return fail(EPIC_ERR_DOMAIN, "a particle left the grid (the reference raises std::out_of_range here)");
   return fail(EPIC_ERR_CUDA, "device flags 0x%x", f);
@@ -1652,8 +1654,6 @@ epic_status epic_poll(epic_sim* s, int* done) {
 epic_status epic_load_particles_device(epic_sim* s, uint64_t seed) {
   if (!s) return fail(EPIC_ERR_INVALID, "null handle");
   invalidate_acc(s);
-  if (!s->conductors.empty())
-    return fail(EPIC_ERR_INVALID, "the device loader does not place particles around conductors (epic_load_particles does)");
   for (int i = 0; i < (int)s->sp.size(); i++) {
     epic_species_state& sp = s->sp[i];
     const long long n = sp.desc.numparticle;
@@ -1664,7 +1664,8 @@ epic_status epic_load_particles_device(epic_sim* s, uint64_t seed) {
     if (parse_load_type(sp.desc.load, &kind, &narg, err)) return fail(EPIC_ERR_INVALID, "%s", err.c_str());
     epic_status st = ensure_staging(s, std::max<size_t>(1, (size_t)n * 5 * sizeof(double)));
     if (st) return st;
-    launch_load(s->stream, s->g, sp.desc, s->cfg, i, kind, narg, (double*)s->staging, seed, s->part_grid);
+    launch_load(s->stream, s->g, sp.desc, s->cfg, i, kind, narg, (double*)s->staging, seed, s->part_grid,
+                (const double4*)s->d_cond_rect, s->cond_nrect, s->d_flags);
     if (n) {
       if (s->mixed)
         launch_aos_to_mixed(s->stream, s->g, (const double*)s->staging, sp.mx, n, s->d_flags, s->part_grid);

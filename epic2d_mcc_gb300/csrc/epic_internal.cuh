@@ -42,6 +42,7 @@ enum : int {
   FLAG_CAPACITY = 2,
   FLAG_TIMEOUT = 4,
   FLAG_BAD_TABLE = 8,
+  FLAG_LOAD_IN_CONDUCTOR = 16,  // a deterministic load placed a particle inside a conductor
 };
 
 // Bounded spin: polls of a device-side wait before it reports FLAG_TIMEOUT
@@ -267,8 +268,12 @@ constexpr int MIXED_OFFSET_BITS = 20;  // deposit weights: offsets quantised to 
 
 // ---- device loading and run digest (epic_load.cu) ----
 // kind: 0 random, 1 uniform, 2 sin(n), 3 cos(n) (the reference's load types).
+// rect: nrect conductor rectangles {min_x, max_x, min_y, max_y} that Init
+// keeps particles out of (a random position is drawn again; a deterministic
+// one inside raises FLAG_LOAD_IN_CONDUCTOR in *flags).
 void launch_load(cudaStream_t st, const Geom& g, const epic_species_desc& d, const epic_config& c, int species,
-                 int kind, int narg, double* aos, unsigned long long seed, int grid);
+                 int kind, int narg, double* aos, unsigned long long seed, int grid, const double4* rect = nullptr,
+                 int nrect = 0, int* flags = nullptr);
 void launch_set_count(cudaStream_t st, long long* d_n, long long n);
 void launch_digest(cudaStream_t st, const void* a, int elem_bytes, const long long* d_n, long long n,
                    unsigned long long tag, unsigned long long* out, int grid);

@@ -10,7 +10,12 @@
 // so a run can be loaded without a host-side pass over its particles (the
 // serving loop admits runs of ~10^7 particles while others are in flight).
 // The host loader (epic_load_particles) remains the one that reproduces the
-// reference's particles.
+// reference's particles.  Conductor rectangles keep particles out as Init's
+// loop does (src/init.cpp:71-86, Grid::IsGrid; a CircularGrid has no
+// electrodes yet): a random position inside one is drawn again from the
+// particle's own stream (up to LOAD_REDRAWS times, then an error), and a
+// deterministic position inside one is an error (the reference would loop
+// forever).
 //
 // The digest is an order-independent 64-bit hash of a run's state: the sum
 // over elements of a mix of (bits, position, array) — integer additions, so
@@ -32,7 +37,20 @@ struct LoadSpec {
   double v_th, vsx, vsy, vel_norm;
   double pi;
   int load_3v;
+  int nrect;
+  const double4* rect;
+  int* flags;
 };
+
+constexpr int LOAD_REDRAWS = 1024;
+
+__device__ __forceinline__ bool load_in_rect(const LoadSpec& L, double x, double y) {
+  for (int k = 0; k < L.nrect; k++) {
+    const double4 r = L.rect[k];
+    if (x >= r.x && x <= r.y && y >= r.z && y <= r.w) return true;
+  }
+  return false;
+}
 
 __global__ void k_load(LoadSpec L, double* __restrict__ aos, unsigned long long seed) {
   for (long long p = (long long)blockIdx.x * blockDim.x + threadIdx.x; p < L.n; p += (long long)gridDim.x * blockDim.x) {
@@ -44,9 +62,18 @@ __global__ void k_load(LoadSpec L, double* __restrict__ aos, unsigned long long 
     r.key1 = (uint32_t)(seed >> 32);
     r.k = 0;
     double x, y;
+    bool bad = false;
     if (L.kind == 0) {
       x = L.x0 + L.Lx * r.next();
       y = L.y0 + L.Ly * r.next();
+      for (int t = 0; L.nrect && load_in_rect(L, x, y); t++) {
+        if (t == LOAD_REDRAWS) {
+          bad = true;
+          break;
+        }
+        x = L.x0 + L.Lx * r.next();
+        y = L.y0 + L.Ly * r.next();
+      }
     } else if (L.kind == 1) {
       const int nxp = (int)sqrt((double)L.n);
       const int px = (int)(p % nxp), py = (int)(p / nxp);
@@ -64,6 +91,8 @@ __global__ void k_load(LoadSpec L, double* __restrict__ aos, unsigned long long 
         y += cos(ky * y);
       }
     }
+    if (L.kind != 0 && L.nrect) bad = load_in_rect(L, x, y);
+    if (bad) atomicOr(L.flags, FLAG_LOAD_IN_CONDUCTOR);
     const double s2 = sqrt(2.0);
     double u1 = r.next(), u2 = r.next(), u3 = r.next();
     double vx = L.v_th * s2 * (u1 + u2 + u3 - 1.5) + L.vsx * L.vel_norm;
@@ -86,7 +115,8 @@ __global__ void k_load(LoadSpec L, double* __restrict__ aos, unsigned long long 
 __global__ void k_set_count(long long* d_n, long long n) { *d_n = n; }
 
 void launch_load(cudaStream_t st, const Geom& g, const epic_species_desc& d, const epic_config& c, int species,
-                 int kind, int narg, double* aos, unsigned long long seed, int grid) {
+                 int kind, int narg, double* aos, unsigned long long seed, int grid, const double4* rect, int nrect,
+                 int* flags) {
   LoadSpec L;
   L.kind = kind;
   L.narg = narg;
@@ -102,6 +132,9 @@ void launch_load(cudaStream_t st, const Geom& g, const epic_species_desc& d, con
   L.vel_norm = c.vel_norm;
   L.pi = PI_REF;
   L.load_3v = c.load_3v;
+  L.nrect = rect && flags ? nrect : 0;
+  L.rect = rect;
+  L.flags = flags;
   if (L.n > 0) k_load<<<grid, PART_THREADS, 0, st>>>(L, aos, seed);
   (void)g;
 }

@@ -256,7 +256,11 @@ epic_status epic_poll(epic_sim* sim, int* done);
  * placements and velocity formula of Init::Init / Init::SampleVel
  * (src/init.cpp:3-114) with uniforms from a Philox stream keyed by
  * (seed, species, particle) instead of the reference's mt19937 (use
- * epic_load_particles for the reference's own particles). */
+ * epic_load_particles for the reference's own particles).  Conductor
+ * rectangles keep particles out as Init's loop does (src/init.cpp:71-86): a
+ * random position inside one is drawn again from the particle's stream; a
+ * deterministic load type that puts one inside makes this call or the next
+ * synchronising one return EPIC_ERR_INVALID. */
 epic_status epic_load_particles_device(epic_sim* sim, uint64_t seed);
 /* Order-independent 64-bit hashes of the run's state: out[0] of phi, out[1]
  * of every species' particle count and particle arrays (in the handle's

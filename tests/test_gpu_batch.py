@@ -206,8 +206,9 @@ def test_batch_emitter_room_is_the_request_steps(gpu_lib, tmp_path):
     ini = decks.write(decks.deck(nx=32, ny=32, ne=2000, ni=2000, emitters=EMIT_A), d)
     b = A.Batch([A.make_request(ini, steps=2, seed=3, precision=1, sort_every=0)], sort_every=0)
     b.initial_field()
-    with pytest.raises(A.EpicError):
+    with pytest.raises(A.EpicError) as ei:
         b.run(400, graph=False)
+    assert ei.value.status == 4  # EPIC_ERR_CAPACITY
     b.close()
 
 

@@ -63,18 +63,37 @@ def test_conductors_track_oracle(gpu_lib, tmp_path, bc, solver):
 
 
 def test_conductors_rules(gpu_lib, tmp_path):
-    # the device loader does not place particles around conductors (the host loader does)
-    ini = decks.write(decks.deck(nx=32, ny=24, ne=1000, ni=1000, grids=GRIDS), str(tmp_path))
-    sim0 = gpu_lib.Simulation.from_ini(ini, precision=1)
-    with pytest.raises(gpu_lib.EpicError):
-        sim0.load_particles_device(1)
-    sim0.close()
-    # a deterministic load type that puts a particle inside a conductor (the reference loops forever)
+    # the device loader keeps particles out of the conductor rectangles as Init does (src/init.cpp:71-86: a
+    # random position inside one is drawn again; the rings have no electrodes before the first SOR solve)
+    ini = decks.write(decks.deck(nx=32, ny=24, ne=4000, ni=4000, grids=GRIDS), str(tmp_path))
+    r = GRIDS[0]
+    sims = []
+    for seed in (1, 1, 2):
+        sim0 = gpu_lib.Simulation.from_ini(ini)
+        sim0.load_particles_device(seed)
+        sim0.initial_field()
+        p = [sim0.particles(s) for s in range(2)]
+        for q in p:
+            assert len(q) == 4000
+            inside = (q[:, 0] >= r["min_x"]) & (q[:, 0] <= r["max_x"]) & (q[:, 1] >= r["min_y"]) & (q[:, 1] <= r["max_y"])
+            assert not inside.any()
+        sims.append(p)
+        sim0.close()
+    assert all(np.array_equal(a, b) for a, b in zip(sims[0], sims[1]))  # same seed, same particles
+    assert not np.array_equal(sims[0][0], sims[2][0])
+    # a deterministic load type that puts a particle inside a conductor (the reference loops forever): both
+    # loaders refuse it
     text = decks.deck(nx=32, ny=24, ne=1024, ni=1024, grids=GRIDS).replace(",random", ",uniform")
     ini2 = decks.write(text, str(tmp_path))
     sim = gpu_lib.Simulation.from_ini(ini2)
     with pytest.raises(gpu_lib.EpicError):
         sim.load_particles(0)
+    sim.close()
+    sim = gpu_lib.Simulation.from_ini(ini2)
+    with pytest.raises(gpu_lib.EpicError) as ei:  # from the load itself or the next synchronising call
+        sim.load_particles_device(0)
+        sim.initial_field()
+    assert ei.value.status == 1  # EPIC_ERR_INVALID
     sim.close()
 
 
